@@ -1,0 +1,801 @@
+// bh.cu -- Barnes-Hut step: cell keys, onesweep radix sort, quadtree build from sorted
+// keys, mass/centre-of-mass reduction and the warp-coherent traversal with the
+// integrator fused into its epilogue.
+//
+// Replaces the seven shaders of src/Simulation/BarnesHut/Shaders/ and the 35 dispatches
+// per step of src/Simulation/BarnesHut/BarnesHutSimulation.cpp:885-918.  The reference
+// clears and fills a fixed 1024x1024 grid and walks 11 levels of it every step; here
+// every stage is sized by N:
+//
+//   k_bbox        (bounding-box mode) min/max of positions, box parameters in FP64
+//   k_keygen      cell key per particle (InitShader.comp:80-98 arithmetic), removal of
+//                 particles outside the fixed box (InitShader.comp:110-117), digit
+//                 histograms for every radix pass
+//   k_sort_pass   onesweep LSD pass: 8-bit digits, decoupled look-back, stable
+//   k_meta_scan   per sorted slot s the internal nodes that start at s: levels
+//                 dmin(s)..dmax(s) from the common prefix with the neighbouring keys,
+//                 exclusive scan E(s) with decoupled look-back
+//   k_records     preorder records: node (d, s) at s + E(s) + d - dmin(s), particle leaf
+//                 at s + E(s) + e(s); skip = end + E(end) - index (the reference's count.y),
+//                 radius = radius0 / 4^d (TreeMoveShader.comp:70-71)
+//   k_sums_level  bottom-up mass and mass-moment sums, finest level first, in the order
+//                 of TreeInitShader.comp:78-80; centre of mass as TreeMoveShader.comp:66-67
+//   k_force       ForceShader.comp:78-152 semantics: one warp walks the preorder records
+//                 for 32 consecutive sorted slots; a record is accepted only if every
+//                 lane satisfies radius <= d2 * theta^2; 32-record window staged in shared
+//                 memory; the integrator and the scatter to original order are fused.
+#include <cstdio>
+#include <cstring>
+
+#include "internal.cuh"
+
+namespace gsim {
+namespace {
+
+// ------------------------------------------------------------------------------------
+// keys
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t spread_bits(uint32_t v) {  // InitShader.comp:88-96
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+// InitShader.comp:80-85: rel = ((p / S) + 1) * 0.5 * 1024, inside iff 0 <= rel < 1024
+__device__ __forceinline__ bool fixed_key(float px, float py, uint32_t& key) {
+    float rx = __fmul_rn(__fmul_rn(__fadd_rn(__fdiv_rn(px, kSimSize), 1.0f), 0.5f), (float)kGrid);
+    float ry = __fmul_rn(__fmul_rn(__fadd_rn(__fdiv_rn(py, kSimSize), 1.0f), 0.5f), (float)kGrid);
+    if (rx >= 0.0f && rx < (float)kGrid && ry >= 0.0f && ry < (float)kGrid) {
+        key = spread_bits((uint32_t)rx) | (spread_bits((uint32_t)ry) << 1);
+        return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t bbox_cell(float p, float c, float scale) {
+    float t = __fadd_rn(__fmul_rn(__fsub_rn(p, c), scale), (float)(1u << (kBBoxBits - 1)));
+    if (!(t >= 0.0f)) return 0u;
+    if (t >= (float)((1u << kBBoxBits) - 1)) return (1u << kBBoxBits) - 1;
+    return (uint32_t)t;
+}
+
+__device__ __forceinline__ int common_bits(uint32_t a, uint32_t b, int key_bits) {
+    return a == b ? key_bits : __clz(a ^ b) - (32 - key_bits);
+}
+// first level at which slot s starts a cell (0 for s == 0); D+1 if none
+__device__ __forceinline__ int slot_dmin(const uint32_t* k, uint32_t s, int D) {
+    return s == 0 ? 0 : common_bits(k[s - 1], k[s], 2 * D) / 2 + 1;
+}
+// finest level at which the cell starting at s holds >= 2 particles; -1 if none
+__device__ __forceinline__ int slot_dmax(const uint32_t* k, uint32_t s, uint32_t nv, int D) {
+    return s + 1 < nv ? common_bits(k[s], k[s + 1], 2 * D) / 2 : -1;
+}
+
+// ------------------------------------------------------------------------------------
+// bounding box: grid-stride min/max; the last block derives the box in FP64
+// ------------------------------------------------------------------------------------
+constexpr int kBBoxThreads = 256;
+constexpr int kBBoxBlocks = 152;
+
+__global__ void __launch_bounds__(kBBoxThreads)
+k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uint32_t* __restrict__ ticket,
+       BHParams* __restrict__ out) {
+    __shared__ float s[4][kBBoxThreads / 32];
+    __shared__ bool last;
+    float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float2 p = pos[i];
+        mnx = fminf(mnx, p.x);
+        mxx = fmaxf(mxx, p.x);
+        mny = fminf(mny, p.y);
+        mxy = fmaxf(mxy, p.y);
+    }
+    for (int o = 16; o; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        s[0][warp] = mnx;
+        s[1][warp] = mxx;
+        s[2][warp] = mny;
+        s[3][warp] = mxy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kBBoxThreads / 32; ++w) {
+            mnx = fminf(mnx, s[0][w]);
+            mxx = fmaxf(mxx, s[1][w]);
+            mny = fminf(mny, s[2][w]);
+            mxy = fmaxf(mxy, s[3][w]);
+        }
+        part[4 * blockIdx.x + 0] = mnx;
+        part[4 * blockIdx.x + 1] = mxx;
+        part[4 * blockIdx.x + 2] = mny;
+        part[4 * blockIdx.x + 3] = mxy;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double a = INFINITY, b = -INFINITY, c = INFINITY, d = -INFINITY;
+    for (uint32_t bl = 0; bl < gridDim.x; ++bl) {
+        double v0 = __ldcg(&part[4 * bl + 0]), v1 = __ldcg(&part[4 * bl + 1]);
+        double v2 = __ldcg(&part[4 * bl + 2]), v3 = __ldcg(&part[4 * bl + 3]);
+        if (v0 < a) a = v0;
+        if (v1 > b) b = v1;
+        if (v2 < c) c = v2;
+        if (v3 > d) d = v3;
+    }
+    // square box around the extent, 1/1024 margin, 2^15 cells per axis
+    double cx = 0.5 * (a + b), cy = 0.5 * (c + d);
+    double ext = b - a > d - c ? b - a : d - c;
+    if (!(ext > 0.0) || !isfinite(ext)) ext = 1.0;
+    if (!isfinite(cx)) cx = 0.0;
+    if (!isfinite(cy)) cy = 0.0;
+    double half = ext * 0.5 * (1.0 + 1.0 / 1024.0);
+    double scale = (double)(1u << (kBBoxBits - 1)) / half;
+    BHParams p;
+    p.cx = (float)cx;
+    p.cy = (float)cy;
+    p.scale = (float)scale;
+    double side0 = (double)(1u << kBBoxBits) / (double)p.scale;
+    p.radius0 = (float)(side0 * side0 * 0.5);
+    *out = p;
+}
+
+// ------------------------------------------------------------------------------------
+// keygen + digit histograms
+// ------------------------------------------------------------------------------------
+constexpr int kKeyThreads = 256;
+
+__global__ void __launch_bounds__(kKeyThreads)
+k_keygen(int bbox_mode, const BHParams* __restrict__ bp, float2* __restrict__ pos_in,
+         float* mass_in, float2* __restrict__ pos_out, float* mass_out,  // mass sets may alias
+         uint32_t n, uint32_t* __restrict__ keys, uint32_t* __restrict__ hist, int passes,
+         uint32_t* __restrict__ valid_count) {
+    __shared__ uint32_t sh[4][256];
+    for (int i = threadIdx.x; i < 4 * 256; i += kKeyThreads) (&sh[0][0])[i] = 0u;
+    __syncthreads();
+    BHParams p;
+    if (bbox_mode) p = *bp;
+    uint32_t valid = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float2 q = pos_in[i];
+        uint32_t key;
+        if (bbox_mode) {
+            key = spread_bits(bbox_cell(q.x, p.cx, p.scale)) | (spread_bits(bbox_cell(q.y, p.cy, p.scale)) << 1);
+            ++valid;
+        } else if (fixed_key(q.x, q.y, key)) {
+            ++valid;
+        } else {  // InitShader.comp:110-117
+            key = kKeyRemovedSort;
+            const float2 gone = make_float2(-kSimSize * 2.0f, -kSimSize * 2.0f);
+            pos_in[i] = gone;
+            pos_out[i] = gone;
+            mass_in[i] = 0.0f;
+            mass_out[i] = 0.0f;
+        }
+        keys[i] = key;
+        for (int ps = 0; ps < passes; ++ps) atomicAdd(&sh[ps][(key >> (8 * ps)) & 255u], 1u);
+    }
+    for (int o = 16; o; o >>= 1) valid += __shfl_xor_sync(0xffffffffu, valid, o);
+    if ((threadIdx.x & 31) == 0 && valid) atomicAdd(valid_count, valid);
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += kKeyThreads) {
+        uint32_t c = (&sh[0][0])[i];
+        if (c) atomicAdd(&hist[i], c);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// block-wide exclusive scan of one value per thread (256 threads)
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_t* s_warp, uint32_t& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < 8 ? s_warp[lane] : 0u;
+        for (int o = 1; o < 8; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < 8) s_warp[lane] = w;  // inclusive per warp
+    }
+    __syncthreads();
+    total = s_warp[7];
+    uint32_t warp_off = warp ? s_warp[warp - 1] : 0u;
+    uint32_t r = warp_off + x - v;
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
+    return *((volatile const uint32_t*)p);
+}
+
+// ------------------------------------------------------------------------------------
+// onesweep radix pass (stable, 8-bit digit at `shift`)
+// ------------------------------------------------------------------------------------
+template <bool IDENTITY>
+__global__ void __launch_bounds__(kSortThreads)
+k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+            uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
+            uint32_t* __restrict__ status, uint32_t* __restrict__ ticket, int* __restrict__ err) {
+    constexpr int KPT = kSortKeysPerThread;
+    constexpr int W = kSortThreads / 32;
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_whist[W][256];
+    __shared__ uint32_t s_start[256];
+    __shared__ uint32_t s_gbase[256];
+    __shared__ uint32_t s_warp[8];
+    __shared__ uint32_t s_keys[kSortTile];
+    __shared__ uint32_t s_vals[kSortTile];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    for (int i = t; i < W * 256; i += kSortThreads) (&s_whist[0][0])[i] = 0u;
+    if (t == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * kSortTile;
+    const uint32_t wbase = base + warp * 32 * KPT;
+
+    uint32_t key[KPT], val[KPT], rank[KPT];
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        uint32_t i = wbase + j * 32 + lane;
+        bool ok = i < n;
+        key[j] = ok ? kin[i] : 0u;
+        val[j] = ok ? (IDENTITY ? i : vin[i]) : 0u;
+    }
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {  // warp-local stable ranks, order (j, lane)
+        uint32_t i = wbase + j * 32 + lane;
+        bool ok = i < n;
+        uint32_t d = (key[j] >> shift) & 255u;
+        uint32_t peers = __match_any_sync(0xffffffffu, ok ? d : 0xffffffffu);
+        uint32_t prev = ok ? s_whist[warp][d] : 0u;
+        rank[j] = prev + __popc(peers & lt);
+        __syncwarp();
+        if (ok && (__ffs(peers) - 1) == lane) s_whist[warp][d] = prev + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit (thread t = digit t): exclusive offsets over warps, tile count
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        uint32_t c = s_whist[w][t];
+        s_whist[w][t] = tot;
+        tot += c;
+    }
+    // decoupled look-back over earlier tiles for digit t
+    uint32_t excl = 0;
+    uint32_t* st = status + (size_t)tile * 256 + t;
+    if (tile == 0) {
+        atomicExch(st, (2u << 30) | tot);
+    } else {
+        atomicExch(st, (1u << 30) | tot);
+        int64_t p = (int64_t)tile - 1;
+        uint32_t spins = 0;
+        while (p >= 0) {
+            uint32_t w = ld_volatile(status + (size_t)p * 256 + t);
+            uint32_t f = w >> 30;
+            if (f == 0u) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(err, kErrSortWait);
+                    break;
+                }
+                continue;
+            }
+            excl += w & 0x3fffffffu;
+            if (f == 2u) break;
+            --p;
+        }
+        atomicExch(st, (2u << 30) | (excl + tot));
+    }
+    uint32_t total;
+    const uint32_t gofs = block_exclusive_scan_256(hist[t], s_warp, total);
+    const uint32_t lstart = block_exclusive_scan_256(tot, s_warp, total);
+    s_start[t] = lstart;
+    s_gbase[t] = gofs + excl - lstart;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        uint32_t i = wbase + j * 32 + lane;
+        if (i < n) {
+            uint32_t d = (key[j] >> shift) & 255u;
+            uint32_t lp = s_start[d] + s_whist[warp][d] + rank[j];
+            s_keys[lp] = key[j];
+            s_vals[lp] = val[j];
+        }
+    }
+    __syncthreads();
+    const uint32_t tile_n = min((uint32_t)kSortTile, n - base);
+    for (uint32_t i = t; i < tile_n; i += kSortThreads) {
+        uint32_t k = s_keys[i];
+        uint32_t g = s_gbase[(k >> shift) & 255u] + i;
+        kout[g] = k;
+        vout[g] = s_vals[i];
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// internal nodes per slot + exclusive scan (decoupled look-back)
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kScanThreads)
+k_meta_scan(const uint32_t* __restrict__ skey, uint32_t n_items, const uint32_t* __restrict__ valid_count,
+            int D, uint32_t* __restrict__ E, uint32_t* __restrict__ status, uint32_t* __restrict__ ticket,
+            uint32_t* __restrict__ internal_count, int* __restrict__ err) {
+    __shared__ uint32_t s_tile, s_prefix;
+    __shared__ uint32_t s_warp[8];
+    const int t = threadIdx.x;
+    if (t == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t nv = *valid_count;
+    const uint32_t first = tile * kScanTile + t * kScanItems;
+    uint32_t e[kScanItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+        uint32_t s = first + j;
+        int c = 0;
+        if (s < nv) c = slot_dmax(skey, s, nv, D) - slot_dmin(skey, s, D) + 1;
+        e[j] = c > 0 ? (uint32_t)c : 0u;
+        sum += e[j];
+    }
+    uint32_t total;
+    uint32_t texcl = block_exclusive_scan_256(sum, s_warp, total);
+    if (t == 0) {
+        uint32_t excl = 0;
+        uint32_t* st = status + tile;
+        if (tile == 0) {
+            atomicExch(st, (2u << 30) | total);
+        } else {
+            atomicExch(st, (1u << 30) | total);
+            int64_t p = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (p >= 0) {
+                uint32_t w = ld_volatile(status + p);
+                uint32_t f = w >> 30;
+                if (f == 0u) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(err, kErrScanWait);
+                        break;
+                    }
+                    continue;
+                }
+                excl += w & 0x3fffffffu;
+                if (f == 2u) break;
+                --p;
+            }
+            atomicExch(st, (2u << 30) | (excl + total));
+        }
+        s_prefix = excl;
+    }
+    __syncthreads();
+    uint32_t run = s_prefix + texcl;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+        uint32_t s = first + j;
+        if (s < n_items) E[s] = run;
+        if (s == nv) *internal_count = run;
+        run += e[j];
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// preorder records (topology, radius, particle leaves)
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cell_end(const uint32_t* k, uint32_t a, uint32_t nv, int shift, uint32_t pre) {
+    // smallest t >= a with (k[t] >> shift) != pre, or nv; all t < a match
+    uint32_t step = 1, hi = a;
+    while (hi < nv && (k[hi] >> shift) == pre) {
+        a = hi + 1;
+        hi = a + step;
+        step <<= 1;
+    }
+    if (hi > nv) hi = nv;
+    while (a < hi) {
+        uint32_t mid = a + ((hi - a) >> 1);
+        if ((k[mid] >> shift) == pre) a = mid + 1;
+        else hi = mid;
+    }
+    return a;
+}
+
+__global__ void __launch_bounds__(256)
+k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ E,
+          const uint32_t* __restrict__ valid_count, int D, const BHParams* __restrict__ bp,
+          const float2* __restrict__ pos, const float* __restrict__ mass, float4* __restrict__ rec,
+          uint32_t* __restrict__ skip, uint32_t* __restrict__ nend, uint64_t cap, int* __restrict__ err) {
+    const uint32_t nv = *valid_count;
+    const float radius0 = bp->radius0;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += gridDim.x * blockDim.x) {
+        const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
+        const uint32_t Es = E[s];
+        const int e = dmax >= dmin ? dmax - dmin + 1 : 0;
+        const uint64_t leaf = (uint64_t)s + Es + e;
+        if (leaf >= cap) {
+            atomicOr(err, kErrTree);
+            continue;
+        }
+        const uint32_t i = sidx[s];
+        const float2 p = pos[i];
+        rec[leaf] = make_float4(p.x, p.y, mass[i], 0.0f);
+        skip[leaf] = 1u;
+        const uint32_t ks = skey[s];
+        uint32_t lo = s + 1;
+        for (int d = dmax; d >= dmin; --d) {  // finest first: each search starts at the last end
+            const int shift = 2 * (D - d);
+            const uint32_t end = cell_end(skey, lo, nv, shift, ks >> shift);
+            const uint32_t at = s + Es + (uint32_t)(d - dmin);
+            rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
+            skip[at] = end + E[end] - at;
+            nend[at] = end;
+            lo = end;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// bottom-up sums for one level
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_sums_level(int d, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
+             const uint32_t* __restrict__ valid_count, int D, float4* __restrict__ rec,
+             const uint32_t* __restrict__ nend, float2* __restrict__ msum) {
+    const uint32_t nv = *valid_count;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += gridDim.x * blockDim.x) {
+        const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
+        if (d < dmin || d > dmax) continue;
+        const uint32_t at = s + E[s] + (uint32_t)(d - dmin);
+        const uint32_t end = nend[at];
+        float sx = 0.0f, sy = 0.0f, sm = 0.0f;
+        if (d == D) {  // finest cell: its particle leaves follow the node record
+            for (uint32_t t = 0; t < end - s; ++t) {
+                float4 q = rec[at + 1 + t];
+                sx = __fadd_rn(sx, __fmul_rn(q.x, q.z));
+                sy = __fadd_rn(sy, __fmul_rn(q.y, q.z));
+                sm = __fadd_rn(sm, q.z);
+            }
+        } else {  // children in Morton order: nodes of level d+1 or single particles
+            uint32_t t = s;
+            while (t < end) {
+                const int cmin = slot_dmin(skey, t, D), cmax = slot_dmax(skey, t, nv, D);
+                if (cmin <= d + 1 && d + 1 <= cmax) {
+                    const uint32_t ch = t + E[t] + (uint32_t)(d + 1 - cmin);
+                    const float2 m2 = msum[ch];
+                    sx = __fadd_rn(sx, m2.x);
+                    sy = __fadd_rn(sy, m2.y);
+                    sm = __fadd_rn(sm, rec[ch].z);
+                    t = nend[ch];
+                } else {
+                    const int ce = cmax >= cmin ? cmax - cmin + 1 : 0;
+                    const float4 q = rec[t + E[t] + (uint32_t)ce];
+                    sx = __fadd_rn(sx, __fmul_rn(q.x, q.z));
+                    sy = __fadd_rn(sy, __fmul_rn(q.y, q.z));
+                    sm = __fadd_rn(sm, q.z);
+                    t += 1;
+                }
+            }
+        }
+        msum[at] = make_float2(sx, sy);
+        float cx = sx, cy = sy;
+        if (sm != 0.0f) {  // TreeMoveShader.comp:66-67
+            cx = __fdiv_rn(sx, sm);
+            cy = __fdiv_rn(sy, sm);
+        }
+        const float r = rec[at].w;
+        rec[at] = make_float4(cx, cy, sm, r);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// traversal + integrator (ForceShader.comp:78-152)
+// ------------------------------------------------------------------------------------
+constexpr int kForceWarps = 4;
+
+template <bool EXACT, bool COUNT>
+__global__ void __launch_bounds__(kForceWarps * 32)
+k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, const float4* __restrict__ rec,
+        const uint32_t* __restrict__ skip, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
+        float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
+        float eps2, float theta2, float k, float hdt, unsigned long long* __restrict__ stat) {
+    __shared__ float4 wrec[kForceWarps][32];
+    __shared__ uint32_t wskip[kForceWarps][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t group = blockIdx.x * kForceWarps + warp;
+    const uint32_t nv = counts[0];
+    const uint32_t T = nv + counts[1];  // preorder records
+    if (group * 32 >= nv) return;       // no particle in this warp: nothing to write
+    const uint32_t s = group * 32 + lane;
+    const bool valid = s < nv;
+    const uint32_t i = valid ? sidx[s] : 0u;
+    const float2 p = valid ? pos_in[i] : make_float2(0.0f, 0.0f);
+    float ax = 0.0f, ay = 0.0f;
+    unsigned long long n_acc = 0, n_vis = 0;
+    uint32_t base = 0, ind = 0;
+    wrec[warp][lane] = rec[lane];
+    wskip[warp][lane] = skip[lane];
+    __syncwarp();
+    while (ind < T) {
+        if (ind - base >= 32u) {  // warp-uniform: reload the 32-record window
+            base = ind & ~31u;
+            __syncwarp();
+            wrec[warp][lane] = rec[base + lane];
+            wskip[warp][lane] = skip[base + lane];
+            __syncwarp();
+        }
+        const float4 q = wrec[warp][ind - base];
+        const float dx = q.x - p.x, dy = q.y - p.y;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
+        const bool ok = !valid || q.w <= d2 * theta2;
+        if (COUNT) ++n_vis;
+        if (__all_sync(0xffffffffu, ok)) {
+            const float r = EXACT ? __fdiv_rn(1.0f, __fsqrt_rn(d2)) : rsqrtf(d2);
+            const float sc = ((q.z * r) * r) * r;
+            ax = fmaf(dx, sc, ax);
+            ay = fmaf(dy, sc, ay);
+            if (COUNT) n_acc += valid;
+            ind += wskip[warp][ind - base];
+        } else {
+            ++ind;
+        }
+    }
+    if (COUNT) {
+        for (int o = 16; o; o >>= 1) n_acc += __shfl_xor_sync(0xffffffffu, n_acc, o);
+        if (lane == 0) {
+            atomicAdd(&stat[0], n_acc);
+            atomicAdd(&stat[1], n_vis);
+        }
+    }
+    if (!valid) return;
+    if (acc_rec) acc_rec[i] = make_float2(ax, ay);
+    const float2 v = vel_in[i];
+    const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);  // ForceShader.comp:145-146
+    pos_out[i] = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
+    vel_out[i] = make_float2(nvx, nvy);
+}
+
+int grid_for(uint64_t n, int threads) {
+    uint64_t b = (n + threads - 1) / threads;
+    if (b > 152ull * 16) b = 152ull * 16;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+}  // namespace
+
+uint64_t bh_capacity(int box_mode, uint64_t n_al) {
+    uint64_t levels = box_mode == GS_BOX_BOUNDING ? kBBoxBits + 1 : kFixedDepth + 1;
+    return n_al + levels * (n_al / 2) + 64;
+}
+
+// counters layout inside the zeroed block
+enum { kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrCount = 12 };
+
+cudaError_t bh_alloc(gs_sim* s) {
+    BHWork& w = s->bh;
+    const uint64_t n = s->n_al;
+    const bool bbox = s->p.box_mode == GS_BOX_BOUNDING;
+    w.depth = bbox ? kBBoxBits : kFixedDepth;
+    w.passes = bbox ? 4 : 3;  // 30-bit keys / 20-bit keys + removal bit
+    w.cap = bh_capacity(s->p.box_mode, n);
+    w.sort_tiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
+    w.scan_tiles = (uint32_t)((n + 1 + kScanTile - 1) / kScanTile);
+    cudaError_t e;
+#define GS_ALLOC(ptr, bytes)                                    \
+    do {                                                        \
+        e = cudaMalloc((void**)&(ptr), (bytes));                \
+        if (e != cudaSuccess) return e;                         \
+    } while (0)
+    for (int b = 0; b < 2; ++b) {
+        GS_ALLOC(w.keys[b], n * sizeof(uint32_t));
+        GS_ALLOC(w.idx[b], n * sizeof(uint32_t));
+    }
+    GS_ALLOC(w.E, (n + 1) * sizeof(uint32_t));
+    GS_ALLOC(w.rec, (w.cap + 32) * sizeof(float4));
+    GS_ALLOC(w.skip, (w.cap + 32) * sizeof(uint32_t));
+    GS_ALLOC(w.nend, w.cap * sizeof(uint32_t));
+    GS_ALLOC(w.msum, w.cap * sizeof(float2));
+    GS_ALLOC(w.bbox_part, kBBoxBlocks * 4 * sizeof(float));
+    GS_ALLOC(w.params, sizeof(BHParams));
+    // one block cleared per step: hist | counters | sort status | scan status
+    const size_t hist_b = 4 * 256 * sizeof(uint32_t);
+    const size_t ctr_b = 16 * sizeof(uint32_t);
+    const size_t sort_b = (size_t)w.passes * w.sort_tiles * 256 * sizeof(uint32_t);
+    const size_t scan_b = (size_t)w.scan_tiles * sizeof(uint32_t);
+    w.zero_bytes = hist_b + ctr_b + sort_b + scan_b;
+    GS_ALLOC(w.zero_base, w.zero_bytes);
+#undef GS_ALLOC
+    char* zb = (char*)w.zero_base;
+    w.hist = (uint32_t*)zb;
+    w.counters = (uint32_t*)(zb + hist_b);
+    w.sort_status = (uint32_t*)(zb + hist_b + ctr_b);
+    w.scan_status = (uint32_t*)(zb + hist_b + ctr_b + sort_b);
+    // zero everything once so that debug reads of a never-built tree are defined
+    e = cudaMemset(w.zero_base, 0, w.zero_bytes);
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(w.rec, 0, (w.cap + 32) * sizeof(float4));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(w.skip, 0, (w.cap + 32) * sizeof(uint32_t));
+    if (e != cudaSuccess) return e;
+    BHParams fixed{0.0f, 0.0f, (float)kGrid / (2.0f * kSimSize), kSimSize * kSimSize * 2.0f};
+    e = cudaMemcpy(w.params, &fixed, sizeof fixed, cudaMemcpyHostToDevice);
+    return e;
+}
+
+void bh_free(gs_sim* s) {
+    BHWork& w = s->bh;
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(w.keys[b]);
+        cudaFree(w.idx[b]);
+        w.keys[b] = w.idx[b] = nullptr;
+    }
+    cudaFree(w.E);
+    cudaFree(w.rec);
+    cudaFree(w.skip);
+    cudaFree(w.nend);
+    cudaFree(w.msum);
+    cudaFree(w.bbox_part);
+    cudaFree(w.params);
+    cudaFree(w.zero_base);
+    w.E = nullptr;
+    w.rec = nullptr;
+    w.skip = w.nend = nullptr;
+    w.msum = nullptr;
+    w.bbox_part = nullptr;
+    w.params = nullptr;
+    w.zero_base = nullptr;
+}
+
+cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
+    BHWork& w = s->bh;
+    cudaStream_t st = s->stream;
+    const uint32_t n = (uint32_t)s->n_al;
+    const bool bbox = s->p.box_mode == GS_BOX_BOUNDING;
+    cudaError_t e = cudaMemsetAsync(w.zero_base, 0, w.zero_bytes, st);
+    if (e != cudaSuccess) return e;
+    uint32_t* ctr = w.counters;
+    if (bbox) {
+        stage_begin(s, kStageBBox, profile);
+        k_bbox<<<kBBoxBlocks, kBBoxThreads, 0, st>>>(s->pos[in], n, w.bbox_part, ctr + kCtrBBox, w.params);
+        count_launch(s);
+        stage_end(s, kStageBBox, profile);
+    }
+    stage_begin(s, kStageKeys, profile);
+    k_keygen<<<grid_for(n, kKeyThreads), kKeyThreads, 0, st>>>(bbox ? 1 : 0, w.params, s->pos[in], s->mass[in],
+                                                               s->pos[out], s->mass[out], n, w.keys[0], w.hist,
+                                                               w.passes, ctr + kCtrValid);
+    count_launch(s);
+    stage_end(s, kStageKeys, profile);
+    stage_begin(s, kStageSort, profile);
+    for (int ps = 0; ps < w.passes; ++ps) {
+        const int a = ps & 1, b = a ^ 1;
+        uint32_t* status = w.sort_status + (size_t)ps * w.sort_tiles * 256;
+        if (ps == 0)
+            k_sort_pass<true><<<w.sort_tiles, kSortThreads, 0, st>>>(w.keys[a], nullptr, w.keys[b], w.idx[b], n,
+                                                                     8 * ps, w.hist + 256 * ps, status,
+                                                                     ctr + kCtrSort + ps, s->d_err);
+        else
+            k_sort_pass<false><<<w.sort_tiles, kSortThreads, 0, st>>>(w.keys[a], w.idx[a], w.keys[b], w.idx[b], n,
+                                                                      8 * ps, w.hist + 256 * ps, status,
+                                                                      ctr + kCtrSort + ps, s->d_err);
+    }
+    count_launch(s, w.passes);
+    w.final_keys = w.passes & 1;
+    stage_end(s, kStageSort, profile);
+    const uint32_t* skey = w.keys[w.final_keys];
+    const uint32_t* sidx = w.idx[w.final_keys];
+    stage_begin(s, kStageScan, profile);
+    k_meta_scan<<<w.scan_tiles, kScanThreads, 0, st>>>(skey, n + 1, ctr + kCtrValid, w.depth, w.E, w.scan_status,
+                                                        ctr + kCtrScan, ctr + kCtrInternal, s->d_err);
+    count_launch(s);
+    stage_end(s, kStageScan, profile);
+    stage_begin(s, kStageRecords, profile);
+    k_records<<<grid_for(n, 256), 256, 0, st>>>(skey, sidx, w.E, ctr + kCtrValid, w.depth, w.params, s->pos[in],
+                                                s->mass[in], w.rec, w.skip, w.nend, w.cap, s->d_err);
+    count_launch(s);
+    stage_end(s, kStageRecords, profile);
+    stage_begin(s, kStageSums, profile);
+    for (int d = w.depth; d >= 0; --d)
+        k_sums_level<<<grid_for(n, 256), 256, 0, st>>>(d, skey, w.E, ctr + kCtrValid, w.depth, w.rec, w.nend, w.msum);
+    count_launch(s, w.depth + 1);
+    stage_end(s, kStageSums, profile);
+    stage_begin(s, kStageForce, profile);
+    const float k = s->G * s->dt_eff;  // ForceShader.comp:145 (GRAVITATIONAL_CONST * SIMULATION_TIME)
+    const float hdt = 0.5f * s->dt_eff;
+    const int blocks = (int)((n / 32 + kForceWarps - 1) / kForceWarps);
+    const bool exact = s->p.math_mode == GS_MATH_REFERENCE;
+    const bool count = (s->p.flags & GS_FLAG_COUNT_INTERACTIONS) != 0;
+    unsigned long long* stat = (unsigned long long*)(ctr + kCtrStat);
+#define GS_FORCE(E_, C_)                                                                                      \
+    k_force<E_, C_><<<blocks, kForceWarps * 32, 0, st>>>(sidx, ctr + kCtrValid, w.rec, w.skip, s->pos[in],    \
+                                                         s->vel[in], s->pos[out], s->vel[out], s->acc, n, s->eps2, \
+                                                         s->theta2, k, hdt, stat)
+    if (exact) {
+        if (count) GS_FORCE(true, true);
+        else GS_FORCE(true, false);
+    } else {
+        if (count) GS_FORCE(false, true);
+        else GS_FORCE(false, false);
+    }
+#undef GS_FORCE
+    count_launch(s);
+    stage_end(s, kStageForce, profile);
+    return cudaGetLastError();
+}
+
+// Host readback of the most recent tree (not on the hot path).
+gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
+                        float* node_pos, float* node_mass, uint64_t capacity, uint64_t* tree_records) {
+    BHWork& w = s->bh;
+    const uint64_t n = s->n_al;
+    uint32_t ctr[kCtrCount];
+    GS_CUDA(cudaMemcpy(ctr, w.counters, sizeof ctr, cudaMemcpyDeviceToHost));
+    const uint64_t nv = ctr[kCtrValid];
+    const uint64_t T = nv + ctr[kCtrInternal];
+    if (tree_records) *tree_records = T;
+    if (keys || sorted_src) {
+        uint32_t* hk = new uint32_t[n];
+        uint32_t* hi = new uint32_t[n];
+        cudaError_t e1 = cudaMemcpy(hk, w.keys[w.final_keys], n * 4, cudaMemcpyDeviceToHost);
+        cudaError_t e2 = cudaMemcpy(hi, w.idx[w.final_keys], n * 4, cudaMemcpyDeviceToHost);
+        if (e1 == cudaSuccess && e2 == cudaSuccess) {
+            for (uint64_t q = 0; q < n; ++q) {
+                if (keys && hi[q] < n) keys[hi[q]] = q < nv ? hk[q] : kKeyRemoved;
+                if (sorted_src) sorted_src[q] = q < nv ? hi[q] : (uint32_t)n;
+            }
+        }
+        delete[] hk;
+        delete[] hi;
+        GS_CUDA(e1);
+        GS_CUDA(e2);
+    }
+    const uint64_t m = T < capacity ? T : capacity;
+    if (m && (node_radius || node_pos || node_mass)) {
+        float4* hr = new float4[m];
+        cudaError_t e1 = cudaMemcpy(hr, w.rec, m * sizeof(float4), cudaMemcpyDeviceToHost);
+        if (e1 == cudaSuccess) {
+            for (uint64_t q = 0; q < m; ++q) {
+                if (node_pos) {
+                    node_pos[2 * q] = hr[q].x;
+                    node_pos[2 * q + 1] = hr[q].y;
+                }
+                if (node_mass) node_mass[q] = hr[q].z;
+                if (node_radius) node_radius[q] = hr[q].w;
+            }
+        }
+        delete[] hr;
+        GS_CUDA(e1);
+    }
+    if (m && node_skip) GS_CUDA(cudaMemcpy(node_skip, w.skip, m * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return GS_OK;
+}
+
+gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits) {
+    uint32_t ctr[kCtrCount];
+    GS_CUDA(cudaMemcpy(ctr, s->bh.counters, sizeof ctr, cudaMemcpyDeviceToHost));
+    *nv = ctr[kCtrValid];
+    *internal = ctr[kCtrInternal];
+    unsigned long long st[2];
+    memcpy(st, ctr + kCtrStat, sizeof st);
+    *inter = st[0];
+    *visits = st[1];
+    return GS_OK;
+}
+
+}  // namespace gsim

@@ -1,0 +1,267 @@
+// direct.cu -- O(N^2) direct-sum force with the integrator fused into the epilogue.
+//
+// Replaces src/Simulation/Direct/Shaders/SimShader.comp:37-74 (one dispatch per step,
+// src/Simulation/Direct/DirectSimulation.cpp:306-319).
+//
+// FAST mode (k_direct_fast): each block owns an i-tile of 128*IPT particles and one
+// j-chunk; j is staged 64 at a time in shared memory as float4 {x, y, m, 0} and
+// broadcast to all threads; every thread keeps IPT targets in registers.  Each 64-wide
+// tile is summed plainly in FP32, and the tile partials are added with Kahan
+// compensation.  When the j-range is split over several blocks (small N, to fill 152
+// SMs), every block stores its compensated partial and the last block to finish an
+// i-tile (ticket counter, no waiting) combines the chunks in chunk order, again with
+// Kahan, and applies the integrator.  Results do not depend on block scheduling.
+//
+// REFERENCE mode (k_direct_ref): one thread per particle, j ascending over all N_al
+// particles, plain FP32 accumulation and correctly rounded 1/sqrt -- the shader's order,
+// bit-identical to the CPU restatement.
+//
+// Roofline: 14 algorithmic FLOP per pair (2 sub, 2 FMA for r^2, rsqrt, 3 mul, 2 FMA),
+// 9 FP32-pipe instructions + 1 MUFU per pair; FP32-bound.
+#include "internal.cuh"
+
+namespace gsim {
+namespace {
+
+constexpr int kDirectBlock = 128;
+constexpr int kDirectTileJ = 64;
+
+template <int IPT>
+__global__ void __launch_bounds__(kDirectBlock)
+k_direct_fast(const float2* __restrict__ pos, const float2* __restrict__ vel,
+              const float* __restrict__ mass, float2* __restrict__ pos_out,
+              float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
+              int chunks, uint32_t jchunk, float eps2, float k, float hdt,
+              float4* __restrict__ partials, uint32_t* __restrict__ tickets) {
+    __shared__ float4 sj[kDirectTileJ];
+    __shared__ uint32_t s_ticket;
+    const int t = threadIdx.x;
+    const uint32_t tile_base = blockIdx.x * (kDirectBlock * IPT);
+    const uint32_t j0 = blockIdx.y * jchunk;
+    const uint32_t j1 = min(j0 + jchunk, n_al);
+
+    float px[IPT], py[IPT], sx[IPT], sy[IPT], cx[IPT], cy[IPT];
+#pragma unroll
+    for (int r = 0; r < IPT; ++r) {
+        uint32_t i = tile_base + t + r * kDirectBlock;
+        float2 p = i < n_al ? pos[i] : make_float2(0.f, 0.f);
+        px[r] = p.x;
+        py[r] = p.y;
+        sx[r] = sy[r] = cx[r] = cy[r] = 0.f;
+    }
+
+    for (uint32_t jt = j0; jt < j1; jt += kDirectTileJ) {
+        __syncthreads();
+        if (t < kDirectTileJ) {
+            float2 q = pos[jt + t];
+            sj[t] = make_float4(q.x, q.y, mass[jt + t], 0.f);
+        }
+        __syncthreads();
+        float tx[IPT], ty[IPT];
+#pragma unroll
+        for (int r = 0; r < IPT; ++r) tx[r] = ty[r] = 0.f;
+#pragma unroll 16
+        for (int jj = 0; jj < kDirectTileJ; ++jj) {
+            const float4 q = sj[jj];
+#pragma unroll
+            for (int r = 0; r < IPT; ++r) {
+                float dx = q.x - px[r];
+                float dy = q.y - py[r];
+                float d2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
+                float rr = rsqrtf(d2);
+                float s = ((q.z * rr) * rr) * rr;
+                tx[r] = fmaf(dx, s, tx[r]);
+                ty[r] = fmaf(dy, s, ty[r]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < IPT; ++r) {  // Kahan-compensated add of the tile partial
+            float y = tx[r] - cx[r];
+            float u = sx[r] + y;
+            cx[r] = (u - sx[r]) - y;
+            sx[r] = u;
+            y = ty[r] - cy[r];
+            u = sy[r] + y;
+            cy[r] = (u - sy[r]) - y;
+            sy[r] = u;
+        }
+    }
+
+    if (chunks > 1) {
+#pragma unroll
+        for (int r = 0; r < IPT; ++r) {
+            uint32_t i = tile_base + t + r * kDirectBlock;
+            if (i < n_al) partials[(size_t)blockIdx.y * n_al + i] = make_float4(sx[r], sy[r], cx[r], cy[r]);
+        }
+        __threadfence();
+        __syncthreads();
+        if (t == 0) s_ticket = atomicAdd(&tickets[blockIdx.x], 1u);
+        __syncthreads();
+        if (s_ticket != (uint32_t)chunks - 1) return;
+        __threadfence();
+#pragma unroll
+        for (int r = 0; r < IPT; ++r) {
+            uint32_t i = tile_base + t + r * kDirectBlock;
+            float ax = 0.f, ay = 0.f, kx = 0.f, ky = 0.f;
+            if (i < n_al) {
+                for (int c = 0; c < chunks; ++c) {
+                    float4 q = __ldcg(&partials[(size_t)c * n_al + i]);
+                    float y = (q.x - q.z) - kx;
+                    float u = ax + y;
+                    kx = (u - ax) - y;
+                    ax = u;
+                    y = (q.y - q.w) - ky;
+                    u = ay + y;
+                    ky = (u - ay) - y;
+                    ay = u;
+                }
+            }
+            sx[r] = ax;
+            cx[r] = kx;
+            sy[r] = ay;
+            cy[r] = ky;
+        }
+        if (t == 0) tickets[blockIdx.x] = 0u;  // ready for the next step
+    }
+
+#pragma unroll
+    for (int r = 0; r < IPT; ++r) {
+        uint32_t i = tile_base + t + r * kDirectBlock;
+        if (i >= n_al) continue;
+        float ax = sx[r] - cx[r], ay = sy[r] - cy[r];
+        if (acc_rec) acc_rec[i] = make_float2(ax, ay);
+        float2 v = vel[i];
+        float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);  // SimShader.comp:68
+        pos_out[i] = make_float2(fmaf(v.x + nvx, hdt, px[r]), fmaf(v.y + nvy, hdt, py[r]));  // :69
+        vel_out[i] = make_float2(nvx, nvy);
+    }
+}
+
+__global__ void __launch_bounds__(64)
+k_direct_ref(const float2* __restrict__ pos, const float2* __restrict__ vel,
+             const float* __restrict__ mass, float2* __restrict__ pos_out,
+             float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
+             float eps2, float k, float hdt) {
+    __shared__ float2 sp[64];
+    __shared__ float sm[64];
+    const uint32_t i = blockIdx.x * 64 + threadIdx.x;
+    const float2 p = pos[i];
+    float ax = 0.f, ay = 0.f;
+    for (uint32_t jt = 0; jt < n_al; jt += 64) {  // SimShader.comp:43-65
+        sp[threadIdx.x] = pos[jt + threadIdx.x];
+        sm[threadIdx.x] = mass[jt + threadIdx.x];
+        __syncthreads();
+        for (int jj = 0; jj < 64; ++jj) {
+            float dx = sp[jj].x - p.x;
+            float dy = sp[jj].y - p.y;
+            float d2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
+            float r = __fdiv_rn(1.0f, __fsqrt_rn(d2));
+            float s = ((sm[jj] * r) * r) * r;
+            ax = fmaf(dx, s, ax);
+            ay = fmaf(dy, s, ay);
+        }
+        __syncthreads();
+    }
+    if (acc_rec) acc_rec[i] = make_float2(ax, ay);
+    float2 v = vel[i];
+    float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);
+    pos_out[i] = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
+    vel_out[i] = make_float2(nvx, nvy);
+}
+
+__global__ void __launch_bounds__(256)
+k_accel_f64(const uint32_t* __restrict__ targets, const float2* __restrict__ pos,
+            const float* __restrict__ mass, uint32_t n, double eps2, double2* __restrict__ out) {
+    __shared__ double sx[256], sy[256];
+    const uint32_t i = targets[blockIdx.x];
+    const double px = pos[i].x, py = pos[i].y;
+    double ax = 0.0, ay = 0.0;
+    for (uint32_t j = threadIdx.x; j < n; j += 256) {
+        double dx = (double)pos[j].x - px, dy = (double)pos[j].y - py;
+        double d2 = dx * dx + dy * dy + eps2;
+        double s = (double)mass[j] / (d2 * sqrt(d2));
+        ax += dx * s;
+        ay += dy * s;
+    }
+    sx[threadIdx.x] = ax;
+    sy[threadIdx.x] = ay;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            sx[threadIdx.x] += sx[threadIdx.x + w];
+            sy[threadIdx.x] += sy[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = make_double2(sx[0], sy[0]);
+}
+
+}  // namespace
+
+static int pick_chunks(uint64_t n_al, int ipt) {
+    const uint64_t itiles = (n_al + kDirectBlock * ipt - 1) / (kDirectBlock * ipt);
+    const uint64_t want_blocks = 152ull * 12;
+    uint64_t c = (want_blocks + itiles - 1) / itiles;
+    uint64_t max_c = n_al / 256;  // keep at least 256 sources per chunk
+    if (c > max_c) c = max_c;
+    if (c < 1) c = 1;
+    if (c > 64) c = 64;
+    return (int)c;
+}
+
+cudaError_t direct_alloc(gs_sim* s) {
+    DirectWork& w = s->dw;
+    w.ipt = 2;
+    w.block = kDirectBlock;
+    w.chunks = pick_chunks(s->n_al, w.ipt);
+    if (w.chunks > 1) {
+        const uint64_t itiles = (s->n_al + kDirectBlock * w.ipt - 1) / (kDirectBlock * w.ipt);
+        cudaError_t e = cudaMalloc(&w.partials, sizeof(float4) * s->n_al * (size_t)w.chunks);
+        if (e != cudaSuccess) return e;
+        e = cudaMalloc(&w.tickets, sizeof(uint32_t) * itiles);
+        if (e != cudaSuccess) return e;
+        e = cudaMemset(w.tickets, 0, sizeof(uint32_t) * itiles);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+void direct_free(gs_sim* s) {
+    cudaFree(s->dw.partials);
+    cudaFree(s->dw.tickets);
+    s->dw.partials = nullptr;
+    s->dw.tickets = nullptr;
+}
+
+cudaError_t direct_step(gs_sim* s, int in, int out, bool profile) {
+    const float k = s->dt_eff * s->G;  // SimShader.comp:68 (SIMULATION_TIME * GRAVITATIONAL_CONST)
+    const float hdt = 0.5f * s->dt_eff;
+    const uint32_t n_al = (uint32_t)s->n_al;
+    stage_begin(s, kStageDirect, profile);
+    if (s->p.math_mode == GS_MATH_REFERENCE) {
+        k_direct_ref<<<n_al / 64, 64, 0, s->stream>>>(s->pos[in], s->vel[in], s->mass[in], s->pos[out],
+                                                       s->vel[out], s->acc, n_al, s->eps2, k, hdt);
+    } else {
+        DirectWork& w = s->dw;
+        const uint32_t itiles = (n_al + kDirectBlock * w.ipt - 1) / (kDirectBlock * w.ipt);
+        uint32_t jchunk = (n_al + w.chunks - 1) / w.chunks;
+        jchunk = (jchunk + kDirectTileJ - 1) / kDirectTileJ * kDirectTileJ;
+        const int chunks = (int)((n_al + jchunk - 1) / jchunk);
+        dim3 grid(itiles, chunks);
+        k_direct_fast<2><<<grid, kDirectBlock, 0, s->stream>>>(
+            s->pos[in], s->vel[in], s->mass[in], s->pos[out], s->vel[out], s->acc, n_al, chunks, jchunk,
+            s->eps2, k, hdt, w.partials, w.tickets);
+    }
+    count_launch(s);
+    stage_end(s, kStageDirect, profile);
+    return cudaGetLastError();
+}
+
+cudaError_t accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* d_targets, double2* d_out) {
+    const double eps2 = (double)s->p.softening_len * (double)s->p.softening_len;
+    k_accel_f64<<<n_targets, 256, 0, s->stream>>>(d_targets, s->pos[s->in], s->mass[s->in],
+                                                  (uint32_t)s->n_al, eps2, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace gsim

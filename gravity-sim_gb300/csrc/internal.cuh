@@ -1,0 +1,144 @@
+// internal.cuh -- shared definitions of the GB300 Gravity-Sim library.
+//
+// Device data layout (one gs_sim, N_al = N rounded up to 64):
+//   state      2 sets x { pos float2[N_al], vel float2[N_al], mass float[N_al] }  (ping-pong,
+//              the reference's compute-input / compute-output buffer pair)
+//   Barnes-Hut scratch (N_al-sized, never a fixed 1024^2 grid):
+//              keys/idx u32[N_al] x 2 (radix-sort ping-pong), E u32[N_al+1] (exclusive
+//              scan of internal nodes per sorted slot), rec float4[cap] = {x, y, m, radius}
+//              and skip u32[cap] (preorder records, cap = N_al + levels*N_al/2 + 64),
+//              nend u32[cap] and msum float2[cap] (cell end slot and mass moments)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/gsim.h"
+
+namespace gsim {
+
+constexpr int kWarp = 32;
+constexpr uint32_t kAlignment = 64;         // GetRequiredParticleAlignment()
+constexpr float kSimSize = 500.0f;          // BarnesHutSimulation.cpp:580
+constexpr uint32_t kGrid = 1024;            // BarnesHutSimulation.cpp:582
+constexpr int kFixedDepth = 10;             // finest level of the fixed box
+constexpr int kBBoxBits = 15;               // per-axis bits in bounding-box mode
+constexpr uint32_t kKeyRemovedSort = 1u << 20;  // sort key of removed particles (fixed box)
+constexpr uint32_t kKeyRemoved = 0xFFFFFFFFu;   // reported key of removed particles
+
+// stage indices of gs_stats.stage_ms
+enum Stage { kStageBBox = 0, kStageKeys, kStageSort, kStageScan, kStageRecords, kStageSums, kStageForce, kStageDirect };
+
+// device error bits (sim->d_err)
+constexpr int kErrSortWait = 1;
+constexpr int kErrScanWait = 2;
+constexpr int kErrTree = 4;
+
+// radix sort shape: 256 threads x 8 keys per tile
+constexpr int kSortThreads = 256;
+constexpr int kSortKeysPerThread = 8;
+constexpr int kSortTile = kSortThreads * kSortKeysPerThread;
+// single-pass scan shape
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+// bounded spin for decoupled look-back: after this many polls the kernel flags an error
+constexpr uint32_t kSpinLimit = 1u << 24;
+
+struct BHParams {
+    float cx, cy, scale, radius0;  // bounding box (fixed box: 0, 0, 1.024, 500000)
+};
+
+struct BHWork {
+    int depth = 0;        // finest level D (10 fixed box, 15 bounding box)
+    int passes = 0;       // radix passes of 8 bits
+    uint64_t cap = 0;     // record capacity
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* idx[2] = {nullptr, nullptr};
+    uint32_t* hist = nullptr;          // [4][256] digit counts
+    uint32_t* sort_status = nullptr;   // [passes][tiles][256]
+    uint32_t* counters = nullptr;      // [0..3] sort tile tickets, [4] scan ticket, [5] bbox ticket,
+                                       // [6] valid count, [7] internal count, [8..9] interactions
+    uint32_t* scan_status = nullptr;   // [scan tiles]
+    uint32_t* E = nullptr;             // [N_al + 1]
+    float4* rec = nullptr;             // [cap + 32]
+    uint32_t* skip = nullptr;          // [cap + 32]
+    uint32_t* nend = nullptr;          // [cap]
+    float2* msum = nullptr;            // [cap]
+    float* bbox_part = nullptr;        // [blocks][4]
+    BHParams* params = nullptr;        // device
+    uint32_t sort_tiles = 0, scan_tiles = 0;
+    int final_keys = 0;                // which keys/idx buffer holds the sorted result
+    size_t zero_bytes = 0;             // bytes of the contiguous block cleared each step
+    void* zero_base = nullptr;
+};
+
+struct DirectWork {
+    int ipt = 2;           // particles per thread
+    int block = 128;       // threads per block
+    int chunks = 1;        // j-range split
+    float4* partials = nullptr;  // [chunks][N_al] {sx, sy, cx, cy}
+    uint32_t* tickets = nullptr; // [i-tiles]
+};
+
+}  // namespace gsim
+
+struct gs_sim {
+    gs_params p{};
+    uint64_t n = 0, n_al = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    float2* pos[2] = {nullptr, nullptr};
+    float2* vel[2] = {nullptr, nullptr};
+    float* mass[2] = {nullptr, nullptr};
+    int in = 0;  // compute-input set
+    float dt_eff = 0, G = 0, eps2 = 0, theta2 = 0;
+    float2* acc = nullptr;  // GS_FLAG_RECORD_ACCEL
+    int* d_err = nullptr;
+    gsim::BHWork bh;
+    gsim::DirectWork dw;
+    cudaEvent_t batch_done = nullptr;
+    bool batch_pending = false;
+    cudaEvent_t ev[2 * GS_STAGE_COUNT] = {};
+    gs_stats stats{};
+    // CUDA graphs: one per ping-pong parity
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    uint64_t steps_done = 0;
+    bool capturing = false;          // stage events become external event-record graph nodes
+    uint32_t stage_ran = 0;          // stages recorded in the current step (GS_FLAG_PROFILE)
+    bool profile_pending = false;    // stage events of the last step not yet accumulated
+    uint32_t graph_stages[2] = {0, 0};  // stages recorded by each captured graph
+    uint32_t launches_in_step = 0;   // kernels enqueued by the step being built
+    uint32_t launches_per_step[2] = {0, 0};  // per ping-pong parity (graph replay count)
+    uint64_t kernel_launches = 0;    // kernels launched since creation
+};
+
+namespace gsim {
+
+// error reporting: thread-local message
+void set_error(const std::string& msg);
+gs_status cuda_fail(cudaError_t e, const char* what);
+
+#define GS_CUDA(call)                                          \
+    do {                                                       \
+        cudaError_t _e = (call);                               \
+        if (_e != cudaSuccess) return gsim::cuda_fail(_e, #call); \
+    } while (0)
+
+// launchers (return cudaError_t of the launch)
+cudaError_t bh_alloc(gs_sim* s);
+void bh_free(gs_sim* s);
+cudaError_t bh_step(gs_sim* s, int in, int out, bool profile);
+cudaError_t direct_alloc(gs_sim* s);
+void direct_free(gs_sim* s);
+cudaError_t direct_step(gs_sim* s, int in, int out, bool profile);
+cudaError_t accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* d_targets, double2* d_out);
+uint64_t bh_capacity(int box_mode, uint64_t n_al);
+
+// profiling helpers
+void stage_begin(gs_sim* s, int stage, bool profile);
+void stage_end(gs_sim* s, int stage, bool profile);
+inline void count_launch(gs_sim* s, uint32_t k = 1) { s->launches_in_step += k; }
+
+}  // namespace gsim

@@ -1,0 +1,429 @@
+// sim.cu -- gs_sim lifecycle and the C ABI entry points of include/gsim.h.
+//
+// The step loop mirrors DirectSimulation::RunSimulations / BarnesHutSimulation::RunSimulations
+// (src/Simulation/Direct/DirectSimulation.cpp:271-353,
+// src/Simulation/BarnesHut/BarnesHutSimulation.cpp:849-952): wait for the previous batch,
+// enqueue `count` steps that read set `in` and write set `out`, flip the indices on the
+// host after every step (ParticleSystem::NextComputeIndices, src/Particles/ParticleSystem.hpp:169-174).
+// Instead of re-recording command buffers, each parity of the ping-pong is captured
+// once into a CUDA graph and replayed.
+#include <chrono>
+#include <cstring>
+#include <new>
+#include <thread>
+
+#include "internal.cuh"
+
+namespace gsim {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+gs_status cuda_fail(cudaError_t e, const char* what) {
+    set_error(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+    if (e == cudaErrorMemoryAllocation) return GS_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GS_ERR_NO_DEVICE;
+    return GS_ERR_CUDA;
+}
+
+static void record(gs_sim* s, cudaEvent_t e) {
+    if (s->capturing) cudaEventRecordWithFlags(e, s->stream, cudaEventRecordExternal);
+    else cudaEventRecord(e, s->stream);
+}
+void stage_begin(gs_sim* s, int stage, bool profile) {
+    if (profile) record(s, s->ev[2 * stage]);
+}
+void stage_end(gs_sim* s, int stage, bool profile) {
+    if (profile) {
+        record(s, s->ev[2 * stage + 1]);
+        s->stage_ran |= 1u << stage;
+    }
+}
+
+gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
+                        float* node_pos, float* node_mass, uint64_t capacity, uint64_t* tree_records);
+gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits);
+
+}  // namespace gsim
+
+using namespace gsim;
+
+namespace {
+
+constexpr uint64_t kMaxParticles = 1ull << 28;
+constexpr uint64_t kDefaultTimeoutNs = 600ull * 1000000000ull;
+
+gs_status invalid(const char* msg) {
+    set_error(msg);
+    return GS_ERR_INVALID_ARGUMENT;
+}
+
+gs_status wait_event(cudaEvent_t ev, uint64_t timeout_ns) {
+    if (!timeout_ns) timeout_ns = kDefaultTimeoutNs;
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaSuccess) return GS_OK;
+        if (e != cudaErrorNotReady) return cuda_fail(e, "cudaEventQuery");
+        auto el = std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+        if ((uint64_t)el > timeout_ns) {
+            set_error("timed out waiting for the GPU");
+            return GS_ERR_TIMEOUT;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+gs_status check_device_error(gs_sim* s) {
+    int err = 0;
+    GS_CUDA(cudaMemcpy(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        set_error(std::string("device-side error flags ") + std::to_string(err) +
+                  " (1: radix-sort look-back wait ran out, 2: scan look-back wait ran out, 4: tree capacity)");
+        return GS_ERR_DEVICE;
+    }
+    return GS_OK;
+}
+
+void free_sim(gs_sim* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (int p = 0; p < 2; ++p)
+        if (s->graph[p]) cudaGraphExecDestroy(s->graph[p]);
+    bh_free(s);
+    direct_free(s);
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(s->pos[b]);
+        cudaFree(s->vel[b]);
+    }
+    cudaFree(s->mass[0]);
+    cudaFree(s->acc);
+    cudaFree(s->d_err);
+    for (auto& e : s->ev)
+        if (e) cudaEventDestroy(e);
+    if (s->batch_done) cudaEventDestroy(s->batch_done);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+// upload N host particles into the input set (one host->device copy per array), pad
+// with zero particles, and copy device-side into the other set: both sets start equal,
+// as the reference's staging upload fills all buffer sets (ParticleSystem.cpp:206-217)
+gs_status upload(gs_sim* s, const float* pos, const float* vel, const float* mass) {
+    const size_t n = s->n, pad = s->n_al - s->n;
+    const int a = s->in, b = a ^ 1;
+    GS_CUDA(cudaMemcpyAsync(s->pos[a], pos, n * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+    if (vel) GS_CUDA(cudaMemcpyAsync(s->vel[a], vel, n * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+    else GS_CUDA(cudaMemsetAsync(s->vel[a], 0, n * sizeof(float2), s->stream));
+    if (pad) {
+        GS_CUDA(cudaMemsetAsync(s->pos[a] + n, 0, pad * sizeof(float2), s->stream));
+        GS_CUDA(cudaMemsetAsync(s->vel[a] + n, 0, pad * sizeof(float2), s->stream));
+    }
+    GS_CUDA(cudaMemcpyAsync(s->pos[b], s->pos[a], s->n_al * sizeof(float2), cudaMemcpyDeviceToDevice, s->stream));
+    GS_CUDA(cudaMemcpyAsync(s->vel[b], s->vel[a], s->n_al * sizeof(float2), cudaMemcpyDeviceToDevice, s->stream));
+    GS_CUDA(cudaMemcpyAsync(s->mass[0], mass, n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (pad) GS_CUDA(cudaMemsetAsync(s->mass[0] + n, 0, pad * sizeof(float), s->stream));
+    GS_CUDA(cudaStreamSynchronize(s->stream));
+    return GS_OK;
+}
+
+cudaError_t enqueue_step(gs_sim* s, int in, bool profile) {
+    const int out = in ^ 1;
+    if (s->p.algorithm == GS_BARNES_HUT) return bh_step(s, in, out, profile);
+    return direct_step(s, in, out, profile);
+}
+
+gs_status account_profile(gs_sim* s) {
+    s->profile_pending = false;
+    for (int st = 0; st < GS_STAGE_COUNT; ++st) {
+        if (!(s->stage_ran & (1u << st))) continue;
+        GS_CUDA(cudaEventSynchronize(s->ev[2 * st + 1]));
+        float ms = 0.f;
+        GS_CUDA(cudaEventElapsedTime(&ms, s->ev[2 * st], s->ev[2 * st + 1]));
+        s->stats.stage_ms[st] += ms;
+        s->stats.stage_launches[st] += 1;
+    }
+    return GS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gs_params_init(gs_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->gravitational_const = 1.0f;  // src/Main.cpp:59-63
+    p->simulation_time = 0.001f;
+    p->simulation_speed = 1.0f;
+    p->softening_len = 0.2f;
+    p->accuracy_parameter = 1.0f;
+    p->algorithm = GS_DIRECT_SUM;
+    p->box_mode = GS_BOX_FIXED_500;
+    p->math_mode = GS_MATH_FAST;
+    p->device = 0;
+    p->flags = 0;
+}
+
+const char* gs_status_string(gs_status s) {
+    switch (s) {
+        case GS_OK: return "ok";
+        case GS_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case GS_ERR_CUDA: return "CUDA error";
+        case GS_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case GS_ERR_TIMEOUT: return "timeout";
+        case GS_ERR_DEVICE: return "device-side error";
+        case GS_ERR_IO: return "I/O error";
+        case GS_ERR_CAPACITY: return "capacity exceeded";
+        case GS_ERR_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* gs_last_error(void) { return g_last_error.c_str(); }
+
+uint64_t gs_required_alignment(int32_t algorithm) {
+    (void)algorithm;  // both simulations align to 64 (DirectSimulation.cpp:26-28, BarnesHutSimulation.cpp:834-836)
+    return kAlignment;
+}
+
+uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count) { return bh_capacity(box_mode, aligned_count); }
+
+gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const float* vel, const float* mass,
+                    gs_sim** out) {
+    if (!out) return invalid("gs_create: out is NULL");
+    *out = nullptr;
+    if (!params) return invalid("gs_create: params is NULL");
+    if (!n) return invalid("The simulation must contain at least one particle!");
+    if (!pos || !mass) return invalid("gs_create: pos_xy and mass are required");
+    if (params->algorithm != GS_DIRECT_SUM && params->algorithm != GS_BARNES_HUT)
+        return invalid("Invalid simulation algorithm requested!");
+    if (params->box_mode != GS_BOX_FIXED_500 && params->box_mode != GS_BOX_BOUNDING)
+        return invalid("gs_create: invalid box_mode");
+    if (params->math_mode != GS_MATH_FAST && params->math_mode != GS_MATH_REFERENCE)
+        return invalid("gs_create: invalid math_mode");
+    if (n > kMaxParticles) {
+        set_error("gs_create: particle count above the 2^28 limit of this build");
+        return GS_ERR_CAPACITY;
+    }
+    int ndev = 0;
+    cudaError_t ce = cudaGetDeviceCount(&ndev);
+    if (ce != cudaSuccess || ndev == 0) {
+        set_error("no CUDA device available");
+        return GS_ERR_NO_DEVICE;
+    }
+    if (params->device < 0 || params->device >= ndev) return invalid("gs_create: device ordinal out of range");
+
+    gs_sim* s = new (std::nothrow) gs_sim();
+    if (!s) return invalid("gs_create: host allocation failed");
+    s->p = *params;
+    s->device = params->device;
+    s->n = n;
+    s->n_al = (n + kAlignment - 1) / kAlignment * kAlignment;  // ParticleSystem.cpp:487
+    // Specialization constants of the reference (DirectSimulation.cpp:175-181, BarnesHutSimulation.cpp:571-582)
+    s->G = params->gravitational_const;
+    s->eps2 = params->softening_len * params->softening_len;
+    s->theta2 = params->accuracy_parameter * params->accuracy_parameter;
+    s->dt_eff = params->algorithm == GS_BARNES_HUT ? params->simulation_time * params->simulation_speed
+                                                   : params->simulation_time;  // direct sum ignores speed
+
+    gs_status st = GS_OK;
+#define GS_TRY(call)                                   \
+    do {                                               \
+        cudaError_t _e = (call);                       \
+        if (_e != cudaSuccess) {                       \
+            st = cuda_fail(_e, #call);                 \
+            free_sim(s);                               \
+            return st;                                 \
+        }                                              \
+    } while (0)
+    GS_TRY(cudaSetDevice(s->device));
+    GS_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    GS_TRY(cudaEventCreateWithFlags(&s->batch_done, cudaEventDisableTiming));
+    for (auto& e : s->ev) GS_TRY(cudaEventCreate(&e));
+    for (int b = 0; b < 2; ++b) {
+        GS_TRY(cudaMalloc(&s->pos[b], s->n_al * sizeof(float2)));
+        GS_TRY(cudaMalloc(&s->vel[b], s->n_al * sizeof(float2)));
+    }
+    GS_TRY(cudaMalloc(&s->mass[0], s->n_al * sizeof(float)));
+    s->mass[1] = s->mass[0];  // no step writes mass except removal, which writes both sets alike
+    GS_TRY(cudaMalloc(&s->d_err, sizeof(int)));
+    GS_TRY(cudaMemset(s->d_err, 0, sizeof(int)));
+    if (params->flags & GS_FLAG_RECORD_ACCEL) {
+        GS_TRY(cudaMalloc(&s->acc, s->n_al * sizeof(float2)));
+        GS_TRY(cudaMemset(s->acc, 0, s->n_al * sizeof(float2)));
+    }
+    if (params->algorithm == GS_BARNES_HUT) GS_TRY(bh_alloc(s));
+    else GS_TRY(direct_alloc(s));
+#undef GS_TRY
+    st = upload(s, pos, vel, mass);
+    if (st != GS_OK) {
+        free_sim(s);
+        return st;
+    }
+    *out = s;
+    return GS_OK;
+}
+
+gs_status gs_run(gs_sim* s, uint32_t count) {
+    if (!s) return invalid("gs_run: sim is NULL");
+    GS_CUDA(cudaSetDevice(s->device));
+    if (s->batch_pending) {  // wait for the previous submit, like the reference's fence wait
+        gs_status w = wait_event(s->batch_done, 0);
+        if (w != GS_OK) return w;
+        s->batch_pending = false;
+    }
+    if (!count) return GS_OK;
+    const bool profile = (s->p.flags & GS_FLAG_PROFILE) != 0;
+    const bool graphs = !(s->p.flags & GS_FLAG_NO_GRAPH);
+    for (uint32_t c = 0; c < count; ++c) {
+        const int in = s->in;
+        if (s->profile_pending) {  // the previous step's stage events are about to be re-recorded
+            gs_status a = account_profile(s);
+            if (a != GS_OK) return a;
+        }
+        s->stage_ran = 0;
+        if (graphs) {
+            if (!s->graph[in]) {
+                cudaGraph_t g = nullptr;
+                s->launches_in_step = 0;
+                s->capturing = true;
+                GS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+                cudaError_t e = enqueue_step(s, in, profile);
+                cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+                s->capturing = false;
+                if (e != cudaSuccess) {
+                    if (g) cudaGraphDestroy(g);
+                    return cuda_fail(e, "step capture");
+                }
+                GS_CUDA(e2);
+                e = cudaGraphInstantiate(&s->graph[in], g, 0);
+                cudaGraphDestroy(g);
+                GS_CUDA(e);
+                s->launches_per_step[in] = s->launches_in_step;
+                s->graph_stages[in] = s->stage_ran;
+            }
+            s->stage_ran = s->graph_stages[in];
+            GS_CUDA(cudaGraphLaunch(s->graph[in], s->stream));
+            s->kernel_launches += s->launches_per_step[in];
+        } else {
+            s->launches_in_step = 0;
+            GS_CUDA(enqueue_step(s, in, profile));
+            s->kernel_launches += s->launches_in_step;
+        }
+        if (profile) s->profile_pending = true;  // read back before the next step records again
+        s->in ^= 1;  // NextComputeIndices
+        ++s->steps_done;
+    }
+    GS_CUDA(cudaEventRecord(s->batch_done, s->stream));
+    s->batch_pending = true;
+    return GS_OK;
+}
+
+gs_status gs_sync(gs_sim* s, uint64_t timeout_ns) {
+    if (!s) return invalid("gs_sync: sim is NULL");
+    GS_CUDA(cudaSetDevice(s->device));
+    if (s->batch_pending) {
+        gs_status w = wait_event(s->batch_done, timeout_ns);
+        if (w != GS_OK) return w;
+        s->batch_pending = false;
+    }
+    GS_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->profile_pending) {
+        gs_status a = account_profile(s);
+        if (a != GS_OK) return a;
+    }
+    return check_device_error(s);
+}
+
+gs_status gs_get_particles(gs_sim* s, float* pos, float* vel, float* mass) {
+    gs_status st = gs_sync(s, 0);
+    if (st != GS_OK) return st;
+    const int in = s->in;  // ParticleSystem::GetParticles reads buffers[computeInputIndex]
+    if (pos) GS_CUDA(cudaMemcpy(pos, s->pos[in], s->n * sizeof(float2), cudaMemcpyDeviceToHost));
+    if (vel) GS_CUDA(cudaMemcpy(vel, s->vel[in], s->n * sizeof(float2), cudaMemcpyDeviceToHost));
+    if (mass) GS_CUDA(cudaMemcpy(mass, s->mass[in], s->n * sizeof(float), cudaMemcpyDeviceToHost));
+    return GS_OK;
+}
+
+gs_status gs_set_particles(gs_sim* s, const float* pos, const float* vel, const float* mass) {
+    if (!pos || !mass) return invalid("gs_set_particles: pos_xy and mass are required");
+    gs_status st = gs_sync(s, 0);
+    if (st != GS_OK) return st;
+    return upload(s, pos, vel, mass);
+}
+
+gs_status gs_get_accel(gs_sim* s, float* acc) {
+    if (!s || !acc) return invalid("gs_get_accel: NULL argument");
+    if (!s->acc) return invalid("gs_get_accel: create the simulation with GS_FLAG_RECORD_ACCEL");
+    gs_status st = gs_sync(s, 0);
+    if (st != GS_OK) return st;
+    GS_CUDA(cudaMemcpy(acc, s->acc, s->n * sizeof(float2), cudaMemcpyDeviceToHost));
+    return GS_OK;
+}
+
+gs_status gs_get_stats(gs_sim* s, gs_stats* out) {
+    if (!s || !out) return invalid("gs_get_stats: NULL argument");
+    gs_status st = gs_sync(s, 0);
+    if (st != GS_OK) return st;
+    *out = s->stats;
+    out->steps_done = s->steps_done;
+    out->kernel_launches = s->kernel_launches;
+    if (s->p.algorithm == GS_BARNES_HUT && s->steps_done) {
+        uint64_t nv, internal, inter, vis;
+        st = bh_read_counts(s, &nv, &internal, &inter, &vis);
+        if (st != GS_OK) return st;
+        out->placed_particles = nv;
+        out->internal_nodes = internal;
+        out->tree_records = nv + internal;
+        out->interactions = inter;
+        out->warp_visits = vis;
+    }
+    return GS_OK;
+}
+
+gs_status gs_reset_stats(gs_sim* s) {
+    if (!s) return invalid("gs_reset_stats: sim is NULL");
+    std::memset(&s->stats, 0, sizeof s->stats);
+    return GS_OK;
+}
+
+uint64_t gs_particle_count(const gs_sim* s) { return s ? s->n : 0; }
+uint64_t gs_aligned_particle_count(const gs_sim* s) { return s ? s->n_al : 0; }
+void* gs_stream(gs_sim* s) { return s ? (void*)s->stream : nullptr; }
+
+void gs_destroy(gs_sim* s) { free_sim(s); }
+
+gs_status gs_accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* targets, double* acc) {
+    if (!s || !targets || !acc) return invalid("gs_accel_f64: NULL argument");
+    if (!n_targets) return GS_OK;
+    for (uint32_t t = 0; t < n_targets; ++t)
+        if (targets[t] >= s->n) return invalid("gs_accel_f64: target index out of range");
+    gs_status st = gs_sync(s, 0);
+    if (st != GS_OK) return st;
+    uint32_t* dt = nullptr;
+    double2* dout = nullptr;
+    GS_CUDA(cudaMalloc(&dt, n_targets * sizeof(uint32_t)));
+    cudaError_t e = cudaMalloc(&dout, n_targets * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMemcpy(dt, targets, n_targets * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = accel_f64(s, n_targets, dt, dout);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(acc, dout, n_targets * sizeof(double2), cudaMemcpyDeviceToHost);
+    cudaFree(dt);
+    cudaFree(dout);
+    GS_CUDA(e);
+    return GS_OK;
+}
+
+gs_status gs_debug_bh_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
+                           float* node_pos, float* node_mass, uint64_t capacity, uint64_t* tree_records) {
+    if (!s) return invalid("gs_debug_bh_tree: sim is NULL");
+    if (s->p.algorithm != GS_BARNES_HUT) return invalid("gs_debug_bh_tree: not a Barnes-Hut simulation");
+    gs_status st = gs_sync(s, 0);
+    if (st != GS_OK) return st;
+    return bh_debug_tree(s, keys, sorted_src, node_skip, node_radius, node_pos, node_mass, capacity, tree_records);
+}
+
+}  // extern "C"

@@ -1,0 +1,260 @@
+"""ctypes binding of libgsim.so (include/gsim.h) -- the binding a Python caller of the
+C ABI would add.  Arrays are numpy float32 (x, y interleaved as shape (N, 2)).
+
+There is no fallback: if libgsim.so is missing or fails to load, every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libgsim.so")
+
+OK = 0
+DIRECT_SUM, BARNES_HUT = 0, 1
+BOX_FIXED_500, BOX_BOUNDING = 0, 1
+MATH_FAST, MATH_REFERENCE = 0, 1
+FLAG_RECORD_ACCEL, FLAG_PROFILE, FLAG_NO_GRAPH, FLAG_COUNT_INTERACTIONS = 0x1, 0x2, 0x4, 0x8
+GEN_RANDOM, GEN_GALAXY, GEN_GALAXY_COLLISION, GEN_SYMMETRICAL_GALAXY_COLLISION = 0, 1, 2, 3
+GEN_UNIFORM_DISK, GEN_SPIRAL, GEN_EXP_DISK_COLLISION = 16, 17, 18
+STAGES = ("bbox", "keys", "sort", "scan", "records", "sums", "force", "direct")
+
+EXPORTS = (
+    "gs_params_init", "gs_status_string", "gs_last_error", "gs_required_alignment", "gs_create", "gs_run",
+    "gs_sync", "gs_get_particles", "gs_set_particles", "gs_get_accel", "gs_get_stats", "gs_reset_stats",
+    "gs_particle_count", "gs_aligned_particle_count", "gs_stream", "gs_destroy", "gs_accel_f64",
+    "gs_debug_bh_tree", "gs_bh_node_capacity", "gs_generate", "gs_read_particles", "gs_write_particles",
+)
+
+
+class Params(C.Structure):
+    _fields_ = [("gravitational_const", C.c_float), ("simulation_time", C.c_float),
+                ("simulation_speed", C.c_float), ("softening_len", C.c_float),
+                ("accuracy_parameter", C.c_float), ("algorithm", C.c_int32), ("box_mode", C.c_int32),
+                ("math_mode", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("steps_done", C.c_uint64), ("tree_records", C.c_uint64), ("internal_nodes", C.c_uint64),
+                ("placed_particles", C.c_uint64), ("interactions", C.c_uint64), ("warp_visits", C.c_uint64),
+                ("kernel_launches", C.c_uint64),
+                ("stage_ms", C.c_float * 8), ("stage_launches", C.c_uint32 * 8)]
+
+
+class GsimError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+_lib = None
+_FP = C.POINTER(C.c_float)
+_UP = C.POINTER(C.c_uint32)
+_DP = C.POINTER(C.c_double)
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise GsimError(-1, f"libgsim.so not built at {LIB_PATH}; run the package build first")
+    L = C.CDLL(LIB_PATH)
+    st = C.c_int
+    sim = C.c_void_p
+    L.gs_params_init.argtypes = [C.POINTER(Params)]
+    L.gs_params_init.restype = None
+    L.gs_status_string.argtypes = [st]
+    L.gs_status_string.restype = C.c_char_p
+    L.gs_last_error.argtypes = []
+    L.gs_last_error.restype = C.c_char_p
+    L.gs_required_alignment.argtypes = [C.c_int32]
+    L.gs_required_alignment.restype = C.c_uint64
+    L.gs_create.argtypes = [C.POINTER(Params), C.c_uint64, _FP, _FP, _FP, C.POINTER(sim)]
+    L.gs_create.restype = st
+    L.gs_run.argtypes = [sim, C.c_uint32]
+    L.gs_run.restype = st
+    L.gs_sync.argtypes = [sim, C.c_uint64]
+    L.gs_sync.restype = st
+    L.gs_get_particles.argtypes = [sim, _FP, _FP, _FP]
+    L.gs_get_particles.restype = st
+    L.gs_set_particles.argtypes = [sim, _FP, _FP, _FP]
+    L.gs_set_particles.restype = st
+    L.gs_get_accel.argtypes = [sim, _FP]
+    L.gs_get_accel.restype = st
+    L.gs_get_stats.argtypes = [sim, C.POINTER(Stats)]
+    L.gs_get_stats.restype = st
+    L.gs_reset_stats.argtypes = [sim]
+    L.gs_reset_stats.restype = st
+    L.gs_particle_count.argtypes = [sim]
+    L.gs_particle_count.restype = C.c_uint64
+    L.gs_aligned_particle_count.argtypes = [sim]
+    L.gs_aligned_particle_count.restype = C.c_uint64
+    L.gs_stream.argtypes = [sim]
+    L.gs_stream.restype = C.c_void_p
+    L.gs_destroy.argtypes = [sim]
+    L.gs_destroy.restype = None
+    L.gs_accel_f64.argtypes = [sim, C.c_uint32, _UP, _DP]
+    L.gs_accel_f64.restype = st
+    L.gs_debug_bh_tree.argtypes = [sim, _UP, _UP, _UP, _FP, _FP, _FP, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.gs_debug_bh_tree.restype = st
+    L.gs_bh_node_capacity.argtypes = [C.c_int32, C.c_uint64]
+    L.gs_bh_node_capacity.restype = C.c_uint64
+    L.gs_generate.argtypes = [C.c_int32, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_uint64,
+                              _FP, _FP, _FP]
+    L.gs_generate.restype = st
+    L.gs_read_particles.argtypes = [C.c_char_p, C.c_uint64, C.POINTER(C.c_uint64), _FP, _FP, _FP]
+    L.gs_read_particles.restype = st
+    L.gs_write_particles.argtypes = [C.c_char_p, C.c_uint64, _FP, _FP, _FP]
+    L.gs_write_particles.restype = st
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != OK:
+        L = lib()
+        raise GsimError(status, L.gs_last_error().decode() or L.gs_status_string(status).decode())
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(_FP)
+
+
+def _f32(a, shape):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a.reshape(shape)
+
+
+def default_params(**kw):
+    p = Params()
+    lib().gs_params_init(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def generate(kind, n, size=100.0, min_mass=1.0, max_mass=10.0, G=1.0, seed=1):
+    pos = np.empty((n, 2), np.float32)
+    vel = np.empty((n, 2), np.float32)
+    mass = np.empty(n, np.float32)
+    _check(lib().gs_generate(kind, n, size, min_mass, max_mass, G, seed, _fp(pos), _fp(vel), _fp(mass)))
+    return pos, vel, mass
+
+
+def read_particles(path):
+    cnt = C.c_uint64(0)
+    L = lib()
+    _check(L.gs_read_particles(path.encode(), 0, C.byref(cnt), None, None, None))
+    n = cnt.value
+    pos = np.empty((n, 2), np.float32)
+    vel = np.empty((n, 2), np.float32)
+    mass = np.empty(n, np.float32)
+    _check(L.gs_read_particles(path.encode(), n, C.byref(cnt), _fp(pos), _fp(vel), _fp(mass)))
+    return pos, vel, mass
+
+
+def write_particles(path, pos, vel, mass):
+    n = len(mass)
+    pos, vel, mass = _f32(pos, (n, 2)), _f32(vel, (n, 2)), _f32(mass, (n,))
+    _check(lib().gs_write_particles(path.encode(), n, _fp(pos), _fp(vel), _fp(mass)))
+
+
+def required_alignment(algorithm=DIRECT_SUM):
+    return int(lib().gs_required_alignment(algorithm))
+
+
+def node_capacity(box_mode, n_al):
+    return int(lib().gs_bh_node_capacity(box_mode, n_al))
+
+
+class Simulation:
+    """One simulated system resident on the GPU (gs_sim)."""
+
+    def __init__(self, pos, vel, mass, params=None, **kw):
+        self._h = C.c_void_p()
+        self.params = params if params is not None else default_params(**kw)
+        n = len(mass)
+        self.n = n
+        pos, vel, mass = _f32(pos, (n, 2)), _f32(vel, (n, 2)), _f32(mass, (n,))
+        _check(lib().gs_create(C.byref(self.params), n, _fp(pos), _fp(vel), _fp(mass), C.byref(self._h)))
+        self.n_al = int(lib().gs_aligned_particle_count(self._h))
+
+    def close(self):
+        if self._h:
+            lib().gs_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def run(self, count=1):
+        _check(lib().gs_run(self._h, count))
+
+    def sync(self, timeout_ns=0):
+        _check(lib().gs_sync(self._h, timeout_ns))
+
+    def get_particles(self):
+        pos = np.empty((self.n, 2), np.float32)
+        vel = np.empty((self.n, 2), np.float32)
+        mass = np.empty(self.n, np.float32)
+        _check(lib().gs_get_particles(self._h, _fp(pos), _fp(vel), _fp(mass)))
+        return pos, vel, mass
+
+    def set_particles(self, pos, vel, mass):
+        n = self.n
+        pos, vel, mass = _f32(pos, (n, 2)), _f32(vel, (n, 2)), _f32(mass, (n,))
+        _check(lib().gs_set_particles(self._h, _fp(pos), _fp(vel), _fp(mass)))
+
+    def get_accel(self):
+        acc = np.empty((self.n, 2), np.float32)
+        _check(lib().gs_get_accel(self._h, _fp(acc)))
+        return acc
+
+    def stats(self):
+        s = Stats()
+        _check(lib().gs_get_stats(self._h, C.byref(s)))
+        return s
+
+    def reset_stats(self):
+        _check(lib().gs_reset_stats(self._h))
+
+    def stream(self):
+        return lib().gs_stream(self._h)
+
+    def accel_f64(self, targets):
+        t = np.ascontiguousarray(targets, dtype=np.uint32)
+        out = np.empty((len(t), 2), np.float64)
+        _check(lib().gs_accel_f64(self._h, len(t), t.ctypes.data_as(_UP), out.ctypes.data_as(_DP)))
+        return out
+
+    def bh_tree(self):
+        n_al = self.n_al
+        cap = node_capacity(self.params.box_mode, n_al)
+        keys = np.empty(n_al, np.uint32)
+        src = np.empty(n_al, np.uint32)
+        skip = np.empty(cap, np.uint32)
+        radius = np.empty(cap, np.float32)
+        npos = np.empty((cap, 2), np.float32)
+        nmass = np.empty(cap, np.float32)
+        T = C.c_uint64(0)
+        _check(lib().gs_debug_bh_tree(self._h, keys.ctypes.data_as(_UP), src.ctypes.data_as(_UP),
+                                      skip.ctypes.data_as(_UP), _fp(radius), _fp(npos), _fp(nmass), cap,
+                                      C.byref(T)))
+        t = T.value
+        return dict(keys=keys, sorted_src=src, skip=skip[:t], radius=radius[:t], pos=npos[:t], mass=nmass[:t],
+                    tree_size=t)

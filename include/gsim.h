@@ -1,0 +1,173 @@
+/*
+ * gsim.h -- C ABI of the GB300 force-and-integrate path for Gravity-Sim.
+ *
+ * One gs_sim replaces one reference simulation object plus the particle buffers it
+ * drives (paths relative to the reference project):
+ *   gs_create      ParticleSystem(...) ctor (src/Particles/ParticleSystem.hpp:58,72) followed by
+ *                  DirectSimulation(device, system) (src/Simulation/Direct/DirectSimulation.hpp:11-81)
+ *                  or BarnesHutSimulation(device, system) (src/Simulation/BarnesHut/BarnesHutSimulation.hpp:11-110)
+ *   gs_run         RunSimulations(uint32_t) (src/Simulation/Direct/DirectSimulation.cpp:271,
+ *                  src/Simulation/BarnesHut/BarnesHutSimulation.cpp:849)
+ *   gs_sync        the simulation fence wait of the destructor and vkDeviceWaitIdle (src/Main.cpp:286)
+ *   gs_get_particles  ParticleSystem::GetParticles (src/Particles/ParticleSystem.hpp:178)
+ *   gs_destroy     ~DirectSimulation / ~BarnesHutSimulation + ~ParticleSystem
+ *   gs_required_alignment  GetRequiredParticleAlignment() (src/Simulation/Direct/DirectSimulation.cpp:26-28,
+ *                  src/Simulation/BarnesHut/BarnesHutSimulation.cpp:834-836)
+ *   gs_read_particles / gs_write_particles  ParticleSystem file ctor and SaveParticles
+ *                  (src/Particles/ParticleSystem.cpp:438-501, 727-750)
+ *   gs_generate    the four generators (src/Particles/ParticleSystem.cpp:15-149), seeded
+ *
+ * Conventions: every call returns a gs_status; nothing throws across the ABI.  Host
+ * arrays are caller-owned, interleaved x,y for vectors, and hold the first N particles
+ * (the library pads to the required alignment with zero particles, like the reference,
+ * src/Particles/ParticleSystem.cpp:487-491).  Device state is library-owned and stays
+ * resident between calls.  Every gs_sim owns one CUDA stream; gs_run is asynchronous.
+ */
+#ifndef GSIM_H
+#define GSIM_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GS_API __attribute__((visibility("default")))
+#else
+#define GS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gs_status {
+    GS_OK = 0,
+    GS_ERR_INVALID_ARGUMENT = 1,
+    GS_ERR_CUDA = 2,
+    GS_ERR_OUT_OF_MEMORY = 3,
+    GS_ERR_TIMEOUT = 4,
+    GS_ERR_DEVICE = 5,   /* a kernel reported an error (e.g. a bounded wait ran out) */
+    GS_ERR_IO = 6,
+    GS_ERR_CAPACITY = 7, /* a size limit of this build was exceeded */
+    GS_ERR_NO_DEVICE = 8
+} gs_status;
+
+/* ParticleSystem::SimulationAlgorithm (src/Particles/ParticleSystem.hpp:27-34). */
+typedef enum gs_algorithm { GS_DIRECT_SUM = 0, GS_BARNES_HUT = 1 } gs_algorithm;
+
+/* Barnes-Hut box: the reference's fixed +-500 box with a 1024x1024 finest grid and
+ * removal of particles that leave it, or a per-step square bounding box with
+ * 2^15 x 2^15 finest cells (30-bit keys) and no removal. */
+typedef enum gs_box_mode { GS_BOX_FIXED_500 = 0, GS_BOX_BOUNDING = 1 } gs_box_mode;
+
+/* FAST: hardware rsqrt; direct sum in shared-memory tiles with Kahan-compensated
+ * tile partials.  REFERENCE: correctly rounded 1/sqrt and the shaders' summation
+ * order, bit-identical to the CPU restatement. */
+typedef enum gs_math_mode { GS_MATH_FAST = 0, GS_MATH_REFERENCE = 1 } gs_math_mode;
+
+/* gs_params.flags */
+#define GS_FLAG_RECORD_ACCEL 0x1u  /* keep the last step's accelerations (gs_get_accel) */
+#define GS_FLAG_PROFILE 0x2u       /* time each stage with CUDA events (gs_get_stats) */
+#define GS_FLAG_NO_GRAPH 0x4u      /* launch kernels one by one instead of a CUDA graph */
+#define GS_FLAG_COUNT_INTERACTIONS 0x8u /* count accepted Barnes-Hut interactions */
+
+typedef struct gs_params {
+    float gravitational_const; /* ParticleSystem::GetGravitationalConst, default 1 (src/Main.cpp:59) */
+    float simulation_time;     /* GetSimulationTime, default 1e-3 */
+    float simulation_speed;    /* GetSimulationSpeed, default 1 (Barnes-Hut only, as in the reference) */
+    float softening_len;       /* GetSofteningLen, default 0.2 */
+    float accuracy_parameter;  /* GetAccuracyParameter (theta), default 1 */
+    int32_t algorithm;         /* gs_algorithm */
+    int32_t box_mode;          /* gs_box_mode, Barnes-Hut only */
+    int32_t math_mode;         /* gs_math_mode */
+    int32_t device;            /* CUDA device ordinal */
+    uint32_t flags;            /* GS_FLAG_* */
+} gs_params;
+
+typedef struct gs_sim gs_sim;
+
+/* Statistics: stage times accumulate over steps since gs_reset_stats (GS_FLAG_PROFILE);
+ * tree counts are those of the most recent step. */
+#define GS_STAGE_COUNT 8
+typedef struct gs_stats {
+    uint64_t steps_done;
+    uint64_t tree_records;     /* Barnes-Hut preorder records (internal nodes + leaves) */
+    uint64_t internal_nodes;
+    uint64_t placed_particles; /* particles inside the box */
+    uint64_t interactions;     /* accepted (particle, record) pairs, GS_FLAG_COUNT_INTERACTIONS */
+    uint64_t warp_visits;      /* records visited summed over warps, GS_FLAG_COUNT_INTERACTIONS */
+    uint64_t kernel_launches;  /* CUDA kernels this simulation launched since creation */
+    float stage_ms[GS_STAGE_COUNT]; /* bbox, keys, sort, scan, records, sums, force, direct */
+    uint32_t stage_launches[GS_STAGE_COUNT];
+} gs_stats;
+
+GS_API void gs_params_init(gs_params* p);
+GS_API const char* gs_status_string(gs_status s);
+/* Message of the last failure on the calling thread ("" if none). */
+GS_API const char* gs_last_error(void);
+
+GS_API uint64_t gs_required_alignment(int32_t algorithm);
+
+GS_API gs_status gs_create(const gs_params* params, uint64_t particle_count, const float* pos_xy,
+                    const float* vel_xy, const float* mass, gs_sim** out);
+/* Enqueue `count` steps.  Like RunSimulations it first waits for the previous gs_run
+ * batch to finish (bounded: GS_ERR_TIMEOUT after 600 s), then submits and returns. */
+GS_API gs_status gs_run(gs_sim* sim, uint32_t count);
+/* Wait for all submitted steps; timeout_ns = 0 waits up to 600 s. */
+GS_API gs_status gs_sync(gs_sim* sim, uint64_t timeout_ns);
+/* Copy the current state (first N particles) to host arrays; any may be NULL. */
+GS_API gs_status gs_get_particles(gs_sim* sim, float* pos_xy, float* vel_xy, float* mass);
+/* Replace the whole state (first N particles; padding reset to zero particles). */
+GS_API gs_status gs_set_particles(gs_sim* sim, const float* pos_xy, const float* vel_xy,
+                           const float* mass);
+/* Accelerations (without G) of the last step, in particle order; needs GS_FLAG_RECORD_ACCEL. */
+GS_API gs_status gs_get_accel(gs_sim* sim, float* acc_xy);
+/* Accumulated per-stage times (GS_FLAG_PROFILE) and tree counts of the last step. */
+GS_API gs_status gs_get_stats(gs_sim* sim, gs_stats* stats);
+GS_API gs_status gs_reset_stats(gs_sim* sim);
+GS_API uint64_t gs_particle_count(const gs_sim* sim);
+GS_API uint64_t gs_aligned_particle_count(const gs_sim* sim);
+/* CUDA stream the simulation runs on (a cudaStream_t), for event timing by callers. */
+GS_API void* gs_stream(gs_sim* sim);
+GS_API void gs_destroy(gs_sim* sim);
+
+/* FP64 direct-sum accelerations (without G) of the current state on the GPU, for the
+ * listed particle indices over all particles; the error reference for every result. */
+GS_API gs_status gs_accel_f64(gs_sim* sim, uint32_t n_targets, const uint32_t* targets, double* acc_xy);
+
+/* Barnes-Hut tree of the most recent step, in the reference's layout
+ * (BarnesHutSimulation.cpp:52-142: counts, radiuses, nodePos, nodeMass, sortedSrc).
+ * keys: per particle cell key (0xFFFFFFFF for removed); sorted_src: original index per
+ * sorted slot (N_al for empty slots).  Any pointer may be NULL. */
+GS_API gs_status gs_debug_bh_tree(gs_sim* sim, uint32_t* keys, uint32_t* sorted_src,
+                           uint32_t* node_skip, float* node_radius, float* node_pos,
+                           float* node_mass, uint64_t capacity, uint64_t* tree_records);
+GS_API uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count);
+
+/* ---- host-only helpers (no GPU) ---- */
+
+/* Generator types: the reference's four presets (ParticleSystem::GenerateType) and the
+ * seeded workloads the measurements are quoted on. */
+typedef enum gs_generate_type {
+    GS_GEN_RANDOM = 0,
+    GS_GEN_GALAXY = 1,
+    GS_GEN_GALAXY_COLLISION = 2,
+    GS_GEN_SYMMETRICAL_GALAXY_COLLISION = 3,
+    GS_GEN_UNIFORM_DISK = 16,       /* r = R*sqrt(u), v = 0 */
+    GS_GEN_SPIRAL = 17,             /* exponential disk, two-arm log spiral, circular v */
+    GS_GEN_EXP_DISK_COLLISION = 18  /* two exponential disks at (+-50, 0), v = (0, +-3) */
+} gs_generate_type;
+
+GS_API gs_status gs_generate(int32_t type, uint64_t count, float generate_size, float min_mass,
+                      float max_mass, float gravitational_const, uint64_t seed, float* pos_xy,
+                      float* vel_xy, float* mass);
+/* Reads "x y vx vy m" records (fscanf %f, stops at the first incomplete record).
+ * Call with NULL arrays to get the count; then again with arrays of that size. */
+GS_API gs_status gs_read_particles(const char* path, uint64_t capacity, uint64_t* count,
+                            float* pos_xy, float* vel_xy, float* mass);
+/* Writes "%.7f %.7f %.7f %.7f %.7f\n" per particle, byte-identical to SaveParticles. */
+GS_API gs_status gs_write_particles(const char* path, uint64_t count, const float* pos_xy,
+                             const float* vel_xy, const float* mass);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,799 @@
+/*
+ * gsim_oracle.c -- CPU restatement of Gravity-Sim's per-step force-and-integrate path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker, never the product).  Compile with
+ * -ffp-contract=off: every fused multiply-add below is written out with fmaf().
+ *
+ * What each function restates (paths relative to the reference project):
+ *   orc_direct_step       src/Simulation/Direct/Shaders/SimShader.comp:37-74
+ *   orc_bh_grid_step      src/Simulation/BarnesHut/Shaders/ClearShader.comp:71-83,
+ *                         InitShader.comp:73-119, TreeInitShader.comp:58-90,
+ *                         TreeSortShader.comp:57-94, TreeMoveShader.comp:53-84,
+ *                         ParticleSortShader.comp:71-110, ForceShader.comp:78-152, in the
+ *                         dispatch order of src/Simulation/BarnesHut/BarnesHutSimulation.cpp:782-825,885-918
+ *   orc_bh_sorted_step    the same tree, built from stably sorted cell keys (the
+ *                         construction the CUDA path uses), plus the bounding-box mode.
+ *
+ * Where the reference is nondeterministic this restatement fixes one meaning:
+ *   - particles inside one finest cell are ordered by ascending original index (the
+ *     reference orders them by atomic arrival, ParticleSortShader.comp:99-103);
+ *   - a finest cell with k >= 2 particles has k + 1 records (InitShader.comp:104-106
+ *     intends this, but its two separate atomics can race);
+ *   - finest-cell mass and mass-moment sums add particles in ascending index order
+ *     (the reference uses float atomics, InitShader.comp:107-109);
+ *   - the root's preorder start is 0 (TreeSortShader.comp:72 reads a never-written slot).
+ */
+#include "gsim_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#define WARP 32
+#define SIM_SIZE 500.0f  /* BarnesHutSimulation.cpp:580 simulationSize */
+#define GRID 1024u       /* BarnesHutSimulation.cpp:582 treeSize */
+#define GRID_LEVELS 11   /* depths 0..10 */
+#define BBOX_BITS 15     /* bounding-box mode: 15 bits per axis, 30-bit keys */
+
+/* ------------------------------------------------------------------------------ */
+/* tiny parallel-for: dynamic chunks over [0, n), deterministic results because   */
+/* every item writes only its own outputs                                          */
+/* ------------------------------------------------------------------------------ */
+typedef void (*item_fn)(void* ctx, uint64_t item, int worker);
+typedef struct {
+    item_fn fn;
+    void* ctx;
+    uint64_t n;
+    uint64_t chunk;
+    atomic_uint_fast64_t next;
+    int worker;
+} pf_job;
+typedef struct {
+    pf_job* job;
+    int worker;
+} pf_arg;
+
+static void* pf_thread(void* p) {
+    pf_arg* a = (pf_arg*)p;
+    pf_job* j = a->job;
+    for (;;) {
+        uint64_t b = atomic_fetch_add(&j->next, j->chunk);
+        if (b >= j->n) break;
+        uint64_t e = b + j->chunk < j->n ? b + j->chunk : j->n;
+        for (uint64_t i = b; i < e; ++i) j->fn(j->ctx, i, a->worker);
+    }
+    return NULL;
+}
+
+static void parallel_for(int nthreads, uint64_t n, uint64_t chunk, item_fn fn, void* ctx) {
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pf_job job;
+    job.fn = fn;
+    job.ctx = ctx;
+    job.n = n;
+    job.chunk = chunk ? chunk : 1;
+    atomic_init(&job.next, 0);
+    if (nthreads == 1) {
+        pf_arg a = {&job, 0};
+        pf_thread(&a);
+        return;
+    }
+    pthread_t th[256];
+    pf_arg args[256];
+    int started = 0;
+    for (int t = 1; t < nthreads; ++t) {
+        args[t].job = &job;
+        args[t].worker = t;
+        if (pthread_create(&th[t], NULL, pf_thread, &args[t]) != 0) break;
+        started = t;
+    }
+    args[0].job = &job;
+    args[0].worker = 0;
+    pf_thread(&args[0]);
+    for (int t = 1; t <= started; ++t) pthread_join(th[t], NULL);
+}
+
+static double now_seconds(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* ------------------------------------------------------------------------------ */
+/* canonical pair arithmetic                                                       */
+/* ------------------------------------------------------------------------------ */
+static inline float pair_d2(float dx, float dy, float eps2) { return fmaf(dx, dx, fmaf(dy, dy, eps2)); }
+static inline float pair_scale(float m, float d2) {
+    float r = 1.0f / sqrtf(d2);
+    return ((m * r) * r) * r;
+}
+
+/* ------------------------------------------------------------------------------ */
+/* direct sum -- SimShader.comp:37-74                                              */
+/* ------------------------------------------------------------------------------ */
+typedef struct {
+    uint32_t n;
+    const float *pos, *vel, *mass;
+    float *pos_out, *vel_out, *acc;
+    float dt, G, eps2;
+} direct_ctx;
+
+static void direct_accel_one(const direct_ctx* c, uint32_t i, float* axo, float* ayo) {
+    const float px = c->pos[2 * i], py = c->pos[2 * i + 1];
+    float ax = 0.0f, ay = 0.0f;
+    for (uint32_t j = 0; j < c->n; ++j) { /* SimShader.comp:43-65: j ascending */
+        float dx = c->pos[2 * j] - px;
+        float dy = c->pos[2 * j + 1] - py;
+        float s = pair_scale(c->mass[j], pair_d2(dx, dy, c->eps2));
+        ax = fmaf(dx, s, ax);
+        ay = fmaf(dy, s, ay);
+    }
+    *axo = ax;
+    *ayo = ay;
+}
+
+static void direct_step_item(void* p, uint64_t i, int w) {
+    (void)w;
+    const direct_ctx* c = (const direct_ctx*)p;
+    float ax, ay;
+    direct_accel_one(c, (uint32_t)i, &ax, &ay);
+    /* SimShader.comp:68-73 */
+    const float k = c->dt * c->G;
+    const float hdt = 0.5f * c->dt;
+    float vx = c->vel[2 * i], vy = c->vel[2 * i + 1];
+    float nvx = fmaf(ax, k, vx), nvy = fmaf(ay, k, vy);
+    c->pos_out[2 * i] = fmaf(vx + nvx, hdt, c->pos[2 * i]);
+    c->pos_out[2 * i + 1] = fmaf(vy + nvy, hdt, c->pos[2 * i + 1]);
+    c->vel_out[2 * i] = nvx;
+    c->vel_out[2 * i + 1] = nvy;
+}
+
+void orc_direct_step(uint32_t n, const float* pos_in, const float* vel_in, const float* mass_in,
+                     float* pos_out, float* vel_out, float dt, float G, float eps2, int nthreads) {
+    direct_ctx c = {n, pos_in, vel_in, mass_in, pos_out, vel_out, NULL, dt, G, eps2};
+    parallel_for(nthreads, n, 16, direct_step_item, &c);
+}
+
+static void direct_accel_item(void* p, uint64_t i, int w) {
+    (void)w;
+    const direct_ctx* c = (const direct_ctx*)p;
+    direct_accel_one(c, (uint32_t)i, &c->acc[2 * i], &c->acc[2 * i + 1]);
+}
+
+void orc_direct_accel(uint32_t n, const float* pos, const float* mass, float eps2, float* acc,
+                      int nthreads) {
+    direct_ctx c = {n, pos, NULL, mass, NULL, NULL, acc, 0, 0, eps2};
+    parallel_for(nthreads, n, 16, direct_accel_item, &c);
+}
+
+typedef struct {
+    uint32_t n;
+    const float *pos, *mass;
+    double eps2;
+    const uint32_t* targets;
+    double* acc;
+} f64_ctx;
+
+static void f64_item(void* p, uint64_t t, int w) {
+    (void)w;
+    const f64_ctx* c = (const f64_ctx*)p;
+    uint32_t i = c->targets ? c->targets[t] : (uint32_t)t;
+    double px = c->pos[2 * i], py = c->pos[2 * i + 1];
+    double ax = 0.0, ay = 0.0;
+    for (uint32_t j = 0; j < c->n; ++j) {
+        double dx = (double)c->pos[2 * j] - px, dy = (double)c->pos[2 * j + 1] - py;
+        double d2 = dx * dx + dy * dy + c->eps2;
+        double s = (double)c->mass[j] / (d2 * sqrt(d2));
+        ax += dx * s;
+        ay += dy * s;
+    }
+    c->acc[2 * t] = ax;
+    c->acc[2 * t + 1] = ay;
+}
+
+void orc_direct_accel_f64(uint32_t n, const float* pos, const float* mass, double eps2,
+                          uint32_t n_targets, const uint32_t* targets, double* acc, int nthreads) {
+    f64_ctx c = {n, pos, mass, eps2, targets, acc};
+    parallel_for(nthreads, n_targets, 4, f64_item, &c);
+}
+
+typedef struct {
+    uint32_t n;
+    const float *pos, *mass;
+    double eps2;
+    double* partial; /* per i */
+} energy_ctx;
+
+static void energy_item(void* p, uint64_t i, int w) {
+    (void)w;
+    const energy_ctx* c = (const energy_ctx*)p;
+    double px = c->pos[2 * i], py = c->pos[2 * i + 1], mi = c->mass[i], e = 0.0;
+    for (uint32_t j = (uint32_t)i + 1; j < c->n; ++j) {
+        double dx = (double)c->pos[2 * j] - px, dy = (double)c->pos[2 * j + 1] - py;
+        e -= mi * (double)c->mass[j] / sqrt(dx * dx + dy * dy + c->eps2);
+    }
+    c->partial[i] = e;
+}
+
+double orc_energy_f64(uint32_t n, const float* pos, const float* vel, const float* mass,
+                      double G, double eps2) {
+    double* part = (double*)calloc(n ? n : 1, sizeof(double));
+    energy_ctx c = {n, pos, mass, eps2, part};
+    parallel_for(8, n, 64, energy_item, &c);
+    double pot = 0.0, kin = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        pot += part[i];
+        double vx = vel[2 * i], vy = vel[2 * i + 1];
+        kin += 0.5 * (double)mass[i] * (vx * vx + vy * vy);
+    }
+    free(part);
+    return kin + G * pot;
+}
+
+/* ------------------------------------------------------------------------------ */
+/* cell keys                                                                       */
+/* ------------------------------------------------------------------------------ */
+static inline uint32_t spread_bits(uint32_t v) { /* InitShader.comp:88-96 (and 15-bit use) */
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+/* InitShader.comp:80-98: returns 1 and the 20-bit key when the particle is inside. */
+static inline int fixed_box_key(float px, float py, uint32_t* key) {
+    float rx = ((px / SIM_SIZE) + 1.0f) * 0.5f;
+    float ry = ((py / SIM_SIZE) + 1.0f) * 0.5f;
+    rx = rx * (float)GRID;
+    ry = ry * (float)GRID;
+    if (rx >= 0.0f && rx < (float)GRID && ry >= 0.0f && ry < (float)GRID) {
+        *key = spread_bits((uint32_t)rx) | (spread_bits((uint32_t)ry) << 1);
+        return 1;
+    }
+    return 0;
+}
+
+typedef struct {
+    float cx, cy, scale, radius0;
+} bbox_params;
+
+/* Bounding-box mode: square box around min/max of all positions, 2^15 cells per axis. */
+static bbox_params bbox_from_minmax(double minx, double maxx, double miny, double maxy) {
+    bbox_params b;
+    double cx = 0.5 * (minx + maxx), cy = 0.5 * (miny + maxy);
+    double ext = maxx - minx > maxy - miny ? maxx - minx : maxy - miny;
+    if (!(ext > 0.0) || !isfinite(ext)) ext = 1.0;
+    if (!isfinite(cx)) cx = 0.0;
+    if (!isfinite(cy)) cy = 0.0;
+    double half = ext * 0.5 * (1.0 + 1.0 / 1024.0);
+    double scale = (double)(1u << (BBOX_BITS - 1)) / half;
+    b.cx = (float)cx;
+    b.cy = (float)cy;
+    b.scale = (float)scale;
+    double side0 = (double)(1u << BBOX_BITS) / (double)b.scale;
+    b.radius0 = (float)(side0 * side0 * 0.5);
+    return b;
+}
+
+static inline uint32_t bbox_cell(float p, float c, float scale) {
+    float t = (p - c) * scale + (float)(1u << (BBOX_BITS - 1));
+    if (!(t >= 0.0f)) return 0;
+    if (t >= (float)((1u << BBOX_BITS) - 1)) return (1u << BBOX_BITS) - 1;
+    return (uint32_t)t;
+}
+
+static inline uint32_t bbox_key(float px, float py, const bbox_params* b) {
+    return spread_bits(bbox_cell(px, b->cx, b->scale)) |
+           (spread_bits(bbox_cell(py, b->cy, b->scale)) << 1);
+}
+
+uint64_t orc_bh_node_capacity(int box_mode, uint32_t n_al) {
+    uint64_t levels = box_mode == ORC_BOX_BOUNDING ? BBOX_BITS + 1 : GRID_LEVELS;
+    return (uint64_t)n_al + levels * (uint64_t)(n_al / 2) + 64;
+}
+
+/* ------------------------------------------------------------------------------ */
+/* force walk -- ForceShader.comp:78-152                                           */
+/* ------------------------------------------------------------------------------ */
+typedef struct {
+    const uint32_t* skip;
+    const float *radius, *npos, *nmass;
+    uint64_t tree_size;
+    const uint32_t* src; /* original index per sorted slot, n_al for empty slots */
+    uint32_t n_al;
+    const float *pos_in, *vel_in, *mass_in;
+    float *pos_out, *vel_out;
+    float eps2, theta2, k, hdt;
+    uint64_t* interactions; /* per worker */
+    uint64_t* visits;       /* per worker */
+    uint32_t stride;        /* walk warps stride*item */
+} walk_ctx;
+
+static void walk_warp(void* p, uint64_t item, int worker) {
+    const walk_ctx* c = (const walk_ctx*)p;
+    const uint64_t w = item * c->stride;
+    float px[WARP], py[WARP], ax[WARP], ay[WARP], dx[WARP], dy[WARP], d2[WARP];
+    int valid[WARP];
+    int nvalid = 0;
+    for (int l = 0; l < WARP; ++l) {
+        uint32_t s = (uint32_t)w * WARP + (uint32_t)l;
+        uint32_t i = c->src[s];
+        valid[l] = i != c->n_al; /* ForceShader.comp:84-92 */
+        px[l] = valid[l] ? c->pos_in[2 * i] : 0.0f;
+        py[l] = valid[l] ? c->pos_in[2 * i + 1] : 0.0f;
+        ax[l] = ay[l] = 0.0f;
+        nvalid += valid[l];
+    }
+    if (!nvalid) return;
+    uint64_t ind = 0, inter = 0, visits = 0;
+    while (ind < c->tree_size) { /* ForceShader.comp:111 */
+        const float nx = c->npos[2 * ind], ny = c->npos[2 * ind + 1];
+        const float nr = c->radius[ind], nm = c->nmass[ind];
+        int all = 1;
+        for (int l = 0; l < WARP; ++l) {
+            if (!valid[l]) continue; /* empty lanes vote yes */
+            dx[l] = nx - px[l];
+            dy[l] = ny - py[l];
+            d2[l] = pair_d2(dx[l], dy[l], c->eps2);
+            if (!(nr <= d2[l] * c->theta2)) all = 0; /* ForceShader.comp:131 */
+        }
+        ++visits;
+        if (all) {
+            for (int l = 0; l < WARP; ++l) {
+                if (!valid[l]) continue;
+                float s = pair_scale(nm, d2[l]);
+                ax[l] = fmaf(dx[l], s, ax[l]);
+                ay[l] = fmaf(dy[l], s, ay[l]);
+            }
+            inter += (uint64_t)nvalid;
+            ind += c->skip[ind];
+        } else {
+            ++ind;
+        }
+    }
+    for (int l = 0; l < WARP; ++l) { /* ForceShader.comp:143-151 */
+        if (!valid[l]) continue;
+        uint32_t i = c->src[(uint32_t)w * WARP + (uint32_t)l];
+        float vx = c->vel_in[2 * i], vy = c->vel_in[2 * i + 1];
+        float nvx = fmaf(ax[l], c->k, vx), nvy = fmaf(ay[l], c->k, vy);
+        c->pos_out[2 * i] = fmaf(vx + nvx, c->hdt, px[l]);
+        c->pos_out[2 * i + 1] = fmaf(vy + nvy, c->hdt, py[l]);
+        c->vel_out[2 * i] = nvx;
+        c->vel_out[2 * i + 1] = nvy;
+    }
+    c->interactions[worker] += inter;
+    c->visits[worker] += visits;
+}
+
+static void run_walk(walk_ctx* c, int nthreads, orc_bh_out* out) {
+    uint64_t inter[256] = {0}, vis[256] = {0};
+    c->interactions = inter;
+    c->visits = vis;
+    c->stride = out && out->walk_stride > 1 ? out->walk_stride : 1;
+    uint64_t warps = c->n_al / WARP;
+    double t0 = now_seconds();
+    parallel_for(nthreads, (warps + c->stride - 1) / c->stride, 4, walk_warp, c);
+    if (out) out->walk_seconds = now_seconds() - t0;
+    if (out) {
+        out->interactions = 0;
+        out->warp_visits = 0;
+        for (int t = 0; t < 256; ++t) {
+            out->interactions += inter[t];
+            out->warp_visits += vis[t];
+        }
+    }
+}
+
+static void copy_tree_out(orc_bh_out* out, const uint32_t* skip, const float* radius,
+                          const float* npos, const float* nmass, uint64_t tree_size) {
+    if (!out) return;
+    uint64_t n = tree_size < out->node_capacity ? tree_size : out->node_capacity;
+    if (out->node_skip) memcpy(out->node_skip, skip, n * sizeof(uint32_t));
+    if (out->node_radius) memcpy(out->node_radius, radius, n * sizeof(float));
+    if (out->node_pos) memcpy(out->node_pos, npos, 2 * n * sizeof(float));
+    if (out->node_mass) memcpy(out->node_mass, nmass, n * sizeof(float));
+}
+
+/* ------------------------------------------------------------------------------ */
+/* literal grid restatement (fixed box)                                            */
+/* ------------------------------------------------------------------------------ */
+int orc_bh_grid_step(uint32_t n_al, float* pos_in, float* vel_in, float* mass_in,
+                     float* pos_out, float* vel_out, float* mass_out, float dt, float G,
+                     float eps2, float theta2, orc_bh_out* out, int nthreads) {
+    uint32_t* cnt[GRID_LEVELS][2];
+    uint32_t* st[GRID_LEVELS][2];
+    float* lp[GRID_LEVELS][2];
+    float* lm[GRID_LEVELS];
+    for (int d = 0; d < GRID_LEVELS; ++d) {
+        size_t nc = (size_t)1 << (2 * d);
+        for (int k = 0; k < 2; ++k) {
+            cnt[d][k] = (uint32_t*)calloc(nc, sizeof(uint32_t));
+            st[d][k] = (uint32_t*)calloc(nc, sizeof(uint32_t));
+            lp[d][k] = (float*)calloc(nc, sizeof(float));
+        }
+        lm[d] = (float*)calloc(nc, sizeof(float));
+    }
+    uint64_t cap = orc_bh_node_capacity(ORC_BOX_FIXED_500, n_al);
+    uint32_t* skip = (uint32_t*)calloc(cap, sizeof(uint32_t));
+    float* radius = (float*)calloc(cap, sizeof(float));
+    float* npos = (float*)calloc(2 * cap, sizeof(float));
+    float* nmass = (float*)calloc(cap, sizeof(float));
+    uint32_t* src = (uint32_t*)malloc((size_t)n_al * sizeof(uint32_t));
+    const double t_build = now_seconds();
+
+    /* ClearShader.comp:71-83 (level 10 arrays are calloc'ed above) */
+    for (uint32_t i = 0; i < n_al; ++i) src[i] = n_al;
+
+    /* InitShader.comp:73-119, particles in ascending index order */
+    const int L = GRID_LEVELS - 1;
+    uint64_t valid = 0;
+    for (uint32_t i = 0; i < n_al; ++i) {
+        float px = pos_in[2 * i], py = pos_in[2 * i + 1], m = mass_in[i];
+        uint32_t key;
+        if (fixed_box_key(px, py, &key)) {
+            if (out && out->keys) out->keys[i] = key;
+            cnt[L][0][key] += 1;
+            if (cnt[L][1][key] == 1) cnt[L][1][key] = 2; /* :105 */
+            cnt[L][1][key] += 1;
+            lp[L][0][key] = lp[L][0][key] + px * m;
+            lp[L][1][key] = lp[L][1][key] + py * m;
+            lm[L][key] = lm[L][key] + m;
+            ++valid;
+        } else { /* :110-117 removal */
+            if (out && out->keys) out->keys[i] = ORC_KEY_REMOVED;
+            pos_in[2 * i] = pos_in[2 * i + 1] = -SIM_SIZE * 2.0f;
+            pos_out[2 * i] = pos_out[2 * i + 1] = -SIM_SIZE * 2.0f;
+            mass_in[i] = 0.0f;
+            mass_out[i] = 0.0f;
+        }
+    }
+
+    /* TreeInitShader.comp:58-90, depths 9 .. 0 */
+    for (int d = L - 1; d >= 0; --d) {
+        size_t nc = (size_t)1 << (2 * d);
+        for (size_t c = 0; c < nc; ++c) {
+            uint32_t cx = 0, cy = 0;
+            float sx = 0.0f, sy = 0.0f, sm = 0.0f;
+            for (int q = 0; q < 4; ++q) {
+                size_t ch = 4 * c + (size_t)q;
+                cx += cnt[d + 1][0][ch];
+                cy += cnt[d + 1][1][ch];
+                if (q == 0) {
+                    sx = lp[d + 1][0][ch];
+                    sy = lp[d + 1][1][ch];
+                    sm = lm[d + 1][ch];
+                } else {
+                    sx = sx + lp[d + 1][0][ch];
+                    sy = sy + lp[d + 1][1][ch];
+                    sm = sm + lm[d + 1][ch];
+                }
+            }
+            cy += (uint32_t)(cy > 1); /* :83 */
+            cnt[d][0][c] = cx;
+            cnt[d][1][c] = cy;
+            lp[d][0][c] = sx;
+            lp[d][1][c] = sy;
+            lm[d][c] = sm;
+        }
+    }
+
+    /* TreeSortShader.comp:57-94, depths 0 .. 9; root start is 0 */
+    for (int d = 0; d < L; ++d) {
+        size_t nc = (size_t)1 << (2 * d);
+        for (size_t c = 0; c < nc; ++c) {
+            uint32_t ox = st[d][0][c], oy = st[d][1][c];
+            if (cnt[d][1][c] > 1) oy += 1;
+            for (int q = 0; q < 4; ++q) {
+                size_t ch = 4 * c + (size_t)q;
+                st[d + 1][0][ch] = ox;
+                st[d + 1][1][ch] = oy;
+                ox += cnt[d + 1][0][ch];
+                oy += cnt[d + 1][1][ch];
+            }
+        }
+    }
+
+    /* TreeMoveShader.comp:53-84, depths 0 .. 10 */
+    for (int d = 0; d <= L; ++d) {
+        size_t nc = (size_t)1 << (2 * d);
+        for (size_t c = 0; c < nc; ++c) {
+            if (cnt[d][1][c] > 1) {
+                float px = lp[d][0][c], py = lp[d][1][c], m = lm[d][c];
+                if (m != 0.0f) {
+                    px = px / m;
+                    py = py / m;
+                }
+                float r = SIM_SIZE * SIM_SIZE * 2.0f;
+                r = r / (float)(1u << (2 * d));
+                uint32_t at = st[d][1][c];
+                skip[at] = cnt[d][1][c];
+                radius[at] = r;
+                npos[2 * at] = px;
+                npos[2 * at + 1] = py;
+                nmass[at] = m;
+                if (d == L) st[d][1][c] += 1;
+            }
+        }
+    }
+
+    /* ParticleSortShader.comp:71-110, ascending index order */
+    for (uint32_t i = 0; i < n_al; ++i) {
+        float px = pos_in[2 * i], py = pos_in[2 * i + 1];
+        uint32_t key;
+        if (!fixed_box_key(px, py, &key)) continue;
+        uint32_t a = st[L][0][key]++;
+        src[a] = i;
+        uint32_t b = st[L][1][key]++;
+        skip[b] = 1;
+        radius[b] = 0.0f;
+        npos[2 * b] = px;
+        npos[2 * b + 1] = py;
+        nmass[b] = mass_in[i];
+    }
+
+    uint64_t tree_size = valid ? skip[0] : 0;
+    if (out) out->build_seconds = now_seconds() - t_build;
+    walk_ctx wc;
+    memset(&wc, 0, sizeof wc);
+    wc.skip = skip;
+    wc.radius = radius;
+    wc.npos = npos;
+    wc.nmass = nmass;
+    wc.tree_size = tree_size;
+    wc.src = src;
+    wc.n_al = n_al;
+    wc.pos_in = pos_in;
+    wc.vel_in = vel_in;
+    wc.mass_in = mass_in;
+    wc.pos_out = pos_out;
+    wc.vel_out = vel_out;
+    wc.eps2 = eps2;
+    wc.theta2 = theta2;
+    wc.k = G * dt;
+    wc.hdt = 0.5f * dt;
+    run_walk(&wc, nthreads, out);
+
+    if (out) {
+        out->tree_size = tree_size;
+        out->valid_count = valid;
+        out->internal_count = tree_size >= valid ? tree_size - valid : 0;
+        if (out->sorted_src) memcpy(out->sorted_src, src, (size_t)n_al * sizeof(uint32_t));
+        copy_tree_out(out, skip, radius, npos, nmass, tree_size);
+        out->box_center_x = out->box_center_y = 0.0f;
+        out->box_scale = (float)GRID / (2.0f * SIM_SIZE);
+        out->box_radius0 = SIM_SIZE * SIM_SIZE * 2.0f;
+    }
+
+    for (int d = 0; d < GRID_LEVELS; ++d) {
+        for (int k = 0; k < 2; ++k) {
+            free(cnt[d][k]);
+            free(st[d][k]);
+            free(lp[d][k]);
+        }
+        free(lm[d]);
+    }
+    free(skip);
+    free(radius);
+    free(npos);
+    free(nmass);
+    free(src);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------ */
+/* sorted-key construction (fixed box and bounding box)                            */
+/* ------------------------------------------------------------------------------ */
+static void stable_sort_keys(uint32_t n, const uint32_t* key, uint32_t* skey, uint32_t* sidx) {
+    uint32_t* k2 = (uint32_t*)malloc((size_t)n * sizeof(uint32_t));
+    uint32_t* i2 = (uint32_t*)malloc((size_t)n * sizeof(uint32_t));
+    for (uint32_t i = 0; i < n; ++i) {
+        skey[i] = key[i];
+        sidx[i] = i;
+    }
+    for (int pass = 0; pass < 4; ++pass) { /* LSD, 8-bit digits, stable */
+        int shift = 8 * pass;
+        uint32_t count[257];
+        memset(count, 0, sizeof count);
+        for (uint32_t i = 0; i < n; ++i) count[((skey[i] >> shift) & 255u) + 1]++;
+        for (int b = 0; b < 256; ++b) count[b + 1] += count[b];
+        for (uint32_t i = 0; i < n; ++i) {
+            uint32_t b = (skey[i] >> shift) & 255u;
+            uint32_t at = count[b]++;
+            k2[at] = skey[i];
+            i2[at] = sidx[i];
+        }
+        memcpy(skey, k2, (size_t)n * sizeof(uint32_t));
+        memcpy(sidx, i2, (size_t)n * sizeof(uint32_t));
+    }
+    free(k2);
+    free(i2);
+}
+
+static inline int common_bits(uint32_t a, uint32_t b, int key_bits) {
+    if (a == b) return key_bits;
+    return __builtin_clz(a ^ b) - (32 - key_bits);
+}
+
+int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in,
+                       float* mass_in, float* pos_out, float* vel_out, float* mass_out,
+                       float dt, float G, float eps2, float theta2, orc_bh_out* out,
+                       int nthreads) {
+    const int D = box_mode == ORC_BOX_BOUNDING ? BBOX_BITS : GRID_LEVELS - 1;
+    const int key_bits = 2 * D;
+    const double t_build = now_seconds();
+    uint32_t* key = (uint32_t*)malloc((size_t)n_al * sizeof(uint32_t));
+    uint32_t* skey = (uint32_t*)malloc((size_t)n_al * sizeof(uint32_t));
+    uint32_t* sidx = (uint32_t*)malloc((size_t)n_al * sizeof(uint32_t));
+    float radius0;
+    bbox_params bp = {0.0f, 0.0f, (float)GRID / (2.0f * SIM_SIZE), SIM_SIZE * SIM_SIZE * 2.0f};
+
+    if (box_mode == ORC_BOX_BOUNDING) {
+        double mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+        for (uint32_t i = 0; i < n_al; ++i) {
+            double x = pos_in[2 * i], y = pos_in[2 * i + 1];
+            if (x < mnx) mnx = x;
+            if (x > mxx) mxx = x;
+            if (y < mny) mny = y;
+            if (y > mxy) mxy = y;
+        }
+        bp = bbox_from_minmax(mnx, mxx, mny, mxy);
+        for (uint32_t i = 0; i < n_al; ++i) key[i] = bbox_key(pos_in[2 * i], pos_in[2 * i + 1], &bp);
+        radius0 = bp.radius0;
+    } else {
+        for (uint32_t i = 0; i < n_al; ++i) {
+            uint32_t k;
+            if (fixed_box_key(pos_in[2 * i], pos_in[2 * i + 1], &k)) {
+                key[i] = k;
+            } else { /* InitShader.comp:110-117 */
+                key[i] = ORC_KEY_REMOVED;
+                pos_in[2 * i] = pos_in[2 * i + 1] = -SIM_SIZE * 2.0f;
+                pos_out[2 * i] = pos_out[2 * i + 1] = -SIM_SIZE * 2.0f;
+                mass_in[i] = 0.0f;
+                mass_out[i] = 0.0f;
+            }
+        }
+        radius0 = SIM_SIZE * SIM_SIZE * 2.0f;
+    }
+    if (out && out->keys) memcpy(out->keys, key, (size_t)n_al * sizeof(uint32_t));
+
+    stable_sort_keys(n_al, key, skey, sidx);
+    uint32_t nv = 0;
+    while (nv < n_al && skey[nv] != ORC_KEY_REMOVED) ++nv;
+
+    /* per-slot levels: nodes (d, s) for d in [dmin(s), dmax(s)] start at slot s */
+    int* dmin = (int*)malloc(((size_t)nv + 1) * sizeof(int));
+    int* dmax = (int*)malloc(((size_t)nv + 1) * sizeof(int));
+    uint64_t* E = (uint64_t*)malloc(((size_t)nv + 1) * sizeof(uint64_t));
+    uint64_t total = 0;
+    for (uint32_t s = 0; s < nv; ++s) {
+        dmin[s] = s == 0 ? 0 : common_bits(skey[s - 1], skey[s], key_bits) / 2 + 1;
+        dmax[s] = s + 1 < nv ? common_bits(skey[s], skey[s + 1], key_bits) / 2 : -1;
+        E[s] = total;
+        int e = dmax[s] - dmin[s] + 1;
+        total += (uint64_t)(e > 0 ? e : 0);
+    }
+    E[nv] = total;
+    const uint64_t tree_size = (uint64_t)nv + total;
+
+    uint64_t cap = orc_bh_node_capacity(box_mode, n_al);
+    uint32_t* skip = (uint32_t*)calloc(cap, sizeof(uint32_t));
+    float* radius = (float*)calloc(cap, sizeof(float));
+    float* npos = (float*)calloc(2 * cap, sizeof(float));
+    float* nmass = (float*)calloc(cap, sizeof(float));
+    uint32_t* nend = (uint32_t*)calloc(cap, sizeof(uint32_t));
+    float* msx = (float*)calloc(cap, sizeof(float));
+    float* msy = (float*)calloc(cap, sizeof(float));
+
+    /* records: topology, radius and particle leaves */
+    for (uint32_t s = 0; s < nv; ++s) {
+        for (int d = dmin[s]; d <= dmax[s]; ++d) {
+            uint64_t at = s + E[s] + (uint64_t)(d - dmin[s]);
+            uint32_t shift = (uint32_t)(key_bits - 2 * d);
+            uint32_t pre = shift >= 32 ? 0 : skey[s] >> shift;
+            uint32_t end = s + 1;
+            while (end < nv && (shift >= 32 ? 0 : skey[end] >> shift) == pre) ++end;
+            nend[at] = end;
+            skip[at] = (uint32_t)((uint64_t)end + E[end] - at);
+            radius[at] = radius0 / (float)(1u << (2 * d));
+        }
+        uint64_t leaf = s + E[s] + (uint64_t)(dmax[s] >= dmin[s] ? dmax[s] - dmin[s] + 1 : 0);
+        uint32_t i = sidx[s];
+        skip[leaf] = 1;
+        radius[leaf] = 0.0f;
+        npos[2 * leaf] = pos_in[2 * i];
+        npos[2 * leaf + 1] = pos_in[2 * i + 1];
+        nmass[leaf] = mass_in[i];
+    }
+
+    /* mass and mass-moment sums, finest level first */
+    for (int d = D; d >= 0; --d) {
+        for (uint32_t s = 0; s < nv; ++s) {
+            if (d < dmin[s] || d > dmax[s]) continue;
+            uint64_t at = s + E[s] + (uint64_t)(d - dmin[s]);
+            uint32_t end = nend[at];
+            float sx = 0.0f, sy = 0.0f, sm = 0.0f;
+            uint32_t t = s;
+            while (t < end) {
+                if (d < D && dmin[t] <= d + 1 && d + 1 <= dmax[t]) {
+                    uint64_t ch = t + E[t] + (uint64_t)(d + 1 - dmin[t]);
+                    sx = sx + msx[ch];
+                    sy = sy + msy[ch];
+                    sm = sm + nmass[ch];
+                    t = nend[ch];
+                } else {
+                    uint32_t i = sidx[t];
+                    float m = mass_in[i];
+                    sx = sx + pos_in[2 * i] * m;
+                    sy = sy + pos_in[2 * i + 1] * m;
+                    sm = sm + m;
+                    t += 1;
+                }
+            }
+            msx[at] = sx;
+            msy[at] = sy;
+            nmass[at] = sm;
+            if (sm != 0.0f) {
+                sx = sx / sm;
+                sy = sy / sm;
+            }
+            npos[2 * at] = sx;
+            npos[2 * at + 1] = sy;
+        }
+    }
+
+    uint32_t* src = (uint32_t*)malloc((size_t)n_al * sizeof(uint32_t));
+    for (uint32_t s = 0; s < n_al; ++s) src[s] = s < nv ? sidx[s] : n_al;
+    if (out) out->build_seconds = now_seconds() - t_build;
+
+    walk_ctx wc;
+    memset(&wc, 0, sizeof wc);
+    wc.skip = skip;
+    wc.radius = radius;
+    wc.npos = npos;
+    wc.nmass = nmass;
+    wc.tree_size = tree_size;
+    wc.src = src;
+    wc.n_al = n_al;
+    wc.pos_in = pos_in;
+    wc.vel_in = vel_in;
+    wc.mass_in = mass_in;
+    wc.pos_out = pos_out;
+    wc.vel_out = vel_out;
+    wc.eps2 = eps2;
+    wc.theta2 = theta2;
+    wc.k = G * dt;
+    wc.hdt = 0.5f * dt;
+    run_walk(&wc, nthreads, out);
+
+    if (out) {
+        out->tree_size = tree_size;
+        out->valid_count = nv;
+        out->internal_count = total;
+        if (out->sorted_src) memcpy(out->sorted_src, src, (size_t)n_al * sizeof(uint32_t));
+        copy_tree_out(out, skip, radius, npos, nmass, tree_size);
+        out->box_center_x = bp.cx;
+        out->box_center_y = bp.cy;
+        out->box_scale = bp.scale;
+        out->box_radius0 = radius0;
+    }
+    free(key);
+    free(skey);
+    free(sidx);
+    free(dmin);
+    free(dmax);
+    free(E);
+    free(skip);
+    free(radius);
+    free(npos);
+    free(nmass);
+    free(nend);
+    free(msx);
+    free(msy);
+    free(src);
+    return 0;
+}

@@ -1,0 +1,129 @@
+"""Barnes-Hut CUDA path (through the C ABI) against the CPU restatement of the seven
+Barnes-Hut shaders.
+
+Cell keys, sorted order and the preorder records (skip, radius, centre of mass, mass)
+are compared bit for bit.  REFERENCE math makes the whole step bit-identical; FAST math
+(hardware rsqrt) keeps the same traversal and differs only in the rounding of 1/sqrt:
+velocities within 1e-4 * max|v| + 2e-6 per component after one step."""
+import numpy as np
+import pytest
+
+from treecheck import check_tree, edge_case_inputs
+
+pytestmark = pytest.mark.gpu
+FIELDS = ("keys", "sorted_src", "skip", "radius", "pos", "mass")
+
+
+def _sim(gs, pos, vel, mass, **kw):
+    p = gs.default_params(algorithm=gs.BARNES_HUT, **kw)
+    return gs.Simulation(pos, vel, mass, params=p)
+
+
+def _compare_tree(g, o):
+    assert g["tree_size"] == o["tree_size"]
+    for k in FIELDS:
+        a, b = g[k], o[k]
+        if not np.array_equal(a, b, equal_nan=True):
+            bad = np.nonzero((a != b).reshape(len(a), -1).any(axis=1))[0]
+            raise AssertionError(f"{k}: {len(bad)} differ, first {bad[:5]}: {a[bad[:3]]} vs {b[bad[:3]]}")
+
+
+CASES = [(17, 3000, 100.0), (16, 4096, 100.0), (2, 2500, 700.0), (0, 777, 100.0), (3, 1024, 300.0)]
+
+
+@pytest.mark.parametrize("box", [0, 1])
+@pytest.mark.parametrize("kind,n,size", CASES)
+def test_reference_math_bit_exact(gs, orc, box, kind, n, size):
+    pos, vel, mass = gs.generate(kind, n, size=size, seed=31)
+    st = orc.State(pos, vel, mass)
+    with _sim(gs, pos, vel, mass, box_mode=box, math_mode=gs.MATH_REFERENCE,
+              flags=gs.FLAG_COUNT_INTERACTIONS) as sim:
+        for step in range(3):
+            sim.reset_stats()
+            sim.run(1)
+            o = orc.bh_step(st, box_mode=box)
+            g = sim.bh_tree()
+            _compare_tree(g, o)
+            s = sim.stats()
+            assert s.interactions == o["interactions"]
+            assert s.placed_particles == o["valid_count"]
+            gp, gv, gm = sim.get_particles()
+            op, ov, om = st.current()
+            np.testing.assert_array_equal(gp, op)
+            np.testing.assert_array_equal(gv, ov)
+            np.testing.assert_array_equal(gm, om)
+
+
+@pytest.mark.parametrize("name", list(edge_case_inputs().keys()))
+def test_edge_cases_bit_exact(gs, orc, name):
+    pos, vel, mass = edge_case_inputs()[name]
+    st = orc.State(pos, vel, mass)
+    with _sim(gs, pos, vel, mass, math_mode=gs.MATH_REFERENCE) as sim:
+        for _ in range(2):
+            sim.run(1)
+            o = orc.bh_step(st)
+            _compare_tree(sim.bh_tree(), o)
+            gp, gv, gm = sim.get_particles()
+            op, ov, om = st.current()
+            np.testing.assert_array_equal(gp, op)
+            np.testing.assert_array_equal(gv, ov)
+            np.testing.assert_array_equal(gm, om)
+
+
+@pytest.mark.parametrize("box", [0, 1])
+def test_fast_math_same_tree_close_state(gs, orc, box):
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 20000, seed=12)
+    st = orc.State(pos, vel, mass)
+    with _sim(gs, pos, vel, mass, box_mode=box) as sim:
+        sim.run(1)
+        o = orc.bh_step(st, box_mode=box)
+        _compare_tree(sim.bh_tree(), o)
+        gp, gv, _ = sim.get_particles()
+    op, ov, _ = st.current()
+    assert np.max(np.abs(gv - ov)) <= 1e-4 * np.abs(ov).max() + 2e-6
+    np.testing.assert_allclose(gp, op, rtol=0, atol=1e-5)
+
+
+@pytest.mark.parametrize("box", [0, 1])
+def test_spiral_100k_tree_bit_exact(gs, orc, box):
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 100000, seed=77)
+    st = orc.State(pos, vel, mass)
+    with _sim(gs, pos, vel, mass, box_mode=box, math_mode=gs.MATH_REFERENCE) as sim:
+        sim.run(1)
+        o = orc.bh_step(st, box_mode=box)
+        _compare_tree(sim.bh_tree(), o)
+        gp, gv, _ = sim.get_particles()
+    op, ov, _ = st.current()
+    np.testing.assert_array_equal(gp, op)
+    np.testing.assert_array_equal(gv, ov)
+
+
+@pytest.mark.parametrize("box", [0, 1])
+def test_config2_full_size_properties(gs, orc, box):
+    # N=500,000 spiral, theta=1: size-independent properties of one full-size step
+    n = 500000
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, n, seed=2002)
+    with _sim(gs, pos, vel, mass, box_mode=box, flags=gs.FLAG_RECORD_ACCEL) as sim:
+        sim.run(1)
+        t = sim.bh_tree()
+        acc = sim.get_accel()
+        n_al = sim.n_al
+        sub = np.random.default_rng(0).choice(n, 4096, replace=False).astype(np.uint32)
+        sim.set_particles(pos, vel, mass)  # back to the step's input for the FP64 reference
+        a64 = sim.accel_f64(sub)
+    valid = n_al  # the spiral lies inside +-500 and the bounding box keeps everything
+    src = t["sorted_src"]
+    assert np.array_equal(np.sort(src), np.arange(n_al, dtype=np.uint32))
+    keys = t["keys"][src]
+    assert np.all(np.diff(keys.astype(np.int64)) >= 0)
+    order_ok = (np.diff(keys.astype(np.int64)) > 0) | (np.diff(src.astype(np.int64)) > 0)
+    assert np.all(order_ok)  # stable: equal keys keep ascending original index
+    r0 = 500000.0 if box == 0 else None
+    if r0 is None:
+        r0 = float(t["radius"][0]) if t["skip"][0] > 1 else 0.0
+    check_tree(t, r0, valid)
+    assert abs(t["mass"][0] - mass.astype(np.float64).sum()) < 1e-4 * mass.sum()
+    err = np.linalg.norm(acc[sub].astype(np.float64) - a64, axis=1) / np.linalg.norm(a64, axis=1)
+    print(f"box {box}: force error vs FP64 on 4096 particles: rms {np.sqrt(np.mean(err**2)):.3e} "
+          f"median {np.median(err):.3e} p99 {np.quantile(err, 0.99):.3e} max {err.max():.3e}")
+    assert np.sqrt(np.mean(err ** 2)) < 5e-2

@@ -1,0 +1,89 @@
+"""The CPU restatement of the Barnes-Hut shaders (no GPU): the literal 1024x1024 grid of
+ClearShader..ForceShader and the sorted-key construction must agree bit for bit; the
+tree must be structurally sound; theta = 0 must reduce to the direct sum."""
+import numpy as np
+import pytest
+
+from treecheck import check_tree, edge_case_inputs
+
+FIELDS = ("keys", "sorted_src", "skip", "radius", "pos", "mass")
+
+
+def _same(a, b):
+    return all(np.array_equal(a[k], b[k], equal_nan=True) for k in FIELDS)
+
+
+@pytest.mark.parametrize("kind,n,size", [(17, 3000, 100.0), (16, 4096, 100.0), (2, 2500, 700.0), (0, 1000, 100.0),
+                                         (3, 1024, 300.0)])
+def test_grid_equals_sorted(gs, orc, kind, n, size):
+    pos, vel, mass = gs.generate(kind, n, size=size, seed=21)
+    a, b = orc.State(pos, vel, mass), orc.State(pos, vel, mass)
+    for _ in range(3):
+        ra = orc.bh_step(a, method="grid")
+        rb = orc.bh_step(b, method="sorted")
+        assert _same(ra, rb)
+        assert ra["interactions"] == rb["interactions"]
+        for x, y in zip(a.current(), b.current()):
+            np.testing.assert_array_equal(x, y)
+        check_tree(rb, 500000.0, rb["valid_count"])
+
+
+@pytest.mark.parametrize("name", list(edge_case_inputs().keys()))
+def test_grid_equals_sorted_edge_cases(orc, name):
+    pos, vel, mass = edge_case_inputs()[name]
+    a, b = orc.State(pos, vel, mass), orc.State(pos, vel, mass)
+    for _ in range(2):
+        ra = orc.bh_step(a, method="grid")
+        rb = orc.bh_step(b, method="sorted")
+        assert _same(ra, rb)
+        for x, y in zip(a.current(), b.current()):
+            np.testing.assert_array_equal(x, y)
+
+
+def test_removal_semantics(orc):
+    # InitShader.comp:110-117: outside particles move to (-1000, -1000) with mass 0 in both sets
+    pos = np.array([[0.0, 0.0], [600.0, 0.0], [10.0, 10.0], [0.0, -501.0]], np.float32)
+    vel = np.ones_like(pos)
+    mass = np.ones(4, np.float32)
+    st = orc.State(pos, vel, mass)
+    r = orc.bh_step(st, method="grid")
+    p, v, m = st.current()
+    assert r["keys"][1] == orc.KEY_REMOVED and r["keys"][3] == orc.KEY_REMOVED
+    np.testing.assert_array_equal(p[[1, 3]], -1000.0)
+    np.testing.assert_array_equal(m, [1, 0, 1, 0])
+    np.testing.assert_array_equal(v[[1, 3]], 1.0)  # never written: the output set's old value
+
+
+def test_theta_zero_is_direct_sum(gs, orc):
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 700, seed=4)
+    a, b = orc.State(pos, vel, mass), orc.State(pos, vel, mass)
+    orc.bh_step(a, theta=0.0)
+    orc.direct_step(b)
+    pa, va, _ = a.current()
+    pb, vb, _ = b.current()
+    np.testing.assert_allclose(va, vb, rtol=2e-4, atol=1e-4 * np.abs(vb).max())
+    np.testing.assert_allclose(pa, pb, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("kind,n", [(17, 5000), (2, 3000), (16, 64)])
+def test_bounding_box_tree(gs, orc, kind, n):
+    pos, vel, mass = gs.generate(kind, n, size=100.0, seed=8)
+    st = orc.State(pos, vel, mass)
+    r = orc.bh_step(st, box_mode=orc.BOX_BOUNDING)
+    assert r["valid_count"] == st.n_al  # nothing is removed
+    check_tree(r, r["box"][3], r["valid_count"])
+    keys = r["keys"][r["sorted_src"][: r["valid_count"]]]
+    assert np.all(np.diff(keys.astype(np.int64)) >= 0)
+    assert np.all(keys < (1 << 30))
+
+
+def test_bounding_box_force_accuracy(gs, orc):
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 4000, seed=2)
+    st = orc.State(pos, vel, mass)
+    k = np.float32(1e-3)
+    orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.5)
+    _, v1, _ = st.current()
+    acc_bh = (v1.astype(np.float64) - vel) / float(k)
+    a64 = orc.direct_accel_f64(*orc.pad_state(pos, vel, mass)[::2])[:4000]
+    err = np.linalg.norm(acc_bh - a64, axis=1) / np.linalg.norm(a64, axis=1)
+    assert np.median(err) < 2e-2
