@@ -326,8 +326,10 @@ k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, 
     for (uint32_t i = t; i < tile_n; i += kSortThreads) {
         uint32_t k = s_keys[i];
         uint32_t g = s_gbase[(k >> shift) & 255u] + i;
-        kout[g] = k;
-        vout[g] = s_vals[i];
+        if (g < n) {  // always true unless a look-back wait gave up (error flag set)
+            kout[g] = k;
+            vout[g] = s_vals[i];
+        }
     }
 }
 
@@ -420,7 +422,8 @@ __global__ void __launch_bounds__(256)
 k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ E,
           const uint32_t* __restrict__ valid_count, int D, const BHParams* __restrict__ bp,
           const float2* __restrict__ pos, const float* __restrict__ mass, float4* __restrict__ rec,
-          uint32_t* __restrict__ skip, uint32_t* __restrict__ nend, uint64_t cap, int* __restrict__ err) {
+          uint32_t* __restrict__ skip, uint32_t* __restrict__ nend, uint64_t cap, uint32_t n_al,
+          int* __restrict__ err) {
     const uint32_t nv = *valid_count;
     const float radius0 = bp->radius0;
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += gridDim.x * blockDim.x) {
@@ -433,6 +436,10 @@ k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, 
             continue;
         }
         const uint32_t i = sidx[s];
+        if (i >= n_al) {  // only after a failed sort (error flag already set)
+            atomicOr(err, kErrTree);
+            continue;
+        }
         const float2 p = pos[i];
         rec[leaf] = make_float4(p.x, p.y, mass[i], 0.0f);
         skip[leaf] = 1u;
@@ -456,12 +463,13 @@ k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, 
 __global__ void __launch_bounds__(256)
 k_sums_level(int d, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
              const uint32_t* __restrict__ valid_count, int D, float4* __restrict__ rec,
-             const uint32_t* __restrict__ nend, float2* __restrict__ msum) {
+             const uint32_t* __restrict__ nend, float2* __restrict__ msum, uint32_t cap) {
     const uint32_t nv = *valid_count;
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += gridDim.x * blockDim.x) {
         const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
         if (d < dmin || d > dmax) continue;
         const uint32_t at = s + E[s] + (uint32_t)(d - dmin);
+        if (at >= cap) continue;  // only after a failed scan (error flag already set)
         const uint32_t end = nend[at];
         float sx = 0.0f, sy = 0.0f, sm = 0.0f;
         if (d == D) {  // finest cell: its particle leaves follow the node record
@@ -513,17 +521,17 @@ __global__ void __launch_bounds__(kForceWarps * 32)
 k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, const float4* __restrict__ rec,
         const uint32_t* __restrict__ skip, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
         float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
-        float eps2, float theta2, float k, float hdt, unsigned long long* __restrict__ stat) {
+        float eps2, float theta2, float k, float hdt, uint32_t cap, unsigned long long* __restrict__ stat) {
     __shared__ float4 wrec[kForceWarps][32];
     __shared__ uint32_t wskip[kForceWarps][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t group = blockIdx.x * kForceWarps + warp;
     const uint32_t nv = counts[0];
-    const uint32_t T = nv + counts[1];  // preorder records
+    const uint32_t T = min(nv + counts[1], cap);  // preorder records
     if (group * 32 >= nv) return;       // no particle in this warp: nothing to write
     const uint32_t s = group * 32 + lane;
-    const bool valid = s < nv;
-    const uint32_t i = valid ? sidx[s] : 0u;
+    const uint32_t i = s < nv ? sidx[s] : 0u;
+    const bool valid = s < nv && i < n_al;  // i < n_al unless the sort failed (error flag set)
     const float2 p = valid ? pos_in[i] : make_float2(0.0f, 0.0f);
     float ax = 0.0f, ay = 0.0f;
     unsigned long long n_acc = 0, n_vis = 0;
@@ -550,7 +558,7 @@ k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, 
             ax = fmaf(dx, sc, ax);
             ay = fmaf(dy, sc, ay);
             if (COUNT) n_acc += valid;
-            ind += wskip[warp][ind - base];
+            ind += max(wskip[warp][ind - base], 1u);  // >= 1: the walk always advances
         } else {
             ++ind;
         }
@@ -707,12 +715,13 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     stage_end(s, kStageScan, profile);
     stage_begin(s, kStageRecords, profile);
     k_records<<<grid_for(n, 256), 256, 0, st>>>(skey, sidx, w.E, ctr + kCtrValid, w.depth, w.params, s->pos[in],
-                                                s->mass[in], w.rec, w.skip, w.nend, w.cap, s->d_err);
+                                                s->mass[in], w.rec, w.skip, w.nend, w.cap, n, s->d_err);
     count_launch(s);
     stage_end(s, kStageRecords, profile);
     stage_begin(s, kStageSums, profile);
     for (int d = w.depth; d >= 0; --d)
-        k_sums_level<<<grid_for(n, 256), 256, 0, st>>>(d, skey, w.E, ctr + kCtrValid, w.depth, w.rec, w.nend, w.msum);
+        k_sums_level<<<grid_for(n, 256), 256, 0, st>>>(d, skey, w.E, ctr + kCtrValid, w.depth, w.rec, w.nend, w.msum,
+                                                        (uint32_t)w.cap);
     count_launch(s, w.depth + 1);
     stage_end(s, kStageSums, profile);
     stage_begin(s, kStageForce, profile);
@@ -725,7 +734,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
 #define GS_FORCE(E_, C_)                                                                                      \
     k_force<E_, C_><<<blocks, kForceWarps * 32, 0, st>>>(sidx, ctr + kCtrValid, w.rec, w.skip, s->pos[in],    \
                                                          s->vel[in], s->pos[out], s->vel[out], s->acc, n, s->eps2, \
-                                                         s->theta2, k, hdt, stat)
+                                                         s->theta2, k, hdt, (uint32_t)w.cap, stat)
     if (exact) {
         if (count) GS_FORCE(true, true);
         else GS_FORCE(true, false);

@@ -258,7 +258,7 @@ cudaError_t direct_step(gs_sim* s, int in, int out, bool profile) {
 }
 
 cudaError_t accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* d_targets, double2* d_out) {
-    const double eps2 = (double)s->p.softening_len * (double)s->p.softening_len;
+    const double eps2 = (double)s->eps2;  // the softening the FP32 path uses, exactly
     k_accel_f64<<<n_targets, 256, 0, s->stream>>>(d_targets, s->pos[s->in], s->mass[s->in],
                                                   (uint32_t)s->n_al, eps2, d_out);
     return cudaGetLastError();

@@ -112,6 +112,27 @@ static inline float pair_scale(float m, float d2) {
     return ((m * r) * r) * r;
 }
 
+/* Quadrupole-corrected acceleration from a node with mass m, centre of mass at offset
+ * (dx, dy) from the particle and second central moments S = {sxx, sxy, syy}:
+ *   a = d (m r^3 + 7.5 u r^7 - 1.5 T r^5) - 3 r^5 S d,   u = d^T S d,  T = sxx + syy,
+ * with r = 1 / sqrt(|d|^2 + eps^2) (Plummer-softened expansion of sum m_k / |x_k - p|). */
+static inline void quad_accumulate(float dx, float dy, float d2, float m, float sxx, float sxy, float syy,
+                                   float* ax, float* ay) {
+    float r = 1.0f / sqrtf(d2);
+    float r2 = r * r;
+    float r3 = r2 * r;
+    float r5 = r3 * r2;
+    float r7 = r5 * r2;
+    float srx = fmaf(sxx, dx, sxy * dy);
+    float sry = fmaf(sxy, dx, syy * dy);
+    float u = fmaf(dx, srx, dy * sry);
+    float T = sxx + syy;
+    float coef = fmaf(7.5f * u, r7, fmaf(-1.5f * T, r5, m * r3));
+    float t3 = 3.0f * r5;
+    *ax = fmaf(-t3, srx, fmaf(dx, coef, *ax));
+    *ay = fmaf(-t3, sry, fmaf(dy, coef, *ay));
+}
+
 /* ------------------------------------------------------------------------------ */
 /* direct sum -- SimShader.comp:37-74                                              */
 /* ------------------------------------------------------------------------------ */
@@ -303,6 +324,7 @@ uint64_t orc_bh_node_capacity(int box_mode, uint32_t n_al) {
 typedef struct {
     const uint32_t* skip;
     const float *radius, *npos, *nmass;
+    const float* quad; /* second central moments {sxx, sxy, syy} per record, NULL: monopoles */
     uint64_t tree_size;
     const uint32_t* src; /* original index per sorted slot, n_al for empty slots */
     uint32_t n_al;
@@ -344,11 +366,19 @@ static void walk_warp(void* p, uint64_t item, int worker) {
         }
         ++visits;
         if (all) {
-            for (int l = 0; l < WARP; ++l) {
-                if (!valid[l]) continue;
-                float s = pair_scale(nm, d2[l]);
-                ax[l] = fmaf(dx[l], s, ax[l]);
-                ay[l] = fmaf(dy[l], s, ay[l]);
+            if (c->quad && c->skip[ind] > 1) { /* internal node: quadrupole term */
+                const float sxx = c->quad[3 * ind], sxy = c->quad[3 * ind + 1], syy = c->quad[3 * ind + 2];
+                for (int l = 0; l < WARP; ++l) {
+                    if (!valid[l]) continue;
+                    quad_accumulate(dx[l], dy[l], d2[l], nm, sxx, sxy, syy, &ax[l], &ay[l]);
+                }
+            } else {
+                for (int l = 0; l < WARP; ++l) {
+                    if (!valid[l]) continue;
+                    float s = pair_scale(nm, d2[l]);
+                    ax[l] = fmaf(dx[l], s, ax[l]);
+                    ay[l] = fmaf(dy[l], s, ay[l]);
+                }
             }
             inter += (uint64_t)nvalid;
             ind += c->skip[ind];
@@ -619,10 +649,49 @@ static inline int common_bits(uint32_t a, uint32_t b, int key_bits) {
     return __builtin_clz(a ^ b) - (32 - key_bits);
 }
 
+static inline uint32_t compact_bits(uint32_t v) { /* inverse of spread_bits */
+    v &= 0x55555555u;
+    v = (v | (v >> 1)) & 0x33333333u;
+    v = (v | (v >> 2)) & 0x0f0f0f0fu;
+    v = (v | (v >> 4)) & 0x00ff00ffu;
+    v = (v | (v >> 8)) & 0x0000ffffu;
+    return v;
+}
+
+/* Squared distance from the centre of mass (cx, cy) to the farthest corner of the cell
+ * at level d that holds key `key` (the opening radius of ORC_BH_SAFE_RADIUS). */
+static float cell_bmax2(int box_mode, const bbox_params* bp, int D, int d, uint32_t key, float cx, float cy) {
+    uint32_t pre = key >> (2 * (D - d));
+    double ix = (double)compact_bits(pre), iy = (double)compact_bits(pre >> 1);
+    double x0, y0, side;
+    if (box_mode == ORC_BOX_BOUNDING) {
+        double w = (double)(1u << (D - d));
+        side = w / (double)bp->scale;
+        x0 = (double)bp->cx + (ix * w - (double)(1u << (D - 1))) / (double)bp->scale;
+        y0 = (double)bp->cy + (iy * w - (double)(1u << (D - 1))) / (double)bp->scale;
+    } else {
+        side = 2.0 * (double)SIM_SIZE / (double)(1u << d);
+        x0 = -(double)SIM_SIZE + ix * side;
+        y0 = -(double)SIM_SIZE + iy * side;
+    }
+    double ax = fabs((double)cx - x0), bx = fabs(x0 + side - (double)cx);
+    double ay = fabs((double)cy - y0), by = fabs(y0 + side - (double)cy);
+    double mx = ax > bx ? ax : bx, my = ay > by ? ay : by;
+    return (float)(mx * mx + my * my);
+}
+
 int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in,
                        float* mass_in, float* pos_out, float* vel_out, float* mass_out,
                        float dt, float G, float eps2, float theta2, orc_bh_out* out,
                        int nthreads) {
+    return orc_bh_sorted_step_ex(box_mode, 0, n_al, pos_in, vel_in, mass_in, pos_out, vel_out, mass_out, dt, G,
+                                 eps2, theta2, out, nthreads);
+}
+
+int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in, float* vel_in,
+                          float* mass_in, float* pos_out, float* vel_out, float* mass_out,
+                          float dt, float G, float eps2, float theta2, orc_bh_out* out,
+                          int nthreads) {
     const int D = box_mode == ORC_BOX_BOUNDING ? BBOX_BITS : GRID_LEVELS - 1;
     const int key_bits = 2 * D;
     const double t_build = now_seconds();
@@ -688,6 +757,7 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
     uint32_t* nend = (uint32_t*)calloc(cap, sizeof(uint32_t));
     float* msx = (float*)calloc(cap, sizeof(float));
     float* msy = (float*)calloc(cap, sizeof(float));
+    float* quad = (flags & ORC_BH_QUADRUPOLE) ? (float*)calloc(3 * cap, sizeof(float)) : NULL;
 
     /* records: topology, radius and particle leaves */
     for (uint32_t s = 0; s < nv; ++s) {
@@ -743,6 +813,38 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
             }
             npos[2 * at] = sx;
             npos[2 * at + 1] = sy;
+            if (quad) { /* second central moments about the centre of mass, children in order */
+                float qxx = 0.0f, qxy = 0.0f, qyy = 0.0f;
+                t = s;
+                while (t < end) {
+                    float mc, xc, yc;
+                    if (d < D && dmin[t] <= d + 1 && d + 1 <= dmax[t]) {
+                        uint64_t ch = t + E[t] + (uint64_t)(d + 1 - dmin[t]);
+                        mc = nmass[ch];
+                        xc = npos[2 * ch];
+                        yc = npos[2 * ch + 1];
+                        qxx = qxx + quad[3 * ch];
+                        qxy = qxy + quad[3 * ch + 1];
+                        qyy = qyy + quad[3 * ch + 2];
+                        t = nend[ch];
+                    } else {
+                        uint32_t i = sidx[t];
+                        mc = mass_in[i];
+                        xc = pos_in[2 * i];
+                        yc = pos_in[2 * i + 1];
+                        t += 1;
+                    }
+                    float ddx = xc - sx, ddy = yc - sy;
+                    float tx = mc * ddx;
+                    qxx = fmaf(tx, ddx, qxx);
+                    qxy = fmaf(tx, ddy, qxy);
+                    qyy = fmaf(mc * ddy, ddy, qyy);
+                }
+                quad[3 * at] = qxx;
+                quad[3 * at + 1] = qxy;
+                quad[3 * at + 2] = qyy;
+            }
+            if (flags & ORC_BH_SAFE_RADIUS) radius[at] = cell_bmax2(box_mode, &bp, D, d, skey[s], sx, sy);
         }
     }
 
@@ -756,6 +858,7 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
     wc.radius = radius;
     wc.npos = npos;
     wc.nmass = nmass;
+    wc.quad = quad;
     wc.tree_size = tree_size;
     wc.src = src;
     wc.n_al = n_al;
@@ -774,6 +877,10 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
         out->tree_size = tree_size;
         out->valid_count = nv;
         out->internal_count = total;
+        if (out->node_quad && quad) {
+            uint64_t nq = tree_size < out->node_capacity ? tree_size : out->node_capacity;
+            memcpy(out->node_quad, quad, 3 * nq * sizeof(float));
+        }
         if (out->sorted_src) memcpy(out->sorted_src, src, (size_t)n_al * sizeof(uint32_t));
         copy_tree_out(out, skip, radius, npos, nmass, tree_size);
         out->box_center_x = bp.cx;
@@ -794,6 +901,7 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
     free(nend);
     free(msx);
     free(msy);
+    free(quad);
     free(src);
     return 0;
 }

@@ -56,6 +56,7 @@ typedef struct orc_bh_out {
     float* node_radius;
     float* node_pos;
     float* node_mass;
+    float* node_quad;        /* [3*capacity] second central moments (ORC_BH_QUADRUPOLE) */
     uint64_t node_capacity;
     uint32_t walk_stride;    /* input: walk only warps w with w % stride == 0 (0 or 1: all) */
     /* filled by the step */
@@ -92,6 +93,20 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
                        float* mass_in, float* pos_out, float* vel_out, float* mass_out,
                        float dt, float G, float eps2, float theta2, orc_bh_out* out,
                        int nthreads);
+
+/* Flags of the accurate Barnes-Hut mode (not in the reference):
+ *   ORC_BH_QUADRUPOLE   nodes carry second central moments; accepted nodes add the
+ *                       quadrupole term (particle leaves stay monopoles)
+ *   ORC_BH_SAFE_RADIUS  the opening radius is the squared distance from the centre of
+ *                       mass to the farthest corner of the cell (the reference's s^2/2
+ *                       is that value for a centred centre of mass), so a cell that holds
+ *                       the particle is never accepted for theta <= 1 */
+#define ORC_BH_QUADRUPOLE 1
+#define ORC_BH_SAFE_RADIUS 2
+int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in, float* vel_in,
+                          float* mass_in, float* pos_out, float* vel_out, float* mass_out,
+                          float dt, float G, float eps2, float theta2, orc_bh_out* out,
+                          int nthreads);
 
 /* Upper bound on preorder records for n_al particles in either mode. */
 uint64_t orc_bh_node_capacity(int box_mode, uint32_t n_al);

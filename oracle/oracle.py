@@ -15,6 +15,8 @@ import numpy as np
 from . import build as _build
 
 BOX_FIXED_500, BOX_BOUNDING = 0, 1
+QUADRUPOLE, SAFE_RADIUS = 1, 2
+ACCURATE = QUADRUPOLE | SAFE_RADIUS
 KEY_REMOVED = 0xFFFFFFFF
 _FP = C.POINTER(C.c_float)
 _UP = C.POINTER(C.c_uint32)
@@ -23,7 +25,8 @@ _DP = C.POINTER(C.c_double)
 
 class BHOut(C.Structure):
     _fields_ = [("keys", _UP), ("sorted_src", _UP), ("node_skip", _UP), ("node_radius", _FP),
-                ("node_pos", _FP), ("node_mass", _FP), ("node_capacity", C.c_uint64), ("walk_stride", C.c_uint32),
+                ("node_pos", _FP), ("node_mass", _FP), ("node_quad", _FP), ("node_capacity", C.c_uint64),
+                ("walk_stride", C.c_uint32),
                 ("tree_size", C.c_uint64), ("valid_count", C.c_uint64), ("internal_count", C.c_uint64),
                 ("interactions", C.c_uint64), ("warp_visits", C.c_uint64),
                 ("box_center_x", C.c_float), ("box_center_y", C.c_float), ("box_scale", C.c_float),
@@ -51,6 +54,9 @@ def lib():
         L.orc_bh_sorted_step.argtypes = [C.c_int, C.c_uint32, _FP, _FP, _FP, _FP, _FP, _FP, C.c_float, C.c_float,
                                          C.c_float, C.c_float, C.POINTER(BHOut), C.c_int]
         L.orc_bh_sorted_step.restype = C.c_int
+        L.orc_bh_sorted_step_ex.argtypes = [C.c_int, C.c_int, C.c_uint32, _FP, _FP, _FP, _FP, _FP, _FP, C.c_float,
+                                            C.c_float, C.c_float, C.c_float, C.POINTER(BHOut), C.c_int]
+        L.orc_bh_sorted_step_ex.restype = C.c_int
         L.orc_bh_node_capacity.argtypes = [C.c_int, C.c_uint32]
         L.orc_bh_node_capacity.restype = C.c_uint64
         L.orc_energy_f64.argtypes = [C.c_uint32, _FP, _FP, _FP, C.c_double, C.c_double]
@@ -131,7 +137,7 @@ def direct_accel_f64(pos, mass, softening=0.2, targets=None, threads=os.cpu_coun
 
 
 def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, G=1.0, softening=0.2, theta=1.0,
-            keep_tree=True, threads=os.cpu_count(), walk_stride=1):
+            keep_tree=True, threads=os.cpu_count(), walk_stride=1, flags=0):
     """One Barnes-Hut step; returns a dict with keys, sorted_src and the preorder records."""
     (pi, vi, mi), (po, vo, mo) = state.sets()
     n_al = state.n_al
@@ -143,13 +149,15 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
     if keep_tree:
         res = dict(keys=np.empty(n_al, np.uint32), sorted_src=np.empty(n_al, np.uint32),
                    skip=np.empty(cap, np.uint32), radius=np.empty(cap, np.float32),
-                   pos=np.empty((cap, 2), np.float32), mass=np.empty(cap, np.float32))
+                   pos=np.empty((cap, 2), np.float32), mass=np.empty(cap, np.float32),
+                   quad=np.zeros((cap, 3), np.float32))
         out.keys = res["keys"].ctypes.data_as(_UP)
         out.sorted_src = res["sorted_src"].ctypes.data_as(_UP)
         out.node_skip = res["skip"].ctypes.data_as(_UP)
         out.node_radius = _fp(res["radius"])
         out.node_pos = _fp(res["pos"])
         out.node_mass = _fp(res["mass"])
+        out.node_quad = _fp(res["quad"])
         out.node_capacity = cap
     dt_eff = float(np.float32(dt) * np.float32(speed))
     eps2 = float(np.float32(softening) * np.float32(softening))
@@ -159,12 +167,12 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
         L.orc_bh_grid_step(n_al, _fp(pi), _fp(vi), _fp(mi), _fp(po), _fp(vo), _fp(mo), dt_eff, G, eps2, th2,
                            C.byref(out), threads)
     else:
-        L.orc_bh_sorted_step(box_mode, n_al, _fp(pi), _fp(vi), _fp(mi), _fp(po), _fp(vo), _fp(mo), dt_eff, G,
-                             eps2, th2, C.byref(out), threads)
+        L.orc_bh_sorted_step_ex(box_mode, flags, n_al, _fp(pi), _fp(vi), _fp(mi), _fp(po), _fp(vo), _fp(mo),
+                                dt_eff, G, eps2, th2, C.byref(out), threads)
     state.flip()
     t = out.tree_size
     if keep_tree:
-        for k in ("skip", "radius", "pos", "mass"):
+        for k in ("skip", "radius", "pos", "mass", "quad"):
             res[k] = res[k][:t]
     res.update(tree_size=t, valid_count=out.valid_count, internal_count=out.internal_count,
                interactions=out.interactions, warp_visits=out.warp_visits,
