@@ -18,6 +18,8 @@
 //
 // Roofline: 14 algorithmic FLOP per pair (2 sub, 2 FMA for r^2, rsqrt, 3 mul, 2 FMA),
 // 9 FP32-pipe instructions + 1 MUFU per pair; FP32-bound.
+#include <mutex>
+
 #include "internal.cuh"
 
 namespace gsim {
@@ -265,3 +267,100 @@ cudaError_t accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* d_targets, 
 }
 
 }  // namespace gsim
+
+// ------------------------------------------------------------------------------------
+// Direct-sum step that allocates nothing (gs_direct_step_noalloc).
+//
+// Some callers cannot let a library allocate device memory: a host application that owns
+// every device allocation and hands its plugins fixed buffers, or a loop with a fixed
+// memory budget that must not pay for (or be synchronised by) cudaMalloc / cudaFree in
+// the middle of a run.  For them this entry point takes the particle buffers from the
+// caller and keeps its own scratch -- the j-chunk partial sums and the per-tile tickets
+// of k_direct_fast -- in the file-scope device arrays below.  Those arrays exist on every
+// GPU that loads this library and stay allocated until the process exits.
+// ------------------------------------------------------------------------------------
+namespace gsim {
+namespace {
+
+constexpr size_t kNoAllocPartialBytes = 4u << 20;  // j-chunk partials, 4 MiB
+constexpr uint32_t kNoAllocMaxTiles = GS_NOALLOC_MAX_PARTICLES / (kDirectBlock * 2);
+
+static __device__ __align__(256) float4 g_noalloc_partials[kNoAllocPartialBytes / sizeof(float4)];
+static __device__ __align__(256) uint32_t g_noalloc_tickets[kNoAllocMaxTiles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+float4* g_noalloc_partials_addr[kMaxDevices] = {};
+uint32_t* g_noalloc_tickets_addr[kMaxDevices] = {};
+
+// Device addresses of the two arrays on the current device, looked up once per device.
+// The host-side names are stand-ins, not device addresses, so they are never passed to
+// a kernel directly.
+gs_status noalloc_scratch(int dev, float4** partials, uint32_t** tickets) {
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("gs_direct_step_noalloc: device ordinal above 63");
+        return GS_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_partials_addr[dev]) {
+        void* p = nullptr;
+        void* t = nullptr;
+        GS_CUDA(cudaGetSymbolAddress(&p, g_noalloc_partials));
+        GS_CUDA(cudaGetSymbolAddress(&t, g_noalloc_tickets));
+        g_noalloc_partials_addr[dev] = (float4*)p;
+        g_noalloc_tickets_addr[dev] = (uint32_t*)t;
+    }
+    *partials = g_noalloc_partials_addr[dev];
+    *tickets = g_noalloc_tickets_addr[dev];
+    return GS_OK;
+}
+
+}  // namespace
+}  // namespace gsim
+
+extern "C" gs_status gs_direct_step_noalloc(const float* d_pos_in, const float* d_vel_in, const float* d_mass,
+                                            float* d_pos_out, float* d_vel_out, uint64_t n,
+                                            float gravitational_const, float simulation_time, float softening_len,
+                                            void* stream) {
+    using namespace gsim;
+    if (!d_pos_in || !d_vel_in || !d_mass || !d_pos_out || !d_vel_out) {
+        set_error("gs_direct_step_noalloc: NULL buffer");
+        return GS_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0 || n % kAlignment != 0) {
+        set_error("gs_direct_step_noalloc: the particle count must be a positive multiple of 64 "
+                  "(pad with zero-mass particles, as ParticleSystem does)");
+        return GS_ERR_INVALID_ARGUMENT;
+    }
+    if (n > GS_NOALLOC_MAX_PARTICLES) {
+        set_error("gs_direct_step_noalloc: particle count above GS_NOALLOC_MAX_PARTICLES (65536), the size "
+                  "of its built-in scratch; use gs_create / gs_run for larger systems");
+        return GS_ERR_CAPACITY;
+    }
+    int dev = 0;
+    GS_CUDA(cudaGetDevice(&dev));
+    float4* partials = nullptr;
+    uint32_t* tickets = nullptr;
+    gs_status st = noalloc_scratch(dev, &partials, &tickets);
+    if (st != GS_OK) return st;
+
+    const uint32_t n_al = (uint32_t)n;
+    const uint32_t itiles = (n_al + kDirectBlock * 2 - 1) / (kDirectBlock * 2);
+    int chunks = pick_chunks(n_al, 2);
+    const int fit = (int)(kNoAllocPartialBytes / (sizeof(float4) * n_al));  // >= 4 for n <= 65536
+    if (chunks > fit) chunks = fit;
+    uint32_t jchunk = (n_al + chunks - 1) / chunks;
+    jchunk = (jchunk + kDirectTileJ - 1) / kDirectTileJ * kDirectTileJ;
+    chunks = (int)((n_al + jchunk - 1) / jchunk);
+    cudaStream_t s = (cudaStream_t)stream;
+    // the tickets must start at zero; the array keeps whatever the previous call left
+    if (chunks > 1) GS_CUDA(cudaMemsetAsync(tickets, 0, itiles * sizeof(uint32_t), s));
+    const float eps2 = softening_len * softening_len;
+    const float k = simulation_time * gravitational_const;
+    const float hdt = 0.5f * simulation_time;
+    k_direct_fast<2><<<dim3(itiles, chunks), kDirectBlock, 0, s>>>(
+        (const float2*)d_pos_in, (const float2*)d_vel_in, d_mass, (float2*)d_pos_out, (float2*)d_vel_out, nullptr,
+        n_al, chunks, jchunk, eps2, k, hdt, partials, tickets);
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+}

@@ -142,6 +142,30 @@ GS_API gs_status gs_debug_bh_tree(gs_sim* sim, uint32_t* keys, uint32_t* sorted_
                            float* node_mass, uint64_t capacity, uint64_t* tree_records);
 GS_API uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count);
 
+/* One direct-sum step (FAST math) on caller-owned device buffers, allocating nothing.
+ * No counterpart in the reference: it is for callers that cannot let a library allocate
+ * device memory -- a host application that owns every allocation and hands its plugins
+ * fixed buffers, or a loop with a fixed memory budget that must not pay for, or be
+ * synchronised by, cudaMalloc / cudaFree mid-run.
+ *   - Inputs pos/vel/mass and outputs pos/vel are device arrays of n particles (x,y
+ *     interleaved for pos and vel); n must be a multiple of 64 (pad with zero-mass
+ *     particles at the origin, as ParticleSystem does) and at most
+ *     GS_NOALLOC_MAX_PARTICLES, else GS_ERR_INVALID_ARGUMENT / GS_ERR_CAPACITY.
+ *     Outputs must not alias inputs.
+ *   - Runs on the calling thread's current device, on `stream` (a cudaStream_t, NULL for
+ *     the legacy default stream), asynchronously.
+ *   - Scratch lives in fixed device arrays inside this library (about 4 MiB per GPU that
+ *     loads it, held until the process exits).  The first call on each device looks up
+ *     their device addresses; make that first call before any stream capture.
+ *   - Every call shares those arrays: calls that overlap on the GPU (other streams,
+ *     other threads) race and give wrong results.  Serialise them on one stream. */
+#define GS_NOALLOC_MAX_PARTICLES 65536
+GS_API gs_status gs_direct_step_noalloc(const float* d_pos_in, const float* d_vel_in,
+                                        const float* d_mass, float* d_pos_out, float* d_vel_out,
+                                        uint64_t n, float gravitational_const,
+                                        float simulation_time, float softening_len,
+                                        void* stream);
+
 /* ---- host-only helpers (no GPU) ---- */
 
 /* Generator types: the reference's four presets (ParticleSystem::GenerateType) and the
