@@ -423,6 +423,7 @@ k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, 
           const uint32_t* __restrict__ valid_count, int D, const BHParams* __restrict__ bp,
           const float2* __restrict__ pos, const float* __restrict__ mass, float4* __restrict__ rec,
           uint32_t* __restrict__ skip, uint32_t* __restrict__ nend, uint64_t cap, uint32_t n_al,
+          uint32_t* __restrict__ level_count, uint32_t* __restrict__ level_slots, uint32_t level_cap,
           int* __restrict__ err) {
     const uint32_t nv = *valid_count;
     const float radius0 = bp->radius0;
@@ -453,6 +454,10 @@ k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, 
             skip[at] = end + E[end] - at;
             nend[at] = end;
             lo = end;
+            // this level's node list (any order: every node of a level is summed independently)
+            const uint32_t li = atomicAdd(&level_count[d], 1u);
+            if (li < level_cap) level_slots[(size_t)d * level_cap + li] = s;
+            else atomicOr(err, kErrTree);
         }
     }
 }
@@ -460,53 +465,143 @@ k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, 
 // ------------------------------------------------------------------------------------
 // bottom-up sums for one level
 // ------------------------------------------------------------------------------------
+// One child of a level-d cell starting at sorted slot t: a node of level d+1 (its record
+// index, mass, centre of mass and end slot) or a single particle (its leaf record).
+struct Child {
+    float m, x, y;
+    uint32_t rec;     // record index (node or particle leaf)
+    uint32_t next;    // first slot after the child
+    bool node;
+};
+
+__device__ __forceinline__ Child child_at(const uint32_t* skey, const uint32_t* E, const float4* rec,
+                                          const uint32_t* nend, uint32_t t, int d, uint32_t nv, int D) {
+    Child c;
+    const int cmin = slot_dmin(skey, t, D), cmax = slot_dmax(skey, t, nv, D);
+    if (d < D && cmin <= d + 1 && d + 1 <= cmax) {
+        c.rec = t + E[t] + (uint32_t)(d + 1 - cmin);
+        c.node = true;
+        c.next = nend[c.rec];
+    } else {
+        const int ce = cmax >= cmin ? cmax - cmin + 1 : 0;
+        c.rec = t + E[t] + (uint32_t)ce;
+        c.node = false;
+        c.next = t + 1;
+    }
+    const float4 q = rec[c.rec];
+    c.x = q.x;
+    c.y = q.y;
+    c.m = q.z;
+    return c;
+}
+
+__device__ __forceinline__ uint32_t compact_bits(uint32_t v) {  // inverse of spread_bits
+    v &= 0x55555555u;
+    v = (v | (v >> 1)) & 0x33333333u;
+    v = (v | (v >> 2)) & 0x0f0f0f0fu;
+    v = (v | (v >> 4)) & 0x00ff00ffu;
+    v = (v | (v >> 8)) & 0x0000ffffu;
+    return v;
+}
+
+// Squared distance from the centre of mass to the farthest corner of the level-d cell
+// holding `key` (the accurate mode's opening radius).  FP64, like the CPU restatement.
+__device__ double cell_bmax2(int bbox_mode, const BHParams& bp, int D, int d, uint32_t key, float cx, float cy) {
+    const uint32_t pre = key >> (2 * (D - d));
+    const double ix = (double)compact_bits(pre), iy = (double)compact_bits(pre >> 1);
+    double x0, y0, side;
+    if (bbox_mode) {
+        const double w = (double)(1u << (D - d));
+        side = w / (double)bp.scale;
+        x0 = (double)bp.cx + (ix * w - (double)(1u << (D - 1))) / (double)bp.scale;
+        y0 = (double)bp.cy + (iy * w - (double)(1u << (D - 1))) / (double)bp.scale;
+    } else {
+        side = 2.0 * (double)kSimSize / (double)(1u << d);
+        x0 = -(double)kSimSize + ix * side;
+        y0 = -(double)kSimSize + iy * side;
+    }
+    const double ax = fabs((double)cx - x0), bx = fabs(x0 + side - (double)cx);
+    const double ay = fabs((double)cy - y0), by = fabs(y0 + side - (double)cy);
+    const double mx = ax > bx ? ax : bx, my = ay > by ? ay : by;
+    return mx * mx + my * my;
+}
+
+// Child descriptors of an internal record (group walk): up to four children in Morton
+// order, each a record index with kKidLeaf set for a particle leaf, kKidNone when absent;
+// a finest-level cell stores {kKidFinest, first leaf, leaf count, -}.
+constexpr uint32_t kKidNone = 0xFFFFFFFFu;
+constexpr uint32_t kKidFinest = 0xFFFFFFFEu;
+constexpr uint32_t kKidLeaf = 0x80000000u;
+
+// Bottom-up sums for the nodes of level d (children were finished by the previous launch):
+// mass and mass moments in child order (TreeInitShader.comp:78-80), centre of mass
+// (TreeMoveShader.comp:66-67); with `quad`, second central moments about the centre of
+// mass; with `safe`, the safe opening radius; with `kids`, the child descriptors.
 __global__ void __launch_bounds__(256)
 k_sums_level(int d, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
              const uint32_t* __restrict__ valid_count, int D, float4* __restrict__ rec,
-             const uint32_t* __restrict__ nend, float2* __restrict__ msum, uint32_t cap) {
+             const uint32_t* __restrict__ nend, float2* __restrict__ msum, uint32_t cap,
+             float4* __restrict__ quad, uint4* __restrict__ kids, int safe, int bbox_mode,
+             const BHParams* __restrict__ bpp, const uint32_t* __restrict__ level_count,
+             const uint32_t* __restrict__ level_slots, uint32_t level_cap) {
     const uint32_t nv = *valid_count;
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += gridDim.x * blockDim.x) {
-        const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
-        if (d < dmin || d > dmax) continue;
+    const uint32_t cnt = min(level_count[d], level_cap);
+    const uint32_t* slots = level_slots + (size_t)d * level_cap;
+    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < cnt; li += gridDim.x * blockDim.x) {
+        const uint32_t s = slots[li];
+        const int dmin = slot_dmin(skey, s, D);
         const uint32_t at = s + E[s] + (uint32_t)(d - dmin);
         if (at >= cap) continue;  // only after a failed scan (error flag already set)
         const uint32_t end = nend[at];
         float sx = 0.0f, sy = 0.0f, sm = 0.0f;
-        if (d == D) {  // finest cell: its particle leaves follow the node record
-            for (uint32_t t = 0; t < end - s; ++t) {
-                float4 q = rec[at + 1 + t];
-                sx = __fadd_rn(sx, __fmul_rn(q.x, q.z));
-                sy = __fadd_rn(sy, __fmul_rn(q.y, q.z));
-                sm = __fadd_rn(sm, q.z);
+        uint32_t kid[4] = {kKidNone, kKidNone, kKidNone, kKidNone};
+        int nk = 0;
+        for (uint32_t t = s; t < end;) {  // children in Morton order
+            const Child c = child_at(skey, E, rec, nend, t, d, nv, D);
+            if (c.node) {
+                const float2 m2 = msum[c.rec];
+                sx = __fadd_rn(sx, m2.x);
+                sy = __fadd_rn(sy, m2.y);
+            } else {
+                sx = __fadd_rn(sx, __fmul_rn(c.x, c.m));
+                sy = __fadd_rn(sy, __fmul_rn(c.y, c.m));
             }
-        } else {  // children in Morton order: nodes of level d+1 or single particles
-            uint32_t t = s;
-            while (t < end) {
-                const int cmin = slot_dmin(skey, t, D), cmax = slot_dmax(skey, t, nv, D);
-                if (cmin <= d + 1 && d + 1 <= cmax) {
-                    const uint32_t ch = t + E[t] + (uint32_t)(d + 1 - cmin);
-                    const float2 m2 = msum[ch];
-                    sx = __fadd_rn(sx, m2.x);
-                    sy = __fadd_rn(sy, m2.y);
-                    sm = __fadd_rn(sm, rec[ch].z);
-                    t = nend[ch];
-                } else {
-                    const int ce = cmax >= cmin ? cmax - cmin + 1 : 0;
-                    const float4 q = rec[t + E[t] + (uint32_t)ce];
-                    sx = __fadd_rn(sx, __fmul_rn(q.x, q.z));
-                    sy = __fadd_rn(sy, __fmul_rn(q.y, q.z));
-                    sm = __fadd_rn(sm, q.z);
-                    t += 1;
-                }
-            }
+            sm = __fadd_rn(sm, c.m);
+            if (nk < 4) kid[nk] = c.node ? c.rec : (c.rec | kKidLeaf);
+            ++nk;
+            t = c.next;
         }
         msum[at] = make_float2(sx, sy);
         float cx = sx, cy = sy;
-        if (sm != 0.0f) {  // TreeMoveShader.comp:66-67
+        if (sm != 0.0f) {
             cx = __fdiv_rn(sx, sm);
             cy = __fdiv_rn(sy, sm);
         }
-        const float r = rec[at].w;
+        float r = rec[at].w;
+        if (quad) {  // second central moments, parallel-axis sum over the children in order
+            float qxx = 0.0f, qxy = 0.0f, qyy = 0.0f;
+            for (uint32_t t = s; t < end;) {
+                const Child c = child_at(skey, E, rec, nend, t, d, nv, D);
+                if (c.node) {
+                    const float4 q = quad[c.rec];
+                    qxx = __fadd_rn(qxx, q.x);
+                    qxy = __fadd_rn(qxy, q.y);
+                    qyy = __fadd_rn(qyy, q.z);
+                }
+                const float ddx = __fsub_rn(c.x, cx), ddy = __fsub_rn(c.y, cy);
+                const float tx = __fmul_rn(c.m, ddx);
+                qxx = __fmaf_rn(tx, ddx, qxx);
+                qxy = __fmaf_rn(tx, ddy, qxy);
+                qyy = __fmaf_rn(__fmul_rn(c.m, ddy), ddy, qyy);
+                t = c.next;
+            }
+            quad[at] = make_float4(qxx, qxy, qyy, 0.0f);
+        }
+        if (kids) {
+            if (d == D) kids[at] = make_uint4(kKidFinest, at + 1, end - s, 0u);  // all children are leaves
+            else kids[at] = make_uint4(kid[0], kid[1], kid[2], kid[3]);
+        }
+        if (safe) r = (float)cell_bmax2(bbox_mode, *bpp, D, d, skey[s], cx, cy);
         rec[at] = make_float4(cx, cy, sm, r);
     }
 }
@@ -578,6 +673,253 @@ k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, 
     vel_out[i] = make_float2(nvx, nvy);
 }
 
+// ------------------------------------------------------------------------------------
+// accurate-mode traversal (no counterpart in the reference): the 32 particles of a warp
+// share one walk; 32 records are tested at once (one per lane) against the bounding box
+// of the group; accepted records and runs of particle leaves become interaction items;
+// all lanes then sum the items as a dense stream (quadrupole term for nodes).
+// ------------------------------------------------------------------------------------
+constexpr int kGroupWarps = 4;
+constexpr int kStackCap = 2048;   // records still to test; depth bound (levels x 128) stays below
+constexpr int kItemCap = 256;     // interaction items between evaluations
+constexpr uint32_t kItemNode = 0x80000000u;
+
+template <bool EXACT>
+__device__ __forceinline__ float inv_sqrt(float d2) {
+    return EXACT ? __fdiv_rn(1.0f, __fsqrt_rn(d2)) : rsqrtf(d2);
+}
+
+template <bool EXACT>
+__device__ __forceinline__ void monopole(float4 q, float px, float py, float eps2, float& ax, float& ay) {
+    const float dx = q.x - px, dy = q.y - py;
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
+    const float r = inv_sqrt<EXACT>(d2);
+    const float sc = ((q.z * r) * r) * r;
+    ax = fmaf(dx, sc, ax);
+    ay = fmaf(dy, sc, ay);
+}
+
+template <bool EXACT>
+__device__ __forceinline__ void quadrupole(float4 q, float4 m2, float px, float py, float eps2, float& ax, float& ay) {
+    const float dx = q.x - px, dy = q.y - py;
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
+    const float r = inv_sqrt<EXACT>(d2);
+    const float r2 = r * r;
+    const float r3 = r2 * r;
+    const float r5 = r3 * r2;
+    const float r7 = r5 * r2;
+    const float srx = fmaf(m2.x, dx, m2.y * dy);
+    const float sry = fmaf(m2.y, dx, m2.z * dy);
+    const float u = fmaf(dx, srx, dy * sry);
+    const float T = m2.x + m2.z;
+    const float coef = fmaf(7.5f * u, r7, fmaf(-1.5f * T, r5, q.z * r3));
+    const float t3 = 3.0f * r5;
+    ax = fmaf(-t3, srx, fmaf(dx, coef, ax));
+    ay = fmaf(-t3, sry, fmaf(dy, coef, ay));
+}
+
+struct GroupSmem {
+    uint32_t stack[kStackCap];
+    uint32_t it_start[kItemCap];
+    uint32_t it_count[kItemCap];  // record count, kItemNode for a node item
+    float4 rec[32];               // gathered records of one evaluation chunk
+    float4 quad[32];
+    uint32_t off[32];             // exclusive record offsets of the items of a batch
+};
+
+// Sum the n_items items in order: batches of 32 items, flattened 32 records at a time;
+// lane l gathers record l of the chunk (coalesced for leaf ranges), every lane then
+// accumulates the chunk in order from shared memory.
+template <bool EXACT, bool QUAD>
+__device__ __forceinline__ void eval_items(GroupSmem& g, uint32_t n_items, const float4* __restrict__ rec,
+                                           const float4* __restrict__ quad, float px, float py, float eps2,
+                                           float& ax, float& ay, int lane) {
+    for (uint32_t b0 = 0; b0 < n_items; b0 += 32) {
+        const uint32_t nb = min(n_items - b0, 32u);
+        const uint32_t cnt = lane < (int)nb ? (g.it_count[b0 + lane] & ~kItemNode) : 0u;
+        uint32_t x = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
+        g.off[lane] = x - cnt;
+        __syncwarp();
+        for (uint32_t f0 = 0; f0 < total; f0 += 32) {
+            const uint32_t f = f0 + lane;
+            uint32_t node = 0;
+            if (f < total) {  // item j of this batch holding flat record f: last j with off[j] <= f
+                uint32_t lo = 0, hi = nb - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (g.off[mid] <= f) lo = mid;
+                    else hi = mid - 1;
+                }
+                const uint32_t c = g.it_count[b0 + lo];
+                const uint32_t r = g.it_start[b0 + lo] + (f - g.off[lo]);
+                node = c & kItemNode;
+                float4 q = __ldg(&rec[r]);
+                if (QUAD && node) g.quad[lane] = __ldg(&quad[r]);
+                q.w = __uint_as_float(node);  // the opening radius is not needed here: reuse w as the flag
+                g.rec[lane] = q;
+            }
+            __syncwarp();
+            const uint32_t m = min(total - f0, 32u);
+            for (uint32_t j = 0; j < m; ++j) {
+                const float4 q = g.rec[j];
+                if (QUAD && __float_as_uint(q.w)) quadrupole<EXACT>(q, g.quad[j], px, py, eps2, ax, ay);
+                else monopole<EXACT>(q, px, py, eps2, ax, ay);
+            }
+            __syncwarp();
+        }
+    }
+}
+
+template <bool EXACT, bool QUAD, bool COUNT>
+__global__ void __launch_bounds__(kGroupWarps * 32)
+k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts,
+              const float4* __restrict__ rec, const uint32_t* __restrict__ skip, const float4* __restrict__ quad,
+              const uint4* __restrict__ kids, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
+              float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
+              uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
+              unsigned long long* __restrict__ stat, int* __restrict__ err) {
+    __shared__ GroupSmem smem[kGroupWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    GroupSmem& g = smem[warp];
+    const uint32_t group = blockIdx.x * kGroupWarps + warp;
+    const uint32_t nv = counts[0];
+    const uint32_t T = min(nv + counts[1], cap);
+    if (group * 32 >= nv || T == 0) return;
+    const uint32_t s = group * 32 + lane;
+    const uint32_t i = s < nv ? sidx[s] : 0u;
+    const bool valid = s < nv && i < n_al;
+    const float2 p = valid ? pos_in[i] : make_float2(0.0f, 0.0f);
+    float gx0 = valid ? p.x : INFINITY, gx1 = valid ? p.x : -INFINITY;
+    float gy0 = valid ? p.y : INFINITY, gy1 = valid ? p.y : -INFINITY;
+    for (int o = 16; o; o >>= 1) {
+        gx0 = fminf(gx0, __shfl_xor_sync(0xffffffffu, gx0, o));
+        gx1 = fmaxf(gx1, __shfl_xor_sync(0xffffffffu, gx1, o));
+        gy0 = fminf(gy0, __shfl_xor_sync(0xffffffffu, gy0, o));
+        gy1 = fmaxf(gy1, __shfl_xor_sync(0xffffffffu, gy1, o));
+    }
+    float ax = 0.0f, ay = 0.0f;
+    unsigned long long n_int = 0, n_test = 0;
+    uint32_t size = 0, n_items = 0;
+    if (skip[0] == 1u) {  // a single particle: the root is its leaf
+        if (lane == 0) {
+            g.it_start[0] = 0u;
+            g.it_count[0] = 1u;
+        }
+        n_items = 1;
+    } else {
+        if (lane == 0) g.stack[0] = 0u;
+        size = 1;
+    }
+    __syncwarp();
+
+    while (size > 0) {
+        if (n_items > (uint32_t)(kItemCap - 64)) {
+            eval_items<EXACT, QUAD>(g, n_items, rec, quad, p.x, p.y, eps2, ax, ay, lane);
+            n_items = 0;
+        }
+        const uint32_t np = min(size, 32u);
+        const uint32_t base = size - np;
+        const bool act = lane < (int)np;
+        const uint32_t n = act ? g.stack[base + lane] : 0u;
+        __syncwarp();
+        size = base;
+        if (COUNT) n_test += np;
+        uint32_t a0 = 0, c0 = 0, a1 = 0, c1 = 0, ni = 0;
+        uint32_t pu0 = 0, pu1 = 0, pu2 = 0, pu3 = 0, npu = 0;
+        if (act) {  // every stacked record is an internal node
+            const float4 q = rec[n];
+            const uint4 kd = kids[n];
+            const float ex = fmaxf(fmaxf(gx0 - q.x, q.x - gx1), 0.0f);
+            const float ey = fmaxf(fmaxf(gy0 - q.y, q.y - gy1), 0.0f);
+            const float d2 = fmaf(ex, ex, fmaf(ey, ey, eps2));
+            if (q.w <= d2 * theta2) {
+                a0 = n;
+                c0 = 1u | kItemNode;
+                ni = 1;
+            } else if (kd.x == kKidFinest) {
+                a0 = kd.y;
+                c0 = kd.z;
+                ni = 1;
+            } else {
+                const uint32_t kk[4] = {kd.x, kd.y, kd.z, kd.w};
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const uint32_t c = kk[t];
+                    if (c == kKidNone) continue;
+                    if (c & kKidLeaf) {
+                        const uint32_t r = c & ~kKidLeaf;
+                        if (ni == 1 && a0 + c0 == r) ++c0;        // extend the open run
+                        else if (ni == 2 && a1 + c1 == r) ++c1;
+                        else if (ni == 0) { a0 = r; c0 = 1; ni = 1; }
+                        else { a1 = r; c1 = 1; ni = 2; }
+                    } else {
+                        if (npu == 0) pu0 = c;
+                        else if (npu == 1) pu1 = c;
+                        else if (npu == 2) pu2 = c;
+                        else pu3 = c;
+                        ++npu;
+                    }
+                }
+            }
+        }
+        // warp-wide offsets in lane order
+        uint32_t x = ni, y = npu;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t xo = __shfl_up_sync(0xffffffffu, x, o), yo = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= o) {
+                x += xo;
+                y += yo;
+            }
+        }
+        const uint32_t ioff = x - ni, poff = y - npu;
+        const uint32_t itot = __shfl_sync(0xffffffffu, x, 31);
+        uint32_t ptot = __shfl_sync(0xffffffffu, y, 31);
+        if (size + ptot > (uint32_t)kStackCap) {  // beyond the depth bound: report, do not overrun
+            if (lane == 0) atomicOr(err, kErrTree);
+            ptot = 0;
+            npu = 0;
+        }
+        if (ni > 0) {
+            g.it_start[n_items + ioff] = a0;
+            g.it_count[n_items + ioff] = c0;
+        }
+        if (ni > 1) {
+            g.it_start[n_items + ioff + 1] = a1;
+            g.it_count[n_items + ioff + 1] = c1;
+        }
+        if (COUNT) n_int += (ni > 0 ? (c0 & ~kItemNode) : 0u) + (ni > 1 ? c1 : 0u);
+        uint32_t* dst = g.stack + size + poff;
+        if (npu > 0) dst[0] = pu0;
+        if (npu > 1) dst[1] = pu1;
+        if (npu > 2) dst[2] = pu2;
+        if (npu > 3) dst[3] = pu3;
+        n_items += itot;
+        size += ptot;
+        __syncwarp();
+    }
+    eval_items<EXACT, QUAD>(g, n_items, rec, quad, p.x, p.y, eps2, ax, ay, lane);
+    if (COUNT) {
+        if (skip[0] == 1u && lane == 0) n_int += 1;
+        for (int o = 16; o; o >>= 1) n_int += __shfl_xor_sync(0xffffffffu, n_int, o);
+        const unsigned long long nval = __popc(__ballot_sync(0xffffffffu, valid));
+        if (lane == 0) {
+            atomicAdd(&stat[0], n_int * nval);
+            atomicAdd(&stat[1], n_test);
+        }
+    }
+    if (!valid) return;
+    if (acc_rec) acc_rec[i] = make_float2(ax, ay);
+    const float2 v = vel_in[i];
+    const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);
+    pos_out[i] = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
+    vel_out[i] = make_float2(nvx, nvy);
+}
+
 int grid_for(uint64_t n, int threads) {
     uint64_t b = (n + threads - 1) / threads;
     if (b > 152ull * 16) b = 152ull * 16;
@@ -593,7 +935,8 @@ uint64_t bh_capacity(int box_mode, uint64_t n_al) {
 }
 
 // counters layout inside the zeroed block
-enum { kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrCount = 12 };
+enum { kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrLevel = 12,
+       kCtrCount = 32 };
 
 cudaError_t bh_alloc(gs_sim* s) {
     BHWork& w = s->bh;
@@ -619,11 +962,19 @@ cudaError_t bh_alloc(gs_sim* s) {
     GS_ALLOC(w.skip, (w.cap + 32) * sizeof(uint32_t));
     GS_ALLOC(w.nend, w.cap * sizeof(uint32_t));
     GS_ALLOC(w.msum, w.cap * sizeof(float2));
+    w.level_cap = (uint32_t)(n / 2 + 1);  // at most N/2 cells of one level hold two particles
+    GS_ALLOC(w.level_slots, (size_t)(w.depth + 1) * w.level_cap * sizeof(uint32_t));
+    if (s->p.flags & GS_FLAG_GROUP_WALK) GS_ALLOC(w.kids, w.cap * sizeof(uint4));
+    if (s->p.flags & GS_FLAG_QUADRUPOLE) {
+        GS_ALLOC(w.quad, w.cap * sizeof(float4));
+        e = cudaMemset(w.quad, 0, w.cap * sizeof(float4));
+        if (e != cudaSuccess) return e;
+    }
     GS_ALLOC(w.bbox_part, kBBoxBlocks * 4 * sizeof(float));
     GS_ALLOC(w.params, sizeof(BHParams));
     // one block cleared per step: hist | counters | sort status | scan status
     const size_t hist_b = 4 * 256 * sizeof(uint32_t);
-    const size_t ctr_b = 16 * sizeof(uint32_t);
+    const size_t ctr_b = kCtrCount * sizeof(uint32_t);
     const size_t sort_b = (size_t)w.passes * w.sort_tiles * 256 * sizeof(uint32_t);
     const size_t scan_b = (size_t)w.scan_tiles * sizeof(uint32_t);
     w.zero_bytes = hist_b + ctr_b + sort_b + scan_b;
@@ -658,6 +1009,12 @@ void bh_free(gs_sim* s) {
     cudaFree(w.skip);
     cudaFree(w.nend);
     cudaFree(w.msum);
+    cudaFree(w.quad);
+    cudaFree(w.kids);
+    cudaFree(w.level_slots);
+    w.kids = nullptr;
+    w.level_slots = nullptr;
+    w.quad = nullptr;
     cudaFree(w.bbox_part);
     cudaFree(w.params);
     cudaFree(w.zero_base);
@@ -715,13 +1072,16 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     stage_end(s, kStageScan, profile);
     stage_begin(s, kStageRecords, profile);
     k_records<<<grid_for(n, 256), 256, 0, st>>>(skey, sidx, w.E, ctr + kCtrValid, w.depth, w.params, s->pos[in],
-                                                s->mass[in], w.rec, w.skip, w.nend, w.cap, n, s->d_err);
+                                                s->mass[in], w.rec, w.skip, w.nend, w.cap, n, ctr + kCtrLevel,
+                                                w.level_slots, w.level_cap, s->d_err);
     count_launch(s);
     stage_end(s, kStageRecords, profile);
     stage_begin(s, kStageSums, profile);
     for (int d = w.depth; d >= 0; --d)
         k_sums_level<<<grid_for(n, 256), 256, 0, st>>>(d, skey, w.E, ctr + kCtrValid, w.depth, w.rec, w.nend, w.msum,
-                                                        (uint32_t)w.cap);
+                                                        (uint32_t)w.cap, w.quad, w.kids,
+                                                        (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0, bbox ? 1 : 0,
+                                                        w.params, ctr + kCtrLevel, w.level_slots, w.level_cap);
     count_launch(s, w.depth + 1);
     stage_end(s, kStageSums, profile);
     stage_begin(s, kStageForce, profile);
@@ -735,13 +1095,28 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     k_force<E_, C_><<<blocks, kForceWarps * 32, 0, st>>>(sidx, ctr + kCtrValid, w.rec, w.skip, s->pos[in],    \
                                                          s->vel[in], s->pos[out], s->vel[out], s->acc, n, s->eps2, \
                                                          s->theta2, k, hdt, (uint32_t)w.cap, stat)
-    if (exact) {
+#define GS_GROUP(E_, Q_, C_)                                                                                    \
+    k_force_group<E_, Q_, C_><<<(int)((n / 32 + kGroupWarps - 1) / kGroupWarps), kGroupWarps * 32, 0, st>>>(    \
+        sidx, ctr + kCtrValid, w.rec, w.skip, w.quad, w.kids, s->pos[in], s->vel[in], s->pos[out], s->vel[out],      \
+        s->acc, n,                                                                                                   \
+        s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err)
+    if (s->p.flags & GS_FLAG_GROUP_WALK) {
+        const bool quad = w.quad != nullptr;
+        if (exact) {
+            if (quad) { if (count) GS_GROUP(true, true, true); else GS_GROUP(true, true, false); }
+            else { if (count) GS_GROUP(true, false, true); else GS_GROUP(true, false, false); }
+        } else {
+            if (quad) { if (count) GS_GROUP(false, true, true); else GS_GROUP(false, true, false); }
+            else { if (count) GS_GROUP(false, false, true); else GS_GROUP(false, false, false); }
+        }
+    } else if (exact) {
         if (count) GS_FORCE(true, true);
         else GS_FORCE(true, false);
     } else {
         if (count) GS_FORCE(false, true);
         else GS_FORCE(false, false);
     }
+#undef GS_GROUP
 #undef GS_FORCE
     count_launch(s);
     stage_end(s, kStageForce, profile);
@@ -750,7 +1125,8 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
 
 // Host readback of the most recent tree (not on the hot path).
 gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
-                        float* node_pos, float* node_mass, uint64_t capacity, uint64_t* tree_records) {
+                        float* node_pos, float* node_mass, float* node_quad, uint64_t capacity,
+                        uint64_t* tree_records) {
     BHWork& w = s->bh;
     const uint64_t n = s->n_al;
     uint32_t ctr[kCtrCount];
@@ -792,6 +1168,26 @@ gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_
         GS_CUDA(e1);
     }
     if (m && node_skip) GS_CUDA(cudaMemcpy(node_skip, w.skip, m * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (m && node_quad) {
+        if (!w.quad) {
+            std::memset(node_quad, 0, 3 * m * sizeof(float));
+        } else {
+            float4* hq = new float4[m];
+            uint32_t* hs = new uint32_t[m];
+            cudaError_t e1 = cudaMemcpy(hq, w.quad, m * sizeof(float4), cudaMemcpyDeviceToHost);
+            if (e1 == cudaSuccess) e1 = cudaMemcpy(hs, w.skip, m * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+            if (e1 == cudaSuccess)
+                for (uint64_t q = 0; q < m; ++q) {  // a particle leaf has no spread: zero moments
+                    const bool leaf = hs[q] == 1u;
+                    node_quad[3 * q] = leaf ? 0.0f : hq[q].x;
+                    node_quad[3 * q + 1] = leaf ? 0.0f : hq[q].y;
+                    node_quad[3 * q + 2] = leaf ? 0.0f : hq[q].z;
+                }
+            delete[] hq;
+            delete[] hs;
+            GS_CUDA(e1);
+        }
+    }
     return GS_OK;
 }
 

@@ -59,13 +59,18 @@ struct BHWork {
     uint32_t* hist = nullptr;          // [4][256] digit counts
     uint32_t* sort_status = nullptr;   // [passes][tiles][256]
     uint32_t* counters = nullptr;      // [0..3] sort tile tickets, [4] scan ticket, [5] bbox ticket,
-                                       // [6] valid count, [7] internal count, [8..9] interactions
+                                       // [6] valid count, [7] internal count, [8..11] interaction
+                                       // and test counts (2 x u64), [12..27] nodes per level
     uint32_t* scan_status = nullptr;   // [scan tiles]
     uint32_t* E = nullptr;             // [N_al + 1]
     float4* rec = nullptr;             // [cap + 32]
     uint32_t* skip = nullptr;          // [cap + 32]
     uint32_t* nend = nullptr;          // [cap]
     float2* msum = nullptr;            // [cap]
+    float4* quad = nullptr;            // [cap] {sxx, sxy, syy, -} (GS_FLAG_QUADRUPOLE)
+    uint4* kids = nullptr;             // [cap] child descriptors (GS_FLAG_GROUP_WALK)
+    uint32_t* level_slots = nullptr;   // [depth+1][level_cap] slots that start a node of that level
+    uint32_t level_cap = 0;
     float* bbox_part = nullptr;        // [blocks][4]
     BHParams* params = nullptr;        // device
     uint32_t sort_tiles = 0, scan_tiles = 0;

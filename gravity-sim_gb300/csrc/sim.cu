@@ -42,7 +42,8 @@ void stage_end(gs_sim* s, int stage, bool profile) {
 }
 
 gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
-                        float* node_pos, float* node_mass, uint64_t capacity, uint64_t* tree_records);
+                        float* node_pos, float* node_mass, float* node_quad, uint64_t capacity,
+                        uint64_t* tree_records);
 gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits);
 
 }  // namespace gsim
@@ -52,6 +53,7 @@ using namespace gsim;
 namespace {
 
 constexpr uint64_t kMaxParticles = 1ull << 28;
+constexpr uint64_t kMaxBarnesHutParticles = 1ull << 26;  // keeps record indices below 2^31
 constexpr uint64_t kDefaultTimeoutNs = 600ull * 1000000000ull;
 
 gs_status invalid(const char* msg) {
@@ -204,8 +206,13 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
         return invalid("gs_create: invalid box_mode");
     if (params->math_mode != GS_MATH_FAST && params->math_mode != GS_MATH_REFERENCE)
         return invalid("gs_create: invalid math_mode");
-    if (n > kMaxParticles) {
-        set_error("gs_create: particle count above the 2^28 limit of this build");
+    if ((params->flags & GS_FLAG_QUADRUPOLE) && !(params->flags & GS_FLAG_GROUP_WALK))
+        return invalid("gs_create: GS_FLAG_QUADRUPOLE needs GS_FLAG_GROUP_WALK");
+    if ((params->flags & (GS_FLAG_QUADRUPOLE | GS_FLAG_SAFE_RADIUS | GS_FLAG_GROUP_WALK)) &&
+        params->algorithm != GS_BARNES_HUT)
+        return invalid("gs_create: the accurate-mode flags apply to Barnes-Hut only");
+    if (n > kMaxParticles || (params->algorithm == GS_BARNES_HUT && n > kMaxBarnesHutParticles)) {
+        set_error("gs_create: particle count above the limit of this build (2^28 direct sum, 2^26 Barnes-Hut)");
         return GS_ERR_CAPACITY;
     }
     int ndev = 0;
@@ -418,12 +425,14 @@ gs_status gs_accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* targets, d
 }
 
 gs_status gs_debug_bh_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
-                           float* node_pos, float* node_mass, uint64_t capacity, uint64_t* tree_records) {
+                           float* node_pos, float* node_mass, float* node_quad, uint64_t capacity,
+                           uint64_t* tree_records) {
     if (!s) return invalid("gs_debug_bh_tree: sim is NULL");
     if (s->p.algorithm != GS_BARNES_HUT) return invalid("gs_debug_bh_tree: not a Barnes-Hut simulation");
     gs_status st = gs_sync(s, 0);
     if (st != GS_OK) return st;
-    return bh_debug_tree(s, keys, sorted_src, node_skip, node_radius, node_pos, node_mass, capacity, tree_records);
+    return bh_debug_tree(s, keys, sorted_src, node_skip, node_radius, node_pos, node_mass, node_quad, capacity,
+                         tree_records);
 }
 
 }  // extern "C"

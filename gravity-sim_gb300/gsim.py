@@ -16,6 +16,8 @@ DIRECT_SUM, BARNES_HUT = 0, 1
 BOX_FIXED_500, BOX_BOUNDING = 0, 1
 MATH_FAST, MATH_REFERENCE = 0, 1
 FLAG_RECORD_ACCEL, FLAG_PROFILE, FLAG_NO_GRAPH, FLAG_COUNT_INTERACTIONS = 0x1, 0x2, 0x4, 0x8
+FLAG_QUADRUPOLE, FLAG_SAFE_RADIUS, FLAG_GROUP_WALK = 0x10, 0x20, 0x40
+FLAGS_ACCURATE = 0x70
 GEN_RANDOM, GEN_GALAXY, GEN_GALAXY_COLLISION, GEN_SYMMETRICAL_GALAXY_COLLISION = 0, 1, 2, 3
 GEN_UNIFORM_DISK, GEN_SPIRAL, GEN_EXP_DISK_COLLISION = 16, 17, 18
 STAGES = ("bbox", "keys", "sort", "scan", "records", "sums", "force", "direct")
@@ -25,6 +27,7 @@ EXPORTS = (
     "gs_sync", "gs_get_particles", "gs_set_particles", "gs_get_accel", "gs_get_stats", "gs_reset_stats",
     "gs_particle_count", "gs_aligned_particle_count", "gs_stream", "gs_destroy", "gs_accel_f64",
     "gs_debug_bh_tree", "gs_bh_node_capacity", "gs_generate", "gs_read_particles", "gs_write_particles",
+    "gs_direct_step_noalloc",
 )
 
 
@@ -97,7 +100,7 @@ def lib():
     L.gs_destroy.restype = None
     L.gs_accel_f64.argtypes = [sim, C.c_uint32, _UP, _DP]
     L.gs_accel_f64.restype = st
-    L.gs_debug_bh_tree.argtypes = [sim, _UP, _UP, _UP, _FP, _FP, _FP, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.gs_debug_bh_tree.argtypes = [sim, _UP, _UP, _UP, _FP, _FP, _FP, _FP, C.c_uint64, C.POINTER(C.c_uint64)]
     L.gs_debug_bh_tree.restype = st
     L.gs_bh_node_capacity.argtypes = [C.c_int32, C.c_uint64]
     L.gs_bh_node_capacity.restype = C.c_uint64
@@ -251,10 +254,11 @@ class Simulation:
         radius = np.empty(cap, np.float32)
         npos = np.empty((cap, 2), np.float32)
         nmass = np.empty(cap, np.float32)
+        quad = np.empty((cap, 3), np.float32)
         T = C.c_uint64(0)
         _check(lib().gs_debug_bh_tree(self._h, keys.ctypes.data_as(_UP), src.ctypes.data_as(_UP),
-                                      skip.ctypes.data_as(_UP), _fp(radius), _fp(npos), _fp(nmass), cap,
+                                      skip.ctypes.data_as(_UP), _fp(radius), _fp(npos), _fp(nmass), _fp(quad), cap,
                                       C.byref(T)))
         t = T.value
         return dict(keys=keys, sorted_src=src, skip=skip[:t], radius=radius[:t], pos=npos[:t], mass=nmass[:t],
-                    tree_size=t)
+                    quad=quad[:t], tree_size=t)

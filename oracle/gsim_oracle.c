@@ -334,6 +334,8 @@ typedef struct {
     uint64_t* interactions; /* per worker */
     uint64_t* visits;       /* per worker */
     uint32_t stride;        /* walk warps stride*item */
+    int group_walk;         /* ORC_BH_GROUP_WALK semantics */
+    uint32_t* max_stack;    /* per worker */
 } walk_ctx;
 
 static void walk_warp(void* p, uint64_t item, int worker) {
@@ -400,14 +402,140 @@ static void walk_warp(void* p, uint64_t item, int worker) {
     c->visits[worker] += visits;
 }
 
+/* Accurate-mode walk (ORC_BH_GROUP_WALK), for the 32 consecutive sorted slots of one warp:
+ *   - the group box is the bounding box of the group's particles;
+ *   - a LIFO stack starts with the root; each step pops the top min(32, size) records
+ *     (lane j gets stack[size - k + j]) and tests each against the box:
+ *       d2 = ex^2 + ey^2 + eps^2 with (ex, ey) the distance from the box to the centre of
+ *       mass, accepted iff radius <= d2 * theta^2;
+ *   - an accepted record becomes one interaction item; an opened record pushes its
+ *     internal children (in preorder) and turns each run of consecutive particle-leaf
+ *     children into one range item;
+ *   - lanes are handled in order, so items and pushes are in lane order;
+ *   - every particle of the group then sums the items in order (nodes with the
+ *     quadrupole term, leaves as monopoles) and is integrated. */
+#define GROUP_STACK_CAP 2048
+static void group_walk_warp(void* p, uint64_t item, int worker) {
+    const walk_ctx* c = (const walk_ctx*)p;
+    const uint64_t w = item * c->stride;
+    float px[WARP], py[WARP], ax[WARP], ay[WARP];
+    int valid[WARP];
+    int nvalid = 0;
+    float gx0 = INFINITY, gx1 = -INFINITY, gy0 = INFINITY, gy1 = -INFINITY;
+    for (int l = 0; l < WARP; ++l) {
+        uint32_t s = (uint32_t)w * WARP + (uint32_t)l;
+        uint32_t i = c->src[s];
+        valid[l] = i != c->n_al;
+        px[l] = valid[l] ? c->pos_in[2 * i] : 0.0f;
+        py[l] = valid[l] ? c->pos_in[2 * i + 1] : 0.0f;
+        ax[l] = ay[l] = 0.0f;
+        if (valid[l]) {
+            nvalid++;
+            gx0 = fminf(gx0, px[l]);
+            gx1 = fmaxf(gx1, px[l]);
+            gy0 = fminf(gy0, py[l]);
+            gy1 = fmaxf(gy1, py[l]);
+        }
+    }
+    if (!nvalid || !c->tree_size) return;
+    uint32_t stack[GROUP_STACK_CAP + 160];
+    uint32_t size = 1, max_size = 1;
+    stack[0] = 0;
+    uint64_t inter = 0, visits = 0;
+    while (size) {
+        uint32_t np = size < WARP ? size : WARP;
+        uint32_t base = size - np;
+        uint32_t popped[WARP];
+        for (uint32_t j = 0; j < np; ++j) popped[j] = stack[base + j];
+        size = base;
+        for (uint32_t j = 0; j < np; ++j) {
+            const uint32_t n = popped[j];
+            ++visits;
+            const uint32_t sk = c->skip[n];
+            int accept = 1;
+            if (sk > 1) {
+                const float cx = c->npos[2 * n], cy = c->npos[2 * n + 1];
+                float ex = fmaxf(fmaxf(gx0 - cx, cx - gx1), 0.0f);
+                float ey = fmaxf(fmaxf(gy0 - cy, cy - gy1), 0.0f);
+                float d2 = pair_d2(ex, ey, c->eps2);
+                accept = c->radius[n] <= d2 * c->theta2;
+            }
+            if (accept) { /* one item: the record itself */
+                const float nx = c->npos[2 * n], ny = c->npos[2 * n + 1], nm = c->nmass[n];
+                for (int l = 0; l < WARP; ++l) {
+                    if (!valid[l]) continue;
+                    float dx = nx - px[l], dy = ny - py[l];
+                    float d2 = pair_d2(dx, dy, c->eps2);
+                    if (c->quad && sk > 1) {
+                        quad_accumulate(dx, dy, d2, nm, c->quad[3 * n], c->quad[3 * n + 1], c->quad[3 * n + 2],
+                                        &ax[l], &ay[l]);
+                    } else {
+                        float sc = pair_scale(nm, d2);
+                        ax[l] = fmaf(dx, sc, ax[l]);
+                        ay[l] = fmaf(dy, sc, ay[l]);
+                    }
+                }
+                inter += (uint64_t)nvalid;
+                continue;
+            }
+            const uint32_t end = n + sk;
+            uint32_t ch = n + 1;
+            while (ch < end) {
+                if (c->skip[ch] == 1) { /* a run of particle leaves: one range item */
+                    uint32_t r = ch;
+                    while (r < end && c->skip[r] == 1) ++r;
+                    for (uint32_t q = ch; q < r; ++q) {
+                        const float nx = c->npos[2 * q], ny = c->npos[2 * q + 1], nm = c->nmass[q];
+                        for (int l = 0; l < WARP; ++l) {
+                            if (!valid[l]) continue;
+                            float dx = nx - px[l], dy = ny - py[l];
+                            float sc = pair_scale(nm, pair_d2(dx, dy, c->eps2));
+                            ax[l] = fmaf(dx, sc, ax[l]);
+                            ay[l] = fmaf(dy, sc, ay[l]);
+                        }
+                    }
+                    inter += (uint64_t)nvalid * (r - ch);
+                    ch = r;
+                } else {
+                    if (size < GROUP_STACK_CAP + 160) stack[size] = ch;
+                    ++size;
+                    ch += c->skip[ch];
+                }
+            }
+        }
+        if (size > max_size) max_size = size;
+        if (size > GROUP_STACK_CAP) size = GROUP_STACK_CAP; /* reported through max_stack */
+    }
+    for (int l = 0; l < WARP; ++l) {
+        if (!valid[l]) continue;
+        uint32_t i = c->src[(uint32_t)w * WARP + (uint32_t)l];
+        float vx = c->vel_in[2 * i], vy = c->vel_in[2 * i + 1];
+        float nvx = fmaf(ax[l], c->k, vx), nvy = fmaf(ay[l], c->k, vy);
+        c->pos_out[2 * i] = fmaf(vx + nvx, c->hdt, px[l]);
+        c->pos_out[2 * i + 1] = fmaf(vy + nvy, c->hdt, py[l]);
+        c->vel_out[2 * i] = nvx;
+        c->vel_out[2 * i + 1] = nvy;
+    }
+    c->interactions[worker] += inter;
+    c->visits[worker] += visits;
+    if (max_size > c->max_stack[worker]) c->max_stack[worker] = max_size;
+}
+
 static void run_walk(walk_ctx* c, int nthreads, orc_bh_out* out) {
     uint64_t inter[256] = {0}, vis[256] = {0};
+    uint32_t mstack[256] = {0};
     c->interactions = inter;
     c->visits = vis;
+    c->max_stack = mstack;
     c->stride = out && out->walk_stride > 1 ? out->walk_stride : 1;
     uint64_t warps = c->n_al / WARP;
     double t0 = now_seconds();
-    parallel_for(nthreads, (warps + c->stride - 1) / c->stride, 4, walk_warp, c);
+    parallel_for(nthreads, (warps + c->stride - 1) / c->stride, 4, c->group_walk ? group_walk_warp : walk_warp, c);
+    if (out) {
+        out->max_stack = 0;
+        for (int t = 0; t < 256; ++t)
+            if (mstack[t] > out->max_stack) out->max_stack = mstack[t];
+    }
     if (out) out->walk_seconds = now_seconds() - t0;
     if (out) {
         out->interactions = 0;
@@ -859,6 +987,7 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
     wc.npos = npos;
     wc.nmass = nmass;
     wc.quad = quad;
+    wc.group_walk = (flags & ORC_BH_GROUP_WALK) != 0;
     wc.tree_size = tree_size;
     wc.src = src;
     wc.n_al = n_al;

@@ -69,6 +69,7 @@ typedef struct orc_bh_out {
     float box_center_x, box_center_y, box_scale, box_radius0;
     double build_seconds;    /* keys, sort and tree (single thread) */
     double walk_seconds;     /* force walk + integration (nthreads) */
+    uint32_t max_stack;      /* deepest group-walk stack seen (ORC_BH_GROUP_WALK) */
 } orc_bh_out;
 
 /* Direct sum, SimShader.comp order: for every i, sum j = 0 .. n-1 in order. */
@@ -103,6 +104,7 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
  *                       the particle is never accepted for theta <= 1 */
 #define ORC_BH_QUADRUPOLE 1
 #define ORC_BH_SAFE_RADIUS 2
+#define ORC_BH_GROUP_WALK 4  /* box-tested 32-wide stack walk, see group_walk_warp */
 int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in, float* vel_in,
                           float* mass_in, float* pos_out, float* vel_out, float* mass_out,
                           float dt, float G, float eps2, float theta2, orc_bh_out* out,

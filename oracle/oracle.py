@@ -15,8 +15,8 @@ import numpy as np
 from . import build as _build
 
 BOX_FIXED_500, BOX_BOUNDING = 0, 1
-QUADRUPOLE, SAFE_RADIUS = 1, 2
-ACCURATE = QUADRUPOLE | SAFE_RADIUS
+QUADRUPOLE, SAFE_RADIUS, GROUP_WALK = 1, 2, 4
+ACCURATE = QUADRUPOLE | SAFE_RADIUS | GROUP_WALK
 KEY_REMOVED = 0xFFFFFFFF
 _FP = C.POINTER(C.c_float)
 _UP = C.POINTER(C.c_uint32)
@@ -30,7 +30,8 @@ class BHOut(C.Structure):
                 ("tree_size", C.c_uint64), ("valid_count", C.c_uint64), ("internal_count", C.c_uint64),
                 ("interactions", C.c_uint64), ("warp_visits", C.c_uint64),
                 ("box_center_x", C.c_float), ("box_center_y", C.c_float), ("box_scale", C.c_float),
-                ("box_radius0", C.c_float), ("build_seconds", C.c_double), ("walk_seconds", C.c_double)]
+                ("box_radius0", C.c_float), ("build_seconds", C.c_double), ("walk_seconds", C.c_double),
+                ("max_stack", C.c_uint32)]
 
 
 _lib = None
@@ -176,7 +177,7 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
             res[k] = res[k][:t]
     res.update(tree_size=t, valid_count=out.valid_count, internal_count=out.internal_count,
                interactions=out.interactions, warp_visits=out.warp_visits,
-               build_seconds=out.build_seconds, walk_seconds=out.walk_seconds,
+               build_seconds=out.build_seconds, walk_seconds=out.walk_seconds, max_stack=out.max_stack,
                box=(out.box_center_x, out.box_center_y, out.box_scale, out.box_radius0))
     return res
 

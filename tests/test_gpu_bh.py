@@ -135,3 +135,69 @@ def test_config2_full_size_properties(gs, orc, box):
     # inherently coarse (tens of percent); hardware rsqrt must not add to that error.
     assert abs(np.sqrt(np.mean(err ** 2)) - np.sqrt(np.mean(err_ref ** 2))) < 1e-4
     assert np.max(np.linalg.norm(acc[sub] - acc_ref[sub], axis=1) / den) < 1e-4
+
+
+# ---- accurate mode (quadrupole + safe radius + group walk; not in the reference) ----
+ACC = 0x70
+
+
+@pytest.mark.parametrize("box", [0, 1])
+@pytest.mark.parametrize("kind,n,size", [(17, 3000, 100.0), (2, 2500, 700.0), (0, 777, 100.0), (16, 64, 100.0)])
+def test_accurate_reference_math_bit_exact(gs, orc, box, kind, n, size):
+    pos, vel, mass = gs.generate(kind, n, size=size, seed=41)
+    st = orc.State(pos, vel, mass)
+    with _sim(gs, pos, vel, mass, box_mode=box, math_mode=gs.MATH_REFERENCE, accuracy_parameter=0.35,
+              flags=ACC | gs.FLAG_COUNT_INTERACTIONS) as sim:
+        for _ in range(2):
+            sim.reset_stats()
+            sim.run(1)
+            o = orc.bh_step(st, box_mode=box, theta=0.35, flags=orc.ACCURATE)
+            g = sim.bh_tree()
+            _compare_tree(g, o)
+            np.testing.assert_array_equal(g["quad"], o["quad"])
+            s = sim.stats()
+            assert s.interactions == o["interactions"]
+            assert s.warp_visits == o["warp_visits"]
+            gp, gv, gm = sim.get_particles()
+            op, ov, om = st.current()
+            np.testing.assert_array_equal(gp, op)
+            np.testing.assert_array_equal(gv, ov)
+            np.testing.assert_array_equal(gm, om)
+
+
+@pytest.mark.parametrize("name", list(edge_case_inputs().keys()))
+def test_accurate_edge_cases_bit_exact(gs, orc, name):
+    pos, vel, mass = edge_case_inputs()[name]
+    st = orc.State(pos, vel, mass)
+    with _sim(gs, pos, vel, mass, math_mode=gs.MATH_REFERENCE, accuracy_parameter=0.5, flags=ACC) as sim:
+        sim.run(1)
+        o = orc.bh_step(st, theta=0.5, flags=orc.ACCURATE)
+        g = sim.bh_tree()
+        _compare_tree(g, o)
+        np.testing.assert_array_equal(g["quad"], o["quad"])
+        gp, gv, _ = sim.get_particles()
+        op, ov, _ = st.current()
+        np.testing.assert_array_equal(gp, op)
+        np.testing.assert_array_equal(gv, ov)
+
+
+def test_accurate_500k_error_gate(gs, orc):
+    """N=500,000 spiral, bounding box, theta=0.35: RMS relative force error <= 1e-3 against
+    the FP64 direct sum on 4096 particles, fast math equal to exact math within 1e-5."""
+    n = 500000
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, n, seed=2002)
+    sub = np.random.default_rng(0).choice(n, 4096, replace=False).astype(np.uint32)
+    res = {}
+    for mm in (gs.MATH_FAST, gs.MATH_REFERENCE):
+        with _sim(gs, pos, vel, mass, box_mode=1, math_mode=mm, accuracy_parameter=0.35,
+                  flags=ACC | gs.FLAG_RECORD_ACCEL) as sim:
+            sim.run(1)
+            res[mm] = sim.get_accel()[sub].astype(np.float64)
+            sim.set_particles(pos, vel, mass)
+            a64 = sim.accel_f64(sub)
+    den = np.linalg.norm(a64, axis=1)
+    err = np.linalg.norm(res[gs.MATH_FAST] - a64, axis=1) / den
+    print(f"accurate mode: rms {np.sqrt(np.mean(err**2)):.3e} median {np.median(err):.3e} "
+          f"p99 {np.quantile(err, 0.99):.3e} max {err.max():.3e}")
+    assert np.sqrt(np.mean(err ** 2)) <= 1e-3
+    assert np.max(np.linalg.norm(res[gs.MATH_FAST] - res[gs.MATH_REFERENCE], axis=1) / den) < 1e-5

@@ -87,3 +87,54 @@ def test_bounding_box_force_accuracy(gs, orc):
     a64 = orc.direct_accel_f64(*orc.pad_state(pos, vel, mass)[::2])[:4000]
     err = np.linalg.norm(acc_bh - a64, axis=1) / np.linalg.norm(a64, axis=1)
     assert np.median(err) < 2e-2
+
+
+def test_accurate_mode_moments_and_radius(gs, orc):
+    """Second central moments and safe opening radius of every node, against numpy."""
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 3000, seed=13)
+    st = orc.State(pos, vel, mass)
+    r = orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.35, flags=orc.ACCURATE)
+    skip, npos, nmass, quad, rad = r["skip"], r["pos"], r["mass"], r["quad"], r["radius"]
+    P, _, M = orc.pad_state(pos, vel, mass)
+    leaf_src = {}
+    # leaves in preorder map to sorted slots in order
+    leaves = np.nonzero(skip == 1)[0]
+    src = r["sorted_src"][: len(leaves)]
+    for li, i in zip(leaves, src):
+        leaf_src[li] = i
+    checked = 0
+    for n in np.nonzero(skip > 1)[0][:300]:
+        members = [leaf_src[q] for q in range(n + 1, n + skip[n]) if skip[q] == 1]
+        m = M[members].astype(np.float64)
+        x = P[members].astype(np.float64)
+        c = (m[:, None] * x).sum(0) / m.sum()
+        d = x - c
+        sxx, sxy, syy = (m * d[:, 0] ** 2).sum(), (m * d[:, 0] * d[:, 1]).sum(), (m * d[:, 1] ** 2).sum()
+        scale = max(1e-3, sxx + syy)
+        assert abs(quad[n, 0] - sxx) < 1e-3 * scale and abs(quad[n, 1] - sxy) < 1e-3 * scale
+        assert abs(quad[n, 2] - syy) < 1e-3 * scale
+        # every member lies within the opening radius of the centre of mass
+        assert np.max(((x - npos[n].astype(np.float64)) ** 2).sum(1)) <= rad[n] * (1 + 1e-5) + 1e-9
+        checked += 1
+    assert checked > 100
+
+
+def test_accurate_mode_theta_zero_is_direct_sum(gs, orc):
+    pos, vel, mass = gs.generate(gs.GEN_UNIFORM_DISK, 900, seed=14)
+    a, b = orc.State(pos, vel, mass), orc.State(pos, vel, mass)
+    orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.0, flags=orc.ACCURATE)
+    orc.direct_step(b)
+    np.testing.assert_allclose(a.current()[1], b.current()[1], rtol=2e-4, atol=1e-4 * np.abs(b.current()[1]).max())
+
+
+def test_accurate_mode_error_small(gs, orc):
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 30000, seed=15)
+    st = orc.State(pos, vel, mass)
+    orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.35, flags=orc.ACCURATE)
+    _, v1, _ = st.current()
+    sub = np.random.default_rng(1).choice(30000, 1024, replace=False).astype(np.uint32)
+    P, _, M = orc.pad_state(pos, vel, mass)
+    a64 = orc.direct_accel_f64(P, M, targets=sub)
+    acc = (v1[sub].astype(np.float64) - vel[sub]) / 1e-3
+    e = np.linalg.norm(acc - a64, axis=1) / np.linalg.norm(a64, axis=1)
+    assert np.sqrt(np.mean(e ** 2)) < 1.5e-3
