@@ -777,7 +777,7 @@ __device__ __forceinline__ void eval_items(GroupSmem& g, uint32_t n_items, const
 
 template <bool EXACT, bool QUAD, bool COUNT>
 __global__ void __launch_bounds__(kGroupWarps * 32)
-k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts,
+k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ counts,
               const float4* __restrict__ rec, const uint32_t* __restrict__ skip, const float4* __restrict__ quad,
               const uint4* __restrict__ kids, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
               float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
@@ -794,13 +794,28 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ co
     const uint32_t i = s < nv ? sidx[s] : 0u;
     const bool valid = s < nv && i < n_al;
     const float2 p = valid ? pos_in[i] : make_float2(0.0f, 0.0f);
-    float gx0 = valid ? p.x : INFINITY, gx1 = valid ? p.x : -INFINITY;
-    float gy0 = valid ? p.y : INFINITY, gy1 = valid ? p.y : -INFINITY;
-    for (int o = 16; o; o >>= 1) {
-        gx0 = fminf(gx0, __shfl_xor_sync(0xffffffffu, gx0, o));
-        gx1 = fmaxf(gx1, __shfl_xor_sync(0xffffffffu, gx1, o));
-        gy0 = fminf(gy0, __shfl_xor_sync(0xffffffffu, gy0, o));
-        gy1 = fmaxf(gy1, __shfl_xor_sync(0xffffffffu, gy1, o));
+    // Sub-boxes: the particles are split by their cell at the coarsest level where the
+    // first and last keys of the group differ, so a group that crosses a coarse Morton
+    // boundary is not given one box spanning the empty space between its ends.
+    const uint32_t kf = skey[group * 32], kl = skey[min(group * 32 + 31, nv - 1)];
+    const int shift = kf == kl ? -1 : ((31 - __clz(kf ^ kl)) & ~1);
+    const int my_box = !valid ? -1 : (shift < 0 ? 0 : (int)((skey[s] >> shift) & 3u));
+    float bx0[4], bx1[4], by0[4], by1[4];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const bool in = my_box == b;
+        float x0 = in ? p.x : INFINITY, x1 = in ? p.x : -INFINITY;
+        float y0 = in ? p.y : INFINITY, y1 = in ? p.y : -INFINITY;
+        for (int o = 16; o; o >>= 1) {
+            x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+            x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+            y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+            y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+        }
+        bx0[b] = x0;
+        bx1[b] = x1;
+        by0[b] = y0;
+        by1[b] = y1;
     }
     float ax = 0.0f, ay = 0.0f;
     unsigned long long n_int = 0, n_test = 0;
@@ -834,9 +849,13 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ co
         if (act) {  // every stacked record is an internal node
             const float4 q = rec[n];
             const uint4 kd = kids[n];
-            const float ex = fmaxf(fmaxf(gx0 - q.x, q.x - gx1), 0.0f);
-            const float ey = fmaxf(fmaxf(gy0 - q.y, q.y - gy1), 0.0f);
-            const float d2 = fmaf(ex, ex, fmaf(ey, ey, eps2));
+            float d2 = INFINITY;  // nearest sub-box; an empty one gives +inf
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const float ex = fmaxf(fmaxf(bx0[b] - q.x, q.x - bx1[b]), 0.0f);
+                const float ey = fmaxf(fmaxf(by0[b] - q.y, q.y - by1[b]), 0.0f);
+                d2 = fminf(d2, fmaf(ex, ex, fmaf(ey, ey, eps2)));
+            }
             if (q.w <= d2 * theta2) {
                 a0 = n;
                 c0 = 1u | kItemNode;
@@ -1097,7 +1116,8 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
                                                          s->theta2, k, hdt, (uint32_t)w.cap, stat)
 #define GS_GROUP(E_, Q_, C_)                                                                                    \
     k_force_group<E_, Q_, C_><<<(int)((n / 32 + kGroupWarps - 1) / kGroupWarps), kGroupWarps * 32, 0, st>>>(    \
-        sidx, ctr + kCtrValid, w.rec, w.skip, w.quad, w.kids, s->pos[in], s->vel[in], s->pos[out], s->vel[out],      \
+        sidx, skey, ctr + kCtrValid, w.rec, w.skip, w.quad, w.kids, s->pos[in], s->vel[in], s->pos[out],             \
+        s->vel[out],                                                                                                 \
         s->acc, n,                                                                                                   \
         s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err)
     if (s->p.flags & GS_FLAG_GROUP_WALK) {

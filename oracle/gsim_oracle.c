@@ -327,6 +327,7 @@ typedef struct {
     const float* quad; /* second central moments {sxx, sxy, syy} per record, NULL: monopoles */
     uint64_t tree_size;
     const uint32_t* src; /* original index per sorted slot, n_al for empty slots */
+    const uint32_t* skey; /* cell key per sorted slot (group walk) */
     uint32_t n_al;
     const float *pos_in, *vel_in, *mass_in;
     float *pos_out, *vel_out;
@@ -336,6 +337,7 @@ typedef struct {
     uint32_t stride;        /* walk warps stride*item */
     int group_walk;         /* ORC_BH_GROUP_WALK semantics */
     uint32_t* max_stack;    /* per worker */
+    uint64_t* max_inter;    /* per worker: largest per-warp interaction count */
 } walk_ctx;
 
 static void walk_warp(void* p, uint64_t item, int worker) {
@@ -403,7 +405,11 @@ static void walk_warp(void* p, uint64_t item, int worker) {
 }
 
 /* Accurate-mode walk (ORC_BH_GROUP_WALK), for the 32 consecutive sorted slots of one warp:
- *   - the group box is the bounding box of the group's particles;
+ *   - the group is cut into at most four sub-boxes: the particles are split by their
+ *     cell at the coarsest level where the first and last cell keys of the group differ
+ *     (so a group that crosses a coarse Morton boundary does not get one box spanning
+ *     the empty space between its two ends); each sub-box is the bounding box of its
+ *     particles;
  *   - a LIFO stack starts with the root; each step pops the top min(32, size) records
  *     (lane j gets stack[size - k + j]) and tests each against the box:
  *       d2 = ex^2 + ey^2 + eps^2 with (ex, ey) the distance from the box to the centre of
@@ -421,7 +427,11 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
     float px[WARP], py[WARP], ax[WARP], ay[WARP];
     int valid[WARP];
     int nvalid = 0;
-    float gx0 = INFINITY, gx1 = -INFINITY, gy0 = INFINITY, gy1 = -INFINITY;
+    float gx0[4], gx1[4], gy0[4], gy1[4];
+    for (int b = 0; b < 4; ++b) {
+        gx0[b] = gy0[b] = INFINITY;
+        gx1[b] = gy1[b] = -INFINITY;
+    }
     for (int l = 0; l < WARP; ++l) {
         uint32_t s = (uint32_t)w * WARP + (uint32_t)l;
         uint32_t i = c->src[s];
@@ -429,15 +439,20 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
         px[l] = valid[l] ? c->pos_in[2 * i] : 0.0f;
         py[l] = valid[l] ? c->pos_in[2 * i + 1] : 0.0f;
         ax[l] = ay[l] = 0.0f;
-        if (valid[l]) {
-            nvalid++;
-            gx0 = fminf(gx0, px[l]);
-            gx1 = fmaxf(gx1, px[l]);
-            gy0 = fminf(gy0, py[l]);
-            gy1 = fmaxf(gy1, py[l]);
-        }
+        nvalid += valid[l];
     }
     if (!nvalid || !c->tree_size) return;
+    {
+        const uint32_t kf = c->skey[(uint32_t)w * WARP], kl = c->skey[(uint32_t)w * WARP + (uint32_t)nvalid - 1];
+        const int shift = kf == kl ? -1 : ((31 - __builtin_clz(kf ^ kl)) & ~1);
+        for (int l = 0; l < nvalid; ++l) { /* valid lanes are a prefix of the warp */
+            const int b = shift < 0 ? 0 : (int)((c->skey[(uint32_t)w * WARP + (uint32_t)l] >> shift) & 3u);
+            gx0[b] = fminf(gx0[b], px[l]);
+            gx1[b] = fmaxf(gx1[b], px[l]);
+            gy0[b] = fminf(gy0[b], py[l]);
+            gy1[b] = fmaxf(gy1[b], py[l]);
+        }
+    }
     uint32_t stack[GROUP_STACK_CAP + 160];
     uint32_t size = 1, max_size = 1;
     stack[0] = 0;
@@ -455,9 +470,12 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
             int accept = 1;
             if (sk > 1) {
                 const float cx = c->npos[2 * n], cy = c->npos[2 * n + 1];
-                float ex = fmaxf(fmaxf(gx0 - cx, cx - gx1), 0.0f);
-                float ey = fmaxf(fmaxf(gy0 - cy, cy - gy1), 0.0f);
-                float d2 = pair_d2(ex, ey, c->eps2);
+                float d2 = INFINITY; /* nearest sub-box (empty sub-boxes give +inf) */
+                for (int b = 0; b < 4; ++b) {
+                    float ex = fmaxf(fmaxf(gx0[b] - cx, cx - gx1[b]), 0.0f);
+                    float ey = fmaxf(fmaxf(gy0[b] - cy, cy - gy1[b]), 0.0f);
+                    d2 = fminf(d2, pair_d2(ex, ey, c->eps2));
+                }
                 accept = c->radius[n] <= d2 * c->theta2;
             }
             if (accept) { /* one item: the record itself */
@@ -519,22 +537,28 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
     c->interactions[worker] += inter;
     c->visits[worker] += visits;
     if (max_size > c->max_stack[worker]) c->max_stack[worker] = max_size;
+    if (inter > c->max_inter[worker]) c->max_inter[worker] = inter;
 }
 
 static void run_walk(walk_ctx* c, int nthreads, orc_bh_out* out) {
     uint64_t inter[256] = {0}, vis[256] = {0};
     uint32_t mstack[256] = {0};
+    uint64_t minter[256] = {0};
     c->interactions = inter;
     c->visits = vis;
     c->max_stack = mstack;
+    c->max_inter = minter;
     c->stride = out && out->walk_stride > 1 ? out->walk_stride : 1;
     uint64_t warps = c->n_al / WARP;
     double t0 = now_seconds();
     parallel_for(nthreads, (warps + c->stride - 1) / c->stride, 4, c->group_walk ? group_walk_warp : walk_warp, c);
     if (out) {
         out->max_stack = 0;
-        for (int t = 0; t < 256; ++t)
+        out->max_warp_interactions = 0;
+        for (int t = 0; t < 256; ++t) {
             if (mstack[t] > out->max_stack) out->max_stack = mstack[t];
+            if (minter[t] > out->max_warp_interactions) out->max_warp_interactions = minter[t];
+        }
     }
     if (out) out->walk_seconds = now_seconds() - t0;
     if (out) {
@@ -988,6 +1012,7 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
     wc.nmass = nmass;
     wc.quad = quad;
     wc.group_walk = (flags & ORC_BH_GROUP_WALK) != 0;
+    wc.skey = skey;
     wc.tree_size = tree_size;
     wc.src = src;
     wc.n_al = n_al;

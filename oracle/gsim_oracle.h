@@ -70,6 +70,7 @@ typedef struct orc_bh_out {
     double build_seconds;    /* keys, sort and tree (single thread) */
     double walk_seconds;     /* force walk + integration (nthreads) */
     uint32_t max_stack;      /* deepest group-walk stack seen (ORC_BH_GROUP_WALK) */
+    uint64_t max_warp_interactions; /* largest interaction count of one warp (valid lanes) */
 } orc_bh_out;
 
 /* Direct sum, SimShader.comp order: for every i, sum j = 0 .. n-1 in order. */

@@ -31,7 +31,7 @@ class BHOut(C.Structure):
                 ("interactions", C.c_uint64), ("warp_visits", C.c_uint64),
                 ("box_center_x", C.c_float), ("box_center_y", C.c_float), ("box_scale", C.c_float),
                 ("box_radius0", C.c_float), ("build_seconds", C.c_double), ("walk_seconds", C.c_double),
-                ("max_stack", C.c_uint32)]
+                ("max_stack", C.c_uint32), ("max_warp_interactions", C.c_uint64)]
 
 
 _lib = None
@@ -178,6 +178,7 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
     res.update(tree_size=t, valid_count=out.valid_count, internal_count=out.internal_count,
                interactions=out.interactions, warp_visits=out.warp_visits,
                build_seconds=out.build_seconds, walk_seconds=out.walk_seconds, max_stack=out.max_stack,
+               max_warp_interactions=out.max_warp_interactions,
                box=(out.box_center_x, out.box_center_y, out.box_scale, out.box_radius0))
     return res
 
