@@ -18,8 +18,9 @@
 //   k_records     preorder records: node (d, s) at s + E(s) + d - dmin(s), particle leaf
 //                 at s + E(s) + e(s); skip = end + E(end) - index (the reference's count.y),
 //                 radius = radius0 / 4^d (TreeMoveShader.comp:70-71)
-//   k_sums_level  bottom-up mass and mass-moment sums, finest level first, in the order
-//                 of TreeInitShader.comp:78-80; centre of mass as TreeMoveShader.comp:66-67
+//   k_bottom_up   bottom-up mass and mass-moment sums in one launch (the last child to
+//                 finish computes its parent), children in the order of
+//                 TreeInitShader.comp:78-80; centre of mass as TreeMoveShader.comp:66-67
 //   k_force       ForceShader.comp:78-152 semantics: one warp walks the preorder records
 //                 for 32 consecutive sorted slots; a record is accepted only if every
 //                 lane satisfies radius <= d2 * theta^2; 32-record window staged in shared
@@ -121,16 +122,37 @@ k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uin
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return;
+    if (!last) return;
     __threadfence();
+    // the last block reduces all block partials in parallel (min/max are exact in any order)
+    mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+    for (uint32_t bl = threadIdx.x; bl < gridDim.x; bl += blockDim.x) {
+        mnx = fminf(mnx, __ldcg(&part[4 * bl + 0]));
+        mxx = fmaxf(mxx, __ldcg(&part[4 * bl + 1]));
+        mny = fminf(mny, __ldcg(&part[4 * bl + 2]));
+        mxy = fmaxf(mxy, __ldcg(&part[4 * bl + 3]));
+    }
+    for (int o = 16; o; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    __syncthreads();
+    if (lane == 0) {
+        s[0][warp] = mnx;
+        s[1][warp] = mxx;
+        s[2][warp] = mny;
+        s[3][warp] = mxy;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     double a = INFINITY, b = -INFINITY, c = INFINITY, d = -INFINITY;
-    for (uint32_t bl = 0; bl < gridDim.x; ++bl) {
-        double v0 = __ldcg(&part[4 * bl + 0]), v1 = __ldcg(&part[4 * bl + 1]);
-        double v2 = __ldcg(&part[4 * bl + 2]), v3 = __ldcg(&part[4 * bl + 3]);
-        if (v0 < a) a = v0;
-        if (v1 > b) b = v1;
-        if (v2 < c) c = v2;
-        if (v3 > d) d = v3;
+    for (int w = 0; w < kBBoxThreads / 32; ++w) {
+        if (s[0][w] < a) a = s[0][w];
+        if (s[1][w] > b) b = s[1][w];
+        if (s[2][w] < c) c = s[2][w];
+        if (s[3][w] > d) d = s[3][w];
     }
     // square box around the extent, 1/1024 margin, 2^15 cells per axis
     double cx = 0.5 * (a + b), cy = 0.5 * (c + d);
@@ -146,6 +168,7 @@ k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uin
     p.scale = (float)scale;
     double side0 = (double)(1u << kBBoxBits) / (double)p.scale;
     p.radius0 = (float)(side0 * side0 * 0.5);
+    p.inv_scale = (float)(1.0 / (double)p.scale);
     *out = p;
 }
 
@@ -418,15 +441,28 @@ __device__ __forceinline__ uint32_t cell_end(const uint32_t* k, uint32_t a, uint
     return a;
 }
 
+// Child descriptors of an internal record: up to four children in Morton order, each a
+// record index with kKidLeaf set for a particle leaf, kKidNone when absent; a
+// finest-level cell stores {kKidFinest, first leaf, leaf count, -}.
+constexpr uint32_t kKidNone = 0xFFFFFFFFu;
+constexpr uint32_t kKidFinest = 0xFFFFFFFEu;
+constexpr uint32_t kKidLeaf = 0x80000000u;
+
+// record index of the particle leaf of sorted slot t
+__device__ __forceinline__ uint32_t leaf_of(const uint32_t* skey, const uint32_t* E, uint32_t t, uint32_t nv, int D) {
+    const int cmin = slot_dmin(skey, t, D), cmax = slot_dmax(skey, t, nv, D);
+    return t + E[t] + (uint32_t)(cmax >= cmin ? cmax - cmin + 1 : 0);
+}
+
+// One thread per sorted slot s: the particle leaf of s, and the slot of every internal
+// node that starts at s in the node -> slot map (internal ordinal j = E(s) + d - dmin(s),
+// record index s + j).
 __global__ void __launch_bounds__(256)
 k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ E,
-          const uint32_t* __restrict__ valid_count, int D, const BHParams* __restrict__ bp,
-          const float2* __restrict__ pos, const float* __restrict__ mass, float4* __restrict__ rec,
-          uint32_t* __restrict__ skip, uint32_t* __restrict__ nend, uint64_t cap, uint32_t n_al,
-          uint32_t* __restrict__ level_count, uint32_t* __restrict__ level_slots, uint32_t level_cap,
-          int* __restrict__ err) {
+          const uint32_t* __restrict__ valid_count, int D, const float2* __restrict__ pos,
+          const float* __restrict__ mass, float4* __restrict__ rec, uint32_t* __restrict__ skip,
+          uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al, int* __restrict__ err) {
     const uint32_t nv = *valid_count;
-    const float radius0 = bp->radius0;
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += gridDim.x * blockDim.x) {
         const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
         const uint32_t Es = E[s];
@@ -444,55 +480,63 @@ k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, 
         const float2 p = pos[i];
         rec[leaf] = make_float4(p.x, p.y, mass[i], 0.0f);
         skip[leaf] = 1u;
-        const uint32_t ks = skey[s];
-        uint32_t lo = s + 1;
-        for (int d = dmax; d >= dmin; --d) {  // finest first: each search starts at the last end
-            const int shift = 2 * (D - d);
-            const uint32_t end = cell_end(skey, lo, nv, shift, ks >> shift);
-            const uint32_t at = s + Es + (uint32_t)(d - dmin);
-            rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
-            skip[at] = end + E[end] - at;
-            nend[at] = end;
-            lo = end;
-            // this level's node list (any order: every node of a level is summed independently)
-            const uint32_t li = atomicAdd(&level_count[d], 1u);
-            if (li < level_cap) level_slots[(size_t)d * level_cap + li] = s;
-            else atomicOr(err, kErrTree);
-        }
+        for (int k = 0; k < e; ++k) node_slot[Es + k] = s;
     }
 }
 
-// ------------------------------------------------------------------------------------
-// bottom-up sums for one level
-// ------------------------------------------------------------------------------------
-// One child of a level-d cell starting at sorted slot t: a node of level d+1 (its record
-// index, mass, centre of mass and end slot) or a single particle (its leaf record).
-struct Child {
-    float m, x, y;
-    uint32_t rec;     // record index (node or particle leaf)
-    uint32_t next;    // first slot after the child
-    bool node;
-};
-
-__device__ __forceinline__ Child child_at(const uint32_t* skey, const uint32_t* E, const float4* rec,
-                                          const uint32_t* nend, uint32_t t, int d, uint32_t nv, int D) {
-    Child c;
-    const int cmin = slot_dmin(skey, t, D), cmax = slot_dmax(skey, t, nv, D);
-    if (d < D && cmin <= d + 1 && d + 1 <= cmax) {
-        c.rec = t + E[t] + (uint32_t)(d + 1 - cmin);
-        c.node = true;
-        c.next = nend[c.rec];
-    } else {
-        const int ce = cmax >= cmin ? cmax - cmin + 1 : 0;
-        c.rec = t + E[t] + (uint32_t)ce;
-        c.node = false;
-        c.next = t + 1;
+// One thread per internal node (d, s): skip (the reference's count.y), the level radius
+// of TreeMoveShader.comp:70-71, the cell end, the child descriptors, the parent link of
+// its internal children and the number of internal children the bottom-up pass waits for.
+__global__ void __launch_bounds__(256)
+k_nodes(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E, const uint32_t* __restrict__ counts,
+        int D, const BHParams* __restrict__ bp, const uint32_t* __restrict__ node_slot, float4* __restrict__ rec,
+        uint32_t* __restrict__ skip, uint32_t* __restrict__ nend, uint4* __restrict__ kids,
+        uint32_t* __restrict__ parent, uint32_t* __restrict__ pending, uint32_t* __restrict__ arrived,
+        uint2* __restrict__ nodeinfo, uint64_t cap, int* __restrict__ err) {
+    const uint32_t nv = counts[0], M = counts[1];
+    const float radius0 = bp->radius0;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
+        const uint32_t s = node_slot[j];
+        const uint32_t at = s + j;
+        if (s >= nv || at >= cap) {  // only after a failed sort or scan (error flag already set)
+            atomicOr(err, kErrTree);
+            continue;
+        }
+        const int d = slot_dmin(skey, s, D) + (int)(j - E[s]);
+        const int shift = 2 * (D - d);
+        const uint32_t end = cell_end(skey, s + 1, nv, shift, skey[s] >> shift);
+        rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
+        skip[at] = end + E[end] - at;
+        nend[at] = end;
+        nodeinfo[at] = make_uint2(s, (uint32_t)d);
+        arrived[at] = 0u;
+        if (d == 0) parent[at] = kKidNone;  // the root
+        if (d == D) {
+            kids[at] = make_uint4(kKidFinest, at + 1, end - s, 0u);  // all children are leaves
+            pending[at] = 0u;
+            continue;
+        }
+        uint32_t kid[4] = {kKidNone, kKidNone, kKidNone, kKidNone};
+        uint32_t nk = 0, nint = 0;
+        const int cshift = 2 * (D - d - 1);
+        for (uint32_t t = s; t < end;) {  // the level-(d+1) cells inside [s, end), in Morton order
+            const uint32_t tend = cell_end(skey, t + 1, nv, cshift, skey[t] >> cshift);
+            uint32_t c;
+            if (tend - t >= 2) {  // an internal node (d+1, t)
+                c = t + E[t] + (uint32_t)(d + 1 - slot_dmin(skey, t, D));
+                parent[c] = at;
+                ++nint;
+            } else {
+                c = leaf_of(skey, E, t, nv, D) | kKidLeaf;
+            }
+            if (nk < 4) kid[nk] = c;
+            ++nk;
+            t = tend;
+        }
+        if (nk > 4) atomicOr(err, kErrTree);
+        kids[at] = make_uint4(kid[0], kid[1], kid[2], kid[3]);
+        pending[at] = nint;
     }
-    const float4 q = rec[c.rec];
-    c.x = q.x;
-    c.y = q.y;
-    c.m = q.z;
-    return c;
 }
 
 __device__ __forceinline__ uint32_t compact_bits(uint32_t v) {  // inverse of spread_bits
@@ -505,104 +549,172 @@ __device__ __forceinline__ uint32_t compact_bits(uint32_t v) {  // inverse of sp
 }
 
 // Squared distance from the centre of mass to the farthest corner of the level-d cell
-// holding `key` (the accurate mode's opening radius).  FP64, like the CPU restatement.
-__device__ double cell_bmax2(int bbox_mode, const BHParams& bp, int D, int d, uint32_t key, float cx, float cy) {
+// holding `key` (the accurate mode's opening radius), in FP32 with the same operation
+// sequence as the CPU restatement:
+//   fixed box:    side = 1000 / 2^d, x0 = -500 + ix * side          (both exact)
+//   bounding box: side = 2^(D-d) * inv, x0 = cx + (ix * 2^(D-d) - 2^(D-1)) * inv
+//   m = max(|c - x0|, |x0 + side - c|) per axis, bmax^2 = fma(mx, mx, my * my)
+__device__ __forceinline__ float cell_bmax2(int bbox_mode, const BHParams& bp, int D, int d, uint32_t key, float cx,
+                                            float cy) {
     const uint32_t pre = key >> (2 * (D - d));
-    const double ix = (double)compact_bits(pre), iy = (double)compact_bits(pre >> 1);
-    double x0, y0, side;
+    const float ix = (float)compact_bits(pre), iy = (float)compact_bits(pre >> 1);
+    float x0, y0, side;
     if (bbox_mode) {
-        const double w = (double)(1u << (D - d));
-        side = w / (double)bp.scale;
-        x0 = (double)bp.cx + (ix * w - (double)(1u << (D - 1))) / (double)bp.scale;
-        y0 = (double)bp.cy + (iy * w - (double)(1u << (D - 1))) / (double)bp.scale;
+        const float w = (float)(1u << (D - d));
+        side = __fmul_rn(w, bp.inv_scale);
+        x0 = __fadd_rn(bp.cx, __fmul_rn(__fsub_rn(__fmul_rn(ix, w), (float)(1u << (D - 1))), bp.inv_scale));
+        y0 = __fadd_rn(bp.cy, __fmul_rn(__fsub_rn(__fmul_rn(iy, w), (float)(1u << (D - 1))), bp.inv_scale));
     } else {
-        side = 2.0 * (double)kSimSize / (double)(1u << d);
-        x0 = -(double)kSimSize + ix * side;
-        y0 = -(double)kSimSize + iy * side;
+        side = __fdiv_rn(2.0f * kSimSize, (float)(1u << d));
+        x0 = __fadd_rn(-kSimSize, __fmul_rn(ix, side));
+        y0 = __fadd_rn(-kSimSize, __fmul_rn(iy, side));
     }
-    const double ax = fabs((double)cx - x0), bx = fabs(x0 + side - (double)cx);
-    const double ay = fabs((double)cy - y0), by = fabs(y0 + side - (double)cy);
-    const double mx = ax > bx ? ax : bx, my = ay > by ? ay : by;
-    return mx * mx + my * my;
+    const float mx = fmaxf(fabsf(__fsub_rn(cx, x0)), fabsf(__fsub_rn(__fadd_rn(x0, side), cx)));
+    const float my = fmaxf(fabsf(__fsub_rn(cy, y0)), fabsf(__fsub_rn(__fadd_rn(y0, side), cy)));
+    return __fmaf_rn(mx, mx, __fmul_rn(my, my));
 }
 
-// Child descriptors of an internal record (group walk): up to four children in Morton
-// order, each a record index with kKidLeaf set for a particle leaf, kKidNone when absent;
-// a finest-level cell stores {kKidFinest, first leaf, leaf count, -}.
-constexpr uint32_t kKidNone = 0xFFFFFFFFu;
-constexpr uint32_t kKidFinest = 0xFFFFFFFEu;
-constexpr uint32_t kKidLeaf = 0x80000000u;
+// One child's contribution: mass, centre of mass and (internal children) moments.
+// Loads go through L2 (ld.cg): internal children were written by other threads of the
+// same launch.
+struct KidData {
+    float m, x, y;   // mass and centre of mass (particle position for a leaf)
+    float mx, my;    // mass moments (x*m, y*m for a leaf)
+    float4 q;        // second central moments (zero for a leaf)
+};
 
-// Bottom-up sums for the nodes of level d (children were finished by the previous launch):
-// mass and mass moments in child order (TreeInitShader.comp:78-80), centre of mass
-// (TreeMoveShader.comp:66-67); with `quad`, second central moments about the centre of
-// mass; with `safe`, the safe opening radius; with `kids`, the child descriptors.
-__global__ void __launch_bounds__(256)
-k_sums_level(int d, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
-             const uint32_t* __restrict__ valid_count, int D, float4* __restrict__ rec,
-             const uint32_t* __restrict__ nend, float2* __restrict__ msum, uint32_t cap,
-             float4* __restrict__ quad, uint4* __restrict__ kids, int safe, int bbox_mode,
-             const BHParams* __restrict__ bpp, const uint32_t* __restrict__ level_count,
-             const uint32_t* __restrict__ level_slots, uint32_t level_cap) {
-    const uint32_t nv = *valid_count;
-    const uint32_t cnt = min(level_count[d], level_cap);
-    const uint32_t* slots = level_slots + (size_t)d * level_cap;
-    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < cnt; li += gridDim.x * blockDim.x) {
-        const uint32_t s = slots[li];
-        const int dmin = slot_dmin(skey, s, D);
-        const uint32_t at = s + E[s] + (uint32_t)(d - dmin);
-        if (at >= cap) continue;  // only after a failed scan (error flag already set)
-        const uint32_t end = nend[at];
-        float sx = 0.0f, sy = 0.0f, sm = 0.0f;
-        uint32_t kid[4] = {kKidNone, kKidNone, kKidNone, kKidNone};
-        int nk = 0;
-        for (uint32_t t = s; t < end;) {  // children in Morton order
-            const Child c = child_at(skey, E, rec, nend, t, d, nv, D);
-            if (c.node) {
-                const float2 m2 = msum[c.rec];
-                sx = __fadd_rn(sx, m2.x);
-                sy = __fadd_rn(sy, m2.y);
-            } else {
-                sx = __fadd_rn(sx, __fmul_rn(c.x, c.m));
-                sy = __fadd_rn(sy, __fmul_rn(c.y, c.m));
-            }
-            sm = __fadd_rn(sm, c.m);
-            if (nk < 4) kid[nk] = c.node ? c.rec : (c.rec | kKidLeaf);
-            ++nk;
-            t = c.next;
+template <bool QUAD>
+__device__ __forceinline__ KidData kid_data(uint32_t c, const float4* rec, const float2* msum, const float4* quad) {
+    KidData k;
+    if (c & kKidLeaf) {
+        const float4 r = __ldcg(&rec[c & ~kKidLeaf]);
+        k.m = r.z;
+        k.x = r.x;
+        k.y = r.y;
+        k.mx = __fmul_rn(r.x, r.z);
+        k.my = __fmul_rn(r.y, r.z);
+        k.q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    } else {
+        const float4 r = __ldcg(&rec[c]);
+        const float2 m2 = __ldcg(&msum[c]);
+        k.m = r.z;
+        k.x = r.x;
+        k.y = r.y;
+        k.mx = m2.x;
+        k.my = m2.y;
+        k.q = QUAD ? __ldcg(&quad[c]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    return k;
+}
+
+// Mass, mass moments (children in Morton order, TreeInitShader.comp:78-80), centre of
+// mass (TreeMoveShader.comp:66-67), second central moments (QUAD) and the safe opening
+// radius (SAFE) of node `at`.
+template <bool QUAD>
+__device__ void compute_node(uint32_t at, int D, int safe, int bbox_mode, const BHParams& bp,
+                             const uint32_t* __restrict__ skey, float4* rec, const uint4* __restrict__ kids,
+                             const uint2* __restrict__ nodeinfo, float2* msum, float4* quad) {
+    const uint4 kd = kids[at];
+    float sx = 0.0f, sy = 0.0f, sm = 0.0f, cx, cy;
+    float qxx = 0.0f, qxy = 0.0f, qyy = 0.0f;
+    if (kd.x == kKidFinest) {  // particle leaves at kd.y .. kd.y + kd.z - 1
+        for (uint32_t t = 0; t < kd.z; ++t) {
+            const float4 r = __ldcg(&rec[kd.y + t]);
+            sx = __fadd_rn(sx, __fmul_rn(r.x, r.z));
+            sy = __fadd_rn(sy, __fmul_rn(r.y, r.z));
+            sm = __fadd_rn(sm, r.z);
         }
-        msum[at] = make_float2(sx, sy);
-        float cx = sx, cy = sy;
+        cx = sx;
+        cy = sy;
         if (sm != 0.0f) {
             cx = __fdiv_rn(sx, sm);
             cy = __fdiv_rn(sy, sm);
         }
-        float r = rec[at].w;
-        if (quad) {  // second central moments, parallel-axis sum over the children in order
-            float qxx = 0.0f, qxy = 0.0f, qyy = 0.0f;
-            for (uint32_t t = s; t < end;) {
-                const Child c = child_at(skey, E, rec, nend, t, d, nv, D);
-                if (c.node) {
-                    const float4 q = quad[c.rec];
-                    qxx = __fadd_rn(qxx, q.x);
-                    qxy = __fadd_rn(qxy, q.y);
-                    qyy = __fadd_rn(qyy, q.z);
-                }
-                const float ddx = __fsub_rn(c.x, cx), ddy = __fsub_rn(c.y, cy);
-                const float tx = __fmul_rn(c.m, ddx);
+        if (QUAD) {
+            for (uint32_t t = 0; t < kd.z; ++t) {
+                const float4 r = __ldcg(&rec[kd.y + t]);
+                const float ddx = __fsub_rn(r.x, cx), ddy = __fsub_rn(r.y, cy);
+                const float tx = __fmul_rn(r.z, ddx);
                 qxx = __fmaf_rn(tx, ddx, qxx);
                 qxy = __fmaf_rn(tx, ddy, qxy);
-                qyy = __fmaf_rn(__fmul_rn(c.m, ddy), ddy, qyy);
-                t = c.next;
+                qyy = __fmaf_rn(__fmul_rn(r.z, ddy), ddy, qyy);
             }
-            quad[at] = make_float4(qxx, qxy, qyy, 0.0f);
         }
-        if (kids) {
-            if (d == D) kids[at] = make_uint4(kKidFinest, at + 1, end - s, 0u);  // all children are leaves
-            else kids[at] = make_uint4(kid[0], kid[1], kid[2], kid[3]);
+    } else {
+        // children fill the descriptor from the front; kKidNone marks the unused tail
+        const uint32_t kk[4] = {kd.x, kd.y, kd.z, kd.w};
+        KidData c[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if (kk[t] != kKidNone) c[t] = kid_data<QUAD>(kk[t], rec, msum, quad);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            if (kk[t] == kKidNone) continue;
+            sx = __fadd_rn(sx, c[t].mx);
+            sy = __fadd_rn(sy, c[t].my);
+            sm = __fadd_rn(sm, c[t].m);
         }
-        if (safe) r = (float)cell_bmax2(bbox_mode, *bpp, D, d, skey[s], cx, cy);
-        rec[at] = make_float4(cx, cy, sm, r);
+        cx = sx;
+        cy = sy;
+        if (sm != 0.0f) {
+            cx = __fdiv_rn(sx, sm);
+            cy = __fdiv_rn(sy, sm);
+        }
+        if (QUAD) {  // parallel-axis sum over the children in order
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                if (kk[t] == kKidNone) continue;
+                if (!(kk[t] & kKidLeaf)) {  // internal child: its own moments
+                    qxx = __fadd_rn(qxx, c[t].q.x);
+                    qxy = __fadd_rn(qxy, c[t].q.y);
+                    qyy = __fadd_rn(qyy, c[t].q.z);
+                }
+                const float ddx = __fsub_rn(c[t].x, cx), ddy = __fsub_rn(c[t].y, cy);
+                const float tx = __fmul_rn(c[t].m, ddx);
+                qxx = __fmaf_rn(tx, ddx, qxx);
+                qxy = __fmaf_rn(tx, ddy, qxy);
+                qyy = __fmaf_rn(__fmul_rn(c[t].m, ddy), ddy, qyy);
+            }
+        }
+    }
+    msum[at] = make_float2(sx, sy);
+    if (QUAD) quad[at] = make_float4(qxx, qxy, qyy, 0.0f);
+    float r = __ldcg(&rec[at]).w;
+    if (safe) {
+        const uint2 info = nodeinfo[at];
+        r = cell_bmax2(bbox_mode, bp, D, (int)info.y, skey[info.x], cx, cy);
+    }
+    rec[at] = make_float4(cx, cy, sm, r);
+}
+
+// Bottom-up pass in one launch: a thread starts at the finest node of its slot when that
+// node has no internal children, computes it, and climbs: the child that completes a
+// parent's count of internal children (atomic ticket, no waiting) computes the parent.
+// Every node sums its children in the fixed Morton order, so the result does not depend
+// on which thread gets there.
+template <bool QUAD>
+__global__ void __launch_bounds__(256)
+k_bottom_up(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
+            const uint32_t* __restrict__ valid_count, int D, float4* rec, const uint4* __restrict__ kids,
+            const uint32_t* __restrict__ parent, const uint32_t* __restrict__ pending, uint32_t* arrived,
+            const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
+            const BHParams* __restrict__ bpp, uint32_t cap) {
+    const uint32_t nv = *valid_count;
+    const BHParams bp = *bpp;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += gridDim.x * blockDim.x) {
+        const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
+        if (dmax < dmin) continue;
+        uint32_t at = s + E[s] + (uint32_t)(dmax - dmin);
+        if (at >= cap || pending[at] != 0u) continue;
+        for (;;) {
+            compute_node<QUAD>(at, D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum, quad);
+            __threadfence();  // publish this node before its parent can be computed
+            const uint32_t p = parent[at];
+            if (p == kKidNone || p >= cap) break;
+            if (atomicAdd(&arrived[p], 1u) + 1u != pending[p]) break;
+            __threadfence();
+            at = p;
+        }
     }
 }
 
@@ -954,8 +1066,7 @@ uint64_t bh_capacity(int box_mode, uint64_t n_al) {
 }
 
 // counters layout inside the zeroed block
-enum { kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrLevel = 12,
-       kCtrCount = 32 };
+enum { kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrCount = 16 };
 
 cudaError_t bh_alloc(gs_sim* s) {
     BHWork& w = s->bh;
@@ -981,9 +1092,12 @@ cudaError_t bh_alloc(gs_sim* s) {
     GS_ALLOC(w.skip, (w.cap + 32) * sizeof(uint32_t));
     GS_ALLOC(w.nend, w.cap * sizeof(uint32_t));
     GS_ALLOC(w.msum, w.cap * sizeof(float2));
-    w.level_cap = (uint32_t)(n / 2 + 1);  // at most N/2 cells of one level hold two particles
-    GS_ALLOC(w.level_slots, (size_t)(w.depth + 1) * w.level_cap * sizeof(uint32_t));
-    if (s->p.flags & GS_FLAG_GROUP_WALK) GS_ALLOC(w.kids, w.cap * sizeof(uint4));
+    GS_ALLOC(w.kids, w.cap * sizeof(uint4));
+    GS_ALLOC(w.parent, w.cap * sizeof(uint32_t));
+    GS_ALLOC(w.pending, w.cap * sizeof(uint32_t));
+    GS_ALLOC(w.arrived, w.cap * sizeof(uint32_t));
+    GS_ALLOC(w.nodeinfo, w.cap * sizeof(uint2));
+    GS_ALLOC(w.node_slot, w.cap * sizeof(uint32_t));
     if (s->p.flags & GS_FLAG_QUADRUPOLE) {
         GS_ALLOC(w.quad, w.cap * sizeof(float4));
         e = cudaMemset(w.quad, 0, w.cap * sizeof(float4));
@@ -1011,7 +1125,8 @@ cudaError_t bh_alloc(gs_sim* s) {
     if (e != cudaSuccess) return e;
     e = cudaMemset(w.skip, 0, (w.cap + 32) * sizeof(uint32_t));
     if (e != cudaSuccess) return e;
-    BHParams fixed{0.0f, 0.0f, (float)kGrid / (2.0f * kSimSize), kSimSize * kSimSize * 2.0f};
+    BHParams fixed{0.0f, 0.0f, (float)kGrid / (2.0f * kSimSize), kSimSize * kSimSize * 2.0f,
+                   2.0f * kSimSize / (float)kGrid};
     e = cudaMemcpy(w.params, &fixed, sizeof fixed, cudaMemcpyHostToDevice);
     return e;
 }
@@ -1030,9 +1145,15 @@ void bh_free(gs_sim* s) {
     cudaFree(w.msum);
     cudaFree(w.quad);
     cudaFree(w.kids);
-    cudaFree(w.level_slots);
+    cudaFree(w.parent);
+    cudaFree(w.pending);
+    cudaFree(w.arrived);
+    cudaFree(w.nodeinfo);
+    cudaFree(w.node_slot);
+    w.node_slot = nullptr;
     w.kids = nullptr;
-    w.level_slots = nullptr;
+    w.parent = w.pending = w.arrived = nullptr;
+    w.nodeinfo = nullptr;
     w.quad = nullptr;
     cudaFree(w.bbox_part);
     cudaFree(w.params);
@@ -1090,18 +1211,27 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     count_launch(s);
     stage_end(s, kStageScan, profile);
     stage_begin(s, kStageRecords, profile);
-    k_records<<<grid_for(n, 256), 256, 0, st>>>(skey, sidx, w.E, ctr + kCtrValid, w.depth, w.params, s->pos[in],
-                                                s->mass[in], w.rec, w.skip, w.nend, w.cap, n, ctr + kCtrLevel,
-                                                w.level_slots, w.level_cap, s->d_err);
-    count_launch(s);
+    k_records<<<grid_for(n, 256), 256, 0, st>>>(skey, sidx, w.E, ctr + kCtrValid, w.depth, s->pos[in], s->mass[in],
+                                                w.rec, w.skip, w.node_slot, w.cap, n, s->d_err);
+    k_nodes<<<grid_for(n, 256), 256, 0, st>>>(skey, w.E, ctr + kCtrValid, w.depth, w.params, w.node_slot, w.rec,
+                                              w.skip, w.nend, w.kids, w.parent, w.pending, w.arrived, w.nodeinfo,
+                                              w.cap, s->d_err);
+    count_launch(s, 2);
     stage_end(s, kStageRecords, profile);
     stage_begin(s, kStageSums, profile);
-    for (int d = w.depth; d >= 0; --d)
-        k_sums_level<<<grid_for(n, 256), 256, 0, st>>>(d, skey, w.E, ctr + kCtrValid, w.depth, w.rec, w.nend, w.msum,
-                                                        (uint32_t)w.cap, w.quad, w.kids,
-                                                        (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0, bbox ? 1 : 0,
-                                                        w.params, ctr + kCtrLevel, w.level_slots, w.level_cap);
-    count_launch(s, w.depth + 1);
+    {
+        const int safe = (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0;
+        if (w.quad)
+            k_bottom_up<true><<<grid_for(n, 256), 256, 0, st>>>(skey, w.E, ctr + kCtrValid, w.depth, w.rec, w.kids,
+                                                                w.parent, w.pending, w.arrived, w.nodeinfo, w.msum,
+                                                                w.quad, safe, bbox ? 1 : 0, w.params, (uint32_t)w.cap);
+        else
+            k_bottom_up<false><<<grid_for(n, 256), 256, 0, st>>>(skey, w.E, ctr + kCtrValid, w.depth, w.rec, w.kids,
+                                                                 w.parent, w.pending, w.arrived, w.nodeinfo, w.msum,
+                                                                 nullptr, safe, bbox ? 1 : 0, w.params,
+                                                                 (uint32_t)w.cap);
+    }
+    count_launch(s);
     stage_end(s, kStageSums, profile);
     stage_begin(s, kStageForce, profile);
     const float k = s->G * s->dt_eff;  // ForceShader.comp:145 (GRAVITATIONAL_CONST * SIMULATION_TIME)

@@ -48,6 +48,7 @@ constexpr uint32_t kSpinLimit = 1u << 24;
 
 struct BHParams {
     float cx, cy, scale, radius0;  // bounding box (fixed box: 0, 0, 1.024, 500000)
+    float inv_scale;               // float(1 / scale), taken once in FP64
 };
 
 struct BHWork {
@@ -60,7 +61,7 @@ struct BHWork {
     uint32_t* sort_status = nullptr;   // [passes][tiles][256]
     uint32_t* counters = nullptr;      // [0..3] sort tile tickets, [4] scan ticket, [5] bbox ticket,
                                        // [6] valid count, [7] internal count, [8..11] interaction
-                                       // and test counts (2 x u64), [12..27] nodes per level
+                                       // and test counts (2 x u64)
     uint32_t* scan_status = nullptr;   // [scan tiles]
     uint32_t* E = nullptr;             // [N_al + 1]
     float4* rec = nullptr;             // [cap + 32]
@@ -68,9 +69,12 @@ struct BHWork {
     uint32_t* nend = nullptr;          // [cap]
     float2* msum = nullptr;            // [cap]
     float4* quad = nullptr;            // [cap] {sxx, sxy, syy, -} (GS_FLAG_QUADRUPOLE)
-    uint4* kids = nullptr;             // [cap] child descriptors (GS_FLAG_GROUP_WALK)
-    uint32_t* level_slots = nullptr;   // [depth+1][level_cap] slots that start a node of that level
-    uint32_t level_cap = 0;
+    uint4* kids = nullptr;             // [cap] child descriptors of internal records
+    uint32_t* parent = nullptr;        // [cap] parent record of an internal record
+    uint32_t* pending = nullptr;       // [cap] internal children of a record
+    uint32_t* arrived = nullptr;       // [cap] internal children finished (bottom-up tickets)
+    uint2* nodeinfo = nullptr;         // [cap] {start slot, level} of an internal record
+    uint32_t* node_slot = nullptr;     // [cap] start slot of internal node j (ordinal)
     float* bbox_part = nullptr;        // [blocks][4]
     BHParams* params = nullptr;        // device
     uint32_t sort_tiles = 0, scan_tiles = 0;

@@ -280,7 +280,7 @@ static inline int fixed_box_key(float px, float py, uint32_t* key) {
 }
 
 typedef struct {
-    float cx, cy, scale, radius0;
+    float cx, cy, scale, radius0, inv_scale;
 } bbox_params;
 
 /* Bounding-box mode: square box around min/max of all positions, 2^15 cells per axis. */
@@ -298,6 +298,7 @@ static bbox_params bbox_from_minmax(double minx, double maxx, double miny, doubl
     b.scale = (float)scale;
     double side0 = (double)(1u << BBOX_BITS) / (double)b.scale;
     b.radius0 = (float)(side0 * side0 * 0.5);
+    b.inv_scale = (float)(1.0 / (double)b.scale);
     return b;
 }
 
@@ -811,25 +812,28 @@ static inline uint32_t compact_bits(uint32_t v) { /* inverse of spread_bits */
 }
 
 /* Squared distance from the centre of mass (cx, cy) to the farthest corner of the cell
- * at level d that holds key `key` (the opening radius of ORC_BH_SAFE_RADIUS). */
+ * at level d that holds key `key` (the opening radius of ORC_BH_SAFE_RADIUS), in FP32:
+ *   fixed box:    side = 1000 / 2^d, x0 = -500 + ix * side          (both exact)
+ *   bounding box: side = 2^(D-d) * inv, x0 = cx + (ix * 2^(D-d) - 2^(D-1)) * inv
+ *                 with inv = float(1 / scale) taken once in FP64
+ *   m = max(|c - x0|, |x0 + side - c|) per axis, bmax^2 = fma(mx, mx, my * my) */
 static float cell_bmax2(int box_mode, const bbox_params* bp, int D, int d, uint32_t key, float cx, float cy) {
     uint32_t pre = key >> (2 * (D - d));
-    double ix = (double)compact_bits(pre), iy = (double)compact_bits(pre >> 1);
-    double x0, y0, side;
+    float ix = (float)compact_bits(pre), iy = (float)compact_bits(pre >> 1);
+    float x0, y0, side;
     if (box_mode == ORC_BOX_BOUNDING) {
-        double w = (double)(1u << (D - d));
-        side = w / (double)bp->scale;
-        x0 = (double)bp->cx + (ix * w - (double)(1u << (D - 1))) / (double)bp->scale;
-        y0 = (double)bp->cy + (iy * w - (double)(1u << (D - 1))) / (double)bp->scale;
+        float w = (float)(1u << (D - d));
+        side = w * bp->inv_scale;
+        x0 = bp->cx + (ix * w - (float)(1u << (D - 1))) * bp->inv_scale;
+        y0 = bp->cy + (iy * w - (float)(1u << (D - 1))) * bp->inv_scale;
     } else {
-        side = 2.0 * (double)SIM_SIZE / (double)(1u << d);
-        x0 = -(double)SIM_SIZE + ix * side;
-        y0 = -(double)SIM_SIZE + iy * side;
+        side = 2.0f * SIM_SIZE / (float)(1u << d);
+        x0 = -SIM_SIZE + ix * side;
+        y0 = -SIM_SIZE + iy * side;
     }
-    double ax = fabs((double)cx - x0), bx = fabs(x0 + side - (double)cx);
-    double ay = fabs((double)cy - y0), by = fabs(y0 + side - (double)cy);
-    double mx = ax > bx ? ax : bx, my = ay > by ? ay : by;
-    return (float)(mx * mx + my * my);
+    float mx = fmaxf(fabsf(cx - x0), fabsf((x0 + side) - cx));
+    float my = fmaxf(fabsf(cy - y0), fabsf((y0 + side) - cy));
+    return fmaf(mx, mx, my * my);
 }
 
 int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in,
@@ -851,7 +855,8 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
     uint32_t* skey = (uint32_t*)malloc((size_t)n_al * sizeof(uint32_t));
     uint32_t* sidx = (uint32_t*)malloc((size_t)n_al * sizeof(uint32_t));
     float radius0;
-    bbox_params bp = {0.0f, 0.0f, (float)GRID / (2.0f * SIM_SIZE), SIM_SIZE * SIM_SIZE * 2.0f};
+    bbox_params bp = {0.0f, 0.0f, (float)GRID / (2.0f * SIM_SIZE), SIM_SIZE * SIM_SIZE * 2.0f,
+                      2.0f * SIM_SIZE / (float)GRID};
 
     if (box_mode == ORC_BOX_BOUNDING) {
         double mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
