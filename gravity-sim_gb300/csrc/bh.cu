@@ -792,13 +792,56 @@ k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, 
 // all lanes then sum the items as a dense stream (quadrupole term for nodes).
 // ------------------------------------------------------------------------------------
 constexpr int kGroupWarps = 4;
-constexpr int kStackCap = 2048;   // records still to test; depth bound (levels x 128) stays below
-constexpr int kItemCap = 256;     // interaction items between evaluations
+// Records still to test.  Pops take the top 32 and push at most four internal children
+// each, one level deeper, so the stack holds at most one block of <= 128 entries per level
+// and blocks of strictly increasing level: <= 96 * D + 128 = 1568 for D = 15 (a full
+// four-way tree reaches 1216).  Overflow is still checked and reported.
+constexpr int kStackCap = 1600;
+constexpr int kItemCap = 128;     // interaction items between evaluations
 constexpr uint32_t kItemNode = 0x80000000u;
+
+// 1/sqrt: correctly rounded (REFERENCE math) or the hardware approximation (FAST math;
+// d2 >= eps^2 > 0 is never subnormal, so the flush-to-zero form loses nothing)
+__device__ __forceinline__ float rsqrt_fast(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 template <bool EXACT>
 __device__ __forceinline__ float inv_sqrt(float d2) {
-    return EXACT ? __fdiv_rn(1.0f, __fsqrt_rn(d2)) : rsqrtf(d2);
+    return EXACT ? __fdiv_rn(1.0f, __fsqrt_rn(d2)) : rsqrt_fast(d2);
+}
+
+// Packed two-lane FP32 (Blackwell f32x2): each lane of the pair rounds exactly like the
+// scalar instruction, so a packed evaluation gives the same bits as two scalar ones.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
 }
 
 template <bool EXACT>
@@ -830,60 +873,147 @@ __device__ __forceinline__ void quadrupole(float4 q, float4 m2, float px, float 
     ay = fmaf(-t3, sry, fmaf(dy, coef, ay));
 }
 
+// Two particle leaves a (into accumulator 0) and b (into accumulator 1) at once.
+template <bool EXACT>
+__device__ __forceinline__ void monopole2(float4 a, float4 b, float2 P, float2 Q, float2 E2, float2& acx,
+                                          float2& acy) {
+    const float2 dx = sub2(make_float2(a.x, b.x), P), dy = sub2(make_float2(a.y, b.y), Q);
+    const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
+    const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
+    const float2 sc = mul2(mul2(mul2(make_float2(a.z, b.z), r), r), r);
+    acx = fma2(dx, sc, acx);
+    acy = fma2(dy, sc, acy);
+}
+
+// Two nodes a (accumulator 0) and b (accumulator 1) with their second moments.
+template <bool EXACT>
+__device__ __forceinline__ void quadrupole2(float4 a, float4 b, float4 qa, float4 qb, float2 P, float2 Q, float2 E2,
+                                            float2& acx, float2& acy) {
+    const float2 dx = sub2(make_float2(a.x, b.x), P), dy = sub2(make_float2(a.y, b.y), Q);
+    const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
+    const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
+    const float2 r2 = mul2(r, r);
+    const float2 r3 = mul2(r2, r);
+    const float2 r5 = mul2(r3, r2);
+    const float2 r7 = mul2(r5, r2);
+    const float2 sxx = make_float2(qa.x, qb.x), sxy = make_float2(qa.y, qb.y), syy = make_float2(qa.z, qb.z);
+    const float2 srx = fma2(sxx, dx, mul2(sxy, dy));
+    const float2 sry = fma2(sxy, dx, mul2(syy, dy));
+    const float2 u = fma2(dx, srx, mul2(dy, sry));
+    const float2 T = add2(sxx, syy);
+    const float2 coef = fma2(mul2(make_float2(7.5f, 7.5f), u), r7,
+                             fma2(mul2(make_float2(-1.5f, -1.5f), T), r5, mul2(make_float2(a.z, b.z), r3)));
+    const float2 nt3 = mul2(make_float2(-3.0f, -3.0f), r5);
+    acx = fma2(nt3, srx, fma2(dx, coef, acx));
+    acy = fma2(nt3, sry, fma2(dy, coef, acy));
+}
+
 struct GroupSmem {
     uint32_t stack[kStackCap];
     uint32_t it_start[kItemCap];
     uint32_t it_count[kItemCap];  // record count, kItemNode for a node item
+    uint32_t off[kItemCap];       // exclusive record offsets of the items
     float4 rec[32];               // gathered records of one evaluation chunk
     float4 quad[32];
-    uint32_t off[32];             // exclusive record offsets of the items of a batch
 };
 
-// Sum the n_items items in order: batches of 32 items, flattened 32 records at a time;
-// lane l gathers record l of the chunk (coalesced for leaf ranges), every lane then
-// accumulates the chunk in order from shared memory.
+// One record into accumulator `which` (0: .x of the pairs, 1: .y).
+template <bool EXACT, bool QUAD>
+__device__ __forceinline__ void eval_one(const GroupSmem& g, uint32_t j, int which, float px, float py, float eps2,
+                                         float2& acx, float2& acy) {
+    const float4 q = g.rec[j];
+    float ax = which ? acx.y : acx.x, ay = which ? acy.y : acy.x;
+    if (QUAD && __float_as_uint(q.w)) quadrupole<EXACT>(q, g.quad[j], px, py, eps2, ax, ay);
+    else monopole<EXACT>(q, px, py, eps2, ax, ay);
+    if (which) {
+        acx.y = ax;
+        acy.y = ay;
+    } else {
+        acx.x = ax;
+        acy.x = ay;
+    }
+}
+
+// Gather flat record f of the item list into registers (last item with off <= f).
+template <bool QUAD>
+__device__ __forceinline__ void gather_record(const GroupSmem& g, uint32_t n_items, uint32_t f,
+                                              const float4* __restrict__ rec, const float4* __restrict__ quad,
+                                              float4& q, float4& qq) {
+    uint32_t lo = 0, hi = n_items - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (g.off[mid] <= f) lo = mid;
+        else hi = mid - 1;
+    }
+    const uint32_t c = g.it_count[lo];
+    const uint32_t r = g.it_start[lo] + (f - g.off[lo]);
+    const uint32_t node = c & kItemNode;
+    q = __ldg(&rec[r]);
+    if (QUAD && node) qq = __ldg(&quad[r]);
+    q.w = __uint_as_float(node);  // the opening radius is not needed here: reuse w as the flag
+}
+
+// Sum the n_items items in order, 32 records at a time: lane l gathers record l of the
+// next chunk into registers while the current chunk is summed from shared memory.  The
+// k-th record of the walk (rk counts them) goes into accumulator k mod 2 (.x / .y of
+// acx, acy); consecutive records of the same kind are evaluated in pairs with packed
+// f32x2 instructions.
 template <bool EXACT, bool QUAD>
 __device__ __forceinline__ void eval_items(GroupSmem& g, uint32_t n_items, const float4* __restrict__ rec,
                                            const float4* __restrict__ quad, float px, float py, float eps2,
-                                           float& ax, float& ay, int lane) {
-    for (uint32_t b0 = 0; b0 < n_items; b0 += 32) {
-        const uint32_t nb = min(n_items - b0, 32u);
-        const uint32_t cnt = lane < (int)nb ? (g.it_count[b0 + lane] & ~kItemNode) : 0u;
-        uint32_t x = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
-        g.off[lane] = x - cnt;
+                                           float2& acx, float2& acy, uint32_t& rk, int lane) {
+    if (!n_items) return;
+    const float2 P = make_float2(px, px), Q = make_float2(py, py), E2 = make_float2(eps2, eps2);
+    // exclusive record offsets of all items: lane l owns items [8l, 8l + 8)
+    uint32_t c8[kItemCap / 32], sum = 0;
+#pragma unroll
+    for (int t = 0; t < kItemCap / 32; ++t) {
+        const uint32_t it = lane * (kItemCap / 32) + t;
+        c8[t] = it < n_items ? (g.it_count[it] & ~kItemNode) : 0u;
+        sum += c8[t];
+    }
+    uint32_t x = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
+    uint32_t run = x - sum;
+#pragma unroll
+    for (int t = 0; t < kItemCap / 32; ++t) {
+        g.off[lane * (kItemCap / 32) + t] = run;
+        run += c8[t];
+    }
+    __syncwarp();
+    float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qq = q;
+    if ((uint32_t)lane < total) gather_record<QUAD>(g, n_items, lane, rec, quad, q, qq);
+    for (uint32_t f0 = 0; f0 < total; f0 += 32) {
+        g.rec[lane] = q;
+        if (QUAD) g.quad[lane] = qq;
         __syncwarp();
-        for (uint32_t f0 = 0; f0 < total; f0 += 32) {
-            const uint32_t f = f0 + lane;
-            uint32_t node = 0;
-            if (f < total) {  // item j of this batch holding flat record f: last j with off[j] <= f
-                uint32_t lo = 0, hi = nb - 1;
-                while (lo < hi) {
-                    const uint32_t mid = (lo + hi + 1) >> 1;
-                    if (g.off[mid] <= f) lo = mid;
-                    else hi = mid - 1;
-                }
-                const uint32_t c = g.it_count[b0 + lo];
-                const uint32_t r = g.it_start[b0 + lo] + (f - g.off[lo]);
-                node = c & kItemNode;
-                float4 q = __ldg(&rec[r]);
-                if (QUAD && node) g.quad[lane] = __ldg(&quad[r]);
-                q.w = __uint_as_float(node);  // the opening radius is not needed here: reuse w as the flag
-                g.rec[lane] = q;
-            }
-            __syncwarp();
-            const uint32_t m = min(total - f0, 32u);
-            for (uint32_t j = 0; j < m; ++j) {
-                const float4 q = g.rec[j];
-                if (QUAD && __float_as_uint(q.w)) quadrupole<EXACT>(q, g.quad[j], px, py, eps2, ax, ay);
-                else monopole<EXACT>(q, px, py, eps2, ax, ay);
-            }
-            __syncwarp();
+        const uint32_t fn = f0 + 32 + lane;  // prefetch the next chunk while this one is summed
+        if (fn < total) gather_record<QUAD>(g, n_items, fn, rec, quad, q, qq);
+        const uint32_t m = min(total - f0, 32u);
+        uint32_t j = 0;
+        if (rk & 1u) {  // odd running index: the first record goes alone into accumulator 1
+            eval_one<EXACT, QUAD>(g, 0, 1, px, py, eps2, acx, acy);
+            j = 1;
         }
+        for (; j + 1 < m; j += 2) {  // record j -> accumulator 0, j + 1 -> accumulator 1
+            const float4 a = g.rec[j], b = g.rec[j + 1];
+            const bool na = QUAD && __float_as_uint(a.w), nb2 = QUAD && __float_as_uint(b.w);
+            if (!na && !nb2) {
+                monopole2<EXACT>(a, b, P, Q, E2, acx, acy);
+            } else if (na && nb2) {
+                quadrupole2<EXACT>(a, b, g.quad[j], g.quad[j + 1], P, Q, E2, acx, acy);
+            } else {
+                eval_one<EXACT, QUAD>(g, j, 0, px, py, eps2, acx, acy);
+                eval_one<EXACT, QUAD>(g, j + 1, 1, px, py, eps2, acx, acy);
+            }
+        }
+        if (j < m) eval_one<EXACT, QUAD>(g, j, 0, px, py, eps2, acx, acy);
+        rk += m;
+        __syncwarp();
     }
 }
 
@@ -929,7 +1059,8 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
         by0[b] = y0;
         by1[b] = y1;
     }
-    float ax = 0.0f, ay = 0.0f;
+    float2 acx = make_float2(0.0f, 0.0f), acy = make_float2(0.0f, 0.0f);  // accumulators 0 (.x) and 1 (.y)
+    uint32_t rk = 0;  // records summed so far
     unsigned long long n_int = 0, n_test = 0;
     uint32_t size = 0, n_items = 0;
     if (skip[0] == 1u) {  // a single particle: the root is its leaf
@@ -946,7 +1077,7 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
 
     while (size > 0) {
         if (n_items > (uint32_t)(kItemCap - 64)) {
-            eval_items<EXACT, QUAD>(g, n_items, rec, quad, p.x, p.y, eps2, ax, ay, lane);
+            eval_items<EXACT, QUAD>(g, n_items, rec, quad, p.x, p.y, eps2, acx, acy, rk, lane);
             n_items = 0;
         }
         const uint32_t np = min(size, 32u);
@@ -1029,11 +1160,12 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
         if (npu > 1) dst[1] = pu1;
         if (npu > 2) dst[2] = pu2;
         if (npu > 3) dst[3] = pu3;
+
         n_items += itot;
         size += ptot;
         __syncwarp();
     }
-    eval_items<EXACT, QUAD>(g, n_items, rec, quad, p.x, p.y, eps2, ax, ay, lane);
+    eval_items<EXACT, QUAD>(g, n_items, rec, quad, p.x, p.y, eps2, acx, acy, rk, lane);
     if (COUNT) {
         if (skip[0] == 1u && lane == 0) n_int += 1;
         for (int o = 16; o; o >>= 1) n_int += __shfl_xor_sync(0xffffffffu, n_int, o);
@@ -1044,6 +1176,7 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
         }
     }
     if (!valid) return;
+    const float ax = acx.x + acx.y, ay = acy.x + acy.y;
     if (acc_rec) acc_rec[i] = make_float2(ax, ay);
     const float2 v = vel_in[i];
     const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);

@@ -339,6 +339,7 @@ typedef struct {
     int group_walk;         /* ORC_BH_GROUP_WALK semantics */
     uint32_t* max_stack;    /* per worker */
     uint64_t* max_inter;    /* per worker: largest per-warp interaction count */
+    uint32_t group_size;    /* particles per group walk (32, or 64 with ORC_BH_GROUP64) */
 } walk_ctx;
 
 static void walk_warp(void* p, uint64_t item, int worker) {
@@ -422,32 +423,34 @@ static void walk_warp(void* p, uint64_t item, int worker) {
  *   - every particle of the group then sums the items in order (nodes with the
  *     quadrupole term, leaves as monopoles) and is integrated. */
 #define GROUP_STACK_CAP 2048
+#define GMAX 64
 static void group_walk_warp(void* p, uint64_t item, int worker) {
     const walk_ctx* c = (const walk_ctx*)p;
     const uint64_t w = item * c->stride;
-    float px[WARP], py[WARP], ax[WARP], ay[WARP];
-    int valid[WARP];
+    float px[GMAX], py[GMAX], ax[GMAX][2], ay[GMAX][2];
+    int valid[GMAX];
+    const uint32_t G = c->group_size;
     int nvalid = 0;
     float gx0[4], gx1[4], gy0[4], gy1[4];
     for (int b = 0; b < 4; ++b) {
         gx0[b] = gy0[b] = INFINITY;
         gx1[b] = gy1[b] = -INFINITY;
     }
-    for (int l = 0; l < WARP; ++l) {
-        uint32_t s = (uint32_t)w * WARP + (uint32_t)l;
+    for (uint32_t l = 0; l < G; ++l) {
+        uint32_t s = (uint32_t)w * G + l;
         uint32_t i = c->src[s];
         valid[l] = i != c->n_al;
         px[l] = valid[l] ? c->pos_in[2 * i] : 0.0f;
         py[l] = valid[l] ? c->pos_in[2 * i + 1] : 0.0f;
-        ax[l] = ay[l] = 0.0f;
+        ax[l][0] = ay[l][0] = ax[l][1] = ay[l][1] = 0.0f;
         nvalid += valid[l];
     }
     if (!nvalid || !c->tree_size) return;
     {
-        const uint32_t kf = c->skey[(uint32_t)w * WARP], kl = c->skey[(uint32_t)w * WARP + (uint32_t)nvalid - 1];
+        const uint32_t kf = c->skey[(uint32_t)w * G], kl = c->skey[(uint32_t)w * G + (uint32_t)nvalid - 1];
         const int shift = kf == kl ? -1 : ((31 - __builtin_clz(kf ^ kl)) & ~1);
         for (int l = 0; l < nvalid; ++l) { /* valid lanes are a prefix of the warp */
-            const int b = shift < 0 ? 0 : (int)((c->skey[(uint32_t)w * WARP + (uint32_t)l] >> shift) & 3u);
+            const int b = shift < 0 ? 0 : (int)((c->skey[(uint32_t)w * G + (uint32_t)l] >> shift) & 3u);
             gx0[b] = fminf(gx0[b], px[l]);
             gx1[b] = fmaxf(gx1[b], px[l]);
             gy0[b] = fminf(gy0[b], py[l]);
@@ -457,7 +460,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
     uint32_t stack[GROUP_STACK_CAP + 160];
     uint32_t size = 1, max_size = 1;
     stack[0] = 0;
-    uint64_t inter = 0, visits = 0;
+    uint64_t inter = 0, visits = 0, rk = 0; /* rk: running record index of the warp */
     while (size) {
         uint32_t np = size < WARP ? size : WARP;
         uint32_t base = size - np;
@@ -481,19 +484,21 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
             }
             if (accept) { /* one item: the record itself */
                 const float nx = c->npos[2 * n], ny = c->npos[2 * n + 1], nm = c->nmass[n];
-                for (int l = 0; l < WARP; ++l) {
+                const int a = (int)(rk & 1u);
+                for (uint32_t l = 0; l < G; ++l) {
                     if (!valid[l]) continue;
                     float dx = nx - px[l], dy = ny - py[l];
                     float d2 = pair_d2(dx, dy, c->eps2);
                     if (c->quad && sk > 1) {
                         quad_accumulate(dx, dy, d2, nm, c->quad[3 * n], c->quad[3 * n + 1], c->quad[3 * n + 2],
-                                        &ax[l], &ay[l]);
+                                        &ax[l][a], &ay[l][a]);
                     } else {
                         float sc = pair_scale(nm, d2);
-                        ax[l] = fmaf(dx, sc, ax[l]);
-                        ay[l] = fmaf(dy, sc, ay[l]);
+                        ax[l][a] = fmaf(dx, sc, ax[l][a]);
+                        ay[l][a] = fmaf(dy, sc, ay[l][a]);
                     }
                 }
+                ++rk;
                 inter += (uint64_t)nvalid;
                 continue;
             }
@@ -505,13 +510,15 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                     while (r < end && c->skip[r] == 1) ++r;
                     for (uint32_t q = ch; q < r; ++q) {
                         const float nx = c->npos[2 * q], ny = c->npos[2 * q + 1], nm = c->nmass[q];
-                        for (int l = 0; l < WARP; ++l) {
+                        const int a = (int)(rk & 1u);
+                        for (uint32_t l = 0; l < G; ++l) {
                             if (!valid[l]) continue;
                             float dx = nx - px[l], dy = ny - py[l];
                             float sc = pair_scale(nm, pair_d2(dx, dy, c->eps2));
-                            ax[l] = fmaf(dx, sc, ax[l]);
-                            ay[l] = fmaf(dy, sc, ay[l]);
+                            ax[l][a] = fmaf(dx, sc, ax[l][a]);
+                            ay[l][a] = fmaf(dy, sc, ay[l][a]);
                         }
+                        ++rk;
                     }
                     inter += (uint64_t)nvalid * (r - ch);
                     ch = r;
@@ -525,11 +532,12 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
         if (size > max_size) max_size = size;
         if (size > GROUP_STACK_CAP) size = GROUP_STACK_CAP; /* reported through max_stack */
     }
-    for (int l = 0; l < WARP; ++l) {
+    for (uint32_t l = 0; l < G; ++l) {
         if (!valid[l]) continue;
-        uint32_t i = c->src[(uint32_t)w * WARP + (uint32_t)l];
+        uint32_t i = c->src[(uint32_t)w * G + l];
         float vx = c->vel_in[2 * i], vy = c->vel_in[2 * i + 1];
-        float nvx = fmaf(ax[l], c->k, vx), nvy = fmaf(ay[l], c->k, vy);
+        const float axl = ax[l][0] + ax[l][1], ayl = ay[l][0] + ay[l][1];
+        float nvx = fmaf(axl, c->k, vx), nvy = fmaf(ayl, c->k, vy);
         c->pos_out[2 * i] = fmaf(vx + nvx, c->hdt, px[l]);
         c->pos_out[2 * i + 1] = fmaf(vy + nvy, c->hdt, py[l]);
         c->vel_out[2 * i] = nvx;
@@ -550,7 +558,7 @@ static void run_walk(walk_ctx* c, int nthreads, orc_bh_out* out) {
     c->max_stack = mstack;
     c->max_inter = minter;
     c->stride = out && out->walk_stride > 1 ? out->walk_stride : 1;
-    uint64_t warps = c->n_al / WARP;
+    uint64_t warps = c->n_al / (c->group_walk ? c->group_size : WARP);
     double t0 = now_seconds();
     parallel_for(nthreads, (warps + c->stride - 1) / c->stride, 4, c->group_walk ? group_walk_warp : walk_warp, c);
     if (out) {
@@ -1018,6 +1026,7 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
     wc.quad = quad;
     wc.group_walk = (flags & ORC_BH_GROUP_WALK) != 0;
     wc.skey = skey;
+    wc.group_size = (flags & ORC_BH_GROUP64) ? 64 : 32;
     wc.tree_size = tree_size;
     wc.src = src;
     wc.n_al = n_al;
