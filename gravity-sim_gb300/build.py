@@ -78,6 +78,16 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             raise RuntimeError("link failed")
         os.replace(LIB + ".tmp", LIB)
+    cli_src = os.path.join(HERE, "cli", "main.cpp")
+    cli = os.path.join(LIBDIR, "gsim-cli")
+    if force or _stale(cli, [cli_src, LIB, os.path.join(INCLUDE, "gsim.hpp")]):
+        cmd = ["g++", "-O2", "-std=c++17", "-I" + INCLUDE, cli_src, "-o", cli + ".tmp", "-L" + LIBDIR, "-lgsim",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+            raise RuntimeError("cli link failed")
+        os.replace(cli + ".tmp", cli)
     return LIB
 
 

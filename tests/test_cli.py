@@ -1,0 +1,55 @@
+"""gsim-cli: the headless command line with the reference's flags (src/Main.cpp:20-48),
+built on the C++ mirror include/gsim.hpp."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "gravity-sim_gb300", "lib", "gsim-cli")
+
+
+def _run(args, **kw):
+    return subprocess.run([CLI] + args, capture_output=True, text=True, timeout=600, **kw)
+
+
+def test_help_exits(gs):
+    r = _run(["--help"])
+    assert r.returncode == 0 and "--simulation-algorithm" in r.stdout and "--particles-out" in r.stdout
+
+
+def test_argument_checks(gs):
+    r = _run(["--simulation-algorithm=barnes-hut", "--simulation-count=5"])
+    assert r.returncode == 1 and "generation args" in r.stdout
+    r = _run(["--particle-count=10", "--generate-type=random", "--generate-size=10", "--min-mass=1",
+              "--max-mass=2", "--simulation-count=5"])
+    assert r.returncode == 1 and "simulation algorithm" in r.stdout
+    r = _run(["--particle-count=10", "--generate-type=random", "--generate-size=10", "--min-mass=1",
+              "--max-mass=2", "--simulation-algorithm=direct-sum"])
+    assert r.returncode == 1 and "simulation count" in r.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algo,extra", [("barnes-hut", ["--math=reference"]), ("direct-sum", []),
+                                        ("barnes-hut", ["--box=bbox", "--accurate", "--accuracy-parameter=0.35"])])
+def test_file_roundtrip_matches_binding(gs, tmp_path, algo, extra):
+    pos, vel, mass = gs.generate(gs.GEN_GALAXY, 3000, size=100.0, seed=17)
+    fin, fout = str(tmp_path / "in.txt"), str(tmp_path / "out.txt")
+    gs.write_particles(fin, pos, vel, mass)
+    r = _run([f"--particles-in={fin}", f"--particles-out={fout}", f"--simulation-algorithm={algo}",
+              "--simulation-count=7", "--no-graphics", "--benchmark"] + extra)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Average runtime/simulation" in r.stdout
+    p2, v2, m2 = gs.read_particles(fin)  # the values the CLI started from
+    kw = dict(algorithm=gs.BARNES_HUT if algo == "barnes-hut" else gs.DIRECT_SUM)
+    if "--math=reference" in extra:
+        kw["math_mode"] = gs.MATH_REFERENCE
+    if "--box=bbox" in extra:
+        kw.update(box_mode=gs.BOX_BOUNDING, flags=gs.FLAGS_ACCURATE, accuracy_parameter=0.35)
+    with gs.Simulation(p2, v2, m2, **kw) as sim:
+        sim.run(7)
+        p, v, m = sim.get_particles()
+    fref = str(tmp_path / "ref.txt")
+    gs.write_particles(fref, p, v, m)
+    assert open(fout).read() == open(fref).read()
