@@ -33,6 +33,16 @@
 namespace gsim {
 namespace {
 
+// Every stage is written as a __device__ body that takes its block's index and the
+// number of blocks working on its system.  A plain launch passes blockIdx.x / gridDim.x;
+// a batched launch (one grid over many systems) passes the block's index within its
+// system.  No body's result depends on how many blocks it gets, so a system computes the
+// same bits alone and in a batch.
+struct Blk {
+    uint32_t id, count;
+};
+__device__ __forceinline__ Blk grid_blk() { return Blk{blockIdx.x, gridDim.x}; }
+
 // ------------------------------------------------------------------------------------
 // keys
 // ------------------------------------------------------------------------------------
@@ -80,13 +90,13 @@ __device__ __forceinline__ int slot_dmax(const uint32_t* k, uint32_t s, uint32_t
 constexpr int kBBoxThreads = 256;
 constexpr int kBBoxBlocks = 152;
 
-__global__ void __launch_bounds__(kBBoxThreads)
-k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uint32_t* __restrict__ ticket,
-       BHParams* __restrict__ out) {
+__device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ pos, uint32_t n,
+                                          float* __restrict__ part, uint32_t* __restrict__ ticket,
+                                          BHParams* __restrict__ out) {
     __shared__ float s[4][kBBoxThreads / 32];
     __shared__ bool last;
     float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = blk.id * kBBoxThreads + threadIdx.x; i < n; i += blk.count * kBBoxThreads) {
         float2 p = pos[i];
         mnx = fminf(mnx, p.x);
         mxx = fmaxf(mxx, p.x);
@@ -114,19 +124,19 @@ k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uin
             mny = fminf(mny, s[2][w]);
             mxy = fmaxf(mxy, s[3][w]);
         }
-        part[4 * blockIdx.x + 0] = mnx;
-        part[4 * blockIdx.x + 1] = mxx;
-        part[4 * blockIdx.x + 2] = mny;
-        part[4 * blockIdx.x + 3] = mxy;
+        part[4 * blk.id + 0] = mnx;
+        part[4 * blk.id + 1] = mxx;
+        part[4 * blk.id + 2] = mny;
+        part[4 * blk.id + 3] = mxy;
         __threadfence();
-        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+        last = atomicAdd(ticket, 1u) == blk.count - 1;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
     // the last block reduces all block partials in parallel (min/max are exact in any order)
     mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
-    for (uint32_t bl = threadIdx.x; bl < gridDim.x; bl += blockDim.x) {
+    for (uint32_t bl = threadIdx.x; bl < blk.count; bl += kBBoxThreads) {
         mnx = fminf(mnx, __ldcg(&part[4 * bl + 0]));
         mxx = fmaxf(mxx, __ldcg(&part[4 * bl + 1]));
         mny = fminf(mny, __ldcg(&part[4 * bl + 2]));
@@ -172,23 +182,29 @@ k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uin
     *out = p;
 }
 
+__global__ void __launch_bounds__(kBBoxThreads)
+k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uint32_t* __restrict__ ticket,
+       BHParams* __restrict__ out) {
+    bbox_body(grid_blk(), pos, n, part, ticket, out);
+}
+
 // ------------------------------------------------------------------------------------
 // keygen + digit histograms
 // ------------------------------------------------------------------------------------
 constexpr int kKeyThreads = 256;
 
-__global__ void __launch_bounds__(kKeyThreads)
-k_keygen(int bbox_mode, const BHParams* __restrict__ bp, float2* __restrict__ pos_in,
-         float* mass_in, float2* __restrict__ pos_out, float* mass_out,  // mass sets may alias
-         uint32_t n, uint32_t* __restrict__ keys, uint32_t* __restrict__ hist, int passes,
-         uint32_t* __restrict__ valid_count) {
+__device__ __forceinline__ void keygen_body(Blk blk, int bbox_mode, const BHParams* __restrict__ bp,
+                                            float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos_out,
+                                            float* mass_out,  // mass sets may alias
+                                            uint32_t n, uint32_t* __restrict__ keys, uint32_t* __restrict__ hist,
+                                            int passes, uint32_t* __restrict__ valid_count) {
     __shared__ uint32_t sh[4][256];
     for (int i = threadIdx.x; i < 4 * 256; i += kKeyThreads) (&sh[0][0])[i] = 0u;
     __syncthreads();
     BHParams p;
     if (bbox_mode) p = *bp;
     uint32_t valid = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = blk.id * kKeyThreads + threadIdx.x; i < n; i += blk.count * kKeyThreads) {
         float2 q = pos_in[i];
         uint32_t key;
         if (bbox_mode) {
@@ -214,6 +230,13 @@ k_keygen(int bbox_mode, const BHParams* __restrict__ bp, float2* __restrict__ po
         uint32_t c = (&sh[0][0])[i];
         if (c) atomicAdd(&hist[i], c);
     }
+}
+
+__global__ void __launch_bounds__(kKeyThreads)
+k_keygen(int bbox_mode, const BHParams* __restrict__ bp, float2* __restrict__ pos_in, float* mass_in,
+         float2* __restrict__ pos_out, float* mass_out, uint32_t n, uint32_t* __restrict__ keys,
+         uint32_t* __restrict__ hist, int passes, uint32_t* __restrict__ valid_count) {
+    keygen_body(grid_blk(), bbox_mode, bp, pos_in, mass_in, pos_out, mass_out, n, keys, hist, passes, valid_count);
 }
 
 // ------------------------------------------------------------------------------------
@@ -251,11 +274,14 @@ __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
 // ------------------------------------------------------------------------------------
 // onesweep radix pass (stable, 8-bit digit at `shift`)
 // ------------------------------------------------------------------------------------
+// Tiles are taken from a per-system ticket, so a tile only waits on tiles that earlier
+// running blocks took: no deadlock, whichever grid the blocks belong to.
 template <bool IDENTITY>
-__global__ void __launch_bounds__(kSortThreads)
-k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
-            uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
-            uint32_t* __restrict__ status, uint32_t* __restrict__ ticket, int* __restrict__ err) {
+__device__ __forceinline__ void sort_pass_body(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
+                                               int shift, const uint32_t* __restrict__ hist,
+                                               uint32_t* __restrict__ status, uint32_t* __restrict__ ticket,
+                                               int* __restrict__ err) {
     constexpr int KPT = kSortKeysPerThread;
     constexpr int W = kSortThreads / 32;
     __shared__ uint32_t s_tile;
@@ -356,13 +382,22 @@ k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, 
     }
 }
 
+template <bool IDENTITY>
+__global__ void __launch_bounds__(kSortThreads)
+k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+            uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
+            uint32_t* __restrict__ status, uint32_t* __restrict__ ticket, int* __restrict__ err) {
+    sort_pass_body<IDENTITY>(kin, vin, kout, vout, n, shift, hist, status, ticket, err);
+}
+
 // ------------------------------------------------------------------------------------
 // internal nodes per slot + exclusive scan (decoupled look-back)
 // ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kScanThreads)
-k_meta_scan(const uint32_t* __restrict__ skey, uint32_t n_items, const uint32_t* __restrict__ valid_count,
-            int D, uint32_t* __restrict__ E, uint32_t* __restrict__ status, uint32_t* __restrict__ ticket,
-            uint32_t* __restrict__ internal_count, int* __restrict__ err) {
+__device__ __forceinline__ void meta_scan_body(const uint32_t* __restrict__ skey, uint32_t n_items,
+                                               const uint32_t* __restrict__ valid_count, int D,
+                                               uint32_t* __restrict__ E, uint32_t* __restrict__ status,
+                                               uint32_t* __restrict__ ticket, uint32_t* __restrict__ internal_count,
+                                               int* __restrict__ err) {
     __shared__ uint32_t s_tile, s_prefix;
     __shared__ uint32_t s_warp[8];
     const int t = threadIdx.x;
@@ -421,6 +456,13 @@ k_meta_scan(const uint32_t* __restrict__ skey, uint32_t n_items, const uint32_t*
     }
 }
 
+__global__ void __launch_bounds__(kScanThreads)
+k_meta_scan(const uint32_t* __restrict__ skey, uint32_t n_items, const uint32_t* __restrict__ valid_count,
+            int D, uint32_t* __restrict__ E, uint32_t* __restrict__ status, uint32_t* __restrict__ ticket,
+            uint32_t* __restrict__ internal_count, int* __restrict__ err) {
+    meta_scan_body(skey, n_items, valid_count, D, E, status, ticket, internal_count, err);
+}
+
 // ------------------------------------------------------------------------------------
 // preorder records (topology, radius, particle leaves)
 // ------------------------------------------------------------------------------------
@@ -457,13 +499,15 @@ __device__ __forceinline__ uint32_t leaf_of(const uint32_t* skey, const uint32_t
 // One thread per sorted slot s: the particle leaf of s, and the slot of every internal
 // node that starts at s in the node -> slot map (internal ordinal j = E(s) + d - dmin(s),
 // record index s + j).
-__global__ void __launch_bounds__(256)
-k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ E,
-          const uint32_t* __restrict__ valid_count, int D, const float2* __restrict__ pos,
-          const float* __restrict__ mass, float4* __restrict__ rec, uint32_t* __restrict__ skip,
-          uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al, int* __restrict__ err) {
+__device__ __forceinline__ void records_body(Blk blk, const uint32_t* __restrict__ skey,
+                                             const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ E,
+                                             const uint32_t* __restrict__ valid_count, int D,
+                                             const float2* __restrict__ pos, const float* __restrict__ mass,
+                                             float4* __restrict__ rec, uint32_t* __restrict__ skip,
+                                             uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al,
+                                             int* __restrict__ err) {
     const uint32_t nv = *valid_count;
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += gridDim.x * blockDim.x) {
+    for (uint32_t s = blk.id * 256 + threadIdx.x; s < nv; s += blk.count * 256) {
         const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
         const uint32_t Es = E[s];
         const int e = dmax >= dmin ? dmax - dmin + 1 : 0;
@@ -484,18 +528,28 @@ k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, 
     }
 }
 
+__global__ void __launch_bounds__(256)
+k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ E,
+          const uint32_t* __restrict__ valid_count, int D, const float2* __restrict__ pos,
+          const float* __restrict__ mass, float4* __restrict__ rec, uint32_t* __restrict__ skip,
+          uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al, int* __restrict__ err) {
+    records_body(grid_blk(), skey, sidx, E, valid_count, D, pos, mass, rec, skip, node_slot, cap, n_al, err);
+}
+
 // One thread per internal node (d, s): skip (the reference's count.y), the level radius
 // of TreeMoveShader.comp:70-71, the cell end, the child descriptors, the parent link of
 // its internal children and the number of internal children the bottom-up pass waits for.
-__global__ void __launch_bounds__(256)
-k_nodes(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E, const uint32_t* __restrict__ counts,
-        int D, const BHParams* __restrict__ bp, const uint32_t* __restrict__ node_slot, float4* __restrict__ rec,
-        uint32_t* __restrict__ skip, uint32_t* __restrict__ nend, uint4* __restrict__ kids,
-        uint32_t* __restrict__ parent, uint32_t* __restrict__ pending, uint32_t* __restrict__ arrived,
-        uint2* __restrict__ nodeinfo, uint64_t cap, int* __restrict__ err) {
+__device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
+                                           const uint32_t* __restrict__ counts, int D,
+                                           const BHParams* __restrict__ bp, const uint32_t* __restrict__ node_slot,
+                                           float4* __restrict__ rec, uint32_t* __restrict__ skip,
+                                           uint32_t* __restrict__ nend, uint4* __restrict__ kids,
+                                           uint32_t* __restrict__ parent, uint32_t* __restrict__ pending,
+                                           uint32_t* __restrict__ arrived, uint2* __restrict__ nodeinfo,
+                                           uint64_t cap, int* __restrict__ err) {
     const uint32_t nv = counts[0], M = counts[1];
     const float radius0 = bp->radius0;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
+    for (uint32_t j = blk.id * 256 + threadIdx.x; j < M; j += blk.count * 256) {
         const uint32_t s = node_slot[j];
         const uint32_t at = s + j;
         if (s >= nv || at >= cap) {  // only after a failed sort or scan (error flag already set)
@@ -537,6 +591,16 @@ k_nodes(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E, const
         kids[at] = make_uint4(kid[0], kid[1], kid[2], kid[3]);
         pending[at] = nint;
     }
+}
+
+__global__ void __launch_bounds__(256)
+k_nodes(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E, const uint32_t* __restrict__ counts,
+        int D, const BHParams* __restrict__ bp, const uint32_t* __restrict__ node_slot, float4* __restrict__ rec,
+        uint32_t* __restrict__ skip, uint32_t* __restrict__ nend, uint4* __restrict__ kids,
+        uint32_t* __restrict__ parent, uint32_t* __restrict__ pending, uint32_t* __restrict__ arrived,
+        uint2* __restrict__ nodeinfo, uint64_t cap, int* __restrict__ err) {
+    nodes_body(grid_blk(), skey, E, counts, D, bp, node_slot, rec, skip, nend, kids, parent, pending, arrived,
+               nodeinfo, cap, err);
 }
 
 __device__ __forceinline__ uint32_t compact_bits(uint32_t v) {  // inverse of spread_bits
@@ -693,15 +757,17 @@ __device__ void compute_node(uint32_t at, int D, int safe, int bbox_mode, const 
 // Every node sums its children in the fixed Morton order, so the result does not depend
 // on which thread gets there.
 template <bool QUAD>
-__global__ void __launch_bounds__(256)
-k_bottom_up(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
-            const uint32_t* __restrict__ valid_count, int D, float4* rec, const uint4* __restrict__ kids,
-            const uint32_t* __restrict__ parent, const uint32_t* __restrict__ pending, uint32_t* arrived,
-            const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
-            const BHParams* __restrict__ bpp, uint32_t cap) {
+__device__ __forceinline__ void bottom_up_body(Blk blk, const uint32_t* __restrict__ skey,
+                                               const uint32_t* __restrict__ E,
+                                               const uint32_t* __restrict__ valid_count, int D, float4* rec,
+                                               const uint4* __restrict__ kids, const uint32_t* __restrict__ parent,
+                                               const uint32_t* __restrict__ pending, uint32_t* arrived,
+                                               const uint2* __restrict__ nodeinfo, float2* msum, float4* quad,
+                                               int safe, int bbox_mode, const BHParams* __restrict__ bpp,
+                                               uint32_t cap) {
     const uint32_t nv = *valid_count;
     const BHParams bp = *bpp;
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += gridDim.x * blockDim.x) {
+    for (uint32_t s = blk.id * 256 + threadIdx.x; s < nv; s += blk.count * 256) {
         const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
         if (dmax < dmin) continue;
         uint32_t at = s + E[s] + (uint32_t)(dmax - dmin);
@@ -718,21 +784,34 @@ k_bottom_up(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
     }
 }
 
+template <bool QUAD>
+__global__ void __launch_bounds__(256)
+k_bottom_up(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
+            const uint32_t* __restrict__ valid_count, int D, float4* rec, const uint4* __restrict__ kids,
+            const uint32_t* __restrict__ parent, const uint32_t* __restrict__ pending, uint32_t* arrived,
+            const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
+            const BHParams* __restrict__ bpp, uint32_t cap) {
+    bottom_up_body<QUAD>(grid_blk(), skey, E, valid_count, D, rec, kids, parent, pending, arrived, nodeinfo, msum,
+                         quad, safe, bbox_mode, bpp, cap);
+}
+
 // ------------------------------------------------------------------------------------
 // traversal + integrator (ForceShader.comp:78-152)
 // ------------------------------------------------------------------------------------
 constexpr int kForceWarps = 4;
 
 template <bool EXACT, bool COUNT>
-__global__ void __launch_bounds__(kForceWarps * 32)
-k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, const float4* __restrict__ rec,
-        const uint32_t* __restrict__ skip, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
-        float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
-        float eps2, float theta2, float k, float hdt, uint32_t cap, unsigned long long* __restrict__ stat) {
+__device__ __forceinline__ void force_body(Blk blk, const uint32_t* __restrict__ sidx,
+                                           const uint32_t* __restrict__ counts, const float4* __restrict__ rec,
+                                           const uint32_t* __restrict__ skip, const float2* __restrict__ pos_in,
+                                           const float2* __restrict__ vel_in, float2* __restrict__ pos_out,
+                                           float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
+                                           float eps2, float theta2, float k, float hdt, uint32_t cap,
+                                           unsigned long long* __restrict__ stat) {
     __shared__ float4 wrec[kForceWarps][32];
     __shared__ uint32_t wskip[kForceWarps][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t group = blockIdx.x * kForceWarps + warp;
+    const uint32_t group = blk.id * kForceWarps + warp;
     const uint32_t nv = counts[0];
     const uint32_t T = min(nv + counts[1], cap);  // preorder records
     if (group * 32 >= nv) return;       // no particle in this warp: nothing to write
@@ -783,6 +862,16 @@ k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, 
     const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);  // ForceShader.comp:145-146
     pos_out[i] = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
     vel_out[i] = make_float2(nvx, nvy);
+}
+
+template <bool EXACT, bool COUNT>
+__global__ void __launch_bounds__(kForceWarps * 32)
+k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, const float4* __restrict__ rec,
+        const uint32_t* __restrict__ skip, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
+        float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
+        float eps2, float theta2, float k, float hdt, uint32_t cap, unsigned long long* __restrict__ stat) {
+    force_body<EXACT, COUNT>(grid_blk(), sidx, counts, rec, skip, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al,
+                             eps2, theta2, k, hdt, cap, stat);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1018,17 +1107,15 @@ __device__ __forceinline__ void eval_items(GroupSmem& g, uint32_t n_items, const
 }
 
 template <bool EXACT, bool QUAD, bool COUNT>
-__global__ void __launch_bounds__(kGroupWarps * 32)
-k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ counts,
-              const float4* __restrict__ rec, const uint32_t* __restrict__ skip, const float4* __restrict__ quad,
-              const uint4* __restrict__ kids, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
-              float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
-              uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
-              unsigned long long* __restrict__ stat, int* __restrict__ err) {
-    __shared__ GroupSmem smem[kGroupWarps];
+__device__ __forceinline__ void force_group_body(
+    Blk blk, GroupSmem& g, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ skey,
+    const uint32_t* __restrict__ counts, const float4* __restrict__ rec, const uint32_t* __restrict__ skip,
+    const float4* __restrict__ quad, const uint4* __restrict__ kids, const float2* __restrict__ pos_in,
+    const float2* __restrict__ vel_in, float2* __restrict__ pos_out, float2* __restrict__ vel_out,
+    float2* __restrict__ acc_rec, uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
+    unsigned long long* __restrict__ stat, int* __restrict__ err) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    GroupSmem& g = smem[warp];
-    const uint32_t group = blockIdx.x * kGroupWarps + warp;
+    const uint32_t group = blk.id * kGroupWarps + warp;
     const uint32_t nv = counts[0];
     const uint32_t T = min(nv + counts[1], cap);
     if (group * 32 >= nv || T == 0) return;
@@ -1182,6 +1269,20 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
     const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);
     pos_out[i] = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
     vel_out[i] = make_float2(nvx, nvy);
+}
+
+template <bool EXACT, bool QUAD, bool COUNT>
+__global__ void __launch_bounds__(kGroupWarps * 32)
+k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ counts,
+              const float4* __restrict__ rec, const uint32_t* __restrict__ skip, const float4* __restrict__ quad,
+              const uint4* __restrict__ kids, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
+              float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
+              uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
+              unsigned long long* __restrict__ stat, int* __restrict__ err) {
+    __shared__ GroupSmem smem[kGroupWarps];
+    force_group_body<EXACT, QUAD, COUNT>(grid_blk(), smem[threadIdx.x >> 5], sidx, skey, counts, rec, skip, quad,
+                                         kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2, theta2, k, hdt,
+                                         cap, stat, err);
 }
 
 int grid_for(uint64_t n, int threads) {
@@ -1484,6 +1585,273 @@ gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* 
     *inter = st[0];
     *visits = st[1];
     return GS_OK;
+}
+
+void bh_set_final_keys(gs_sim* s) { s->bh.final_keys = s->bh.passes & 1; }
+
+// ------------------------------------------------------------------------------------
+// Batched stages: one launch per stage covers every Barnes-Hut system of a plan.  Block
+// b of a launch belongs to the system whose range of the stage's block table holds b,
+// and runs the same body as a plain launch with its index inside that system.  The
+// force stage is persistent: resident blocks take the next block index from a counter,
+// largest systems first.
+// ------------------------------------------------------------------------------------
+namespace {
+
+// system s with first[s] <= b < first[s + 1] (systems with no blocks are skipped)
+__device__ __forceinline__ uint32_t batch_sys(const uint32_t* __restrict__ first, uint32_t nsys, uint32_t b) {
+    uint32_t lo = 0, hi = nsys;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&first[mid]) <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+struct BatchArgs {
+    const SysDesc* descs;
+    const uint32_t* first;
+    uint32_t nsys;
+    uint32_t step;
+};
+
+struct BatchBlock {
+    const SysDesc* d;
+    Blk blk;
+    int in, out;
+};
+
+__device__ __forceinline__ BatchBlock batch_block(const BatchArgs& a, uint32_t b) {
+    const uint32_t s = batch_sys(a.first, a.nsys, b);
+    const uint32_t f0 = __ldg(&a.first[s]), f1 = __ldg(&a.first[s + 1]);
+    BatchBlock r;
+    r.d = a.descs + s;
+    r.blk = Blk{b - f0, f1 - f0};
+    r.in = (int)((r.d->parity + a.step) & 1u);
+    r.out = r.in ^ 1;
+    return r;
+}
+
+__global__ void __launch_bounds__(256) kb_clear(BatchArgs a, uint32_t* __restrict__ work) {
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    if (blockIdx.x == 0 && threadIdx.x < 4) work[threadIdx.x] = 0u;
+    uint32_t* z = bb.d->zero_base;
+    const uint32_t nw = bb.d->zero_words;
+    for (uint32_t i = bb.blk.id * 256 + threadIdx.x; i < nw; i += bb.blk.count * 256) z[i] = 0u;
+}
+
+__global__ void __launch_bounds__(kBBoxThreads) kb_bbox(BatchArgs a) {
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    bbox_body(bb.blk, d.pos[bb.in], d.n_al, d.bbox_part, d.counters + kCtrBBox, d.params);
+}
+
+__global__ void __launch_bounds__(kKeyThreads) kb_keygen(BatchArgs a) {
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    keygen_body(bb.blk, d.bbox, d.params, d.pos[bb.in], d.mass[bb.in], d.pos[bb.out], d.mass[bb.out], d.n_al,
+                d.keys[0], d.hist, d.passes, d.counters + kCtrValid);
+}
+
+template <bool IDENTITY>
+__global__ void __launch_bounds__(kSortThreads) kb_sort_pass(BatchArgs a, int ps) {
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    const int x = ps & 1, y = x ^ 1;
+    sort_pass_body<IDENTITY>(d.keys[x], IDENTITY ? nullptr : d.idx[x], d.keys[y], d.idx[y], d.n_al, 8 * ps,
+                             d.hist + 256 * ps, d.sort_status + (size_t)ps * d.sort_tiles * 256,
+                             d.counters + kCtrSort + ps, d.err);
+}
+
+__global__ void __launch_bounds__(kScanThreads) kb_meta_scan(BatchArgs a) {
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    meta_scan_body(d.keys[d.passes & 1], d.n_al + 1, d.counters + kCtrValid, d.depth, d.E, d.scan_status,
+                   d.counters + kCtrScan, d.counters + kCtrInternal, d.err);
+}
+
+__global__ void __launch_bounds__(256) kb_records(BatchArgs a) {
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    const int f = d.passes & 1;
+    records_body(bb.blk, d.keys[f], d.idx[f], d.E, d.counters + kCtrValid, d.depth, d.pos[bb.in], d.mass[bb.in],
+                 d.rec, d.skip, d.node_slot, d.cap, d.n_al, d.err);
+}
+
+__global__ void __launch_bounds__(256) kb_nodes(BatchArgs a) {
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    nodes_body(bb.blk, d.keys[d.passes & 1], d.E, d.counters + kCtrValid, d.depth, d.params, d.node_slot, d.rec,
+               d.skip, d.nend, d.kids, d.parent, d.pending, d.arrived, d.nodeinfo, d.cap, d.err);
+}
+
+template <bool QUAD>
+__global__ void __launch_bounds__(256) kb_bottom_up(BatchArgs a) {
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    bottom_up_body<QUAD>(bb.blk, d.keys[d.passes & 1], d.E, d.counters + kCtrValid, d.depth, d.rec, d.kids,
+                         d.parent, d.pending, d.arrived, d.nodeinfo, d.msum, d.quad, d.safe, d.bbox, d.params,
+                         d.cap);
+}
+
+template <bool EXACT, bool QUAD, bool COUNT>
+__global__ void __launch_bounds__(kGroupWarps * 32) kb_force_group(BatchArgs a, uint32_t* __restrict__ work) {
+    __shared__ GroupSmem smem[kGroupWarps];
+    __shared__ uint32_t s_b;
+    const uint32_t total = __ldg(&a.first[a.nsys]);
+    for (;;) {
+        __syncthreads();  // every thread has read the previous s_b
+        if (threadIdx.x == 0) s_b = atomicAdd(work, 1u);
+        __syncthreads();
+        const uint32_t b = s_b;
+        if (b >= total) break;
+        const BatchBlock bb = batch_block(a, b);
+        const SysDesc& d = *bb.d;
+        const int f = d.passes & 1;
+        force_group_body<EXACT, QUAD, COUNT>(bb.blk, smem[threadIdx.x >> 5], d.idx[f], d.keys[f],
+                                             d.counters + kCtrValid, d.rec, d.skip, d.quad, d.kids, d.pos[bb.in],
+                                             d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2,
+                                             d.theta2, d.k, d.hdt, d.cap,
+                                             (unsigned long long*)(d.counters + kCtrStat), d.err);
+    }
+}
+
+template <bool EXACT, bool COUNT>
+__global__ void __launch_bounds__(kForceWarps * 32) kb_force(BatchArgs a, uint32_t* __restrict__ work) {
+    __shared__ uint32_t s_b;
+    const uint32_t total = __ldg(&a.first[a.nsys]);
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_b = atomicAdd(work, 1u);
+        __syncthreads();
+        const uint32_t b = s_b;
+        if (b >= total) break;
+        const BatchBlock bb = batch_block(a, b);
+        const SysDesc& d = *bb.d;
+        const int f = d.passes & 1;
+        force_body<EXACT, COUNT>(bb.blk, d.idx[f], d.counters + kCtrValid, d.rec, d.skip, d.pos[bb.in],
+                                 d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2, d.theta2, d.k,
+                                 d.hdt, d.cap, (unsigned long long*)(d.counters + kCtrStat));
+    }
+}
+
+}  // namespace
+
+// Descriptor and per-stage block counts of one Barnes-Hut system; the counts are the
+// plain path's, except that the bounding box uses no more blocks than its particles fill.
+void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
+    const BHWork& w = s->bh;
+    d.keys[0] = w.keys[0];
+    d.keys[1] = w.keys[1];
+    d.idx[0] = w.idx[0];
+    d.idx[1] = w.idx[1];
+    d.hist = w.hist;
+    d.sort_status = w.sort_status;
+    d.counters = w.counters;
+    d.scan_status = w.scan_status;
+    d.E = w.E;
+    d.rec = w.rec;
+    d.skip = w.skip;
+    d.nend = w.nend;
+    d.msum = w.msum;
+    d.quad = w.quad;
+    d.kids = w.kids;
+    d.parent = w.parent;
+    d.pending = w.pending;
+    d.arrived = w.arrived;
+    d.nodeinfo = w.nodeinfo;
+    d.node_slot = w.node_slot;
+    d.bbox_part = w.bbox_part;
+    d.params = w.params;
+    d.zero_base = (uint32_t*)w.zero_base;
+    d.zero_words = (uint32_t)(w.zero_bytes / sizeof(uint32_t));
+    d.cap = (uint32_t)w.cap;
+    d.sort_tiles = w.sort_tiles;
+    d.scan_tiles = w.scan_tiles;
+    d.depth = w.depth;
+    d.passes = w.passes;
+    d.bbox = s->p.box_mode == GS_BOX_BOUNDING ? 1 : 0;
+    d.safe = (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0;
+    const uint64_t n = s->n_al;
+    for (int t = 0; t < kTabCount; ++t) blocks[t] = 0;
+    uint64_t cb = (d.zero_words + 1023) / 1024;
+    blocks[kTabClear] = (uint32_t)(cb < 1 ? 1 : cb > 64 ? 64 : cb);
+    if (d.bbox) {
+        uint64_t bb = (n + kBBoxThreads - 1) / kBBoxThreads;
+        blocks[kTabBBox] = (uint32_t)(bb > (uint64_t)kBBoxBlocks ? kBBoxBlocks : bb);
+    }
+    blocks[kTabGrid] = (uint32_t)grid_for(n, 256);
+    blocks[kTabSort] = w.sort_tiles;
+    blocks[kTabScan] = w.scan_tiles;
+    const int warps = (s->p.flags & GS_FLAG_GROUP_WALK) ? kGroupWarps : kForceWarps;
+    blocks[kTabForce] = (uint32_t)((n / 32 + warps - 1) / warps);
+}
+
+int bh_batch_force_grid(const BatchPlan& p) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e;
+    if (p.group) {
+        if (p.exact)
+            e = p.quad ? (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<true, true, true>, kGroupWarps * 32, 0)
+                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<true, true, false>, kGroupWarps * 32, 0))
+                       : (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<true, false, true>, kGroupWarps * 32, 0)
+                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<true, false, false>, kGroupWarps * 32, 0));
+        else
+            e = p.quad ? (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<false, true, true>, kGroupWarps * 32, 0)
+                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<false, true, false>, kGroupWarps * 32, 0))
+                       : (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<false, false, true>, kGroupWarps * 32, 0)
+                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<false, false, false>, kGroupWarps * 32, 0));
+    } else {
+        e = p.exact ? (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<true, true>, kForceWarps * 32, 0)
+                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<true, false>, kForceWarps * 32, 0))
+                    : (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<false, true>, kForceWarps * 32, 0)
+                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<false, false>, kForceWarps * 32, 0));
+    }
+    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (sms < 1) sms = 152;
+    return sms * per_sm;
+}
+
+cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st) {
+    if (!p.n_bh) return cudaSuccess;
+    auto args = [&](int tab) { return BatchArgs{p.d_descs, p.d_tab[tab], p.n_bh, step}; };
+    kb_clear<<<p.total[kTabClear], 256, 0, st>>>(args(kTabClear), p.d_work);
+    if (p.bbox) kb_bbox<<<p.total[kTabBBox], kBBoxThreads, 0, st>>>(args(kTabBBox));
+    kb_keygen<<<p.total[kTabGrid], kKeyThreads, 0, st>>>(args(kTabGrid));
+    for (int ps = 0; ps < p.passes; ++ps) {
+        if (ps == 0) kb_sort_pass<true><<<p.total[kTabSort], kSortThreads, 0, st>>>(args(kTabSort), ps);
+        else kb_sort_pass<false><<<p.total[kTabSort], kSortThreads, 0, st>>>(args(kTabSort), ps);
+    }
+    kb_meta_scan<<<p.total[kTabScan], kScanThreads, 0, st>>>(args(kTabScan));
+    kb_records<<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
+    kb_nodes<<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
+    if (p.quad) kb_bottom_up<true><<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
+    else kb_bottom_up<false><<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
+    const uint32_t fg = p.force_grid < (int)p.total[kTabForce] ? (uint32_t)p.force_grid : p.total[kTabForce];
+    uint32_t* work = p.d_work;
+#define GS_BGROUP(E_, Q_, C_) kb_force_group<E_, Q_, C_><<<fg, kGroupWarps * 32, 0, st>>>(args(kTabForce), work)
+#define GS_BFORCE(E_, C_) kb_force<E_, C_><<<fg, kForceWarps * 32, 0, st>>>(args(kTabForce), work)
+    if (p.group) {
+        if (p.exact) {
+            if (p.quad) { if (p.count) GS_BGROUP(true, true, true); else GS_BGROUP(true, true, false); }
+            else { if (p.count) GS_BGROUP(true, false, true); else GS_BGROUP(true, false, false); }
+        } else {
+            if (p.quad) { if (p.count) GS_BGROUP(false, true, true); else GS_BGROUP(false, true, false); }
+            else { if (p.count) GS_BGROUP(false, false, true); else GS_BGROUP(false, false, false); }
+        }
+    } else if (p.exact) {
+        if (p.count) GS_BFORCE(true, true);
+        else GS_BFORCE(true, false);
+    } else {
+        if (p.count) GS_BFORCE(false, true);
+        else GS_BFORCE(false, false);
+    }
+#undef GS_BGROUP
+#undef GS_BFORCE
+    return cudaGetLastError();
 }
 
 }  // namespace gsim

@@ -28,18 +28,20 @@ namespace {
 constexpr int kDirectBlock = 128;
 constexpr int kDirectTileJ = 64;
 
+// Block (bx, by) of a system: i-tile bx, j-chunk by.  A plain launch passes blockIdx.x /
+// blockIdx.y, a batched launch the block's position inside its system's grid.
 template <int IPT>
-__global__ void __launch_bounds__(kDirectBlock)
-k_direct_fast(const float2* __restrict__ pos, const float2* __restrict__ vel,
-              const float* __restrict__ mass, float2* __restrict__ pos_out,
-              float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
-              int chunks, uint32_t jchunk, float eps2, float k, float hdt,
-              float4* __restrict__ partials, uint32_t* __restrict__ tickets) {
+__device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const float2* __restrict__ pos,
+                                                 const float2* __restrict__ vel, const float* __restrict__ mass,
+                                                 float2* __restrict__ pos_out, float2* __restrict__ vel_out,
+                                                 float2* __restrict__ acc_rec, uint32_t n_al, int chunks,
+                                                 uint32_t jchunk, float eps2, float k, float hdt,
+                                                 float4* __restrict__ partials, uint32_t* __restrict__ tickets) {
     __shared__ float4 sj[kDirectTileJ];
     __shared__ uint32_t s_ticket;
     const int t = threadIdx.x;
-    const uint32_t tile_base = blockIdx.x * (kDirectBlock * IPT);
-    const uint32_t j0 = blockIdx.y * jchunk;
+    const uint32_t tile_base = bx * (kDirectBlock * IPT);
+    const uint32_t j0 = by * jchunk;
     const uint32_t j1 = min(j0 + jchunk, n_al);
 
     float px[IPT], py[IPT], sx[IPT], sy[IPT], cx[IPT], cy[IPT];
@@ -93,11 +95,11 @@ k_direct_fast(const float2* __restrict__ pos, const float2* __restrict__ vel,
 #pragma unroll
         for (int r = 0; r < IPT; ++r) {
             uint32_t i = tile_base + t + r * kDirectBlock;
-            if (i < n_al) partials[(size_t)blockIdx.y * n_al + i] = make_float4(sx[r], sy[r], cx[r], cy[r]);
+            if (i < n_al) partials[(size_t)by * n_al + i] = make_float4(sx[r], sy[r], cx[r], cy[r]);
         }
         __threadfence();
         __syncthreads();
-        if (t == 0) s_ticket = atomicAdd(&tickets[blockIdx.x], 1u);
+        if (t == 0) s_ticket = atomicAdd(&tickets[bx], 1u);
         __syncthreads();
         if (s_ticket != (uint32_t)chunks - 1) return;
         __threadfence();
@@ -123,7 +125,7 @@ k_direct_fast(const float2* __restrict__ pos, const float2* __restrict__ vel,
             sy[r] = ay;
             cy[r] = ky;
         }
-        if (t == 0) tickets[blockIdx.x] = 0u;  // ready for the next step
+        if (t == 0) tickets[bx] = 0u;  // ready for the next step
     }
 
 #pragma unroll
@@ -139,14 +141,14 @@ k_direct_fast(const float2* __restrict__ pos, const float2* __restrict__ vel,
     }
 }
 
-__global__ void __launch_bounds__(64)
-k_direct_ref(const float2* __restrict__ pos, const float2* __restrict__ vel,
-             const float* __restrict__ mass, float2* __restrict__ pos_out,
-             float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
-             float eps2, float k, float hdt) {
+__device__ __forceinline__ void direct_ref_body(uint32_t bx, const float2* __restrict__ pos,
+                                                const float2* __restrict__ vel, const float* __restrict__ mass,
+                                                float2* __restrict__ pos_out, float2* __restrict__ vel_out,
+                                                float2* __restrict__ acc_rec, uint32_t n_al, float eps2, float k,
+                                                float hdt) {
     __shared__ float2 sp[64];
     __shared__ float sm[64];
-    const uint32_t i = blockIdx.x * 64 + threadIdx.x;
+    const uint32_t i = bx * 64 + threadIdx.x;
     const float2 p = pos[i];
     float ax = 0.f, ay = 0.f;
     for (uint32_t jt = 0; jt < n_al; jt += 64) {  // SimShader.comp:43-65
@@ -169,6 +171,52 @@ k_direct_ref(const float2* __restrict__ pos, const float2* __restrict__ vel,
     float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);
     pos_out[i] = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
     vel_out[i] = make_float2(nvx, nvy);
+}
+
+template <int IPT>
+__global__ void __launch_bounds__(kDirectBlock)
+k_direct_fast(const float2* __restrict__ pos, const float2* __restrict__ vel, const float* __restrict__ mass,
+              float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
+              uint32_t n_al, int chunks, uint32_t jchunk, float eps2, float k, float hdt,
+              float4* __restrict__ partials, uint32_t* __restrict__ tickets) {
+    direct_fast_body<IPT>(blockIdx.x, blockIdx.y, pos, vel, mass, pos_out, vel_out, acc_rec, n_al, chunks, jchunk,
+                          eps2, k, hdt, partials, tickets);
+}
+
+__global__ void __launch_bounds__(64)
+k_direct_ref(const float2* __restrict__ pos, const float2* __restrict__ vel, const float* __restrict__ mass,
+             float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
+             uint32_t n_al, float eps2, float k, float hdt) {
+    direct_ref_body(blockIdx.x, pos, vel, mass, pos_out, vel_out, acc_rec, n_al, eps2, k, hdt);
+}
+
+// Batched direct sum: one launch over every direct-sum system of a plan.  Block b belongs
+// to the system whose table range holds it; inside the system it is block (b mod i-tiles,
+// b div i-tiles) of the plain grid, so each system sums in the plain order.
+__device__ __forceinline__ uint32_t direct_batch_sys(const uint32_t* __restrict__ first, uint32_t nsys,
+                                                     uint32_t b) {
+    uint32_t lo = 0, hi = nsys;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&first[mid]) <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(EXACT ? 64 : kDirectBlock)
+kb_direct(const SysDesc* __restrict__ descs, const uint32_t* __restrict__ first, uint32_t nsys, uint32_t step) {
+    const uint32_t s = direct_batch_sys(first, nsys, blockIdx.x);
+    const SysDesc& d = descs[s];
+    const uint32_t b = blockIdx.x - __ldg(&first[s]);
+    const int in = (int)((d.parity + step) & 1u), out = in ^ 1;
+    if (EXACT)
+        direct_ref_body(b, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out], d.acc, d.n_al, d.eps2, d.k,
+                        d.hdt);
+    else
+        direct_fast_body<2>(b % d.itiles, b / d.itiles, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out],
+                            d.acc, d.n_al, (int)d.chunks, d.jchunk, d.eps2, d.k, d.hdt, d.partials, d.tickets);
 }
 
 __global__ void __launch_bounds__(256)
@@ -228,6 +276,16 @@ cudaError_t direct_alloc(gs_sim* s) {
     return cudaSuccess;
 }
 
+// plain-path grid of k_direct_fast: i-tiles x j-chunks, each chunk a multiple of 64 sources
+static void direct_shape(const gs_sim* s, uint32_t& itiles, uint32_t& jchunk, uint32_t& chunks) {
+    const uint32_t n_al = (uint32_t)s->n_al;
+    const DirectWork& w = s->dw;
+    itiles = (n_al + kDirectBlock * w.ipt - 1) / (kDirectBlock * w.ipt);
+    jchunk = (n_al + w.chunks - 1) / w.chunks;
+    jchunk = (jchunk + kDirectTileJ - 1) / kDirectTileJ * kDirectTileJ;
+    chunks = (n_al + jchunk - 1) / jchunk;
+}
+
 void direct_free(gs_sim* s) {
     cudaFree(s->dw.partials);
     cudaFree(s->dw.tickets);
@@ -245,17 +303,35 @@ cudaError_t direct_step(gs_sim* s, int in, int out, bool profile) {
                                                        s->vel[out], s->acc, n_al, s->eps2, k, hdt);
     } else {
         DirectWork& w = s->dw;
-        const uint32_t itiles = (n_al + kDirectBlock * w.ipt - 1) / (kDirectBlock * w.ipt);
-        uint32_t jchunk = (n_al + w.chunks - 1) / w.chunks;
-        jchunk = (jchunk + kDirectTileJ - 1) / kDirectTileJ * kDirectTileJ;
-        const int chunks = (int)((n_al + jchunk - 1) / jchunk);
+        uint32_t itiles, jchunk, chunks;
+        direct_shape(s, itiles, jchunk, chunks);
         dim3 grid(itiles, chunks);
         k_direct_fast<2><<<grid, kDirectBlock, 0, s->stream>>>(
-            s->pos[in], s->vel[in], s->mass[in], s->pos[out], s->vel[out], s->acc, n_al, chunks, jchunk,
+            s->pos[in], s->vel[in], s->mass[in], s->pos[out], s->vel[out], s->acc, n_al, (int)chunks, jchunk,
             s->eps2, k, hdt, w.partials, w.tickets);
     }
     count_launch(s);
     stage_end(s, kStageDirect, profile);
+    return cudaGetLastError();
+}
+
+void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
+    for (int t = 0; t < kTabCount; ++t) blocks[t] = 0;
+    uint32_t itiles, jchunk, chunks;
+    direct_shape(s, itiles, jchunk, chunks);
+    d.itiles = itiles;
+    d.jchunk = jchunk;
+    d.chunks = chunks;
+    d.partials = s->dw.partials;
+    d.tickets = s->dw.tickets;
+    blocks[kTabDirect] = s->p.math_mode == GS_MATH_REFERENCE ? (uint32_t)(s->n_al / 64) : itiles * chunks;
+}
+
+cudaError_t direct_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st) {
+    if (!p.n_direct) return cudaSuccess;
+    const SysDesc* descs = p.d_descs + p.n_bh;
+    if (p.direct_exact) kb_direct<true><<<p.total[kTabDirect], 64, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct, step);
+    else kb_direct<false><<<p.total[kTabDirect], kDirectBlock, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct, step);
     return cudaGetLastError();
 }
 

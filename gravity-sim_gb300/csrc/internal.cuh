@@ -91,6 +91,66 @@ struct DirectWork {
     uint32_t* tickets = nullptr; // [i-tiles]
 };
 
+// One system of a batch as the batched stage kernels see it: its buffers (both ping-pong
+// sets; the compute-input set of batch step t is (parity + t) & 1) and its scalars.
+struct SysDesc {
+    float2* pos[2];
+    float2* vel[2];
+    float* mass[2];
+    float2* acc;
+    int* err;
+    uint32_t n_al;
+    uint32_t parity;
+    float eps2, theta2, k, hdt;
+    // Barnes-Hut scratch (BHWork)
+    uint32_t* keys[2];
+    uint32_t* idx[2];
+    uint32_t* hist;
+    uint32_t* sort_status;
+    uint32_t* counters;
+    uint32_t* scan_status;
+    uint32_t* E;
+    float4* rec;
+    uint32_t* skip;
+    uint32_t* nend;
+    float2* msum;
+    float4* quad;
+    uint4* kids;
+    uint32_t* parent;
+    uint32_t* pending;
+    uint32_t* arrived;
+    uint2* nodeinfo;
+    uint32_t* node_slot;
+    float* bbox_part;
+    BHParams* params;
+    uint32_t* zero_base;
+    uint32_t zero_words;
+    uint32_t cap;
+    uint32_t sort_tiles, scan_tiles;
+    int depth, passes, bbox, safe;
+    // direct sum (DirectWork)
+    float4* partials;
+    uint32_t* tickets;
+    uint32_t itiles, chunks, jchunk;
+};
+
+// Per-stage block tables of a batch: table t holds the exclusive prefix of the blocks each
+// system gets in stage t; a block finds its system by binary search.
+enum BatchTable { kTabClear = 0, kTabBBox, kTabGrid, kTabSort, kTabScan, kTabForce, kTabDirect, kTabCount };
+
+// What the batched launchers need: descriptors (Barnes-Hut systems first, largest first),
+// block tables, and the batch-wide work counters cleared by the first stage.
+struct BatchPlan {
+    uint32_t n_bh = 0, n_direct = 0;
+    SysDesc* d_descs = nullptr;
+    uint32_t* d_tab[kTabCount] = {};
+    uint32_t total[kTabCount] = {};
+    uint32_t* d_work = nullptr;  // [0] next force block
+    int passes = 0;
+    bool bbox = false, quad = false, group = false, exact = false, count = false, direct_exact = false;
+    int force_grid = 0;          // persistent force grid (resident blocks)
+};
+
 }  // namespace gsim
 
 struct gs_sim {
@@ -144,6 +204,14 @@ void direct_free(gs_sim* s);
 cudaError_t direct_step(gs_sim* s, int in, int out, bool profile);
 cudaError_t accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* d_targets, double2* d_out);
 uint64_t bh_capacity(int box_mode, uint64_t n_al);
+
+// batched stages (one launch per stage over every system of a plan)
+void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]);
+void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]);
+int bh_batch_force_grid(const BatchPlan& p);
+cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st);
+cudaError_t direct_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st);
+void bh_set_final_keys(gs_sim* s);
 
 // profiling helpers
 void stage_begin(gs_sim* s, int stage, bool profile);

@@ -27,8 +27,11 @@ EXPORTS = (
     "gs_sync", "gs_get_particles", "gs_set_particles", "gs_get_accel", "gs_get_stats", "gs_reset_stats",
     "gs_particle_count", "gs_aligned_particle_count", "gs_stream", "gs_destroy", "gs_accel_f64",
     "gs_debug_bh_tree", "gs_bh_node_capacity", "gs_generate", "gs_read_particles", "gs_write_particles",
-    "gs_direct_step_noalloc",
+    "gs_direct_step_noalloc", "gs_batch_create", "gs_batch_run", "gs_batch_sync", "gs_batch_kernels_per_step",
+    "gs_batch_stream", "gs_batch_destroy", "gs_tune_crossover",
 )
+BATCH_NO_GRAPH = 0x1
+TUNE_MAX_SIZES = 16
 
 
 class Params(C.Structure):
@@ -43,6 +46,11 @@ class Stats(C.Structure):
                 ("placed_particles", C.c_uint64), ("interactions", C.c_uint64), ("warp_visits", C.c_uint64),
                 ("kernel_launches", C.c_uint64),
                 ("stage_ms", C.c_float * 8), ("stage_launches", C.c_uint32 * 8)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("crossover", C.c_uint64), ("sizes", C.c_uint32), ("n", C.c_uint64 * 16),
+                ("direct_ms", C.c_double * 16), ("bh_ms", C.c_double * 16)]
 
 
 class GsimError(RuntimeError):
@@ -111,6 +119,22 @@ def lib():
     L.gs_read_particles.restype = st
     L.gs_write_particles.argtypes = [C.c_char_p, C.c_uint64, _FP, _FP, _FP]
     L.gs_write_particles.restype = st
+    batch = C.c_void_p
+    L.gs_batch_create.argtypes = [C.POINTER(sim), C.c_uint32, C.c_uint32, C.POINTER(batch)]
+    L.gs_batch_create.restype = st
+    L.gs_batch_run.argtypes = [batch, C.c_uint32]
+    L.gs_batch_run.restype = st
+    L.gs_batch_sync.argtypes = [batch, C.c_uint64]
+    L.gs_batch_sync.restype = st
+    L.gs_batch_kernels_per_step.argtypes = [batch]
+    L.gs_batch_kernels_per_step.restype = C.c_uint32
+    L.gs_batch_stream.argtypes = [batch]
+    L.gs_batch_stream.restype = C.c_void_p
+    L.gs_batch_destroy.argtypes = [batch]
+    L.gs_batch_destroy.restype = None
+    L.gs_tune_crossover.argtypes = [C.POINTER(Params), C.POINTER(Params), C.c_uint64, C.c_uint64, C.c_uint64,
+                                    C.c_uint64, C.POINTER(Tuning)]
+    L.gs_tune_crossover.restype = st
     _lib = L
     return L
 
@@ -262,3 +286,55 @@ class Simulation:
         t = T.value
         return dict(keys=keys, sorted_src=src, skip=skip[:t], radius=radius[:t], pos=npos[:t], mass=nmass[:t],
                     quad=quad[:t], tree_size=t)
+
+
+class Batch:
+    """Independent systems advanced together, one launch per stage (gs_batch).  Holds
+    references to its members so that they outlive it."""
+
+    def __init__(self, sims, flags=0):
+        self.sims = list(sims)
+        arr = (C.c_void_p * len(self.sims))(*[s.handle.value for s in self.sims])
+        self._h = C.c_void_p()
+        _check(lib().gs_batch_create(arr, len(self.sims), flags, C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().gs_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, steps=1):
+        _check(lib().gs_batch_run(self._h, steps))
+
+    def sync(self, timeout_ns=0):
+        _check(lib().gs_batch_sync(self._h, timeout_ns))
+
+    @property
+    def kernels_per_step(self):
+        return int(lib().gs_batch_kernels_per_step(self._h))
+
+    @property
+    def stream(self):
+        return lib().gs_batch_stream(self._h)
+
+
+def tune_crossover(direct_params, bh_params, min_n=1024, max_n=262144, particles_per_probe=1 << 21, seed=4000):
+    """gs_tune_crossover: measured direct-sum / Barnes-Hut crossover N and the timings."""
+    t = Tuning()
+    _check(lib().gs_tune_crossover(C.byref(direct_params), C.byref(bh_params), min_n, max_n, particles_per_probe,
+                                   seed, C.byref(t)))
+    k = t.sizes
+    return dict(crossover=int(t.crossover), n=[int(x) for x in t.n[:k]], direct_ms=list(t.direct_ms[:k]),
+                bh_ms=list(t.bh_ms[:k]))

@@ -182,6 +182,50 @@ GS_API gs_status gs_direct_step_noalloc(const float* d_pos_in, const float* d_ve
                                         float simulation_time, float softening_len,
                                         void* stream);
 
+/* ---- many systems at once (no counterpart in the reference, which runs one system) ----
+ *
+ * A batch advances a set of independent gs_sim systems together: every stage of the step
+ * is ONE kernel launch over all member systems (Barnes-Hut: clear, bounding box, keys,
+ * radix passes, scan, records, nodes, moments, force; direct sum: one launch, run beside
+ * the Barnes-Hut stages), and the step is captured once per ping-pong parity as a CUDA
+ * graph.  Each system keeps its own device buffers and parameters and computes the same
+ * bits in a batch as with gs_run.
+ *   - Members live on one device, appear once, and the Barnes-Hut members share
+ *     box_mode, math_mode and the GS_FLAG_QUADRUPOLE / SAFE_RADIUS / GROUP_WALK /
+ *     COUNT_INTERACTIONS flags; the direct-sum members share math_mode.
+ *   - gs_batch_run is asynchronous.  It orders itself after work already submitted to
+ *     each member (gs_run), and later calls on a member wait for the batch.
+ *   - The batch does not own its members: destroy it before them. */
+typedef struct gs_batch gs_batch;
+#define GS_BATCH_NO_GRAPH 0x1u  /* launch the stage kernels one by one every step */
+GS_API gs_status gs_batch_create(gs_sim* const* sims, uint32_t count, uint32_t flags,
+                                 gs_batch** out);
+GS_API gs_status gs_batch_run(gs_batch* batch, uint32_t steps);
+/* Waits for the batch, then checks every member's device-side error flags. */
+GS_API gs_status gs_batch_sync(gs_batch* batch, uint64_t timeout_ns);
+/* Kernel launches per batched step (the same for any number of members). */
+GS_API uint32_t gs_batch_kernels_per_step(const gs_batch* batch);
+GS_API void* gs_batch_stream(gs_batch* batch);
+GS_API void gs_batch_destroy(gs_batch* batch);
+
+/* Direct-sum / Barnes-Hut crossover by measurement.  For N = min_n, 2*min_n, ... up to
+ * max_n, runs a batch of max(1, particles_per_probe / N) uniform-disk systems with each
+ * algorithm (direct_params, bh_params; seeded), times warm batched steps with CUDA events
+ * and records the time per system-step.  crossover = the smallest measured N at which
+ * Barnes-Hut was faster, from a log-log interpolation between the two sizes around it
+ * (max_n when direct sum wins throughout).  Probing stops one size after Barnes-Hut wins. */
+#define GS_TUNE_MAX_SIZES 16
+typedef struct gs_tuning {
+    uint64_t crossover;
+    uint32_t sizes;
+    uint64_t n[GS_TUNE_MAX_SIZES];
+    double direct_ms[GS_TUNE_MAX_SIZES];  /* per system-step, batched */
+    double bh_ms[GS_TUNE_MAX_SIZES];
+} gs_tuning;
+GS_API gs_status gs_tune_crossover(const gs_params* direct_params, const gs_params* bh_params,
+                                   uint64_t min_n, uint64_t max_n, uint64_t particles_per_probe,
+                                   uint64_t seed, gs_tuning* out);
+
 /* ---- host-only helpers (no GPU) ---- */
 
 /* Generator types: the reference's four presets (ParticleSystem::GenerateType) and the

@@ -1,0 +1,147 @@
+"""Batched systems (gs_batch_*): one launch per stage over many systems of uneven N.
+
+Every member of a batch must end bit-identical to the same system stepped alone with
+gs_run: the batched kernels run the plain path's per-system bodies, only the mapping of
+blocks to systems changes.  Compared through the C ABI on the full state (positions,
+velocities, masses) and, for Barnes-Hut, on the last tree and interaction counts."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ACCURATE_BH = dict(algorithm=1, box_mode=1, flags=0x70 | 0x8, accuracy_parameter=0.7)
+REFRULE_BH = dict(algorithm=1, box_mode=0, flags=0x8, accuracy_parameter=1.0)
+DIRECT = dict(algorithm=0)
+
+# (generator, N, size, params): uneven sizes, both algorithms, padding (N not a multiple
+# of 64), a one-block system and a system larger than the sort tile
+MIXED = [
+    (17, 40000, 100.0, ACCURATE_BH),
+    (16, 700, 100.0, ACCURATE_BH),
+    (17, 9000, 100.0, ACCURATE_BH),
+    (16, 64, 100.0, ACCURATE_BH),
+    (16, 3000, 100.0, DIRECT),
+    (17, 1000, 100.0, DIRECT),
+    (16, 70, 100.0, DIRECT),
+    (16, 20000, 100.0, DIRECT),
+]
+
+
+def _make(gs, specs, seed0, math=0):
+    sims = []
+    for j, (kind, n, size, prm) in enumerate(specs):
+        pos, vel, mass = gs.generate(kind, n, size=size, seed=seed0 + j)
+        p = gs.default_params(math_mode=math, **prm)
+        sims.append(gs.Simulation(pos, vel, mass, params=p))
+    return sims
+
+
+def _state(sim):
+    p, v, m = sim.get_particles()
+    return np.concatenate([p.ravel(), v.ravel(), m.ravel()]).view(np.uint32)
+
+
+def _assert_same(alone, batched, specs):
+    for j, (a, b) in enumerate(zip(alone, batched)):
+        sa, sb = _state(a), _state(b)
+        bad = np.nonzero(sa != sb)[0]
+        assert bad.size == 0, f"system {j} {specs[j][:2]}: {bad.size} words differ, first {bad[:5]}"
+        if specs[j][3]["algorithm"] == 1:
+            ta, tb = a.bh_tree(), b.bh_tree()
+            assert ta["tree_size"] == tb["tree_size"]
+            for k in ("keys", "sorted_src", "skip", "radius", "pos", "mass", "quad"):
+                assert np.array_equal(ta[k].view(np.uint32), tb[k].view(np.uint32)), (j, k)
+            assert a.stats().interactions == b.stats().interactions, j
+
+
+def _run_alone(sims, steps):
+    for s in sims:
+        s.run(steps)
+    for s in sims:
+        s.sync()
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_mixed_batch_bit_identical(gs, flags):
+    alone = _make(gs, MIXED, 500)
+    batched = _make(gs, MIXED, 500)
+    for s in alone + batched:
+        s.reset_stats()
+    _run_alone(alone, 3)
+    with gs.Batch(batched, flags=flags) as b:
+        assert b.kernels_per_step == 13  # clear bbox keys 4x sort scan records nodes sums force + direct
+        b.run(3)
+        b.sync()
+        _assert_same(alone, batched, MIXED)
+
+
+def test_reference_rule_batch_bit_identical(gs):
+    """The reference's algorithm (fixed box with removal, theta 1, REFERENCE math) in a
+    batch: removal touches both particle sets, so a member must match alone exactly."""
+    specs = [(0, 5000, 700.0, REFRULE_BH), (2, 2500, 300.0, REFRULE_BH), (1, 777, 100.0, REFRULE_BH),
+             (16, 1500, 100.0, DIRECT)]
+    alone = _make(gs, specs, 900, math=1)
+    batched = _make(gs, specs, 900, math=1)
+    for s in alone + batched:
+        s.reset_stats()
+    _run_alone(alone, 2)
+    with gs.Batch(batched) as b:
+        assert b.kernels_per_step == 3 + 3 + 4 + 1  # clear keys 3x sort scan records nodes sums force + direct
+        b.run(2)
+        b.sync()
+        _assert_same(alone, batched, specs)
+
+
+def test_member_runs_alone_between_batches(gs):
+    """A member stepped with gs_run between two batch runs changes ping-pong parity; the
+    batch re-plans and every system still matches its plain twin."""
+    specs = MIXED[:2] + MIXED[4:6]
+    alone = _make(gs, specs, 700)
+    batched = _make(gs, specs, 700)
+    with gs.Batch(batched) as b:
+        b.run(2)
+        b.sync()
+        batched[1].run(1)
+        batched[2].run(1)
+        b.run(3)
+        b.sync()
+        for j, s in enumerate(alone):
+            s.run(6 if j in (1, 2) else 5)
+            s.sync()
+        _assert_same(alone, batched, specs)
+
+
+def test_batch_many_small_systems(gs):
+    """Hundreds of members (more than one table search level per block)."""
+    rng = np.random.default_rng(5)
+    specs = [(int(rng.choice([16, 17])), int(rng.integers(64, 3000)), 100.0,
+              ACCURATE_BH if rng.random() < 0.5 else DIRECT) for _ in range(300)]
+    alone = _make(gs, specs, 1300)
+    batched = _make(gs, specs, 1300)
+    _run_alone(alone, 2)
+    with gs.Batch(batched) as b:
+        b.run(2)
+        b.sync()
+    for j, (a, c) in enumerate(zip(alone, batched)):
+        assert np.array_equal(_state(a), _state(c)), j
+
+
+def test_batch_rejects_bad_members(gs):
+    a = _make(gs, [MIXED[0]], 1)[0]
+    c = _make(gs, [(16, 500, 100.0, REFRULE_BH)], 2)[0]
+    with pytest.raises(gs.GsimError):
+        gs.Batch([a, c])  # Barnes-Hut members with different box mode and flags
+    with pytest.raises(gs.GsimError):
+        gs.Batch([a, a])
+    with pytest.raises(gs.GsimError):
+        gs.Batch([])
+
+
+def test_tuner_smoke(gs):
+    d = gs.default_params(algorithm=0)
+    h = gs.default_params(accuracy_parameter=0.7, **{k: v for k, v in ACCURATE_BH.items() if k != "accuracy_parameter"})
+    h.flags = 0x70
+    t = gs.tune_crossover(d, h, min_n=1024, max_n=8192, particles_per_probe=1 << 16)
+    assert 1 <= len(t["n"]) <= 4
+    assert all(x > 0 for x in t["direct_ms"] + t["bh_ms"])
+    assert 1024 <= t["crossover"] <= 8192
