@@ -190,6 +190,185 @@ def measure(gsim, torch, wl, pos, vel, mass, args, local, dist, sample_clocks):
     return out
 
 
+BATCH_DESC = ("512 independent systems, N log-uniform in [1024, 262144] (seed 1004), each a uniform disk "
+              "(r=100) or a spiral galaxy with p=0.5; direct sum (Kahan FP32) below the tuned crossover N, "
+              "Barnes-Hut accurate mode theta=%g above it; softening 0.2, dt=1e-3")
+
+
+def batch_specs(count=512, seed=1004, lo=1024, hi=262144):
+    import gsim
+
+    rng = np.random.default_rng(seed)
+    n = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64)
+    kind = np.where(rng.random(count) < 0.5, gsim.GEN_UNIFORM_DISK, gsim.GEN_SPIRAL)
+    return [(int(k), int(x), seed * 1000 + j) for j, (k, x) in enumerate(zip(kind, n))]
+
+
+def batch_params(gsim, local, n, crossover, theta, flags=0):
+    if n < crossover:
+        return gsim.default_params(algorithm=gsim.DIRECT_SUM, device=local, flags=flags)
+    return gsim.default_params(algorithm=gsim.BARNES_HUT, box_mode=gsim.BOX_BOUNDING, accuracy_parameter=theta,
+                               device=local, flags=ACCURATE | flags)
+
+
+def measure_batched(gsim, torch, args, local):
+    """Config of many systems: the batched path (one launch per stage, a CUDA graph per
+    step) against the plain path run one system at a time (gs_run of each system in turn,
+    each with its own step graph), both timed with CUDA events on the device."""
+    t_setup = time.perf_counter()
+    d = gsim.default_params(algorithm=gsim.DIRECT_SUM, device=local)
+    theta = args.batch_theta
+    h = batch_params(gsim, local, 1 << 30, 0, theta)
+    tune = gsim.tune_crossover(d, h, min_n=1024, max_n=262144, particles_per_probe=1 << 21, seed=4000)
+    xo = tune["crossover"]
+    specs = batch_specs()
+    sims = []
+    for kind, n, seed in specs:
+        pos, vel, mass = gsim.generate(kind, n, size=100.0, seed=seed)
+        sims.append(gsim.Simulation(pos, vel, mass, params=batch_params(gsim, local, n, xo, theta)))
+    total_n = float(sum(n for _, n, _ in specs))
+    n_bh = sum(1 for _, n, _ in specs if n >= xo)
+    setup_s = time.perf_counter() - t_setup
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    steps = args.batch_steps
+
+    batch = gsim.Batch(sims)
+    stream = torch.cuda.ExternalStream(batch.stream, device=local)
+    batch.run(args.warmup)
+    batch.sync()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            flush.zero_()  # L2 flush before every timed batched step
+            starts[k].record(stream)
+            batch.run(1)
+            ends[k].record(stream)
+    batch.sync()
+    torch.cuda.synchronize()
+    wall_b = time.perf_counter() - w0
+    dev_b = float(sum(s.elapsed_time(e) for s, e in zip(starts, ends))) / 1e3
+    kps = batch.kernels_per_step
+    batch.close()
+
+    # plain path, one system at a time: warm (graph capture), then `steps` steps each
+    dev_p = 0.0
+    w0 = time.perf_counter()
+    for s in sims:
+        s.run(args.warmup)
+        s.sync()
+        st = torch.cuda.ExternalStream(s.stream(), device=local)
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st):
+            flush.zero_()  # each system starts cold, as when it runs on its own
+            a.record(st)
+            s.run(steps)
+            z.record(st)
+        s.sync()
+        dev_p += a.elapsed_time(z) / 1e3
+    wall_p = time.perf_counter() - w0  # includes the warm-up steps
+
+    # force error of a sample of members (one step from the current state vs FP64)
+    errs = []
+    rng = np.random.default_rng(1)
+    for j in sorted(rng.choice(len(sims), 8, replace=False)):
+        kind, n, seed = specs[j]
+        pos, vel, mass = sims[j].get_particles()
+        with gsim.Simulation(pos, vel, mass, params=batch_params(gsim, local, n, xo, theta,
+                                                                 gsim.FLAG_RECORD_ACCEL)) as es:
+            es.run(1)
+            acc = es.get_accel().astype(np.float64)
+            es.set_particles(pos, vel, mass)
+            sub = rng.choice(n, min(1024, n), replace=False).astype(np.uint32)
+            a64 = es.accel_f64(sub)
+        e = np.linalg.norm(acc[sub] - a64, axis=1) / np.maximum(np.linalg.norm(a64, axis=1), 1e-30)
+        errs.append({"n": n, "kind": "spiral" if kind == gsim.GEN_SPIRAL else "uniform disk",
+                     "algorithm": "barnes-hut" if n >= xo else "direct", "rms": float(np.sqrt(np.mean(e ** 2))),
+                     "max": float(e.max())})
+    for s in sims:
+        s.close()
+    value = total_n * steps / dev_b
+    plain = total_n * steps / dev_p
+    return {"workload": BATCH_DESC % theta, "theta": theta, "value": value, "unit": "particle-steps/s", "steps": steps,
+            "ms_per_step": dev_b * 1e3 / steps, "systems": len(specs), "particles": int(total_n),
+            "barnes_hut_systems": n_bh, "direct_systems": len(specs) - n_bh, "crossover_n": xo, "tuning": tune,
+            "kernels_per_step": kps, "gpu_launches": kps * steps,
+            "plain_one_at_a_time": {"value": plain, "device_s": dev_p, "wall_s_incl_warmup": wall_p},
+            "speedup_vs_plain": value / plain, "wall_value": total_n * steps / wall_b,
+            "force_error_sample": errs, "setup_s": setup_s,
+            "l2": "flushed (256 MiB write) before every timed batched step and before each plain system"}
+
+
+SERVE_DESC = ("Poisson stream (mean 200 requests/s, seed 1005) of simulation requests: N log-uniform in "
+              "[2048, 1048576], steps uniform in [10, 1000], generator uniform over uniform disk / spiral galaxy / "
+              "two-disk collision; direct sum below the tuned crossover, Barnes-Hut accurate mode above; "
+              "150 GB device-memory budget; softening 0.2, dt=1e-3")
+
+
+def serve_trace(count, seed=1005, rate=200.0, lo=2048, hi=1 << 20):
+    import gsim
+
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, count)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    n = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64)
+    steps = rng.integers(10, 1001, count)
+    gen = rng.choice([gsim.GEN_UNIFORM_DISK, gsim.GEN_SPIRAL, gsim.GEN_EXP_DISK_COLLISION], count)
+    reqs = [gsim.make_request(int(n[j]), int(steps[j]), int(gen[j]), seed=seed * 100000 + j) for j in range(count)]
+    return reqs, arrivals
+
+
+def _latency_summary(lat):
+    lat = np.asarray(lat)
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "max_s": float(lat.max())}
+
+
+def measure_served(gsim, torch, args, local, crossover, theta):
+    """The served workload through gs_server (continuous batching, admission by device
+    footprint), and the plain sequential path on the same trace: each request in arrival
+    order, generated, created, run with gs_run and read back, one at a time."""
+    reqs, arrivals = serve_trace(args.serve_requests)
+    d = gsim.default_params(algorithm=gsim.DIRECT_SUM, device=local)
+    b = gsim.default_params(algorithm=gsim.BARNES_HUT, box_mode=gsim.BOX_BOUNDING, accuracy_parameter=theta,
+                            device=local, flags=ACCURATE)
+    work = float(sum(r.particle_count * r.steps for r in reqs))
+    with gsim.Server(150 * 10 ** 9, crossover, d, b, max_resident_particles=args.serve_max_particles,
+                     steps_in_flight=2, policy=gsim.SERVE_FIFO) as srv:
+        t0 = srv.clock()
+        ids = srv.run_trace(reqs, arrivals, timeout_s=1800)
+        info = [srv.request(i) for i in ids]
+        st = srv.stats()
+    lat = [x.finish_s - x.arrival_s for x in info]
+    makespan = max(x.finish_s for x in info) - (t0 + float(arrivals[0]))
+    served = {"value": work / makespan, "makespan_s": makespan, "latency": _latency_summary(lat),
+              "queue_wait": _latency_summary([x.admit_s - x.arrival_s for x in info]),
+              "batched_steps": st["batched_steps"], "plan_changes": st["plan_changes"],
+              "peak_memory_gb": st["peak_memory_in_use"] / 1e9,
+              "peak_resident_particles": st["peak_resident_particles"], "failed": st["failed"]}
+
+    # plain sequential path: one request at a time in arrival order, real-time arrivals
+    lat_p = []
+    start = time.perf_counter()
+    for r, a in zip(reqs, arrivals):
+        now = time.perf_counter() - start
+        if now < a:
+            time.sleep(a - now)
+        pos, vel, mass = gsim.generate(r.generator, r.particle_count, size=r.generate_size, seed=r.seed)
+        with gsim.Simulation(pos, vel, mass, params=d if r.particle_count < crossover else b) as sim:
+            sim.run(r.steps)
+            sim.get_particles()
+        lat_p.append(time.perf_counter() - start - a)
+    makespan_p = time.perf_counter() - start - float(arrivals[0])
+    plain = {"value": work / makespan_p, "makespan_s": makespan_p, "latency": _latency_summary(lat_p)}
+    return {"workload": SERVE_DESC, "requests": len(reqs), "theta": theta, "crossover_n": crossover,
+            "particle_steps": work, "value": served["value"], "unit": "particle-steps/s", "served": served,
+            "plain_sequential": plain, "speedup_vs_plain": served["value"] / plain["value"],
+            "max_resident_particles": args.serve_max_particles, "policy": "fifo with conservative backfill"}
+
+
 def force_error(gsim, wl, pos, vel, mass, local):
     """RMS / median / p99 / max relative force error of one step against the FP64 direct
     sum (GPU FP64 kernel) on a 4096-particle subsample."""
@@ -311,6 +490,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true", help="skip the reference-rule theta=1 line")
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 512-system batched line")
+    ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--batch-theta", type=float, default=0.35, help="theta of the batched Barnes-Hut systems")
+    ap.add_argument("--no-served", action="store_true", help="skip the served (request stream) line")
+    ap.add_argument("--serve-requests", type=int, default=100)
+    ap.add_argument("--serve-max-particles", type=int, default=0, help="resident particle cap (0: budget only)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -367,6 +552,12 @@ def main():
         secondary = {"workload": wl2["desc"], "value": wl2["n"] * args.steps / (m2["dev_ms"] / 1e3),
                      "ms_per_step": m2["dev_ms"] / args.steps, "stage_ms_per_step": m2["stage_ms"],
                      "force_error_vs_fp64": force_error(gsim, wl2, pos, vel, mass, local)}
+    batched = served = None
+    if rank == 0 and world == 1 and not args.no_batched:
+        batched = measure_batched(gsim, torch, args, local)
+    if rank == 0 and world == 1 and not args.no_served:
+        xo = batched["crossover_n"] if batched else 2500
+        served = measure_served(gsim, torch, args, local, xo, args.batch_theta)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, pos, vel, mass)
@@ -379,7 +570,7 @@ def main():
                           "l2": "flushed (256 MiB write) before every timed step"},
                "e2e": e2e, "gpu_launches": m["launches"] * world, "roofline": roofline_of(gsim, wl, m),
                "cpu_baseline": cpu, "force_error_vs_fp64": err, "clocks": m["clocks"],
-               "reference_rule_theta1": secondary}
+               "reference_rule_theta1": secondary, "batched": batched, "served": served}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

@@ -3,10 +3,10 @@
 //
 // The reference runs one system per process (src/Main.cpp:250-321).  A batch runs every
 // stage of the step as one launch over all of its systems: the Barnes-Hut stages of
-// bh.cu (bh_batch_step) on the batch's stream, and the direct-sum kernel of direct.cu
+// bh.cu (bh_batch_step) on the root stream, and the direct-sum kernel of direct.cu
 // (direct_batch_step) beside them on a second stream.  Each block finds its system in a
 // per-stage table of block prefixes (BatchPlan); the per-system work is the plain path's,
-// so results are bit-identical to gs_run.  The step is captured once per ping-pong
+// so results are bit-identical to gs_run.  gs_batch captures the step once per ping-pong
 // parity into a CUDA graph, so a step costs one graph launch whatever the member count.
 #include <algorithm>
 #include <chrono>
@@ -15,97 +15,88 @@
 #include <new>
 #include <vector>
 
-#include "internal.cuh"
+#include "batch.cuh"
 
-using namespace gsim;
-
-struct gs_batch {
-    std::vector<gs_sim*> sims;   // caller order
-    std::vector<gs_sim*> order;  // plan order: Barnes-Hut largest first, then direct sum
-    int device = 0;
-    uint32_t flags = 0;
-    cudaStream_t root = nullptr, side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, done = nullptr;
-    std::vector<cudaEvent_t> member_ev;  // orders the batch after each member's own work
-    BatchPlan plan;
-    void* d_block = nullptr;  // descriptors | tables | work counters
-    size_t d_block_bytes = 0;
-    std::vector<int> parity0;  // each member's compute-input set when the plan was built
-    uint64_t step = 0;         // batched steps since then
-    bool planned = false;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    bool pending = false;
-};
+namespace gsim {
 
 namespace {
-
-gs_status fail(const char* msg) {
-    set_error(msg);
-    return GS_ERR_INVALID_ARGUMENT;
-}
-
-void drop_graphs(gs_batch* b) {
-    for (auto& g : b->graph)
-        if (g) {
-            cudaGraphExecDestroy(g);
-            g = nullptr;
-        }
-}
-
-void free_batch(gs_batch* b) {
-    if (!b) return;
-    cudaSetDevice(b->device);
-    if (b->root) cudaStreamSynchronize(b->root);
-    if (b->side) cudaStreamSynchronize(b->side);
-    drop_graphs(b);
-    for (auto e : b->member_ev)
-        if (e) cudaEventDestroy(e);
-    if (b->fork) cudaEventDestroy(b->fork);
-    if (b->join) cudaEventDestroy(b->join);
-    if (b->done) cudaEventDestroy(b->done);
-    if (b->root) cudaStreamDestroy(b->root);
-    if (b->side) cudaStreamDestroy(b->side);
-    cudaFree(b->d_block);
-    delete b;
-}
-
 constexpr uint32_t kBHFlagMask = GS_FLAG_QUADRUPOLE | GS_FLAG_SAFE_RADIUS | GS_FLAG_GROUP_WALK |
                                  GS_FLAG_COUNT_INTERACTIONS;
 
-gs_status check_members(gs_sim* const* sims, uint32_t count) {
+gs_status fail(const std::string& msg) {
+    set_error(msg);
+    return GS_ERR_INVALID_ARGUMENT;
+}
+}  // namespace
+
+gs_status check_batch_members(gs_sim* const* sims, size_t count, const char* who) {
+    const std::string w(who);
     const gs_sim* bh0 = nullptr;
     const gs_sim* dir0 = nullptr;
-    for (uint32_t i = 0; i < count; ++i) {
+    for (size_t i = 0; i < count; ++i) {
         const gs_sim* s = sims[i];
-        if (!s) return fail("gs_batch_create: NULL system");
-        if (s->device != sims[0]->device) return fail("gs_batch_create: all systems must live on one device");
-        for (uint32_t j = 0; j < i; ++j)
-            if (sims[j] == s) return fail("gs_batch_create: a system appears twice");
+        if (!s) return fail(w + ": NULL system");
+        if (s->device != sims[0]->device) return fail(w + ": all systems must live on one device");
         if (s->p.algorithm == GS_BARNES_HUT) {
             if (!bh0) bh0 = s;
             else if (s->p.box_mode != bh0->p.box_mode || s->p.math_mode != bh0->p.math_mode ||
                      (s->p.flags & kBHFlagMask) != (bh0->p.flags & kBHFlagMask))
-                return fail("gs_batch_create: Barnes-Hut systems must share box_mode, math_mode and the "
-                            "QUADRUPOLE / SAFE_RADIUS / GROUP_WALK / COUNT_INTERACTIONS flags");
+                return fail(w + ": Barnes-Hut systems must share box_mode, math_mode and the "
+                                "QUADRUPOLE / SAFE_RADIUS / GROUP_WALK / COUNT_INTERACTIONS flags");
         } else {
             if (!dir0) dir0 = s;
-            else if (s->p.math_mode != dir0->p.math_mode)
-                return fail("gs_batch_create: direct-sum systems must share math_mode");
+            else if (s->p.math_mode != dir0->p.math_mode) return fail(w + ": direct-sum systems must share math_mode");
         }
     }
     return GS_OK;
 }
 
-// Descriptors, block tables and launch shapes for the current member states.
-gs_status build_plan(gs_batch* b) {
-    BatchPlan& p = b->plan;
-    const size_t n = b->order.size();
+cudaError_t BatchEngine::init(int dev) {
+    device = dev;
+    cudaError_t e = cudaSetDevice(dev);
+    if (e == cudaSuccess) e = keep_pool_memory(dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&root, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&staged[k], cudaEventDisableTiming);
+    return e;
+}
+
+void BatchEngine::destroy() {
+    cudaSetDevice(device);
+    if (root) cudaStreamSynchronize(root);
+    if (side) cudaStreamSynchronize(side);
+    for (int k = 0; k < 2; ++k) {
+        if (d_block[k]) cudaFreeAsync(d_block[k], root);
+        if (h_stage[k]) cudaFreeHost(h_stage[k]);
+        if (staged[k]) cudaEventDestroy(staged[k]);
+        d_block[k] = h_stage[k] = nullptr;
+        staged[k] = nullptr;
+    }
+    if (root) cudaStreamSynchronize(root);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (root) cudaStreamDestroy(root);
+    if (side) cudaStreamDestroy(side);
+    fork = join = nullptr;
+    root = side = nullptr;
+}
+
+gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
+    order = members;
+    std::stable_sort(order.begin(), order.end(), [](const gs_sim* x, const gs_sim* y) {
+        const bool bx = x->p.algorithm == GS_BARNES_HUT, by = y->p.algorithm == GS_BARNES_HUT;
+        if (bx != by) return bx;
+        return x->n_al > y->n_al;
+    });
+    const size_t n = order.size();
+    BatchPlan p;
     std::vector<SysDesc> descs(n);
-    std::vector<std::vector<uint32_t>> blocks(n, std::vector<uint32_t>(kTabCount, 0));
-    p.n_bh = p.n_direct = 0;
-    b->parity0.assign(n, 0);
+    std::vector<uint32_t> blocks(n * kTabCount, 0u);
+    parity0.assign(n, 0);
     for (size_t i = 0; i < n; ++i) {
-        gs_sim* s = b->order[i];
+        gs_sim* s = order[i];
         SysDesc& d = descs[i];
         std::memset(&d, 0, sizeof d);
         for (int t = 0; t < 2; ++t) {
@@ -121,53 +112,70 @@ gs_status build_plan(gs_batch* b) {
         d.theta2 = s->theta2;
         d.k = s->G * s->dt_eff;  // the factor of both integrators (ForceShader.comp:145, SimShader.comp:68)
         d.hdt = 0.5f * s->dt_eff;
-        b->parity0[i] = s->in;
+        parity0[i] = s->in;
         if (s->p.algorithm == GS_BARNES_HUT) {
-            bh_batch_desc(s, d, blocks[i].data());
+            bh_batch_desc(s, d, &blocks[i * kTabCount]);
             bh_set_final_keys(s);
             ++p.n_bh;
         } else {
-            direct_batch_desc(s, d, blocks[i].data());
+            direct_batch_desc(s, d, &blocks[i * kTabCount]);
             ++p.n_direct;
         }
     }
     // tables: Barnes-Hut stages over members [0, n_bh), the direct table over [n_bh, n)
-    std::vector<uint32_t> tabs;
     size_t off[kTabCount];
+    size_t words = 0;
     for (int t = 0; t < kTabCount; ++t) {
-        const size_t lo = t == kTabDirect ? p.n_bh : 0, hi = t == kTabDirect ? n : p.n_bh;
-        off[t] = tabs.size();
-        uint64_t acc = 0;
-        tabs.push_back(0u);
-        for (size_t i = lo; i < hi; ++i) {
-            acc += blocks[i][t];
-            if (acc > 0x7fffffffull) return fail("gs_batch_create: too many blocks in one stage");
-            tabs.push_back((uint32_t)acc);
-        }
-        p.total[t] = (uint32_t)acc;
+        off[t] = words;
+        words += (t == kTabDirect ? p.n_direct : p.n_bh) + 1;
     }
     const size_t desc_b = n * sizeof(SysDesc);
     const size_t tab_off = (desc_b + 255) / 256 * 256;
-    const size_t work_off = (tab_off + tabs.size() * sizeof(uint32_t) + 255) / 256 * 256;
+    const size_t work_off = (tab_off + words * sizeof(uint32_t) + 255) / 256 * 256;
     const size_t bytes = work_off + 256;
-    if (bytes > b->d_block_bytes) {
-        cudaFree(b->d_block);
-        b->d_block = nullptr;
-        b->d_block_bytes = 0;
-        GS_CUDA(cudaMalloc(&b->d_block, bytes));
-        b->d_block_bytes = bytes;
+
+    const int k = cur ^ 1;  // the block the steps in flight are not reading
+    GS_CUDA(cudaEventSynchronize(staged[k]));  // staging k is free again (long done in practice)
+    if (h_bytes[k] < bytes) {
+        if (h_stage[k]) GS_CUDA(cudaFreeHost(h_stage[k]));
+        h_stage[k] = nullptr;
+        h_bytes[k] = 0;
+        const size_t want = std::max(bytes, 2 * h_bytes[k ^ 1]);
+        GS_CUDA(cudaHostAlloc(&h_stage[k], want, cudaHostAllocDefault));
+        h_bytes[k] = want;
     }
-    char* base = (char*)b->d_block;
-    GS_CUDA(cudaMemcpyAsync(base, descs.data(), desc_b, cudaMemcpyHostToDevice, b->root));
-    GS_CUDA(cudaMemcpyAsync(base + tab_off, tabs.data(), tabs.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                            b->root));
-    GS_CUDA(cudaMemsetAsync(base + work_off, 0, 256, b->root));
-    GS_CUDA(cudaStreamSynchronize(b->root));  // the host vectors go out of scope
-    p.d_descs = (SysDesc*)base;
-    for (int t = 0; t < kTabCount; ++t) p.d_tab[t] = (uint32_t*)(base + tab_off) + off[t];
-    p.d_work = (uint32_t*)(base + work_off);
-    const gs_sim* bh0 = p.n_bh ? b->order[0] : nullptr;
-    const gs_sim* dir0 = p.n_direct ? b->order[p.n_bh] : nullptr;
+    char* h = (char*)h_stage[k];
+    std::memcpy(h, descs.data(), desc_b);
+    uint32_t* tabs = (uint32_t*)(h + tab_off);
+    for (int t = 0; t < kTabCount; ++t) {
+        const size_t lo = t == kTabDirect ? p.n_bh : 0, hi = t == kTabDirect ? n : p.n_bh;
+        uint64_t acc = 0;
+        uint32_t* out = tabs + off[t];
+        out[0] = 0u;
+        for (size_t i = lo; i < hi; ++i) {
+            acc += blocks[i * kTabCount + t];
+            if (acc > 0x7fffffffull) return fail("batch plan: too many blocks in one stage");
+            out[i - lo + 1] = (uint32_t)acc;
+        }
+        p.total[t] = (uint32_t)acc;
+    }
+    std::memset(h + work_off, 0, 256);
+    if (d_bytes[k] < bytes) {  // stream-ordered: after every step that read the old block
+        if (d_block[k]) GS_CUDA(cudaFreeAsync(d_block[k], root));
+        d_block[k] = nullptr;
+        d_bytes[k] = 0;
+        const size_t want = std::max(bytes, d_bytes[k ^ 1]);
+        GS_CUDA(cudaMallocAsync(&d_block[k], want, root));
+        d_bytes[k] = want;
+    }
+    char* d = (char*)d_block[k];
+    GS_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, root));
+    GS_CUDA(cudaEventRecord(staged[k], root));
+    p.d_descs = (SysDesc*)d;
+    for (int t = 0; t < kTabCount; ++t) p.d_tab[t] = (uint32_t*)(d + tab_off) + off[t];
+    p.d_work = (uint32_t*)(d + work_off);
+    const gs_sim* bh0 = p.n_bh ? order[0] : nullptr;
+    const gs_sim* dir0 = p.n_direct ? order[p.n_bh] : nullptr;
     p.passes = bh0 ? bh0->bh.passes : 0;
     p.bbox = bh0 && bh0->p.box_mode == GS_BOX_BOUNDING;
     p.quad = bh0 && bh0->bh.quad != nullptr;
@@ -175,36 +183,92 @@ gs_status build_plan(gs_batch* b) {
     p.exact = bh0 && bh0->p.math_mode == GS_MATH_REFERENCE;
     p.count = bh0 && (bh0->p.flags & GS_FLAG_COUNT_INTERACTIONS);
     p.direct_exact = dir0 && dir0->p.math_mode == GS_MATH_REFERENCE;
-    p.force_grid = bh0 ? bh_batch_force_grid(p) : 0;
-    b->step = 0;
-    b->planned = true;
-    drop_graphs(b);
+    if (bh0) {
+        const int variant = (p.group ? 1 : 0) | (p.exact ? 2 : 0) | (p.quad ? 4 : 0) | (p.count ? 8 : 0);
+        if (!force_grid_cache[variant]) force_grid_cache[variant] = bh_batch_force_grid(p);
+        p.force_grid = force_grid_cache[variant];
+    }
+    plan = p;
+    cur = k;
+    step = 0;
     return GS_OK;
 }
 
-// One batched step: the Barnes-Hut stages on root, the direct-sum launch on side.
-cudaError_t enqueue(gs_batch* b, uint32_t step) {
-    const BatchPlan& p = b->plan;
+cudaError_t BatchEngine::enqueue(uint32_t par) {
+    const bool both = plan.n_bh && plan.n_direct;
     cudaError_t e = cudaSuccess;
-    const bool both = p.n_bh && p.n_direct;
     if (both) {
-        e = cudaEventRecord(b->fork, b->root);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->fork, 0);
+        e = cudaEventRecord(fork, root);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
     }
-    if (e == cudaSuccess) e = bh_batch_step(p, step, b->root);
-    if (e == cudaSuccess) e = direct_batch_step(p, step, both ? b->side : b->root);
+    if (e == cudaSuccess) e = bh_batch_step(plan, par, root);
+    if (e == cudaSuccess) e = direct_batch_step(plan, par, both ? side : root);
     if (both) {
-        if (e == cudaSuccess) e = cudaEventRecord(b->join, b->side);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->root, b->join, 0);
+        if (e == cudaSuccess) e = cudaEventRecord(join, side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(root, join, 0);
     }
     return e;
 }
 
-uint32_t launches_per_step(const BatchPlan& p) {
+void BatchEngine::advance() {
+    ++step;
+    for (gs_sim* s : order) {
+        s->in ^= 1;  // NextComputeIndices
+        ++s->steps_done;
+    }
+}
+
+bool BatchEngine::in_step() const {
+    for (size_t i = 0; i < order.size(); ++i)
+        if (order[i]->in != ((parity0[i] + (int)(step & 1)) & 1)) return false;
+    return true;
+}
+
+uint32_t BatchEngine::launches_per_step() const {
     uint32_t k = 0;
-    if (p.n_bh) k += 7u + (uint32_t)p.passes + (p.bbox ? 1u : 0u);  // clear keys scan records nodes sums force
-    if (p.n_direct) k += 1u;
+    if (plan.n_bh) k += 7u + (uint32_t)plan.passes + (plan.bbox ? 1u : 0u);  // clear keys scan records nodes sums force
+    if (plan.n_direct) k += 1u;
     return k;
+}
+
+}  // namespace gsim
+
+using namespace gsim;
+
+struct gs_batch {
+    std::vector<gs_sim*> sims;  // caller order
+    uint32_t flags = 0;
+    BatchEngine eng;
+    std::vector<cudaEvent_t> member_ev;  // orders the batch after each member's own work
+    cudaEvent_t done = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool pending = false;
+};
+
+namespace {
+
+void drop_graphs(gs_batch* b) {
+    for (auto& g : b->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+void free_batch(gs_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->eng.device);
+    for (gs_sim* s : b->sims)  // the event goes away: members follow it now
+        if (s->follow == b->done) {
+            cudaStreamWaitEvent(s->stream, b->done, 0);
+            s->follow = nullptr;
+        }
+    drop_graphs(b);
+    b->eng.destroy();
+    for (auto e : b->member_ev)
+        if (e) cudaEventDestroy(e);
+    if (b->done) cudaEventDestroy(b->done);
+    delete b;
 }
 
 }  // namespace
@@ -216,28 +280,20 @@ gs_status gs_batch_create(gs_sim* const* sims, uint32_t count, uint32_t flags, g
     *out = nullptr;
     if (!sims || !count) return fail("gs_batch_create: empty system list");
     if (flags & ~GS_BATCH_NO_GRAPH) return fail("gs_batch_create: unknown flags");
-    gs_status st = check_members(sims, count);
+    gs_status st = check_batch_members(sims, count, "gs_batch_create");
     if (st != GS_OK) return st;
+    for (uint32_t i = 0; i < count; ++i)
+        for (uint32_t j = 0; j < i; ++j)
+            if (sims[j] == sims[i]) return fail("gs_batch_create: a system appears twice");
     gs_batch* b = new (std::nothrow) gs_batch();
     if (!b) {
         set_error("gs_batch_create: host allocation failed");
         return GS_ERR_OUT_OF_MEMORY;
     }
     b->sims.assign(sims, sims + count);
-    b->order = b->sims;
-    std::stable_sort(b->order.begin(), b->order.end(), [](const gs_sim* x, const gs_sim* y) {
-        const bool bx = x->p.algorithm == GS_BARNES_HUT, by = y->p.algorithm == GS_BARNES_HUT;
-        if (bx != by) return bx;
-        return x->n_al > y->n_al;
-    });
-    b->device = sims[0]->device;
     b->flags = flags;
     b->member_ev.assign(count, nullptr);
-    cudaError_t e = cudaSetDevice(b->device);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+    cudaError_t e = b->eng.init(sims[0]->device);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
     for (uint32_t i = 0; i < count && e == cudaSuccess; ++i)
         e = cudaEventCreateWithFlags(&b->member_ev[i], cudaEventDisableTiming);
@@ -246,7 +302,7 @@ gs_status gs_batch_create(gs_sim* const* sims, uint32_t count, uint32_t flags, g
         free_batch(b);
         return st;
     }
-    st = build_plan(b);
+    st = b->eng.set_members(b->sims);
     if (st != GS_OK) {
         free_batch(b);
         return st;
@@ -257,30 +313,32 @@ gs_status gs_batch_create(gs_sim* const* sims, uint32_t count, uint32_t flags, g
 
 gs_status gs_batch_run(gs_batch* b, uint32_t steps) {
     if (!b) return fail("gs_batch_run: batch is NULL");
-    GS_CUDA(cudaSetDevice(b->device));
+    GS_CUDA(cudaSetDevice(b->eng.device));
     if (!steps) return GS_OK;
-    // members moved on alone since the plan was built: re-plan (parities changed)
-    bool stale = !b->planned;
-    for (size_t i = 0; i < b->order.size() && !stale; ++i)
-        if (b->order[i]->in != ((b->parity0[i] + (int)(b->step & 1)) & 1)) stale = true;
-    if (stale) {
-        gs_status st = build_plan(b);
+    if (!b->eng.in_step()) {  // members moved on alone since the plan was built
+        drop_graphs(b);
+        gs_status st = b->eng.set_members(b->sims);
         if (st != GS_OK) return st;
     }
-    for (size_t i = 0; i < b->sims.size(); ++i) {  // after each member's own submitted work
+    for (size_t i = 0; i < b->sims.size(); ++i) {  // after work submitted on a member's own stream
         gs_sim* s = b->sims[i];
+        if (s->follow == b->done) s->follow = nullptr;  // nothing ran alone since: already ordered
+        if (!s->own_work && !s->follow) continue;
+        if (s->follow) GS_CUDA(cudaStreamWaitEvent(s->stream, s->follow, 0));
+        s->follow = nullptr;
         GS_CUDA(cudaEventRecord(b->member_ev[i], s->stream));
-        GS_CUDA(cudaStreamWaitEvent(b->root, b->member_ev[i], 0));
+        GS_CUDA(cudaStreamWaitEvent(b->eng.root, b->member_ev[i], 0));
+        s->own_work = false;
     }
     const bool graphs = !(b->flags & GS_BATCH_NO_GRAPH);
     for (uint32_t c = 0; c < steps; ++c) {
-        const uint32_t par = (uint32_t)(b->step & 1);
+        const uint32_t par = (uint32_t)(b->eng.step & 1);
         if (graphs) {
             if (!b->graph[par]) {
                 cudaGraph_t g = nullptr;
-                GS_CUDA(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal));
-                cudaError_t e = enqueue(b, par);
-                cudaError_t e2 = cudaStreamEndCapture(b->root, &g);
+                GS_CUDA(cudaStreamBeginCapture(b->eng.root, cudaStreamCaptureModeThreadLocal));
+                cudaError_t e = b->eng.enqueue(par);
+                cudaError_t e2 = cudaStreamEndCapture(b->eng.root, &g);
                 if (e != cudaSuccess) {
                     if (g) cudaGraphDestroy(g);
                     return cuda_fail(e, "gs_batch_run capture");
@@ -290,25 +348,21 @@ gs_status gs_batch_run(gs_batch* b, uint32_t steps) {
                 cudaGraphDestroy(g);
                 GS_CUDA(e);
             }
-            GS_CUDA(cudaGraphLaunch(b->graph[par], b->root));
+            GS_CUDA(cudaGraphLaunch(b->graph[par], b->eng.root));
         } else {
-            GS_CUDA(enqueue(b, par));
+            GS_CUDA(b->eng.enqueue(par));
         }
-        ++b->step;
-        for (gs_sim* s : b->sims) {
-            s->in ^= 1;  // NextComputeIndices
-            ++s->steps_done;
-        }
+        b->eng.advance();
     }
-    GS_CUDA(cudaEventRecord(b->done, b->root));
-    for (gs_sim* s : b->sims) GS_CUDA(cudaStreamWaitEvent(s->stream, b->done, 0));
+    GS_CUDA(cudaEventRecord(b->done, b->eng.root));
+    for (gs_sim* s : b->sims) s->follow = b->done;  // a member's next own work waits for this
     b->pending = true;
     return GS_OK;
 }
 
 gs_status gs_batch_sync(gs_batch* b, uint64_t timeout_ns) {
     if (!b) return fail("gs_batch_sync: batch is NULL");
-    GS_CUDA(cudaSetDevice(b->device));
+    GS_CUDA(cudaSetDevice(b->eng.device));
     if (b->pending) {
         if (!timeout_ns) timeout_ns = 600ull * 1000000000ull;
         const auto t0 = std::chrono::steady_clock::now();
@@ -331,9 +385,9 @@ gs_status gs_batch_sync(gs_batch* b, uint64_t timeout_ns) {
     return GS_OK;
 }
 
-uint32_t gs_batch_kernels_per_step(const gs_batch* b) { return b ? launches_per_step(b->plan) : 0u; }
+uint32_t gs_batch_kernels_per_step(const gs_batch* b) { return b ? b->eng.launches_per_step() : 0u; }
 
-void* gs_batch_stream(gs_batch* b) { return b ? (void*)b->root : nullptr; }
+void* gs_batch_stream(gs_batch* b) { return b ? (void*)b->eng.root : nullptr; }
 
 void gs_batch_destroy(gs_batch* b) { free_batch(b); }
 
@@ -375,7 +429,7 @@ gs_status time_probe(const gs_params* params, uint64_t n, uint32_t count, uint64
     cudaEvent_t a = nullptr, z = nullptr;
     GS_CUDA(cudaEventCreate(&a));
     GS_CUDA(cudaEventCreate(&z));
-    const uint32_t steps = 4;
+    const uint32_t steps = 8;
     cudaEventRecord(a, root);
     st = gs_batch_run(pr.batch, steps);
     cudaEventRecord(z, root);
@@ -414,12 +468,12 @@ extern "C" gs_status gs_tune_crossover(const gs_params* direct_params, const gs_
             bh_won = true;
             if (k == 0) {
                 out->crossover = n;
-            } else {  // log(ratio) is close to linear in log(N): interpolate its zero
+            } else {  // log(direct / bh) is close to linear in log N: interpolate its zero
                 const double r0 = std::log(out->direct_ms[k - 1] / out->bh_ms[k - 1]);
                 const double r1 = std::log(td / tb);
                 const double f = r0 < 0.0 && r1 > r0 ? -r0 / (r1 - r0) : 1.0;
-                const double ln = std::log((double)out->n[k - 1]) + f * (std::log((double)n) - std::log((double)out->n[k - 1]));
-                out->crossover = (uint64_t)std::llround(std::exp(ln));
+                const double l0 = std::log((double)out->n[k - 1]);
+                out->crossover = (uint64_t)std::llround(std::exp(l0 + f * (std::log((double)n) - l0)));
             }
         } else if (bh_won) {
             break;  // one size past the crossover

@@ -1302,7 +1302,9 @@ uint64_t bh_capacity(int box_mode, uint64_t n_al) {
 // counters layout inside the zeroed block
 enum { kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrCount = 16 };
 
-cudaError_t bh_alloc(gs_sim* s) {
+// Lays the Barnes-Hut scratch out in the system's slab (sim_carve); while the system is
+// being sized (no slab yet) this only counts bytes.
+void bh_carve(gs_sim* s) {
     BHWork& w = s->bh;
     const uint64_t n = s->n_al;
     const bool bbox = s->p.box_mode == GS_BOX_BOUNDING;
@@ -1311,94 +1313,53 @@ cudaError_t bh_alloc(gs_sim* s) {
     w.cap = bh_capacity(s->p.box_mode, n);
     w.sort_tiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     w.scan_tiles = (uint32_t)((n + 1 + kScanTile - 1) / kScanTile);
-    cudaError_t e;
-#define GS_ALLOC(ptr, bytes)                                    \
-    do {                                                        \
-        e = cudaMalloc((void**)&(ptr), (bytes));                \
-        if (e != cudaSuccess) return e;                         \
-    } while (0)
     for (int b = 0; b < 2; ++b) {
-        GS_ALLOC(w.keys[b], n * sizeof(uint32_t));
-        GS_ALLOC(w.idx[b], n * sizeof(uint32_t));
+        sim_carve(s, (void**)&w.keys[b], n * sizeof(uint32_t));
+        sim_carve(s, (void**)&w.idx[b], n * sizeof(uint32_t));
     }
-    GS_ALLOC(w.E, (n + 1) * sizeof(uint32_t));
-    GS_ALLOC(w.rec, (w.cap + 32) * sizeof(float4));
-    GS_ALLOC(w.skip, (w.cap + 32) * sizeof(uint32_t));
-    GS_ALLOC(w.nend, w.cap * sizeof(uint32_t));
-    GS_ALLOC(w.msum, w.cap * sizeof(float2));
-    GS_ALLOC(w.kids, w.cap * sizeof(uint4));
-    GS_ALLOC(w.parent, w.cap * sizeof(uint32_t));
-    GS_ALLOC(w.pending, w.cap * sizeof(uint32_t));
-    GS_ALLOC(w.arrived, w.cap * sizeof(uint32_t));
-    GS_ALLOC(w.nodeinfo, w.cap * sizeof(uint2));
-    GS_ALLOC(w.node_slot, w.cap * sizeof(uint32_t));
-    if (s->p.flags & GS_FLAG_QUADRUPOLE) {
-        GS_ALLOC(w.quad, w.cap * sizeof(float4));
-        e = cudaMemset(w.quad, 0, w.cap * sizeof(float4));
-        if (e != cudaSuccess) return e;
-    }
-    GS_ALLOC(w.bbox_part, kBBoxBlocks * 4 * sizeof(float));
-    GS_ALLOC(w.params, sizeof(BHParams));
+    sim_carve(s, (void**)&w.E, (n + 1) * sizeof(uint32_t));
+    sim_carve(s, (void**)&w.rec, (w.cap + 32) * sizeof(float4));
+    sim_carve(s, (void**)&w.skip, (w.cap + 32) * sizeof(uint32_t));
+    sim_carve(s, (void**)&w.nend, w.cap * sizeof(uint32_t));
+    sim_carve(s, (void**)&w.msum, w.cap * sizeof(float2));
+    sim_carve(s, (void**)&w.kids, w.cap * sizeof(uint4));
+    sim_carve(s, (void**)&w.parent, w.cap * sizeof(uint32_t));
+    sim_carve(s, (void**)&w.pending, w.cap * sizeof(uint32_t));
+    sim_carve(s, (void**)&w.arrived, w.cap * sizeof(uint32_t));
+    sim_carve(s, (void**)&w.nodeinfo, w.cap * sizeof(uint2));
+    sim_carve(s, (void**)&w.node_slot, w.cap * sizeof(uint32_t));
+    w.quad = nullptr;
+    if (s->p.flags & GS_FLAG_QUADRUPOLE) sim_carve(s, (void**)&w.quad, w.cap * sizeof(float4));
+    sim_carve(s, (void**)&w.bbox_part, kBBoxBlocks * 4 * sizeof(float));
+    sim_carve(s, (void**)&w.params, sizeof(BHParams));
     // one block cleared per step: hist | counters | sort status | scan status
     const size_t hist_b = 4 * 256 * sizeof(uint32_t);
     const size_t ctr_b = kCtrCount * sizeof(uint32_t);
     const size_t sort_b = (size_t)w.passes * w.sort_tiles * 256 * sizeof(uint32_t);
     const size_t scan_b = (size_t)w.scan_tiles * sizeof(uint32_t);
     w.zero_bytes = hist_b + ctr_b + sort_b + scan_b;
-    GS_ALLOC(w.zero_base, w.zero_bytes);
-#undef GS_ALLOC
+    sim_carve(s, &w.zero_base, w.zero_bytes);
     char* zb = (char*)w.zero_base;
-    w.hist = (uint32_t*)zb;
-    w.counters = (uint32_t*)(zb + hist_b);
-    w.sort_status = (uint32_t*)(zb + hist_b + ctr_b);
-    w.scan_status = (uint32_t*)(zb + hist_b + ctr_b + sort_b);
-    // zero everything once so that debug reads of a never-built tree are defined
-    e = cudaMemset(w.zero_base, 0, w.zero_bytes);
-    if (e != cudaSuccess) return e;
-    e = cudaMemset(w.rec, 0, (w.cap + 32) * sizeof(float4));
-    if (e != cudaSuccess) return e;
-    e = cudaMemset(w.skip, 0, (w.cap + 32) * sizeof(uint32_t));
-    if (e != cudaSuccess) return e;
-    BHParams fixed{0.0f, 0.0f, (float)kGrid / (2.0f * kSimSize), kSimSize * kSimSize * 2.0f,
-                   2.0f * kSimSize / (float)kGrid};
-    e = cudaMemcpy(w.params, &fixed, sizeof fixed, cudaMemcpyHostToDevice);
-    return e;
+    w.hist = zb ? (uint32_t*)zb : nullptr;
+    w.counters = zb ? (uint32_t*)(zb + hist_b) : nullptr;
+    w.sort_status = zb ? (uint32_t*)(zb + hist_b + ctr_b) : nullptr;
+    w.scan_status = zb ? (uint32_t*)(zb + hist_b + ctr_b + sort_b) : nullptr;
 }
 
-void bh_free(gs_sim* s) {
+// Initial contents: everything a debug read of a never-built tree could see is zero, the
+// fixed-box parameters are in place.
+cudaError_t bh_init(gs_sim* s) {
     BHWork& w = s->bh;
-    for (int b = 0; b < 2; ++b) {
-        cudaFree(w.keys[b]);
-        cudaFree(w.idx[b]);
-        w.keys[b] = w.idx[b] = nullptr;
-    }
-    cudaFree(w.E);
-    cudaFree(w.rec);
-    cudaFree(w.skip);
-    cudaFree(w.nend);
-    cudaFree(w.msum);
-    cudaFree(w.quad);
-    cudaFree(w.kids);
-    cudaFree(w.parent);
-    cudaFree(w.pending);
-    cudaFree(w.arrived);
-    cudaFree(w.nodeinfo);
-    cudaFree(w.node_slot);
-    w.node_slot = nullptr;
-    w.kids = nullptr;
-    w.parent = w.pending = w.arrived = nullptr;
-    w.nodeinfo = nullptr;
-    w.quad = nullptr;
-    cudaFree(w.bbox_part);
-    cudaFree(w.params);
-    cudaFree(w.zero_base);
-    w.E = nullptr;
-    w.rec = nullptr;
-    w.skip = w.nend = nullptr;
-    w.msum = nullptr;
-    w.bbox_part = nullptr;
-    w.params = nullptr;
-    w.zero_base = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (w.quad) e = cudaMemsetAsync(w.quad, 0, w.cap * sizeof(float4), s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.zero_base, 0, w.zero_bytes, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.rec, 0, (w.cap + 32) * sizeof(float4), s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.skip, 0, (w.cap + 32) * sizeof(uint32_t), s->stream);
+    BHParams fixed{0.0f, 0.0f, (float)kGrid / (2.0f * kSimSize), kSimSize * kSimSize * 2.0f,
+                   2.0f * kSimSize / (float)kGrid};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w.params, &fixed, sizeof fixed, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);  // `fixed` lives on this stack frame
+    return e;
 }
 
 cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {

@@ -259,21 +259,26 @@ static int pick_chunks(uint64_t n_al, int ipt) {
     return (int)c;
 }
 
-cudaError_t direct_alloc(gs_sim* s) {
+// Lays the j-chunk partials and tickets out in the system's slab (sizing pass: counts).
+void direct_carve(gs_sim* s) {
     DirectWork& w = s->dw;
     w.ipt = 2;
     w.block = kDirectBlock;
     w.chunks = pick_chunks(s->n_al, w.ipt);
+    w.partials = nullptr;
+    w.tickets = nullptr;
     if (w.chunks > 1) {
         const uint64_t itiles = (s->n_al + kDirectBlock * w.ipt - 1) / (kDirectBlock * w.ipt);
-        cudaError_t e = cudaMalloc(&w.partials, sizeof(float4) * s->n_al * (size_t)w.chunks);
-        if (e != cudaSuccess) return e;
-        e = cudaMalloc(&w.tickets, sizeof(uint32_t) * itiles);
-        if (e != cudaSuccess) return e;
-        e = cudaMemset(w.tickets, 0, sizeof(uint32_t) * itiles);
-        if (e != cudaSuccess) return e;
+        sim_carve(s, (void**)&w.partials, sizeof(float4) * s->n_al * (size_t)w.chunks);
+        sim_carve(s, (void**)&w.tickets, sizeof(uint32_t) * itiles);
     }
-    return cudaSuccess;
+}
+
+cudaError_t direct_init(gs_sim* s) {
+    const DirectWork& w = s->dw;
+    if (!w.tickets) return cudaSuccess;
+    const uint64_t itiles = (s->n_al + kDirectBlock * w.ipt - 1) / (kDirectBlock * w.ipt);
+    return cudaMemsetAsync(w.tickets, 0, sizeof(uint32_t) * itiles, s->stream);
 }
 
 // plain-path grid of k_direct_fast: i-tiles x j-chunks, each chunk a multiple of 64 sources
@@ -284,13 +289,6 @@ static void direct_shape(const gs_sim* s, uint32_t& itiles, uint32_t& jchunk, ui
     jchunk = (n_al + w.chunks - 1) / w.chunks;
     jchunk = (jchunk + kDirectTileJ - 1) / kDirectTileJ * kDirectTileJ;
     chunks = (n_al + jchunk - 1) / jchunk;
-}
-
-void direct_free(gs_sim* s) {
-    cudaFree(s->dw.partials);
-    cudaFree(s->dw.tickets);
-    s->dw.partials = nullptr;
-    s->dw.tickets = nullptr;
 }
 
 cudaError_t direct_step(gs_sim* s, int in, int out, bool profile) {

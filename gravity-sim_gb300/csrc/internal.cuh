@@ -181,6 +181,10 @@ struct gs_sim {
     uint32_t launches_in_step = 0;   // kernels enqueued by the step being built
     uint32_t launches_per_step[2] = {0, 0};  // per ping-pong parity (graph replay count)
     uint64_t kernel_launches = 0;    // kernels launched since creation
+    void* slab = nullptr;            // every device buffer of the system
+    size_t carved = 0;               // bytes laid out so far (sim_carve)
+    cudaEvent_t follow = nullptr;    // a batch step this system's next work must follow
+    bool own_work = false;           // work submitted on its own stream since the last batch run
 };
 
 namespace gsim {
@@ -195,12 +199,18 @@ gs_status cuda_fail(cudaError_t e, const char* what);
         if (_e != cudaSuccess) return gsim::cuda_fail(_e, #call); \
     } while (0)
 
-// launchers (return cudaError_t of the launch)
-cudaError_t bh_alloc(gs_sim* s);
-void bh_free(gs_sim* s);
+// Device memory of a system: one slab from the device's default pool (stream-ordered on
+// the system's stream, kept cached), carved into 256-byte aligned buffers.  Carving with
+// no slab yet only counts bytes, which sizes the slab and gives gs_footprint.
+void sim_carve(gs_sim* s, void** p, size_t bytes);
+cudaError_t keep_pool_memory(int device);
+
+// layout, initial contents and step launchers (return cudaError_t of the launch)
+void bh_carve(gs_sim* s);
+cudaError_t bh_init(gs_sim* s);
 cudaError_t bh_step(gs_sim* s, int in, int out, bool profile);
-cudaError_t direct_alloc(gs_sim* s);
-void direct_free(gs_sim* s);
+void direct_carve(gs_sim* s);
+cudaError_t direct_init(gs_sim* s);
 cudaError_t direct_step(gs_sim* s, int in, int out, bool profile);
 cudaError_t accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* d_targets, double2* d_out);
 uint64_t bh_capacity(int box_mode, uint64_t n_al);

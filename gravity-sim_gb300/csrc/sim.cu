@@ -9,6 +9,7 @@
 // once into a CUDA graph and replayed.
 #include <chrono>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <thread>
 
@@ -39,6 +40,55 @@ void stage_end(gs_sim* s, int stage, bool profile) {
         record(s, s->ev[2 * stage + 1]);
         s->stage_ran |= 1u << stage;
     }
+}
+
+// A system's device memory is one slab from the device's default pool, allocated and
+// freed in order on the system's stream: creating or destroying a system never waits for
+// work elsewhere on the device (cudaFree would), and freed slabs stay in the pool for the
+// next system.  One allocation per system keeps the pool's bookkeeping small however
+// many systems are alive.
+void sim_carve(gs_sim* s, void** p, size_t bytes) {
+    const size_t off = (s->carved + 255) & ~(size_t)255;
+    s->carved = off + bytes;
+    *p = s->slab ? (void*)((char*)s->slab + off) : nullptr;
+}
+
+// every buffer of the system, in one fixed order
+void carve_all(gs_sim* s) {
+    s->carved = 0;
+    for (int b = 0; b < 2; ++b) {
+        sim_carve(s, (void**)&s->pos[b], s->n_al * sizeof(float2));
+        sim_carve(s, (void**)&s->vel[b], s->n_al * sizeof(float2));
+    }
+    sim_carve(s, (void**)&s->mass[0], s->n_al * sizeof(float));
+    s->mass[1] = s->mass[0];  // no step writes mass except removal, which writes both sets alike
+    sim_carve(s, (void**)&s->d_err, sizeof(int));
+    s->acc = nullptr;
+    if (s->p.flags & GS_FLAG_RECORD_ACCEL) sim_carve(s, (void**)&s->acc, s->n_al * sizeof(float2));
+    if (s->p.algorithm == GS_BARNES_HUT) bh_carve(s);
+    else direct_carve(s);
+}
+
+// A batch left this system an event to follow (gs_batch_run): its next work on its own
+// stream waits for that batch step.
+void follow_batch(gs_sim* s) {
+    if (s->follow) {
+        cudaStreamWaitEvent(s->stream, s->follow, 0);
+        s->follow = nullptr;
+    }
+}
+
+cudaError_t keep_pool_memory(int device) {
+    static std::mutex mu;
+    static bool done[64] = {};
+    std::lock_guard<std::mutex> lock(mu);
+    if (device < 0 || device >= 64 || done[device]) return cudaSuccess;
+    cudaMemPool_t pool;
+    cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, device);
+    uint64_t keep = ~0ull;  // never trim freed blocks back to the driver
+    if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e == cudaSuccess) done[device] = true;
+    return e;
 }
 
 gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
@@ -94,15 +144,8 @@ void free_sim(gs_sim* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (int p = 0; p < 2; ++p)
         if (s->graph[p]) cudaGraphExecDestroy(s->graph[p]);
-    bh_free(s);
-    direct_free(s);
-    for (int b = 0; b < 2; ++b) {
-        cudaFree(s->pos[b]);
-        cudaFree(s->vel[b]);
-    }
-    cudaFree(s->mass[0]);
-    cudaFree(s->acc);
-    cudaFree(s->d_err);
+    if (s->slab) cudaFreeAsync(s->slab, s->stream);
+    s->slab = nullptr;
     for (auto& e : s->ev)
         if (e) cudaEventDestroy(e);
     if (s->batch_done) cudaEventDestroy(s->batch_done);
@@ -193,6 +236,16 @@ uint64_t gs_required_alignment(int32_t algorithm) {
 
 uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count) { return bh_capacity(box_mode, aligned_count); }
 
+uint64_t gs_footprint(const gs_params* p, uint64_t n) {
+    if (!p || !n) return 0;
+    gs_sim t;  // a sizing pass of gs_create's layout: host only, no slab
+    t.p = *p;
+    t.n = n;
+    t.n_al = (n + kAlignment - 1) / kAlignment * kAlignment;
+    carve_all(&t);
+    return t.carved;
+}
+
 gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const float* vel, const float* mass,
                     gs_sim** out) {
     if (!out) return invalid("gs_create: out is NULL");
@@ -247,23 +300,17 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
         }                                              \
     } while (0)
     GS_TRY(cudaSetDevice(s->device));
+    GS_TRY(keep_pool_memory(s->device));
     GS_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     GS_TRY(cudaEventCreateWithFlags(&s->batch_done, cudaEventDisableTiming));
     for (auto& e : s->ev) GS_TRY(cudaEventCreate(&e));
-    for (int b = 0; b < 2; ++b) {
-        GS_TRY(cudaMalloc(&s->pos[b], s->n_al * sizeof(float2)));
-        GS_TRY(cudaMalloc(&s->vel[b], s->n_al * sizeof(float2)));
-    }
-    GS_TRY(cudaMalloc(&s->mass[0], s->n_al * sizeof(float)));
-    s->mass[1] = s->mass[0];  // no step writes mass except removal, which writes both sets alike
-    GS_TRY(cudaMalloc(&s->d_err, sizeof(int)));
-    GS_TRY(cudaMemset(s->d_err, 0, sizeof(int)));
-    if (params->flags & GS_FLAG_RECORD_ACCEL) {
-        GS_TRY(cudaMalloc(&s->acc, s->n_al * sizeof(float2)));
-        GS_TRY(cudaMemset(s->acc, 0, s->n_al * sizeof(float2)));
-    }
-    if (params->algorithm == GS_BARNES_HUT) GS_TRY(bh_alloc(s));
-    else GS_TRY(direct_alloc(s));
+    carve_all(s);  // sizing pass
+    GS_TRY(cudaMallocAsync(&s->slab, s->carved, s->stream));
+    carve_all(s);  // the same layout inside the slab
+    GS_TRY(cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream));
+    if (s->acc) GS_TRY(cudaMemsetAsync(s->acc, 0, s->n_al * sizeof(float2), s->stream));
+    if (params->algorithm == GS_BARNES_HUT) GS_TRY(bh_init(s));
+    else GS_TRY(direct_init(s));
 #undef GS_TRY
     st = upload(s, pos, vel, mass);
     if (st != GS_OK) {
@@ -277,6 +324,8 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
 gs_status gs_run(gs_sim* s, uint32_t count) {
     if (!s) return invalid("gs_run: sim is NULL");
     GS_CUDA(cudaSetDevice(s->device));
+    follow_batch(s);
+    s->own_work = true;
     if (s->batch_pending) {  // wait for the previous submit, like the reference's fence wait
         gs_status w = wait_event(s->batch_done, 0);
         if (w != GS_OK) return w;
@@ -332,6 +381,7 @@ gs_status gs_run(gs_sim* s, uint32_t count) {
 gs_status gs_sync(gs_sim* s, uint64_t timeout_ns) {
     if (!s) return invalid("gs_sync: sim is NULL");
     GS_CUDA(cudaSetDevice(s->device));
+    follow_batch(s);
     if (s->batch_pending) {
         gs_status w = wait_event(s->batch_done, timeout_ns);
         if (w != GS_OK) return w;
@@ -359,6 +409,7 @@ gs_status gs_set_particles(gs_sim* s, const float* pos, const float* vel, const 
     if (!pos || !mass) return invalid("gs_set_particles: pos_xy and mass are required");
     gs_status st = gs_sync(s, 0);
     if (st != GS_OK) return st;
+    s->own_work = true;
     return upload(s, pos, vel, mass);
 }
 
@@ -410,16 +461,19 @@ gs_status gs_accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* targets, d
         if (targets[t] >= s->n) return invalid("gs_accel_f64: target index out of range");
     gs_status st = gs_sync(s, 0);
     if (st != GS_OK) return st;
+    s->own_work = true;
     uint32_t* dt = nullptr;
     double2* dout = nullptr;
-    GS_CUDA(cudaMalloc(&dt, n_targets * sizeof(uint32_t)));
-    cudaError_t e = cudaMalloc(&dout, n_targets * sizeof(double2));
-    if (e == cudaSuccess) e = cudaMemcpy(dt, targets, n_targets * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    GS_CUDA(cudaMallocAsync(&dt, n_targets * sizeof(uint32_t), s->stream));
+    cudaError_t e = cudaMallocAsync(&dout, n_targets * sizeof(double2), s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dt, targets, n_targets * sizeof(uint32_t), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = accel_f64(s, n_targets, dt, dout);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(acc, dout, n_targets * sizeof(double2), cudaMemcpyDeviceToHost, s->stream);
+    if (dt) cudaFreeAsync(dt, s->stream);
+    if (dout) cudaFreeAsync(dout, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e == cudaSuccess) e = cudaMemcpy(acc, dout, n_targets * sizeof(double2), cudaMemcpyDeviceToHost);
-    cudaFree(dt);
-    cudaFree(dout);
     GS_CUDA(e);
     return GS_OK;
 }

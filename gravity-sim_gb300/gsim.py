@@ -28,8 +28,12 @@ EXPORTS = (
     "gs_particle_count", "gs_aligned_particle_count", "gs_stream", "gs_destroy", "gs_accel_f64",
     "gs_debug_bh_tree", "gs_bh_node_capacity", "gs_generate", "gs_read_particles", "gs_write_particles",
     "gs_direct_step_noalloc", "gs_batch_create", "gs_batch_run", "gs_batch_sync", "gs_batch_kernels_per_step",
-    "gs_batch_stream", "gs_batch_destroy", "gs_tune_crossover",
+    "gs_batch_stream", "gs_batch_destroy", "gs_tune_crossover", "gs_footprint", "gs_server_create",
+    "gs_server_submit", "gs_server_poll", "gs_server_request", "gs_server_result", "gs_server_get_stats",
+    "gs_server_clock", "gs_server_run_trace", "gs_server_destroy",
 )
+SERVE_FIFO, SERVE_SHORTEST_FIRST = 0, 1
+REQUEST_QUEUED, REQUEST_RESIDENT, REQUEST_DONE, REQUEST_FAILED = 0, 1, 2, 3
 BATCH_NO_GRAPH = 0x1
 TUNE_MAX_SIZES = 16
 
@@ -51,6 +55,30 @@ class Stats(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("crossover", C.c_uint64), ("sizes", C.c_uint32), ("n", C.c_uint64 * 16),
                 ("direct_ms", C.c_double * 16), ("bh_ms", C.c_double * 16)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("memory_budget", C.c_uint64), ("max_resident_particles", C.c_uint64), ("crossover", C.c_uint64),
+                ("direct_params", Params), ("bh_params", Params), ("steps_in_flight", C.c_uint32),
+                ("policy", C.c_uint32), ("keep_results", C.c_uint32), ("worker_threads", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("particle_count", C.c_uint64), ("steps", C.c_uint32), ("generator", C.c_int32), ("seed", C.c_uint64),
+                ("generate_size", C.c_float), ("min_mass", C.c_float), ("max_mass", C.c_float),
+                ("pos_xy", C.POINTER(C.c_float)), ("vel_xy", C.POINTER(C.c_float)), ("mass", C.POINTER(C.c_float))]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int32), ("algorithm", C.c_int32), ("steps_enqueued", C.c_uint32), ("steps", C.c_uint32),
+                ("particle_count", C.c_uint64), ("footprint", C.c_uint64), ("arrival_s", C.c_double),
+                ("admit_s", C.c_double), ("finish_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "finished", "failed", "queued", "resident", "memory_in_use",
+                                          "peak_memory_in_use", "resident_particles", "peak_resident_particles",
+                                          "batched_steps", "plan_changes", "particle_steps")]
 
 
 class GsimError(RuntimeError):
@@ -135,6 +163,28 @@ def lib():
     L.gs_tune_crossover.argtypes = [C.POINTER(Params), C.POINTER(Params), C.c_uint64, C.c_uint64, C.c_uint64,
                                     C.c_uint64, C.POINTER(Tuning)]
     L.gs_tune_crossover.restype = st
+    srv = C.c_void_p
+    L.gs_footprint.argtypes = [C.POINTER(Params), C.c_uint64]
+    L.gs_footprint.restype = C.c_uint64
+    L.gs_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(srv)]
+    L.gs_server_create.restype = st
+    L.gs_server_submit.argtypes = [srv, C.POINTER(Request), C.c_double, C.POINTER(C.c_uint64)]
+    L.gs_server_submit.restype = st
+    L.gs_server_poll.argtypes = [srv, C.POINTER(C.c_uint32)]
+    L.gs_server_poll.restype = st
+    L.gs_server_request.argtypes = [srv, C.c_uint64, C.POINTER(RequestStatus)]
+    L.gs_server_request.restype = st
+    L.gs_server_result.argtypes = [srv, C.c_uint64, _FP, _FP, _FP]
+    L.gs_server_result.restype = st
+    L.gs_server_get_stats.argtypes = [srv, C.POINTER(ServerStats)]
+    L.gs_server_get_stats.restype = st
+    L.gs_server_clock.argtypes = [srv]
+    L.gs_server_clock.restype = C.c_double
+    L.gs_server_run_trace.argtypes = [srv, C.POINTER(Request), C.POINTER(C.c_double), C.c_uint32, C.c_double,
+                                      C.POINTER(C.c_uint64)]
+    L.gs_server_run_trace.restype = st
+    L.gs_server_destroy.argtypes = [srv]
+    L.gs_server_destroy.restype = None
     _lib = L
     return L
 
@@ -338,3 +388,89 @@ def tune_crossover(direct_params, bh_params, min_n=1024, max_n=262144, particles
     k = t.sizes
     return dict(crossover=int(t.crossover), n=[int(x) for x in t.n[:k]], direct_ms=list(t.direct_ms[:k]),
                 bh_ms=list(t.bh_ms[:k]))
+
+
+def footprint(params, n):
+    """gs_footprint: device bytes gs_create allocates for N particles with these parameters."""
+    return int(lib().gs_footprint(C.byref(params), n))
+
+
+def make_request(n, steps, generator=GEN_UNIFORM_DISK, seed=1, size=100.0, min_mass=1.0, max_mass=10.0):
+    r = Request()
+    r.particle_count, r.steps, r.generator, r.seed = n, steps, generator, seed
+    r.generate_size, r.min_mass, r.max_mass = size, min_mass, max_mass
+    return r
+
+
+class Server:
+    """Continuous batching of simulation requests (gs_server)."""
+
+    def __init__(self, memory_budget, crossover, direct_params, bh_params, max_resident_particles=0,
+                 steps_in_flight=0, policy=SERVE_FIFO, keep_results=False, worker_threads=0):
+        c = ServerConfig()
+        c.memory_budget, c.max_resident_particles, c.crossover = memory_budget, max_resident_particles, crossover
+        c.direct_params, c.bh_params = direct_params, bh_params
+        c.steps_in_flight, c.policy, c.keep_results, c.worker_threads = steps_in_flight, policy, int(keep_results), \
+            worker_threads
+        self.config = c
+        self._h = C.c_void_p()
+        _check(lib().gs_server_create(C.byref(c), C.byref(self._h)))
+        self._n = {}
+
+    def close(self):
+        if self._h:
+            lib().gs_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, request, arrival_s=-1.0):
+        rid = C.c_uint64()
+        _check(lib().gs_server_submit(self._h, C.byref(request), arrival_s, C.byref(rid)))
+        self._n[rid.value] = request.particle_count
+        return rid.value
+
+    def poll(self):
+        f = C.c_uint32()
+        _check(lib().gs_server_poll(self._h, C.byref(f)))
+        return f.value
+
+    def request(self, rid):
+        st = RequestStatus()
+        _check(lib().gs_server_request(self._h, rid, C.byref(st)))
+        return st
+
+    def result(self, rid):
+        n = self._n[rid]
+        pos, vel, mass = np.empty((n, 2), np.float32), np.empty((n, 2), np.float32), np.empty(n, np.float32)
+        _check(lib().gs_server_result(self._h, rid, _fp(pos), _fp(vel), _fp(mass)))
+        return pos, vel, mass
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().gs_server_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def clock(self):
+        return float(lib().gs_server_clock(self._h))
+
+    def run_trace(self, requests, arrival_s, timeout_s=0.0):
+        n = len(requests)
+        arr = (Request * n)(*requests)
+        t = (C.c_double * n)(*[float(x) for x in arrival_s])
+        ids = (C.c_uint64 * n)()
+        _check(lib().gs_server_run_trace(self._h, arr, t, n, timeout_s, ids))
+        out = list(ids)
+        for r, i in zip(requests, out):
+            self._n[i] = r.particle_count
+        return out

@@ -226,6 +226,93 @@ GS_API gs_status gs_tune_crossover(const gs_params* direct_params, const gs_para
                                    uint64_t min_n, uint64_t max_n, uint64_t particles_per_probe,
                                    uint64_t seed, gs_tuning* out);
 
+/* Device bytes gs_create allocates for a system with these parameters (the admission
+ * measure of gs_server).  The default memory pool may round each allocation up. */
+GS_API uint64_t gs_footprint(const gs_params* params, uint64_t particle_count);
+
+/* ---- serving: continuous batching of simulation requests (no counterpart in the
+ * reference) ----
+ *
+ * A server keeps every admitted system resident on the device and advances all of them
+ * together, one batched step (gs_batch machinery) per gs_server_poll.  Requests that
+ * arrive while others run are admitted between two steps as soon as their footprint
+ * (gs_footprint) fits the memory budget, and leave the batch as soon as their last step
+ * is enqueued; their final state is read back once that step has finished.  Systems with
+ * N below `crossover` use direct_params (direct sum), the others bh_params (Barnes-Hut).
+ * Generator inputs are made on worker threads.  One host thread drives a server. */
+typedef struct gs_server gs_server;
+#define GS_SERVE_FIFO 0           /* admit in arrival order (later requests may pass a
+                                     blocked one when they fit) */
+#define GS_SERVE_SHORTEST_FIRST 1 /* admit the queued request with the least N x steps first */
+typedef struct gs_server_config {
+    uint64_t memory_budget;       /* bytes the resident systems may hold (sum of footprints) */
+    uint64_t max_resident_particles; /* sum of N of resident systems (0: no limit) */
+    uint64_t crossover;           /* direct sum below this N, Barnes-Hut at or above */
+    gs_params direct_params;
+    gs_params bh_params;
+    uint32_t steps_in_flight;     /* batched steps the host may run ahead of the GPU (0: 2) */
+    uint32_t policy;              /* GS_SERVE_FIFO or GS_SERVE_SHORTEST_FIRST */
+    uint32_t keep_results;        /* nonzero: keep final particles for gs_server_result */
+    uint32_t worker_threads;      /* input generators (0: 4) */
+} gs_server_config;
+
+typedef struct gs_request {
+    uint64_t particle_count;
+    uint32_t steps;
+    int32_t generator;            /* gs_generate type, used when pos_xy is NULL */
+    uint64_t seed;
+    float generate_size, min_mass, max_mass;
+    const float* pos_xy;          /* or the caller's particles, copied at submit (vel_xy may be NULL) */
+    const float* vel_xy;
+    const float* mass;
+} gs_request;
+
+#define GS_REQUEST_QUEUED 0
+#define GS_REQUEST_RESIDENT 1
+#define GS_REQUEST_DONE 2
+#define GS_REQUEST_FAILED 3
+typedef struct gs_request_status {
+    int32_t state;
+    int32_t algorithm;
+    uint32_t steps_enqueued;
+    uint32_t steps;
+    uint64_t particle_count;
+    uint64_t footprint;
+    double arrival_s, admit_s, finish_s;  /* server clock, seconds since gs_server_create */
+} gs_request_status;
+
+typedef struct gs_server_stats {
+    uint64_t submitted, finished, failed, queued, resident;
+    uint64_t memory_in_use, peak_memory_in_use;
+    uint64_t resident_particles, peak_resident_particles;
+    uint64_t batched_steps;       /* gs_server_poll steps enqueued */
+    uint64_t plan_changes;        /* member-set changes */
+    uint64_t particle_steps;      /* sum of N x steps of finished requests */
+} gs_server_stats;
+
+GS_API gs_status gs_server_create(const gs_server_config* config, gs_server** out);
+/* Queues a request; its latency is counted from `arrival_s` on the server clock (pass a
+ * negative value for "now"). */
+GS_API gs_status gs_server_submit(gs_server* server, const gs_request* request, double arrival_s,
+                                  uint64_t* id);
+/* One scheduling turn: retire finished requests, admit queued ones that fit, enqueue one
+ * batched step.  *finished (may be NULL) gets the number of requests retired. */
+GS_API gs_status gs_server_poll(gs_server* server, uint32_t* finished);
+GS_API gs_status gs_server_request(gs_server* server, uint64_t id, gs_request_status* out);
+/* Final particles of a finished request (keep_results); the first N particles. */
+GS_API gs_status gs_server_result(gs_server* server, uint64_t id, float* pos_xy, float* vel_xy,
+                                  float* mass);
+GS_API gs_status gs_server_get_stats(gs_server* server, gs_server_stats* out);
+GS_API double gs_server_clock(gs_server* server);
+/* Replays a trace in real time: request i is submitted when the server clock reaches
+ * start + arrival_s[i] (start = the clock at the call), and the server is polled until
+ * every request of the trace has finished or failed, or timeout_s passed
+ * (GS_ERR_TIMEOUT).  ids (may be NULL) receives the request ids. */
+GS_API gs_status gs_server_run_trace(gs_server* server, const gs_request* requests,
+                                     const double* arrival_s, uint32_t count, double timeout_s,
+                                     uint64_t* ids);
+GS_API void gs_server_destroy(gs_server* server);
+
 /* ---- host-only helpers (no GPU) ---- */
 
 /* Generator types: the reference's four presets (ParticleSystem::GenerateType) and the
