@@ -186,6 +186,7 @@ def measure(gsim, torch, wl, pos, vel, mass, args, local, dist, sample_clocks):
            "stage_ms": {nm: st.stage_ms[i] / st.stage_launches[i] for i, nm in enumerate(gsim.STAGES)
                         if st.stage_launches[i]},
            "interactions": int(st.interactions), "tests": int(st.warp_visits), "tree_records": int(st.tree_records),
+           "node_interactions": int(st.node_interactions),
            "internal_nodes": int(st.internal_nodes)}
     return out
 
@@ -386,14 +387,16 @@ def force_error(gsim, wl, pos, vel, mass, local):
 def roofline_of(gsim, wl, m):
     if wl["algo"] == gsim.BARNES_HUT:
         t = m["stage_ms"]["force"] / 1e3
-        # monopole 14 FLOP, quadrupole 31 FLOP per interaction; the library counts all
-        # accepted interactions, so this charges every one as a monopole (a lower bound)
-        flops = 14.0 * m["interactions"]
+        # 14 FLOP per monopole interaction (particle leaves; every record under the
+        # reference rule), 37 per quadrupole interaction (accurate-mode nodes)
+        quads = m["node_interactions"] if wl["flags"] & 0x10 else 0
+        flops = 14.0 * (m["interactions"] - quads) + 37.0 * quads
         achieved = flops / t / 1e12
         extra = {"kernel": "k_force_group" if wl["flags"] & 0x40 else "k_force",
-                 "interactions_per_step": m["interactions"], "tests_per_step": m["tests"],
-                 "tree_records": m["tree_records"], "internal_nodes": m["internal_nodes"],
-                 "flop_model": "14 FLOP per accepted interaction (monopole count; quadrupoles cost more)"}
+                 "interactions_per_step": m["interactions"], "quadrupole_interactions_per_step": quads,
+                 "tests_per_step": m["tests"], "tree_records": m["tree_records"],
+                 "internal_nodes": m["internal_nodes"],
+                 "flop_model": "14 FLOP per monopole (leaf) interaction, 37 per quadrupole (node) interaction"}
     else:
         t = m["stage_ms"]["direct"] / 1e3
         n_al = (wl["n"] + 63) // 64 * 64

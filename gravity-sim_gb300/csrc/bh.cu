@@ -887,7 +887,6 @@ constexpr int kGroupWarps = 4;
 // four-way tree reaches 1216).  Overflow is still checked and reported.
 constexpr int kStackCap = 1600;
 constexpr int kItemCap = 128;     // interaction items between evaluations
-constexpr uint32_t kItemNode = 0x80000000u;
 
 // 1/sqrt: correctly rounded (REFERENCE math) or the hardware approximation (FAST math;
 // d2 >= eps^2 > 0 is never subnormal, so the flush-to-zero form loses nothing)
@@ -962,59 +961,43 @@ __device__ __forceinline__ void quadrupole(float4 q, float4 m2, float px, float 
     ay = fmaf(-t3, sry, fmaf(dy, coef, ay));
 }
 
-// Two particle leaves a (into accumulator 0) and b (into accumulator 1) at once.
-template <bool EXACT>
-__device__ __forceinline__ void monopole2(float4 a, float4 b, float2 P, float2 Q, float2 E2, float2& acx,
-                                          float2& acy) {
-    const float2 dx = sub2(make_float2(a.x, b.x), P), dy = sub2(make_float2(a.y, b.y), Q);
-    const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
-    const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
-    const float2 sc = mul2(mul2(mul2(make_float2(a.z, b.z), r), r), r);
-    acx = fma2(dx, sc, acx);
-    acy = fma2(dy, sc, acy);
-}
-
-// Two nodes a (accumulator 0) and b (accumulator 1) with their second moments.
-template <bool EXACT>
-__device__ __forceinline__ void quadrupole2(float4 a, float4 b, float4 qa, float4 qb, float2 P, float2 Q, float2 E2,
-                                            float2& acx, float2& acy) {
-    const float2 dx = sub2(make_float2(a.x, b.x), P), dy = sub2(make_float2(a.y, b.y), Q);
-    const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
-    const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
-    const float2 r2 = mul2(r, r);
-    const float2 r3 = mul2(r2, r);
-    const float2 r5 = mul2(r3, r2);
-    const float2 r7 = mul2(r5, r2);
-    const float2 sxx = make_float2(qa.x, qb.x), sxy = make_float2(qa.y, qb.y), syy = make_float2(qa.z, qb.z);
-    const float2 srx = fma2(sxx, dx, mul2(sxy, dy));
-    const float2 sry = fma2(sxy, dx, mul2(syy, dy));
-    const float2 u = fma2(dx, srx, mul2(dy, sry));
-    const float2 T = add2(sxx, syy);
-    const float2 coef = fma2(mul2(make_float2(7.5f, 7.5f), u), r7,
-                             fma2(mul2(make_float2(-1.5f, -1.5f), T), r5, mul2(make_float2(a.z, b.z), r3)));
-    const float2 nt3 = mul2(make_float2(-3.0f, -3.0f), r5);
-    acx = fma2(nt3, srx, fma2(dx, coef, acx));
-    acy = fma2(nt3, sry, fma2(dy, coef, acy));
-}
-
+// Evaluation order.  Accepted nodes and particle leaves are summed separately, each in
+// walk order: the k-th node of the walk goes into node accumulator k mod 2, the k-th
+// leaf into leaf accumulator k mod 2, and a particle's acceleration is
+// (node0 + node1) + (leaf0 + leaf1).  How the warp batches its evaluations therefore does
+// not change a bit of the result.
+//
+// A chunk of up to 32 gathered records is staged as structure of arrays, record j at
+// position p = j + (r & 1) (r = records of its kind summed before the chunk): positions
+// (2t, 2t+1) go to accumulators (0, 1) and load as one aligned float2 each -- already
+// the operand pair of an f32x2 instruction.
+constexpr int kChunkSlots = 34;  // 32 records + the parity shift, rounded to a pair
+constexpr int kNodeCap = 96;     // accepted nodes between evaluations
 struct GroupSmem {
     uint32_t stack[kStackCap];
-    uint32_t it_start[kItemCap];
-    uint32_t it_count[kItemCap];  // record count, kItemNode for a node item
-    uint32_t off[kItemCap];       // exclusive record offsets of the items
-    float4 rec[32];               // gathered records of one evaluation chunk
-    float4 quad[32];
+    uint32_t node[kNodeCap];      // accepted node records
+    uint32_t it_start[kItemCap];  // runs of particle leaves: first record
+    uint32_t it_count[kItemCap];  // record count
+    uint32_t off[kItemCap];       // exclusive record offsets of the runs
+    alignas(8) float cx[kChunkSlots];  // centre of mass (or particle position), mass
+    alignas(8) float cy[kChunkSlots];
+    alignas(8) float cm[kChunkSlots];
+    alignas(8) float qxx[kChunkSlots];  // second moments of node records
+    alignas(8) float qxy[kChunkSlots];
+    alignas(8) float qyy[kChunkSlots];
 };
 
-// One record into accumulator `which` (0: .x of the pairs, 1: .y).
+__device__ __forceinline__ float2 ld_pair(const float* a, uint32_t p) { return *reinterpret_cast<const float2*>(a + p); }
+
+// The record at position p into accumulator p & 1 of (ax, ay).
 template <bool EXACT, bool QUAD>
-__device__ __forceinline__ void eval_one(const GroupSmem& g, uint32_t j, int which, float px, float py, float eps2,
-                                         float2& acx, float2& acy) {
-    const float4 q = g.rec[j];
-    float ax = which ? acx.y : acx.x, ay = which ? acy.y : acy.x;
-    if (QUAD && __float_as_uint(q.w)) quadrupole<EXACT>(q, g.quad[j], px, py, eps2, ax, ay);
+__device__ __forceinline__ void eval_slot(const GroupSmem& g, uint32_t p, float px, float py, float eps2,
+                                          float2& acx, float2& acy) {
+    const float4 q = make_float4(g.cx[p], g.cy[p], g.cm[p], 0.0f);
+    float ax = (p & 1u) ? acx.y : acx.x, ay = (p & 1u) ? acy.y : acy.x;
+    if (QUAD) quadrupole<EXACT>(q, make_float4(g.qxx[p], g.qxy[p], g.qyy[p], 0.0f), px, py, eps2, ax, ay);
     else monopole<EXACT>(q, px, py, eps2, ax, ay);
-    if (which) {
+    if (p & 1u) {
         acx.y = ax;
         acy.y = ay;
     } else {
@@ -1023,43 +1006,123 @@ __device__ __forceinline__ void eval_one(const GroupSmem& g, uint32_t j, int whi
     }
 }
 
-// Gather flat record f of the item list into registers (last item with off <= f).
-template <bool QUAD>
-__device__ __forceinline__ void gather_record(const GroupSmem& g, uint32_t n_items, uint32_t f,
-                                              const float4* __restrict__ rec, const float4* __restrict__ quad,
-                                              float4& q, float4& qq) {
+// Positions p (accumulator 0) and p + 1 (accumulator 1), p even, as monopoles.
+template <bool EXACT>
+__device__ __forceinline__ void monopole_pair(const GroupSmem& g, uint32_t p, float2 P, float2 Q, float2 E2,
+                                              float2& acx, float2& acy) {
+    const float2 dx = sub2(ld_pair(g.cx, p), P), dy = sub2(ld_pair(g.cy, p), Q);
+    const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
+    const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
+    const float2 sc = mul2(mul2(mul2(ld_pair(g.cm, p), r), r), r);
+    acx = fma2(dx, sc, acx);
+    acy = fma2(dy, sc, acy);
+}
+
+// Positions p and p + 1, both nodes with second moments (the operation sequence of
+// `quadrupole`, two lanes at once).
+template <bool EXACT>
+__device__ __forceinline__ void quadrupole_pair(const GroupSmem& g, uint32_t p, float2 P, float2 Q, float2 E2,
+                                                float2& acx, float2& acy) {
+    const float2 dx = sub2(ld_pair(g.cx, p), P), dy = sub2(ld_pair(g.cy, p), Q);
+    const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
+    const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
+    const float2 r2 = mul2(r, r);
+    const float2 r3 = mul2(r2, r);
+    const float2 r5 = mul2(r3, r2);
+    const float2 r7 = mul2(r5, r2);
+    const float2 sxx = ld_pair(g.qxx, p), sxy = ld_pair(g.qxy, p), syy = ld_pair(g.qyy, p);
+    const float2 srx = fma2(sxx, dx, mul2(sxy, dy));
+    const float2 sry = fma2(sxy, dx, mul2(syy, dy));
+    const float2 u = fma2(dx, srx, mul2(dy, sry));
+    const float2 T = add2(sxx, syy);
+    const float2 coef = fma2(mul2(make_float2(7.5f, 7.5f), u), r7,
+                             fma2(mul2(make_float2(-1.5f, -1.5f), T), r5, mul2(ld_pair(g.cm, p), r3)));
+    const float2 nt3 = mul2(make_float2(-3.0f, -3.0f), r5);
+    acx = fma2(nt3, srx, fma2(dx, coef, acx));
+    acy = fma2(nt3, sry, fma2(dy, coef, acy));
+}
+
+// Sum the staged chunk of m records shifted by sh into (acx, acy).
+template <bool EXACT, bool QUAD>
+__device__ __forceinline__ void eval_chunk(const GroupSmem& g, uint32_t sh, uint32_t m, float px, float py,
+                                           float eps2, float2& acx, float2& acy) {
+    const float2 P = make_float2(px, px), Q = make_float2(py, py), E2 = make_float2(eps2, eps2);
+    uint32_t p = sh;
+    const uint32_t end = sh + m;
+    if (p & 1u) {  // odd running index: the first record goes alone into accumulator 1
+        eval_slot<EXACT, QUAD>(g, p, px, py, eps2, acx, acy);
+        ++p;
+    }
+#pragma unroll 2
+    for (; p + 1 < end; p += 2) {
+        if (QUAD) quadrupole_pair<EXACT>(g, p, P, Q, E2, acx, acy);
+        else monopole_pair<EXACT>(g, p, P, Q, E2, acx, acy);
+    }
+    if (p < end) eval_slot<EXACT, QUAD>(g, p, px, py, eps2, acx, acy);
+}
+
+// Sum the count accepted nodes (quadrupole term with QUAD), 32 at a time: lane l loads
+// node l of the next chunk while the current one is summed.
+template <bool EXACT, bool QUAD>
+__device__ __forceinline__ void eval_nodes(GroupSmem& g, uint32_t count, const float4* __restrict__ rec,
+                                           const float4* __restrict__ quad, float px, float py, float eps2,
+                                           float2& acx, float2& acy, uint32_t& rn, int lane) {
+    if (!count) return;
+    float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qq = q;
+    if ((uint32_t)lane < count) {
+        const uint32_t r = g.node[lane];
+        q = __ldg(&rec[r]);
+        if (QUAD) qq = __ldg(&quad[r]);
+    }
+    for (uint32_t f0 = 0; f0 < count; f0 += 32) {
+        const uint32_t m = min(count - f0, 32u);
+        const uint32_t sh = rn & 1u;
+        g.cx[lane + sh] = q.x;
+        g.cy[lane + sh] = q.y;
+        g.cm[lane + sh] = q.z;
+        if (QUAD) {
+            g.qxx[lane + sh] = qq.x;
+            g.qxy[lane + sh] = qq.y;
+            g.qyy[lane + sh] = qq.z;
+        }
+        __syncwarp();
+        const uint32_t fn = f0 + 32 + lane;
+        if (fn < count) {
+            const uint32_t r = g.node[fn];
+            q = __ldg(&rec[r]);
+            if (QUAD) qq = __ldg(&quad[r]);
+        }
+        eval_chunk<EXACT, QUAD>(g, sh, m, px, py, eps2, acx, acy);
+        rn += m;
+        __syncwarp();
+    }
+}
+
+// Record f of the leaf runs (last run with off <= f).
+__device__ __forceinline__ float4 gather_leaf(const GroupSmem& g, uint32_t n_items, uint32_t f,
+                                              const float4* __restrict__ rec) {
     uint32_t lo = 0, hi = n_items - 1;
     while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
         if (g.off[mid] <= f) lo = mid;
         else hi = mid - 1;
     }
-    const uint32_t c = g.it_count[lo];
-    const uint32_t r = g.it_start[lo] + (f - g.off[lo]);
-    const uint32_t node = c & kItemNode;
-    q = __ldg(&rec[r]);
-    if (QUAD && node) qq = __ldg(&quad[r]);
-    q.w = __uint_as_float(node);  // the opening radius is not needed here: reuse w as the flag
+    return __ldg(&rec[g.it_start[lo] + (f - g.off[lo])]);
 }
 
-// Sum the n_items items in order, 32 records at a time: lane l gathers record l of the
-// next chunk into registers while the current chunk is summed from shared memory.  The
-// k-th record of the walk (rk counts them) goes into accumulator k mod 2 (.x / .y of
-// acx, acy); consecutive records of the same kind are evaluated in pairs with packed
-// f32x2 instructions.
-template <bool EXACT, bool QUAD>
-__device__ __forceinline__ void eval_items(GroupSmem& g, uint32_t n_items, const float4* __restrict__ rec,
-                                           const float4* __restrict__ quad, float px, float py, float eps2,
-                                           float2& acx, float2& acy, uint32_t& rk, int lane) {
+// Sum the particle leaves of the n_items runs as monopoles, 32 records at a time.
+template <bool EXACT>
+__device__ __forceinline__ void eval_leaves(GroupSmem& g, uint32_t n_items, const float4* __restrict__ rec,
+                                            float px, float py, float eps2, float2& acx, float2& acy, uint32_t& rl,
+                                            int lane) {
     if (!n_items) return;
-    const float2 P = make_float2(px, px), Q = make_float2(py, py), E2 = make_float2(eps2, eps2);
-    // exclusive record offsets of all items: lane l owns items [8l, 8l + 8)
-    uint32_t c8[kItemCap / 32], sum = 0;
+    // exclusive record offsets of all runs: lane l owns runs [4l, 4l + 4)
+    uint32_t c4[kItemCap / 32], sum = 0;
 #pragma unroll
     for (int t = 0; t < kItemCap / 32; ++t) {
         const uint32_t it = lane * (kItemCap / 32) + t;
-        c8[t] = it < n_items ? (g.it_count[it] & ~kItemNode) : 0u;
-        sum += c8[t];
+        c4[t] = it < n_items ? g.it_count[it] : 0u;
+        sum += c4[t];
     }
     uint32_t x = sum;
     for (int o = 1; o < 32; o <<= 1) {
@@ -1071,37 +1134,22 @@ __device__ __forceinline__ void eval_items(GroupSmem& g, uint32_t n_items, const
 #pragma unroll
     for (int t = 0; t < kItemCap / 32; ++t) {
         g.off[lane * (kItemCap / 32) + t] = run;
-        run += c8[t];
+        run += c4[t];
     }
     __syncwarp();
-    float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qq = q;
-    if ((uint32_t)lane < total) gather_record<QUAD>(g, n_items, lane, rec, quad, q, qq);
+    float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if ((uint32_t)lane < total) q = gather_leaf(g, n_items, lane, rec);
     for (uint32_t f0 = 0; f0 < total; f0 += 32) {
-        g.rec[lane] = q;
-        if (QUAD) g.quad[lane] = qq;
-        __syncwarp();
-        const uint32_t fn = f0 + 32 + lane;  // prefetch the next chunk while this one is summed
-        if (fn < total) gather_record<QUAD>(g, n_items, fn, rec, quad, q, qq);
         const uint32_t m = min(total - f0, 32u);
-        uint32_t j = 0;
-        if (rk & 1u) {  // odd running index: the first record goes alone into accumulator 1
-            eval_one<EXACT, QUAD>(g, 0, 1, px, py, eps2, acx, acy);
-            j = 1;
-        }
-        for (; j + 1 < m; j += 2) {  // record j -> accumulator 0, j + 1 -> accumulator 1
-            const float4 a = g.rec[j], b = g.rec[j + 1];
-            const bool na = QUAD && __float_as_uint(a.w), nb2 = QUAD && __float_as_uint(b.w);
-            if (!na && !nb2) {
-                monopole2<EXACT>(a, b, P, Q, E2, acx, acy);
-            } else if (na && nb2) {
-                quadrupole2<EXACT>(a, b, g.quad[j], g.quad[j + 1], P, Q, E2, acx, acy);
-            } else {
-                eval_one<EXACT, QUAD>(g, j, 0, px, py, eps2, acx, acy);
-                eval_one<EXACT, QUAD>(g, j + 1, 1, px, py, eps2, acx, acy);
-            }
-        }
-        if (j < m) eval_one<EXACT, QUAD>(g, j, 0, px, py, eps2, acx, acy);
-        rk += m;
+        const uint32_t sh = rl & 1u;
+        g.cx[lane + sh] = q.x;
+        g.cy[lane + sh] = q.y;
+        g.cm[lane + sh] = q.z;
+        __syncwarp();
+        const uint32_t fn = f0 + 32 + lane;
+        if (fn < total) q = gather_leaf(g, n_items, fn, rec);
+        eval_chunk<EXACT, false>(g, sh, m, px, py, eps2, acx, acy);
+        rl += m;
         __syncwarp();
     }
 }
@@ -1146,10 +1194,11 @@ __device__ __forceinline__ void force_group_body(
         by0[b] = y0;
         by1[b] = y1;
     }
-    float2 acx = make_float2(0.0f, 0.0f), acy = make_float2(0.0f, 0.0f);  // accumulators 0 (.x) and 1 (.y)
-    uint32_t rk = 0;  // records summed so far
-    unsigned long long n_int = 0, n_test = 0;
-    uint32_t size = 0, n_items = 0;
+    // node accumulators {0, 1} and leaf accumulators {0, 1}, x and y
+    float2 anx = make_float2(0.0f, 0.0f), any = anx, alx = anx, aly = anx;
+    uint32_t rn = 0, rl = 0;  // nodes / leaves summed so far
+    unsigned long long n_int = 0, n_test = 0, n_node = 0;
+    uint32_t size = 0, n_nodes = 0, n_items = 0;
     if (skip[0] == 1u) {  // a single particle: the root is its leaf
         if (lane == 0) {
             g.it_start[0] = 0u;
@@ -1163,8 +1212,12 @@ __device__ __forceinline__ void force_group_body(
     __syncwarp();
 
     while (size > 0) {
+        if (n_nodes > (uint32_t)(kNodeCap - 32)) {
+            eval_nodes<EXACT, QUAD>(g, n_nodes, rec, quad, p.x, p.y, eps2, anx, any, rn, lane);
+            n_nodes = 0;
+        }
         if (n_items > (uint32_t)(kItemCap - 64)) {
-            eval_items<EXACT, QUAD>(g, n_items, rec, quad, p.x, p.y, eps2, acx, acy, rk, lane);
+            eval_leaves<EXACT>(g, n_items, rec, p.x, p.y, eps2, alx, aly, rl, lane);
             n_items = 0;
         }
         const uint32_t np = min(size, 32u);
@@ -1174,7 +1227,7 @@ __device__ __forceinline__ void force_group_body(
         __syncwarp();
         size = base;
         if (COUNT) n_test += np;
-        uint32_t a0 = 0, c0 = 0, a1 = 0, c1 = 0, ni = 0;
+        uint32_t a0 = 0, c0 = 0, a1 = 0, c1 = 0, nl = 0, nn = 0;
         uint32_t pu0 = 0, pu1 = 0, pu2 = 0, pu3 = 0, npu = 0;
         if (act) {  // every stacked record is an internal node
             const float4 q = rec[n];
@@ -1187,13 +1240,11 @@ __device__ __forceinline__ void force_group_body(
                 d2 = fminf(d2, fmaf(ex, ex, fmaf(ey, ey, eps2)));
             }
             if (q.w <= d2 * theta2) {
-                a0 = n;
-                c0 = 1u | kItemNode;
-                ni = 1;
+                nn = 1;
             } else if (kd.x == kKidFinest) {
                 a0 = kd.y;
                 c0 = kd.z;
-                ni = 1;
+                nl = 1;
             } else {
                 const uint32_t kk[4] = {kd.x, kd.y, kd.z, kd.w};
 #pragma unroll
@@ -1202,10 +1253,10 @@ __device__ __forceinline__ void force_group_body(
                     if (c == kKidNone) continue;
                     if (c & kKidLeaf) {
                         const uint32_t r = c & ~kKidLeaf;
-                        if (ni == 1 && a0 + c0 == r) ++c0;        // extend the open run
-                        else if (ni == 2 && a1 + c1 == r) ++c1;
-                        else if (ni == 0) { a0 = r; c0 = 1; ni = 1; }
-                        else { a1 = r; c1 = 1; ni = 2; }
+                        if (nl == 1 && a0 + c0 == r) ++c0;        // extend the open run
+                        else if (nl == 2 && a1 + c1 == r) ++c1;
+                        else if (nl == 0) { a0 = r; c0 = 1; nl = 1; }
+                        else { a1 = r; c1 = 1; nl = 2; }
                     } else {
                         if (npu == 0) pu0 = c;
                         else if (npu == 1) pu1 = c;
@@ -1216,54 +1267,64 @@ __device__ __forceinline__ void force_group_body(
                 }
             }
         }
-        // warp-wide offsets in lane order
-        uint32_t x = ni, y = npu;
+        // offsets in lane order, three counts in one scan: nodes <= 32, runs <= 64 and
+        // pushes <= 128 in warp total, so the 8/8/16-bit fields never carry
+        const uint32_t mine = nn | (nl << 8) | (npu << 16);
+        uint32_t x = mine;
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t xo = __shfl_up_sync(0xffffffffu, x, o), yo = __shfl_up_sync(0xffffffffu, y, o);
-            if (lane >= o) {
-                x += xo;
-                y += yo;
-            }
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        const uint32_t ioff = x - ni, poff = y - npu;
-        const uint32_t itot = __shfl_sync(0xffffffffu, x, 31);
-        uint32_t ptot = __shfl_sync(0xffffffffu, y, 31);
+        const uint32_t ex = x - mine, tot = __shfl_sync(0xffffffffu, x, 31);
+        const uint32_t noff = ex & 0xffu, loff = (ex >> 8) & 0xffu, poff = ex >> 16;
+        const uint32_t ntot = tot & 0xffu, ltot = (tot >> 8) & 0xffu;
+        uint32_t ptot = tot >> 16;
         if (size + ptot > (uint32_t)kStackCap) {  // beyond the depth bound: report, do not overrun
             if (lane == 0) atomicOr(err, kErrTree);
             ptot = 0;
             npu = 0;
         }
-        if (ni > 0) {
-            g.it_start[n_items + ioff] = a0;
-            g.it_count[n_items + ioff] = c0;
+        if (nn) g.node[n_nodes + noff] = n;
+        if (nl > 0) {
+            g.it_start[n_items + loff] = a0;
+            g.it_count[n_items + loff] = c0;
         }
-        if (ni > 1) {
-            g.it_start[n_items + ioff + 1] = a1;
-            g.it_count[n_items + ioff + 1] = c1;
+        if (nl > 1) {
+            g.it_start[n_items + loff + 1] = a1;
+            g.it_count[n_items + loff + 1] = c1;
         }
-        if (COUNT) n_int += (ni > 0 ? (c0 & ~kItemNode) : 0u) + (ni > 1 ? c1 : 0u);
+        if (COUNT) {
+            n_int += nn + (nl > 0 ? c0 : 0u) + (nl > 1 ? c1 : 0u);
+            n_node += nn;
+        }
         uint32_t* dst = g.stack + size + poff;
         if (npu > 0) dst[0] = pu0;
         if (npu > 1) dst[1] = pu1;
         if (npu > 2) dst[2] = pu2;
         if (npu > 3) dst[3] = pu3;
 
-        n_items += itot;
+        n_nodes += ntot;
+        n_items += ltot;
         size += ptot;
         __syncwarp();
     }
-    eval_items<EXACT, QUAD>(g, n_items, rec, quad, p.x, p.y, eps2, acx, acy, rk, lane);
+    eval_nodes<EXACT, QUAD>(g, n_nodes, rec, quad, p.x, p.y, eps2, anx, any, rn, lane);
+    eval_leaves<EXACT>(g, n_items, rec, p.x, p.y, eps2, alx, aly, rl, lane);
     if (COUNT) {
         if (skip[0] == 1u && lane == 0) n_int += 1;
-        for (int o = 16; o; o >>= 1) n_int += __shfl_xor_sync(0xffffffffu, n_int, o);
+        for (int o = 16; o; o >>= 1) {
+            n_int += __shfl_xor_sync(0xffffffffu, n_int, o);
+            n_node += __shfl_xor_sync(0xffffffffu, n_node, o);
+        }
         const unsigned long long nval = __popc(__ballot_sync(0xffffffffu, valid));
         if (lane == 0) {
             atomicAdd(&stat[0], n_int * nval);
             atomicAdd(&stat[1], n_test);
+            atomicAdd(&stat[2], n_node * nval);
         }
     }
     if (!valid) return;
-    const float ax = acx.x + acx.y, ay = acy.x + acy.y;
+    const float ax = (anx.x + anx.y) + (alx.x + alx.y), ay = (any.x + any.y) + (aly.x + aly.y);
     if (acc_rec) acc_rec[i] = make_float2(ax, ay);
     const float2 v = vel_in[i];
     const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);
@@ -1300,6 +1361,7 @@ uint64_t bh_capacity(int box_mode, uint64_t n_al) {
 }
 
 // counters layout inside the zeroed block
+// [kCtrStat..+5]: accepted interactions, records tested, node interactions (u64 each)
 enum { kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrCount = 16 };
 
 // Lays the Barnes-Hut scratch out in the system's slab (sim_carve); while the system is
@@ -1536,15 +1598,17 @@ gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_
     return GS_OK;
 }
 
-gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits) {
+gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits,
+                         uint64_t* nodes) {
     uint32_t ctr[kCtrCount];
     GS_CUDA(cudaMemcpy(ctr, s->bh.counters, sizeof ctr, cudaMemcpyDeviceToHost));
     *nv = ctr[kCtrValid];
     *internal = ctr[kCtrInternal];
-    unsigned long long st[2];
+    unsigned long long st[3];
     memcpy(st, ctr + kCtrStat, sizeof st);
     *inter = st[0];
     *visits = st[1];
+    *nodes = st[2];
     return GS_OK;
 }
 

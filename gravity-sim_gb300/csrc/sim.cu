@@ -94,7 +94,8 @@ cudaError_t keep_pool_memory(int device) {
 gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
                         float* node_pos, float* node_mass, float* node_quad, uint64_t capacity,
                         uint64_t* tree_records);
-gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits);
+gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits,
+                         uint64_t* nodes);
 
 }  // namespace gsim
 
@@ -430,14 +431,15 @@ gs_status gs_get_stats(gs_sim* s, gs_stats* out) {
     out->steps_done = s->steps_done;
     out->kernel_launches = s->kernel_launches;
     if (s->p.algorithm == GS_BARNES_HUT && s->steps_done) {
-        uint64_t nv, internal, inter, vis;
-        st = bh_read_counts(s, &nv, &internal, &inter, &vis);
+        uint64_t nv, internal, inter, vis, nodes;
+        st = bh_read_counts(s, &nv, &internal, &inter, &vis, &nodes);
         if (st != GS_OK) return st;
         out->placed_particles = nv;
         out->internal_nodes = internal;
         out->tree_records = nv + internal;
         out->interactions = inter;
         out->warp_visits = vis;
+        out->node_interactions = nodes;
     }
     return GS_OK;
 }

@@ -49,7 +49,7 @@ class Stats(C.Structure):
     _fields_ = [("steps_done", C.c_uint64), ("tree_records", C.c_uint64), ("internal_nodes", C.c_uint64),
                 ("placed_particles", C.c_uint64), ("interactions", C.c_uint64), ("warp_visits", C.c_uint64),
                 ("kernel_launches", C.c_uint64),
-                ("stage_ms", C.c_float * 8), ("stage_launches", C.c_uint32 * 8)]
+                ("stage_ms", C.c_float * 8), ("stage_launches", C.c_uint32 * 8), ("node_interactions", C.c_uint64)]
 
 
 class Tuning(C.Structure):

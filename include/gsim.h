@@ -111,6 +111,8 @@ typedef struct gs_stats {
     uint64_t kernel_launches;  /* CUDA kernels this simulation launched since creation */
     float stage_ms[GS_STAGE_COUNT]; /* bbox, keys, sort, scan, records, sums, force, direct */
     uint32_t stage_launches[GS_STAGE_COUNT];
+    uint64_t node_interactions; /* of `interactions`, those with internal nodes (accurate mode:
+                                   quadrupoles), GS_FLAG_COUNT_INTERACTIONS with GS_FLAG_GROUP_WALK */
 } gs_stats;
 
 GS_API void gs_params_init(gs_params* p);

@@ -420,14 +420,18 @@ static void walk_warp(void* p, uint64_t item, int worker) {
  *     internal children (in preorder) and turns each run of consecutive particle-leaf
  *     children into one range item;
  *   - lanes are handled in order, so items and pushes are in lane order;
- *   - every particle of the group then sums the items in order (nodes with the
- *     quadrupole term, leaves as monopoles) and is integrated. */
+ *   - every particle of the group sums the accepted nodes (quadrupole term) and the
+ *     particle leaves (monopoles) separately, each in walk order: the k-th node goes into
+ *     node accumulator k mod 2, the k-th leaf into leaf accumulator k mod 2, and the
+ *     acceleration is (node0 + node1) + (leaf0 + leaf1); then it is integrated.
+ * The CUDA kernel (bh.cu, force_group_body) batches its evaluations differently; with
+ * this accumulation rule the batching changes no bit. */
 #define GROUP_STACK_CAP 2048
 #define GMAX 64
 static void group_walk_warp(void* p, uint64_t item, int worker) {
     const walk_ctx* c = (const walk_ctx*)p;
     const uint64_t w = item * c->stride;
-    float px[GMAX], py[GMAX], ax[GMAX][2], ay[GMAX][2];
+    float px[GMAX], py[GMAX], ax[GMAX][4], ay[GMAX][4]; /* node 0, node 1, leaf 0, leaf 1 */
     int valid[GMAX];
     const uint32_t G = c->group_size;
     int nvalid = 0;
@@ -442,7 +446,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
         valid[l] = i != c->n_al;
         px[l] = valid[l] ? c->pos_in[2 * i] : 0.0f;
         py[l] = valid[l] ? c->pos_in[2 * i + 1] : 0.0f;
-        ax[l][0] = ay[l][0] = ax[l][1] = ay[l][1] = 0.0f;
+        for (int a = 0; a < 4; ++a) ax[l][a] = ay[l][a] = 0.0f;
         nvalid += valid[l];
     }
     if (!nvalid || !c->tree_size) return;
@@ -460,7 +464,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
     uint32_t stack[GROUP_STACK_CAP + 160];
     uint32_t size = 1, max_size = 1;
     stack[0] = 0;
-    uint64_t inter = 0, visits = 0, rk = 0; /* rk: running record index of the warp */
+    uint64_t inter = 0, visits = 0, rn = 0, rl = 0; /* running node / leaf index of the warp */
     while (size) {
         uint32_t np = size < WARP ? size : WARP;
         uint32_t base = size - np;
@@ -482,9 +486,9 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                 }
                 accept = c->radius[n] <= d2 * c->theta2;
             }
-            if (accept) { /* one item: the record itself */
+            if (accept) { /* one item: the record itself (a leaf only when the root is one) */
                 const float nx = c->npos[2 * n], ny = c->npos[2 * n + 1], nm = c->nmass[n];
-                const int a = (int)(rk & 1u);
+                const int a = sk > 1 ? (int)(rn & 1u) : 2 + (int)(rl & 1u);
                 for (uint32_t l = 0; l < G; ++l) {
                     if (!valid[l]) continue;
                     float dx = nx - px[l], dy = ny - py[l];
@@ -498,7 +502,8 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                         ay[l][a] = fmaf(dy, sc, ay[l][a]);
                     }
                 }
-                ++rk;
+                if (sk > 1) ++rn;
+                else ++rl;
                 inter += (uint64_t)nvalid;
                 continue;
             }
@@ -510,7 +515,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                     while (r < end && c->skip[r] == 1) ++r;
                     for (uint32_t q = ch; q < r; ++q) {
                         const float nx = c->npos[2 * q], ny = c->npos[2 * q + 1], nm = c->nmass[q];
-                        const int a = (int)(rk & 1u);
+                        const int a = 2 + (int)(rl & 1u);
                         for (uint32_t l = 0; l < G; ++l) {
                             if (!valid[l]) continue;
                             float dx = nx - px[l], dy = ny - py[l];
@@ -518,7 +523,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                             ax[l][a] = fmaf(dx, sc, ax[l][a]);
                             ay[l][a] = fmaf(dy, sc, ay[l][a]);
                         }
-                        ++rk;
+                        ++rl;
                     }
                     inter += (uint64_t)nvalid * (r - ch);
                     ch = r;
@@ -536,7 +541,8 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
         if (!valid[l]) continue;
         uint32_t i = c->src[(uint32_t)w * G + l];
         float vx = c->vel_in[2 * i], vy = c->vel_in[2 * i + 1];
-        const float axl = ax[l][0] + ax[l][1], ayl = ay[l][0] + ay[l][1];
+        const float axl = (ax[l][0] + ax[l][1]) + (ax[l][2] + ax[l][3]);
+        const float ayl = (ay[l][0] + ay[l][1]) + (ay[l][2] + ay[l][3]);
         float nvx = fmaf(axl, c->k, vx), nvy = fmaf(ayl, c->k, vy);
         c->pos_out[2 * i] = fmaf(vx + nvx, c->hdt, px[l]);
         c->pos_out[2 * i + 1] = fmaf(vy + nvy, c->hdt, py[l]);
