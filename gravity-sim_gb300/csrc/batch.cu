@@ -177,6 +177,7 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
     const gs_sim* bh0 = p.n_bh ? order[0] : nullptr;
     const gs_sim* dir0 = p.n_direct ? order[p.n_bh] : nullptr;
     p.passes = bh0 ? bh0->bh.passes : 0;
+    p.depth = bh0 ? bh0->bh.depth : 0;
     p.bbox = bh0 && bh0->p.box_mode == GS_BOX_BOUNDING;
     p.quad = bh0 && bh0->bh.quad != nullptr;
     p.group = bh0 && (bh0->p.flags & GS_FLAG_GROUP_WALK);
@@ -226,7 +227,8 @@ bool BatchEngine::in_step() const {
 
 uint32_t BatchEngine::launches_per_step() const {
     uint32_t k = 0;
-    if (plan.n_bh) k += 7u + (uint32_t)plan.passes + (plan.bbox ? 1u : 0u);  // clear keys scan records nodes sums force
+    if (plan.n_bh)  // clear keys scan records nodes force, radix passes, box, moment levels
+        k += 6u + (uint32_t)plan.passes + (plan.bbox ? 1u : 0u) + (uint32_t)(plan.depth - kLevelTop + 1);
     if (plan.n_direct) k += 1u;
     return k;
 }

@@ -18,13 +18,14 @@
 //   k_records     preorder records: node (d, s) at s + E(s) + d - dmin(s), particle leaf
 //                 at s + E(s) + e(s); skip = end + E(end) - index (the reference's count.y),
 //                 radius = radius0 / 4^d (TreeMoveShader.comp:70-71)
-//   k_bottom_up   bottom-up mass and mass-moment sums in one launch (the last child to
-//                 finish computes its parent), children in the order of
+//   k_level_sums  mass and mass-moment sums level by level, finest first (one launch per
+//                 deep level, one block for the top levels), children in the order of
 //                 TreeInitShader.comp:78-80; centre of mass as TreeMoveShader.comp:66-67
 //   k_force       ForceShader.comp:78-152 semantics: one warp walks the preorder records
 //                 for 32 consecutive sorted slots; a record is accepted only if every
 //                 lane satisfies radius <= d2 * theta^2; 32-record window staged in shared
 //                 memory; the integrator and the scatter to original order are fused.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 
@@ -536,71 +537,91 @@ k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, 
     records_body(grid_blk(), skey, sidx, E, valid_count, D, pos, mass, rec, skip, node_slot, cap, n_al, err);
 }
 
+// Internal nodes by level: the nodes of level d are listed in levels[level_off(d) ..),
+// at most level_cap(d) of them (disjoint cells of >= 2 particles: <= 4^d and <= N/2).
+__host__ __device__ __forceinline__ uint32_t level_cap(int d, uint32_t n_al) {
+    const uint64_t c = 1ull << (2 * d), h = n_al / 2 + 1;
+    return (uint32_t)(c < h ? c : h);
+}
+__host__ __device__ __forceinline__ uint32_t level_off(int d, uint32_t n_al) {
+    uint32_t o = 0;
+    for (int e = 0; e < d; ++e) o += level_cap(e, n_al);
+    return o;
+}
+
 // One thread per internal node (d, s): skip (the reference's count.y), the level radius
-// of TreeMoveShader.comp:70-71, the cell end, the child descriptors, the parent link of
-// its internal children and the number of internal children the bottom-up pass waits for.
+// of TreeMoveShader.comp:70-71, the child descriptors, and the node's entry in the list
+// of its level (slots reserved per block: a shared histogram, one atomic per level).
 __device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
                                            const uint32_t* __restrict__ counts, int D,
                                            const BHParams* __restrict__ bp, const uint32_t* __restrict__ node_slot,
                                            float4* __restrict__ rec, uint32_t* __restrict__ skip,
-                                           uint32_t* __restrict__ nend, uint4* __restrict__ kids,
-                                           uint32_t* __restrict__ parent, uint32_t* __restrict__ pending,
-                                           uint32_t* __restrict__ arrived, uint2* __restrict__ nodeinfo,
-                                           uint64_t cap, int* __restrict__ err) {
+                                           uint4* __restrict__ kids, uint2* __restrict__ nodeinfo,
+                                           uint32_t* __restrict__ level_count, uint32_t* __restrict__ levels,
+                                           uint32_t n_al, uint64_t cap, int* __restrict__ err) {
+    __shared__ uint32_t s_cnt[16], s_base[16];
     const uint32_t nv = counts[0], M = counts[1];
     const float radius0 = bp->radius0;
-    for (uint32_t j = blk.id * 256 + threadIdx.x; j < M; j += blk.count * 256) {
-        const uint32_t s = node_slot[j];
-        const uint32_t at = s + j;
-        if (s >= nv || at >= cap) {  // only after a failed sort or scan (error flag already set)
-            atomicOr(err, kErrTree);
-            continue;
-        }
-        const int d = slot_dmin(skey, s, D) + (int)(j - E[s]);
-        const int shift = 2 * (D - d);
-        const uint32_t end = cell_end(skey, s + 1, nv, shift, skey[s] >> shift);
-        rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
-        skip[at] = end + E[end] - at;
-        nend[at] = end;
-        nodeinfo[at] = make_uint2(s, (uint32_t)d);
-        arrived[at] = 0u;
-        if (d == 0) parent[at] = kKidNone;  // the root
-        if (d == D) {
-            kids[at] = make_uint4(kKidFinest, at + 1, end - s, 0u);  // all children are leaves
-            pending[at] = 0u;
-            continue;
-        }
-        uint32_t kid[4] = {kKidNone, kKidNone, kKidNone, kKidNone};
-        uint32_t nk = 0, nint = 0;
-        const int cshift = 2 * (D - d - 1);
-        for (uint32_t t = s; t < end;) {  // the level-(d+1) cells inside [s, end), in Morton order
-            const uint32_t tend = cell_end(skey, t + 1, nv, cshift, skey[t] >> cshift);
-            uint32_t c;
-            if (tend - t >= 2) {  // an internal node (d+1, t)
-                c = t + E[t] + (uint32_t)(d + 1 - slot_dmin(skey, t, D));
-                parent[c] = at;
-                ++nint;
+    for (uint32_t j0 = blk.id * 256; j0 < M; j0 += blk.count * 256) {  // uniform over the block
+        if (threadIdx.x < 16) s_cnt[threadIdx.x] = 0u;
+        __syncthreads();
+        const uint32_t j = j0 + threadIdx.x;
+        int d = -1;
+        uint32_t at = 0, rank = 0;
+        if (j < M) {
+            const uint32_t s = node_slot[j];
+            at = s + j;
+            if (s >= nv || at >= cap) {  // only after a failed sort or scan (error flag already set)
+                atomicOr(err, kErrTree);
             } else {
-                c = leaf_of(skey, E, t, nv, D) | kKidLeaf;
+                d = slot_dmin(skey, s, D) + (int)(j - E[s]);
+                const int shift = 2 * (D - d);
+                const uint32_t ks = skey[s];
+                const uint32_t end = cell_end(skey, s + 1, nv, shift, ks >> shift);
+                rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
+                skip[at] = end + E[end] - at;
+                nodeinfo[at] = make_uint2(ks, (uint32_t)d);  // a key of the cell, its level
+                if (d == D) {
+                    kids[at] = make_uint4(kKidFinest, at + 1, end - s, 0u);  // all children are leaves
+                } else {
+                    uint32_t kid[4] = {kKidNone, kKidNone, kKidNone, kKidNone};
+                    uint32_t nk = 0;
+                    const int cshift = 2 * (D - d - 1);
+                    for (uint32_t t = s; t < end;) {  // the level-(d+1) cells inside [s, end), in Morton order
+                        const uint32_t tend = cell_end(skey, t + 1, nv, cshift, skey[t] >> cshift);
+                        uint32_t c;
+                        if (tend - t >= 2) c = t + E[t] + (uint32_t)(d + 1 - slot_dmin(skey, t, D));  // node (d+1, t)
+                        else c = leaf_of(skey, E, t, nv, D) | kKidLeaf;
+                        if (nk < 4) kid[nk] = c;
+                        ++nk;
+                        t = tend;
+                    }
+                    if (nk > 4) atomicOr(err, kErrTree);
+                    kids[at] = make_uint4(kid[0], kid[1], kid[2], kid[3]);
+                }
+                rank = atomicAdd(&s_cnt[d], 1u);
             }
-            if (nk < 4) kid[nk] = c;
-            ++nk;
-            t = tend;
         }
-        if (nk > 4) atomicOr(err, kErrTree);
-        kids[at] = make_uint4(kid[0], kid[1], kid[2], kid[3]);
-        pending[at] = nint;
+        __syncthreads();
+        if (threadIdx.x < 16 && s_cnt[threadIdx.x]) s_base[threadIdx.x] = atomicAdd(&level_count[threadIdx.x], s_cnt[threadIdx.x]);
+        __syncthreads();
+        if (d >= 0) {
+            const uint32_t slot = s_base[d] + rank;
+            if (slot < level_cap(d, n_al)) levels[level_off(d, n_al) + slot] = at;
+            else atomicOr(err, kErrTree);
+        }
+        __syncthreads();  // s_cnt / s_base are reused
     }
 }
 
 __global__ void __launch_bounds__(256)
 k_nodes(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E, const uint32_t* __restrict__ counts,
         int D, const BHParams* __restrict__ bp, const uint32_t* __restrict__ node_slot, float4* __restrict__ rec,
-        uint32_t* __restrict__ skip, uint32_t* __restrict__ nend, uint4* __restrict__ kids,
-        uint32_t* __restrict__ parent, uint32_t* __restrict__ pending, uint32_t* __restrict__ arrived,
-        uint2* __restrict__ nodeinfo, uint64_t cap, int* __restrict__ err) {
-    nodes_body(grid_blk(), skey, E, counts, D, bp, node_slot, rec, skip, nend, kids, parent, pending, arrived,
-               nodeinfo, cap, err);
+        uint32_t* __restrict__ skip, uint4* __restrict__ kids, uint2* __restrict__ nodeinfo,
+        uint32_t* __restrict__ level_count, uint32_t* __restrict__ levels, uint32_t n_al, uint64_t cap,
+        int* __restrict__ err) {
+    nodes_body(grid_blk(), skey, E, counts, D, bp, node_slot, rec, skip, kids, nodeinfo, level_count, levels, n_al,
+               cap, err);
 }
 
 __device__ __forceinline__ uint32_t compact_bits(uint32_t v) {  // inverse of spread_bits
@@ -679,6 +700,8 @@ __device__ void compute_node(uint32_t at, int D, int safe, int bbox_mode, const 
                              const uint32_t* __restrict__ skey, float4* rec, const uint4* __restrict__ kids,
                              const uint2* __restrict__ nodeinfo, float2* msum, float4* quad) {
     const uint4 kd = kids[at];
+    const uint2 info = nodeinfo[at];                    // {a key of the cell, level}
+    const float r0 = safe ? 0.0f : __ldcg(&rec[at]).w;  // the level radius k_nodes wrote
     float sx = 0.0f, sy = 0.0f, sm = 0.0f, cx, cy;
     float qxx = 0.0f, qxy = 0.0f, qyy = 0.0f;
     if (kd.x == kKidFinest) {  // particle leaves at kd.y .. kd.y + kd.z - 1
@@ -743,56 +766,62 @@ __device__ void compute_node(uint32_t at, int D, int safe, int bbox_mode, const 
     }
     msum[at] = make_float2(sx, sy);
     if (QUAD) quad[at] = make_float4(qxx, qxy, qyy, 0.0f);
-    float r = __ldcg(&rec[at]).w;
-    if (safe) {
-        const uint2 info = nodeinfo[at];
-        r = cell_bmax2(bbox_mode, bp, D, (int)info.y, skey[info.x], cx, cy);
-    }
+    const float r = safe ? cell_bmax2(bbox_mode, bp, D, (int)info.y, info.x, cx, cy) : r0;
     rec[at] = make_float4(cx, cy, sm, r);
 }
 
-// Bottom-up pass in one launch: a thread starts at the finest node of its slot when that
-// node has no internal children, computes it, and climbs: the child that completes a
-// parent's count of internal children (atomic ticket, no waiting) computes the parent.
-// Every node sums its children in the fixed Morton order, so the result does not depend
-// on which thread gets there.
+// Moments level by level, finest first: every node of level d is computed by one thread
+// once the launch for level d + 1 has finished, so no node waits on another.  Every node
+// sums its children in the fixed Morton order.
 template <bool QUAD>
-__device__ __forceinline__ void bottom_up_body(Blk blk, const uint32_t* __restrict__ skey,
-                                               const uint32_t* __restrict__ E,
-                                               const uint32_t* __restrict__ valid_count, int D, float4* rec,
-                                               const uint4* __restrict__ kids, const uint32_t* __restrict__ parent,
-                                               const uint32_t* __restrict__ pending, uint32_t* arrived,
-                                               const uint2* __restrict__ nodeinfo, float2* msum, float4* quad,
-                                               int safe, int bbox_mode, const BHParams* __restrict__ bpp,
-                                               uint32_t cap) {
-    const uint32_t nv = *valid_count;
+__device__ __forceinline__ void level_sums_body(Blk blk, int d, const uint32_t* __restrict__ level_count,
+                                                const uint32_t* __restrict__ levels, uint32_t n_al,
+                                                const uint32_t* __restrict__ skey, int D, float4* rec,
+                                                const uint4* __restrict__ kids, const uint2* __restrict__ nodeinfo,
+                                                float2* msum, float4* quad, int safe, int bbox_mode,
+                                                const BHParams* __restrict__ bpp) {
+    const uint32_t cnt = min(level_count[d], level_cap(d, n_al));
+    const uint32_t* list = levels + level_off(d, n_al);
     const BHParams bp = *bpp;
-    for (uint32_t s = blk.id * 256 + threadIdx.x; s < nv; s += blk.count * 256) {
-        const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
-        if (dmax < dmin) continue;
-        uint32_t at = s + E[s] + (uint32_t)(dmax - dmin);
-        if (at >= cap || pending[at] != 0u) continue;
-        for (;;) {
-            compute_node<QUAD>(at, D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum, quad);
-            __threadfence();  // publish this node before its parent can be computed
-            const uint32_t p = parent[at];
-            if (p == kKidNone || p >= cap) break;
-            if (atomicAdd(&arrived[p], 1u) + 1u != pending[p]) break;
-            __threadfence();
-            at = p;
-        }
+    for (uint32_t t = blk.id * 256 + threadIdx.x; t < cnt; t += blk.count * 256)
+        compute_node<QUAD>(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum, quad);
+}
+
+// Levels kLevelTop .. 0 in one block, a barrier between levels.
+template <bool QUAD>
+__device__ __forceinline__ void top_sums_body(const uint32_t* __restrict__ level_count,
+                                              const uint32_t* __restrict__ levels, uint32_t n_al,
+                                              const uint32_t* __restrict__ skey, int D, float4* rec,
+                                              const uint4* __restrict__ kids, const uint2* __restrict__ nodeinfo,
+                                              float2* msum, float4* quad, int safe, int bbox_mode,
+                                              const BHParams* __restrict__ bpp) {
+    const BHParams bp = *bpp;
+    for (int d = min(kLevelTop, D); d >= 0; --d) {
+        const uint32_t cnt = min(level_count[d], level_cap(d, n_al));
+        const uint32_t* list = levels + level_off(d, n_al);
+        for (uint32_t t = threadIdx.x; t < cnt; t += blockDim.x)
+            compute_node<QUAD>(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum, quad);
+        __syncthreads();  // level d is complete (and visible to the block) before level d - 1
     }
 }
 
 template <bool QUAD>
 __global__ void __launch_bounds__(256)
-k_bottom_up(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
-            const uint32_t* __restrict__ valid_count, int D, float4* rec, const uint4* __restrict__ kids,
-            const uint32_t* __restrict__ parent, const uint32_t* __restrict__ pending, uint32_t* arrived,
-            const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
-            const BHParams* __restrict__ bpp, uint32_t cap) {
-    bottom_up_body<QUAD>(grid_blk(), skey, E, valid_count, D, rec, kids, parent, pending, arrived, nodeinfo, msum,
-                         quad, safe, bbox_mode, bpp, cap);
+k_level_sums(int d, const uint32_t* __restrict__ level_count, const uint32_t* __restrict__ levels, uint32_t n_al,
+             const uint32_t* __restrict__ skey, int D, float4* rec, const uint4* __restrict__ kids,
+             const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
+             const BHParams* __restrict__ bpp) {
+    level_sums_body<QUAD>(grid_blk(), d, level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, quad, safe,
+                          bbox_mode, bpp);
+}
+
+template <bool QUAD>
+__global__ void __launch_bounds__(512)
+k_top_sums(const uint32_t* __restrict__ level_count, const uint32_t* __restrict__ levels, uint32_t n_al,
+           const uint32_t* __restrict__ skey, int D, float4* rec, const uint4* __restrict__ kids,
+           const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
+           const BHParams* __restrict__ bpp) {
+    top_sums_body<QUAD>(level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, quad, safe, bbox_mode, bpp);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1361,8 +1390,12 @@ uint64_t bh_capacity(int box_mode, uint64_t n_al) {
 }
 
 // counters layout inside the zeroed block
-// [kCtrStat..+5]: accepted interactions, records tested, node interactions (u64 each)
-enum { kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrCount = 16 };
+// [kCtrStat..+5]: accepted interactions, records tested, node interactions (u64 each);
+// [kCtrLevel..+15]: internal nodes per level
+enum {
+    kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrLevel = 16,
+    kCtrCount = 32
+};
 
 // Lays the Barnes-Hut scratch out in the system's slab (sim_carve); while the system is
 // being sized (no slab yet) this only counts bytes.
@@ -1382,12 +1415,9 @@ void bh_carve(gs_sim* s) {
     sim_carve(s, (void**)&w.E, (n + 1) * sizeof(uint32_t));
     sim_carve(s, (void**)&w.rec, (w.cap + 32) * sizeof(float4));
     sim_carve(s, (void**)&w.skip, (w.cap + 32) * sizeof(uint32_t));
-    sim_carve(s, (void**)&w.nend, w.cap * sizeof(uint32_t));
     sim_carve(s, (void**)&w.msum, w.cap * sizeof(float2));
     sim_carve(s, (void**)&w.kids, w.cap * sizeof(uint4));
-    sim_carve(s, (void**)&w.parent, w.cap * sizeof(uint32_t));
-    sim_carve(s, (void**)&w.pending, w.cap * sizeof(uint32_t));
-    sim_carve(s, (void**)&w.arrived, w.cap * sizeof(uint32_t));
+    sim_carve(s, (void**)&w.levels, (size_t)level_off(w.depth + 1, (uint32_t)n) * sizeof(uint32_t));
     sim_carve(s, (void**)&w.nodeinfo, w.cap * sizeof(uint2));
     sim_carve(s, (void**)&w.node_slot, w.cap * sizeof(uint32_t));
     w.quad = nullptr;
@@ -1471,24 +1501,31 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     k_records<<<grid_for(n, 256), 256, 0, st>>>(skey, sidx, w.E, ctr + kCtrValid, w.depth, s->pos[in], s->mass[in],
                                                 w.rec, w.skip, w.node_slot, w.cap, n, s->d_err);
     k_nodes<<<grid_for(n, 256), 256, 0, st>>>(skey, w.E, ctr + kCtrValid, w.depth, w.params, w.node_slot, w.rec,
-                                              w.skip, w.nend, w.kids, w.parent, w.pending, w.arrived, w.nodeinfo,
-                                              w.cap, s->d_err);
+                                              w.skip, w.kids, w.nodeinfo, ctr + kCtrLevel, w.levels, n, w.cap,
+                                              s->d_err);
     count_launch(s, 2);
     stage_end(s, kStageRecords, profile);
     stage_begin(s, kStageSums, profile);
     {
         const int safe = (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0;
+        const int bb = bbox ? 1 : 0;
+        for (int d = w.depth; d > kLevelTop; --d) {
+            const int blocks = (int)std::min<uint64_t>((uint64_t)grid_for(n, 256), (level_cap(d, n) + 255) / 256);
+            if (w.quad)
+                k_level_sums<true><<<blocks, 256, 0, st>>>(d, ctr + kCtrLevel, w.levels, n, skey, w.depth, w.rec,
+                                                           w.kids, w.nodeinfo, w.msum, w.quad, safe, bb, w.params);
+            else
+                k_level_sums<false><<<blocks, 256, 0, st>>>(d, ctr + kCtrLevel, w.levels, n, skey, w.depth, w.rec,
+                                                            w.kids, w.nodeinfo, w.msum, nullptr, safe, bb, w.params);
+        }
         if (w.quad)
-            k_bottom_up<true><<<grid_for(n, 256), 256, 0, st>>>(skey, w.E, ctr + kCtrValid, w.depth, w.rec, w.kids,
-                                                                w.parent, w.pending, w.arrived, w.nodeinfo, w.msum,
-                                                                w.quad, safe, bbox ? 1 : 0, w.params, (uint32_t)w.cap);
+            k_top_sums<true><<<1, 512, 0, st>>>(ctr + kCtrLevel, w.levels, n, skey, w.depth, w.rec, w.kids,
+                                                w.nodeinfo, w.msum, w.quad, safe, bb, w.params);
         else
-            k_bottom_up<false><<<grid_for(n, 256), 256, 0, st>>>(skey, w.E, ctr + kCtrValid, w.depth, w.rec, w.kids,
-                                                                 w.parent, w.pending, w.arrived, w.nodeinfo, w.msum,
-                                                                 nullptr, safe, bbox ? 1 : 0, w.params,
-                                                                 (uint32_t)w.cap);
+            k_top_sums<false><<<1, 512, 0, st>>>(ctr + kCtrLevel, w.levels, n, skey, w.depth, w.rec, w.kids,
+                                                 w.nodeinfo, w.msum, nullptr, safe, bb, w.params);
     }
-    count_launch(s);
+    count_launch(s, (uint32_t)(w.depth - kLevelTop + 1));
     stage_end(s, kStageSums, profile);
     stage_begin(s, kStageForce, profile);
     const float k = s->G * s->dt_eff;  // ForceShader.comp:145 (GRAVITATIONAL_CONST * SIMULATION_TIME)
@@ -1708,16 +1745,25 @@ __global__ void __launch_bounds__(256) kb_nodes(BatchArgs a) {
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     nodes_body(bb.blk, d.keys[d.passes & 1], d.E, d.counters + kCtrValid, d.depth, d.params, d.node_slot, d.rec,
-               d.skip, d.nend, d.kids, d.parent, d.pending, d.arrived, d.nodeinfo, d.cap, d.err);
+               d.skip, d.kids, d.nodeinfo, d.counters + kCtrLevel, d.levels, d.n_al, d.cap, d.err);
+}
+
+// level lv of every system (systems shallower than lv have nothing to do)
+template <bool QUAD>
+__global__ void __launch_bounds__(256) kb_level_sums(BatchArgs a, int lv) {
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    if (lv > d.depth) return;
+    level_sums_body<QUAD>(bb.blk, lv, d.counters + kCtrLevel, d.levels, d.n_al, d.keys[d.passes & 1], d.depth, d.rec,
+                          d.kids, d.nodeinfo, d.msum, d.quad, d.safe, d.bbox, d.params);
 }
 
 template <bool QUAD>
-__global__ void __launch_bounds__(256) kb_bottom_up(BatchArgs a) {
+__global__ void __launch_bounds__(512) kb_top_sums(BatchArgs a) {
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
-    bottom_up_body<QUAD>(bb.blk, d.keys[d.passes & 1], d.E, d.counters + kCtrValid, d.depth, d.rec, d.kids,
-                         d.parent, d.pending, d.arrived, d.nodeinfo, d.msum, d.quad, d.safe, d.bbox, d.params,
-                         d.cap);
+    top_sums_body<QUAD>(d.counters + kCtrLevel, d.levels, d.n_al, d.keys[d.passes & 1], d.depth, d.rec, d.kids,
+                        d.nodeinfo, d.msum, d.quad, d.safe, d.bbox, d.params);
 }
 
 template <bool EXACT, bool QUAD, bool COUNT>
@@ -1778,13 +1824,11 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
     d.E = w.E;
     d.rec = w.rec;
     d.skip = w.skip;
-    d.nend = w.nend;
+
     d.msum = w.msum;
     d.quad = w.quad;
     d.kids = w.kids;
-    d.parent = w.parent;
-    d.pending = w.pending;
-    d.arrived = w.arrived;
+    d.levels = w.levels;
     d.nodeinfo = w.nodeinfo;
     d.node_slot = w.node_slot;
     d.bbox_part = w.bbox_part;
@@ -1809,6 +1853,7 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
     blocks[kTabGrid] = (uint32_t)grid_for(n, 256);
     blocks[kTabSort] = w.sort_tiles;
     blocks[kTabScan] = w.scan_tiles;
+    blocks[kTabOne] = 1;
     const int warps = (s->p.flags & GS_FLAG_GROUP_WALK) ? kGroupWarps : kForceWarps;
     blocks[kTabForce] = (uint32_t)((n / 32 + warps - 1) / warps);
 }
@@ -1853,8 +1898,12 @@ cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st) {
     kb_meta_scan<<<p.total[kTabScan], kScanThreads, 0, st>>>(args(kTabScan));
     kb_records<<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
     kb_nodes<<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
-    if (p.quad) kb_bottom_up<true><<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
-    else kb_bottom_up<false><<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
+    for (int lv = p.depth; lv > kLevelTop; --lv) {
+        if (p.quad) kb_level_sums<true><<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid), lv);
+        else kb_level_sums<false><<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid), lv);
+    }
+    if (p.quad) kb_top_sums<true><<<p.total[kTabOne], 512, 0, st>>>(args(kTabOne));
+    else kb_top_sums<false><<<p.total[kTabOne], 512, 0, st>>>(args(kTabOne));
     const uint32_t fg = p.force_grid < (int)p.total[kTabForce] ? (uint32_t)p.force_grid : p.total[kTabForce];
     uint32_t* work = p.d_work;
 #define GS_BGROUP(E_, Q_, C_) kb_force_group<E_, Q_, C_><<<fg, kGroupWarps * 32, 0, st>>>(args(kTabForce), work)

@@ -43,6 +43,9 @@ constexpr int kSortTile = kSortThreads * kSortKeysPerThread;
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
+// moments: levels at or above kLevelTop (<= 341 nodes) are summed by one block, every
+// deeper level by a launch of its own
+constexpr int kLevelTop = 4;
 // bounded spin for decoupled look-back: after this many polls the kernel flags an error
 constexpr uint32_t kSpinLimit = 1u << 24;
 
@@ -60,20 +63,17 @@ struct BHWork {
     uint32_t* hist = nullptr;          // [4][256] digit counts
     uint32_t* sort_status = nullptr;   // [passes][tiles][256]
     uint32_t* counters = nullptr;      // [0..3] sort tile tickets, [4] scan ticket, [5] bbox ticket,
-                                       // [6] valid count, [7] internal count, [8..11] interaction
-                                       // and test counts (2 x u64)
+                                       // [6] valid count, [7] internal count, [8..13] interaction,
+                                       // test and node counts (3 x u64), [16..31] nodes per level
     uint32_t* scan_status = nullptr;   // [scan tiles]
     uint32_t* E = nullptr;             // [N_al + 1]
     float4* rec = nullptr;             // [cap + 32]
     uint32_t* skip = nullptr;          // [cap + 32]
-    uint32_t* nend = nullptr;          // [cap]
     float2* msum = nullptr;            // [cap]
     float4* quad = nullptr;            // [cap] {sxx, sxy, syy, -} (GS_FLAG_QUADRUPOLE)
     uint4* kids = nullptr;             // [cap] child descriptors of internal records
-    uint32_t* parent = nullptr;        // [cap] parent record of an internal record
-    uint32_t* pending = nullptr;       // [cap] internal children of a record
-    uint32_t* arrived = nullptr;       // [cap] internal children finished (bottom-up tickets)
-    uint2* nodeinfo = nullptr;         // [cap] {start slot, level} of an internal record
+    uint32_t* levels = nullptr;        // internal records by level (level_off / level_cap in bh.cu)
+    uint2* nodeinfo = nullptr;         // [cap] {a key of the cell, level} of an internal record
     uint32_t* node_slot = nullptr;     // [cap] start slot of internal node j (ordinal)
     float* bbox_part = nullptr;        // [blocks][4]
     BHParams* params = nullptr;        // device
@@ -112,13 +112,10 @@ struct SysDesc {
     uint32_t* E;
     float4* rec;
     uint32_t* skip;
-    uint32_t* nend;
     float2* msum;
     float4* quad;
     uint4* kids;
-    uint32_t* parent;
-    uint32_t* pending;
-    uint32_t* arrived;
+    uint32_t* levels;
     uint2* nodeinfo;
     uint32_t* node_slot;
     float* bbox_part;
@@ -136,7 +133,7 @@ struct SysDesc {
 
 // Per-stage block tables of a batch: table t holds the exclusive prefix of the blocks each
 // system gets in stage t; a block finds its system by binary search.
-enum BatchTable { kTabClear = 0, kTabBBox, kTabGrid, kTabSort, kTabScan, kTabForce, kTabDirect, kTabCount };
+enum BatchTable { kTabClear = 0, kTabBBox, kTabGrid, kTabSort, kTabScan, kTabOne, kTabForce, kTabDirect, kTabCount };
 
 // What the batched launchers need: descriptors (Barnes-Hut systems first, largest first),
 // block tables, and the batch-wide work counters cleared by the first stage.
@@ -147,6 +144,7 @@ struct BatchPlan {
     uint32_t total[kTabCount] = {};
     uint32_t* d_work = nullptr;  // [0] next force block
     int passes = 0;
+    int depth = 0;               // finest level of the Barnes-Hut members (all share the box mode)
     bool bbox = false, quad = false, group = false, exact = false, count = false, direct_exact = false;
     int force_grid = 0;          // persistent force grid (resident blocks)
 };

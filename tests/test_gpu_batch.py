@@ -69,7 +69,8 @@ def test_mixed_batch_bit_identical(gs, flags):
         s.reset_stats()
     _run_alone(alone, 3)
     with gs.Batch(batched, flags=flags) as b:
-        assert b.kernels_per_step == 13  # clear bbox keys 4x sort scan records nodes sums force + direct
+        # clear bbox keys 4x sort scan records nodes, moments (levels 15..5 + one top launch), force; direct
+        assert b.kernels_per_step == 1 + 1 + 1 + 4 + 1 + 1 + 1 + 12 + 1 + 1
         b.run(3)
         b.sync()
         _assert_same(alone, batched, MIXED)
@@ -86,7 +87,8 @@ def test_reference_rule_batch_bit_identical(gs):
         s.reset_stats()
     _run_alone(alone, 2)
     with gs.Batch(batched) as b:
-        assert b.kernels_per_step == 3 + 3 + 4 + 1  # clear keys 3x sort scan records nodes sums force + direct
+        # clear keys 3x sort scan records nodes, moments (levels 10..5 + top), force; direct
+        assert b.kernels_per_step == 1 + 1 + 3 + 1 + 1 + 1 + 7 + 1 + 1
         b.run(2)
         b.sync()
         _assert_same(alone, batched, specs)
