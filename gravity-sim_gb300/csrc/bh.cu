@@ -89,7 +89,13 @@ __device__ __forceinline__ int slot_dmax(const uint32_t* k, uint32_t s, uint32_t
 // bounding box: grid-stride min/max; the last block derives the box in FP64
 // ------------------------------------------------------------------------------------
 constexpr int kBBoxThreads = 256;
-constexpr int kBBoxBlocks = 152;
+constexpr int kBBoxBlocks = 608;  // 4 per SM: enough loads in flight to reach HBM rate
+
+// bbox_blocks(n): blocks of a plain launch, every thread reading at least 4 particle pairs
+inline int bbox_blocks(uint64_t n) {
+    const uint64_t b = (n / 2 + kBBoxThreads * 4 - 1) / (kBBoxThreads * 4);
+    return (int)(b < 1 ? 1 : b > (uint64_t)kBBoxBlocks ? kBBoxBlocks : b);
+}
 
 __device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ pos, uint32_t n,
                                           float* __restrict__ part, uint32_t* __restrict__ ticket,
@@ -97,12 +103,14 @@ __device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ po
     __shared__ float s[4][kBBoxThreads / 32];
     __shared__ bool last;
     float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
-    for (uint32_t i = blk.id * kBBoxThreads + threadIdx.x; i < n; i += blk.count * kBBoxThreads) {
-        float2 p = pos[i];
-        mnx = fminf(mnx, p.x);
-        mxx = fmaxf(mxx, p.x);
-        mny = fminf(mny, p.y);
-        mxy = fmaxf(mxy, p.y);
+    // n is a multiple of 64: two particles per 16-byte load
+    const float4* __restrict__ pos2 = reinterpret_cast<const float4*>(pos);
+    for (uint32_t i = blk.id * kBBoxThreads + threadIdx.x; i < n / 2; i += blk.count * kBBoxThreads) {
+        const float4 p = pos2[i];
+        mnx = fminf(mnx, fminf(p.x, p.z));
+        mxx = fmaxf(mxx, fmaxf(p.x, p.z));
+        mny = fminf(mny, fminf(p.y, p.w));
+        mxy = fmaxf(mxy, fmaxf(p.y, p.w));
     }
     for (int o = 16; o; o >>= 1) {
         mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
@@ -904,18 +912,21 @@ k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, 
 }
 
 // ------------------------------------------------------------------------------------
-// accurate-mode traversal (no counterpart in the reference): the 32 particles of a warp
-// share one walk; 32 records are tested at once (one per lane) against the bounding box
-// of the group; accepted records and runs of particle leaves become interaction items;
-// all lanes then sum the items as a dense stream (quadrupole term for nodes).
+// accurate-mode traversal (no counterpart in the reference): the 64 particles of 64
+// consecutive sorted slots share one walk, run by one warp (two particles per lane); 32
+// records are tested at once (one per lane) against the bounding boxes of the group;
+// accepted nodes and runs of particle leaves are collected and every lane then sums them
+// for its two particles with packed f32x2 instructions (quadrupole term for nodes).
 // ------------------------------------------------------------------------------------
 constexpr int kGroupWarps = 4;
+constexpr int kGroupSize = 64;  // particles per walk
 // Records still to test.  Pops take the top 32 and push at most four internal children
 // each, one level deeper, so the stack holds at most one block of <= 128 entries per level
 // and blocks of strictly increasing level: <= 96 * D + 128 = 1568 for D = 15 (a full
 // four-way tree reaches 1216).  Overflow is still checked and reported.
 constexpr int kStackCap = 1600;
-constexpr int kItemCap = 128;     // interaction items between evaluations
+constexpr int kItemCap = 128;     // runs of particle leaves between evaluations
+constexpr int kNodeCap = 96;      // accepted nodes between evaluations
 
 // 1/sqrt: correctly rounded (REFERENCE math) or the hardware approximation (FAST math;
 // d2 >= eps^2 > 0 is never subnormal, so the flush-to-zero form loses nothing)
@@ -990,112 +1001,63 @@ __device__ __forceinline__ void quadrupole(float4 q, float4 m2, float px, float 
     ay = fmaf(-t3, sry, fmaf(dy, coef, ay));
 }
 
-// Evaluation order.  Accepted nodes and particle leaves are summed separately, each in
-// walk order: the k-th node of the walk goes into node accumulator k mod 2, the k-th
-// leaf into leaf accumulator k mod 2, and a particle's acceleration is
-// (node0 + node1) + (leaf0 + leaf1).  How the warp batches its evaluations therefore does
-// not change a bit of the result.
-//
-// A chunk of up to 32 gathered records is staged as structure of arrays, record j at
-// position p = j + (r & 1) (r = records of its kind summed before the chunk): positions
-// (2t, 2t+1) go to accumulators (0, 1) and load as one aligned float2 each -- already
-// the operand pair of an f32x2 instruction.
-constexpr int kChunkSlots = 34;  // 32 records + the parity shift, rounded to a pair
-constexpr int kNodeCap = 96;     // accepted nodes between evaluations
+// Evaluation order.  Each particle sums the accepted nodes and the particle leaves of its
+// walk separately, each in walk order, into a node and a leaf accumulator; its
+// acceleration is node + leaf.  How the warp batches its evaluations therefore does not
+// change a bit of the result.
 struct GroupSmem {
     uint32_t stack[kStackCap];
     uint32_t node[kNodeCap];      // accepted node records
     uint32_t it_start[kItemCap];  // runs of particle leaves: first record
     uint32_t it_count[kItemCap];  // record count
     uint32_t off[kItemCap];       // exclusive record offsets of the runs
-    alignas(8) float cx[kChunkSlots];  // centre of mass (or particle position), mass
-    alignas(8) float cy[kChunkSlots];
-    alignas(8) float cm[kChunkSlots];
-    alignas(8) float qxx[kChunkSlots];  // second moments of node records
-    alignas(8) float qxy[kChunkSlots];
-    alignas(8) float qyy[kChunkSlots];
+    float cx[32], cy[32], cm[32];     // one chunk of gathered records: centre of mass (or particle), mass
+    float qxx[32], qxy[32], qyy[32];  // second moments of node records
 };
 
-__device__ __forceinline__ float2 ld_pair(const float* a, uint32_t p) { return *reinterpret_cast<const float2*>(a + p); }
-
-// The record at position p into accumulator p & 1 of (ax, ay).
-template <bool EXACT, bool QUAD>
-__device__ __forceinline__ void eval_slot(const GroupSmem& g, uint32_t p, float px, float py, float eps2,
-                                          float2& acx, float2& acy) {
-    const float4 q = make_float4(g.cx[p], g.cy[p], g.cm[p], 0.0f);
-    float ax = (p & 1u) ? acx.y : acx.x, ay = (p & 1u) ? acy.y : acy.x;
-    if (QUAD) quadrupole<EXACT>(q, make_float4(g.qxx[p], g.qxy[p], g.qyy[p], 0.0f), px, py, eps2, ax, ay);
-    else monopole<EXACT>(q, px, py, eps2, ax, ay);
-    if (p & 1u) {
-        acx.y = ax;
-        acy.y = ay;
-    } else {
-        acx.x = ax;
-        acy.x = ay;
-    }
-}
-
-// Positions p (accumulator 0) and p + 1 (accumulator 1), p even, as monopoles.
+// One record (x, y, m) on the lane's two particles (P = their x, Q = their y): the
+// operation sequence of `monopole`, two particles at once.
 template <bool EXACT>
-__device__ __forceinline__ void monopole_pair(const GroupSmem& g, uint32_t p, float2 P, float2 Q, float2 E2,
-                                              float2& acx, float2& acy) {
-    const float2 dx = sub2(ld_pair(g.cx, p), P), dy = sub2(ld_pair(g.cy, p), Q);
+__device__ __forceinline__ void monopole_x2(float x, float y, float m, float2 P, float2 Q, float2 E2, float2& acx,
+                                            float2& acy) {
+    const float2 dx = sub2(make_float2(x, x), P), dy = sub2(make_float2(y, y), Q);
     const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
     const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
-    const float2 sc = mul2(mul2(mul2(ld_pair(g.cm, p), r), r), r);
+    const float2 sc = mul2(mul2(mul2(make_float2(m, m), r), r), r);
     acx = fma2(dx, sc, acx);
     acy = fma2(dy, sc, acy);
 }
 
-// Positions p and p + 1, both nodes with second moments (the operation sequence of
-// `quadrupole`, two lanes at once).
+// One node with second moments on the lane's two particles: the operation sequence of
+// `quadrupole` (the particle-independent T and -1.5 T once per record).
 template <bool EXACT>
-__device__ __forceinline__ void quadrupole_pair(const GroupSmem& g, uint32_t p, float2 P, float2 Q, float2 E2,
-                                                float2& acx, float2& acy) {
-    const float2 dx = sub2(ld_pair(g.cx, p), P), dy = sub2(ld_pair(g.cy, p), Q);
+__device__ __forceinline__ void quadrupole_x2(float x, float y, float m, float sxx, float sxy, float syy, float2 P,
+                                              float2 Q, float2 E2, float2& acx, float2& acy) {
+    const float2 dx = sub2(make_float2(x, x), P), dy = sub2(make_float2(y, y), Q);
     const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
     const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
     const float2 r2 = mul2(r, r);
     const float2 r3 = mul2(r2, r);
     const float2 r5 = mul2(r3, r2);
     const float2 r7 = mul2(r5, r2);
-    const float2 sxx = ld_pair(g.qxx, p), sxy = ld_pair(g.qxy, p), syy = ld_pair(g.qyy, p);
-    const float2 srx = fma2(sxx, dx, mul2(sxy, dy));
-    const float2 sry = fma2(sxy, dx, mul2(syy, dy));
+    const float2 Sxx = make_float2(sxx, sxx), Sxy = make_float2(sxy, sxy), Syy = make_float2(syy, syy);
+    const float2 srx = fma2(Sxx, dx, mul2(Sxy, dy));
+    const float2 sry = fma2(Sxy, dx, mul2(Syy, dy));
     const float2 u = fma2(dx, srx, mul2(dy, sry));
-    const float2 T = add2(sxx, syy);
+    const float mt = -1.5f * (sxx + syy);
     const float2 coef = fma2(mul2(make_float2(7.5f, 7.5f), u), r7,
-                             fma2(mul2(make_float2(-1.5f, -1.5f), T), r5, mul2(ld_pair(g.cm, p), r3)));
+                             fma2(make_float2(mt, mt), r5, mul2(make_float2(m, m), r3)));
     const float2 nt3 = mul2(make_float2(-3.0f, -3.0f), r5);
     acx = fma2(nt3, srx, fma2(dx, coef, acx));
     acy = fma2(nt3, sry, fma2(dy, coef, acy));
 }
 
-// Sum the staged chunk of m records shifted by sh into (acx, acy).
-template <bool EXACT, bool QUAD>
-__device__ __forceinline__ void eval_chunk(const GroupSmem& g, uint32_t sh, uint32_t m, float px, float py,
-                                           float eps2, float2& acx, float2& acy) {
-    const float2 P = make_float2(px, px), Q = make_float2(py, py), E2 = make_float2(eps2, eps2);
-    uint32_t p = sh;
-    const uint32_t end = sh + m;
-    if (p & 1u) {  // odd running index: the first record goes alone into accumulator 1
-        eval_slot<EXACT, QUAD>(g, p, px, py, eps2, acx, acy);
-        ++p;
-    }
-#pragma unroll 2
-    for (; p + 1 < end; p += 2) {
-        if (QUAD) quadrupole_pair<EXACT>(g, p, P, Q, E2, acx, acy);
-        else monopole_pair<EXACT>(g, p, P, Q, E2, acx, acy);
-    }
-    if (p < end) eval_slot<EXACT, QUAD>(g, p, px, py, eps2, acx, acy);
-}
-
-// Sum the count accepted nodes (quadrupole term with QUAD), 32 at a time: lane l loads
-// node l of the next chunk while the current one is summed.
+// Sum the count accepted nodes (quadrupole term with QUAD) for the lane's two particles,
+// 32 at a time: lane l loads node l of the next chunk while the current one is summed.
 template <bool EXACT, bool QUAD>
 __device__ __forceinline__ void eval_nodes(GroupSmem& g, uint32_t count, const float4* __restrict__ rec,
-                                           const float4* __restrict__ quad, float px, float py, float eps2,
-                                           float2& acx, float2& acy, uint32_t& rn, int lane) {
+                                           const float4* __restrict__ quad, float2 P, float2 Q, float2 E2,
+                                           float2& acx, float2& acy, int lane) {
     if (!count) return;
     float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qq = q;
     if ((uint32_t)lane < count) {
@@ -1105,14 +1067,13 @@ __device__ __forceinline__ void eval_nodes(GroupSmem& g, uint32_t count, const f
     }
     for (uint32_t f0 = 0; f0 < count; f0 += 32) {
         const uint32_t m = min(count - f0, 32u);
-        const uint32_t sh = rn & 1u;
-        g.cx[lane + sh] = q.x;
-        g.cy[lane + sh] = q.y;
-        g.cm[lane + sh] = q.z;
+        g.cx[lane] = q.x;
+        g.cy[lane] = q.y;
+        g.cm[lane] = q.z;
         if (QUAD) {
-            g.qxx[lane + sh] = qq.x;
-            g.qxy[lane + sh] = qq.y;
-            g.qyy[lane + sh] = qq.z;
+            g.qxx[lane] = qq.x;
+            g.qxy[lane] = qq.y;
+            g.qyy[lane] = qq.z;
         }
         __syncwarp();
         const uint32_t fn = f0 + 32 + lane;
@@ -1121,8 +1082,13 @@ __device__ __forceinline__ void eval_nodes(GroupSmem& g, uint32_t count, const f
             q = __ldg(&rec[r]);
             if (QUAD) qq = __ldg(&quad[r]);
         }
-        eval_chunk<EXACT, QUAD>(g, sh, m, px, py, eps2, acx, acy);
-        rn += m;
+#pragma unroll 4
+        for (uint32_t j = 0; j < m; ++j) {
+            if (QUAD)
+                quadrupole_x2<EXACT>(g.cx[j], g.cy[j], g.cm[j], g.qxx[j], g.qxy[j], g.qyy[j], P, Q, E2, acx, acy);
+            else
+                monopole_x2<EXACT>(g.cx[j], g.cy[j], g.cm[j], P, Q, E2, acx, acy);
+        }
         __syncwarp();
     }
 }
@@ -1142,8 +1108,7 @@ __device__ __forceinline__ float4 gather_leaf(const GroupSmem& g, uint32_t n_ite
 // Sum the particle leaves of the n_items runs as monopoles, 32 records at a time.
 template <bool EXACT>
 __device__ __forceinline__ void eval_leaves(GroupSmem& g, uint32_t n_items, const float4* __restrict__ rec,
-                                            float px, float py, float eps2, float2& acx, float2& acy, uint32_t& rl,
-                                            int lane) {
+                                            float2 P, float2 Q, float2 E2, float2& acx, float2& acy, int lane) {
     if (!n_items) return;
     // exclusive record offsets of all runs: lane l owns runs [4l, 4l + 4)
     uint32_t c4[kItemCap / 32], sum = 0;
@@ -1170,15 +1135,14 @@ __device__ __forceinline__ void eval_leaves(GroupSmem& g, uint32_t n_items, cons
     if ((uint32_t)lane < total) q = gather_leaf(g, n_items, lane, rec);
     for (uint32_t f0 = 0; f0 < total; f0 += 32) {
         const uint32_t m = min(total - f0, 32u);
-        const uint32_t sh = rl & 1u;
-        g.cx[lane + sh] = q.x;
-        g.cy[lane + sh] = q.y;
-        g.cm[lane + sh] = q.z;
+        g.cx[lane] = q.x;
+        g.cy[lane] = q.y;
+        g.cm[lane] = q.z;
         __syncwarp();
         const uint32_t fn = f0 + 32 + lane;
         if (fn < total) q = gather_leaf(g, n_items, fn, rec);
-        eval_chunk<EXACT, false>(g, sh, m, px, py, eps2, acx, acy);
-        rl += m;
+#pragma unroll 4
+        for (uint32_t j = 0; j < m; ++j) monopole_x2<EXACT>(g.cx[j], g.cy[j], g.cm[j], P, Q, E2, acx, acy);
         __syncwarp();
     }
 }
@@ -1195,23 +1159,29 @@ __device__ __forceinline__ void force_group_body(
     const uint32_t group = blk.id * kGroupWarps + warp;
     const uint32_t nv = counts[0];
     const uint32_t T = min(nv + counts[1], cap);
-    if (group * 32 >= nv || T == 0) return;
-    const uint32_t s = group * 32 + lane;
-    const uint32_t i = s < nv ? sidx[s] : 0u;
-    const bool valid = s < nv && i < n_al;
-    const float2 p = valid ? pos_in[i] : make_float2(0.0f, 0.0f);
+    const uint32_t g0 = group * kGroupSize;
+    if (g0 >= nv || T == 0) return;
+    // particles: slot g0 + lane (.x of every pair) and g0 + 32 + lane (.y)
+    const uint32_t s0 = g0 + lane, s1 = s0 + 32;
+    const uint32_t i0 = s0 < nv ? sidx[s0] : 0u, i1 = s1 < nv ? sidx[s1] : 0u;
+    const bool v0 = s0 < nv && i0 < n_al, v1 = s1 < nv && i1 < n_al;  // i < n_al unless the sort failed
+    const float2 p0 = v0 ? pos_in[i0] : make_float2(0.0f, 0.0f);
+    const float2 p1 = v1 ? pos_in[i1] : make_float2(0.0f, 0.0f);
     // Sub-boxes: the particles are split by their cell at the coarsest level where the
     // first and last keys of the group differ, so a group that crosses a coarse Morton
     // boundary is not given one box spanning the empty space between its ends.
-    const uint32_t kf = skey[group * 32], kl = skey[min(group * 32 + 31, nv - 1)];
+    const uint32_t kf = skey[g0], kl = skey[min(g0 + kGroupSize - 1, nv - 1)];
     const int shift = kf == kl ? -1 : ((31 - __clz(kf ^ kl)) & ~1);
-    const int my_box = !valid ? -1 : (shift < 0 ? 0 : (int)((skey[s] >> shift) & 3u));
+    const int box0 = !v0 ? -1 : (shift < 0 ? 0 : (int)((skey[s0] >> shift) & 3u));
+    const int box1 = !v1 ? -1 : (shift < 0 ? 0 : (int)((skey[s1] >> shift) & 3u));
     float bx0[4], bx1[4], by0[4], by1[4];
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        const bool in = my_box == b;
-        float x0 = in ? p.x : INFINITY, x1 = in ? p.x : -INFINITY;
-        float y0 = in ? p.y : INFINITY, y1 = in ? p.y : -INFINITY;
+        const bool in0 = box0 == b, in1 = box1 == b;
+        float x0 = fminf(in0 ? p0.x : INFINITY, in1 ? p1.x : INFINITY);
+        float x1 = fmaxf(in0 ? p0.x : -INFINITY, in1 ? p1.x : -INFINITY);
+        float y0 = fminf(in0 ? p0.y : INFINITY, in1 ? p1.y : INFINITY);
+        float y1 = fmaxf(in0 ? p0.y : -INFINITY, in1 ? p1.y : -INFINITY);
         for (int o = 16; o; o >>= 1) {
             x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
             x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
@@ -1223,9 +1193,9 @@ __device__ __forceinline__ void force_group_body(
         by0[b] = y0;
         by1[b] = y1;
     }
-    // node accumulators {0, 1} and leaf accumulators {0, 1}, x and y
+    const float2 P = make_float2(p0.x, p1.x), Q = make_float2(p0.y, p1.y), E2 = make_float2(eps2, eps2);
+    // node and leaf accumulators of the two particles (.x particle 0, .y particle 1)
     float2 anx = make_float2(0.0f, 0.0f), any = anx, alx = anx, aly = anx;
-    uint32_t rn = 0, rl = 0;  // nodes / leaves summed so far
     unsigned long long n_int = 0, n_test = 0, n_node = 0;
     uint32_t size = 0, n_nodes = 0, n_items = 0;
     if (skip[0] == 1u) {  // a single particle: the root is its leaf
@@ -1242,11 +1212,11 @@ __device__ __forceinline__ void force_group_body(
 
     while (size > 0) {
         if (n_nodes > (uint32_t)(kNodeCap - 32)) {
-            eval_nodes<EXACT, QUAD>(g, n_nodes, rec, quad, p.x, p.y, eps2, anx, any, rn, lane);
+            eval_nodes<EXACT, QUAD>(g, n_nodes, rec, quad, P, Q, E2, anx, any, lane);
             n_nodes = 0;
         }
         if (n_items > (uint32_t)(kItemCap - 64)) {
-            eval_leaves<EXACT>(g, n_items, rec, p.x, p.y, eps2, alx, aly, rl, lane);
+            eval_leaves<EXACT>(g, n_items, rec, P, Q, E2, alx, aly, lane);
             n_items = 0;
         }
         const uint32_t np = min(size, 32u);
@@ -1337,28 +1307,36 @@ __device__ __forceinline__ void force_group_body(
         size += ptot;
         __syncwarp();
     }
-    eval_nodes<EXACT, QUAD>(g, n_nodes, rec, quad, p.x, p.y, eps2, anx, any, rn, lane);
-    eval_leaves<EXACT>(g, n_items, rec, p.x, p.y, eps2, alx, aly, rl, lane);
+    eval_nodes<EXACT, QUAD>(g, n_nodes, rec, quad, P, Q, E2, anx, any, lane);
+    eval_leaves<EXACT>(g, n_items, rec, P, Q, E2, alx, aly, lane);
     if (COUNT) {
         if (skip[0] == 1u && lane == 0) n_int += 1;
         for (int o = 16; o; o >>= 1) {
             n_int += __shfl_xor_sync(0xffffffffu, n_int, o);
             n_node += __shfl_xor_sync(0xffffffffu, n_node, o);
         }
-        const unsigned long long nval = __popc(__ballot_sync(0xffffffffu, valid));
+        const unsigned long long nval = __popc(__ballot_sync(0xffffffffu, v0)) + __popc(__ballot_sync(0xffffffffu, v1));
         if (lane == 0) {
             atomicAdd(&stat[0], n_int * nval);
             atomicAdd(&stat[1], n_test);
             atomicAdd(&stat[2], n_node * nval);
         }
     }
-    if (!valid) return;
-    const float ax = (anx.x + anx.y) + (alx.x + alx.y), ay = (any.x + any.y) + (aly.x + aly.y);
-    if (acc_rec) acc_rec[i] = make_float2(ax, ay);
-    const float2 v = vel_in[i];
-    const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);
-    pos_out[i] = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
-    vel_out[i] = make_float2(nvx, nvy);
+    const float2 ax = add2(anx, alx), ay = add2(any, aly);  // node + leaf, per particle
+    if (v0) {
+        if (acc_rec) acc_rec[i0] = make_float2(ax.x, ay.x);
+        const float2 v = vel_in[i0];
+        const float nvx = fmaf(ax.x, k, v.x), nvy = fmaf(ay.x, k, v.y);
+        pos_out[i0] = make_float2(fmaf(v.x + nvx, hdt, p0.x), fmaf(v.y + nvy, hdt, p0.y));
+        vel_out[i0] = make_float2(nvx, nvy);
+    }
+    if (v1) {
+        if (acc_rec) acc_rec[i1] = make_float2(ax.y, ay.y);
+        const float2 v = vel_in[i1];
+        const float nvx = fmaf(ax.y, k, v.x), nvy = fmaf(ay.y, k, v.y);
+        pos_out[i1] = make_float2(fmaf(v.x + nvx, hdt, p1.x), fmaf(v.y + nvy, hdt, p1.y));
+        vel_out[i1] = make_float2(nvx, nvy);
+    }
 }
 
 template <bool EXACT, bool QUAD, bool COUNT>
@@ -1464,7 +1442,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     uint32_t* ctr = w.counters;
     if (bbox) {
         stage_begin(s, kStageBBox, profile);
-        k_bbox<<<kBBoxBlocks, kBBoxThreads, 0, st>>>(s->pos[in], n, w.bbox_part, ctr + kCtrBBox, w.params);
+        k_bbox<<<bbox_blocks(n), kBBoxThreads, 0, st>>>(s->pos[in], n, w.bbox_part, ctr + kCtrBBox, w.params);
         count_launch(s);
         stage_end(s, kStageBBox, profile);
     }
@@ -1539,7 +1517,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
                                                          s->vel[in], s->pos[out], s->vel[out], s->acc, n, s->eps2, \
                                                          s->theta2, k, hdt, (uint32_t)w.cap, stat)
 #define GS_GROUP(E_, Q_, C_)                                                                                    \
-    k_force_group<E_, Q_, C_><<<(int)((n / 32 + kGroupWarps - 1) / kGroupWarps), kGroupWarps * 32, 0, st>>>(    \
+    k_force_group<E_, Q_, C_><<<(int)((n / kGroupSize + kGroupWarps - 1) / kGroupWarps), kGroupWarps * 32, 0, st>>>( \
         sidx, skey, ctr + kCtrValid, w.rec, w.skip, w.quad, w.kids, s->pos[in], s->vel[in], s->pos[out],             \
         s->vel[out],                                                                                                 \
         s->acc, n,                                                                                                   \
@@ -1847,15 +1825,15 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
     uint64_t cb = (d.zero_words + 1023) / 1024;
     blocks[kTabClear] = (uint32_t)(cb < 1 ? 1 : cb > 64 ? 64 : cb);
     if (d.bbox) {
-        uint64_t bb = (n + kBBoxThreads - 1) / kBBoxThreads;
-        blocks[kTabBBox] = (uint32_t)(bb > (uint64_t)kBBoxBlocks ? kBBoxBlocks : bb);
+        blocks[kTabBBox] = (uint32_t)bbox_blocks(n);
     }
     blocks[kTabGrid] = (uint32_t)grid_for(n, 256);
     blocks[kTabSort] = w.sort_tiles;
     blocks[kTabScan] = w.scan_tiles;
     blocks[kTabOne] = 1;
-    const int warps = (s->p.flags & GS_FLAG_GROUP_WALK) ? kGroupWarps : kForceWarps;
-    blocks[kTabForce] = (uint32_t)((n / 32 + warps - 1) / warps);
+    const uint64_t per_block = (s->p.flags & GS_FLAG_GROUP_WALK) ? (uint64_t)kGroupWarps * kGroupSize
+                                                                   : (uint64_t)kForceWarps * 32;
+    blocks[kTabForce] = (uint32_t)((n + per_block - 1) / per_block);
 }
 
 int bh_batch_force_grid(const BatchPlan& p) {

@@ -339,7 +339,7 @@ typedef struct {
     int group_walk;         /* ORC_BH_GROUP_WALK semantics */
     uint32_t* max_stack;    /* per worker */
     uint64_t* max_inter;    /* per worker: largest per-warp interaction count */
-    uint32_t group_size;    /* particles per group walk (32, or 64 with ORC_BH_GROUP64) */
+    uint32_t group_size;    /* particles per group walk (64) */
 } walk_ctx;
 
 static void walk_warp(void* p, uint64_t item, int worker) {
@@ -406,7 +406,7 @@ static void walk_warp(void* p, uint64_t item, int worker) {
     c->visits[worker] += visits;
 }
 
-/* Accurate-mode walk (ORC_BH_GROUP_WALK), for the 32 consecutive sorted slots of one warp:
+/* Accurate-mode walk (ORC_BH_GROUP_WALK), for the 64 consecutive sorted slots of one group:
  *   - the group is cut into at most four sub-boxes: the particles are split by their
  *     cell at the coarsest level where the first and last cell keys of the group differ
  *     (so a group that crosses a coarse Morton boundary does not get one box spanning
@@ -421,17 +421,17 @@ static void walk_warp(void* p, uint64_t item, int worker) {
  *     children into one range item;
  *   - lanes are handled in order, so items and pushes are in lane order;
  *   - every particle of the group sums the accepted nodes (quadrupole term) and the
- *     particle leaves (monopoles) separately, each in walk order: the k-th node goes into
- *     node accumulator k mod 2, the k-th leaf into leaf accumulator k mod 2, and the
- *     acceleration is (node0 + node1) + (leaf0 + leaf1); then it is integrated.
+ *     particle leaves (monopoles) separately, each in walk order, into a node and a leaf
+ *     accumulator; its acceleration is node + leaf; then it is integrated.
  * The CUDA kernel (bh.cu, force_group_body) batches its evaluations differently; with
  * this accumulation rule the batching changes no bit. */
+#define GROUP_SIZE 64
 #define GROUP_STACK_CAP 2048
 #define GMAX 64
 static void group_walk_warp(void* p, uint64_t item, int worker) {
     const walk_ctx* c = (const walk_ctx*)p;
     const uint64_t w = item * c->stride;
-    float px[GMAX], py[GMAX], ax[GMAX][4], ay[GMAX][4]; /* node 0, node 1, leaf 0, leaf 1 */
+    float px[GMAX], py[GMAX], ax[GMAX][2], ay[GMAX][2]; /* node, leaf */
     int valid[GMAX];
     const uint32_t G = c->group_size;
     int nvalid = 0;
@@ -446,7 +446,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
         valid[l] = i != c->n_al;
         px[l] = valid[l] ? c->pos_in[2 * i] : 0.0f;
         py[l] = valid[l] ? c->pos_in[2 * i + 1] : 0.0f;
-        for (int a = 0; a < 4; ++a) ax[l][a] = ay[l][a] = 0.0f;
+        ax[l][0] = ay[l][0] = ax[l][1] = ay[l][1] = 0.0f;
         nvalid += valid[l];
     }
     if (!nvalid || !c->tree_size) return;
@@ -464,7 +464,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
     uint32_t stack[GROUP_STACK_CAP + 160];
     uint32_t size = 1, max_size = 1;
     stack[0] = 0;
-    uint64_t inter = 0, visits = 0, rn = 0, rl = 0; /* running node / leaf index of the warp */
+    uint64_t inter = 0, visits = 0;
     while (size) {
         uint32_t np = size < WARP ? size : WARP;
         uint32_t base = size - np;
@@ -488,7 +488,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
             }
             if (accept) { /* one item: the record itself (a leaf only when the root is one) */
                 const float nx = c->npos[2 * n], ny = c->npos[2 * n + 1], nm = c->nmass[n];
-                const int a = sk > 1 ? (int)(rn & 1u) : 2 + (int)(rl & 1u);
+                const int a = sk > 1 ? 0 : 1;
                 for (uint32_t l = 0; l < G; ++l) {
                     if (!valid[l]) continue;
                     float dx = nx - px[l], dy = ny - py[l];
@@ -502,8 +502,6 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                         ay[l][a] = fmaf(dy, sc, ay[l][a]);
                     }
                 }
-                if (sk > 1) ++rn;
-                else ++rl;
                 inter += (uint64_t)nvalid;
                 continue;
             }
@@ -515,7 +513,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                     while (r < end && c->skip[r] == 1) ++r;
                     for (uint32_t q = ch; q < r; ++q) {
                         const float nx = c->npos[2 * q], ny = c->npos[2 * q + 1], nm = c->nmass[q];
-                        const int a = 2 + (int)(rl & 1u);
+                        const int a = 1;
                         for (uint32_t l = 0; l < G; ++l) {
                             if (!valid[l]) continue;
                             float dx = nx - px[l], dy = ny - py[l];
@@ -523,7 +521,6 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                             ax[l][a] = fmaf(dx, sc, ax[l][a]);
                             ay[l][a] = fmaf(dy, sc, ay[l][a]);
                         }
-                        ++rl;
                     }
                     inter += (uint64_t)nvalid * (r - ch);
                     ch = r;
@@ -541,8 +538,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
         if (!valid[l]) continue;
         uint32_t i = c->src[(uint32_t)w * G + l];
         float vx = c->vel_in[2 * i], vy = c->vel_in[2 * i + 1];
-        const float axl = (ax[l][0] + ax[l][1]) + (ax[l][2] + ax[l][3]);
-        const float ayl = (ay[l][0] + ay[l][1]) + (ay[l][2] + ay[l][3]);
+        const float axl = ax[l][0] + ax[l][1], ayl = ay[l][0] + ay[l][1];
         float nvx = fmaf(axl, c->k, vx), nvy = fmaf(ayl, c->k, vy);
         c->pos_out[2 * i] = fmaf(vx + nvx, c->hdt, px[l]);
         c->pos_out[2 * i + 1] = fmaf(vy + nvy, c->hdt, py[l]);
@@ -1032,7 +1028,7 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
     wc.quad = quad;
     wc.group_walk = (flags & ORC_BH_GROUP_WALK) != 0;
     wc.skey = skey;
-    wc.group_size = (flags & ORC_BH_GROUP64) ? 64 : 32;
+    wc.group_size = GROUP_SIZE;
     wc.tree_size = tree_size;
     wc.src = src;
     wc.n_al = n_al;

@@ -105,8 +105,7 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
  *                       the particle is never accepted for theta <= 1 */
 #define ORC_BH_QUADRUPOLE 1
 #define ORC_BH_SAFE_RADIUS 2
-#define ORC_BH_GROUP_WALK 4  /* box-tested 32-wide stack walk, see group_walk_warp */
-#define ORC_BH_GROUP64 8     /* group walk over 64 consecutive particles instead of 32 */
+#define ORC_BH_GROUP_WALK 4  /* box-tested stack walk shared by 64 particles, see group_walk_warp */
 int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in, float* vel_in,
                           float* mass_in, float* pos_out, float* vel_out, float* mass_out,
                           float dt, float G, float eps2, float theta2, orc_bh_out* out,
