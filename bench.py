@@ -165,10 +165,23 @@ def interaction_counts(gsim, wl, pos, vel, mass, local):
                 "node_interactions": int(st.node_interactions)}
 
 
+def stage_times(gsim, wl, pos, vel, mass, local, steps):
+    """Per-stage milliseconds per step from a separate run with GS_FLAG_PROFILE (stage
+    events inside the step graph; they also turn the overlapped launches off, so the
+    timed run does not use this flag)."""
+    with gsim.Simulation(pos, vel, mass, params=make_params(gsim, wl, local, gsim.FLAG_PROFILE)) as ps:
+        ps.run(3)
+        ps.sync()
+        ps.reset_stats()
+        ps.run(steps)
+        ps.sync()
+        st = ps.stats()
+        return {nm: st.stage_ms[i] / st.stage_launches[i] for i, nm in enumerate(gsim.STAGES) if st.stage_launches[i]}
+
+
 def measure(gsim, torch, wl, pos, vel, mass, args, local, dist, sample_clocks):
-    """Device-timed steps with an L2 flush before each; per-stage times from the
-    library's CUDA events recorded inside its step graph."""
-    sim = gsim.Simulation(pos, vel, mass, params=make_params(gsim, wl, local, gsim.FLAG_PROFILE))
+    """Device-timed steps with an L2 flush before each (the state stays resident)."""
+    sim = gsim.Simulation(pos, vel, mass, params=make_params(gsim, wl, local, 0))
     stream = torch.cuda.ExternalStream(sim.stream(), device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     sim.run(args.warmup)
@@ -195,8 +208,7 @@ def measure(gsim, torch, wl, pos, vel, mass, args, local, dist, sample_clocks):
     st = sim.stats()
     dev_ms = float(sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
     out = {"dev_ms": dev_ms, "launches": int(st.kernel_launches - launches0), "clocks": clk, "sim": sim,
-           "stage_ms": {nm: st.stage_ms[i] / st.stage_launches[i] for i, nm in enumerate(gsim.STAGES)
-                        if st.stage_launches[i]}}
+           "stage_ms": stage_times(gsim, wl, pos, vel, mass, local, max(3, args.steps))}
     out.update(interaction_counts(gsim, wl, pos, vel, mass, local))
     return out
 

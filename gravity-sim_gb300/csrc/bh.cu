@@ -44,6 +44,16 @@ struct Blk {
 };
 __device__ __forceinline__ Blk grid_blk() { return Blk{blockIdx.x, gridDim.x}; }
 
+// Programmatic dependent launch: every step kernel lets the next launch in its stream
+// start as soon as all of its blocks have begun, then waits until the kernel before it
+// has finished and its writes are visible.  Each kernel therefore still runs strictly
+// after its predecessor (and transitively after all earlier ones); only the launch
+// latency between them is hidden.  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // ------------------------------------------------------------------------------------
 // keys
 // ------------------------------------------------------------------------------------
@@ -194,6 +204,7 @@ __device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ po
 __global__ void __launch_bounds__(kBBoxThreads)
 k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uint32_t* __restrict__ ticket,
        BHParams* __restrict__ out) {
+    pdl_enter();
     bbox_body(grid_blk(), pos, n, part, ticket, out);
 }
 
@@ -245,6 +256,7 @@ __global__ void __launch_bounds__(kKeyThreads)
 k_keygen(int bbox_mode, const BHParams* __restrict__ bp, float2* __restrict__ pos_in, float* mass_in,
          float2* __restrict__ pos_out, float* mass_out, uint32_t n, uint32_t* __restrict__ keys,
          uint32_t* __restrict__ hist, int passes, uint32_t* __restrict__ valid_count) {
+    pdl_enter();
     keygen_body(grid_blk(), bbox_mode, bp, pos_in, mass_in, pos_out, mass_out, n, keys, hist, passes, valid_count);
 }
 
@@ -396,6 +408,7 @@ __global__ void __launch_bounds__(kSortThreads)
 k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
             uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
             uint32_t* __restrict__ status, uint32_t* __restrict__ ticket, int* __restrict__ err) {
+    pdl_enter();
     sort_pass_body<IDENTITY>(kin, vin, kout, vout, n, shift, hist, status, ticket, err);
 }
 
@@ -469,6 +482,7 @@ __global__ void __launch_bounds__(kScanThreads)
 k_meta_scan(const uint32_t* __restrict__ skey, uint32_t n_items, const uint32_t* __restrict__ valid_count,
             int D, uint32_t* __restrict__ E, uint32_t* __restrict__ status, uint32_t* __restrict__ ticket,
             uint32_t* __restrict__ internal_count, int* __restrict__ err) {
+    pdl_enter();
     meta_scan_body(skey, n_items, valid_count, D, E, status, ticket, internal_count, err);
 }
 
@@ -542,6 +556,7 @@ k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, 
           const uint32_t* __restrict__ valid_count, int D, const float2* __restrict__ pos,
           const float* __restrict__ mass, float4* __restrict__ rec, uint32_t* __restrict__ skip,
           uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al, int* __restrict__ err) {
+    pdl_enter();
     records_body(grid_blk(), skey, sidx, E, valid_count, D, pos, mass, rec, skip, node_slot, cap, n_al, err);
 }
 
@@ -628,6 +643,7 @@ k_nodes(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E, const
         uint32_t* __restrict__ skip, uint4* __restrict__ kids, uint2* __restrict__ nodeinfo,
         uint32_t* __restrict__ level_count, uint32_t* __restrict__ levels, uint32_t n_al, uint64_t cap,
         int* __restrict__ err) {
+    pdl_enter();
     nodes_body(grid_blk(), skey, E, counts, D, bp, node_slot, rec, skip, kids, nodeinfo, level_count, levels, n_al,
                cap, err);
 }
@@ -819,6 +835,7 @@ k_level_sums(int d, const uint32_t* __restrict__ level_count, const uint32_t* __
              const uint32_t* __restrict__ skey, int D, float4* rec, const uint4* __restrict__ kids,
              const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
              const BHParams* __restrict__ bpp) {
+    pdl_enter();
     level_sums_body<QUAD>(grid_blk(), d, level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, quad, safe,
                           bbox_mode, bpp);
 }
@@ -829,6 +846,7 @@ k_top_sums(const uint32_t* __restrict__ level_count, const uint32_t* __restrict_
            const uint32_t* __restrict__ skey, int D, float4* rec, const uint4* __restrict__ kids,
            const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
            const BHParams* __restrict__ bpp) {
+    pdl_enter();
     top_sums_body<QUAD>(level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, quad, safe, bbox_mode, bpp);
 }
 
@@ -907,6 +925,7 @@ k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, 
         const uint32_t* __restrict__ skip, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
         float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
         float eps2, float theta2, float k, float hdt, uint32_t cap, unsigned long long* __restrict__ stat) {
+    pdl_enter();
     force_body<EXACT, COUNT>(grid_blk(), sidx, counts, rec, skip, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al,
                              eps2, theta2, k, hdt, cap, stat);
 }
@@ -1347,6 +1366,7 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
               float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
               uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
               unsigned long long* __restrict__ stat, int* __restrict__ err) {
+    pdl_enter();
     __shared__ GroupSmem smem[kGroupWarps];
     force_group_body<EXACT, QUAD, COUNT>(grid_blk(), smem[threadIdx.x >> 5], sidx, skey, counts, rec, skip, quad,
                                          kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2, theta2, k, hdt,
@@ -1432,6 +1452,31 @@ cudaError_t bh_init(gs_sim* s) {
     return e;
 }
 
+namespace {
+// Launch `kernel` on `st`.  With `pdl` the launch may begin while the previous kernel in
+// the stream is still running; the kernel waits for it on entry (pdl_enter).
+template <typename... KArgs, typename... Args>
+cudaError_t launch(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+}  // namespace
+
+#define GS_TRY_LAUNCH(call)                    \
+    do {                                       \
+        cudaError_t _e = (call);               \
+        if (_e != cudaSuccess) return _e;      \
+    } while (0)
+
 cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     BHWork& w = s->bh;
     cudaStream_t st = s->stream;
@@ -1440,30 +1485,36 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     cudaError_t e = cudaMemsetAsync(w.zero_base, 0, w.zero_bytes, st);
     if (e != cudaSuccess) return e;
     uint32_t* ctr = w.counters;
+    // programmatic launches everywhere except right after the memset, and not while
+    // stage events sit between the launches
+    const bool pdl = !profile;
+    bool first = true;
+    auto next_pdl = [&]() {
+        const bool r = pdl && !first;
+        first = false;
+        return r;
+    };
     if (bbox) {
         stage_begin(s, kStageBBox, profile);
-        k_bbox<<<bbox_blocks(n), kBBoxThreads, 0, st>>>(s->pos[in], n, w.bbox_part, ctr + kCtrBBox, w.params);
+        GS_TRY_LAUNCH(launch(next_pdl(), k_bbox, bbox_blocks(n), kBBoxThreads, st, s->pos[in], n, w.bbox_part,
+                             ctr + kCtrBBox, w.params));
         count_launch(s);
         stage_end(s, kStageBBox, profile);
     }
     stage_begin(s, kStageKeys, profile);
-    k_keygen<<<grid_for(n, kKeyThreads), kKeyThreads, 0, st>>>(bbox ? 1 : 0, w.params, s->pos[in], s->mass[in],
-                                                               s->pos[out], s->mass[out], n, w.keys[0], w.hist,
-                                                               w.passes, ctr + kCtrValid);
+    GS_TRY_LAUNCH(launch(next_pdl(), k_keygen, grid_for(n, kKeyThreads), kKeyThreads, st, bbox ? 1 : 0,
+                         (const BHParams*)w.params, s->pos[in], s->mass[in], s->pos[out], s->mass[out], n, w.keys[0],
+                         w.hist, w.passes, ctr + kCtrValid));
     count_launch(s);
     stage_end(s, kStageKeys, profile);
     stage_begin(s, kStageSort, profile);
     for (int ps = 0; ps < w.passes; ++ps) {
         const int a = ps & 1, b = a ^ 1;
         uint32_t* status = w.sort_status + (size_t)ps * w.sort_tiles * 256;
-        if (ps == 0)
-            k_sort_pass<true><<<w.sort_tiles, kSortThreads, 0, st>>>(w.keys[a], nullptr, w.keys[b], w.idx[b], n,
-                                                                     8 * ps, w.hist + 256 * ps, status,
-                                                                     ctr + kCtrSort + ps, s->d_err);
-        else
-            k_sort_pass<false><<<w.sort_tiles, kSortThreads, 0, st>>>(w.keys[a], w.idx[a], w.keys[b], w.idx[b], n,
-                                                                      8 * ps, w.hist + 256 * ps, status,
-                                                                      ctr + kCtrSort + ps, s->d_err);
+        GS_TRY_LAUNCH(launch(next_pdl(), ps == 0 ? k_sort_pass<true> : k_sort_pass<false>, (int)w.sort_tiles,
+                             kSortThreads, st, (const uint32_t*)w.keys[a], (const uint32_t*)(ps == 0 ? nullptr : w.idx[a]),
+                             w.keys[b], w.idx[b], n, 8 * ps, (const uint32_t*)(w.hist + 256 * ps), status,
+                             ctr + kCtrSort + ps, s->d_err));
     }
     count_launch(s, w.passes);
     w.final_keys = w.passes & 1;
@@ -1471,75 +1522,67 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     const uint32_t* skey = w.keys[w.final_keys];
     const uint32_t* sidx = w.idx[w.final_keys];
     stage_begin(s, kStageScan, profile);
-    k_meta_scan<<<w.scan_tiles, kScanThreads, 0, st>>>(skey, n + 1, ctr + kCtrValid, w.depth, w.E, w.scan_status,
-                                                        ctr + kCtrScan, ctr + kCtrInternal, s->d_err);
+    GS_TRY_LAUNCH(launch(next_pdl(), k_meta_scan, (int)w.scan_tiles, kScanThreads, st, skey, n + 1,
+                         (const uint32_t*)(ctr + kCtrValid), w.depth, w.E, w.scan_status, ctr + kCtrScan,
+                         ctr + kCtrInternal, s->d_err));
     count_launch(s);
     stage_end(s, kStageScan, profile);
     stage_begin(s, kStageRecords, profile);
-    k_records<<<grid_for(n, 256), 256, 0, st>>>(skey, sidx, w.E, ctr + kCtrValid, w.depth, s->pos[in], s->mass[in],
-                                                w.rec, w.skip, w.node_slot, w.cap, n, s->d_err);
-    k_nodes<<<grid_for(n, 256), 256, 0, st>>>(skey, w.E, ctr + kCtrValid, w.depth, w.params, w.node_slot, w.rec,
-                                              w.skip, w.kids, w.nodeinfo, ctr + kCtrLevel, w.levels, n, w.cap,
-                                              s->d_err);
+    GS_TRY_LAUNCH(launch(next_pdl(), k_records, grid_for(n, 256), 256, st, skey, sidx, (const uint32_t*)w.E,
+                         (const uint32_t*)(ctr + kCtrValid), w.depth, (const float2*)s->pos[in],
+                         (const float*)s->mass[in], w.rec, w.skip, w.node_slot, w.cap, n, s->d_err));
+    GS_TRY_LAUNCH(launch(next_pdl(), k_nodes, grid_for(n, 256), 256, st, skey, (const uint32_t*)w.E,
+                         (const uint32_t*)(ctr + kCtrValid), w.depth, (const BHParams*)w.params,
+                         (const uint32_t*)w.node_slot, w.rec, w.skip, w.kids, w.nodeinfo, ctr + kCtrLevel, w.levels,
+                         n, w.cap, s->d_err));
     count_launch(s, 2);
     stage_end(s, kStageRecords, profile);
     stage_begin(s, kStageSums, profile);
     {
         const int safe = (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0;
         const int bb = bbox ? 1 : 0;
+        float4* quad = w.quad;
         for (int d = w.depth; d > kLevelTop; --d) {
             const int blocks = (int)std::min<uint64_t>((uint64_t)grid_for(n, 256), (level_cap(d, n) + 255) / 256);
-            if (w.quad)
-                k_level_sums<true><<<blocks, 256, 0, st>>>(d, ctr + kCtrLevel, w.levels, n, skey, w.depth, w.rec,
-                                                           w.kids, w.nodeinfo, w.msum, w.quad, safe, bb, w.params);
-            else
-                k_level_sums<false><<<blocks, 256, 0, st>>>(d, ctr + kCtrLevel, w.levels, n, skey, w.depth, w.rec,
-                                                            w.kids, w.nodeinfo, w.msum, nullptr, safe, bb, w.params);
+            GS_TRY_LAUNCH(launch(next_pdl(), quad ? k_level_sums<true> : k_level_sums<false>, blocks, 256, st, d,
+                                 (const uint32_t*)(ctr + kCtrLevel), (const uint32_t*)w.levels, n, skey, w.depth,
+                                 w.rec, (const uint4*)w.kids, (const uint2*)w.nodeinfo, w.msum, quad, safe, bb,
+                                 (const BHParams*)w.params));
         }
-        if (w.quad)
-            k_top_sums<true><<<1, 512, 0, st>>>(ctr + kCtrLevel, w.levels, n, skey, w.depth, w.rec, w.kids,
-                                                w.nodeinfo, w.msum, w.quad, safe, bb, w.params);
-        else
-            k_top_sums<false><<<1, 512, 0, st>>>(ctr + kCtrLevel, w.levels, n, skey, w.depth, w.rec, w.kids,
-                                                 w.nodeinfo, w.msum, nullptr, safe, bb, w.params);
+        GS_TRY_LAUNCH(launch(next_pdl(), quad ? k_top_sums<true> : k_top_sums<false>, 1, 512, st,
+                             (const uint32_t*)(ctr + kCtrLevel), (const uint32_t*)w.levels, n, skey, w.depth, w.rec,
+                             (const uint4*)w.kids, (const uint2*)w.nodeinfo, w.msum, quad, safe, bb,
+                             (const BHParams*)w.params));
     }
     count_launch(s, (uint32_t)(w.depth - kLevelTop + 1));
     stage_end(s, kStageSums, profile);
     stage_begin(s, kStageForce, profile);
     const float k = s->G * s->dt_eff;  // ForceShader.comp:145 (GRAVITATIONAL_CONST * SIMULATION_TIME)
     const float hdt = 0.5f * s->dt_eff;
-    const int blocks = (int)((n / 32 + kForceWarps - 1) / kForceWarps);
     const bool exact = s->p.math_mode == GS_MATH_REFERENCE;
     const bool count = (s->p.flags & GS_FLAG_COUNT_INTERACTIONS) != 0;
     unsigned long long* stat = (unsigned long long*)(ctr + kCtrStat);
-#define GS_FORCE(E_, C_)                                                                                      \
-    k_force<E_, C_><<<blocks, kForceWarps * 32, 0, st>>>(sidx, ctr + kCtrValid, w.rec, w.skip, s->pos[in],    \
-                                                         s->vel[in], s->pos[out], s->vel[out], s->acc, n, s->eps2, \
-                                                         s->theta2, k, hdt, (uint32_t)w.cap, stat)
-#define GS_GROUP(E_, Q_, C_)                                                                                    \
-    k_force_group<E_, Q_, C_><<<(int)((n / kGroupSize + kGroupWarps - 1) / kGroupWarps), kGroupWarps * 32, 0, st>>>( \
-        sidx, skey, ctr + kCtrValid, w.rec, w.skip, w.quad, w.kids, s->pos[in], s->vel[in], s->pos[out],             \
-        s->vel[out],                                                                                                 \
-        s->acc, n,                                                                                                   \
-        s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err)
+    const bool fpdl = next_pdl();
     if (s->p.flags & GS_FLAG_GROUP_WALK) {
         const bool quad = w.quad != nullptr;
-        if (exact) {
-            if (quad) { if (count) GS_GROUP(true, true, true); else GS_GROUP(true, true, false); }
-            else { if (count) GS_GROUP(true, false, true); else GS_GROUP(true, false, false); }
-        } else {
-            if (quad) { if (count) GS_GROUP(false, true, true); else GS_GROUP(false, true, false); }
-            else { if (count) GS_GROUP(false, false, true); else GS_GROUP(false, false, false); }
-        }
-    } else if (exact) {
-        if (count) GS_FORCE(true, true);
-        else GS_FORCE(true, false);
+        auto fn = exact ? (quad ? (count ? k_force_group<true, true, true> : k_force_group<true, true, false>)
+                                : (count ? k_force_group<true, false, true> : k_force_group<true, false, false>))
+                        : (quad ? (count ? k_force_group<false, true, true> : k_force_group<false, true, false>)
+                                : (count ? k_force_group<false, false, true> : k_force_group<false, false, false>));
+        const int blocks = (int)((n / kGroupSize + kGroupWarps - 1) / kGroupWarps);
+        GS_TRY_LAUNCH(launch(fpdl, fn, blocks, kGroupWarps * 32, st, sidx, skey, (const uint32_t*)(ctr + kCtrValid),
+                             (const float4*)w.rec, (const uint32_t*)w.skip, (const float4*)w.quad,
+                             (const uint4*)w.kids, (const float2*)s->pos[in], (const float2*)s->vel[in], s->pos[out],
+                             s->vel[out], s->acc, n, s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err));
     } else {
-        if (count) GS_FORCE(false, true);
-        else GS_FORCE(false, false);
+        auto fn = exact ? (count ? k_force<true, true> : k_force<true, false>)
+                        : (count ? k_force<false, true> : k_force<false, false>);
+        const int blocks = (int)((n / 32 + kForceWarps - 1) / kForceWarps);
+        GS_TRY_LAUNCH(launch(fpdl, fn, blocks, kForceWarps * 32, st, sidx, (const uint32_t*)(ctr + kCtrValid),
+                             (const float4*)w.rec, (const uint32_t*)w.skip, (const float2*)s->pos[in],
+                             (const float2*)s->vel[in], s->pos[out], s->vel[out], s->acc, n, s->eps2, s->theta2, k,
+                             hdt, (uint32_t)w.cap, stat));
     }
-#undef GS_GROUP
-#undef GS_FORCE
     count_launch(s);
     stage_end(s, kStageForce, profile);
     return cudaGetLastError();
