@@ -1725,12 +1725,14 @@ __global__ void __launch_bounds__(256) kb_clear(BatchArgs a, uint32_t* __restric
 }
 
 __global__ void __launch_bounds__(kBBoxThreads) kb_bbox(BatchArgs a) {
+    pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     bbox_body(bb.blk, d.pos[bb.in], d.n_al, d.bbox_part, d.counters + kCtrBBox, d.params);
 }
 
 __global__ void __launch_bounds__(kKeyThreads) kb_keygen(BatchArgs a) {
+    pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     keygen_body(bb.blk, d.bbox, d.params, d.pos[bb.in], d.mass[bb.in], d.pos[bb.out], d.mass[bb.out], d.n_al,
@@ -1739,6 +1741,7 @@ __global__ void __launch_bounds__(kKeyThreads) kb_keygen(BatchArgs a) {
 
 template <bool IDENTITY>
 __global__ void __launch_bounds__(kSortThreads) kb_sort_pass(BatchArgs a, int ps) {
+    pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     const int x = ps & 1, y = x ^ 1;
@@ -1748,6 +1751,7 @@ __global__ void __launch_bounds__(kSortThreads) kb_sort_pass(BatchArgs a, int ps
 }
 
 __global__ void __launch_bounds__(kScanThreads) kb_meta_scan(BatchArgs a) {
+    pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     meta_scan_body(d.keys[d.passes & 1], d.n_al + 1, d.counters + kCtrValid, d.depth, d.E, d.scan_status,
@@ -1755,6 +1759,7 @@ __global__ void __launch_bounds__(kScanThreads) kb_meta_scan(BatchArgs a) {
 }
 
 __global__ void __launch_bounds__(256) kb_records(BatchArgs a) {
+    pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     const int f = d.passes & 1;
@@ -1763,6 +1768,7 @@ __global__ void __launch_bounds__(256) kb_records(BatchArgs a) {
 }
 
 __global__ void __launch_bounds__(256) kb_nodes(BatchArgs a) {
+    pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     nodes_body(bb.blk, d.keys[d.passes & 1], d.E, d.counters + kCtrValid, d.depth, d.params, d.node_slot, d.rec,
@@ -1772,6 +1778,7 @@ __global__ void __launch_bounds__(256) kb_nodes(BatchArgs a) {
 // level lv of every system (systems shallower than lv have nothing to do)
 template <bool QUAD>
 __global__ void __launch_bounds__(256) kb_level_sums(BatchArgs a, int lv) {
+    pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     if (lv > d.depth) return;
@@ -1781,6 +1788,7 @@ __global__ void __launch_bounds__(256) kb_level_sums(BatchArgs a, int lv) {
 
 template <bool QUAD>
 __global__ void __launch_bounds__(512) kb_top_sums(BatchArgs a) {
+    pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     top_sums_body<QUAD>(d.counters + kCtrLevel, d.levels, d.n_al, d.keys[d.passes & 1], d.depth, d.rec, d.kids,
@@ -1789,6 +1797,7 @@ __global__ void __launch_bounds__(512) kb_top_sums(BatchArgs a) {
 
 template <bool EXACT, bool QUAD, bool COUNT>
 __global__ void __launch_bounds__(kGroupWarps * 32) kb_force_group(BatchArgs a, uint32_t* __restrict__ work) {
+    pdl_enter();
     __shared__ GroupSmem smem[kGroupWarps];
     __shared__ uint32_t s_b;
     const uint32_t total = __ldg(&a.first[a.nsys]);
@@ -1811,6 +1820,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kb_force_group(BatchArgs a, 
 
 template <bool EXACT, bool COUNT>
 __global__ void __launch_bounds__(kForceWarps * 32) kb_force(BatchArgs a, uint32_t* __restrict__ work) {
+    pdl_enter();
     __shared__ uint32_t s_b;
     const uint32_t total = __ldg(&a.first[a.nsys]);
     for (;;) {
@@ -1909,43 +1919,35 @@ int bh_batch_force_grid(const BatchPlan& p) {
 cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st) {
     if (!p.n_bh) return cudaSuccess;
     auto args = [&](int tab) { return BatchArgs{p.d_descs, p.d_tab[tab], p.n_bh, step}; };
-    kb_clear<<<p.total[kTabClear], 256, 0, st>>>(args(kTabClear), p.d_work);
-    if (p.bbox) kb_bbox<<<p.total[kTabBBox], kBBoxThreads, 0, st>>>(args(kTabBBox));
-    kb_keygen<<<p.total[kTabGrid], kKeyThreads, 0, st>>>(args(kTabGrid));
-    for (int ps = 0; ps < p.passes; ++ps) {
-        if (ps == 0) kb_sort_pass<true><<<p.total[kTabSort], kSortThreads, 0, st>>>(args(kTabSort), ps);
-        else kb_sort_pass<false><<<p.total[kTabSort], kSortThreads, 0, st>>>(args(kTabSort), ps);
-    }
-    kb_meta_scan<<<p.total[kTabScan], kScanThreads, 0, st>>>(args(kTabScan));
-    kb_records<<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
-    kb_nodes<<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid));
-    for (int lv = p.depth; lv > kLevelTop; --lv) {
-        if (p.quad) kb_level_sums<true><<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid), lv);
-        else kb_level_sums<false><<<p.total[kTabGrid], 256, 0, st>>>(args(kTabGrid), lv);
-    }
-    if (p.quad) kb_top_sums<true><<<p.total[kTabOne], 512, 0, st>>>(args(kTabOne));
-    else kb_top_sums<false><<<p.total[kTabOne], 512, 0, st>>>(args(kTabOne));
-    const uint32_t fg = p.force_grid < (int)p.total[kTabForce] ? (uint32_t)p.force_grid : p.total[kTabForce];
-    uint32_t* work = p.d_work;
-#define GS_BGROUP(E_, Q_, C_) kb_force_group<E_, Q_, C_><<<fg, kGroupWarps * 32, 0, st>>>(args(kTabForce), work)
-#define GS_BFORCE(E_, C_) kb_force<E_, C_><<<fg, kForceWarps * 32, 0, st>>>(args(kTabForce), work)
+    // the clear follows whatever the stream did before; every later stage overlaps its
+    // launch with the stage before it (programmatic dependent launch)
+    GS_TRY_LAUNCH(launch(false, kb_clear, (int)p.total[kTabClear], 256, st, args(kTabClear), p.d_work));
+    if (p.bbox) GS_TRY_LAUNCH(launch(true, kb_bbox, (int)p.total[kTabBBox], kBBoxThreads, st, args(kTabBBox)));
+    GS_TRY_LAUNCH(launch(true, kb_keygen, (int)p.total[kTabGrid], kKeyThreads, st, args(kTabGrid)));
+    for (int ps = 0; ps < p.passes; ++ps)
+        GS_TRY_LAUNCH(launch(true, ps == 0 ? kb_sort_pass<true> : kb_sort_pass<false>, (int)p.total[kTabSort],
+                             kSortThreads, st, args(kTabSort), ps));
+    GS_TRY_LAUNCH(launch(true, kb_meta_scan, (int)p.total[kTabScan], kScanThreads, st, args(kTabScan)));
+    GS_TRY_LAUNCH(launch(true, kb_records, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
+    GS_TRY_LAUNCH(launch(true, kb_nodes, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
+    for (int lv = p.depth; lv > kLevelTop; --lv)
+        GS_TRY_LAUNCH(launch(true, p.quad ? kb_level_sums<true> : kb_level_sums<false>, (int)p.total[kTabGrid], 256,
+                             st, args(kTabGrid), lv));
+    GS_TRY_LAUNCH(launch(true, p.quad ? kb_top_sums<true> : kb_top_sums<false>, (int)p.total[kTabOne], 512, st,
+                         args(kTabOne)));
+    const int fg = p.force_grid < (int)p.total[kTabForce] ? p.force_grid : (int)p.total[kTabForce];
     if (p.group) {
-        if (p.exact) {
-            if (p.quad) { if (p.count) GS_BGROUP(true, true, true); else GS_BGROUP(true, true, false); }
-            else { if (p.count) GS_BGROUP(true, false, true); else GS_BGROUP(true, false, false); }
-        } else {
-            if (p.quad) { if (p.count) GS_BGROUP(false, true, true); else GS_BGROUP(false, true, false); }
-            else { if (p.count) GS_BGROUP(false, false, true); else GS_BGROUP(false, false, false); }
-        }
-    } else if (p.exact) {
-        if (p.count) GS_BFORCE(true, true);
-        else GS_BFORCE(true, false);
+        auto fn = p.exact ? (p.quad ? (p.count ? kb_force_group<true, true, true> : kb_force_group<true, true, false>)
+                                    : (p.count ? kb_force_group<true, false, true> : kb_force_group<true, false, false>))
+                          : (p.quad ? (p.count ? kb_force_group<false, true, true> : kb_force_group<false, true, false>)
+                                    : (p.count ? kb_force_group<false, false, true>
+                                               : kb_force_group<false, false, false>));
+        GS_TRY_LAUNCH(launch(true, fn, fg, kGroupWarps * 32, st, args(kTabForce), p.d_work));
     } else {
-        if (p.count) GS_BFORCE(false, true);
-        else GS_BFORCE(false, false);
+        auto fn = p.exact ? (p.count ? kb_force<true, true> : kb_force<true, false>)
+                          : (p.count ? kb_force<false, true> : kb_force<false, false>);
+        GS_TRY_LAUNCH(launch(true, fn, fg, kForceWarps * 32, st, args(kTabForce), p.d_work));
     }
-#undef GS_BGROUP
-#undef GS_BFORCE
     return cudaGetLastError();
 }
 
