@@ -15,8 +15,13 @@ A step is one simulation step of the whole system.
          state from pinned host memory (gs_set_particles), runs one step (gs_run) and
          reads the state back (gs_get_particles), host wall clock
   roofline  the traversal kernel: algorithmic FLOP of the accepted interactions
-         (14 per monopole, 31 per quadrupole) over its CUDA-event time, against the
+         (14 per monopole, 37 per quadrupole) over its CUDA-event time, against the
          FP32 FMA rate
+  batched  512 systems of uneven N stepped together, against each run alone
+  served   a Poisson stream of simulation requests through the serving loop, against the
+           plain path taking them one at a time (p50 / p99 latency)
+  direct_precision_study  N=50k direct sum over 1000 steps: Kahan-compensated against
+           plain FP32 sums, force error against FP64 and energy drift
 
 Multi-GPU: independent replicas (the path has no exchange step), one per rank.
 `--impl reference` times the CPU restatement of the reference's algorithm (oracle/,
@@ -392,6 +397,57 @@ def measure_served(gsim, torch, args, local, crossover, theta):
             "max_resident_particles": args.serve_max_particles, "policy": "fifo with conservative backfill"}
 
 
+PREC_DESC = ("direct sum N=50000, two exponential disks (scale length 20, truncated at r <= 50) centred at "
+             "(+-50, 0) with bulk velocities (0, +-3) and circular speeds inside each disk, masses U[1,10], "
+             "softening 0.2, dt=1e-3, 1000 steps (seed 1003)")
+
+
+def precision_study(gsim, torch, args, local, steps=1000, every=100, sample=2048):
+    """Direct-sum precision study: the same 1000-step run with Kahan-compensated FP32 tile
+    sums (the default), with plain FP32 tile sums, and with the shader's plain sequential
+    FP32 sum (REFERENCE math).  Every `every` steps: relative force error of the step
+    against the FP64 direct sum on a fixed subsample, and the FP64 energy drift."""
+    n = 50000
+    pos, vel, mass = gsim.generate(gsim.GEN_EXP_DISK_COLLISION, n, size=100.0, seed=1003)
+    sub = np.random.default_rng(3).choice(n, sample, replace=False).astype(np.uint32)
+    variants = (("kahan_fp32", gsim.MATH_FAST, 0),
+                ("plain_fp32_tiles", gsim.MATH_FAST, gsim.FLAG_PLAIN_SUM),
+                ("plain_fp32_sequential_reference_math", gsim.MATH_REFERENCE, 0))
+    out = {}
+    for name, mm, fl in variants:
+        p = gsim.default_params(algorithm=gsim.DIRECT_SUM, math_mode=mm, device=local, flags=fl | gsim.FLAG_RECORD_ACCEL)
+        with gsim.Simulation(pos, vel, mass, params=p) as sim:
+            ke, pe = sim.energy_f64()
+            e0 = ke + pe
+            rms, mx, drift = [], [], []
+            for k in range(0, steps, every):
+                a64 = sim.accel_f64(sub)  # FP64 forces of the current state
+                sim.run(1)                # the FP32 step from that state records its forces
+                acc = sim.get_accel()[sub].astype(np.float64)
+                e = np.linalg.norm(acc - a64, axis=1) / np.maximum(np.linalg.norm(a64, axis=1), 1e-300)
+                rms.append(float(np.sqrt(np.mean(e ** 2))))
+                mx.append(float(e.max()))
+                sim.run(every - 1)
+                ke, pe = sim.energy_f64()
+                drift.append(abs((ke + pe) - e0) / abs(e0))
+            # device time per step of the same variant, state resident
+            stream = torch.cuda.ExternalStream(sim.stream(), device=local)
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            sim.sync()
+            with torch.cuda.stream(stream):
+                a.record(stream)
+                sim.run(20)
+                z.record(stream)
+            sim.sync()
+            ms = a.elapsed_time(z) / 20
+        out[name] = {"force_error_rms_max_over_checkpoints": max(rms), "force_error_rms_mean": float(np.mean(rms)),
+                     "force_error_max": max(mx), "energy_drift_final": drift[-1], "energy_drift_max": max(drift),
+                     "ms_per_step": ms, "checkpoint_rms": rms}
+    return {"workload": PREC_DESC, "steps": steps, "checkpoint_every": every, "subsample": sample,
+            "energy": "FP64 kinetic + softened potential (gs_energy_f64), drift = |E(t) - E(0)| / |E(0)|",
+            "variants": out}
+
+
 def force_error(gsim, wl, pos, vel, mass, local):
     """RMS / median / p99 / max relative force error of one step against the FP64 direct
     sum (GPU FP64 kernel) on a 4096-particle subsample."""
@@ -519,6 +575,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--batch-theta", type=float, default=0.37, help="theta of the batched Barnes-Hut systems")
     ap.add_argument("--no-served", action="store_true", help="skip the served (request stream) line")
+    ap.add_argument("--no-precision", action="store_true", help="skip the direct-sum precision study")
     ap.add_argument("--serve-requests", type=int, default=100)
     ap.add_argument("--serve-max-particles", type=int, default=0, help="resident particle cap (0: budget only)")
     args = ap.parse_args()
@@ -583,6 +640,9 @@ def main():
     if rank == 0 and world == 1 and not args.no_served:
         xo = batched["crossover_n"] if batched else 2500
         served = measure_served(gsim, torch, args, local, xo, args.batch_theta)
+    precision = None
+    if rank == 0 and world == 1 and not args.no_precision:
+        precision = precision_study(gsim, torch, args, local)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, pos, vel, mass)
@@ -595,7 +655,8 @@ def main():
                           "l2": "flushed (256 MiB write) before every timed step"},
                "e2e": e2e, "gpu_launches": m["launches"] * world, "roofline": roofline_of(gsim, wl, m),
                "cpu_baseline": cpu, "force_error_vs_fp64": err, "clocks": m["clocks"],
-               "reference_rule_theta1": secondary, "batched": batched, "served": served}
+               "reference_rule_theta1": secondary, "batched": batched, "served": served,
+               "direct_precision_study": precision}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

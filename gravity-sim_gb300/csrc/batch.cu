@@ -45,7 +45,9 @@ gs_status check_batch_members(gs_sim* const* sims, size_t count, const char* who
                                 "QUADRUPOLE / SAFE_RADIUS / GROUP_WALK / COUNT_INTERACTIONS flags");
         } else {
             if (!dir0) dir0 = s;
-            else if (s->p.math_mode != dir0->p.math_mode) return fail(w + ": direct-sum systems must share math_mode");
+            else if (s->p.math_mode != dir0->p.math_mode ||
+                     (s->p.flags & GS_FLAG_PLAIN_SUM) != (dir0->p.flags & GS_FLAG_PLAIN_SUM))
+                return fail(w + ": direct-sum systems must share math_mode and GS_FLAG_PLAIN_SUM");
         }
     }
     return GS_OK;
@@ -184,6 +186,7 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
     p.exact = bh0 && bh0->p.math_mode == GS_MATH_REFERENCE;
     p.count = bh0 && (bh0->p.flags & GS_FLAG_COUNT_INTERACTIONS);
     p.direct_exact = dir0 && dir0->p.math_mode == GS_MATH_REFERENCE;
+    p.direct_plain = dir0 && (dir0->p.flags & GS_FLAG_PLAIN_SUM);
     if (bh0) {
         const int variant = (p.group ? 1 : 0) | (p.exact ? 2 : 0) | (p.quad ? 4 : 0) | (p.count ? 8 : 0);
         if (!force_grid_cache[variant]) force_grid_cache[variant] = bh_batch_force_grid(p);

@@ -29,8 +29,10 @@ constexpr int kDirectBlock = 128;
 constexpr int kDirectTileJ = 64;
 
 // Block (bx, by) of a system: i-tile bx, j-chunk by.  A plain launch passes blockIdx.x /
-// blockIdx.y, a batched launch the block's position inside its system's grid.
-template <int IPT>
+// blockIdx.y, a batched launch the block's position inside its system's grid.  KAHAN
+// false (GS_FLAG_PLAIN_SUM) adds the tile partials and the chunks plainly, for the
+// precision study against the compensated sums.
+template <int IPT, bool KAHAN>
 __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const float2* __restrict__ pos,
                                                  const float2* __restrict__ vel, const float* __restrict__ mass,
                                                  float2* __restrict__ pos_out, float2* __restrict__ vel_out,
@@ -80,6 +82,11 @@ __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const
         }
 #pragma unroll
         for (int r = 0; r < IPT; ++r) {  // Kahan-compensated add of the tile partial
+            if (!KAHAN) {
+                sx[r] += tx[r];
+                sy[r] += ty[r];
+                continue;
+            }
             float y = tx[r] - cx[r];
             float u = sx[r] + y;
             cx[r] = (u - sx[r]) - y;
@@ -110,6 +117,11 @@ __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const
             if (i < n_al) {
                 for (int c = 0; c < chunks; ++c) {
                     float4 q = __ldcg(&partials[(size_t)c * n_al + i]);
+                    if (!KAHAN) {
+                        ax += q.x;
+                        ay += q.y;
+                        continue;
+                    }
                     float y = (q.x - q.z) - kx;
                     float u = ax + y;
                     kx = (u - ax) - y;
@@ -173,13 +185,13 @@ __device__ __forceinline__ void direct_ref_body(uint32_t bx, const float2* __res
     vel_out[i] = make_float2(nvx, nvy);
 }
 
-template <int IPT>
+template <int IPT, bool KAHAN>
 __global__ void __launch_bounds__(kDirectBlock)
 k_direct_fast(const float2* __restrict__ pos, const float2* __restrict__ vel, const float* __restrict__ mass,
               float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
               uint32_t n_al, int chunks, uint32_t jchunk, float eps2, float k, float hdt,
               float4* __restrict__ partials, uint32_t* __restrict__ tickets) {
-    direct_fast_body<IPT>(blockIdx.x, blockIdx.y, pos, vel, mass, pos_out, vel_out, acc_rec, n_al, chunks, jchunk,
+    direct_fast_body<IPT, KAHAN>(blockIdx.x, blockIdx.y, pos, vel, mass, pos_out, vel_out, acc_rec, n_al, chunks, jchunk,
                           eps2, k, hdt, partials, tickets);
 }
 
@@ -204,7 +216,7 @@ __device__ __forceinline__ uint32_t direct_batch_sys(const uint32_t* __restrict_
     return lo;
 }
 
-template <bool EXACT>
+template <bool EXACT, bool KAHAN>
 __global__ void __launch_bounds__(EXACT ? 64 : kDirectBlock)
 kb_direct(const SysDesc* __restrict__ descs, const uint32_t* __restrict__ first, uint32_t nsys, uint32_t step) {
     const uint32_t s = direct_batch_sys(first, nsys, blockIdx.x);
@@ -215,7 +227,7 @@ kb_direct(const SysDesc* __restrict__ descs, const uint32_t* __restrict__ first,
         direct_ref_body(b, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out], d.acc, d.n_al, d.eps2, d.k,
                         d.hdt);
     else
-        direct_fast_body<2>(b % d.itiles, b / d.itiles, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out],
+        direct_fast_body<2, KAHAN>(b % d.itiles, b / d.itiles, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out],
                             d.acc, d.n_al, (int)d.chunks, d.jchunk, d.eps2, d.k, d.hdt, d.partials, d.tickets);
 }
 
@@ -246,7 +258,70 @@ k_accel_f64(const uint32_t* __restrict__ targets, const float2* __restrict__ pos
     if (threadIdx.x == 0) out[blockIdx.x] = make_double2(sx[0], sy[0]);
 }
 
+// Energy in FP64 (diagnostic, not on the step path): per block of 256 particles i, the
+// kinetic energy 1/2 m |v|^2 and m_i * sum_{j != i} m_j / sqrt(|p_j - p_i|^2 + eps^2), the
+// latter over j tiles staged in shared memory; block sums in a fixed tree order.
+__global__ void __launch_bounds__(256)
+k_energy_f64(const float2* __restrict__ pos, const float2* __restrict__ vel, const float* __restrict__ mass,
+             uint32_t n, double eps2, double2* __restrict__ part) {
+    __shared__ double sx[256], sy[256], sm[256];
+    const uint32_t t = threadIdx.x, i = blockIdx.x * 256 + t;
+    const bool own = i < n;
+    const double px = own ? (double)pos[i].x : 0.0, py = own ? (double)pos[i].y : 0.0;
+    const double mi = own ? (double)mass[i] : 0.0;
+    double pot = 0.0;
+    for (uint32_t jt = 0; jt < n; jt += 256) {
+        const uint32_t j = jt + t;
+        sx[t] = j < n ? (double)pos[j].x : 0.0;
+        sy[t] = j < n ? (double)pos[j].y : 0.0;
+        sm[t] = j < n ? (double)mass[j] : 0.0;
+        __syncthreads();
+        for (uint32_t jj = 0; jj < 256; ++jj) {
+            if (jt + jj == i) continue;
+            const double dx = sx[jj] - px, dy = sy[jj] - py;
+            pot += sm[jj] / sqrt(dx * dx + dy * dy + eps2);
+        }
+        __syncthreads();
+    }
+    const double vx = own ? (double)vel[i].x : 0.0, vy = own ? (double)vel[i].y : 0.0;
+    sx[t] = 0.5 * mi * (vx * vx + vy * vy);
+    sy[t] = mi * pot;
+    __syncthreads();
+    for (uint32_t w = 128; w > 0; w >>= 1) {
+        if (t < w) {
+            sx[t] += sx[t + w];
+            sy[t] += sy[t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) part[blockIdx.x] = make_double2(sx[0], sy[0]);
+}
+
 }  // namespace
+
+cudaError_t energy_f64(gs_sim* s, double* kinetic, double* potential) {
+    const uint32_t n = (uint32_t)s->n_al;
+    const uint32_t blocks = (n + 255) / 256;
+    double2* part = nullptr;
+    cudaError_t e = cudaMallocAsync(&part, blocks * sizeof(double2), s->stream);
+    if (e != cudaSuccess) return e;
+    k_energy_f64<<<blocks, 256, 0, s->stream>>>(s->pos[s->in], s->vel[s->in], s->mass[s->in], n, (double)s->eps2,
+                                                 part);
+    double2* host = new double2[blocks];
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, part, blocks * sizeof(double2), cudaMemcpyDeviceToHost, s->stream);
+    cudaFreeAsync(part, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    double ke = 0.0, pp = 0.0;
+    for (uint32_t b = 0; b < blocks; ++b) {
+        ke += host[b].x;
+        pp += host[b].y;
+    }
+    delete[] host;
+    *kinetic = ke;
+    *potential = -0.5 * (double)s->G * pp;  // every pair was counted from both ends
+    return e;
+}
 
 static int pick_chunks(uint64_t n_al, int ipt) {
     const uint64_t itiles = (n_al + kDirectBlock * ipt - 1) / (kDirectBlock * ipt);
@@ -304,9 +379,10 @@ cudaError_t direct_step(gs_sim* s, int in, int out, bool profile) {
         uint32_t itiles, jchunk, chunks;
         direct_shape(s, itiles, jchunk, chunks);
         dim3 grid(itiles, chunks);
-        k_direct_fast<2><<<grid, kDirectBlock, 0, s->stream>>>(
-            s->pos[in], s->vel[in], s->mass[in], s->pos[out], s->vel[out], s->acc, n_al, (int)chunks, jchunk,
-            s->eps2, k, hdt, w.partials, w.tickets);
+        auto fn = (s->p.flags & GS_FLAG_PLAIN_SUM) ? k_direct_fast<2, false> : k_direct_fast<2, true>;
+        fn<<<grid, kDirectBlock, 0, s->stream>>>(s->pos[in], s->vel[in], s->mass[in], s->pos[out], s->vel[out],
+                                                  s->acc, n_al, (int)chunks, jchunk, s->eps2, k, hdt, w.partials,
+                                                  w.tickets);
     }
     count_launch(s);
     stage_end(s, kStageDirect, profile);
@@ -328,8 +404,14 @@ void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
 cudaError_t direct_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st) {
     if (!p.n_direct) return cudaSuccess;
     const SysDesc* descs = p.d_descs + p.n_bh;
-    if (p.direct_exact) kb_direct<true><<<p.total[kTabDirect], 64, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct, step);
-    else kb_direct<false><<<p.total[kTabDirect], kDirectBlock, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct, step);
+    if (p.direct_exact)
+        kb_direct<true, false><<<p.total[kTabDirect], 64, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct, step);
+    else if (p.direct_plain)
+        kb_direct<false, false><<<p.total[kTabDirect], kDirectBlock, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct,
+                                                                              step);
+    else
+        kb_direct<false, true><<<p.total[kTabDirect], kDirectBlock, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct,
+                                                                             step);
     return cudaGetLastError();
 }
 
@@ -432,7 +514,7 @@ extern "C" gs_status gs_direct_step_noalloc(const float* d_pos_in, const float* 
     const float eps2 = softening_len * softening_len;
     const float k = simulation_time * gravitational_const;
     const float hdt = 0.5f * simulation_time;
-    k_direct_fast<2><<<dim3(itiles, chunks), kDirectBlock, 0, s>>>(
+    k_direct_fast<2, true><<<dim3(itiles, chunks), kDirectBlock, 0, s>>>(
         (const float2*)d_pos_in, (const float2*)d_vel_in, d_mass, (float2*)d_pos_out, (float2*)d_vel_out, nullptr,
         n_al, chunks, jchunk, eps2, k, hdt, partials, tickets);
     GS_CUDA(cudaGetLastError());

@@ -146,6 +146,7 @@ struct BatchPlan {
     int passes = 0;
     int depth = 0;               // finest level of the Barnes-Hut members (all share the box mode)
     bool bbox = false, quad = false, group = false, exact = false, count = false, direct_exact = false;
+    bool direct_plain = false;   // direct-sum members add their partials plainly (GS_FLAG_PLAIN_SUM)
     int force_grid = 0;          // persistent force grid (resident blocks)
 };
 
@@ -211,6 +212,7 @@ void direct_carve(gs_sim* s);
 cudaError_t direct_init(gs_sim* s);
 cudaError_t direct_step(gs_sim* s, int in, int out, bool profile);
 cudaError_t accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* d_targets, double2* d_out);
+cudaError_t energy_f64(gs_sim* s, double* kinetic, double* potential);
 uint64_t bh_capacity(int box_mode, uint64_t n_al);
 
 // batched stages (one launch per stage over every system of a plan)

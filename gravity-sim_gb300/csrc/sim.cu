@@ -262,6 +262,8 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
         return invalid("gs_create: invalid math_mode");
     if ((params->flags & GS_FLAG_QUADRUPOLE) && !(params->flags & GS_FLAG_GROUP_WALK))
         return invalid("gs_create: GS_FLAG_QUADRUPOLE needs GS_FLAG_GROUP_WALK");
+    if ((params->flags & GS_FLAG_PLAIN_SUM) && params->algorithm != GS_DIRECT_SUM)
+        return invalid("gs_create: GS_FLAG_PLAIN_SUM applies to direct sum only");
     if ((params->flags & (GS_FLAG_QUADRUPOLE | GS_FLAG_SAFE_RADIUS | GS_FLAG_GROUP_WALK)) &&
         params->algorithm != GS_BARNES_HUT)
         return invalid("gs_create: the accurate-mode flags apply to Barnes-Hut only");
@@ -477,6 +479,15 @@ gs_status gs_accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* targets, d
     if (dout) cudaFreeAsync(dout, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     GS_CUDA(e);
+    return GS_OK;
+}
+
+gs_status gs_energy_f64(gs_sim* s, double* kinetic, double* potential) {
+    if (!s || !kinetic || !potential) return invalid("gs_energy_f64: NULL argument");
+    gs_status st = gs_sync(s, 0);
+    if (st != GS_OK) return st;
+    s->own_work = true;
+    GS_CUDA(energy_f64(s, kinetic, potential));
     return GS_OK;
 }
 

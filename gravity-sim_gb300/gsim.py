@@ -30,8 +30,9 @@ EXPORTS = (
     "gs_direct_step_noalloc", "gs_batch_create", "gs_batch_run", "gs_batch_sync", "gs_batch_kernels_per_step",
     "gs_batch_stream", "gs_batch_destroy", "gs_tune_crossover", "gs_footprint", "gs_server_create",
     "gs_server_submit", "gs_server_poll", "gs_server_request", "gs_server_result", "gs_server_get_stats",
-    "gs_server_clock", "gs_server_run_trace", "gs_server_destroy",
+    "gs_server_clock", "gs_server_run_trace", "gs_server_destroy", "gs_energy_f64",
 )
+FLAG_PLAIN_SUM = 0x80
 SERVE_FIFO, SERVE_SHORTEST_FIRST = 0, 1
 REQUEST_QUEUED, REQUEST_RESIDENT, REQUEST_DONE, REQUEST_FAILED = 0, 1, 2, 3
 BATCH_NO_GRAPH = 0x1
@@ -164,6 +165,8 @@ def lib():
                                     C.c_uint64, C.POINTER(Tuning)]
     L.gs_tune_crossover.restype = st
     srv = C.c_void_p
+    L.gs_energy_f64.argtypes = [sim, _DP, _DP]
+    L.gs_energy_f64.restype = st
     L.gs_footprint.argtypes = [C.POINTER(Params), C.c_uint64]
     L.gs_footprint.restype = C.c_uint64
     L.gs_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(srv)]
@@ -312,6 +315,12 @@ class Simulation:
 
     def stream(self):
         return lib().gs_stream(self._h)
+
+    def energy_f64(self):
+        """(kinetic, potential) of the current state in FP64."""
+        k, p = C.c_double(), C.c_double()
+        _check(lib().gs_energy_f64(self._h, C.byref(k), C.byref(p)))
+        return k.value, p.value
 
     def accel_f64(self, targets):
         t = np.ascontiguousarray(targets, dtype=np.uint32)

@@ -82,6 +82,9 @@ typedef enum gs_math_mode { GS_MATH_FAST = 0, GS_MATH_REFERENCE = 1 } gs_math_mo
 #define GS_FLAG_SAFE_RADIUS 0x20u
 #define GS_FLAG_GROUP_WALK 0x40u
 #define GS_FLAGS_ACCURATE 0x70u
+/* Direct sum, FAST math: add the 64-wide tile partials and the j-chunks plainly instead
+ * of with Kahan compensation (the precision study's uncompensated variant). */
+#define GS_FLAG_PLAIN_SUM 0x80u
 
 typedef struct gs_params {
     float gravitational_const; /* ParticleSystem::GetGravitationalConst, default 1 (src/Main.cpp:59) */
@@ -148,6 +151,10 @@ GS_API void gs_destroy(gs_sim* sim);
 /* FP64 direct-sum accelerations (without G) of the current state on the GPU, for the
  * listed particle indices over all particles; the error reference for every result. */
 GS_API gs_status gs_accel_f64(gs_sim* sim, uint32_t n_targets, const uint32_t* targets, double* acc_xy);
+/* Energy of the current state in FP64 (diagnostic, O(N^2)): kinetic = sum 1/2 m |v|^2,
+ * potential = -G sum_{i<j} m_i m_j / sqrt(|p_i - p_j|^2 + softening^2), the potential of
+ * the softened force law.  No counterpart in the reference. */
+GS_API gs_status gs_energy_f64(gs_sim* sim, double* kinetic, double* potential);
 
 /* Barnes-Hut tree of the most recent step, in the reference's layout
  * (BarnesHutSimulation.cpp:52-142: counts, radiuses, nodePos, nodeMass, sortedSrc).

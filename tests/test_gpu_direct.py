@@ -112,3 +112,41 @@ def test_run_zero_and_async_batches(gs, orc):
         gp, gv, _ = sim.get_particles()
     np.testing.assert_array_equal(gp, st.current()[0])
     np.testing.assert_array_equal(gv, st.current()[1])
+
+
+def test_energy_f64_matches_oracle(gs, orc):
+    """gs_energy_f64 (GPU, FP64) against the CPU FP64 energy of the oracle."""
+    pos, vel, mass = gs.generate(gs.GEN_EXP_DISK_COLLISION, 3000, seed=77)
+    with _sim(gs, pos, vel, mass) as sim:
+        ke, pe = sim.energy_f64()
+    e_orc = orc.energy_f64(pos, vel, mass, G=1.0, softening=0.2)
+    ke_ref = 0.5 * np.sum(mass.astype(np.float64) * np.sum(vel.astype(np.float64) ** 2, axis=1))
+    assert abs(ke - ke_ref) <= 1e-12 * abs(ke_ref)
+    assert abs((ke + pe) - e_orc) <= 1e-10 * abs(e_orc)
+    assert pe < 0.0
+
+
+def test_plain_sum_variant(gs):
+    """GS_FLAG_PLAIN_SUM: the uncompensated tile sums stay close to FP64 but no closer
+    than the compensated ones on average; it is rejected for Barnes-Hut and in a batch
+    with compensated direct-sum members."""
+    n = 20000
+    pos, vel, mass = gs.generate(gs.GEN_EXP_DISK_COLLISION, n, seed=3)
+    sub = np.arange(0, n, 10, dtype=np.uint32)
+    err = {}
+    for flag in (0, gs.FLAG_PLAIN_SUM):
+        with _sim(gs, pos, vel, mass, flags=flag | gs.FLAG_RECORD_ACCEL) as sim:
+            sim.run(1)
+            acc = sim.get_accel()[sub].astype(np.float64)
+            sim.set_particles(pos, vel, mass)
+            a64 = sim.accel_f64(sub)
+        e = np.linalg.norm(acc - a64, axis=1) / np.linalg.norm(a64, axis=1)
+        err[flag] = np.sqrt(np.mean(e ** 2))
+    assert err[gs.FLAG_PLAIN_SUM] < 1e-4
+    assert err[0] <= err[gs.FLAG_PLAIN_SUM]
+    with pytest.raises(gs.GsimError):
+        gs.Simulation(pos, vel, mass, params=gs.default_params(algorithm=gs.BARNES_HUT, flags=gs.FLAG_PLAIN_SUM))
+    a = _sim(gs, pos[:500], vel[:500], mass[:500])
+    b = _sim(gs, pos[:700], vel[:700], mass[:700], flags=gs.FLAG_PLAIN_SUM)
+    with pytest.raises(gs.GsimError):
+        gs.Batch([a, b])
