@@ -20,7 +20,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", "-I" + INCLUDE]
-CUDA_SOURCES = ["direct.cu", "bh.cu", "sim.cu", "batch.cu", "serve.cu"]
+CUDA_SOURCES = ["direct.cu", "bh.cu", "sim.cu", "batch.cu", "serve.cu", "render.cu"]
 CXX_SOURCES = ["host.cpp"]
 
 

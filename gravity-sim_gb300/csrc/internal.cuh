@@ -213,6 +213,7 @@ cudaError_t direct_init(gs_sim* s);
 cudaError_t direct_step(gs_sim* s, int in, int out, bool profile);
 cudaError_t accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* d_targets, double2* d_out);
 cudaError_t energy_f64(gs_sim* s, double* kinetic, double* potential);
+void free_snapshot_ring(const gs_sim* s);
 uint64_t bh_capacity(int box_mode, uint64_t n_al);
 
 // batched stages (one launch per stage over every system of a plan)

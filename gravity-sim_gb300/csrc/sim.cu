@@ -143,6 +143,7 @@ void free_sim(gs_sim* s) {
     if (!s) return;
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    free_snapshot_ring(s);
     for (int p = 0; p < 2; ++p)
         if (s->graph[p]) cudaGraphExecDestroy(s->graph[p]);
     if (s->slab) cudaFreeAsync(s->slab, s->stream);

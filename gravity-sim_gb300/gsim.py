@@ -30,7 +30,8 @@ EXPORTS = (
     "gs_direct_step_noalloc", "gs_batch_create", "gs_batch_run", "gs_batch_sync", "gs_batch_kernels_per_step",
     "gs_batch_stream", "gs_batch_destroy", "gs_tune_crossover", "gs_footprint", "gs_server_create",
     "gs_server_submit", "gs_server_poll", "gs_server_request", "gs_server_result", "gs_server_get_stats",
-    "gs_server_clock", "gs_server_run_trace", "gs_server_destroy", "gs_energy_f64",
+    "gs_server_clock", "gs_server_run_trace", "gs_server_destroy", "gs_energy_f64", "gs_camera_start",
+    "gs_render_points", "gs_snapshot_take", "gs_snapshot_positions", "gs_snapshot_render", "gs_write_ppm",
 )
 FLAG_PLAIN_SUM = 0x80
 SERVE_FIFO, SERVE_SHORTEST_FIRST = 0, 1
@@ -165,6 +166,19 @@ def lib():
                                     C.c_uint64, C.POINTER(Tuning)]
     L.gs_tune_crossover.restype = st
     srv = C.c_void_p
+    _BP = C.POINTER(C.c_uint8)
+    L.gs_camera_start.argtypes = [sim, _FP]
+    L.gs_camera_start.restype = st
+    L.gs_render_points.argtypes = [sim, C.c_uint32, C.c_uint32, _FP, _BP]
+    L.gs_render_points.restype = st
+    L.gs_snapshot_take.argtypes = [sim, C.c_uint32, C.POINTER(C.c_uint64)]
+    L.gs_snapshot_take.restype = st
+    L.gs_snapshot_positions.argtypes = [sim, C.c_uint64, _FP]
+    L.gs_snapshot_positions.restype = st
+    L.gs_snapshot_render.argtypes = [sim, C.c_uint64, C.c_uint32, C.c_uint32, _FP, _BP]
+    L.gs_snapshot_render.restype = st
+    L.gs_write_ppm.argtypes = [C.c_char_p, C.c_uint32, C.c_uint32, _BP]
+    L.gs_write_ppm.restype = st
     L.gs_energy_f64.argtypes = [sim, _DP, _DP]
     L.gs_energy_f64.restype = st
     L.gs_footprint.argtypes = [C.POINTER(Params), C.c_uint64]
@@ -315,6 +329,36 @@ class Simulation:
 
     def stream(self):
         return lib().gs_stream(self._h)
+
+    def camera_start(self):
+        """The reference's start camera {x, y, size, size} of the current state."""
+        cam = np.empty(4, np.float32)
+        _check(lib().gs_camera_start(self._h, _fp(cam)))
+        return cam
+
+    def render(self, width, height, camera):
+        """Point splat of the current state: (height, width) uint8 image, 255 = particle."""
+        cam = np.ascontiguousarray(camera, np.float32)
+        img = np.empty((height, width), np.uint8)
+        _check(lib().gs_render_points(self._h, width, height, _fp(cam), img.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return img
+
+    def snapshot(self, slots=3):
+        t = C.c_uint64()
+        _check(lib().gs_snapshot_take(self._h, slots, C.byref(t)))
+        return t.value
+
+    def snapshot_positions(self, ticket):
+        pos = np.empty((self.n, 2), np.float32)
+        _check(lib().gs_snapshot_positions(self._h, ticket, _fp(pos)))
+        return pos
+
+    def snapshot_render(self, ticket, width, height, camera):
+        cam = np.ascontiguousarray(camera, np.float32)
+        img = np.empty((height, width), np.uint8)
+        _check(lib().gs_snapshot_render(self._h, ticket, width, height, _fp(cam),
+                                        img.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return img
 
     def energy_f64(self):
         """(kinetic, potential) of the current state in FP64."""
@@ -483,3 +527,9 @@ class Server:
         for r, i in zip(requests, out):
             self._n[i] = r.particle_count
         return out
+
+
+def write_ppm(path, image):
+    """Binary PPM of a (height, width) uint8 image from Simulation.render."""
+    img = np.ascontiguousarray(image, np.uint8)
+    _check(lib().gs_write_ppm(path.encode(), img.shape[1], img.shape[0], img.ctypes.data_as(C.POINTER(C.c_uint8))))

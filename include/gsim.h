@@ -322,6 +322,35 @@ GS_API gs_status gs_server_run_trace(gs_server* server, const gs_request* reques
                                      uint64_t* ids);
 GS_API void gs_server_destroy(gs_server* server);
 
+/* ---- headless point splat and snapshot ring ----
+ *
+ * The reference draws each particle as a one-pixel white point on black through Vulkan
+ * (src/Graphics/Shaders/VertShader.vert:13-18, FragShader.frag, GraphicsPipeline.cpp:287-391).
+ * Here a CUDA kernel writes the same picture into a device framebuffer: camera =
+ * {x, y, width, height} in world units, screen = (pos - camera.xy) / camera.wh with y
+ * flipped, pixel = floor((screen + 1) * size / 2); image = width x height bytes, row 0
+ * at the top, 255 where a particle lands and 0 elsewhere.  No graphics API is used. */
+/* The reference's start camera (ParticleSystem::GetCameraInfo, src/Particles/ParticleSystem.cpp:408-435):
+ * centre of the particles' extent and its larger side, as {x, y, size, size}; the
+ * reference's window then uses {x, y, size * aspect / zoom, size / zoom}. */
+GS_API gs_status gs_camera_start(gs_sim* sim, float* camera4);
+/* Render the current state (waits for submitted steps). */
+GS_API gs_status gs_render_points(gs_sim* sim, uint32_t width, uint32_t height, const float* camera4,
+                                  uint8_t* image);
+/* Snapshot ring, the counterpart of the reference's third particle buffer set that the
+ * graphics path reads while compute uses the other two (src/Particles/ParticleSystem.hpp:146-174).
+ * gs_snapshot_take copies the current positions into slot (ticket mod slots) in stream
+ * order -- after every step submitted so far, before any submitted later -- without
+ * waiting.  Reading or rendering a ticket waits only for that copy and runs beside the
+ * simulation's stream.  A ticket is valid until `slots` later snapshots reuse its slot
+ * (then GS_ERR_CAPACITY).  The slot count is fixed by the first call on a system. */
+GS_API gs_status gs_snapshot_take(gs_sim* sim, uint32_t slots, uint64_t* ticket);
+GS_API gs_status gs_snapshot_positions(gs_sim* sim, uint64_t ticket, float* pos_xy);
+GS_API gs_status gs_snapshot_render(gs_sim* sim, uint64_t ticket, uint32_t width, uint32_t height,
+                                    const float* camera4, uint8_t* image);
+/* Binary PPM (P6) of an image from the calls above, white points on black. */
+GS_API gs_status gs_write_ppm(const char* path, uint32_t width, uint32_t height, const uint8_t* image);
+
 /* ---- host-only helpers (no GPU) ---- */
 
 /* Generator types: the reference's four presets (ParticleSystem::GenerateType) and the

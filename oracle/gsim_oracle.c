@@ -240,6 +240,24 @@ static void energy_item(void* p, uint64_t i, int w) {
     c->partial[i] = e;
 }
 
+/* src/Graphics/Shaders/VertShader.vert:13-18 (screenPos = (pos - cameraPos) / cameraSize,
+ * y negated, point size 1), FragShader.frag:5-7 (white), the viewport transform of
+ * GraphicsPipeline.cpp:349-358 written as (ndc + 1) * size / 2, over a black clear
+ * (GraphicsPipeline.cpp:327). */
+void orc_render_points(uint32_t n, const float* pos, const float* camera, uint32_t width, uint32_t height,
+                       uint8_t* image) {
+    memset(image, 0, (size_t)width * height);
+    const float hw = 0.5f * (float)width, hh = 0.5f * (float)height;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float sx = (pos[2 * i] - camera[0]) / camera[2];
+        const float sy = -((pos[2 * i + 1] - camera[1]) / camera[3]);
+        const float fx = (sx + 1.0f) * hw, fy = (sy + 1.0f) * hh;
+        if (!(fx >= 0.0f && fx < (float)width && fy >= 0.0f && fy < (float)height)) continue;
+        const uint32_t x = (uint32_t)fx, y = (uint32_t)fy;
+        if (x < width && y < height) image[(size_t)y * width + x] = 255;
+    }
+}
+
 double orc_energy_f64(uint32_t n, const float* pos, const float* vel, const float* mass,
                       double G, double eps2) {
     double* part = (double*)calloc(n ? n : 1, sizeof(double));

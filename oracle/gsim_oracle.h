@@ -115,6 +115,11 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
 uint64_t orc_bh_node_capacity(int box_mode, uint32_t n_al);
 
 /* Energy of a state (kinetic + softened pairwise potential, FP64, includes G). */
+/* Point splat of VertShader.vert:13-18 / FragShader.frag (one white pixel per particle on
+ * black): camera = {x, y, width, height}; screen = (p - cam.xy) / cam.wh, y flipped;
+ * pixel = floor((screen + 1) * size / 2) when inside; image = width x height bytes. */
+void orc_render_points(uint32_t n, const float* pos, const float* camera, uint32_t width, uint32_t height,
+                       uint8_t* image);
 double orc_energy_f64(uint32_t n, const float* pos, const float* vel, const float* mass,
                       double G, double eps2);
 

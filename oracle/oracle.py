@@ -62,6 +62,8 @@ def lib():
         L.orc_bh_node_capacity.restype = C.c_uint64
         L.orc_energy_f64.argtypes = [C.c_uint32, _FP, _FP, _FP, C.c_double, C.c_double]
         L.orc_energy_f64.restype = C.c_double
+        L.orc_render_points.argtypes = [C.c_uint32, _FP, _FP, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint8)]
+        L.orc_render_points.restype = None
         _lib = L
     return _lib
 
@@ -189,3 +191,12 @@ def energy_f64(pos, vel, mass, G=1.0, softening=0.2):
     mass = np.ascontiguousarray(mass, np.float32)
     eps2 = float(np.float32(softening) * np.float32(softening))
     return lib().orc_energy_f64(len(mass), _fp(pos), _fp(vel), _fp(mass), G, eps2)
+
+
+def render_points(pos, camera, width, height):
+    """Point splat of the reference's vertex/fragment shaders: (height, width) uint8."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    cam = np.ascontiguousarray(camera, np.float32)
+    img = np.empty((height, width), np.uint8)
+    lib().orc_render_points(len(pos), _fp(pos), _fp(cam), width, height, img.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return img

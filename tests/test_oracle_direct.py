@@ -73,3 +73,17 @@ def test_reference_padding_and_step_shape(gs, orc):
     orc.direct_step(st)
     p, v, m = st.current()
     assert p.shape == (63, 2) and np.all(np.isfinite(p)) and np.array_equal(m, mass)
+
+
+def test_render_points_pixel_mapping(orc):
+    """The oracle's point splat: screen = (p - c) / size, y flipped, pixel = floor((s + 1) * n / 2)."""
+    cam = (0.0, 0.0, 2.0, 2.0)
+    pos = np.array([[0.0, 0.0], [-1.0, 1.0], [0.99, -0.99], [1.0, 0.0], [-1.01, 0.0]], np.float32)
+    img = orc.render_points(pos, cam, 4, 4)
+    # (0, 0) -> screen (0, 0) -> pixel (2, 2); (-1, 1) -> screen (-0.5, -0.5) -> (1, 1)
+    # (0.99, -0.99) -> screen (0.495, 0.495) -> (2, 2) again; x = 1 lands at 3.0 -> pixel 3;
+    # x = -1.01 -> screen -0.505 -> 0.99 -> pixel 0
+    expect = np.zeros((4, 4), np.uint8)
+    expect[2, 2] = expect[1, 1] = expect[2, 3] = expect[2, 0] = 255
+    assert np.array_equal(img, expect)
+    assert not orc.render_points(np.array([[5.0, 5.0]], np.float32), cam, 4, 4).any()
