@@ -8,13 +8,17 @@
 //   - the windowed mode does not exist: every run is headless (--no-graphics is accepted);
 //   - --benchmark reports wall-clock time around the synchronised run, not clock() CPU time;
 //   - generators take --seed (the reference seeds from time(nullptr));
-//   - extra switches select this build's modes: --box=fixed|bbox, --accurate, --math=fast|reference.
+//   - extra switches select this build's modes: --box=fixed|bbox, --accurate, --math=fast|reference;
+//   - the window's picture can be saved instead: --image-out=file.ppm writes the final state as
+//     the reference would draw it (one white pixel per particle, the start camera of the initial
+//     state, src/Main.cpp:351-352, corrected for the image's aspect ratio as at :133).
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <vector>
 
 #include "../../include/gsim.hpp"
 
@@ -40,6 +44,8 @@ const char* kHelp =
     "\t--simulation-count: The number of simulations to run (required).\n"
     "\t--box: fixed (the reference's +-500 box, default) | bbox (per-step bounding box)\n"
     "\t--math: fast (default) | reference (bit-identical to the CPU restatement)\n"
+    "\t--image-out: Optional PPM file with the final state drawn as the reference's window would.\n"
+    "\t--image-size: WIDTHxHEIGHT of that image, defaulted to 1280x720.\n"
     "Available options:\n"
     "\t--help: Displays the current message and exits the program.\n"
     "\t--log-detailed: Outputs non-crucial logs.\n"
@@ -73,7 +79,8 @@ bool starts(const char* a, const char* p, const char** v) {
 
 int main(int argc, char** argv) {
     using namespace gsim_gb300;
-    const char *log_file = nullptr, *in_file = nullptr, *out_file = nullptr;
+    const char *log_file = nullptr, *in_file = nullptr, *out_file = nullptr, *image_file = nullptr;
+    unsigned image_w = 1280, image_h = 720;
     uint64_t count = 0, seed = 1, max_steps = 0;
     int gen = -1, algo = -1;
     float gen_size = 0, min_mass = 0, max_mass = 0, G = 1.0f, dt = 0.001f, speed = 1.0f, eps = 0.2f, theta = 1.0f;
@@ -88,6 +95,13 @@ int main(int argc, char** argv) {
         } else if (starts(a, "--log-file=", &v)) log_file = v;
         else if (starts(a, "--particles-in=", &v)) in_file = v;
         else if (starts(a, "--particles-out=", &v)) out_file = v;
+        else if (starts(a, "--image-out=", &v)) image_file = v;
+        else if (starts(a, "--image-size=", &v)) {
+            if (std::sscanf(v, "%ux%u", &image_w, &image_h) != 2 || !image_w || !image_h) {
+                std::printf("[FATAL] --image-size must be WIDTHxHEIGHT\n");
+                return 1;
+            }
+        }
         else if (starts(a, "--particle-count=", &v)) count = std::strtoull(v, nullptr, 10);
         else if (starts(a, "--generate-type=", &v)) {
             if (!std::strcmp(v, "random")) gen = GS_GEN_RANDOM;
@@ -149,6 +163,11 @@ int main(int argc, char** argv) {
         std::unique_ptr<detail::SimulationBase> sim;
         if (algo == GS_DIRECT_SUM) sim.reset(new DirectSimulation(system.get()));
         else sim.reset(new BarnesHutSimulation(system.get()));
+        float camera[4] = {0.0f, 0.0f, 1.0f, 1.0f};  // the start camera of the initial state
+        if (image_file) {
+            Check(gs_camera_start(sim->Handle(), camera));
+            camera[2] = camera[3] * ((float)image_w / (float)image_h);  // size * aspect / zoom, zoom 1
+        }
         auto t0 = std::chrono::steady_clock::now();
         for (uint64_t done = 0; done < max_steps;) {  // batches of at most 100 steps (src/Main.cpp:280)
             uint64_t k = max_steps - done < 100 ? max_steps - done : 100;
@@ -166,6 +185,12 @@ int main(int argc, char** argv) {
             else log.log("INFO", true, "Average runtime/simulation: %.1fus", avg_ms * 1000);
         }
         if (out_file) system->SaveParticles(out_file);
+        if (image_file) {
+            std::vector<uint8_t> image((size_t)image_w * image_h);
+            Check(gs_render_points(sim->Handle(), image_w, image_h, camera, image.data()));
+            Check(gs_write_ppm(image_file, image_w, image_h, image.data()));
+            log.log("INFO", false, "Wrote %ux%u image to %s", image_w, image_h, image_file);
+        }
         sim.reset();
     } catch (const Exception& e) {
         log.log("FATAL", true, "%s (status %d)", e.what(), (int)e.GetStatus());

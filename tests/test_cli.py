@@ -53,3 +53,26 @@ def test_file_roundtrip_matches_binding(gs, tmp_path, algo, extra):
     fref = str(tmp_path / "ref.txt")
     gs.write_particles(fref, p, v, m)
     assert open(fout).read() == open(fref).read()
+
+
+@pytest.mark.gpu
+def test_image_out_matches_binding(gs, orc, tmp_path):
+    """--image-out draws the final state with the start camera of the initial state,
+    widened to the image's aspect ratio."""
+    pos, vel, mass = gs.generate(gs.GEN_GALAXY, 2000, size=100.0, seed=5)
+    fin, img = str(tmp_path / "in.txt"), str(tmp_path / "frame.ppm")
+    gs.write_particles(fin, pos, vel, mass)
+    r = _run([f"--particles-in={fin}", f"--image-out={img}", "--image-size=160x90", "--simulation-algorithm=direct-sum",
+              "--simulation-count=3"])
+    assert r.returncode == 0, r.stdout + r.stderr
+    p2, v2, m2 = gs.read_particles(fin)
+    with gs.Simulation(p2, v2, m2, algorithm=gs.DIRECT_SUM) as sim:
+        cam = sim.camera_start()
+        cam[2] = cam[3] * (np.float32(160.0) / np.float32(90.0))
+        sim.run(3)
+        expect = sim.render(160, 90, cam)
+    data = open(img, "rb").read()
+    header = b"P6\n160 90\n255\n"
+    assert data.startswith(header)
+    got = np.frombuffer(data[len(header):], np.uint8).reshape(90, 160, 3)[:, :, 0]
+    assert np.array_equal(got, expect) and got.any()
