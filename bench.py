@@ -46,6 +46,11 @@ for _p in (ROOT, PKG):
 METRIC = "particle-steps/s (BH N=500k; batched/served vs plain) at <=1e-3 rel force err"
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA at 2070 MHz
 ACCURATE = 0x70  # GS_FLAGS_ACCURATE
+# DRAM bytes per launch of the traversal kernel, from one ncu capture of that workload
+FORCE_TRAFFIC_BYTES = {
+    "Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, safe radius, 64-particle group "
+    "walk) theta=0.37, softening 0.2, dt=1e-3": 53.336832e6 + 0.950784e6,
+}
 
 
 def workloads():
@@ -480,8 +485,11 @@ def roofline_of(gsim, wl, m):
         n_al = (wl["n"] + 63) // 64 * 64
         achieved = 14.0 * n_al * n_al / t / 1e12
         extra = {"kernel": "k_direct_fast", "pairs_per_step": n_al * n_al, "flop_model": "14 FLOP per pair"}
+    traffic = FORCE_TRAFFIC_BYTES.get(wl["desc"])
     r = {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-         "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": None,
+         "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": traffic,
+         "traffic_source": ("dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this "
+                            "workload (ncu --set full, profiles/k_force_group_bh500k_accurate.md)") if traffic else None,
          "peak_source": "nominal FP32 FMA rate at 2070 MHz (MEASURED_PEAKS.json has no FP32 figure)",
          "stage_ms_per_step": m["stage_ms"]}
     r.update(extra)
