@@ -358,6 +358,9 @@ typedef struct {
     uint32_t* max_stack;    /* per worker */
     uint64_t* max_inter;    /* per worker: largest per-warp interaction count */
     uint32_t group_size;    /* particles per group walk (64) */
+    float rel_alpha;        /* ORC_BH_RELATIVE_MAC: alpha, previous and new |a| per particle */
+    const float* amag_in;
+    float* amag_out;
 } walk_ctx;
 
 static void walk_warp(void* p, uint64_t item, int worker) {
@@ -479,6 +482,17 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
             gy1[b] = fmaxf(gy1[b], py[l]);
         }
     }
+    /* relative criterion: the group's smallest previous |a|; NaN if any is unknown */
+    float amin = INFINITY;
+    if (c->amag_in)
+        for (uint32_t l = 0; l < G; ++l) {
+            if (!valid[l]) continue;
+            const float a = c->amag_in[c->src[(uint32_t)w * G + l]];
+            if (isnan(a) || isnan(amin)) amin = NAN;
+            else if (a < amin) amin = a;
+        }
+    const int relative = c->amag_in && amin >= 0.0f;
+    const float tol = c->rel_alpha * amin, tol2 = tol * tol;
     uint32_t stack[GROUP_STACK_CAP + 160];
     uint32_t size = 1, max_size = 1;
     stack[0] = 0;
@@ -502,7 +516,15 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                     float ey = fmaxf(fmaxf(gy0[b] - cy, cy - gy1[b]), 0.0f);
                     d2 = fminf(d2, pair_d2(ex, ey, c->eps2));
                 }
-                accept = c->radius[n] <= d2 * c->theta2;
+                if (relative) {
+                    const float r = c->radius[n], m = c->nmass[n];
+                    const float lhs = (m * m) * ((r * r) * r);
+                    const float d4 = d2 * d2;
+                    const float rhs = tol2 * ((d4 * d4) * d2);
+                    accept = r <= d2 && lhs <= rhs;
+                } else {
+                    accept = c->radius[n] <= d2 * c->theta2;
+                }
             }
             if (accept) { /* one item: the record itself (a leaf only when the root is one) */
                 const float nx = c->npos[2 * n], ny = c->npos[2 * n + 1], nm = c->nmass[n];
@@ -557,6 +579,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
         uint32_t i = c->src[(uint32_t)w * G + l];
         float vx = c->vel_in[2 * i], vy = c->vel_in[2 * i + 1];
         const float axl = ax[l][0] + ax[l][1], ayl = ay[l][0] + ay[l][1];
+        if (c->amag_out) c->amag_out[i] = sqrtf(fmaf(axl, axl, ayl * ayl));
         float nvx = fmaf(axl, c->k, vx), nvy = fmaf(ayl, c->k, vy);
         c->pos_out[2 * i] = fmaf(vx + nvx, c->hdt, px[l]);
         c->pos_out[2 * i + 1] = fmaf(vy + nvy, c->hdt, py[l]);
@@ -1059,6 +1082,11 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
     wc.theta2 = theta2;
     wc.k = G * dt;
     wc.hdt = 0.5f * dt;
+    if ((flags & ORC_BH_RELATIVE_MAC) && out) {
+        wc.rel_alpha = out->rel_alpha;
+        wc.amag_in = out->amag_in;
+        wc.amag_out = out->amag_out;
+    }
     run_walk(&wc, nthreads, out);
 
     if (out) {

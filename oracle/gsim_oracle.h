@@ -71,6 +71,10 @@ typedef struct orc_bh_out {
     double walk_seconds;     /* force walk + integration (nthreads) */
     uint32_t max_stack;      /* deepest group-walk stack seen (ORC_BH_GROUP_WALK) */
     uint64_t max_warp_interactions; /* largest interaction count of one warp (valid lanes) */
+    /* inputs of ORC_BH_RELATIVE_MAC */
+    float rel_alpha;         /* alpha of the relative opening criterion */
+    const float* amag_in;    /* [n_al] |a| of the previous step per particle (NaN: unknown) */
+    float* amag_out;         /* [n_al] |a| of this step (written when not NULL) */
 } orc_bh_out;
 
 /* Direct sum, SimShader.comp order: for every i, sum j = 0 .. n-1 in order. */
@@ -106,6 +110,13 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
 #define ORC_BH_QUADRUPOLE 1
 #define ORC_BH_SAFE_RADIUS 2
 #define ORC_BH_GROUP_WALK 4  /* box-tested stack walk shared by 64 particles, see group_walk_warp */
+/* With ORC_BH_GROUP_WALK: relative opening criterion (not in the reference).  A node of
+ * mass m and stored squared opening radius R is accepted for a group at softened squared
+ * distance D (nearest sub-box) when R <= D and m^2 R^3 <= (alpha a_min)^2 D^5, in that
+ * FP32 operation order: lhs = (m*m)*((R*R)*R), rhs = tol^2*((D^2*D^2)*D) with
+ * tol = alpha*a_min, a_min the smallest previous |a| (without G) of the group's particles
+ * (out->amag_in); a group with an unknown |a| (NaN) uses the geometric test. */
+#define ORC_BH_RELATIVE_MAC 8
 int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in, float* vel_in,
                           float* mass_in, float* pos_out, float* vel_out, float* mass_out,
                           float dt, float G, float eps2, float theta2, orc_bh_out* out,

@@ -15,7 +15,7 @@ import numpy as np
 from . import build as _build
 
 BOX_FIXED_500, BOX_BOUNDING = 0, 1
-QUADRUPOLE, SAFE_RADIUS, GROUP_WALK = 1, 2, 4
+QUADRUPOLE, SAFE_RADIUS, GROUP_WALK, RELATIVE_MAC = 1, 2, 4, 8
 ACCURATE = QUADRUPOLE | SAFE_RADIUS | GROUP_WALK
 KEY_REMOVED = 0xFFFFFFFF
 _FP = C.POINTER(C.c_float)
@@ -31,7 +31,8 @@ class BHOut(C.Structure):
                 ("interactions", C.c_uint64), ("warp_visits", C.c_uint64),
                 ("box_center_x", C.c_float), ("box_center_y", C.c_float), ("box_scale", C.c_float),
                 ("box_radius0", C.c_float), ("build_seconds", C.c_double), ("walk_seconds", C.c_double),
-                ("max_stack", C.c_uint32), ("max_warp_interactions", C.c_uint64)]
+                ("max_stack", C.c_uint32), ("max_warp_interactions", C.c_uint64),
+                ("rel_alpha", C.c_float), ("amag_in", _FP), ("amag_out", _FP)]
 
 
 _lib = None
@@ -93,6 +94,7 @@ class State:
         self.vel = [V.copy(), V.copy()]
         self.mass = [M.copy(), M.copy()]
         self.inp = 0
+        self.amag = np.full(len(M), np.nan, np.float32)  # |a| of the last Barnes-Hut step (relative criterion)
 
     @property
     def n_al(self):
@@ -140,7 +142,7 @@ def direct_accel_f64(pos, mass, softening=0.2, targets=None, threads=os.cpu_coun
 
 
 def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, G=1.0, softening=0.2, theta=1.0,
-            keep_tree=True, threads=os.cpu_count(), walk_stride=1, flags=0):
+            keep_tree=True, threads=os.cpu_count(), walk_stride=1, flags=0, rel_alpha=0.0):
     """One Barnes-Hut step; returns a dict with keys, sorted_src and the preorder records."""
     (pi, vi, mi), (po, vo, mo) = state.sets()
     n_al = state.n_al
@@ -148,6 +150,12 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
     cap = int(L.orc_bh_node_capacity(box_mode, n_al))
     out = BHOut()
     out.walk_stride = walk_stride
+    amag_out = None
+    if flags & RELATIVE_MAC:  # |a| of this step; particles the walk skips keep their value
+        amag_out = state.amag.copy()
+        out.rel_alpha = rel_alpha
+        out.amag_in = _fp(state.amag)
+        out.amag_out = _fp(amag_out)
     res = {}
     if keep_tree:
         res = dict(keys=np.empty(n_al, np.uint32), sorted_src=np.empty(n_al, np.uint32),
@@ -173,6 +181,8 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
         L.orc_bh_sorted_step_ex(box_mode, flags, n_al, _fp(pi), _fp(vi), _fp(mi), _fp(po), _fp(vo), _fp(mo),
                                 dt_eff, G, eps2, th2, C.byref(out), threads)
     state.flip()
+    if amag_out is not None:
+        state.amag = amag_out
     t = out.tree_size
     if keep_tree:
         for k in ("skip", "radius", "pos", "mass", "quad"):

@@ -138,3 +138,61 @@ def test_accurate_mode_error_small(gs, orc):
     acc = (v1[sub].astype(np.float64) - vel[sub]) / 1e-3
     e = np.linalg.norm(acc - a64, axis=1) / np.linalg.norm(a64, axis=1)
     assert np.sqrt(np.mean(e ** 2)) < 1.5e-3
+
+
+# ---- relative opening criterion (not in the reference) ----
+def _acc_err(orc, pos, vel, mass, v1, sub, dt=1e-3):
+    P, _, M = orc.pad_state(pos, vel, mass)
+    a64 = orc.direct_accel_f64(P, M, targets=sub)
+    acc = (v1[sub].astype(np.float64) - vel[sub]) / dt
+    e = np.linalg.norm(acc - a64, axis=1) / np.linalg.norm(a64, axis=1)
+    return np.sqrt(np.mean(e ** 2))
+
+
+def test_relative_criterion_first_step_is_theta(gs, orc):
+    """With no previous |a| (NaN) every group takes the theta test: the step is the
+    theta step bit for bit, and it leaves |a| of every particle behind."""
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 5000, seed=16)
+    a, b = orc.State(pos, vel, mass), orc.State(pos, vel, mass)
+    ra = orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.4, flags=orc.ACCURATE | orc.RELATIVE_MAC, rel_alpha=0.01)
+    rb = orc.bh_step(b, box_mode=orc.BOX_BOUNDING, theta=0.4, flags=orc.ACCURATE)
+    assert ra["interactions"] == rb["interactions"]
+    for x, y in zip(a.current(), b.current()):
+        assert np.array_equal(x, y)
+    assert np.all(np.isfinite(a.amag[:5000])) and np.all(a.amag[:5000] > 0)
+    acc = (b.current()[1][:5000].astype(np.float64) - vel) / 1e-3
+    dev = np.abs(a.amag[:5000] / np.linalg.norm(acc, axis=1) - 1.0)  # velocity rounding blurs acc
+    assert np.median(dev) < 1e-4 and dev.max() < 5e-2
+
+
+def test_relative_criterion_beats_theta(gs, orc):
+    """Second step of a 100k spiral: alpha = 0.01 tests fewer records and sums fewer
+    interactions than theta = 0.37 and is more accurate."""
+    n = 100000
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, n, seed=2002)
+    st = orc.State(pos, vel, mass)
+    orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.37, flags=orc.ACCURATE | orc.RELATIVE_MAC, rel_alpha=0.01)
+    p1, v1, m1 = [x[:n].copy() for x in st.current()]
+    rel = orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.37, flags=orc.ACCURATE | orc.RELATIVE_MAC,
+                      rel_alpha=0.01, keep_tree=False)
+    geo_state = orc.State(p1, v1, m1)
+    geo = orc.bh_step(geo_state, box_mode=orc.BOX_BOUNDING, theta=0.37, flags=orc.ACCURATE, keep_tree=False)
+    sub = np.random.default_rng(3).choice(n, 1024, replace=False).astype(np.uint32)
+    e_rel = _acc_err(orc, p1, v1, m1, st.current()[1], sub)
+    e_geo = _acc_err(orc, p1, v1, m1, geo_state.current()[1], sub)
+    assert rel["interactions"] < geo["interactions"] and rel["warp_visits"] < geo["warp_visits"]
+    assert e_rel < e_geo < 1.5e-3
+
+
+def test_relative_criterion_alpha_zero_is_direct_sum(gs, orc):
+    """alpha = 0 accepts no node of nonzero mass and size: every particle sums every
+    particle leaf, as the direct sum does (to rounding)."""
+    pos, vel, mass = gs.generate(gs.GEN_UNIFORM_DISK, 900, seed=17)
+    a, b = orc.State(pos, vel, mass), orc.State(pos, vel, mass)
+    flags = orc.ACCURATE | orc.RELATIVE_MAC
+    orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.5, flags=flags, rel_alpha=0.0)
+    orc.direct_step(b)
+    a.pos[a.inp][:900], a.vel[a.inp][:900] = b.current()[:2]  # continue both from the same state
+    orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.5, flags=flags, rel_alpha=0.0)
+    orc.direct_step(b)
+    np.testing.assert_allclose(a.current()[1], b.current()[1], rtol=2e-4, atol=1e-4 * np.abs(b.current()[1]).max())
