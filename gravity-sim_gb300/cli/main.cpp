@@ -8,7 +8,8 @@
 //   - the windowed mode does not exist: every run is headless (--no-graphics is accepted);
 //   - --benchmark reports wall-clock time around the synchronised run, not clock() CPU time;
 //   - generators take --seed (the reference seeds from time(nullptr));
-//   - extra switches select this build's modes: --box=fixed|bbox, --accurate, --math=fast|reference;
+//   - extra switches select this build's modes: --box=fixed|bbox, --accurate, --relative-accuracy,
+//     --math=fast|reference;
 //   - the window's picture can be saved instead: --image-out=file.ppm writes the final state as
 //     the reference would draw it (one white pixel per particle, the start camera of the initial
 //     state, src/Main.cpp:351-352, corrected for the image's aspect ratio as at :133).
@@ -51,7 +52,9 @@ const char* kHelp =
     "\t--log-detailed: Outputs non-crucial logs.\n"
     "\t--no-graphics: Accepted for compatibility; every run is headless.\n"
     "\t--benchmark: Reports the wall-clock runtime of all simulations.\n"
-    "\t--accurate: Barnes-Hut accurate mode (quadrupoles, safe opening radius, group walk).\n";
+    "\t--accurate: Barnes-Hut accurate mode (quadrupoles, safe opening radius, group walk).\n"
+    "\t--relative-accuracy: With --accurate, open nodes by the relative criterion with this alpha\n"
+    "\t\t(0.007 gives about 1e-3 RMS force error) instead of the accuracy parameter.\n";
 
 struct Logger {
     FILE* file = nullptr;
@@ -85,6 +88,7 @@ int main(int argc, char** argv) {
     int gen = -1, algo = -1;
     float gen_size = 0, min_mass = 0, max_mass = 0, G = 1.0f, dt = 0.001f, speed = 1.0f, eps = 0.2f, theta = 1.0f;
     bool detailed = false, benchmark = false, accurate = false, have_steps = false;
+    float rel_alpha = -1.0f;  // < 0: theta criterion
     int box = GS_BOX_FIXED_500, math = GS_MATH_FAST;
     for (int i = 1; i < argc; ++i) {
         const char* a = argv[i];
@@ -117,6 +121,7 @@ int main(int argc, char** argv) {
         else if (starts(a, "--simulation-speed=", &v)) speed = std::strtof(v, nullptr);
         else if (starts(a, "--softening-len=", &v)) eps = std::strtof(v, nullptr);
         else if (starts(a, "--accuracy-parameter=", &v)) theta = std::strtof(v, nullptr);
+        else if (starts(a, "--relative-accuracy=", &v)) rel_alpha = std::strtof(v, nullptr);
         else if (starts(a, "--simulation-algorithm=", &v)) {
             if (!std::strcmp(v, "direct-sum")) algo = GS_DIRECT_SUM;
             else if (!std::strcmp(v, "barnes-hut")) algo = GS_BARNES_HUT;
@@ -147,7 +152,12 @@ int main(int argc, char** argv) {
         log.log("FATAL", true, "A valid simulation count must be given (every run is headless)!");
         return 1;
     }
+    if (rel_alpha >= 0.0f && !accurate) {
+        log.log("FATAL", true, "--relative-accuracy needs --accurate!");
+        return 1;
+    }
     uint32_t flags = accurate ? GS_FLAGS_ACCURATE : 0u;
+    if (rel_alpha >= 0.0f) flags |= GS_FLAG_RELATIVE_MAC;
     try {
         const auto sa = (ParticleSystem::SimulationAlgorithm)algo;
         std::unique_ptr<ParticleSystem> system;
@@ -158,6 +168,7 @@ int main(int argc, char** argv) {
                                             dt, speed, eps, theta, sa, seed, 0, flags));
         system->GetParams().box_mode = box;
         system->GetParams().math_mode = math;
+        if (rel_alpha >= 0.0f) system->GetParams().relative_accuracy = rel_alpha;
         log.log("INFO", false, "%zu particles (%zu aligned), algorithm %s", system->GetParticleCount(),
                 system->GetAlignedParticleCount(), algo == GS_BARNES_HUT ? "barnes-hut" : "direct-sum");
         std::unique_ptr<detail::SimulationBase> sim;

@@ -1173,7 +1173,7 @@ __device__ __forceinline__ void force_group_body(
     const float4* __restrict__ quad, const uint4* __restrict__ kids, const float2* __restrict__ pos_in,
     const float2* __restrict__ vel_in, float2* __restrict__ pos_out, float2* __restrict__ vel_out,
     float2* __restrict__ acc_rec, uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
-    unsigned long long* __restrict__ stat, int* __restrict__ err) {
+    unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t group = blk.id * kGroupWarps + warp;
     const uint32_t nv = counts[0];
@@ -1211,6 +1211,20 @@ __device__ __forceinline__ void force_group_body(
         bx1[b] = x1;
         by0[b] = y0;
         by1[b] = y1;
+    }
+    // Relative criterion: the smallest previous |a| of the group, NaN when any is unknown
+    // (then the group takes the theta test).  Each group reads and rewrites only its own
+    // particles' |a|, so one buffer serves as input and output.
+    bool relative = false;
+    float tol2 = 0.0f;
+    if (amag) {
+        const float a0 = v0 ? amag[i0] : INFINITY, a1 = v1 ? amag[i1] : INFINITY;
+        const bool unknown = __any_sync(0xffffffffu, isnan(a0) || isnan(a1));
+        float amin = fminf(a0, a1);
+        for (int o = 16; o; o >>= 1) amin = fminf(amin, __shfl_xor_sync(0xffffffffu, amin, o));
+        relative = !unknown;
+        const float tol = alpha * amin;
+        tol2 = tol * tol;
     }
     const float2 P = make_float2(p0.x, p1.x), Q = make_float2(p0.y, p1.y), E2 = make_float2(eps2, eps2);
     // node and leaf accumulators of the two particles (.x particle 0, .y particle 1)
@@ -1257,7 +1271,15 @@ __device__ __forceinline__ void force_group_body(
                 const float ey = fmaxf(fmaxf(by0[b] - q.y, q.y - by1[b]), 0.0f);
                 d2 = fminf(d2, fmaf(ex, ex, fmaf(ey, ey, eps2)));
             }
-            if (q.w <= d2 * theta2) {
+            bool accept;
+            if (relative) {  // m^2 R^3 <= tol^2 D^5 with R <= D (R: squared opening radius)
+                const float lhs = (q.z * q.z) * ((q.w * q.w) * q.w);
+                const float d4 = d2 * d2;
+                accept = q.w <= d2 && lhs <= tol2 * ((d4 * d4) * d2);
+            } else {
+                accept = q.w <= d2 * theta2;
+            }
+            if (accept) {
                 nn = 1;
             } else if (kd.x == kKidFinest) {
                 a0 = kd.y;
@@ -1342,6 +1364,10 @@ __device__ __forceinline__ void force_group_body(
         }
     }
     const float2 ax = add2(anx, alx), ay = add2(any, aly);  // node + leaf, per particle
+    if (amag) {
+        if (v0) amag[i0] = __fsqrt_rn(fmaf(ax.x, ax.x, ay.x * ay.x));
+        if (v1) amag[i1] = __fsqrt_rn(fmaf(ax.y, ax.y, ay.y * ay.y));
+    }
     if (v0) {
         if (acc_rec) acc_rec[i0] = make_float2(ax.x, ay.x);
         const float2 v = vel_in[i0];
@@ -1365,12 +1391,12 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
               const uint4* __restrict__ kids, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
               float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
               uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
-              unsigned long long* __restrict__ stat, int* __restrict__ err) {
+              unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha) {
     pdl_enter();
     __shared__ GroupSmem smem[kGroupWarps];
     force_group_body<EXACT, QUAD, COUNT>(grid_blk(), smem[threadIdx.x >> 5], sidx, skey, counts, rec, skip, quad,
                                          kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2, theta2, k, hdt,
-                                         cap, stat, err);
+                                         cap, stat, err, amag, alpha);
 }
 
 int grid_for(uint64_t n, int threads) {
@@ -1420,6 +1446,8 @@ void bh_carve(gs_sim* s) {
     sim_carve(s, (void**)&w.node_slot, w.cap * sizeof(uint32_t));
     w.quad = nullptr;
     if (s->p.flags & GS_FLAG_QUADRUPOLE) sim_carve(s, (void**)&w.quad, w.cap * sizeof(float4));
+    w.amag = nullptr;
+    if (s->p.flags & GS_FLAG_RELATIVE_MAC) sim_carve(s, (void**)&w.amag, n * sizeof(float));
     sim_carve(s, (void**)&w.bbox_part, kBBoxBlocks * 4 * sizeof(float));
     sim_carve(s, (void**)&w.params, sizeof(BHParams));
     // one block cleared per step: hist | counters | sort status | scan status
@@ -1573,7 +1601,8 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
         GS_TRY_LAUNCH(launch(fpdl, fn, blocks, kGroupWarps * 32, st, sidx, skey, (const uint32_t*)(ctr + kCtrValid),
                              (const float4*)w.rec, (const uint32_t*)w.skip, (const float4*)w.quad,
                              (const uint4*)w.kids, (const float2*)s->pos[in], (const float2*)s->vel[in], s->pos[out],
-                             s->vel[out], s->acc, n, s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err));
+                             s->vel[out], s->acc, n, s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err,
+                             w.amag, s->p.relative_accuracy));
     } else {
         auto fn = exact ? (count ? k_force<true, true> : k_force<true, false>)
                         : (count ? k_force<false, true> : k_force<false, false>);
@@ -1814,7 +1843,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kb_force_group(BatchArgs a, 
                                              d.counters + kCtrValid, d.rec, d.skip, d.quad, d.kids, d.pos[bb.in],
                                              d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2,
                                              d.theta2, d.k, d.hdt, d.cap,
-                                             (unsigned long long*)(d.counters + kCtrStat), d.err);
+                                             (unsigned long long*)(d.counters + kCtrStat), d.err, d.amag, d.alpha);
     }
 }
 
@@ -1858,6 +1887,8 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
 
     d.msum = w.msum;
     d.quad = w.quad;
+    d.amag = w.amag;
+    d.alpha = s->p.relative_accuracy;
     d.kids = w.kids;
     d.levels = w.levels;
     d.nodeinfo = w.nodeinfo;

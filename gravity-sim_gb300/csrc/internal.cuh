@@ -71,6 +71,7 @@ struct BHWork {
     uint32_t* skip = nullptr;          // [cap + 32]
     float2* msum = nullptr;            // [cap]
     float4* quad = nullptr;            // [cap] {sxx, sxy, syy, -} (GS_FLAG_QUADRUPOLE)
+    float* amag = nullptr;             // [n_al] |a| of the last step, NaN: unknown (GS_FLAG_RELATIVE_MAC)
     uint4* kids = nullptr;             // [cap] child descriptors of internal records
     uint32_t* levels = nullptr;        // internal records by level (level_off / level_cap in bh.cu)
     uint2* nodeinfo = nullptr;         // [cap] {a key of the cell, level} of an internal record
@@ -114,6 +115,8 @@ struct SysDesc {
     uint32_t* skip;
     float2* msum;
     float4* quad;
+    float* amag;      // relative criterion: |a| per particle, or null for the theta test
+    float alpha;
     uint4* kids;
     uint32_t* levels;
     uint2* nodeinfo;

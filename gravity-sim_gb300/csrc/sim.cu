@@ -8,6 +8,7 @@
 // Instead of re-recording command buffers, each parity of the ping-pong is captured
 // once into a CUDA graph and replayed.
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -172,6 +173,8 @@ gs_status upload(gs_sim* s, const float* pos, const float* vel, const float* mas
     GS_CUDA(cudaMemcpyAsync(s->vel[b], s->vel[a], s->n_al * sizeof(float2), cudaMemcpyDeviceToDevice, s->stream));
     GS_CUDA(cudaMemcpyAsync(s->mass[0], mass, n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     if (pad) GS_CUDA(cudaMemsetAsync(s->mass[0] + n, 0, pad * sizeof(float), s->stream));
+    // no previous |a| yet: all-ones words are NaN, so the next step uses the theta test
+    if (s->bh.amag) GS_CUDA(cudaMemsetAsync(s->bh.amag, 0xFF, s->n_al * sizeof(float), s->stream));
     GS_CUDA(cudaStreamSynchronize(s->stream));
     return GS_OK;
 }
@@ -212,6 +215,7 @@ void gs_params_init(gs_params* p) {
     p->math_mode = GS_MATH_FAST;
     p->device = 0;
     p->flags = 0;
+    p->relative_accuracy = 0.007f;
 }
 
 const char* gs_status_string(gs_status s) {
@@ -263,6 +267,12 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
         return invalid("gs_create: invalid math_mode");
     if ((params->flags & GS_FLAG_QUADRUPOLE) && !(params->flags & GS_FLAG_GROUP_WALK))
         return invalid("gs_create: GS_FLAG_QUADRUPOLE needs GS_FLAG_GROUP_WALK");
+    if ((params->flags & GS_FLAG_RELATIVE_MAC) &&
+        (~params->flags & (GS_FLAG_GROUP_WALK | GS_FLAG_QUADRUPOLE)))
+        return invalid("gs_create: GS_FLAG_RELATIVE_MAC needs GS_FLAG_GROUP_WALK and GS_FLAG_QUADRUPOLE");
+    if ((params->flags & GS_FLAG_RELATIVE_MAC) &&
+        !(params->relative_accuracy >= 0.0f && params->relative_accuracy < INFINITY))
+        return invalid("gs_create: relative_accuracy must be finite and >= 0");
     if ((params->flags & GS_FLAG_PLAIN_SUM) && params->algorithm != GS_DIRECT_SUM)
         return invalid("gs_create: GS_FLAG_PLAIN_SUM applies to direct sum only");
     if ((params->flags & (GS_FLAG_QUADRUPOLE | GS_FLAG_SAFE_RADIUS | GS_FLAG_GROUP_WALK)) &&

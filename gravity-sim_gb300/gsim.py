@@ -34,6 +34,7 @@ EXPORTS = (
     "gs_render_points", "gs_snapshot_take", "gs_snapshot_positions", "gs_snapshot_render", "gs_write_ppm",
 )
 FLAG_PLAIN_SUM = 0x80
+FLAG_RELATIVE_MAC = 0x100
 SERVE_FIFO, SERVE_SHORTEST_FIRST = 0, 1
 REQUEST_QUEUED, REQUEST_RESIDENT, REQUEST_DONE, REQUEST_FAILED = 0, 1, 2, 3
 BATCH_NO_GRAPH = 0x1
@@ -44,7 +45,8 @@ class Params(C.Structure):
     _fields_ = [("gravitational_const", C.c_float), ("simulation_time", C.c_float),
                 ("simulation_speed", C.c_float), ("softening_len", C.c_float),
                 ("accuracy_parameter", C.c_float), ("algorithm", C.c_int32), ("box_mode", C.c_int32),
-                ("math_mode", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32)]
+                ("math_mode", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32),
+                ("relative_accuracy", C.c_float)]
 
 
 class Stats(C.Structure):

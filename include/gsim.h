@@ -74,8 +74,9 @@ typedef enum gs_math_mode { GS_MATH_FAST = 0, GS_MATH_REFERENCE = 1 } gs_math_mo
  *   QUADRUPOLE   second central moments per node, quadrupole term for accepted nodes
  *   SAFE_RADIUS  opening radius = squared distance from the centre of mass to the
  *                farthest cell corner (equals s^2/2 for a centred mass)
- *   GROUP_WALK   each warp's 32 particles share one walk that tests records against the
- *                group's bounding box, 32 at a time, and sums interaction items densely
+ *   GROUP_WALK   each warp's 64 particles (two per lane) share one walk that tests
+ *                records against up to four sub-boxes of the group, 32 records at a
+ *                time, and sums interaction items densely
  * GS_FLAGS_ACCURATE sets all three (theta = 0.35 gives <= 1e-3 RMS force error on the
  * 500k spiral). */
 #define GS_FLAG_QUADRUPOLE 0x10u
@@ -85,6 +86,17 @@ typedef enum gs_math_mode { GS_MATH_FAST = 0, GS_MATH_REFERENCE = 1 } gs_math_mo
 /* Direct sum, FAST math: add the 64-wide tile partials and the j-chunks plainly instead
  * of with Kahan compensation (the precision study's uncompensated variant). */
 #define GS_FLAG_PLAIN_SUM 0x80u
+/* Barnes-Hut with GS_FLAG_GROUP_WALK and GS_FLAG_QUADRUPOLE: open nodes by the relative
+ * criterion instead of theta.  A node of mass m and opening radius r (the stored squared
+ * radius R = r^2) is accepted for a group at softened squared distance D = d^2 + eps^2
+ * from the group's nearest sub-box when
+ *     R <= D   and   m^2 R^3 <= (alpha a_min)^2 D^5
+ * i.e. m r^3 / d^5 (the size of the first term a quadrupole expansion leaves out) is at
+ * most alpha times the smallest |a| the group's particles had in the previous step
+ * (without G).  alpha is gs_params.relative_accuracy.  A step with no previous |a|
+ * for some particle of the group (the first step after gs_create or
+ * gs_set_particles) uses the theta test for that group. */
+#define GS_FLAG_RELATIVE_MAC 0x100u
 
 typedef struct gs_params {
     float gravitational_const; /* ParticleSystem::GetGravitationalConst, default 1 (src/Main.cpp:59) */
@@ -97,6 +109,8 @@ typedef struct gs_params {
     int32_t math_mode;         /* gs_math_mode */
     int32_t device;            /* CUDA device ordinal */
     uint32_t flags;            /* GS_FLAG_* */
+    float relative_accuracy;   /* alpha of GS_FLAG_RELATIVE_MAC, default 0.007 (<= 1e-3 RMS force
+                                  error on the 500k spiral) */
 } gs_params;
 
 typedef struct gs_sim gs_sim;

@@ -147,3 +147,22 @@ def test_tuner_smoke(gs):
     assert 1 <= len(t["n"]) <= 4
     assert all(x > 0 for x in t["direct_ms"] + t["bh_ms"])
     assert 1024 <= t["crossover"] <= 8192
+
+
+def test_relative_criterion_batch_bit_identical(gs):
+    """Members with the relative opening criterion and different alphas: each keeps its
+    own |a| buffer and alpha in the batch and matches its twin stepped alone, through a
+    first step (theta test) and later ones (relative test)."""
+    rel = dict(algorithm=1, box_mode=1, flags=0x170 | 0x8, accuracy_parameter=0.5)
+    specs = [(17, 30000, 100.0, dict(rel, relative_accuracy=0.007)),
+             (16, 5000, 100.0, dict(rel, relative_accuracy=0.02)),
+             (17, 700, 100.0, dict(rel, relative_accuracy=0.001)), (16, 2000, 100.0, DIRECT)]
+    alone = _make(gs, specs, 1500)
+    batched = _make(gs, specs, 1500)
+    for s in alone + batched:
+        s.reset_stats()
+    _run_alone(alone, 3)
+    with gs.Batch(batched) as b:
+        b.run(3)
+        b.sync()
+        _assert_same(alone, batched, specs)

@@ -202,3 +202,71 @@ def test_accurate_500k_error_gate(gs, orc):
           f"p99 {np.quantile(err, 0.99):.3e} max {err.max():.3e}")
     assert np.sqrt(np.mean(err ** 2)) <= 1e-3
     assert np.max(np.linalg.norm(res[gs.MATH_FAST] - res[gs.MATH_REFERENCE], axis=1) / den) < 3e-5
+
+
+# ---- relative opening criterion (GS_FLAG_RELATIVE_MAC; not in the reference) ----
+REL = ACC | 0x100
+
+
+@pytest.mark.parametrize("box", [0, 1])
+@pytest.mark.parametrize("kind,n,size,alpha", [(17, 3000, 100.0, 0.007), (2, 2500, 700.0, 0.02),
+                                               (16, 64, 100.0, 0.007), (0, 777, 100.0, 0.0)])
+def test_relative_criterion_bit_exact(gs, orc, box, kind, n, size, alpha):
+    """REFERENCE math over three steps (the first takes the theta test, the next ones the
+    relative test on the |a| the step before left), then again after gs_set_particles,
+    which forgets |a|: state, interaction and visit counts bit-identical to the oracle."""
+    pos, vel, mass = gs.generate(kind, n, size=size, seed=43)
+    st = orc.State(pos, vel, mass)
+    flags = orc.ACCURATE | orc.RELATIVE_MAC
+    with _sim(gs, pos, vel, mass, box_mode=box, math_mode=gs.MATH_REFERENCE, accuracy_parameter=0.35,
+              relative_accuracy=alpha, flags=REL | gs.FLAG_COUNT_INTERACTIONS) as sim:
+        for step in range(4):
+            if step == 3:
+                sim.set_particles(pos, vel, mass)
+                st = orc.State(pos, vel, mass)
+            sim.reset_stats()
+            sim.run(1)
+            o = orc.bh_step(st, box_mode=box, theta=0.35, flags=flags, rel_alpha=alpha)
+            s = sim.stats()
+            assert (s.interactions, s.warp_visits) == (o["interactions"], o["warp_visits"]), step
+            for g, c in zip(sim.get_particles(), st.current()):
+                np.testing.assert_array_equal(g, c)
+
+
+def test_relative_criterion_500k_error_gate(gs):
+    """N=500,000 spiral, bounding box, alpha=0.007: the second step (the first with a
+    previous |a|) has RMS relative force error <= 1e-3 against the FP64 direct sum on 4096
+    particles, with fewer interactions than theta=0.37."""
+    n = 500000
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, n, seed=2002)
+    sub = np.random.default_rng(0).choice(n, 4096, replace=False).astype(np.uint32)
+    counts = {}
+    for rel in (True, False):
+        flags = (REL if rel else ACC) | gs.FLAG_RECORD_ACCEL | gs.FLAG_COUNT_INTERACTIONS
+        with _sim(gs, pos, vel, mass, box_mode=1, accuracy_parameter=0.37, relative_accuracy=0.007,
+                  flags=flags) as sim:
+            sim.run(1)
+            p1, v1, m1 = sim.get_particles()
+            sim.reset_stats()
+            sim.run(1)
+            counts[rel] = sim.stats().interactions
+            if rel:
+                acc = sim.get_accel()[sub].astype(np.float64)
+                sim.set_particles(p1, v1, m1)
+                a64 = sim.accel_f64(sub)
+    err = np.linalg.norm(acc - a64, axis=1) / np.linalg.norm(a64, axis=1)
+    print(f"relative criterion: rms {np.sqrt(np.mean(err**2)):.3e} p99 {np.quantile(err, 0.99):.3e} "
+          f"interactions {counts[True] / n:.0f} vs theta {counts[False] / n:.0f} per particle")
+    assert np.sqrt(np.mean(err ** 2)) <= 1e-3
+    assert counts[True] < 0.92 * counts[False]
+
+
+def test_relative_criterion_needs_accurate_walk(gs):
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 1000, seed=1)
+    for flags in (0x100, 0x100 | 0x40 | 0x20, 0x100 | 0x10 | 0x20):  # no quadrupoles / no group walk
+        with pytest.raises(gs.GsimError):
+            _sim(gs, pos, vel, mass, flags=flags)
+    with pytest.raises(gs.GsimError):
+        _sim(gs, pos, vel, mass, flags=REL, relative_accuracy=float("nan"))
+    with pytest.raises(gs.GsimError):
+        _sim(gs, pos, vel, mass, flags=REL, relative_accuracy=-1.0)
