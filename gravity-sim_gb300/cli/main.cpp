@@ -53,8 +53,8 @@ const char* kHelp =
     "\t--no-graphics: Accepted for compatibility; every run is headless.\n"
     "\t--benchmark: Reports the wall-clock runtime of all simulations.\n"
     "\t--accurate: Barnes-Hut accurate mode (quadrupoles, safe opening radius, group walk).\n"
-    "\t--relative-accuracy: With --accurate, open nodes by the relative criterion with this alpha\n"
-    "\t\t(0.007 gives about 1e-3 RMS force error) instead of the accuracy parameter.\n";
+    "\t--relative-accuracy: With --accurate, open nodes by the relative criterion with this alpha,\n"
+    "\t\tthe accuracy parameter as its floor (0.006 with 0.3: about 1e-3 RMS force error).\n";
 
 struct Logger {
     FILE* file = nullptr;

@@ -1272,10 +1272,10 @@ __device__ __forceinline__ void force_group_body(
                 d2 = fminf(d2, fmaf(ex, ex, fmaf(ey, ey, eps2)));
             }
             bool accept;
-            if (relative) {  // m^2 R^3 <= tol^2 D^5 with R <= D (R: squared opening radius)
+            if (relative) {  // m^2 R^3 <= tol^2 D^5 with R <= D (R: squared opening radius), or theta
                 const float lhs = (q.z * q.z) * ((q.w * q.w) * q.w);
                 const float d4 = d2 * d2;
-                accept = q.w <= d2 && lhs <= tol2 * ((d4 * d4) * d2);
+                accept = (q.w <= d2 && lhs <= tol2 * ((d4 * d4) * d2)) || q.w <= d2 * theta2;
             } else {
                 accept = q.w <= d2 * theta2;
             }

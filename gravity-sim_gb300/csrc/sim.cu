@@ -215,7 +215,7 @@ void gs_params_init(gs_params* p) {
     p->math_mode = GS_MATH_FAST;
     p->device = 0;
     p->flags = 0;
-    p->relative_accuracy = 0.007f;
+    p->relative_accuracy = 0.006f;
 }
 
 const char* gs_status_string(gs_status s) {

@@ -521,7 +521,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                     const float lhs = (m * m) * ((r * r) * r);
                     const float d4 = d2 * d2;
                     const float rhs = tol2 * ((d4 * d4) * d2);
-                    accept = r <= d2 && lhs <= rhs;
+                    accept = (r <= d2 && lhs <= rhs) || r <= d2 * c->theta2;
                 } else {
                     accept = c->radius[n] <= d2 * c->theta2;
                 }

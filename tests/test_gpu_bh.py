@@ -234,17 +234,17 @@ def test_relative_criterion_bit_exact(gs, orc, box, kind, n, size, alpha):
 
 
 def test_relative_criterion_500k_error_gate(gs):
-    """N=500,000 spiral, bounding box, alpha=0.007: the second step (the first with a
-    previous |a|) has RMS relative force error <= 1e-3 against the FP64 direct sum on 4096
-    particles, with fewer interactions than theta=0.37."""
+    """N=500,000 spiral, bounding box, alpha=0.006 with theta=0.3 as the floor: the second
+    step (the first with a previous |a|) has RMS relative force error <= 1e-3 against the
+    FP64 direct sum on 4096 particles, with fewer interactions than theta=0.35 alone."""
     n = 500000
     pos, vel, mass = gs.generate(gs.GEN_SPIRAL, n, seed=2002)
     sub = np.random.default_rng(0).choice(n, 4096, replace=False).astype(np.uint32)
     counts = {}
     for rel in (True, False):
         flags = (REL if rel else ACC) | gs.FLAG_RECORD_ACCEL | gs.FLAG_COUNT_INTERACTIONS
-        with _sim(gs, pos, vel, mass, box_mode=1, accuracy_parameter=0.37, relative_accuracy=0.007,
-                  flags=flags) as sim:
+        with _sim(gs, pos, vel, mass, box_mode=1, accuracy_parameter=0.3 if rel else 0.35,
+                  relative_accuracy=0.006, flags=flags) as sim:
             sim.run(1)
             p1, v1, m1 = sim.get_particles()
             sim.reset_stats()
@@ -258,7 +258,7 @@ def test_relative_criterion_500k_error_gate(gs):
     print(f"relative criterion: rms {np.sqrt(np.mean(err**2)):.3e} p99 {np.quantile(err, 0.99):.3e} "
           f"interactions {counts[True] / n:.0f} vs theta {counts[False] / n:.0f} per particle")
     assert np.sqrt(np.mean(err ** 2)) <= 1e-3
-    assert counts[True] < 0.92 * counts[False]
+    assert counts[True] < 0.85 * counts[False]
 
 
 def test_relative_criterion_needs_accurate_walk(gs):

@@ -166,33 +166,34 @@ def test_relative_criterion_first_step_is_theta(gs, orc):
 
 
 def test_relative_criterion_beats_theta(gs, orc):
-    """Second step of a 100k spiral: alpha = 0.01 tests fewer records and sums fewer
-    interactions than theta = 0.37 and is more accurate."""
+    """Second step of a 100k spiral: alpha = 0.006 with theta = 0.3 as the floor tests
+    fewer records, sums fewer interactions and is more accurate than theta = 0.35 alone."""
     n = 100000
     pos, vel, mass = gs.generate(gs.GEN_SPIRAL, n, seed=2002)
     st = orc.State(pos, vel, mass)
-    orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.37, flags=orc.ACCURATE | orc.RELATIVE_MAC, rel_alpha=0.01)
+    orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.3, flags=orc.ACCURATE | orc.RELATIVE_MAC, rel_alpha=0.006)
     p1, v1, m1 = [x[:n].copy() for x in st.current()]
-    rel = orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.37, flags=orc.ACCURATE | orc.RELATIVE_MAC,
-                      rel_alpha=0.01, keep_tree=False)
+    rel = orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.3, flags=orc.ACCURATE | orc.RELATIVE_MAC,
+                      rel_alpha=0.006, keep_tree=False)
     geo_state = orc.State(p1, v1, m1)
-    geo = orc.bh_step(geo_state, box_mode=orc.BOX_BOUNDING, theta=0.37, flags=orc.ACCURATE, keep_tree=False)
+    geo = orc.bh_step(geo_state, box_mode=orc.BOX_BOUNDING, theta=0.35, flags=orc.ACCURATE, keep_tree=False)
     sub = np.random.default_rng(3).choice(n, 1024, replace=False).astype(np.uint32)
     e_rel = _acc_err(orc, p1, v1, m1, st.current()[1], sub)
     e_geo = _acc_err(orc, p1, v1, m1, geo_state.current()[1], sub)
+    print(f"relative {e_rel:.3e} {rel['interactions'] / n:.0f}/particle, theta {e_geo:.3e} {geo['interactions'] / n:.0f}")
     assert rel["interactions"] < geo["interactions"] and rel["warp_visits"] < geo["warp_visits"]
-    assert e_rel < e_geo < 1.5e-3
+    assert e_rel < e_geo < 1e-3
 
 
 def test_relative_criterion_alpha_zero_is_direct_sum(gs, orc):
-    """alpha = 0 accepts no node of nonzero mass and size: every particle sums every
-    particle leaf, as the direct sum does (to rounding)."""
+    """alpha = 0 with theta = 0 accepts no node of nonzero mass and size: every particle
+    sums every particle leaf, as the direct sum does (to rounding)."""
     pos, vel, mass = gs.generate(gs.GEN_UNIFORM_DISK, 900, seed=17)
     a, b = orc.State(pos, vel, mass), orc.State(pos, vel, mass)
     flags = orc.ACCURATE | orc.RELATIVE_MAC
-    orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.5, flags=flags, rel_alpha=0.0)
+    orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.0, flags=flags, rel_alpha=0.0)
     orc.direct_step(b)
     a.pos[a.inp][:900], a.vel[a.inp][:900] = b.current()[:2]  # continue both from the same state
-    orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.5, flags=flags, rel_alpha=0.0)
+    orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.0, flags=flags, rel_alpha=0.0)
     orc.direct_step(b)
     np.testing.assert_allclose(a.current()[1], b.current()[1], rtol=2e-4, atol=1e-4 * np.abs(b.current()[1]).max())
