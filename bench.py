@@ -4,16 +4,19 @@ Headline workload: Barnes-Hut, N = 500,000 spiral galaxy (exponential disk, scal
 r <= 100, two-arm logarithmic spiral, pitch 15 deg, amplitude 0.3, circular velocities
 from the enclosed mass + 5% dispersion, masses U[1,10]), softening 0.2, dt = 1e-3,
 seeded synthetic input, gated at <= 1e-3 RMS relative force error against the FP64
-direct sum: accurate mode (bounding box, quadrupoles, safe opening radius, group walk),
-theta = 0.37.  The reference's own opening rule at theta = 1 (fixed +-500 box,
-monopoles, warp vote) is measured beside it with its error; it does not meet the gate.
-A step is one simulation step of the whole system.
+direct sum at every measured step: accurate mode (bounding box, quadrupoles, safe opening
+radius, group walk) with the relative opening criterion, alpha = 0.006 and theta = 0.3 as
+its floor.  Beside it: the same accurate mode with the geometric criterion alone at
+theta = 0.35 (the cheapest theta that holds the gate at every step), and the reference's
+own opening rule at theta = 1 (fixed +-500 box, monopoles, warp vote) with its error; the
+latter does not meet the gate.  A step is one simulation step of the whole system.
 
   value  particle-steps/s, device time (CUDA events on the simulation's stream), state
          resident in HBM; L2 flushed (256 MiB write) before every timed step
   e2e    the same metric through the C ABI with host buffers: every step uploads the
          state from pinned host memory (gs_set_particles), runs one step (gs_run) and
-         reads the state back (gs_get_particles), host wall clock
+         reads the state back (gs_get_particles), host wall clock.  An upload forgets
+         the previous |a|, so these steps open nodes by the theta floor alone
   roofline  the traversal kernel: algorithmic FLOP of the accepted interactions
          (14 per monopole, 37 per quadrupole) over its CUDA-event time, against the
          FP32 FMA rate
@@ -46,11 +49,9 @@ for _p in (ROOT, PKG):
 METRIC = "particle-steps/s (BH N=500k; batched/served vs plain) at <=1e-3 rel force err"
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA at 2070 MHz
 ACCURATE = 0x70  # GS_FLAGS_ACCURATE
+RELATIVE = 0x100  # GS_FLAG_RELATIVE_MAC
 # DRAM bytes per launch of the traversal kernel, from one ncu capture of that workload
-FORCE_TRAFFIC_BYTES = {
-    "Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, safe radius, 64-particle group "
-    "walk) theta=0.37, softening 0.2, dt=1e-3": 53.336832e6 + 0.950784e6,
-}
+FORCE_TRAFFIC_BYTES = {}
 
 
 def workloads():
@@ -58,9 +59,15 @@ def workloads():
 
     spiral = dict(algo=gsim.BARNES_HUT, gen=gsim.GEN_SPIRAL, n=500000, size=100.0, seed=2002)
     return {
-        "bh500k": dict(spiral, box=gsim.BOX_BOUNDING, theta=0.37, flags=ACCURATE, oracle_flags=7,
+        "bh500k": dict(spiral, box=gsim.BOX_BOUNDING, theta=0.3, alpha=0.006, flags=ACCURATE | RELATIVE,
+                       oracle_flags=15,
                        desc="Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, safe "
-                            "radius, 64-particle group walk) theta=0.37, softening 0.2, dt=1e-3"),
+                            "radius, 64-particle group walk), relative opening criterion alpha=0.006 with "
+                            "theta=0.3 floor, softening 0.2, dt=1e-3"),
+        "bh500k-theta": dict(spiral, box=gsim.BOX_BOUNDING, theta=0.35, flags=ACCURATE, oracle_flags=7,
+                             desc="Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, "
+                                  "safe radius, 64-particle group walk), geometric criterion theta=0.35, "
+                                  "softening 0.2, dt=1e-3"),
         "bh500k-reference-rule": dict(spiral, box=gsim.BOX_FIXED_500, theta=1.0, flags=0, oracle_flags=0,
                                       desc="Barnes-Hut N=500000 spiral galaxy, the reference's opening rule "
                                            "(fixed +-500 box, monopoles, warp vote) theta=1, softening 0.2, dt=1e-3"),
@@ -159,16 +166,38 @@ def reduce_op(dist, x, op):
 
 def make_params(gsim, wl, local, flags):
     return gsim.default_params(algorithm=wl["algo"], box_mode=wl["box"], accuracy_parameter=wl["theta"],
-                               device=local, flags=wl["flags"] | flags)
+                               relative_accuracy=wl.get("alpha", 0.0), device=local, flags=wl["flags"] | flags)
+
+
+def step_errors(gsim, params, pos, vel, mass, sub, steps):
+    """Relative force error against the FP64 direct sum on the particles `sub`, for each
+    of `steps` consecutive steps after one warm step (which leaves the previous |a| that
+    the relative criterion needs).  FP64 forces of each step's starting state come from a
+    direct-sum system holding that state (gs_accel_f64)."""
+    p = gsim.Params.from_buffer_copy(params)
+    p.flags |= gsim.FLAG_RECORD_ACCEL
+    d = gsim.default_params(algorithm=gsim.DIRECT_SUM, device=p.device)
+    errs = []
+    with gsim.Simulation(pos, vel, mass, params=p) as es:
+        es.run(1)
+        for _ in range(steps):
+            start = es.get_particles()
+            es.run(1)
+            acc = es.get_accel()[sub].astype(np.float64)
+            with gsim.Simulation(*start, params=d) as fs:
+                a64 = fs.accel_f64(sub)
+            errs.append(np.linalg.norm(acc - a64, axis=1) / np.maximum(np.linalg.norm(a64, axis=1), 1e-30))
+    return errs
 
 
 def interaction_counts(gsim, wl, pos, vel, mass, local):
-    """Tree and interaction counts of one step, from a separate simulation built with
-    GS_FLAG_COUNT_INTERACTIONS (the counting kernels are not the timed ones)."""
+    """Tree and interaction counts of the second step (the first with a previous |a|),
+    from a separate simulation built with GS_FLAG_COUNT_INTERACTIONS (the counting
+    kernels are not the timed ones)."""
     if wl["algo"] != gsim.BARNES_HUT:
         return {}
     with gsim.Simulation(pos, vel, mass, params=make_params(gsim, wl, local, gsim.FLAG_COUNT_INTERACTIONS)) as cs:
-        cs.run(1)
+        cs.run(2)
         st = cs.stats()
         return {"interactions": int(st.interactions), "tests": int(st.warp_visits),
                 "tree_records": int(st.tree_records), "internal_nodes": int(st.internal_nodes),
@@ -225,7 +254,7 @@ def measure(gsim, torch, wl, pos, vel, mass, args, local, dist, sample_clocks):
 
 BATCH_DESC = ("512 independent systems, N log-uniform in [1024, 262144] (seed 1004), each a uniform disk "
               "(r=100) or a spiral galaxy with p=0.5; direct sum (Kahan FP32) below the tuned crossover N, "
-              "Barnes-Hut accurate mode theta=%g above it; softening 0.2, dt=1e-3")
+              "Barnes-Hut accurate mode (%s) above it; softening 0.2, dt=1e-3")
 
 
 def batch_specs(count=512, seed=1004, lo=1024, hi=262144):
@@ -237,11 +266,18 @@ def batch_specs(count=512, seed=1004, lo=1024, hi=262144):
     return [(int(k), int(x), seed * 1000 + j) for j, (k, x) in enumerate(zip(kind, n))]
 
 
-def batch_params(gsim, local, n, crossover, theta, flags=0):
+def batch_params(gsim, local, n, crossover, theta, alpha, flags=0):
+    """Direct sum below the crossover; above it accurate-mode Barnes-Hut with the relative
+    criterion (alpha > 0, theta its floor) or theta alone (alpha = 0)."""
     if n < crossover:
         return gsim.default_params(algorithm=gsim.DIRECT_SUM, device=local, flags=flags)
     return gsim.default_params(algorithm=gsim.BARNES_HUT, box_mode=gsim.BOX_BOUNDING, accuracy_parameter=theta,
-                               device=local, flags=ACCURATE | flags)
+                               relative_accuracy=alpha, device=local,
+                               flags=ACCURATE | (RELATIVE if alpha > 0 else 0) | flags)
+
+
+def bh_mode_desc(theta, alpha):
+    return (f"relative criterion alpha={alpha:g} with theta={theta:g} floor" if alpha > 0 else f"theta={theta:g}")
 
 
 def measure_batched(gsim, torch, args, local):
@@ -250,15 +286,15 @@ def measure_batched(gsim, torch, args, local):
     each with its own step graph), both timed with CUDA events on the device."""
     t_setup = time.perf_counter()
     d = gsim.default_params(algorithm=gsim.DIRECT_SUM, device=local)
-    theta = args.batch_theta
-    h = batch_params(gsim, local, 1 << 30, 0, theta)
+    theta, alpha = args.batch_theta, args.batch_alpha
+    h = batch_params(gsim, local, 1 << 30, 0, theta, alpha)
     tune = gsim.tune_crossover(d, h, min_n=1024, max_n=262144, particles_per_probe=1 << 21, seed=4000)
     xo = tune["crossover"]
     specs = batch_specs()
     sims = []
     for kind, n, seed in specs:
         pos, vel, mass = gsim.generate(kind, n, size=100.0, seed=seed)
-        sims.append(gsim.Simulation(pos, vel, mass, params=batch_params(gsim, local, n, xo, theta)))
+        sims.append(gsim.Simulation(pos, vel, mass, params=batch_params(gsim, local, n, xo, theta, alpha)))
     total_n = float(sum(n for _, n, _ in specs))
     n_bh = sum(1 for _, n, _ in specs if n >= xo)
     setup_s = time.perf_counter() - t_setup
@@ -303,20 +339,15 @@ def measure_batched(gsim, torch, args, local):
         dev_p += a.elapsed_time(z) / 1e3
     wall_p = time.perf_counter() - w0  # includes the warm-up steps
 
-    # force error of a sample of members (one step from the current state vs FP64)
+    # force error of a sample of members (from the current state: a warm step, then the
+    # next step against FP64)
     errs = []
     rng = np.random.default_rng(1)
     for j in sorted(rng.choice(len(sims), 8, replace=False)):
         kind, n, seed = specs[j]
         pos, vel, mass = sims[j].get_particles()
-        with gsim.Simulation(pos, vel, mass, params=batch_params(gsim, local, n, xo, theta,
-                                                                 gsim.FLAG_RECORD_ACCEL)) as es:
-            es.run(1)
-            acc = es.get_accel().astype(np.float64)
-            es.set_particles(pos, vel, mass)
-            sub = rng.choice(n, min(1024, n), replace=False).astype(np.uint32)
-            a64 = es.accel_f64(sub)
-        e = np.linalg.norm(acc[sub] - a64, axis=1) / np.maximum(np.linalg.norm(a64, axis=1), 1e-30)
+        sub = rng.choice(n, min(1024, n), replace=False).astype(np.uint32)
+        e = step_errors(gsim, batch_params(gsim, local, n, xo, theta, alpha), pos, vel, mass, sub, 1)[0]
         errs.append({"n": n, "kind": "spiral" if kind == gsim.GEN_SPIRAL else "uniform disk",
                      "algorithm": "barnes-hut" if n >= xo else "direct", "rms": float(np.sqrt(np.mean(e ** 2))),
                      "max": float(e.max())})
@@ -324,7 +355,7 @@ def measure_batched(gsim, torch, args, local):
         s.close()
     value = total_n * steps / dev_b
     plain = total_n * steps / dev_p
-    return {"workload": BATCH_DESC % theta, "theta": theta, "value": value, "unit": "particle-steps/s", "steps": steps,
+    return {"workload": BATCH_DESC % bh_mode_desc(theta, alpha), "theta": theta, "alpha": alpha, "value": value, "unit": "particle-steps/s", "steps": steps,
             "ms_per_step": dev_b * 1e3 / steps, "systems": len(specs), "particles": int(total_n),
             "barnes_hut_systems": n_bh, "direct_systems": len(specs) - n_bh, "crossover_n": xo, "tuning": tune,
             "kernels_per_step": kps, "gpu_launches": kps * steps,
@@ -336,7 +367,7 @@ def measure_batched(gsim, torch, args, local):
 
 SERVE_DESC = ("Poisson stream (mean 200 requests/s, seed 1005) of simulation requests: N log-uniform in "
               "[2048, 1048576], steps uniform in [10, 1000], generator uniform over uniform disk / spiral galaxy / "
-              "two-disk collision; direct sum below the tuned crossover, Barnes-Hut accurate mode above; "
+              "two-disk collision; direct sum below the tuned crossover, Barnes-Hut accurate mode (%s) above; "
               "150 GB device-memory budget; softening 0.2, dt=1e-3")
 
 
@@ -359,14 +390,13 @@ def _latency_summary(lat):
             "mean_s": float(lat.mean()), "max_s": float(lat.max())}
 
 
-def measure_served(gsim, torch, args, local, crossover, theta):
+def measure_served(gsim, torch, args, local, crossover, theta, alpha):
     """The served workload through gs_server (continuous batching, admission by device
     footprint), and the plain sequential path on the same trace: each request in arrival
     order, generated, created, run with gs_run and read back, one at a time."""
     reqs, arrivals = serve_trace(args.serve_requests)
     d = gsim.default_params(algorithm=gsim.DIRECT_SUM, device=local)
-    b = gsim.default_params(algorithm=gsim.BARNES_HUT, box_mode=gsim.BOX_BOUNDING, accuracy_parameter=theta,
-                            device=local, flags=ACCURATE)
+    b = batch_params(gsim, local, 1 << 30, 0, theta, alpha)
     work = float(sum(r.particle_count * r.steps for r in reqs))
     with gsim.Server(150 * 10 ** 9, crossover, d, b, max_resident_particles=args.serve_max_particles,
                      steps_in_flight=2, policy=gsim.SERVE_FIFO) as srv:
@@ -396,7 +426,8 @@ def measure_served(gsim, torch, args, local, crossover, theta):
         lat_p.append(time.perf_counter() - start - a)
     makespan_p = time.perf_counter() - start - float(arrivals[0])
     plain = {"value": work / makespan_p, "makespan_s": makespan_p, "latency": _latency_summary(lat_p)}
-    return {"workload": SERVE_DESC, "requests": len(reqs), "theta": theta, "crossover_n": crossover,
+    return {"workload": SERVE_DESC % bh_mode_desc(theta, alpha), "requests": len(reqs), "theta": theta,
+            "alpha": alpha, "crossover_n": crossover,
             "particle_steps": work, "value": served["value"], "unit": "particle-steps/s", "served": served,
             "plain_sequential": plain, "speedup_vs_plain": served["value"] / plain["value"],
             "max_resident_particles": args.serve_max_particles, "policy": "fifo with conservative backfill"}
@@ -453,18 +484,16 @@ def precision_study(gsim, torch, args, local, steps=1000, every=100, sample=2048
             "variants": out}
 
 
-def force_error(gsim, wl, pos, vel, mass, local):
-    """RMS / median / p99 / max relative force error of one step against the FP64 direct
-    sum (GPU FP64 kernel) on a 4096-particle subsample."""
-    with gsim.Simulation(pos, vel, mass, params=make_params(gsim, wl, local, gsim.FLAG_RECORD_ACCEL)) as es:
-        es.run(1)
-        acc = es.get_accel().astype(np.float64)
-        es.set_particles(pos, vel, mass)
-        sub = np.random.default_rng(0).choice(wl["n"], min(4096, wl["n"]), replace=False).astype(np.uint32)
-        a64 = es.accel_f64(sub)
-    e = np.linalg.norm(acc[sub] - a64, axis=1) / np.maximum(np.linalg.norm(a64, axis=1), 1e-30)
-    return {"rms": float(np.sqrt(np.mean(e ** 2))), "median": float(np.median(e)),
-            "p99": float(np.quantile(e, 0.99)), "max": float(e.max()), "subsample": int(len(sub))}
+def force_error(gsim, wl, pos, vel, mass, local, steps=4):
+    """Relative force error against the FP64 direct sum (GPU FP64 kernel) on a
+    4096-particle subsample, at each of `steps` steps after a warm step: the RMS of the
+    worst step (the gated figure), each step's RMS, and median / p99 / max over all."""
+    sub = np.random.default_rng(0).choice(wl["n"], min(4096, wl["n"]), replace=False).astype(np.uint32)
+    errs = step_errors(gsim, make_params(gsim, wl, local, 0), pos, vel, mass, sub, steps)
+    rms = [float(np.sqrt(np.mean(e ** 2))) for e in errs]
+    e = np.concatenate(errs)
+    return {"rms": max(rms), "rms_per_step": rms, "median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)),
+            "max": float(e.max()), "subsample": int(len(sub)), "steps": f"steps 2..{steps + 1} from the generated state"}
 
 
 def roofline_of(gsim, wl, m):
@@ -504,16 +533,21 @@ def cpu_baseline(wl, pos, vel, mass, seconds_budget=30.0):
     threads = os.cpu_count() or 1
     if wl["algo"] == 1:
         st = oracle.State(pos, vel, mass)
-        r = oracle.bh_step(st, box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads,
-                           walk_stride=16, flags=wl["oracle_flags"])
+        kw = dict(box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads, flags=wl["oracle_flags"],
+                  rel_alpha=wl.get("alpha", 0.0))
+        r = oracle.bh_step(st, walk_stride=16, **kw)  # time estimate
         est = r["build_seconds"] + 16 * r["walk_seconds"]
         stride = max(1, int(np.ceil(est / seconds_budget)))
-        st = oracle.State(pos, vel, mass)
-        r = oracle.bh_step(st, box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads,
-                           walk_stride=stride, flags=wl["oracle_flags"])
+        if wl["oracle_flags"] & oracle.RELATIVE_MAC:  # a full first step leaves every particle's |a|
+            st = oracle.State(pos, vel, mass)
+            oracle.bh_step(st, **kw)
+        r = oracle.bh_step(st, walk_stride=stride, **kw)
         t = r["build_seconds"] + stride * r["walk_seconds"]
-        sample = (f"1 step of the same {wl['n']}-particle system: full tree build (1 thread), force walk of "
-                  f"every {stride}-th group of 32 on {threads} threads, walk time scaled by {stride}")
+        sample = (f"1 step of the same {wl['n']}-particle system (the second, after a full first step): full "
+                  f"tree build (1 thread), force walk of every {stride}-th group of 64 on {threads} threads, "
+                  f"walk time scaled by {stride}" if stride > 1 else
+                  f"1 full step of the same {wl['n']}-particle system (the second, after a full first step): "
+                  f"tree build on 1 thread, force walk on {threads} threads")
     else:
         st = oracle.State(pos, vel, mass)
         t0 = time.perf_counter()
@@ -536,16 +570,16 @@ def run_reference(args, wl):
     st = oracle.State(pos, vel, mass)
     budget = 150.0 / max(1, args.steps + args.warmup)  # whole run within a few minutes
     stride, times = 1, []
+    kw = dict(box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads, flags=wl["oracle_flags"],
+              rel_alpha=wl.get("alpha", 0.0))
     for k in range(args.warmup + args.steps):
         if wl["algo"] == 1:
-            if k == 0:
-                r = oracle.bh_step(st, box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads,
-                                   walk_stride=16, flags=wl["oracle_flags"])
-                t = r["build_seconds"] + 16 * r["walk_seconds"]
+            if k == 0:  # a full step: time estimate, and every particle's |a| for the next
+                r = oracle.bh_step(st, **kw)
+                t = r["build_seconds"] + r["walk_seconds"]
                 stride = max(1, int(np.ceil(t / budget)))
                 continue
-            r = oracle.bh_step(st, box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads,
-                               walk_stride=stride, flags=wl["oracle_flags"])
+            r = oracle.bh_step(st, walk_stride=stride, **kw)
             t = r["build_seconds"] + stride * r["walk_seconds"]
         else:
             t0 = time.perf_counter()
@@ -555,7 +589,7 @@ def run_reference(args, wl):
             times.append(t)
     tot = float(np.sum(times))
     value = wl["n"] * len(times) / tot
-    sample = (f"each step: full tree build + force walk of every {stride}-th group of 32, walk time scaled by "
+    sample = (f"each step: full tree build + force walk of every {stride}-th group of 64, walk time scaled by "
               f"{stride}" if wl["algo"] == 1 and stride > 1 else "each step: one full step of the system")
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "impl": "reference", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
@@ -581,7 +615,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-system batched line")
     ap.add_argument("--batch-steps", type=int, default=50)
-    ap.add_argument("--batch-theta", type=float, default=0.37, help="theta of the batched Barnes-Hut systems")
+    ap.add_argument("--batch-theta", type=float, default=0.3,
+                    help="theta of the batched and served Barnes-Hut systems (the floor with --batch-alpha > 0)")
+    ap.add_argument("--batch-alpha", type=float, default=0.006,
+                    help="relative criterion alpha of the batched and served Barnes-Hut systems (0: theta alone)")
     ap.add_argument("--no-served", action="store_true", help="skip the served (request stream) line")
     ap.add_argument("--no-precision", action="store_true", help="skip the direct-sum precision study")
     ap.add_argument("--serve-requests", type=int, default=100)
@@ -634,20 +671,24 @@ def main():
     sim.close()
 
     err = force_error(gsim, wl, pos, vel, mass, local) if rank == 0 else None
-    secondary = None
-    if rank == 0 and world == 1 and wl["algo"] == gsim.BARNES_HUT and not args.no_secondary:
-        wl2 = workloads()["bh500k-reference-rule"]
-        m2 = measure(gsim, torch, wl2, pos, vel, mass, args, local, None, sample_clocks=False)
-        m2.pop("sim").close()
-        secondary = {"workload": wl2["desc"], "value": wl2["n"] * args.steps / (m2["dev_ms"] / 1e3),
-                     "ms_per_step": m2["dev_ms"] / args.steps, "stage_ms_per_step": m2["stage_ms"],
-                     "force_error_vs_fp64": force_error(gsim, wl2, pos, vel, mass, local)}
+    secondary = theta_only = None
+    if rank == 0 and world == 1 and args.workload == "bh500k" and not args.no_secondary:
+        lines = []
+        for name in ("bh500k-theta", "bh500k-reference-rule"):
+            wl2 = workloads()[name]
+            m2 = measure(gsim, torch, wl2, pos, vel, mass, args, local, None, sample_clocks=False)
+            m2.pop("sim").close()
+            lines.append({"workload": wl2["desc"], "value": wl2["n"] * args.steps / (m2["dev_ms"] / 1e3),
+                          "ms_per_step": m2["dev_ms"] / args.steps, "stage_ms_per_step": m2["stage_ms"],
+                          "interactions_per_step": m2.get("interactions"),
+                          "force_error_vs_fp64": force_error(gsim, wl2, pos, vel, mass, local)})
+        theta_only, secondary = lines
     batched = served = None
     if rank == 0 and world == 1 and not args.no_batched:
         batched = measure_batched(gsim, torch, args, local)
     if rank == 0 and world == 1 and not args.no_served:
         xo = batched["crossover_n"] if batched else 2500
-        served = measure_served(gsim, torch, args, local, xo, args.batch_theta)
+        served = measure_served(gsim, torch, args, local, xo, args.batch_theta, args.batch_alpha)
     precision = None
     if rank == 0 and world == 1 and not args.no_precision:
         precision = precision_study(gsim, torch, args, local)
@@ -663,7 +704,8 @@ def main():
                           "l2": "flushed (256 MiB write) before every timed step"},
                "e2e": e2e, "gpu_launches": m["launches"] * world, "roofline": roofline_of(gsim, wl, m),
                "cpu_baseline": cpu, "force_error_vs_fp64": err, "clocks": m["clocks"],
-               "reference_rule_theta1": secondary, "batched": batched, "served": served,
+               "accurate_theta_only": theta_only, "reference_rule_theta1": secondary, "batched": batched,
+               "served": served,
                "direct_precision_study": precision}
         print(json.dumps(out))
     if dist is not None:
