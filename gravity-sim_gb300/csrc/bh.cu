@@ -18,9 +18,10 @@
 //   k_records     preorder records: node (d, s) at s + E(s) + d - dmin(s), particle leaf
 //                 at s + E(s) + e(s); skip = end + E(end) - index (the reference's count.y),
 //                 radius = radius0 / 4^d (TreeMoveShader.comp:70-71)
-//   k_level_sums  mass and mass-moment sums level by level, finest first (one launch per
-//                 deep level, one block for the top levels), children in the order of
-//                 TreeInitShader.comp:78-80; centre of mass as TreeMoveShader.comp:66-67
+//   k_coop_sums   mass and mass-moment sums level by level, finest first (one cooperative
+//                 launch, a grid barrier between deep levels, one block for the top
+//                 levels; a batch launches kb_level_sums per level), children in the order
+//                 of TreeInitShader.comp:78-80; centre of mass as TreeMoveShader.comp:66-67
 //   k_force       ForceShader.comp:78-152 semantics: one warp walks the preorder records
 //                 for 32 consecutive sorted slots; a record is accepted only if every
 //                 lane satisfies radius <= d2 * theta^2; 32-record window staged in shared
@@ -829,25 +830,67 @@ __device__ __forceinline__ void top_sums_body(const uint32_t* __restrict__ level
     }
 }
 
-template <bool QUAD>
-__global__ void __launch_bounds__(256)
-k_level_sums(int d, const uint32_t* __restrict__ level_count, const uint32_t* __restrict__ levels, uint32_t n_al,
-             const uint32_t* __restrict__ skey, int D, float4* rec, const uint4* __restrict__ kids,
-             const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
-             const BHParams* __restrict__ bpp) {
-    pdl_enter();
-    level_sums_body<QUAD>(grid_blk(), d, level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, quad, safe,
-                          bbox_mode, bpp);
+// Acquire load of a barrier counter.
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
 }
 
+// Barrier over every block of a cooperative launch (all blocks are co-resident, so
+// every block reaches it).  Block leaders count arrivals on `bar` and wait for `target`;
+// the wait is bounded, and a block that gives up sets the error flag, which makes the
+// others stop waiting too.  Returns false after a failed wait.
+__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, int* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();  // this block's moments are visible before it is counted
+        atomicAdd(bar, 1u);
+        int ok = 1;
+        uint32_t spins = 0;
+        while (ld_acquire_u32(bar) < target) {
+            if (++spins > kSpinLimit) {
+                atomicOr(err, kErrBarrierWait);
+                ok = 0;
+                break;
+            }
+            if ((spins & 255u) == 0u && ld_volatile((const uint32_t*)err) & kErrBarrierWait) {
+                ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Moments of every level in one cooperative launch: levels D .. kLevelTop + 1 spread over
+// the whole grid, a grid barrier after each, then levels kLevelTop .. 0 in block 0 with
+// block barriers.  Each level's nodes are computed exactly as by the per-level launches.
+constexpr int kCoopSumsThreads = 256;
+
 template <bool QUAD>
-__global__ void __launch_bounds__(512)
-k_top_sums(const uint32_t* __restrict__ level_count, const uint32_t* __restrict__ levels, uint32_t n_al,
-           const uint32_t* __restrict__ skey, int D, float4* rec, const uint4* __restrict__ kids,
-           const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
-           const BHParams* __restrict__ bpp) {
+__global__ void __launch_bounds__(kCoopSumsThreads, 2)
+k_coop_sums(const uint32_t* __restrict__ level_count, const uint32_t* __restrict__ levels, uint32_t n_al,
+            const uint32_t* __restrict__ skey, int D, float4* rec, const uint4* __restrict__ kids,
+            const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
+            const BHParams* __restrict__ bpp, uint32_t* __restrict__ bar, int* __restrict__ err) {
     pdl_enter();
-    top_sums_body<QUAD>(level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, quad, safe, bbox_mode, bpp);
+    const BHParams bp = *bpp;
+    uint32_t target = 0;
+    for (int d = D; d > kLevelTop; --d) {
+        const uint32_t cnt = min(level_count[d], level_cap(d, n_al));
+        const uint32_t* list = levels + level_off(d, n_al);
+        for (uint32_t t = blockIdx.x * kCoopSumsThreads + threadIdx.x; t < cnt; t += gridDim.x * kCoopSumsThreads)
+            compute_node<QUAD>(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum, quad);
+        target += gridDim.x;
+        if (!grid_sync(bar, target, err)) return;
+    }
+    if (blockIdx.x == 0)
+        top_sums_body<QUAD>(level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, quad, safe, bbox_mode, bpp);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1418,7 +1461,7 @@ uint64_t bh_capacity(int box_mode, uint64_t n_al) {
 // [kCtrLevel..+15]: internal nodes per level
 enum {
     kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrLevel = 16,
-    kCtrCount = 32
+    kCtrBarrier = 32, kCtrCount = 40
 };
 
 // Lays the Barnes-Hut scratch out in the system's slab (sim_carve); while the system is
@@ -1477,6 +1520,14 @@ cudaError_t bh_init(gs_sim* s) {
                    2.0f * kSimSize / (float)kGrid};
     if (e == cudaSuccess) e = cudaMemcpyAsync(w.params, &fixed, sizeof fixed, cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);  // `fixed` lives on this stack frame
+    // the cooperative moments launch: as many blocks as fit on the device at once
+    int per_sm = 0, sms = 0;
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, w.quad ? k_coop_sums<true> : k_coop_sums<false>, kCoopSumsThreads, 0);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    if (e == cudaSuccess && per_sm < 1) e = cudaErrorCooperativeLaunchTooLarge;
+    w.sums_grid = per_sm * sms;
     return e;
 }
 
@@ -1495,6 +1546,24 @@ cudaError_t launch(bool pdl, void (*kernel)(KArgs...), int grid, int block, cuda
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+// The same as a cooperative launch: every block of the grid is resident at once.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_coop(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 2 : 1;
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 }  // namespace
@@ -1570,19 +1639,12 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
         const int safe = (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0;
         const int bb = bbox ? 1 : 0;
         float4* quad = w.quad;
-        for (int d = w.depth; d > kLevelTop; --d) {
-            const int blocks = (int)std::min<uint64_t>((uint64_t)grid_for(n, 256), (level_cap(d, n) + 255) / 256);
-            GS_TRY_LAUNCH(launch(next_pdl(), quad ? k_level_sums<true> : k_level_sums<false>, blocks, 256, st, d,
-                                 (const uint32_t*)(ctr + kCtrLevel), (const uint32_t*)w.levels, n, skey, w.depth,
-                                 w.rec, (const uint4*)w.kids, (const uint2*)w.nodeinfo, w.msum, quad, safe, bb,
-                                 (const BHParams*)w.params));
-        }
-        GS_TRY_LAUNCH(launch(next_pdl(), quad ? k_top_sums<true> : k_top_sums<false>, 1, 512, st,
-                             (const uint32_t*)(ctr + kCtrLevel), (const uint32_t*)w.levels, n, skey, w.depth, w.rec,
-                             (const uint4*)w.kids, (const uint2*)w.nodeinfo, w.msum, quad, safe, bb,
-                             (const BHParams*)w.params));
+        GS_TRY_LAUNCH(launch_coop(next_pdl(), quad ? k_coop_sums<true> : k_coop_sums<false>, w.sums_grid,
+                                  kCoopSumsThreads, st, (const uint32_t*)(ctr + kCtrLevel), (const uint32_t*)w.levels,
+                                  n, skey, w.depth, w.rec, (const uint4*)w.kids, (const uint2*)w.nodeinfo, w.msum,
+                                  quad, safe, bb, (const BHParams*)w.params, ctr + kCtrBarrier, s->d_err));
     }
-    count_launch(s, (uint32_t)(w.depth - kLevelTop + 1));
+    count_launch(s);
     stage_end(s, kStageSums, profile);
     stage_begin(s, kStageForce, profile);
     const float k = s->G * s->dt_eff;  // ForceShader.comp:145 (GRAVITATIONAL_CONST * SIMULATION_TIME)

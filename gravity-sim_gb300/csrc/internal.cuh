@@ -34,6 +34,7 @@ enum Stage { kStageBBox = 0, kStageKeys, kStageSort, kStageScan, kStageRecords, 
 constexpr int kErrSortWait = 1;
 constexpr int kErrScanWait = 2;
 constexpr int kErrTree = 4;
+constexpr int kErrBarrierWait = 8;
 
 // radix sort shape: 256 threads x 8 keys per tile
 constexpr int kSortThreads = 256;
@@ -72,6 +73,7 @@ struct BHWork {
     float2* msum = nullptr;            // [cap]
     float4* quad = nullptr;            // [cap] {sxx, sxy, syy, -} (GS_FLAG_QUADRUPOLE)
     float* amag = nullptr;             // [n_al] |a| of the last step, NaN: unknown (GS_FLAG_RELATIVE_MAC)
+    int sums_grid = 0;                 // blocks of the cooperative moments launch (all co-resident)
     uint4* kids = nullptr;             // [cap] child descriptors of internal records
     uint32_t* levels = nullptr;        // internal records by level (level_off / level_cap in bh.cu)
     uint2* nodeinfo = nullptr;         // [cap] {a key of the cell, level} of an internal record

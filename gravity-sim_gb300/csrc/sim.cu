@@ -134,7 +134,8 @@ gs_status check_device_error(gs_sim* s) {
     GS_CUDA(cudaMemcpy(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {
         set_error(std::string("device-side error flags ") + std::to_string(err) +
-                  " (1: radix-sort look-back wait ran out, 2: scan look-back wait ran out, 4: tree capacity)");
+                  " (1: radix-sort look-back wait ran out, 2: scan look-back wait ran out, 4: tree capacity, "
+                  "8: moments grid barrier wait ran out)");
         return GS_ERR_DEVICE;
     }
     return GS_OK;
