@@ -213,6 +213,14 @@ k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uin
 // keygen + digit histograms
 // ------------------------------------------------------------------------------------
 constexpr int kKeyThreads = 256;
+// Keygen blocks: each block adds its digit histograms to the global ones with up to
+// 4 x 256 atomics, so a few blocks per SM (grid-stride) keep those atomics few; one
+// block per 256 particles spent 25 us of a 500k step on them, 608 blocks 10 us.
+constexpr int kKeyBlocks = 608;
+inline int keygen_blocks(uint64_t n) {
+    const uint64_t b = (n + kKeyThreads - 1) / kKeyThreads;
+    return (int)(b < 1 ? 1 : b > (uint64_t)kKeyBlocks ? kKeyBlocks : b);
+}
 
 __device__ __forceinline__ void keygen_body(Blk blk, int bbox_mode, const BHParams* __restrict__ bp,
                                             float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos_out,
@@ -1599,7 +1607,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
         stage_end(s, kStageBBox, profile);
     }
     stage_begin(s, kStageKeys, profile);
-    GS_TRY_LAUNCH(launch(next_pdl(), k_keygen, grid_for(n, kKeyThreads), kKeyThreads, st, bbox ? 1 : 0,
+    GS_TRY_LAUNCH(launch(next_pdl(), k_keygen, keygen_blocks(n), kKeyThreads, st, bbox ? 1 : 0,
                          (const BHParams*)w.params, s->pos[in], s->mass[in], s->pos[out], s->mass[out], n, w.keys[0],
                          w.hist, w.passes, ctr + kCtrValid));
     count_launch(s);
@@ -1974,6 +1982,7 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
         blocks[kTabBBox] = (uint32_t)bbox_blocks(n);
     }
     blocks[kTabGrid] = (uint32_t)grid_for(n, 256);
+    blocks[kTabKeys] = (uint32_t)keygen_blocks(n);
     blocks[kTabSort] = w.sort_tiles;
     blocks[kTabScan] = w.scan_tiles;
     blocks[kTabOne] = 1;
@@ -2016,7 +2025,7 @@ cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st) {
     // launch with the stage before it (programmatic dependent launch)
     GS_TRY_LAUNCH(launch(false, kb_clear, (int)p.total[kTabClear], 256, st, args(kTabClear), p.d_work));
     if (p.bbox) GS_TRY_LAUNCH(launch(true, kb_bbox, (int)p.total[kTabBBox], kBBoxThreads, st, args(kTabBBox)));
-    GS_TRY_LAUNCH(launch(true, kb_keygen, (int)p.total[kTabGrid], kKeyThreads, st, args(kTabGrid)));
+    GS_TRY_LAUNCH(launch(true, kb_keygen, (int)p.total[kTabKeys], kKeyThreads, st, args(kTabKeys)));
     for (int ps = 0; ps < p.passes; ++ps)
         GS_TRY_LAUNCH(launch(true, ps == 0 ? kb_sort_pass<true> : kb_sort_pass<false>, (int)p.total[kTabSort],
                              kSortThreads, st, args(kTabSort), ps));

@@ -138,7 +138,9 @@ struct SysDesc {
 
 // Per-stage block tables of a batch: table t holds the exclusive prefix of the blocks each
 // system gets in stage t; a block finds its system by binary search.
-enum BatchTable { kTabClear = 0, kTabBBox, kTabGrid, kTabSort, kTabScan, kTabOne, kTabForce, kTabDirect, kTabCount };
+enum BatchTable {
+    kTabClear = 0, kTabBBox, kTabKeys, kTabGrid, kTabSort, kTabScan, kTabOne, kTabForce, kTabDirect, kTabCount
+};
 
 // What the batched launchers need: descriptors (Barnes-Hut systems first, largest first),
 // block tables, and the batch-wide work counters cleared by the first stage.
