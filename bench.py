@@ -18,7 +18,7 @@ latter does not meet the gate.  A step is one simulation step of the whole syste
          reads the state back (gs_get_particles), host wall clock.  An upload forgets
          the previous |a|, so these steps open nodes by the theta floor alone
   roofline  the traversal kernel: algorithmic FLOP of the accepted interactions
-         (14 per monopole, 37 per quadrupole) over its CUDA-event time, against the
+         (14 per monopole, 33 per quadrupole) over its CUDA-event time, against the
          FP32 FMA rate
   batched  512 systems of uneven N stepped together, against each run alone
   served   a Poisson stream of simulation requests through the serving loop, against the
@@ -504,15 +504,15 @@ def roofline_of(gsim, wl, m):
     if wl["algo"] == gsim.BARNES_HUT:
         t = m["stage_ms"]["force"] / 1e3
         # 14 FLOP per monopole interaction (particle leaves; every record under the
-        # reference rule), 37 per quadrupole interaction (accurate-mode nodes)
+        # reference rule), 33 per quadrupole interaction (accurate-mode nodes)
         quads = m["node_interactions"] if wl["flags"] & 0x10 else 0
-        flops = 14.0 * (m["interactions"] - quads) + 37.0 * quads
+        flops = 14.0 * (m["interactions"] - quads) + 33.0 * quads
         achieved = flops / t / 1e12
         extra = {"kernel": "k_force_group" if wl["flags"] & 0x40 else "k_force",
                  "interactions_per_step": m["interactions"], "quadrupole_interactions_per_step": quads,
                  "tests_per_step": m["tests"], "tree_records": m["tree_records"],
                  "internal_nodes": m["internal_nodes"],
-                 "flop_model": "14 FLOP per monopole (leaf) interaction, 37 per quadrupole (node) interaction"}
+                 "flop_model": "14 FLOP per monopole (leaf) interaction, 33 per quadrupole (node) interaction (FMA = 2)"}
     else:
         t = m["stage_ms"]["direct"] / 1e3
         n_al = (wl["n"] + 63) // 64 * 64

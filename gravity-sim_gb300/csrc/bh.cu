@@ -1042,35 +1042,6 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
     return d;
 }
 
-template <bool EXACT>
-__device__ __forceinline__ void monopole(float4 q, float px, float py, float eps2, float& ax, float& ay) {
-    const float dx = q.x - px, dy = q.y - py;
-    const float d2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
-    const float r = inv_sqrt<EXACT>(d2);
-    const float sc = ((q.z * r) * r) * r;
-    ax = fmaf(dx, sc, ax);
-    ay = fmaf(dy, sc, ay);
-}
-
-template <bool EXACT>
-__device__ __forceinline__ void quadrupole(float4 q, float4 m2, float px, float py, float eps2, float& ax, float& ay) {
-    const float dx = q.x - px, dy = q.y - py;
-    const float d2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
-    const float r = inv_sqrt<EXACT>(d2);
-    const float r2 = r * r;
-    const float r3 = r2 * r;
-    const float r5 = r3 * r2;
-    const float r7 = r5 * r2;
-    const float srx = fmaf(m2.x, dx, m2.y * dy);
-    const float sry = fmaf(m2.y, dx, m2.z * dy);
-    const float u = fmaf(dx, srx, dy * sry);
-    const float T = m2.x + m2.z;
-    const float coef = fmaf(7.5f * u, r7, fmaf(-1.5f * T, r5, q.z * r3));
-    const float t3 = 3.0f * r5;
-    ax = fmaf(-t3, srx, fmaf(dx, coef, ax));
-    ay = fmaf(-t3, sry, fmaf(dy, coef, ay));
-}
-
 // Evaluation order.  Each particle sums the accepted nodes and the particle leaves of its
 // walk separately, each in walk order, into a node and a leaf accumulator; its
 // acceleration is node + leaf.  How the warp batches its evaluations therefore does not
@@ -1082,11 +1053,12 @@ struct GroupSmem {
     uint32_t it_count[kItemCap];  // record count
     uint32_t off[kItemCap];       // exclusive record offsets of the runs
     float cx[32], cy[32], cm[32];     // one chunk of gathered records: centre of mass (or particle), mass
-    float qxx[32], qxy[32], qyy[32];  // second moments of node records
+    float qxx[32], qxy[32], qyy[32], mt[32];  // node terms 7.5 S and -1.5 tr(S) of node records
 };
 
-// One record (x, y, m) on the lane's two particles (P = their x, Q = their y): the
-// operation sequence of `monopole`, two particles at once.
+// One record (x, y, m) on the lane's two particles (P = their x, Q = their y):
+// d = (x, y) - p, d2 = dx^2 + dy^2 + eps^2, a += d * (((m r) r) r) with r = 1/sqrt(d2),
+// the CPU restatement's pair_scale sequence, two particles at once.
 template <bool EXACT>
 __device__ __forceinline__ void monopole_x2(float x, float y, float m, float2 P, float2 Q, float2 E2, float2& acx,
                                             float2& acy) {
@@ -1098,28 +1070,30 @@ __device__ __forceinline__ void monopole_x2(float x, float y, float m, float2 P,
     acy = fma2(dy, sc, acy);
 }
 
-// One node with second moments on the lane's two particles: the operation sequence of
-// `quadrupole` (the particle-independent T and -1.5 T once per record).
+// One node with second moments on the lane's two particles.  The monopole and
+// quadrupole terms of the softened potential,
+//   a = d (m r^3 - 1.5 tr(S) r^5 + 7.5 (d.S.d) r^7) - 3 r^5 S d,   r = 1/sqrt(d2),
+// are evaluated as r^3 (d (m + r^2 (mt + r^2 u)) - 0.4 r^2 S'' d) with the node terms
+// S'' = 7.5 S and mt = -1.5 tr(S) formed once per node (eval_nodes): 21 operations per
+// particle instead of 23, the CPU restatement's sequence (quad_accumulate).
 template <bool EXACT>
-__device__ __forceinline__ void quadrupole_x2(float x, float y, float m, float sxx, float sxy, float syy, float2 P,
-                                              float2 Q, float2 E2, float2& acx, float2& acy) {
+__device__ __forceinline__ void quadrupole_x2(float x, float y, float m, float qxx, float qxy, float qyy, float mt,
+                                              float2 P, float2 Q, float2 E2, float2& acx, float2& acy) {
     const float2 dx = sub2(make_float2(x, x), P), dy = sub2(make_float2(y, y), Q);
     const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
     const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
     const float2 r2 = mul2(r, r);
     const float2 r3 = mul2(r2, r);
-    const float2 r5 = mul2(r3, r2);
-    const float2 r7 = mul2(r5, r2);
-    const float2 Sxx = make_float2(sxx, sxx), Sxy = make_float2(sxy, sxy), Syy = make_float2(syy, syy);
+    const float2 Sxx = make_float2(qxx, qxx), Sxy = make_float2(qxy, qxy), Syy = make_float2(qyy, qyy);
     const float2 srx = fma2(Sxx, dx, mul2(Sxy, dy));
     const float2 sry = fma2(Sxy, dx, mul2(Syy, dy));
     const float2 u = fma2(dx, srx, mul2(dy, sry));
-    const float mt = -1.5f * (sxx + syy);
-    const float2 coef = fma2(mul2(make_float2(7.5f, 7.5f), u), r7,
-                             fma2(make_float2(mt, mt), r5, mul2(make_float2(m, m), r3)));
-    const float2 nt3 = mul2(make_float2(-3.0f, -3.0f), r5);
-    acx = fma2(nt3, srx, fma2(dx, coef, acx));
-    acy = fma2(nt3, sry, fma2(dy, coef, acy));
+    const float2 t = fma2(fma2(u, r2, make_float2(mt, mt)), r2, make_float2(m, m));
+    const float2 k = mul2(make_float2(-0.4f, -0.4f), r2);
+    const float2 ix = fma2(srx, k, mul2(dx, t));
+    const float2 iy = fma2(sry, k, mul2(dy, t));
+    acx = fma2(r3, ix, acx);
+    acy = fma2(r3, iy, acy);
 }
 
 // Sum the count accepted nodes (quadrupole term with QUAD) for the lane's two particles,
@@ -1141,9 +1115,10 @@ __device__ __forceinline__ void eval_nodes(GroupSmem& g, uint32_t count, const f
         g.cy[lane] = q.y;
         g.cm[lane] = q.z;
         if (QUAD) {
-            g.qxx[lane] = qq.x;
-            g.qxy[lane] = qq.y;
-            g.qyy[lane] = qq.z;
+            g.qxx[lane] = 7.5f * qq.x;
+            g.qxy[lane] = 7.5f * qq.y;
+            g.qyy[lane] = 7.5f * qq.z;
+            g.mt[lane] = -1.5f * (qq.x + qq.z);
         }
         __syncwarp();
         const uint32_t fn = f0 + 32 + lane;
@@ -1155,7 +1130,8 @@ __device__ __forceinline__ void eval_nodes(GroupSmem& g, uint32_t count, const f
 #pragma unroll 4
         for (uint32_t j = 0; j < m; ++j) {
             if (QUAD)
-                quadrupole_x2<EXACT>(g.cx[j], g.cy[j], g.cm[j], g.qxx[j], g.qxy[j], g.qyy[j], P, Q, E2, acx, acy);
+                quadrupole_x2<EXACT>(g.cx[j], g.cy[j], g.cm[j], g.qxx[j], g.qxy[j], g.qyy[j], g.mt[j], P, Q, E2, acx,
+                                     acy);
             else
                 monopole_x2<EXACT>(g.cx[j], g.cy[j], g.cm[j], P, Q, E2, acx, acy);
         }

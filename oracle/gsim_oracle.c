@@ -116,21 +116,29 @@ static inline float pair_scale(float m, float d2) {
  * (dx, dy) from the particle and second central moments S = {sxx, sxy, syy}:
  *   a = d (m r^3 + 7.5 u r^7 - 1.5 T r^5) - 3 r^5 S d,   u = d^T S d,  T = sxx + syy,
  * with r = 1 / sqrt(|d|^2 + eps^2) (Plummer-softened expansion of sum m_k / |x_k - p|). */
-static inline void quad_accumulate(float dx, float dy, float d2, float m, float sxx, float sxy, float syy,
-                                   float* ax, float* ay) {
+/* Node terms of the quadrupole formula, once per node: S'' = 7.5 S, mt = -1.5 tr S. */
+typedef struct { float qxx, qxy, qyy, mt; } quad_terms;
+static inline quad_terms quad_node(float sxx, float sxy, float syy) {
+    quad_terms q = {7.5f * sxx, 7.5f * sxy, 7.5f * syy, -1.5f * (sxx + syy)};
+    return q;
+}
+
+/* Monopole + quadrupole term of the softened potential, r = 1/sqrt(d2):
+ *   a = d (m r^3 - 1.5 tr(S) r^5 + 7.5 (d.S.d) r^7) - 3 r^5 S d
+ * evaluated as r^3 (d (m + r^2 (mt + r^2 u'')) - 0.4 r^2 S'' d), u'' = d.S''.d. */
+static inline void quad_accumulate(float dx, float dy, float d2, float m, quad_terms q, float* ax, float* ay) {
     float r = 1.0f / sqrtf(d2);
     float r2 = r * r;
     float r3 = r2 * r;
-    float r5 = r3 * r2;
-    float r7 = r5 * r2;
-    float srx = fmaf(sxx, dx, sxy * dy);
-    float sry = fmaf(sxy, dx, syy * dy);
+    float srx = fmaf(q.qxx, dx, q.qxy * dy);
+    float sry = fmaf(q.qxy, dx, q.qyy * dy);
     float u = fmaf(dx, srx, dy * sry);
-    float T = sxx + syy;
-    float coef = fmaf(7.5f * u, r7, fmaf(-1.5f * T, r5, m * r3));
-    float t3 = 3.0f * r5;
-    *ax = fmaf(-t3, srx, fmaf(dx, coef, *ax));
-    *ay = fmaf(-t3, sry, fmaf(dy, coef, *ay));
+    float t = fmaf(fmaf(u, r2, q.mt), r2, m);
+    float k = -0.4f * r2;
+    float ix = fmaf(srx, k, dx * t);
+    float iy = fmaf(sry, k, dy * t);
+    *ax = fmaf(r3, ix, *ax);
+    *ay = fmaf(r3, iy, *ay);
 }
 
 /* ------------------------------------------------------------------------------ */
@@ -394,10 +402,10 @@ static void walk_warp(void* p, uint64_t item, int worker) {
         ++visits;
         if (all) {
             if (c->quad && c->skip[ind] > 1) { /* internal node: quadrupole term */
-                const float sxx = c->quad[3 * ind], sxy = c->quad[3 * ind + 1], syy = c->quad[3 * ind + 2];
+                const quad_terms qt = quad_node(c->quad[3 * ind], c->quad[3 * ind + 1], c->quad[3 * ind + 2]);
                 for (int l = 0; l < WARP; ++l) {
                     if (!valid[l]) continue;
-                    quad_accumulate(dx[l], dy[l], d2[l], nm, sxx, sxy, syy, &ax[l], &ay[l]);
+                    quad_accumulate(dx[l], dy[l], d2[l], nm, qt, &ax[l], &ay[l]);
                 }
             } else {
                 for (int l = 0; l < WARP; ++l) {
@@ -529,13 +537,14 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
             if (accept) { /* one item: the record itself (a leaf only when the root is one) */
                 const float nx = c->npos[2 * n], ny = c->npos[2 * n + 1], nm = c->nmass[n];
                 const int a = sk > 1 ? 0 : 1;
+                const quad_terms qt = c->quad ? quad_node(c->quad[3 * n], c->quad[3 * n + 1], c->quad[3 * n + 2])
+                                              : quad_node(0.0f, 0.0f, 0.0f);
                 for (uint32_t l = 0; l < G; ++l) {
                     if (!valid[l]) continue;
                     float dx = nx - px[l], dy = ny - py[l];
                     float d2 = pair_d2(dx, dy, c->eps2);
                     if (c->quad && sk > 1) {
-                        quad_accumulate(dx, dy, d2, nm, c->quad[3 * n], c->quad[3 * n + 1], c->quad[3 * n + 2],
-                                        &ax[l][a], &ay[l][a]);
+                        quad_accumulate(dx, dy, d2, nm, qt, &ax[l][a], &ay[l][a]);
                     } else {
                         float sc = pair_scale(nm, d2);
                         ax[l][a] = fmaf(dx, sc, ax[l][a]);
