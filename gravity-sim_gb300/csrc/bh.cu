@@ -1435,9 +1435,13 @@ int grid_for(uint64_t n, int threads) {
 
 }  // namespace
 
+// Records: the particle leaves plus at most level_cap(d) internal nodes per level d
+// (disjoint cells of >= 2 particles).
 uint64_t bh_capacity(int box_mode, uint64_t n_al) {
-    uint64_t levels = box_mode == GS_BOX_BOUNDING ? kBBoxBits + 1 : kFixedDepth + 1;
-    return n_al + levels * (n_al / 2) + 64;
+    const int D = box_mode == GS_BOX_BOUNDING ? kBBoxBits : kFixedDepth;
+    uint64_t c = n_al + 64;
+    for (int d = 0; d <= D; ++d) c += level_cap(d, (uint32_t)n_al);
+    return c;
 }
 
 // counters layout inside the zeroed block

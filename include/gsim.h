@@ -181,6 +181,9 @@ GS_API gs_status gs_debug_bh_tree(gs_sim* sim, uint32_t* keys, uint32_t* sorted_
                            uint32_t* node_skip, float* node_radius, float* node_pos,
                            float* node_mass, float* node_quad, uint64_t capacity,
                            uint64_t* tree_records);
+/* Records the tree of aligned_count particles can hold: the leaves plus, for every level
+ * d of the box mode (0..10 fixed box, 0..15 bounding box), min(4^d, aligned_count/2 + 1)
+ * internal nodes, plus 64. */
 GS_API uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count);
 
 /* One direct-sum step (FAST math) on caller-owned device buffers, allocating nothing.

@@ -31,8 +31,11 @@ def test_exports_every_declared_symbol(gs):
 def test_alignment_and_capacity(gs):
     assert gs.required_alignment(gs.DIRECT_SUM) == 64
     assert gs.required_alignment(gs.BARNES_HUT) == 64
-    assert gs.node_capacity(gs.BOX_FIXED_500, 64) == 64 + 11 * 32 + 64
-    assert gs.node_capacity(gs.BOX_BOUNDING, 64) == 64 + 16 * 32 + 64
+    # leaves + at most min(4^d, n/2 + 1) internal nodes per level d (levels 0..10 / 0..15) + 64
+    for box, depth in ((gs.BOX_FIXED_500, 10), (gs.BOX_BOUNDING, 15)):
+        for n in (64, 640, 1 << 20):
+            levels = sum(min(4 ** d, n // 2 + 1) for d in range(depth + 1))
+            assert gs.node_capacity(box, n) == n + levels + 64
 
 
 def test_generators_deterministic(gs):
