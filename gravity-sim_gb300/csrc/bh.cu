@@ -609,17 +609,17 @@ __device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__
                 d = slot_dmin(skey, s, D) + (int)(j - E[s]);
                 const int shift = 2 * (D - d);
                 const uint32_t ks = skey[s];
-                const uint32_t end = cell_end(skey, s + 1, nv, shift, ks >> shift);
-                rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
-                skip[at] = end + E[end] - at;
-                nodeinfo[at] = make_uint2(ks, (uint32_t)d);  // a key of the cell, its level
+                uint32_t end;
                 if (d == D) {
+                    end = cell_end(skey, s + 1, nv, shift, ks >> shift);
                     kids[at] = make_uint4(kKidFinest, at + 1, end - s, 0u);  // all children are leaves
                 } else {
+                    // the level-(d+1) cells of the cell, in Morton order; the last one ends it
                     uint32_t kid[4] = {kKidNone, kKidNone, kKidNone, kKidNone};
                     uint32_t nk = 0;
                     const int cshift = 2 * (D - d - 1);
-                    for (uint32_t t = s; t < end;) {  // the level-(d+1) cells inside [s, end), in Morton order
+                    uint32_t t = s;
+                    do {
                         const uint32_t tend = cell_end(skey, t + 1, nv, cshift, skey[t] >> cshift);
                         uint32_t c;
                         if (tend - t >= 2) c = t + E[t] + (uint32_t)(d + 1 - slot_dmin(skey, t, D));  // node (d+1, t)
@@ -627,10 +627,14 @@ __device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__
                         if (nk < 4) kid[nk] = c;
                         ++nk;
                         t = tend;
-                    }
+                    } while (t < nv && (skey[t] >> shift) == (ks >> shift));
+                    end = t;
                     if (nk > 4) atomicOr(err, kErrTree);
                     kids[at] = make_uint4(kid[0], kid[1], kid[2], kid[3]);
                 }
+                rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
+                skip[at] = end + E[end] - at;
+                nodeinfo[at] = make_uint2(ks, (uint32_t)d);  // a key of the cell, its level
                 rank = atomicAdd(&s_cnt[d], 1u);
             }
         }
