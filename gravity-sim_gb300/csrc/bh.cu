@@ -7,7 +7,8 @@
 // clears and fills a fixed 1024x1024 grid and walks 11 levels of it every step; here
 // every stage is sized by N:
 //
-//   k_bbox        (bounding-box mode) min/max of positions, box parameters in FP64
+//   k_bbox_keys   (bounding-box mode) min/max of positions, box parameters in FP64, then
+//                 the keys (one cooperative launch; a batch runs kb_bbox and kb_keygen)
 //   k_keygen      cell key per particle (InitShader.comp:80-98 arithmetic), removal of
 //                 particles outside the fixed box (InitShader.comp:110-117), digit
 //                 histograms for every radix pass
@@ -108,13 +109,12 @@ inline int bbox_blocks(uint64_t n) {
     return (int)(b < 1 ? 1 : b > (uint64_t)kBBoxBlocks ? kBBoxBlocks : b);
 }
 
-__device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ pos, uint32_t n,
-                                          float* __restrict__ part, uint32_t* __restrict__ ticket,
-                                          BHParams* __restrict__ out) {
+// Min/max of this block's particles, reduced over the block (every thread returns it).
+// n is a multiple of 64: two particles per 16-byte load.  Min/max ignore NaN and are
+// exact in any order.
+__device__ __forceinline__ float4 bbox_block_minmax(Blk blk, const float2* __restrict__ pos, uint32_t n) {
     __shared__ float s[4][kBBoxThreads / 32];
-    __shared__ bool last;
     float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
-    // n is a multiple of 64: two particles per 16-byte load
     const float4* __restrict__ pos2 = reinterpret_cast<const float4*>(pos);
     for (uint32_t i = blk.id * kBBoxThreads + threadIdx.x; i < n / 2; i += blk.count * kBBoxThreads) {
         const float4 p = pos2[i];
@@ -130,6 +130,7 @@ __device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ po
         mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();  // s may still be read from a previous call
     if (lane == 0) {
         s[0][warp] = mnx;
         s[1][warp] = mxx;
@@ -137,54 +138,19 @@ __device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ po
         s[3][warp] = mxy;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < kBBoxThreads / 32; ++w) {
-            mnx = fminf(mnx, s[0][w]);
-            mxx = fmaxf(mxx, s[1][w]);
-            mny = fminf(mny, s[2][w]);
-            mxy = fmaxf(mxy, s[3][w]);
-        }
-        part[4 * blk.id + 0] = mnx;
-        part[4 * blk.id + 1] = mxx;
-        part[4 * blk.id + 2] = mny;
-        part[4 * blk.id + 3] = mxy;
-        __threadfence();
-        last = atomicAdd(ticket, 1u) == blk.count - 1;
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    // the last block reduces all block partials in parallel (min/max are exact in any order)
-    mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
-    for (uint32_t bl = threadIdx.x; bl < blk.count; bl += kBBoxThreads) {
-        mnx = fminf(mnx, __ldcg(&part[4 * bl + 0]));
-        mxx = fmaxf(mxx, __ldcg(&part[4 * bl + 1]));
-        mny = fminf(mny, __ldcg(&part[4 * bl + 2]));
-        mxy = fmaxf(mxy, __ldcg(&part[4 * bl + 3]));
-    }
-    for (int o = 16; o; o >>= 1) {
-        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
-        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
-        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
-        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
-    }
-    __syncthreads();
-    if (lane == 0) {
-        s[0][warp] = mnx;
-        s[1][warp] = mxx;
-        s[2][warp] = mny;
-        s[3][warp] = mxy;
-    }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    double a = INFINITY, b = -INFINITY, c = INFINITY, d = -INFINITY;
     for (int w = 0; w < kBBoxThreads / 32; ++w) {
-        if (s[0][w] < a) a = s[0][w];
-        if (s[1][w] > b) b = s[1][w];
-        if (s[2][w] < c) c = s[2][w];
-        if (s[3][w] > d) d = s[3][w];
+        mnx = fminf(mnx, s[0][w]);
+        mxx = fmaxf(mxx, s[1][w]);
+        mny = fminf(mny, s[2][w]);
+        mxy = fmaxf(mxy, s[3][w]);
     }
-    // square box around the extent, 1/1024 margin, 2^15 cells per axis
+    return make_float4(mnx, mxx, mny, mxy);
+}
+
+// The box parameters from the extent: a square around it, 1/1024 margin, 2^15 cells per
+// axis, in FP64.
+__device__ __forceinline__ BHParams bbox_params(float4 ext4) {
+    const double a = ext4.x, b = ext4.y, c = ext4.z, d = ext4.w;
     double cx = 0.5 * (a + b), cy = 0.5 * (c + d);
     double ext = b - a > d - c ? b - a : d - c;
     if (!(ext > 0.0) || !isfinite(ext)) ext = 1.0;
@@ -199,14 +165,63 @@ __device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ po
     double side0 = (double)(1u << kBBoxBits) / (double)p.scale;
     p.radius0 = (float)(side0 * side0 * 0.5);
     p.inv_scale = (float)(1.0 / (double)p.scale);
-    *out = p;
+    return p;
 }
 
-__global__ void __launch_bounds__(kBBoxThreads)
-k_bbox(const float2* __restrict__ pos, uint32_t n, float* __restrict__ part, uint32_t* __restrict__ ticket,
-       BHParams* __restrict__ out) {
-    pdl_enter();
-    bbox_body(grid_blk(), pos, n, part, ticket, out);
+// The extent of `count` block partials, reduced by the whole block (every thread).
+__device__ __forceinline__ float4 bbox_reduce_partials(const float* __restrict__ part, uint32_t count) {
+    float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+    for (uint32_t bl = threadIdx.x; bl < count; bl += kBBoxThreads) {
+        mnx = fminf(mnx, __ldcg(&part[4 * bl + 0]));
+        mxx = fmaxf(mxx, __ldcg(&part[4 * bl + 1]));
+        mny = fminf(mny, __ldcg(&part[4 * bl + 2]));
+        mxy = fmaxf(mxy, __ldcg(&part[4 * bl + 3]));
+    }
+    __shared__ float s[4][kBBoxThreads / 32];
+    for (int o = 16; o; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) {
+        s[0][warp] = mnx;
+        s[1][warp] = mxx;
+        s[2][warp] = mny;
+        s[3][warp] = mxy;
+    }
+    __syncthreads();
+    for (int w = 0; w < kBBoxThreads / 32; ++w) {
+        mnx = fminf(mnx, s[0][w]);
+        mxx = fmaxf(mxx, s[1][w]);
+        mny = fminf(mny, s[2][w]);
+        mxy = fmaxf(mxy, s[3][w]);
+    }
+    return make_float4(mnx, mxx, mny, mxy);
+}
+
+// One launch: block partials, then the last block to finish (ticket) reduces them all
+// and writes the box parameters.
+__device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ pos, uint32_t n,
+                                          float* __restrict__ part, uint32_t* __restrict__ ticket,
+                                          BHParams* __restrict__ out) {
+    __shared__ bool last;
+    const float4 m = bbox_block_minmax(blk, pos, n);
+    if (threadIdx.x == 0) {
+        part[4 * blk.id + 0] = m.x;
+        part[4 * blk.id + 1] = m.y;
+        part[4 * blk.id + 2] = m.z;
+        part[4 * blk.id + 3] = m.w;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == blk.count - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const float4 e = bbox_reduce_partials(part, blk.count);
+    if (threadIdx.x == 0) *out = bbox_params(e);
 }
 
 // ------------------------------------------------------------------------------------
@@ -300,6 +315,74 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
     return *((volatile const uint32_t*)p);
 }
+
+// Acquire load of a barrier counter.
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Barrier over every block of a cooperative launch (all blocks are co-resident, so
+// every block reaches it).  Block leaders count arrivals on `bar` and wait for `target`;
+// the wait is bounded, and a block that gives up sets the error flag, which makes the
+// others stop waiting too.  Returns false after a failed wait.
+__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, int* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();  // this block's moments are visible before it is counted
+        atomicAdd(bar, 1u);
+        int ok = 1;
+        uint32_t spins = 0;
+        while (ld_acquire_u32(bar) < target) {
+            if (++spins > kSpinLimit) {
+                atomicOr(err, kErrBarrierWait);
+                ok = 0;
+                break;
+            }
+            if ((spins & 255u) == 0u && ld_volatile((const uint32_t*)err) & kErrBarrierWait) {
+                ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Bounding box and keys in one cooperative launch (bounding-box mode): every block
+// writes the min/max of its particles, and after a grid barrier every block reduces all
+// partials and derives the box itself (the same arithmetic, so the same bits in every
+// block and as a batch's kb_bbox), block 0 stores it for the later stages, and every block goes on
+// to the keys of its particles, which it has just read (L2).
+__global__ void __launch_bounds__(kKeyThreads)
+k_bbox_keys(float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos_out, float* mass_out, uint32_t n,
+            uint32_t* __restrict__ keys, uint32_t* __restrict__ hist, int passes, uint32_t* __restrict__ valid_count,
+            float* __restrict__ part, BHParams* __restrict__ params, uint32_t* __restrict__ bar,
+            int* __restrict__ err) {
+    static_assert(kKeyThreads == kBBoxThreads, "one block shape for both halves");
+    pdl_enter();
+    const float4 m = bbox_block_minmax(grid_blk(), pos_in, n);
+    if (threadIdx.x == 0) {
+        part[4 * blockIdx.x + 0] = m.x;
+        part[4 * blockIdx.x + 1] = m.y;
+        part[4 * blockIdx.x + 2] = m.z;
+        part[4 * blockIdx.x + 3] = m.w;
+    }
+    if (!grid_sync(bar, gridDim.x, err)) return;
+    __shared__ BHParams sp;
+    const float4 e = bbox_reduce_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+        sp = bbox_params(e);
+        if (blockIdx.x == 0) *params = sp;
+    }
+    __syncthreads();
+    keygen_body(grid_blk(), 1, &sp, pos_in, mass_in, pos_out, mass_out, n, keys, hist, passes, valid_count);
+}
+
 
 // ------------------------------------------------------------------------------------
 // onesweep radix pass (stable, 8-bit digit at `shift`)
@@ -840,43 +923,6 @@ __device__ __forceinline__ void top_sums_body(const uint32_t* __restrict__ level
             compute_node<QUAD>(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum, quad);
         __syncthreads();  // level d is complete (and visible to the block) before level d - 1
     }
-}
-
-// Acquire load of a barrier counter.
-__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Barrier over every block of a cooperative launch (all blocks are co-resident, so
-// every block reaches it).  Block leaders count arrivals on `bar` and wait for `target`;
-// the wait is bounded, and a block that gives up sets the error flag, which makes the
-// others stop waiting too.  Returns false after a failed wait.
-__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, int* err) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();  // this block's moments are visible before it is counted
-        atomicAdd(bar, 1u);
-        int ok = 1;
-        uint32_t spins = 0;
-        while (ld_acquire_u32(bar) < target) {
-            if (++spins > kSpinLimit) {
-                atomicOr(err, kErrBarrierWait);
-                ok = 0;
-                break;
-            }
-            if ((spins & 255u) == 0u && ld_volatile((const uint32_t*)err) & kErrBarrierWait) {
-                ok = 0;
-                break;
-            }
-            __nanosleep(32);
-        }
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
 }
 
 // Moments of every level in one cooperative launch: levels D .. kLevelTop + 1 spread over
@@ -1520,6 +1566,10 @@ cudaError_t bh_init(gs_sim* s) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     if (e == cudaSuccess && per_sm < 1) e = cudaErrorCooperativeLaunchTooLarge;
     w.sums_grid = per_sm * sms;
+    // the cooperative box-and-keys launch: the keygen grid, if it fits on the device at once
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bbox_keys, kKeyThreads, 0);
+    if (e == cudaSuccess && per_sm < 1) e = cudaErrorCooperativeLaunchTooLarge;
+    w.keys_grid = std::min(keygen_blocks(s->n_al), per_sm * sms);
     return e;
 }
 
@@ -1583,17 +1633,16 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
         first = false;
         return r;
     };
-    if (bbox) {
-        stage_begin(s, kStageBBox, profile);
-        GS_TRY_LAUNCH(launch(next_pdl(), k_bbox, bbox_blocks(n), kBBoxThreads, st, s->pos[in], n, w.bbox_part,
-                             ctr + kCtrBBox, w.params));
-        count_launch(s);
-        stage_end(s, kStageBBox, profile);
-    }
     stage_begin(s, kStageKeys, profile);
-    GS_TRY_LAUNCH(launch(next_pdl(), k_keygen, keygen_blocks(n), kKeyThreads, st, bbox ? 1 : 0,
-                         (const BHParams*)w.params, s->pos[in], s->mass[in], s->pos[out], s->mass[out], n, w.keys[0],
-                         w.hist, w.passes, ctr + kCtrValid));
+    if (bbox) {  // box and keys in one cooperative launch
+        GS_TRY_LAUNCH(launch_coop(next_pdl(), k_bbox_keys, w.keys_grid, kKeyThreads, st, s->pos[in], s->mass[in],
+                                  s->pos[out], s->mass[out], n, w.keys[0], w.hist, w.passes, ctr + kCtrValid,
+                                  w.bbox_part, w.params, ctr + kCtrBarrier + 1, s->d_err));
+    } else {
+        GS_TRY_LAUNCH(launch(next_pdl(), k_keygen, keygen_blocks(n), kKeyThreads, st, 0,
+                             (const BHParams*)w.params, s->pos[in], s->mass[in], s->pos[out], s->mass[out], n,
+                             w.keys[0], w.hist, w.passes, ctr + kCtrValid));
+    }
     count_launch(s);
     stage_end(s, kStageKeys, profile);
     stage_begin(s, kStageSort, profile);

@@ -74,6 +74,7 @@ struct BHWork {
     float4* quad = nullptr;            // [cap] {sxx, sxy, syy, -} (GS_FLAG_QUADRUPOLE)
     float* amag = nullptr;             // [n_al] |a| of the last step, NaN: unknown (GS_FLAG_RELATIVE_MAC)
     int sums_grid = 0;                 // blocks of the cooperative moments launch (all co-resident)
+    int keys_grid = 0;                 // blocks of the cooperative box-and-keys launch
     uint4* kids = nullptr;             // [cap] child descriptors of internal records
     uint32_t* levels = nullptr;        // internal records by level (level_off / level_cap in bh.cu)
     uint2* nodeinfo = nullptr;         // [cap] {a key of the cell, level} of an internal record
