@@ -5,8 +5,8 @@ r <= 100, two-arm logarithmic spiral, pitch 15 deg, amplitude 0.3, circular velo
 from the enclosed mass + 5% dispersion, masses U[1,10]), softening 0.2, dt = 1e-3,
 seeded synthetic input, gated at <= 1e-3 RMS relative force error against the FP64
 direct sum at every measured step: accurate mode (bounding box, quadrupoles, safe opening
-radius, group walk) with the relative opening criterion, alpha = 0.006 and theta = 0.3 as
-its floor.  Beside it: the same accurate mode with the geometric criterion alone at
+radius, group walk) with the relative opening criterion, alpha = 0.006 with a theta floor
+of 0.3 (the first step, which has no previous |a|, uses theta = 0.35).  Beside it: the same accurate mode with the geometric criterion alone at
 theta = 0.35 (the cheapest theta that holds the gate at every step), and the reference's
 own opening rule at theta = 1 (fixed +-500 box, monopoles, warp vote) with its error; the
 latter does not meet the gate.  A step is one simulation step of the whole system.
@@ -16,7 +16,7 @@ latter does not meet the gate.  A step is one simulation step of the whole syste
   e2e    the same metric through the C ABI with host buffers: every step uploads the
          state from pinned host memory (gs_set_particles), runs one step (gs_run) and
          reads the state back (gs_get_particles), host wall clock.  An upload forgets
-         the previous |a|, so these steps open nodes by the theta floor alone
+         the previous |a|, so these steps open nodes by theta = 0.35 alone
   roofline  the traversal kernel: algorithmic FLOP of the accepted interactions
          (14 per monopole, 33 per quadrupole) over its CUDA-event time, against the
          FP32 FMA rate
@@ -63,11 +63,11 @@ def workloads():
 
     spiral = dict(algo=gsim.BARNES_HUT, gen=gsim.GEN_SPIRAL, n=500000, size=100.0, seed=2002)
     return {
-        "bh500k": dict(spiral, box=gsim.BOX_BOUNDING, theta=0.3, alpha=0.006, flags=ACCURATE | RELATIVE,
+        "bh500k": dict(spiral, box=gsim.BOX_BOUNDING, theta=0.35, alpha=0.006, floor=0.3, flags=ACCURATE | RELATIVE,
                        oracle_flags=15,
                        desc="Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, safe "
                             "radius, 64-particle group walk), relative opening criterion alpha=0.006 with "
-                            "theta=0.3 floor, softening 0.2, dt=1e-3"),
+                            "theta floor 0.3 (theta=0.35 without a previous |a|), softening 0.2, dt=1e-3"),
         "bh500k-theta": dict(spiral, box=gsim.BOX_BOUNDING, theta=0.35, flags=ACCURATE, oracle_flags=7,
                              desc="Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, "
                                   "safe radius, 64-particle group walk), geometric criterion theta=0.35, "
@@ -170,7 +170,8 @@ def reduce_op(dist, x, op):
 
 def make_params(gsim, wl, local, flags):
     return gsim.default_params(algorithm=wl["algo"], box_mode=wl["box"], accuracy_parameter=wl["theta"],
-                               relative_accuracy=wl.get("alpha", 0.0), device=local, flags=wl["flags"] | flags)
+                               relative_accuracy=wl.get("alpha", 0.0), relative_theta_floor=wl.get("floor", 0.0),
+                               device=local, flags=wl["flags"] | flags)
 
 
 def step_errors(gsim, params, pos, vel, mass, sub, steps):
@@ -270,18 +271,20 @@ def batch_specs(count=512, seed=1004, lo=1024, hi=262144):
     return [(int(k), int(x), seed * 1000 + j) for j, (k, x) in enumerate(zip(kind, n))]
 
 
-def batch_params(gsim, local, n, crossover, theta, alpha, flags=0):
+def batch_params(gsim, local, n, crossover, theta, alpha, floor=0.0, flags=0):
     """Direct sum below the crossover; above it accurate-mode Barnes-Hut with the relative
-    criterion (alpha > 0, theta its floor) or theta alone (alpha = 0)."""
+    criterion (alpha > 0, with its theta floor; theta for steps without a previous |a|) or
+    theta alone (alpha = 0)."""
     if n < crossover:
         return gsim.default_params(algorithm=gsim.DIRECT_SUM, device=local, flags=flags)
     return gsim.default_params(algorithm=gsim.BARNES_HUT, box_mode=gsim.BOX_BOUNDING, accuracy_parameter=theta,
-                               relative_accuracy=alpha, device=local,
+                               relative_accuracy=alpha, relative_theta_floor=floor, device=local,
                                flags=ACCURATE | (RELATIVE if alpha > 0 else 0) | flags)
 
 
-def bh_mode_desc(theta, alpha):
-    return (f"relative criterion alpha={alpha:g} with theta={theta:g} floor" if alpha > 0 else f"theta={theta:g}")
+def bh_mode_desc(theta, alpha, floor=0.0):
+    return (f"relative criterion alpha={alpha:g} with theta floor {floor or theta:g}, theta={theta:g} without a "
+            f"previous |a|" if alpha > 0 else f"theta={theta:g}")
 
 
 def measure_batched(gsim, torch, args, local):
@@ -290,15 +293,15 @@ def measure_batched(gsim, torch, args, local):
     each with its own step graph), both timed with CUDA events on the device."""
     t_setup = time.perf_counter()
     d = gsim.default_params(algorithm=gsim.DIRECT_SUM, device=local)
-    theta, alpha = args.batch_theta, args.batch_alpha
-    h = batch_params(gsim, local, 1 << 30, 0, theta, alpha)
+    theta, alpha, floor = args.batch_theta, args.batch_alpha, args.batch_floor
+    h = batch_params(gsim, local, 1 << 30, 0, theta, alpha, floor)
     tune = gsim.tune_crossover(d, h, min_n=1024, max_n=262144, particles_per_probe=1 << 21, seed=4000)
     xo = tune["crossover"]
     specs = batch_specs()
     sims = []
     for kind, n, seed in specs:
         pos, vel, mass = gsim.generate(kind, n, size=100.0, seed=seed)
-        sims.append(gsim.Simulation(pos, vel, mass, params=batch_params(gsim, local, n, xo, theta, alpha)))
+        sims.append(gsim.Simulation(pos, vel, mass, params=batch_params(gsim, local, n, xo, theta, alpha, floor)))
     total_n = float(sum(n for _, n, _ in specs))
     n_bh = sum(1 for _, n, _ in specs if n >= xo)
     setup_s = time.perf_counter() - t_setup
@@ -351,7 +354,7 @@ def measure_batched(gsim, torch, args, local):
         kind, n, seed = specs[j]
         pos, vel, mass = sims[j].get_particles()
         sub = rng.choice(n, min(1024, n), replace=False).astype(np.uint32)
-        e = step_errors(gsim, batch_params(gsim, local, n, xo, theta, alpha), pos, vel, mass, sub, 1)[0]
+        e = step_errors(gsim, batch_params(gsim, local, n, xo, theta, alpha, floor), pos, vel, mass, sub, 1)[0]
         errs.append({"n": n, "kind": "spiral" if kind == gsim.GEN_SPIRAL else "uniform disk",
                      "algorithm": "barnes-hut" if n >= xo else "direct", "rms": float(np.sqrt(np.mean(e ** 2))),
                      "max": float(e.max())})
@@ -359,7 +362,8 @@ def measure_batched(gsim, torch, args, local):
         s.close()
     value = total_n * steps / dev_b
     plain = total_n * steps / dev_p
-    return {"workload": BATCH_DESC % bh_mode_desc(theta, alpha), "theta": theta, "alpha": alpha, "value": value, "unit": "particle-steps/s", "steps": steps,
+    return {"workload": BATCH_DESC % bh_mode_desc(theta, alpha, floor), "theta": theta, "alpha": alpha,
+            "theta_floor": floor, "value": value, "unit": "particle-steps/s", "steps": steps,
             "ms_per_step": dev_b * 1e3 / steps, "systems": len(specs), "particles": int(total_n),
             "barnes_hut_systems": n_bh, "direct_systems": len(specs) - n_bh, "crossover_n": xo, "tuning": tune,
             "kernels_per_step": kps, "gpu_launches": kps * steps,
@@ -394,13 +398,13 @@ def _latency_summary(lat):
             "mean_s": float(lat.mean()), "max_s": float(lat.max())}
 
 
-def measure_served(gsim, torch, args, local, crossover, theta, alpha):
+def measure_served(gsim, torch, args, local, crossover, theta, alpha, floor):
     """The served workload through gs_server (continuous batching, admission by device
     footprint), and the plain sequential path on the same trace: each request in arrival
     order, generated, created, run with gs_run and read back, one at a time."""
     reqs, arrivals = serve_trace(args.serve_requests)
     d = gsim.default_params(algorithm=gsim.DIRECT_SUM, device=local)
-    b = batch_params(gsim, local, 1 << 30, 0, theta, alpha)
+    b = batch_params(gsim, local, 1 << 30, 0, theta, alpha, floor)
     work = float(sum(r.particle_count * r.steps for r in reqs))
     with gsim.Server(150 * 10 ** 9, crossover, d, b, max_resident_particles=args.serve_max_particles,
                      steps_in_flight=2, policy=gsim.SERVE_FIFO) as srv:
@@ -430,8 +434,8 @@ def measure_served(gsim, torch, args, local, crossover, theta, alpha):
         lat_p.append(time.perf_counter() - start - a)
     makespan_p = time.perf_counter() - start - float(arrivals[0])
     plain = {"value": work / makespan_p, "makespan_s": makespan_p, "latency": _latency_summary(lat_p)}
-    return {"workload": SERVE_DESC % bh_mode_desc(theta, alpha), "requests": len(reqs), "theta": theta,
-            "alpha": alpha, "crossover_n": crossover,
+    return {"workload": SERVE_DESC % bh_mode_desc(theta, alpha, floor), "requests": len(reqs), "theta": theta,
+            "alpha": alpha, "theta_floor": floor, "crossover_n": crossover,
             "particle_steps": work, "value": served["value"], "unit": "particle-steps/s", "served": served,
             "plain_sequential": plain, "speedup_vs_plain": served["value"] / plain["value"],
             "max_resident_particles": args.serve_max_particles, "policy": "fifo with conservative backfill"}
@@ -538,7 +542,7 @@ def cpu_baseline(wl, pos, vel, mass, seconds_budget=30.0):
     if wl["algo"] == 1:
         st = oracle.State(pos, vel, mass)
         kw = dict(box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads, flags=wl["oracle_flags"],
-                  rel_alpha=wl.get("alpha", 0.0))
+                  rel_alpha=wl.get("alpha", 0.0), rel_floor=wl.get("floor"))
         r = oracle.bh_step(st, walk_stride=16, **kw)  # time estimate
         est = r["build_seconds"] + 16 * r["walk_seconds"]
         stride = max(1, int(np.ceil(est / seconds_budget)))
@@ -575,7 +579,7 @@ def run_reference(args, wl):
     budget = 150.0 / max(1, args.steps + args.warmup)  # whole run within a few minutes
     stride, times = 1, []
     kw = dict(box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads, flags=wl["oracle_flags"],
-              rel_alpha=wl.get("alpha", 0.0))
+              rel_alpha=wl.get("alpha", 0.0), rel_floor=wl.get("floor"))
     for k in range(args.warmup + args.steps):
         if wl["algo"] == 1:
             if k == 0:  # a full step: time estimate, and every particle's |a| for the next
@@ -619,8 +623,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-system batched line")
     ap.add_argument("--batch-steps", type=int, default=50)
-    ap.add_argument("--batch-theta", type=float, default=0.3,
-                    help="theta of the batched and served Barnes-Hut systems (the floor with --batch-alpha > 0)")
+    ap.add_argument("--batch-theta", type=float, default=0.35,
+                    help="theta of the batched and served Barnes-Hut systems (steps without a previous |a|)")
+    ap.add_argument("--batch-floor", type=float, default=0.3,
+                    help="theta floor of the relative criterion of the batched and served systems")
     ap.add_argument("--batch-alpha", type=float, default=0.006,
                     help="relative criterion alpha of the batched and served Barnes-Hut systems (0: theta alone)")
     ap.add_argument("--no-served", action="store_true", help="skip the served (request stream) line")
@@ -692,7 +698,7 @@ def main():
         batched = measure_batched(gsim, torch, args, local)
     if rank == 0 and world == 1 and not args.no_served:
         xo = batched["crossover_n"] if batched else 2500
-        served = measure_served(gsim, torch, args, local, xo, args.batch_theta, args.batch_alpha)
+        served = measure_served(gsim, torch, args, local, xo, args.batch_theta, args.batch_alpha, args.batch_floor)
     precision = None
     if rank == 0 and world == 1 and not args.no_precision:
         precision = precision_study(gsim, torch, args, local)

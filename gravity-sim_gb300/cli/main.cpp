@@ -53,8 +53,9 @@ const char* kHelp =
     "\t--no-graphics: Accepted for compatibility; every run is headless.\n"
     "\t--benchmark: Reports the wall-clock runtime of all simulations.\n"
     "\t--accurate: Barnes-Hut accurate mode (quadrupoles, safe opening radius, group walk).\n"
-    "\t--relative-accuracy: With --accurate, open nodes by the relative criterion with this alpha,\n"
-    "\t\tthe accuracy parameter as its floor (0.006 with 0.3: about 1e-3 RMS force error).\n";
+    "\t--relative-accuracy: With --accurate, open nodes by the relative criterion with this alpha\n"
+    "\t\t(0.006 with floor 0.3 and accuracy parameter 0.35: about 1e-3 RMS force error).\n"
+    "\t--relative-floor: The theta floor of that criterion, defaulted to the accuracy parameter.\n";
 
 struct Logger {
     FILE* file = nullptr;
@@ -89,6 +90,7 @@ int main(int argc, char** argv) {
     float gen_size = 0, min_mass = 0, max_mass = 0, G = 1.0f, dt = 0.001f, speed = 1.0f, eps = 0.2f, theta = 1.0f;
     bool detailed = false, benchmark = false, accurate = false, have_steps = false;
     float rel_alpha = -1.0f;  // < 0: theta criterion
+    float rel_floor = 0.0f;   // 0: the accuracy parameter
     int box = GS_BOX_FIXED_500, math = GS_MATH_FAST;
     for (int i = 1; i < argc; ++i) {
         const char* a = argv[i];
@@ -122,6 +124,7 @@ int main(int argc, char** argv) {
         else if (starts(a, "--softening-len=", &v)) eps = std::strtof(v, nullptr);
         else if (starts(a, "--accuracy-parameter=", &v)) theta = std::strtof(v, nullptr);
         else if (starts(a, "--relative-accuracy=", &v)) rel_alpha = std::strtof(v, nullptr);
+        else if (starts(a, "--relative-floor=", &v)) rel_floor = std::strtof(v, nullptr);
         else if (starts(a, "--simulation-algorithm=", &v)) {
             if (!std::strcmp(v, "direct-sum")) algo = GS_DIRECT_SUM;
             else if (!std::strcmp(v, "barnes-hut")) algo = GS_BARNES_HUT;
@@ -168,7 +171,10 @@ int main(int argc, char** argv) {
                                             dt, speed, eps, theta, sa, seed, 0, flags));
         system->GetParams().box_mode = box;
         system->GetParams().math_mode = math;
-        if (rel_alpha >= 0.0f) system->GetParams().relative_accuracy = rel_alpha;
+        if (rel_alpha >= 0.0f) {
+            system->GetParams().relative_accuracy = rel_alpha;
+            system->GetParams().relative_theta_floor = rel_floor;
+        }
         log.log("INFO", false, "%zu particles (%zu aligned), algorithm %s", system->GetParticleCount(),
                 system->GetAlignedParticleCount(), algo == GS_BARNES_HUT ? "barnes-hut" : "direct-sum");
         std::unique_ptr<detail::SimulationBase> sim;

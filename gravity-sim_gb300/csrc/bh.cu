@@ -1250,7 +1250,8 @@ __device__ __forceinline__ void force_group_body(
     const float4* __restrict__ quad, const uint4* __restrict__ kids, const float2* __restrict__ pos_in,
     const float2* __restrict__ vel_in, float2* __restrict__ pos_out, float2* __restrict__ vel_out,
     float2* __restrict__ acc_rec, uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
-    unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha) {
+    unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha,
+    float floor2) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t group = blk.id * kGroupWarps + warp;
     const uint32_t nv = counts[0];
@@ -1352,7 +1353,7 @@ __device__ __forceinline__ void force_group_body(
             if (relative) {  // m^2 R^3 <= tol^2 D^5 with R <= D (R: squared opening radius), or theta
                 const float lhs = (q.z * q.z) * ((q.w * q.w) * q.w);
                 const float d4 = d2 * d2;
-                accept = (q.w <= d2 && lhs <= tol2 * ((d4 * d4) * d2)) || q.w <= d2 * theta2;
+                accept = (q.w <= d2 && lhs <= tol2 * ((d4 * d4) * d2)) || q.w <= d2 * floor2;
             } else {
                 accept = q.w <= d2 * theta2;
             }
@@ -1468,12 +1469,13 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
               const uint4* __restrict__ kids, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
               float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
               uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
-              unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha) {
+              unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha,
+              float floor2) {
     pdl_enter();
     __shared__ GroupSmem smem[kGroupWarps];
     force_group_body<EXACT, QUAD, COUNT>(grid_blk(), smem[threadIdx.x >> 5], sidx, skey, counts, rec, skip, quad,
                                          kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2, theta2, k, hdt,
-                                         cap, stat, err, amag, alpha);
+                                         cap, stat, err, amag, alpha, floor2);
 }
 
 int grid_for(uint64_t n, int threads) {
@@ -1705,7 +1707,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
                              (const float4*)w.rec, (const uint32_t*)w.skip, (const float4*)w.quad,
                              (const uint4*)w.kids, (const float2*)s->pos[in], (const float2*)s->vel[in], s->pos[out],
                              s->vel[out], s->acc, n, s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err,
-                             w.amag, s->p.relative_accuracy));
+                             w.amag, s->p.relative_accuracy, s->floor2));
     } else {
         auto fn = exact ? (count ? k_force<true, true> : k_force<true, false>)
                         : (count ? k_force<false, true> : k_force<false, false>);
@@ -1946,7 +1948,8 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kb_force_group(BatchArgs a, 
                                              d.counters + kCtrValid, d.rec, d.skip, d.quad, d.kids, d.pos[bb.in],
                                              d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2,
                                              d.theta2, d.k, d.hdt, d.cap,
-                                             (unsigned long long*)(d.counters + kCtrStat), d.err, d.amag, d.alpha);
+                                             (unsigned long long*)(d.counters + kCtrStat), d.err, d.amag, d.alpha,
+                                             d.floor2);
     }
 }
 
@@ -1992,6 +1995,7 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
     d.quad = w.quad;
     d.amag = w.amag;
     d.alpha = s->p.relative_accuracy;
+    d.floor2 = s->floor2;
     d.kids = w.kids;
     d.levels = w.levels;
     d.nodeinfo = w.nodeinfo;

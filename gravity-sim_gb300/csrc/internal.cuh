@@ -119,7 +119,7 @@ struct SysDesc {
     float2* msum;
     float4* quad;
     float* amag;      // relative criterion: |a| per particle, or null for the theta test
-    float alpha;
+    float alpha, floor2;
     uint4* kids;
     uint32_t* levels;
     uint2* nodeinfo;
@@ -170,6 +170,7 @@ struct gs_sim {
     float* mass[2] = {nullptr, nullptr};
     int in = 0;  // compute-input set
     float dt_eff = 0, G = 0, eps2 = 0, theta2 = 0;
+    float floor2 = 0;       // squared theta floor of the relative criterion
     float2* acc = nullptr;  // GS_FLAG_RECORD_ACCEL
     int* d_err = nullptr;
     gsim::BHWork bh;

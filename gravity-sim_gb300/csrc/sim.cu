@@ -217,6 +217,7 @@ void gs_params_init(gs_params* p) {
     p->device = 0;
     p->flags = 0;
     p->relative_accuracy = 0.006f;
+    p->relative_theta_floor = 0.0f;
 }
 
 const char* gs_status_string(gs_status s) {
@@ -274,6 +275,9 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
     if ((params->flags & GS_FLAG_RELATIVE_MAC) &&
         !(params->relative_accuracy >= 0.0f && params->relative_accuracy < INFINITY))
         return invalid("gs_create: relative_accuracy must be finite and >= 0");
+    if ((params->flags & GS_FLAG_RELATIVE_MAC) &&
+        !(params->relative_theta_floor >= 0.0f && params->relative_theta_floor < INFINITY))
+        return invalid("gs_create: relative_theta_floor must be finite and >= 0");
     if ((params->flags & GS_FLAG_PLAIN_SUM) && params->algorithm != GS_DIRECT_SUM)
         return invalid("gs_create: GS_FLAG_PLAIN_SUM applies to direct sum only");
     if ((params->flags & (GS_FLAG_QUADRUPOLE | GS_FLAG_SAFE_RADIUS | GS_FLAG_GROUP_WALK)) &&
@@ -301,6 +305,10 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
     s->G = params->gravitational_const;
     s->eps2 = params->softening_len * params->softening_len;
     s->theta2 = params->accuracy_parameter * params->accuracy_parameter;
+    {
+        const float f = params->relative_theta_floor > 0.0f ? params->relative_theta_floor : params->accuracy_parameter;
+        s->floor2 = f * f;
+    }
     s->dt_eff = params->algorithm == GS_BARNES_HUT ? params->simulation_time * params->simulation_speed
                                                    : params->simulation_time;  // direct sum ignores speed
 

@@ -46,7 +46,7 @@ class Params(C.Structure):
                 ("simulation_speed", C.c_float), ("softening_len", C.c_float),
                 ("accuracy_parameter", C.c_float), ("algorithm", C.c_int32), ("box_mode", C.c_int32),
                 ("math_mode", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32),
-                ("relative_accuracy", C.c_float)]
+                ("relative_accuracy", C.c_float), ("relative_theta_floor", C.c_float)]
 
 
 class Stats(C.Structure):

@@ -93,12 +93,13 @@ typedef enum gs_math_mode { GS_MATH_FAST = 0, GS_MATH_REFERENCE = 1 } gs_math_mo
  *     R <= D   and   m^2 R^3 <= (alpha a_min)^2 D^5
  * i.e. m r^3 / d^5 (the size of the first term a quadrupole expansion leaves out) is at
  * most alpha times the smallest |a| the group's particles had in the previous step
- * (without G) -- or when the theta test passes: theta (accuracy_parameter) is a floor
- * that bounds the walk of a group whose smallest |a| is tiny, as near the centre of a
- * disk.  alpha is gs_params.relative_accuracy.  A step with no previous |a| for some
- * particle of the group (the first step after gs_create or gs_set_particles) uses the
- * theta test alone for that group.  alpha = 0.006 with theta = 0.3 gives <= 1e-3 RMS
- * force error on the 500k spiral at every step. */
+ * (without G) -- or when R <= D theta_f^2: the floor theta_f bounds the walk of a group
+ * whose smallest |a| is tiny, as near the centre of a disk.  alpha is
+ * gs_params.relative_accuracy, theta_f gs_params.relative_theta_floor (0: theta).  A
+ * step with no previous |a| for some particle of the group (the first step after
+ * gs_create or gs_set_particles) uses the theta test (accuracy_parameter) alone for that
+ * group.  alpha = 0.006 with floor 0.3 and theta 0.35 gives <= 1e-3 RMS force error on
+ * the 500k spiral at every step. */
 #define GS_FLAG_RELATIVE_MAC 0x100u
 
 typedef struct gs_params {
@@ -113,6 +114,7 @@ typedef struct gs_params {
     int32_t device;            /* CUDA device ordinal */
     uint32_t flags;            /* GS_FLAG_* */
     float relative_accuracy;   /* alpha of GS_FLAG_RELATIVE_MAC, default 0.006 */
+    float relative_theta_floor; /* theta floor of GS_FLAG_RELATIVE_MAC, default 0: accuracy_parameter */
 } gs_params;
 
 typedef struct gs_sim gs_sim;

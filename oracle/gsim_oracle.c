@@ -366,7 +366,7 @@ typedef struct {
     uint32_t* max_stack;    /* per worker */
     uint64_t* max_inter;    /* per worker: largest per-warp interaction count */
     uint32_t group_size;    /* particles per group walk (64) */
-    float rel_alpha;        /* ORC_BH_RELATIVE_MAC: alpha, previous and new |a| per particle */
+    float rel_alpha, rel_floor2; /* ORC_BH_RELATIVE_MAC: alpha, floor^2, previous and new |a| */
     const float* amag_in;
     float* amag_out;
 } walk_ctx;
@@ -529,7 +529,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                     const float lhs = (m * m) * ((r * r) * r);
                     const float d4 = d2 * d2;
                     const float rhs = tol2 * ((d4 * d4) * d2);
-                    accept = (r <= d2 && lhs <= rhs) || r <= d2 * c->theta2;
+                    accept = (r <= d2 && lhs <= rhs) || r <= d2 * c->rel_floor2;
                 } else {
                     accept = c->radius[n] <= d2 * c->theta2;
                 }
@@ -1093,6 +1093,7 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
     wc.hdt = 0.5f * dt;
     if ((flags & ORC_BH_RELATIVE_MAC) && out) {
         wc.rel_alpha = out->rel_alpha;
+        wc.rel_floor2 = out->rel_floor2;
         wc.amag_in = out->amag_in;
         wc.amag_out = out->amag_out;
     }

@@ -73,6 +73,7 @@ typedef struct orc_bh_out {
     uint64_t max_warp_interactions; /* largest interaction count of one warp (valid lanes) */
     /* inputs of ORC_BH_RELATIVE_MAC */
     float rel_alpha;         /* alpha of the relative opening criterion */
+    float rel_floor2;        /* squared theta floor of the relative criterion */
     const float* amag_in;    /* [n_al] |a| of the previous step per particle (NaN: unknown) */
     float* amag_out;         /* [n_al] |a| of this step (written when not NULL) */
 } orc_bh_out;
@@ -115,9 +116,9 @@ int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in
  * distance D (nearest sub-box) when R <= D and m^2 R^3 <= (alpha a_min)^2 D^5, in that
  * FP32 operation order: lhs = (m*m)*((R*R)*R), rhs = tol^2*((D^2*D^2)*D) with
  * tol = alpha*a_min, a_min the smallest previous |a| (without G) of the group's particles
- * (out->amag_in) -- or when the geometric test R <= D theta^2 passes (theta bounds the
- * walk of a group whose a_min is tiny).  A group with an unknown |a| (NaN) uses the
- * geometric test alone. */
+ * (out->amag_in) -- or when R <= D floor^2 (out->rel_floor2; the floor bounds the walk
+ * of a group whose a_min is tiny).  A group with an unknown |a| (NaN) uses the
+ * geometric test R <= D theta^2 alone. */
 #define ORC_BH_RELATIVE_MAC 8
 int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in, float* vel_in,
                           float* mass_in, float* pos_out, float* vel_out, float* mass_out,

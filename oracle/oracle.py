@@ -32,7 +32,7 @@ class BHOut(C.Structure):
                 ("box_center_x", C.c_float), ("box_center_y", C.c_float), ("box_scale", C.c_float),
                 ("box_radius0", C.c_float), ("build_seconds", C.c_double), ("walk_seconds", C.c_double),
                 ("max_stack", C.c_uint32), ("max_warp_interactions", C.c_uint64),
-                ("rel_alpha", C.c_float), ("amag_in", _FP), ("amag_out", _FP)]
+                ("rel_alpha", C.c_float), ("rel_floor2", C.c_float), ("amag_in", _FP), ("amag_out", _FP)]
 
 
 _lib = None
@@ -142,7 +142,7 @@ def direct_accel_f64(pos, mass, softening=0.2, targets=None, threads=os.cpu_coun
 
 
 def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, G=1.0, softening=0.2, theta=1.0,
-            keep_tree=True, threads=os.cpu_count(), walk_stride=1, flags=0, rel_alpha=0.0):
+            keep_tree=True, threads=os.cpu_count(), walk_stride=1, flags=0, rel_alpha=0.0, rel_floor=None):
     """One Barnes-Hut step; returns a dict with keys, sorted_src and the preorder records."""
     (pi, vi, mi), (po, vo, mo) = state.sets()
     n_al = state.n_al
@@ -154,6 +154,8 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
     if flags & RELATIVE_MAC:  # |a| of this step; particles the walk skips keep their value
         amag_out = state.amag.copy()
         out.rel_alpha = rel_alpha
+        f = np.float32(theta if not rel_floor else rel_floor)
+        out.rel_floor2 = float(f * f)
         out.amag_in = _fp(state.amag)
         out.amag_out = _fp(amag_out)
     res = {}

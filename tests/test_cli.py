@@ -28,11 +28,17 @@ def test_argument_checks(gs):
     r = _run(["--particle-count=10", "--generate-type=random", "--generate-size=10", "--min-mass=1",
               "--max-mass=2", "--simulation-algorithm=direct-sum"])
     assert r.returncode == 1 and "simulation count" in r.stdout
+    r = _run(["--particle-count=10", "--generate-type=random", "--generate-size=10", "--min-mass=1",
+              "--max-mass=2", "--simulation-algorithm=barnes-hut", "--simulation-count=5",
+              "--relative-accuracy=0.006"])
+    assert r.returncode == 1 and "needs --accurate" in r.stdout
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("algo,extra", [("barnes-hut", ["--math=reference"]), ("direct-sum", []),
-                                        ("barnes-hut", ["--box=bbox", "--accurate", "--accuracy-parameter=0.35"])])
+                                        ("barnes-hut", ["--box=bbox", "--accurate", "--accuracy-parameter=0.35"]),
+                                        ("barnes-hut", ["--box=bbox", "--accurate", "--accuracy-parameter=0.35",
+                                                        "--relative-accuracy=0.006", "--relative-floor=0.3"])])
 def test_file_roundtrip_matches_binding(gs, tmp_path, algo, extra):
     pos, vel, mass = gs.generate(gs.GEN_GALAXY, 3000, size=100.0, seed=17)
     fin, fout = str(tmp_path / "in.txt"), str(tmp_path / "out.txt")
@@ -47,6 +53,8 @@ def test_file_roundtrip_matches_binding(gs, tmp_path, algo, extra):
         kw["math_mode"] = gs.MATH_REFERENCE
     if "--box=bbox" in extra:
         kw.update(box_mode=gs.BOX_BOUNDING, flags=gs.FLAGS_ACCURATE, accuracy_parameter=0.35)
+    if "--relative-accuracy=0.006" in extra:
+        kw.update(flags=gs.FLAGS_ACCURATE | gs.FLAG_RELATIVE_MAC, relative_accuracy=0.006, relative_theta_floor=0.3)
     with gs.Simulation(p2, v2, m2, **kw) as sim:
         sim.run(7)
         p, v, m = sim.get_particles()

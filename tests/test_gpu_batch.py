@@ -150,13 +150,14 @@ def test_tuner_smoke(gs):
 
 
 def test_relative_criterion_batch_bit_identical(gs):
-    """Members with the relative opening criterion and different alphas: each keeps its
-    own |a| buffer and alpha in the batch and matches its twin stepped alone, through a
+    """Members with the relative opening criterion and different alphas and floors: each
+    keeps its own |a| buffer, alpha and floor in the batch and matches its twin alone, through a
     first step (theta test) and later ones (relative test)."""
     rel = dict(algorithm=1, box_mode=1, flags=0x170 | 0x8, accuracy_parameter=0.5)
-    specs = [(17, 30000, 100.0, dict(rel, relative_accuracy=0.007)),
+    specs = [(17, 30000, 100.0, dict(rel, relative_accuracy=0.007, relative_theta_floor=0.3)),
              (16, 5000, 100.0, dict(rel, relative_accuracy=0.02)),
-             (17, 700, 100.0, dict(rel, relative_accuracy=0.001)), (16, 2000, 100.0, DIRECT)]
+             (17, 700, 100.0, dict(rel, relative_accuracy=0.001, relative_theta_floor=0.4)),
+             (16, 2000, 100.0, DIRECT)]
     alone = _make(gs, specs, 1500)
     batched = _make(gs, specs, 1500)
     for s in alone + batched:

@@ -209,24 +209,25 @@ REL = ACC | 0x100
 
 
 @pytest.mark.parametrize("box", [0, 1])
-@pytest.mark.parametrize("kind,n,size,alpha", [(17, 3000, 100.0, 0.007), (2, 2500, 700.0, 0.02),
-                                               (16, 64, 100.0, 0.007), (0, 777, 100.0, 0.0)])
-def test_relative_criterion_bit_exact(gs, orc, box, kind, n, size, alpha):
+@pytest.mark.parametrize("kind,n,size,alpha,floor", [(17, 3000, 100.0, 0.007, 0.3), (2, 2500, 700.0, 0.02, 0.0),
+                                                     (16, 64, 100.0, 0.007, 0.25), (0, 777, 100.0, 0.0, 0.0)])
+def test_relative_criterion_bit_exact(gs, orc, box, kind, n, size, alpha, floor):
     """REFERENCE math over three steps (the first takes the theta test, the next ones the
-    relative test on the |a| the step before left), then again after gs_set_particles,
-    which forgets |a|: state, interaction and visit counts bit-identical to the oracle."""
+    relative test on the |a| the step before left, with its floor; floor 0 is theta),
+    then again after gs_set_particles, which forgets |a|: state, interaction and visit
+    counts bit-identical to the oracle."""
     pos, vel, mass = gs.generate(kind, n, size=size, seed=43)
     st = orc.State(pos, vel, mass)
     flags = orc.ACCURATE | orc.RELATIVE_MAC
     with _sim(gs, pos, vel, mass, box_mode=box, math_mode=gs.MATH_REFERENCE, accuracy_parameter=0.35,
-              relative_accuracy=alpha, flags=REL | gs.FLAG_COUNT_INTERACTIONS) as sim:
+              relative_accuracy=alpha, relative_theta_floor=floor, flags=REL | gs.FLAG_COUNT_INTERACTIONS) as sim:
         for step in range(4):
             if step == 3:
                 sim.set_particles(pos, vel, mass)
                 st = orc.State(pos, vel, mass)
             sim.reset_stats()
             sim.run(1)
-            o = orc.bh_step(st, box_mode=box, theta=0.35, flags=flags, rel_alpha=alpha)
+            o = orc.bh_step(st, box_mode=box, theta=0.35, flags=flags, rel_alpha=alpha, rel_floor=floor)
             s = sim.stats()
             assert (s.interactions, s.warp_visits) == (o["interactions"], o["warp_visits"]), step
             for g, c in zip(sim.get_particles(), st.current()):
@@ -234,17 +235,18 @@ def test_relative_criterion_bit_exact(gs, orc, box, kind, n, size, alpha):
 
 
 def test_relative_criterion_500k_error_gate(gs):
-    """N=500,000 spiral, bounding box, alpha=0.006 with theta=0.3 as the floor: the second
-    step (the first with a previous |a|) has RMS relative force error <= 1e-3 against the
-    FP64 direct sum on 4096 particles, with fewer interactions than theta=0.35 alone."""
+    """N=500,000 spiral, bounding box, alpha=0.006 with floor 0.3 and theta 0.35 (the
+    first step): the second step (the first with a previous |a|) has RMS relative force
+    error <= 1e-3 against the FP64 direct sum on 4096 particles, with fewer interactions
+    than theta=0.35 alone."""
     n = 500000
     pos, vel, mass = gs.generate(gs.GEN_SPIRAL, n, seed=2002)
     sub = np.random.default_rng(0).choice(n, 4096, replace=False).astype(np.uint32)
     counts = {}
     for rel in (True, False):
         flags = (REL if rel else ACC) | gs.FLAG_RECORD_ACCEL | gs.FLAG_COUNT_INTERACTIONS
-        with _sim(gs, pos, vel, mass, box_mode=1, accuracy_parameter=0.3 if rel else 0.35,
-                  relative_accuracy=0.006, flags=flags) as sim:
+        with _sim(gs, pos, vel, mass, box_mode=1, accuracy_parameter=0.35, relative_accuracy=0.006,
+                  relative_theta_floor=0.3, flags=flags) as sim:
             sim.run(1)
             p1, v1, m1 = sim.get_particles()
             sim.reset_stats()

@@ -150,11 +150,12 @@ def _acc_err(orc, pos, vel, mass, v1, sub, dt=1e-3):
 
 
 def test_relative_criterion_first_step_is_theta(gs, orc):
-    """With no previous |a| (NaN) every group takes the theta test: the step is the
-    theta step bit for bit, and it leaves |a| of every particle behind."""
+    """With no previous |a| (NaN) every group takes the theta test (not the floor): the
+    step is the theta step bit for bit, and it leaves |a| of every particle behind."""
     pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 5000, seed=16)
     a, b = orc.State(pos, vel, mass), orc.State(pos, vel, mass)
-    ra = orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.4, flags=orc.ACCURATE | orc.RELATIVE_MAC, rel_alpha=0.01)
+    ra = orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.4, flags=orc.ACCURATE | orc.RELATIVE_MAC, rel_alpha=0.01,
+                     rel_floor=0.2)
     rb = orc.bh_step(b, box_mode=orc.BOX_BOUNDING, theta=0.4, flags=orc.ACCURATE)
     assert ra["interactions"] == rb["interactions"]
     for x, y in zip(a.current(), b.current()):
