@@ -38,7 +38,7 @@ constexpr int kErrBarrierWait = 8;
 
 // radix sort shape: 256 threads x 8 keys per tile
 constexpr int kSortThreads = 256;
-constexpr int kSortKeysPerThread = 8;
+constexpr int kSortKeysPerThread = 16;
 constexpr int kSortTile = kSortThreads * kSortKeysPerThread;
 // single-pass scan shape
 constexpr int kScanThreads = 256;
