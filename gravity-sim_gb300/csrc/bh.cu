@@ -1038,15 +1038,16 @@ k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, 
 // accepted nodes and runs of particle leaves are collected and every lane then sums them
 // for its two particles with packed f32x2 instructions (quadrupole term for nodes).
 // ------------------------------------------------------------------------------------
-constexpr int kGroupWarps = 4;
+constexpr int kGroupWarps = 2;
 constexpr int kGroupSize = 64;  // particles per walk
 // Records still to test.  Pops take the top 32 and push at most four internal children
 // each, one level deeper, so the stack holds at most one block of <= 128 entries per level
-// and blocks of strictly increasing level: <= 96 * D + 128 = 1568 for D = 15 (a full
-// four-way tree reaches 1216).  Overflow is still checked and reported.
-constexpr int kStackCap = 1600;
+// and blocks of strictly increasing level: <= 96 * D + 128 = 1280 for D = 12.  Overflow
+// is still checked and reported.
+constexpr int kStackCap = 1280;
+static_assert(kStackCap >= 96 * (kBBoxBits > kFixedDepth ? kBBoxBits : kFixedDepth) + 128, "walk stack bound");
 constexpr int kItemCap = 128;     // runs of particle leaves between evaluations
-constexpr int kNodeCap = 96;      // accepted nodes between evaluations
+constexpr int kNodeCap = 160;     // accepted nodes between evaluations
 
 // 1/sqrt: correctly rounded (REFERENCE math) or the hardware approximation (FAST math;
 // d2 >= eps^2 > 0 is never subnormal, so the flush-to-zero form loses nothing)
@@ -1511,7 +1512,7 @@ void bh_carve(gs_sim* s) {
     const uint64_t n = s->n_al;
     const bool bbox = s->p.box_mode == GS_BOX_BOUNDING;
     w.depth = bbox ? kBBoxBits : kFixedDepth;
-    w.passes = bbox ? 4 : 3;  // 30-bit keys / 20-bit keys + removal bit
+    w.passes = 3;  // 24-bit keys (bounding box) / 20-bit keys + removal bit (fixed box)
     w.cap = bh_capacity(s->p.box_mode, n);
     w.sort_tiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     w.scan_tiles = (uint32_t)((n + 1 + kScanTile - 1) / kScanTile);

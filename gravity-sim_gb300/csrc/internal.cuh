@@ -6,7 +6,7 @@
 //   Barnes-Hut scratch (N_al-sized, never a fixed 1024^2 grid):
 //              keys/idx u32[N_al] x 2 (radix-sort ping-pong), E u32[N_al+1] (exclusive
 //              scan of internal nodes per sorted slot), rec float4[cap] = {x, y, m, radius}
-//              and skip u32[cap] (preorder records, cap = N_al + levels*N_al/2 + 64),
+//              and skip u32[cap] (preorder records, cap = N_al + 64 + sum over levels of min(4^d, N_al/2 + 1)),
 //              nend u32[cap] and msum float2[cap] (cell end slot and mass moments)
 #pragma once
 #include <cuda_runtime.h>
@@ -23,7 +23,7 @@ constexpr uint32_t kAlignment = 64;         // GetRequiredParticleAlignment()
 constexpr float kSimSize = 500.0f;          // BarnesHutSimulation.cpp:580
 constexpr uint32_t kGrid = 1024;            // BarnesHutSimulation.cpp:582
 constexpr int kFixedDepth = 10;             // finest level of the fixed box
-constexpr int kBBoxBits = 15;               // per-axis bits in bounding-box mode
+constexpr int kBBoxBits = 12;               // per-axis bits in bounding-box mode (24-bit keys)
 constexpr uint32_t kKeyRemovedSort = 1u << 20;  // sort key of removed particles (fixed box)
 constexpr uint32_t kKeyRemoved = 0xFFFFFFFFu;   // reported key of removed particles
 
@@ -36,7 +36,7 @@ constexpr int kErrScanWait = 2;
 constexpr int kErrTree = 4;
 constexpr int kErrBarrierWait = 8;
 
-// radix sort shape: 256 threads x 8 keys per tile
+// radix sort shape: 256 threads x 16 keys per tile
 constexpr int kSortThreads = 256;
 constexpr int kSortKeysPerThread = 16;
 constexpr int kSortTile = kSortThreads * kSortKeysPerThread;

@@ -55,7 +55,7 @@ typedef enum gs_algorithm { GS_DIRECT_SUM = 0, GS_BARNES_HUT = 1 } gs_algorithm;
 
 /* Barnes-Hut box: the reference's fixed +-500 box with a 1024x1024 finest grid and
  * removal of particles that leave it, or a per-step square bounding box with
- * 2^15 x 2^15 finest cells (30-bit keys) and no removal. */
+ * 2^12 x 2^12 finest cells (24-bit keys) and no removal. */
 typedef enum gs_box_mode { GS_BOX_FIXED_500 = 0, GS_BOX_BOUNDING = 1 } gs_box_mode;
 
 /* FAST: hardware rsqrt; direct sum in shared-memory tiles with Kahan-compensated
@@ -184,7 +184,7 @@ GS_API gs_status gs_debug_bh_tree(gs_sim* sim, uint32_t* keys, uint32_t* sorted_
                            float* node_mass, float* node_quad, uint64_t capacity,
                            uint64_t* tree_records);
 /* Records the tree of aligned_count particles can hold: the leaves plus, for every level
- * d of the box mode (0..10 fixed box, 0..15 bounding box), min(4^d, aligned_count/2 + 1)
+ * d of the box mode (0..10 fixed box, 0..12 bounding box), min(4^d, aligned_count/2 + 1)
  * internal nodes, plus 64. */
 GS_API uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count);
 

@@ -36,7 +36,7 @@
 #define SIM_SIZE 500.0f  /* BarnesHutSimulation.cpp:580 simulationSize */
 #define GRID 1024u       /* BarnesHutSimulation.cpp:582 treeSize */
 #define GRID_LEVELS 11   /* depths 0..10 */
-#define BBOX_BITS 15     /* bounding-box mode: 15 bits per axis, 30-bit keys */
+#define BBOX_BITS 12     /* bounding-box mode: 12 bits per axis, 24-bit keys */
 
 /* ------------------------------------------------------------------------------ */
 /* tiny parallel-for: dynamic chunks over [0, n), deterministic results because   */

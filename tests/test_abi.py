@@ -31,8 +31,8 @@ def test_exports_every_declared_symbol(gs):
 def test_alignment_and_capacity(gs):
     assert gs.required_alignment(gs.DIRECT_SUM) == 64
     assert gs.required_alignment(gs.BARNES_HUT) == 64
-    # leaves + at most min(4^d, n/2 + 1) internal nodes per level d (levels 0..10 / 0..15) + 64
-    for box, depth in ((gs.BOX_FIXED_500, 10), (gs.BOX_BOUNDING, 15)):
+    # leaves + at most min(4^d, n/2 + 1) internal nodes per level d (levels 0..10 / 0..12) + 64
+    for box, depth in ((gs.BOX_FIXED_500, 10), (gs.BOX_BOUNDING, 12)):
         for n in (64, 640, 1 << 20):
             levels = sum(min(4 ** d, n // 2 + 1) for d in range(depth + 1))
             assert gs.node_capacity(box, n) == n + levels + 64

@@ -74,7 +74,7 @@ def test_bounding_box_tree(gs, orc, kind, n):
     check_tree(r, r["box"][3], r["valid_count"])
     keys = r["keys"][r["sorted_src"][: r["valid_count"]]]
     assert np.all(np.diff(keys.astype(np.int64)) >= 0)
-    assert np.all(keys < (1 << 30))
+    assert np.all(keys < (1 << 24))
 
 
 def test_bounding_box_force_accuracy(gs, orc):
