@@ -173,6 +173,7 @@ struct gs_sim {
     float floor2 = 0;       // squared theta floor of the relative criterion
     float2* acc = nullptr;  // GS_FLAG_RECORD_ACCEL
     int* d_err = nullptr;
+    int* h_err = nullptr;   // pinned host copy of d_err (check_device_error)
     gsim::BHWork bh;
     gsim::DirectWork dw;
     cudaEvent_t batch_done = nullptr;

@@ -7,6 +7,7 @@
 // host after every step (ParticleSystem::NextComputeIndices, src/Particles/ParticleSystem.hpp:169-174).
 // Instead of re-recording command buffers, each parity of the ping-pong is captured
 // once into a CUDA graph and replayed.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -125,13 +126,15 @@ gs_status wait_event(cudaEvent_t ev, uint64_t timeout_ns) {
             set_error("timed out waiting for the GPU");
             return GS_ERR_TIMEOUT;
         }
-        std::this_thread::sleep_for(std::chrono::microseconds(20));
+        // spin for the first 2 ms: a sleep lasts the thread's timer slack (50 us on Linux)
+        // on top of the 20 asked for, which is a tenth of a 500k-particle step
+        if (el < 2000000) std::this_thread::yield();
+        else std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
 }
 
-gs_status check_device_error(gs_sim* s) {
-    int err = 0;
-    GS_CUDA(cudaMemcpy(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+// Status of a device error word.
+gs_status device_error(int err) {
     if (err) {
         set_error(std::string("device-side error flags ") + std::to_string(err) +
                   " (1: radix-sort look-back wait ran out, 2: scan look-back wait ran out, 4: tree capacity, "
@@ -139,6 +142,14 @@ gs_status check_device_error(gs_sim* s) {
         return GS_ERR_DEVICE;
     }
     return GS_OK;
+}
+
+// Reads the device error word after everything enqueued so far (one round trip: the copy
+// into the system's pinned word, then the stream synchronisation).
+gs_status check_device_error(gs_sim* s) {
+    GS_CUDA(cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    GS_CUDA(cudaStreamSynchronize(s->stream));
+    return device_error(*s->h_err);
 }
 
 void free_sim(gs_sim* s) {
@@ -154,28 +165,87 @@ void free_sim(gs_sim* s) {
         if (e) cudaEventDestroy(e);
     if (s->batch_done) cudaEventDestroy(s->batch_done);
     if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->h_err) cudaFreeHost(s->h_err);
     delete s;
 }
 
-// upload N host particles into the input set (one host->device copy per array), pad
-// with zero particles, and copy device-side into the other set: both sets start equal,
-// as the reference's staging upload fills all buffer sets (ParticleSystem.cpp:206-217)
-gs_status upload(gs_sim* s, const float* pos, const float* vel, const float* mass) {
-    const size_t n = s->n, pad = s->n_al - s->n;
-    const int a = s->in, b = a ^ 1;
-    GS_CUDA(cudaMemcpyAsync(s->pos[a], pos, n * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
-    if (vel) GS_CUDA(cudaMemcpyAsync(s->vel[a], vel, n * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
-    else GS_CUDA(cudaMemsetAsync(s->vel[a], 0, n * sizeof(float2), s->stream));
-    if (pad) {
-        GS_CUDA(cudaMemsetAsync(s->pos[a] + n, 0, pad * sizeof(float2), s->stream));
-        GS_CUDA(cudaMemsetAsync(s->vel[a] + n, 0, pad * sizeof(float2), s->stream));
+// Device address of a host array that the GPU can read and write in place (pinned or
+// registered host memory of this device, mapped under unified addressing), or null for
+// pageable memory, a device pointer, or an address not aligned to `align` bytes.
+const void* host_mapped(const gs_sim* s, const void* p, uintptr_t align) {
+    if (!p || ((uintptr_t)p & (align - 1))) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
     }
-    GS_CUDA(cudaMemcpyAsync(s->pos[b], s->pos[a], s->n_al * sizeof(float2), cudaMemcpyDeviceToDevice, s->stream));
-    GS_CUDA(cudaMemcpyAsync(s->vel[b], s->vel[a], s->n_al * sizeof(float2), cudaMemcpyDeviceToDevice, s->stream));
-    GS_CUDA(cudaMemcpyAsync(s->mass[0], mass, n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    if (pad) GS_CUDA(cudaMemsetAsync(s->mass[0] + n, 0, pad * sizeof(float), s->stream));
-    // no previous |a| yet: all-ones words are NaN, so the next step uses the theta test
-    if (s->bh.amag) GS_CUDA(cudaMemsetAsync(s->bh.amag, 0xFF, s->n_al * sizeof(float), s->stream));
+    return a.type == cudaMemoryTypeHost && a.device == s->device ? a.devicePointer : nullptr;
+}
+
+// Fills both sets from the N source particles (mapped host arrays read in place, or set a
+// after the copy engine filled it), zeroes the padding slots (and every velocity when none
+// was given) and marks every |a| unknown (all-ones words are NaN, so the next step opens
+// nodes by theta).  The sources may alias set a, so no pointer is restrict-qualified.
+__global__ void k_upload(const float2* src_pos, const float2* src_vel, const float* src_mass, float2* pos_a,
+                         float2* vel_a, float* mass, float2* pos_b, float2* vel_b, float* amag, uint32_t n,
+                         uint32_t n_al) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_al; i += gridDim.x * blockDim.x) {
+        float2 p = make_float2(0.0f, 0.0f), v = p;
+        float m = 0.0f;
+        if (i < n) {
+            p = src_pos[i];
+            if (src_vel) v = src_vel[i];
+            m = src_mass[i];
+        }
+        pos_a[i] = p;
+        pos_b[i] = p;
+        vel_a[i] = v;
+        vel_b[i] = v;
+        mass[i] = m;
+        if (amag) amag[i] = __uint_as_float(0xFFFFFFFFu);
+    }
+}
+
+// Writes the N particles of one set into mapped host arrays (any of them may be null) and
+// the device error word into the system's pinned word.
+__global__ void k_download(const float2* __restrict__ pos, const float2* __restrict__ vel,
+                           const float* __restrict__ mass, float2* __restrict__ host_pos, float2* __restrict__ host_vel,
+                           float* __restrict__ host_mass, uint32_t n, const int* __restrict__ d_err,
+                           int* __restrict__ h_err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (host_pos) host_pos[i] = pos[i];
+        if (host_vel) host_vel[i] = vel[i];
+        if (host_mass) host_mass[i] = mass[i];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *h_err = *d_err;
+}
+
+uint32_t copy_blocks(uint64_t n) { return (uint32_t)std::min<uint64_t>((n + 255) / 256, 152ull * 8); }
+
+// Uploads N host particles into both sets (ParticleSystem.cpp:206-217: the reference's
+// staging upload fills every buffer set) and pads with zero particles.  Pinned host arrays
+// are read in place by one kernel; any other memory goes through the copy engine into set
+// a first.  Returns after the host arrays have been read.
+gs_status upload(gs_sim* s, const float* pos, const float* vel, const float* mass) {
+    const size_t n = s->n;
+    const int a = s->in, b = a ^ 1;
+    const float2* sp = (const float2*)host_mapped(s, pos, 8);
+    const float2* sv = vel ? (const float2*)host_mapped(s, vel, 8) : nullptr;
+    const float* sm = (const float*)host_mapped(s, mass, 4);
+    if (!sp || (vel && !sv) || !sm) {
+        GS_CUDA(cudaMemcpyAsync(s->pos[a], pos, n * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+        sp = s->pos[a];
+        if (vel) {
+            GS_CUDA(cudaMemcpyAsync(s->vel[a], vel, n * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+            sv = s->vel[a];
+        }
+        GS_CUDA(cudaMemcpyAsync(s->mass[0], mass, n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        sm = s->mass[0];
+    }
+    k_upload<<<copy_blocks(s->n_al), 256, 0, s->stream>>>(sp, sv, sm, s->pos[a], s->vel[a], s->mass[0], s->pos[b],
+                                                          s->vel[b], s->bh.amag, (uint32_t)n, (uint32_t)s->n_al);
+    GS_CUDA(cudaGetLastError());
+    ++s->kernel_launches;
     GS_CUDA(cudaStreamSynchronize(s->stream));
     return GS_OK;
 }
@@ -326,6 +396,7 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
     GS_TRY(keep_pool_memory(s->device));
     GS_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     GS_TRY(cudaEventCreateWithFlags(&s->batch_done, cudaEventDisableTiming));
+    GS_TRY(cudaMallocHost((void**)&s->h_err, sizeof(int)));
     for (auto& e : s->ev) GS_TRY(cudaEventCreate(&e));
     carve_all(s);  // sizing pass
     GS_TRY(cudaMallocAsync(&s->slab, s->carved, s->stream));
@@ -410,21 +481,46 @@ gs_status gs_sync(gs_sim* s, uint64_t timeout_ns) {
         if (w != GS_OK) return w;
         s->batch_pending = false;
     }
-    GS_CUDA(cudaStreamSynchronize(s->stream));
     if (s->profile_pending) {
         gs_status a = account_profile(s);
         if (a != GS_OK) return a;
     }
-    return check_device_error(s);
+    return check_device_error(s);  // synchronises the stream
 }
 
 gs_status gs_get_particles(gs_sim* s, float* pos, float* vel, float* mass) {
-    gs_status st = gs_sync(s, 0);
-    if (st != GS_OK) return st;
+    if (!s) return invalid("gs_get_particles: sim is NULL");
+    GS_CUDA(cudaSetDevice(s->device));
+    follow_batch(s);
+    if (s->batch_pending) {
+        gs_status w = wait_event(s->batch_done, 0);
+        if (w != GS_OK) return w;
+        s->batch_pending = false;
+    }
+    if (s->profile_pending) {
+        gs_status a = account_profile(s);
+        if (a != GS_OK) return a;
+    }
     const int in = s->in;  // ParticleSystem::GetParticles reads buffers[computeInputIndex]
-    if (pos) GS_CUDA(cudaMemcpy(pos, s->pos[in], s->n * sizeof(float2), cudaMemcpyDeviceToHost));
-    if (vel) GS_CUDA(cudaMemcpy(vel, s->vel[in], s->n * sizeof(float2), cudaMemcpyDeviceToHost));
-    if (mass) GS_CUDA(cudaMemcpy(mass, s->mass[in], s->n * sizeof(float), cudaMemcpyDeviceToHost));
+    float2* hp = (float2*)host_mapped(s, pos, 8);
+    float2* hv = (float2*)host_mapped(s, vel, 8);
+    float* hm = (float*)host_mapped(s, mass, 4);
+    if ((!pos || hp) && (!vel || hv) && (!mass || hm)) {
+        // pinned arrays: one kernel writes them and the error word, one synchronisation
+        k_download<<<copy_blocks(s->n), 256, 0, s->stream>>>(s->pos[in], s->vel[in], s->mass[in], hp, hv, hm,
+                                                             (uint32_t)s->n, s->d_err, s->h_err);
+        GS_CUDA(cudaGetLastError());
+        ++s->kernel_launches;
+        GS_CUDA(cudaStreamSynchronize(s->stream));
+        return device_error(*s->h_err);
+    }
+    gs_status st = check_device_error(s);
+    if (st != GS_OK) return st;
+    // copies in order on the stream, one synchronisation for all three
+    if (pos) GS_CUDA(cudaMemcpyAsync(pos, s->pos[in], s->n * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    if (vel) GS_CUDA(cudaMemcpyAsync(vel, s->vel[in], s->n * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    if (mass) GS_CUDA(cudaMemcpyAsync(mass, s->mass[in], s->n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    GS_CUDA(cudaStreamSynchronize(s->stream));
     return GS_OK;
 }
 
