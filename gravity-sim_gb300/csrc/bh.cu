@@ -697,22 +697,37 @@ __device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__
                     end = cell_end(skey, s + 1, nv, shift, ks >> shift);
                     kids[at] = make_uint4(kKidFinest, at + 1, end - s, 0u);  // all children are leaves
                 } else {
-                    // the level-(d+1) cells of the cell, in Morton order; the last one ends it
-                    uint32_t kid[4] = {kKidNone, kKidNone, kKidNone, kKidNone};
-                    uint32_t nk = 0;
+                    // The cell ends where its level-d prefix changes (galloping search); its
+                    // level-(d+1) cells, in Morton order, are the runs of prefix 4p + c,
+                    // c = 0..3, inside it.  The ends of the first three are found by three
+                    // binary searches run in lockstep (their loads overlap), so a large cell
+                    // costs about three times log2(size) dependent loads, not four gallops.
+                    end = cell_end(skey, s + 1, nv, shift, ks >> shift);
                     const int cshift = 2 * (D - d - 1);
-                    uint32_t t = s;
-                    do {
-                        const uint32_t tend = cell_end(skey, t + 1, nv, cshift, skey[t] >> cshift);
-                        uint32_t c;
-                        if (tend - t >= 2) c = t + E[t] + (uint32_t)(d + 1 - slot_dmin(skey, t, D));  // node (d+1, t)
-                        else c = leaf_of(skey, E, t, nv, D) | kKidLeaf;
-                        if (nk < 4) kid[nk] = c;
+                    const uint32_t p4 = (ks >> shift) << 2;
+                    uint32_t lo[3] = {s, s, s}, hi[3] = {end, end, end};
+                    while (lo[0] < hi[0] || lo[1] < hi[1] || lo[2] < hi[2]) {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            if (lo[c] < hi[c]) {
+                                const uint32_t mid = lo[c] + ((hi[c] - lo[c]) >> 1);
+                                if ((skey[mid] >> cshift) <= p4 + (uint32_t)c) lo[c] = mid + 1;
+                                else hi[c] = mid;
+                            }
+                        }
+                    }
+                    const uint32_t cend[4] = {lo[0], lo[1], lo[2], end};
+                    uint32_t kid[4] = {kKidNone, kKidNone, kKidNone, kKidNone};
+                    uint32_t nk = 0, t = s;
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const uint32_t tend = cend[c];
+                        if (tend == t) continue;  // no particle in this child cell
+                        if (tend - t >= 2) kid[nk] = t + E[t] + (uint32_t)(d + 1 - slot_dmin(skey, t, D));  // node (d+1, t)
+                        else kid[nk] = leaf_of(skey, E, t, nv, D) | kKidLeaf;
                         ++nk;
                         t = tend;
-                    } while (t < nv && (skey[t] >> shift) == (ks >> shift));
-                    end = t;
-                    if (nk > 4) atomicOr(err, kErrTree);
+                    }
                     kids[at] = make_uint4(kid[0], kid[1], kid[2], kid[3]);
                 }
                 rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
