@@ -51,10 +51,9 @@ FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # 152 SMs x 128 FP32 lanes
 ACCURATE = 0x70  # GS_FLAGS_ACCURATE
 RELATIVE = 0x100  # GS_FLAG_RELATIVE_MAC
 # DRAM bytes per launch of the traversal kernel, from one ncu capture of that workload
+# (dram__bytes_read.sum + dram__bytes_write.sum), by workload name
 FORCE_TRAFFIC_BYTES = {
-    "Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, safe radius, 64-particle group "
-    "walk), relative opening criterion alpha=0.006 with theta=0.3 floor, softening 0.2, dt=1e-3":
-        55.336448e6 + 1.928448e6,
+    "bh500k": 55.017472e6 + 1.798656e6,
 }
 
 
@@ -522,7 +521,7 @@ def roofline_of(gsim, wl, m):
         n_al = (wl["n"] + 63) // 64 * 64
         achieved = 14.0 * n_al * n_al / t / 1e12
         extra = {"kernel": "k_direct_fast", "pairs_per_step": n_al * n_al, "flop_model": "14 FLOP per pair"}
-    traffic = FORCE_TRAFFIC_BYTES.get(wl["desc"])
+    traffic = FORCE_TRAFFIC_BYTES.get(wl.get("name"))
     r = {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
          "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": traffic,
          "traffic_source": ("dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this "
@@ -638,7 +637,7 @@ def main():
 
     import gsim
 
-    wl = workloads()[args.workload]
+    wl = dict(workloads()[args.workload], name=args.workload)
     if args.impl == "reference":
         return run_reference(args, wl)
 
@@ -685,7 +684,7 @@ def main():
     if rank == 0 and world == 1 and args.workload == "bh500k" and not args.no_secondary:
         lines = []
         for name in ("bh500k-theta", "bh500k-reference-rule"):
-            wl2 = workloads()[name]
+            wl2 = dict(workloads()[name], name=name)
             m2 = measure(gsim, torch, wl2, pos, vel, mass, args, local, None, sample_clocks=False)
             m2.pop("sim").close()
             lines.append({"workload": wl2["desc"], "value": wl2["n"] * args.steps / (m2["dev_ms"] / 1e3),
