@@ -442,7 +442,9 @@ __device__ __forceinline__ void sort_pass_body(const uint32_t* __restrict__ kin,
         s_whist[w][t] = tot;
         tot += c;
     }
-    // decoupled look-back over earlier tiles for digit t
+    // decoupled look-back over earlier tiles for digit t, kLookback tiles per round trip:
+    // the aggregates are added nearest first up to the first inclusive prefix; a tile not
+    // yet published ends the window, and the next window starts there
     uint32_t excl = 0;
     uint32_t* st = status + (size_t)tile * 256 + t;
     if (tile == 0) {
@@ -452,18 +454,30 @@ __device__ __forceinline__ void sort_pass_body(const uint32_t* __restrict__ kin,
         int64_t p = (int64_t)tile - 1;
         uint32_t spins = 0;
         while (p >= 0) {
-            uint32_t w = ld_volatile(status + (size_t)p * 256 + t);
-            uint32_t f = w >> 30;
-            if (f == 0u) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(err, kErrSortWait);
-                    break;
+            uint32_t w[kLookback];
+#pragma unroll
+            for (int k = 0; k < kLookback; ++k)
+                w[k] = p - k >= 0 ? ld_volatile(status + (size_t)(p - k) * 256 + t) : (2u << 30);
+            bool stop = false, done = false;
+            int used = 0;
+#pragma unroll
+            for (int k = 0; k < kLookback; ++k) {
+                if (stop) continue;
+                const uint32_t f = w[k] >> 30;
+                if (f == 0u) {
+                    stop = true;
+                } else {
+                    excl += w[k] & 0x3fffffffu;
+                    ++used;
+                    if (f == 2u) stop = done = true;
                 }
-                continue;
             }
-            excl += w & 0x3fffffffu;
-            if (f == 2u) break;
-            --p;
+            if (done) break;
+            if (used < kLookback && ++spins > kSpinLimit) {
+                atomicOr(err, kErrSortWait);
+                break;
+            }
+            p -= used;
         }
         atomicExch(st, (2u << 30) | (excl + tot));
     }
@@ -532,32 +546,39 @@ __device__ __forceinline__ void meta_scan_body(const uint32_t* __restrict__ skey
     }
     uint32_t total;
     uint32_t texcl = block_exclusive_scan_256(sum, s_warp, total);
-    if (t == 0) {
+    if (t < 32) {  // warp 0: publish, then look back over 32 earlier tiles per round trip
         uint32_t excl = 0;
         uint32_t* st = status + tile;
         if (tile == 0) {
-            atomicExch(st, (2u << 30) | total);
+            if (t == 0) atomicExch(st, (2u << 30) | total);
         } else {
-            atomicExch(st, (1u << 30) | total);
+            if (t == 0) atomicExch(st, (1u << 30) | total);
             int64_t p = (int64_t)tile - 1;
             uint32_t spins = 0;
-            while (p >= 0) {
-                uint32_t w = ld_volatile(status + p);
-                uint32_t f = w >> 30;
-                if (f == 0u) {
+            while (p >= 0) {  // every value below is uniform over the warp
+                const int64_t q = p - t;  // lane t reads the t-th tile back
+                const uint32_t w = q >= 0 ? ld_volatile(status + q) : (2u << 30);
+                const uint32_t f = w >> 30;
+                const uint32_t stopm = __ballot_sync(0xffffffffu, f != 1u);  // unpublished or inclusive
+                const int k = stopm ? __ffs(stopm) - 1 : 32;
+                const uint32_t kf = __shfl_sync(0xffffffffu, f, k & 31);
+                const bool inclusive = k < 32 && kf == 2u;
+                // the aggregates nearer than lane k, and lane k's value if it is inclusive
+                excl += __reduce_add_sync(0xffffffffu, (t < k || (t == k && inclusive)) ? (w & 0x3fffffffu) : 0u);
+                if (inclusive) break;
+                if (k < 32) {  // tile p - k has not published yet: wait for it
                     if (++spins > kSpinLimit) {
-                        atomicOr(err, kErrScanWait);
+                        if (t == 0) atomicOr(err, kErrScanWait);
                         break;
                     }
-                    continue;
+                    p -= k;
+                } else {
+                    p -= 32;
                 }
-                excl += w & 0x3fffffffu;
-                if (f == 2u) break;
-                --p;
             }
-            atomicExch(st, (2u << 30) | (excl + total));
+            if (t == 0) atomicExch(st, (2u << 30) | (excl + total));
         }
-        s_prefix = excl;
+        if (t == 0) s_prefix = excl;
     }
     __syncthreads();
     uint32_t run = s_prefix + texcl;

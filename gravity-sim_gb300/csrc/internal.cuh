@@ -49,6 +49,8 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kLevelTop = 4;
 // bounded spin for decoupled look-back: after this many polls the kernel flags an error
 constexpr uint32_t kSpinLimit = 1u << 24;
+// earlier tiles whose status a look-back reads per round trip
+constexpr int kLookback = 8;
 
 struct BHParams {
     float cx, cy, scale, radius0;  // bounding box (fixed box: 0, 0, 1.024, 500000)
