@@ -83,6 +83,75 @@ def workloads():
     }
 
 
+class NvmlClockSampler:
+    """SM clock and clock-event (throttle) reasons read through NVML every millisecond
+    during the timed region (read-only queries; the timed region of a default run lasts
+    about 10 ms, too short for nvidia-smi's 200 ms sampling)."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, device, period_s=0.001):
+        import ctypes as C
+        self.C = C
+        self.nvml = C.CDLL("libnvidia-ml.so.1")
+        if self.nvml.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit_v2 failed")
+        self.h = C.c_void_p()
+        if self.nvml.nvmlDeviceGetHandleByIndex_v2(C.c_uint(device), C.byref(self.h)) != 0:
+            raise OSError("nvmlDeviceGetHandleByIndex_v2 failed")
+        fn = getattr(self.nvml, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = fn or self.nvml.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.period = period_s
+        self.samples = []
+        self.stop_flag = threading.Event()
+
+    def _one(self):
+        C = self.C
+        clk, mx, rs = C.c_uint(0), C.c_uint(0), C.c_ulonglong(0)
+        if self.nvml.nvmlDeviceGetClockInfo(self.h, 1, C.byref(clk)) != 0:  # NVML_CLOCK_SM
+            return None
+        self.nvml.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(mx))
+        self.reasons_fn(self.h, C.byref(rs))
+        return clk.value, mx.value, rs.value
+
+    def _run(self):
+        while not self.stop_flag.is_set():
+            s = self._one()
+            if s:
+                self.samples.append(s)
+            time.sleep(self.period)
+
+    def start(self):
+        s = self._one()  # one sample at the start, then the polling thread
+        if s:
+            self.samples.append(s)
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+
+    def stop(self):
+        self.stop_flag.set()
+        self.t.join(timeout=2)
+        s = self._one()
+        if s:
+            self.samples.append(s)
+        self.nvml.nvmlShutdown()
+        if not self.samples:
+            return None
+        reasons = set()
+        for _, _, r in self.samples:
+            reasons.update(nm for bit, nm in self.REASONS.items() if r & bit)
+        return {"sm_mhz": float(np.median([c for c, _, _ in self.samples])),
+                "sm_max_mhz": float(max(m for _, m, _ in self.samples)), "samples": len(self.samples),
+                "reasons": sorted(reasons), "source": "NVML, every 1 ms"}
+
+
+def clock_sampler(device):
+    try:
+        return NvmlClockSampler(device)
+    except (OSError, AttributeError):
+        return ClockSampler(device)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
 
@@ -233,7 +302,7 @@ def measure(gsim, torch, wl, pos, vel, mass, args, local, dist, sample_clocks):
     launches0 = sim.stats().kernel_launches
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    clocks = ClockSampler(local) if sample_clocks else None
+    clocks = clock_sampler(local) if sample_clocks else None
     barrier(dist, local)
     torch.cuda.synchronize()
     if clocks:
