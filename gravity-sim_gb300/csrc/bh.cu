@@ -7,8 +7,9 @@
 // clears and fills a fixed 1024x1024 grid and walks 11 levels of it every step; here
 // every stage is sized by N:
 //
-//   k_bbox_keys   (bounding-box mode) min/max of positions, box parameters in FP64, then
-//                 the keys (one cooperative launch; a batch runs kb_bbox and kb_keygen)
+//   k_ext_keys    (bounding-box mode) box parameters in FP64 from the extent of the input
+//                 positions, which the traversal kernel that wrote them (or the upload)
+//                 gathered with atomics, then the keys (a batch runs kb_bbox and kb_keygen)
 //   k_keygen      cell key per particle (InitShader.comp:80-98 arithmetic), removal of
 //                 particles outside the fixed box (InitShader.comp:110-117), digit
 //                 histograms for every radix pass
@@ -147,8 +148,8 @@ __device__ __forceinline__ float4 bbox_block_minmax(Blk blk, const float2* __res
     return make_float4(mnx, mxx, mny, mxy);
 }
 
-// The box parameters from the extent: a square around it, 1/1024 margin, 2^15 cells per
-// axis, in FP64.
+// The box parameters from the extent: a square around it, 1/1024 margin, 2^kBBoxBits
+// cells per axis, in FP64.
 __device__ __forceinline__ BHParams bbox_params(float4 ext4) {
     const double a = ext4.x, b = ext4.y, c = ext4.z, d = ext4.w;
     double cx = 0.5 * (a + b), cy = 0.5 * (c + d);
@@ -353,31 +354,46 @@ __device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, int* e
     return s_ok != 0;
 }
 
-// Bounding box and keys in one cooperative launch (bounding-box mode): every block
-// writes the min/max of its particles, and after a grid barrier every block reduces all
-// partials and derives the box itself (the same arithmetic, so the same bits in every
-// block and as a batch's kb_bbox), block 0 stores it for the later stages, and every block goes on
-// to the keys of its particles, which it has just read (L2).
-__global__ void __launch_bounds__(kKeyThreads)
-k_bbox_keys(float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos_out, float* mass_out, uint32_t n,
-            uint32_t* __restrict__ keys, uint32_t* __restrict__ hist, int passes, uint32_t* __restrict__ valid_count,
-            float* __restrict__ part, BHParams* __restrict__ params, uint32_t* __restrict__ bar,
-            int* __restrict__ err) {
-    static_assert(kKeyThreads == kBBoxThreads, "one block shape for both halves");
-    pdl_enter();
-    const float4 m = bbox_block_minmax(grid_blk(), pos_in, n);
-    if (threadIdx.x == 0) {
-        part[4 * blockIdx.x + 0] = m.x;
-        part[4 * blockIdx.x + 1] = m.y;
-        part[4 * blockIdx.x + 2] = m.z;
-        part[4 * blockIdx.x + 3] = m.w;
+// The extent {min x, max x, min y, max y} of a state set from its ordered words.
+__device__ __forceinline__ float4 ext_decode(const uint32_t* __restrict__ ext) {
+    return make_float4(__uint_as_float(ord_bits(__ldcg(ext + 0))), __uint_as_float(ord_bits(~__ldcg(ext + 1))),
+                       __uint_as_float(ord_bits(__ldcg(ext + 2))), __uint_as_float(ord_bits(~__ldcg(ext + 3))));
+}
+
+// Adds min/max of positions to a state set's extent words: a warp reduction (fminf/fmaxf
+// skip NaN), then one atomic per word from lane 0.  Every lane of the warp must call it.
+__device__ __forceinline__ void ext_add(uint32_t* __restrict__ ext, float mnx, float mxx, float mny, float mxy) {
+    for (int o = 16; o; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
     }
-    if (!grid_sync(bar, gridDim.x, err)) return;
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(ext + 0, ord_word(__float_as_uint(mnx)));
+        atomicMin(ext + 1, ~ord_word(__float_as_uint(mxx)));
+        atomicMin(ext + 2, ord_word(__float_as_uint(mny)));
+        atomicMin(ext + 3, ~ord_word(__float_as_uint(mxy)));
+    }
+}
+
+// Keys in bounding-box mode.  The extent of the input positions was gathered while they
+// were written (by the previous step's traversal kernel, or by the upload), so every
+// block derives the box from those four words and goes on to the keys: no pass over
+// the positions and no grid barrier before them.  Block 0 stores the box for the later
+// stages and clears the output set's extent for this step's traversal kernel.
+__global__ void __launch_bounds__(kKeyThreads)
+k_ext_keys(float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos_out, float* mass_out, uint32_t n,
+           uint32_t* __restrict__ keys, uint32_t* __restrict__ hist, int passes, uint32_t* __restrict__ valid_count,
+           BHParams* __restrict__ params, const uint32_t* __restrict__ ext_in, uint32_t* __restrict__ ext_out) {
+    pdl_enter();
     __shared__ BHParams sp;
-    const float4 e = bbox_reduce_partials(part, gridDim.x);
     if (threadIdx.x == 0) {
-        sp = bbox_params(e);
-        if (blockIdx.x == 0) *params = sp;
+        sp = bbox_params(ext_decode(ext_in));
+        if (blockIdx.x == 0) {
+            *params = sp;
+            for (int j = 0; j < 4; ++j) ext_out[j] = 0xFFFFFFFFu;
+        }
     }
     __syncthreads();
     keygen_body(grid_blk(), 1, &sp, pos_in, mass_in, pos_out, mass_out, n, keys, hist, passes, valid_count);
@@ -999,7 +1015,7 @@ __device__ __forceinline__ void force_body(Blk blk, const uint32_t* __restrict__
                                            const float2* __restrict__ vel_in, float2* __restrict__ pos_out,
                                            float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
                                            float eps2, float theta2, float k, float hdt, uint32_t cap,
-                                           unsigned long long* __restrict__ stat) {
+                                           unsigned long long* __restrict__ stat, uint32_t* __restrict__ ext) {
     __shared__ float4 wrec[kForceWarps][32];
     __shared__ uint32_t wskip[kForceWarps][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1048,12 +1064,18 @@ __device__ __forceinline__ void force_body(Blk blk, const uint32_t* __restrict__
             atomicAdd(&stat[1], n_vis);
         }
     }
-    if (!valid) return;
-    if (acc_rec) acc_rec[i] = make_float2(ax, ay);
-    const float2 v = vel_in[i];
-    const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);  // ForceShader.comp:145-146
-    pos_out[i] = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
-    vel_out[i] = make_float2(nvx, nvy);
+    float2 np = make_float2(0.0f, 0.0f);
+    if (valid) {
+        if (acc_rec) acc_rec[i] = make_float2(ax, ay);
+        const float2 v = vel_in[i];
+        const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);  // ForceShader.comp:145-146
+        np = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
+        pos_out[i] = np;
+        vel_out[i] = make_float2(nvx, nvy);
+    }
+    if (ext)  // bounding-box mode: the next step's box
+        ext_add(ext, valid ? np.x : INFINITY, valid ? np.x : -INFINITY, valid ? np.y : INFINITY,
+                valid ? np.y : -INFINITY);
 }
 
 template <bool EXACT, bool COUNT>
@@ -1061,10 +1083,11 @@ __global__ void __launch_bounds__(kForceWarps * 32)
 k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, const float4* __restrict__ rec,
         const uint32_t* __restrict__ skip, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
         float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
-        float eps2, float theta2, float k, float hdt, uint32_t cap, unsigned long long* __restrict__ stat) {
+        float eps2, float theta2, float k, float hdt, uint32_t cap, unsigned long long* __restrict__ stat,
+        uint32_t* __restrict__ ext) {
     pdl_enter();
     force_body<EXACT, COUNT>(grid_blk(), sidx, counts, rec, skip, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al,
-                             eps2, theta2, k, hdt, cap, stat);
+                             eps2, theta2, k, hdt, cap, stat, ext);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1288,7 +1311,7 @@ __device__ __forceinline__ void force_group_body(
     const float2* __restrict__ vel_in, float2* __restrict__ pos_out, float2* __restrict__ vel_out,
     float2* __restrict__ acc_rec, uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
     unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha,
-    float floor2) {
+    float floor2, uint32_t* __restrict__ ext) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t group = blk.id * kGroupWarps + warp;
     const uint32_t nv = counts[0];
@@ -1483,20 +1506,32 @@ __device__ __forceinline__ void force_group_body(
         if (v0) amag[i0] = __fsqrt_rn(fmaf(ax.x, ax.x, ay.x * ay.x));
         if (v1) amag[i1] = __fsqrt_rn(fmaf(ax.y, ax.y, ay.y * ay.y));
     }
+    float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;  // of the new positions
     if (v0) {
         if (acc_rec) acc_rec[i0] = make_float2(ax.x, ay.x);
         const float2 v = vel_in[i0];
         const float nvx = fmaf(ax.x, k, v.x), nvy = fmaf(ay.x, k, v.y);
-        pos_out[i0] = make_float2(fmaf(v.x + nvx, hdt, p0.x), fmaf(v.y + nvy, hdt, p0.y));
+        const float2 np = make_float2(fmaf(v.x + nvx, hdt, p0.x), fmaf(v.y + nvy, hdt, p0.y));
+        pos_out[i0] = np;
         vel_out[i0] = make_float2(nvx, nvy);
+        mnx = fminf(mnx, np.x);
+        mxx = fmaxf(mxx, np.x);
+        mny = fminf(mny, np.y);
+        mxy = fmaxf(mxy, np.y);
     }
     if (v1) {
         if (acc_rec) acc_rec[i1] = make_float2(ax.y, ay.y);
         const float2 v = vel_in[i1];
         const float nvx = fmaf(ax.y, k, v.x), nvy = fmaf(ay.y, k, v.y);
-        pos_out[i1] = make_float2(fmaf(v.x + nvx, hdt, p1.x), fmaf(v.y + nvy, hdt, p1.y));
+        const float2 np = make_float2(fmaf(v.x + nvx, hdt, p1.x), fmaf(v.y + nvy, hdt, p1.y));
+        pos_out[i1] = np;
         vel_out[i1] = make_float2(nvx, nvy);
+        mnx = fminf(mnx, np.x);
+        mxx = fmaxf(mxx, np.x);
+        mny = fminf(mny, np.y);
+        mxy = fmaxf(mxy, np.y);
     }
+    if (ext) ext_add(ext, mnx, mxx, mny, mxy);  // bounding-box mode: the next step's box
 }
 
 template <bool EXACT, bool QUAD, bool COUNT>
@@ -1507,12 +1542,12 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
               float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
               uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
               unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha,
-              float floor2) {
+              float floor2, uint32_t* __restrict__ ext) {
     pdl_enter();
     __shared__ GroupSmem smem[kGroupWarps];
     force_group_body<EXACT, QUAD, COUNT>(grid_blk(), smem[threadIdx.x >> 5], sidx, skey, counts, rec, skip, quad,
                                          kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2, theta2, k, hdt,
-                                         cap, stat, err, amag, alpha, floor2);
+                                         cap, stat, err, amag, alpha, floor2, ext);
 }
 
 int grid_for(uint64_t n, int threads) {
@@ -1568,6 +1603,8 @@ void bh_carve(gs_sim* s) {
     if (s->p.flags & GS_FLAG_QUADRUPOLE) sim_carve(s, (void**)&w.quad, w.cap * sizeof(float4));
     w.amag = nullptr;
     if (s->p.flags & GS_FLAG_RELATIVE_MAC) sim_carve(s, (void**)&w.amag, n * sizeof(float));
+    w.ext = nullptr;
+    if (bbox) sim_carve(s, (void**)&w.ext, 8 * sizeof(uint32_t));
     sim_carve(s, (void**)&w.bbox_part, kBBoxBlocks * 4 * sizeof(float));
     sim_carve(s, (void**)&w.params, sizeof(BHParams));
     // one block cleared per step: hist | counters | sort status | scan status
@@ -1605,10 +1642,6 @@ cudaError_t bh_init(gs_sim* s) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     if (e == cudaSuccess && per_sm < 1) e = cudaErrorCooperativeLaunchTooLarge;
     w.sums_grid = per_sm * sms;
-    // the cooperative box-and-keys launch: the keygen grid, if it fits on the device at once
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bbox_keys, kKeyThreads, 0);
-    if (e == cudaSuccess && per_sm < 1) e = cudaErrorCooperativeLaunchTooLarge;
-    w.keys_grid = std::min(keygen_blocks(s->n_al), per_sm * sms);
     return e;
 }
 
@@ -1673,10 +1706,10 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
         return r;
     };
     stage_begin(s, kStageKeys, profile);
-    if (bbox) {  // box and keys in one cooperative launch
-        GS_TRY_LAUNCH(launch_coop(next_pdl(), k_bbox_keys, w.keys_grid, kKeyThreads, st, s->pos[in], s->mass[in],
-                                  s->pos[out], s->mass[out], n, w.keys[0], w.hist, w.passes, ctr + kCtrValid,
-                                  w.bbox_part, w.params, ctr + kCtrBarrier + 1, s->d_err));
+    if (bbox) {  // the box from the extent carried with the input set
+        GS_TRY_LAUNCH(launch(next_pdl(), k_ext_keys, keygen_blocks(n), kKeyThreads, st, s->pos[in], s->mass[in],
+                             s->pos[out], s->mass[out], n, w.keys[0], w.hist, w.passes, ctr + kCtrValid, w.params,
+                             (const uint32_t*)(w.ext + 4 * in), w.ext + 4 * out));
     } else {
         GS_TRY_LAUNCH(launch(next_pdl(), k_keygen, keygen_blocks(n), kKeyThreads, st, 0,
                              (const BHParams*)w.params, s->pos[in], s->mass[in], s->pos[out], s->mass[out], n,
@@ -1744,7 +1777,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
                              (const float4*)w.rec, (const uint32_t*)w.skip, (const float4*)w.quad,
                              (const uint4*)w.kids, (const float2*)s->pos[in], (const float2*)s->vel[in], s->pos[out],
                              s->vel[out], s->acc, n, s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err,
-                             w.amag, s->p.relative_accuracy, s->floor2));
+                             w.amag, s->p.relative_accuracy, s->floor2, w.ext ? w.ext + 4 * out : nullptr));
     } else {
         auto fn = exact ? (count ? k_force<true, true> : k_force<true, false>)
                         : (count ? k_force<false, true> : k_force<false, false>);
@@ -1752,7 +1785,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
         GS_TRY_LAUNCH(launch(fpdl, fn, blocks, kForceWarps * 32, st, sidx, (const uint32_t*)(ctr + kCtrValid),
                              (const float4*)w.rec, (const uint32_t*)w.skip, (const float2*)s->pos[in],
                              (const float2*)s->vel[in], s->pos[out], s->vel[out], s->acc, n, s->eps2, s->theta2, k,
-                             hdt, (uint32_t)w.cap, stat));
+                             hdt, (uint32_t)w.cap, stat, w.ext ? w.ext + 4 * out : nullptr));
     }
     count_launch(s);
     stage_end(s, kStageForce, profile);
@@ -1906,6 +1939,9 @@ __global__ void __launch_bounds__(kKeyThreads) kb_keygen(BatchArgs a) {
     pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
+    // the output set's extent, gathered by this step's traversal kernel (kb_bbox derived the
+    // box from the positions themselves)
+    if (d.ext && bb.blk.id == 0 && threadIdx.x < 4) d.ext[4 * bb.out + threadIdx.x] = 0xFFFFFFFFu;
     keygen_body(bb.blk, d.bbox, d.params, d.pos[bb.in], d.mass[bb.in], d.pos[bb.out], d.mass[bb.out], d.n_al,
                 d.keys[0], d.hist, d.passes, d.counters + kCtrValid);
 }
@@ -1986,7 +2022,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kb_force_group(BatchArgs a, 
                                              d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2,
                                              d.theta2, d.k, d.hdt, d.cap,
                                              (unsigned long long*)(d.counters + kCtrStat), d.err, d.amag, d.alpha,
-                                             d.floor2);
+                                             d.floor2, d.ext ? d.ext + 4 * bb.out : nullptr);
     }
 }
 
@@ -2006,7 +2042,8 @@ __global__ void __launch_bounds__(kForceWarps * 32) kb_force(BatchArgs a, uint32
         const int f = d.passes & 1;
         force_body<EXACT, COUNT>(bb.blk, d.idx[f], d.counters + kCtrValid, d.rec, d.skip, d.pos[bb.in],
                                  d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2, d.theta2, d.k,
-                                 d.hdt, d.cap, (unsigned long long*)(d.counters + kCtrStat));
+                                 d.hdt, d.cap, (unsigned long long*)(d.counters + kCtrStat),
+                                 d.ext ? d.ext + 4 * bb.out : nullptr);
     }
 }
 
@@ -2031,6 +2068,7 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
     d.msum = w.msum;
     d.quad = w.quad;
     d.amag = w.amag;
+    d.ext = w.ext;
     d.alpha = s->p.relative_accuracy;
     d.floor2 = s->floor2;
     d.kids = w.kids;

@@ -52,6 +52,17 @@ constexpr uint32_t kSpinLimit = 1u << 24;
 // earlier tiles whose status a look-back reads per round trip
 constexpr int kLookback = 8;
 
+// Order-preserving code of a float: unsigned comparison of the words orders the values
+// (-inf < ... < -0 < +0 < ... < +inf), so atomicMin on words takes a minimum and atomicMin
+// on complemented words a maximum.  All-ones words (the cleared state) decode to NaN and
+// lose to every value.  NaN inputs are left out by the callers, as fminf/fmaxf do.
+__host__ __device__ __forceinline__ uint32_t ord_word(uint32_t bits) {
+    return (bits & 0x80000000u) ? ~bits : (bits | 0x80000000u);
+}
+__host__ __device__ __forceinline__ uint32_t ord_bits(uint32_t w) {
+    return (w & 0x80000000u) ? (w & 0x7FFFFFFFu) : ~w;
+}
+
 struct BHParams {
     float cx, cy, scale, radius0;  // bounding box (fixed box: 0, 0, 1.024, 500000)
     float inv_scale;               // float(1 / scale), taken once in FP64
@@ -75,8 +86,9 @@ struct BHWork {
     float2* msum = nullptr;            // [cap]
     float4* quad = nullptr;            // [cap] {sxx, sxy, syy, -} (GS_FLAG_QUADRUPOLE)
     float* amag = nullptr;             // [n_al] |a| of the last step, NaN: unknown (GS_FLAG_RELATIVE_MAC)
+    uint32_t* ext = nullptr;           // [2][4] extent of each state set's positions (bounding-box mode):
+                                       // {min x, ~max x, min y, ~max y} as ordered words (ord_word)
     int sums_grid = 0;                 // blocks of the cooperative moments launch (all co-resident)
-    int keys_grid = 0;                 // blocks of the cooperative box-and-keys launch
     uint4* kids = nullptr;             // [cap] child descriptors of internal records
     uint32_t* levels = nullptr;        // internal records by level (level_off / level_cap in bh.cu)
     uint2* nodeinfo = nullptr;         // [cap] {a key of the cell, level} of an internal record
@@ -121,6 +133,7 @@ struct SysDesc {
     float2* msum;
     float4* quad;
     float* amag;      // relative criterion: |a| per particle, or null for the theta test
+    uint32_t* ext;    // extents of the two state sets (bounding-box mode), or null
     float alpha, floor2;
     uint4* kids;
     uint32_t* levels;

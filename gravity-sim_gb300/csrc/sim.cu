@@ -185,10 +185,13 @@ const void* host_mapped(const gs_sim* s, const void* p, uintptr_t align) {
 // Fills both sets from the N source particles (mapped host arrays read in place, or set a
 // after the copy engine filled it), zeroes the padding slots (and every velocity when none
 // was given) and marks every |a| unknown (all-ones words are NaN, so the next step opens
-// nodes by theta).  The sources may alias set a, so no pointer is restrict-qualified.
+// nodes by theta).  With `ext` (bounding-box mode, words cleared before the launch) it
+// gathers the extent of set a's positions, padding included, for the next step's box.
+// The sources may alias set a, so no pointer is restrict-qualified.
 __global__ void k_upload(const float2* src_pos, const float2* src_vel, const float* src_mass, float2* pos_a,
                          float2* vel_a, float* mass, float2* pos_b, float2* vel_b, float* amag, uint32_t n,
-                         uint32_t n_al) {
+                         uint32_t n_al, uint32_t* ext) {
+    float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_al; i += gridDim.x * blockDim.x) {
         float2 p = make_float2(0.0f, 0.0f), v = p;
         float m = 0.0f;
@@ -203,6 +206,23 @@ __global__ void k_upload(const float2* src_pos, const float2* src_vel, const flo
         vel_b[i] = v;
         mass[i] = m;
         if (amag) amag[i] = __uint_as_float(0xFFFFFFFFu);
+        mnx = fminf(mnx, p.x);
+        mxx = fmaxf(mxx, p.x);
+        mny = fminf(mny, p.y);
+        mxy = fmaxf(mxy, p.y);
+    }
+    if (!ext) return;  // uniform over the grid
+    for (int o = 16; o; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(ext + 0, gsim::ord_word(__float_as_uint(mnx)));
+        atomicMin(ext + 1, ~gsim::ord_word(__float_as_uint(mxx)));
+        atomicMin(ext + 2, gsim::ord_word(__float_as_uint(mny)));
+        atomicMin(ext + 3, ~gsim::ord_word(__float_as_uint(mxy)));
     }
 }
 
@@ -242,8 +262,10 @@ gs_status upload(gs_sim* s, const float* pos, const float* vel, const float* mas
         GS_CUDA(cudaMemcpyAsync(s->mass[0], mass, n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
         sm = s->mass[0];
     }
+    uint32_t* ext = s->bh.ext ? s->bh.ext + 4 * a : nullptr;
+    if (ext) GS_CUDA(cudaMemsetAsync(ext, 0xFF, 4 * sizeof(uint32_t), s->stream));
     k_upload<<<copy_blocks(s->n_al), 256, 0, s->stream>>>(sp, sv, sm, s->pos[a], s->vel[a], s->mass[0], s->pos[b],
-                                                          s->vel[b], s->bh.amag, (uint32_t)n, (uint32_t)s->n_al);
+                                                          s->vel[b], s->bh.amag, (uint32_t)n, (uint32_t)s->n_al, ext);
     GS_CUDA(cudaGetLastError());
     ++s->kernel_launches;
     GS_CUDA(cudaStreamSynchronize(s->stream));
