@@ -17,7 +17,8 @@
 // bit-identical to the CPU restatement.
 //
 // Roofline: 14 algorithmic FLOP per pair (2 sub, 2 FMA for r^2, rsqrt, 3 mul, 2 FMA),
-// 9 FP32-pipe instructions + 1 MUFU per pair; FP32-bound.
+// 9 FP32 operations + 1 MUFU per pair, issued as packed f32x2 instructions for a thread's
+// two targets (4.5 issues + 1 MUFU per pair); FP32-bound.
 #include <mutex>
 
 #include "internal.cuh"
@@ -46,6 +47,7 @@ __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const
     const uint32_t j0 = by * jchunk;
     const uint32_t j1 = min(j0 + jchunk, n_al);
 
+    static_assert(IPT == 2, "two targets per thread: one packed f32x2 pair");
     float px[IPT], py[IPT], sx[IPT], sy[IPT], cx[IPT], cy[IPT];
 #pragma unroll
     for (int r = 0; r < IPT; ++r) {
@@ -55,6 +57,7 @@ __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const
         py[r] = p.y;
         sx[r] = sy[r] = cx[r] = cy[r] = 0.f;
     }
+    const float2 P2 = make_float2(px[0], px[1]), Q2 = make_float2(py[0], py[1]), E2 = make_float2(eps2, eps2);
 
     for (uint32_t jt = j0; jt < j1; jt += kDirectTileJ) {
         __syncthreads();
@@ -63,23 +66,21 @@ __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const
             sj[t] = make_float4(q.x, q.y, mass[jt + t], 0.f);
         }
         __syncthreads();
-        float tx[IPT], ty[IPT];
-#pragma unroll
-        for (int r = 0; r < IPT; ++r) tx[r] = ty[r] = 0.f;
+        // The thread's two targets share packed f32x2 instructions (each lane rounds like
+        // the scalar one, in the same order: dx, dy, d2 = fma(dx, dx, fma(dy, dy, eps2)),
+        // s = ((m r) r) r, t += d s), so the bits are those of two scalar evaluations.
+        float2 tx2 = make_float2(0.f, 0.f), ty2 = tx2;
 #pragma unroll 16
         for (int jj = 0; jj < kDirectTileJ; ++jj) {
             const float4 q = sj[jj];
-#pragma unroll
-            for (int r = 0; r < IPT; ++r) {
-                float dx = q.x - px[r];
-                float dy = q.y - py[r];
-                float d2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
-                float rr = rsqrtf(d2);
-                float s = ((q.z * rr) * rr) * rr;
-                tx[r] = fmaf(dx, s, tx[r]);
-                ty[r] = fmaf(dy, s, ty[r]);
-            }
+            const float2 dx = sub2(make_float2(q.x, q.x), P2), dy = sub2(make_float2(q.y, q.y), Q2);
+            const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
+            const float2 rr = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
+            const float2 s = mul2(mul2(mul2(make_float2(q.z, q.z), rr), rr), rr);
+            tx2 = fma2(dx, s, tx2);
+            ty2 = fma2(dy, s, ty2);
         }
+        const float tx[IPT] = {tx2.x, tx2.y}, ty[IPT] = {ty2.x, ty2.y};
 #pragma unroll
         for (int r = 0; r < IPT; ++r) {  // Kahan-compensated add of the tile partial
             if (!KAHAN) {
