@@ -28,6 +28,7 @@ namespace {
 
 constexpr int kDirectBlock = 128;
 constexpr int kDirectTileJ = 64;
+constexpr int kDirectIpt = 2;  // targets per thread, kDirectIpt / 2 packed f32x2 pairs
 
 // Block (bx, by) of a system: i-tile bx, j-chunk by.  A plain launch passes blockIdx.x /
 // blockIdx.y, a batched launch the block's position inside its system's grid.  KAHAN
@@ -47,7 +48,7 @@ __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const
     const uint32_t j0 = by * jchunk;
     const uint32_t j1 = min(j0 + jchunk, n_al);
 
-    static_assert(IPT == 2, "two targets per thread: one packed f32x2 pair");
+    static_assert(IPT % 2 == 0, "targets per thread come in packed f32x2 pairs");
     float px[IPT], py[IPT], sx[IPT], sy[IPT], cx[IPT], cy[IPT];
 #pragma unroll
     for (int r = 0; r < IPT; ++r) {
@@ -57,7 +58,14 @@ __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const
         py[r] = p.y;
         sx[r] = sy[r] = cx[r] = cy[r] = 0.f;
     }
-    const float2 P2 = make_float2(px[0], px[1]), Q2 = make_float2(py[0], py[1]), E2 = make_float2(eps2, eps2);
+    constexpr int NP = IPT / 2;
+    float2 P2[NP], Q2[NP];
+#pragma unroll
+    for (int h = 0; h < NP; ++h) {
+        P2[h] = make_float2(px[2 * h], px[2 * h + 1]);
+        Q2[h] = make_float2(py[2 * h], py[2 * h + 1]);
+    }
+    const float2 E2 = make_float2(eps2, eps2);
 
     for (uint32_t jt = j0; jt < j1; jt += kDirectTileJ) {
         __syncthreads();
@@ -66,21 +74,33 @@ __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const
             sj[t] = make_float4(q.x, q.y, mass[jt + t], 0.f);
         }
         __syncthreads();
-        // The thread's two targets share packed f32x2 instructions (each lane rounds like
-        // the scalar one, in the same order: dx, dy, d2 = fma(dx, dx, fma(dy, dy, eps2)),
-        // s = ((m r) r) r, t += d s), so the bits are those of two scalar evaluations.
-        float2 tx2 = make_float2(0.f, 0.f), ty2 = tx2;
+        // Pairs of the thread's targets share packed f32x2 instructions (each lane rounds
+        // like the scalar one, in the same order: dx, dy, d2 = fma(dx, dx, fma(dy, dy,
+        // eps2)), s = ((m r) r) r, t += d s), so the bits are those of scalar evaluations.
+        float2 tx2[NP], ty2[NP];
+#pragma unroll
+        for (int h = 0; h < NP; ++h) tx2[h] = ty2[h] = make_float2(0.f, 0.f);
 #pragma unroll 16
         for (int jj = 0; jj < kDirectTileJ; ++jj) {
             const float4 q = sj[jj];
-            const float2 dx = sub2(make_float2(q.x, q.x), P2), dy = sub2(make_float2(q.y, q.y), Q2);
-            const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
-            const float2 rr = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
-            const float2 s = mul2(mul2(mul2(make_float2(q.z, q.z), rr), rr), rr);
-            tx2 = fma2(dx, s, tx2);
-            ty2 = fma2(dy, s, ty2);
+#pragma unroll
+            for (int h = 0; h < NP; ++h) {
+                const float2 dx = sub2(make_float2(q.x, q.x), P2[h]), dy = sub2(make_float2(q.y, q.y), Q2[h]);
+                const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
+                const float2 rr = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
+                const float2 s = mul2(mul2(mul2(make_float2(q.z, q.z), rr), rr), rr);
+                tx2[h] = fma2(dx, s, tx2[h]);
+                ty2[h] = fma2(dy, s, ty2[h]);
+            }
         }
-        const float tx[IPT] = {tx2.x, tx2.y}, ty[IPT] = {ty2.x, ty2.y};
+        float tx[IPT], ty[IPT];
+#pragma unroll
+        for (int h = 0; h < NP; ++h) {
+            tx[2 * h] = tx2[h].x;
+            tx[2 * h + 1] = tx2[h].y;
+            ty[2 * h] = ty2[h].x;
+            ty[2 * h + 1] = ty2[h].y;
+        }
 #pragma unroll
         for (int r = 0; r < IPT; ++r) {  // Kahan-compensated add of the tile partial
             if (!KAHAN) {
@@ -228,7 +248,7 @@ kb_direct(const SysDesc* __restrict__ descs, const uint32_t* __restrict__ first,
         direct_ref_body(b, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out], d.acc, d.n_al, d.eps2, d.k,
                         d.hdt);
     else
-        direct_fast_body<2, KAHAN>(b % d.itiles, b / d.itiles, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out],
+        direct_fast_body<kDirectIpt, KAHAN>(b % d.itiles, b / d.itiles, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out],
                             d.acc, d.n_al, (int)d.chunks, d.jchunk, d.eps2, d.k, d.hdt, d.partials, d.tickets);
 }
 
@@ -338,7 +358,7 @@ static int pick_chunks(uint64_t n_al, int ipt) {
 // Lays the j-chunk partials and tickets out in the system's slab (sizing pass: counts).
 void direct_carve(gs_sim* s) {
     DirectWork& w = s->dw;
-    w.ipt = 2;
+    w.ipt = kDirectIpt;
     w.block = kDirectBlock;
     w.chunks = pick_chunks(s->n_al, w.ipt);
     w.partials = nullptr;
@@ -380,7 +400,7 @@ cudaError_t direct_step(gs_sim* s, int in, int out, bool profile) {
         uint32_t itiles, jchunk, chunks;
         direct_shape(s, itiles, jchunk, chunks);
         dim3 grid(itiles, chunks);
-        auto fn = (s->p.flags & GS_FLAG_PLAIN_SUM) ? k_direct_fast<2, false> : k_direct_fast<2, true>;
+        auto fn = (s->p.flags & GS_FLAG_PLAIN_SUM) ? k_direct_fast<kDirectIpt, false> : k_direct_fast<kDirectIpt, true>;
         fn<<<grid, kDirectBlock, 0, s->stream>>>(s->pos[in], s->vel[in], s->mass[in], s->pos[out], s->vel[out],
                                                   s->acc, n_al, (int)chunks, jchunk, s->eps2, k, hdt, w.partials,
                                                   w.tickets);
@@ -502,8 +522,8 @@ extern "C" gs_status gs_direct_step_noalloc(const float* d_pos_in, const float* 
     if (st != GS_OK) return st;
 
     const uint32_t n_al = (uint32_t)n;
-    const uint32_t itiles = (n_al + kDirectBlock * 2 - 1) / (kDirectBlock * 2);
-    int chunks = pick_chunks(n_al, 2);
+    const uint32_t itiles = (n_al + kDirectBlock * kDirectIpt - 1) / (kDirectBlock * kDirectIpt);
+    int chunks = pick_chunks(n_al, kDirectIpt);
     const int fit = (int)(kNoAllocPartialBytes / (sizeof(float4) * n_al));  // >= 4 for n <= 65536
     if (chunks > fit) chunks = fit;
     uint32_t jchunk = (n_al + chunks - 1) / chunks;
@@ -515,7 +535,7 @@ extern "C" gs_status gs_direct_step_noalloc(const float* d_pos_in, const float* 
     const float eps2 = softening_len * softening_len;
     const float k = simulation_time * gravitational_const;
     const float hdt = 0.5f * simulation_time;
-    k_direct_fast<2, true><<<dim3(itiles, chunks), kDirectBlock, 0, s>>>(
+    k_direct_fast<kDirectIpt, true><<<dim3(itiles, chunks), kDirectBlock, 0, s>>>(
         (const float2*)d_pos_in, (const float2*)d_vel_in, d_mass, (float2*)d_pos_out, (float2*)d_vel_out, nullptr,
         n_al, chunks, jchunk, eps2, k, hdt, partials, tickets);
     GS_CUDA(cudaGetLastError());
