@@ -76,6 +76,42 @@ def test_mixed_batch_bit_identical(gs, flags):
         _assert_same(alone, batched, MIXED)
 
 
+# bounding-box systems whose next box comes from the extent their last step gathered
+# (accurate walk with and without the relative criterion; the reference's walk in the
+# bounding box), each batch with a direct-sum member
+AFTER_BATCH = {
+    "accurate": [
+        (17, 9000, 100.0, ACCURATE_BH),
+        (16, 3000, 100.0, dict(ACCURATE_BH, flags=0x70 | 0x8 | 0x100, accuracy_parameter=0.35)),
+        (16, 2000, 100.0, DIRECT),
+    ],
+    "reference-walk": [
+        (17, 5000, 100.0, dict(algorithm=1, box_mode=1, flags=0x8, accuracy_parameter=0.7)),
+        (16, 1500, 100.0, dict(algorithm=1, box_mode=1, flags=0x8, accuracy_parameter=0.7)),
+        (16, 2000, 100.0, DIRECT),
+    ],
+}
+
+
+@pytest.mark.parametrize("kind", sorted(AFTER_BATCH))
+def test_plain_steps_after_batch_bit_identical(gs, kind):
+    """Steps alone, then in a batch, then alone again end bit-identical to the same steps
+    alone throughout: a batched step leaves each system's parity and the extent of its new
+    positions (the next plain step's box) as a plain step would."""
+    specs = AFTER_BATCH[kind]
+    alone = _make(gs, specs, 700)
+    mixed = _make(gs, specs, 700)
+    for s in alone + mixed:
+        s.reset_stats()
+    _run_alone(alone, 7)
+    _run_alone(mixed, 2)
+    with gs.Batch(mixed) as b:
+        b.run(3)
+        b.sync()
+    _run_alone(mixed, 2)
+    _assert_same(alone, mixed, specs)
+
+
 def test_reference_rule_batch_bit_identical(gs):
     """The reference's algorithm (fixed box with removal, theta 1, REFERENCE math) in a
     batch: removal touches both particle sets, so a member must match alone exactly."""
