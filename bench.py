@@ -207,7 +207,10 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def dist_setup():
+def dist_setup(backend="nccl"):
+    """Ranks from torchrun's environment: one replica per GPU (every rank steps its own
+    system; no data-path collective), NCCL for the timing barrier and reductions.  The
+    gloo backend serves the CPU tests of this logic."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -215,25 +218,36 @@ def dist_setup():
         import torch
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
         return world, rank, local, dist
     return 1, 0, 0, None
 
 
 def barrier(dist, local):
-    if dist is not None:
+    if dist is None:
+        return
+    if dist.get_backend() == "nccl":
         dist.barrier(device_ids=[local])
+    else:
+        dist.barrier()
 
 
 def reduce_op(dist, x, op):
+    """max or sum of x over the ranks (x itself on one rank)."""
     if dist is None:
         return x
     import torch
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def job_value(dist, particles, steps, dev_ms):
+    """Whole-job particle-steps/s: the particles of every rank over the slowest rank's time."""
+    return reduce_op(dist, float(particles), "sum") * steps / (reduce_op(dist, dev_ms, "max") / 1e3)
 
 
 def make_params(gsim, wl, local, flags):
@@ -722,7 +736,7 @@ def main():
     sim = m.pop("sim")
     max_ms = reduce_op(dist, m["dev_ms"], "max")
     total_particles = reduce_op(dist, float(wl["n"]), "sum")
-    value = total_particles * args.steps / (max_ms / 1e3)
+    value = job_value(dist, wl["n"], args.steps, m["dev_ms"])
 
     # end to end through the C ABI with pinned host buffers
     import ctypes as C
