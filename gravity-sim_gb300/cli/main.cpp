@@ -8,7 +8,7 @@
 //   - the windowed mode does not exist: every run is headless (--no-graphics is accepted);
 //   - --benchmark reports wall-clock time around the synchronised run, not clock() CPU time;
 //   - generators take --seed (the reference seeds from time(nullptr));
-//   - extra switches select this build's modes: --box=fixed|bbox, --accurate, --relative-accuracy,
+//   - extra switches select the library's modes: --box=fixed|bbox, --accurate, --relative-accuracy,
 //     --math=fast|reference;
 //   - the window's picture can be saved instead: --image-out=file.ppm writes the final state as
 //     the reference would draw it (one white pixel per particle, the start camera of the initial

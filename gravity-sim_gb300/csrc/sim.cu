@@ -376,7 +376,7 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
         params->algorithm != GS_BARNES_HUT)
         return invalid("gs_create: the accurate-mode flags apply to Barnes-Hut only");
     if (n > kMaxParticles || (params->algorithm == GS_BARNES_HUT && n > kMaxBarnesHutParticles)) {
-        set_error("gs_create: particle count above the limit of this build (2^28 direct sum, 2^26 Barnes-Hut)");
+        set_error("gs_create: particle count above the library's limit (2^28 direct sum, 2^26 Barnes-Hut)");
         return GS_ERR_CAPACITY;
     }
     int ndev = 0;

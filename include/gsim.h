@@ -46,7 +46,7 @@ typedef enum gs_status {
     GS_ERR_TIMEOUT = 4,
     GS_ERR_DEVICE = 5,   /* a kernel reported an error (e.g. a bounded wait ran out) */
     GS_ERR_IO = 6,
-    GS_ERR_CAPACITY = 7, /* a size limit of this build was exceeded */
+    GS_ERR_CAPACITY = 7, /* a size limit of the library was exceeded */
     GS_ERR_NO_DEVICE = 8
 } gs_status;
 

@@ -1,7 +1,7 @@
 /*
  * gsim_oracle.c -- CPU restatement of Gravity-Sim's per-step force-and-integrate path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker, never the product).  Compile with
+ * TEST INFRASTRUCTURE ONLY (the tests' reference, never the product).  Compile with
  * -ffp-contract=off: every fused multiply-add below is written out with fmaf().
  *
  * What each function restates (paths relative to the reference project):

@@ -14,7 +14,7 @@
  * shaders (orc_bh_grid_step) and the sorted-key construction (orc_bh_sorted_step).
  *
  * Canonical arithmetic.  GLSL leaves FMA contraction and the precision of division
- * to the driver; this build fixes one sequence and uses it on both sides:
+ * to the driver; the library and this restatement fix one sequence and use it alike:
  *   d2  = fma(dx, dx, fma(dy, dy, eps2))
  *   r   = 1 / sqrt(d2)           (correctly rounded sqrt, then correctly rounded divide)
  *   s   = ((m * r) * r) * r
