@@ -514,6 +514,28 @@ gs_status gs_get_particles(gs_sim* s, float* pos, float* vel, float* mass) {
     if (!s) return invalid("gs_get_particles: sim is NULL");
     GS_CUDA(cudaSetDevice(s->device));
     follow_batch(s);
+    const int in = s->in;  // ParticleSystem::GetParticles reads buffers[computeInputIndex]
+    float2* hp = (float2*)host_mapped(s, pos, 8);
+    float2* hv = (float2*)host_mapped(s, vel, 8);
+    float* hm = (float*)host_mapped(s, mass, 4);
+    if ((!pos || hp) && (!vel || hv) && (!mass || hm)) {
+        // pinned arrays: one kernel writes them and the error word, enqueued right behind
+        // the submitted steps (stream order), then one bounded wait for all of it
+        k_download<<<copy_blocks(s->n), 256, 0, s->stream>>>(s->pos[in], s->vel[in], s->mass[in], hp, hv, hm,
+                                                             (uint32_t)s->n, s->d_err, s->h_err);
+        GS_CUDA(cudaGetLastError());
+        ++s->kernel_launches;
+        GS_CUDA(cudaEventRecord(s->batch_done, s->stream));
+        s->batch_pending = true;
+        gs_status w = wait_event(s->batch_done, 0);
+        if (w != GS_OK) return w;
+        s->batch_pending = false;
+        if (s->profile_pending) {
+            gs_status a = account_profile(s);
+            if (a != GS_OK) return a;
+        }
+        return device_error(*s->h_err);
+    }
     if (s->batch_pending) {
         gs_status w = wait_event(s->batch_done, 0);
         if (w != GS_OK) return w;
@@ -522,19 +544,6 @@ gs_status gs_get_particles(gs_sim* s, float* pos, float* vel, float* mass) {
     if (s->profile_pending) {
         gs_status a = account_profile(s);
         if (a != GS_OK) return a;
-    }
-    const int in = s->in;  // ParticleSystem::GetParticles reads buffers[computeInputIndex]
-    float2* hp = (float2*)host_mapped(s, pos, 8);
-    float2* hv = (float2*)host_mapped(s, vel, 8);
-    float* hm = (float*)host_mapped(s, mass, 4);
-    if ((!pos || hp) && (!vel || hv) && (!mass || hm)) {
-        // pinned arrays: one kernel writes them and the error word, one synchronisation
-        k_download<<<copy_blocks(s->n), 256, 0, s->stream>>>(s->pos[in], s->vel[in], s->mass[in], hp, hv, hm,
-                                                             (uint32_t)s->n, s->d_err, s->h_err);
-        GS_CUDA(cudaGetLastError());
-        ++s->kernel_launches;
-        GS_CUDA(cudaStreamSynchronize(s->stream));
-        return device_error(*s->h_err);
     }
     gs_status st = check_device_error(s);
     if (st != GS_OK) return st;
