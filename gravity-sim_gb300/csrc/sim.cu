@@ -190,7 +190,9 @@ const void* host_mapped(const gs_sim* s, const void* p, uintptr_t align) {
 // The sources may alias set a, so no pointer is restrict-qualified.
 __global__ void k_upload(const float2* src_pos, const float2* src_vel, const float* src_mass, float2* pos_a,
                          float2* vel_a, float* mass, float2* pos_b, float2* vel_b, float* amag, uint32_t n,
-                         uint32_t n_al, uint32_t* ext) {
+                         uint32_t n_al, uint32_t* ext, const int* d_err, int* h_err) {
+    // the error word of the work before the upload (stream order), for the caller's check
+    if (blockIdx.x == 0 && threadIdx.x == 0) *h_err = *d_err;
     float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_al; i += gridDim.x * blockDim.x) {
         float2 p = make_float2(0.0f, 0.0f), v = p;
@@ -265,11 +267,14 @@ gs_status upload(gs_sim* s, const float* pos, const float* vel, const float* mas
     uint32_t* ext = s->bh.ext ? s->bh.ext + 4 * a : nullptr;
     if (ext) GS_CUDA(cudaMemsetAsync(ext, 0xFF, 4 * sizeof(uint32_t), s->stream));
     k_upload<<<copy_blocks(s->n_al), 256, 0, s->stream>>>(sp, sv, sm, s->pos[a], s->vel[a], s->mass[0], s->pos[b],
-                                                          s->vel[b], s->bh.amag, (uint32_t)n, (uint32_t)s->n_al, ext);
+                                                          s->vel[b], s->bh.amag, (uint32_t)n, (uint32_t)s->n_al, ext,
+                                                          s->d_err, s->h_err);
     GS_CUDA(cudaGetLastError());
     ++s->kernel_launches;
-    GS_CUDA(cudaStreamSynchronize(s->stream));
-    return GS_OK;
+    // the host arrays must have been read before this returns; a bounded wait (it also
+    // covers whatever was submitted before the upload)
+    GS_CUDA(cudaEventRecord(s->batch_done, s->stream));
+    return wait_event(s->batch_done, 0);
 }
 
 cudaError_t enqueue_step(gs_sim* s, int in, bool profile) {
@@ -556,11 +561,21 @@ gs_status gs_get_particles(gs_sim* s, float* pos, float* vel, float* mass) {
 }
 
 gs_status gs_set_particles(gs_sim* s, const float* pos, const float* vel, const float* mass) {
+    if (!s) return invalid("gs_set_particles: sim is NULL");
     if (!pos || !mass) return invalid("gs_set_particles: pos_xy and mass are required");
-    gs_status st = gs_sync(s, 0);
-    if (st != GS_OK) return st;
+    GS_CUDA(cudaSetDevice(s->device));
+    follow_batch(s);
     s->own_work = true;
-    return upload(s, pos, vel, mass);
+    // enqueued behind the submitted steps (stream order); the upload's synchronisation
+    // covers them, and its kernel reports their error word
+    gs_status st = upload(s, pos, vel, mass);
+    if (st != GS_OK) return st;
+    s->batch_pending = false;
+    if (s->profile_pending) {
+        st = account_profile(s);
+        if (st != GS_OK) return st;
+    }
+    return device_error(*s->h_err);
 }
 
 gs_status gs_get_accel(gs_sim* s, float* acc) {
