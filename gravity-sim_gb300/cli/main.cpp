@@ -44,6 +44,7 @@ const char* kHelp =
     "\t--simulation-algorithm: direct-sum | barnes-hut\n"
     "\t--simulation-count: The number of simulations to run (required).\n"
     "\t--box: fixed (the reference's +-500 box, default) | bbox (per-step bounding box)\n"
+    "\t--key-bits: With --box=bbox, Morton bits per axis, 1..15 (default 12: 24-bit keys; 15: 30-bit).\n"
     "\t--math: fast (default) | reference (bit-identical to the CPU restatement)\n"
     "\t--image-out: Optional PPM file with the final state drawn as the reference's window would.\n"
     "\t--image-size: WIDTHxHEIGHT of that image, defaulted to 1280x720.\n"
@@ -91,7 +92,7 @@ int main(int argc, char** argv) {
     bool detailed = false, benchmark = false, accurate = false, have_steps = false;
     float rel_alpha = -1.0f;  // < 0: theta criterion
     float rel_floor = 0.0f;   // 0: the accuracy parameter
-    int box = GS_BOX_FIXED_500, math = GS_MATH_FAST;
+    int box = GS_BOX_FIXED_500, math = GS_MATH_FAST, key_bits = 0;
     for (int i = 1; i < argc; ++i) {
         const char* a = argv[i];
         const char* v;
@@ -132,6 +133,7 @@ int main(int argc, char** argv) {
             max_steps = std::strtoull(v, nullptr, 10);
             have_steps = true;
         } else if (starts(a, "--box=", &v)) box = !std::strcmp(v, "bbox") ? GS_BOX_BOUNDING : GS_BOX_FIXED_500;
+        else if (starts(a, "--key-bits=", &v)) key_bits = (int)std::strtol(v, nullptr, 10);
         else if (starts(a, "--math=", &v)) math = !std::strcmp(v, "reference") ? GS_MATH_REFERENCE : GS_MATH_FAST;
         else if (!std::strcmp(a, "--log-detailed")) detailed = true;
         else if (!std::strcmp(a, "--no-graphics")) {
@@ -171,6 +173,7 @@ int main(int argc, char** argv) {
                                             dt, speed, eps, theta, sa, seed, 0, flags));
         system->GetParams().box_mode = box;
         system->GetParams().math_mode = math;
+        if (key_bits) system->GetParams().key_bits = key_bits;
         if (rel_alpha >= 0.0f) {
             system->GetParams().relative_accuracy = rel_alpha;
             system->GetParams().relative_theta_floor = rel_floor;

@@ -40,8 +40,8 @@ gs_status check_batch_members(gs_sim* const* sims, size_t count, const char* who
         if (s->p.algorithm == GS_BARNES_HUT) {
             if (!bh0) bh0 = s;
             else if (s->p.box_mode != bh0->p.box_mode || s->p.math_mode != bh0->p.math_mode ||
-                     (s->p.flags & kBHFlagMask) != (bh0->p.flags & kBHFlagMask))
-                return fail(w + ": Barnes-Hut systems must share box_mode, math_mode and the "
+                     (s->p.flags & kBHFlagMask) != (bh0->p.flags & kBHFlagMask) || s->bh.depth != bh0->bh.depth)
+                return fail(w + ": Barnes-Hut systems must share box_mode, key_bits, math_mode and the "
                                 "QUADRUPOLE / SAFE_RADIUS / GROUP_WALK / COUNT_INTERACTIONS flags");
         } else {
             if (!dir0) dir0 = s;
@@ -67,8 +67,8 @@ cudaError_t BatchEngine::init(int dev) {
 
 void BatchEngine::destroy() {
     cudaSetDevice(device);
-    if (root) cudaStreamSynchronize(root);
-    if (side) cudaStreamSynchronize(side);
+    if (root) (void)wait_stream(root, 0);
+    if (side) (void)wait_stream(side, 0);
     for (int k = 0; k < 2; ++k) {
         if (d_block[k]) cudaFreeAsync(d_block[k], root);
         if (h_stage[k]) cudaFreeHost(h_stage[k]);
@@ -76,7 +76,7 @@ void BatchEngine::destroy() {
         d_block[k] = h_stage[k] = nullptr;
         staged[k] = nullptr;
     }
-    if (root) cudaStreamSynchronize(root);
+    if (root) (void)wait_stream(root, 0);
     if (fork) cudaEventDestroy(fork);
     if (join) cudaEventDestroy(join);
     if (root) cudaStreamDestroy(root);
@@ -137,7 +137,10 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
     const size_t bytes = work_off + 256;
 
     const int k = cur ^ 1;  // the block the steps in flight are not reading
-    GS_CUDA(cudaEventSynchronize(staged[k]));  // staging k is free again (long done in practice)
+    {  // staging k is free again (long done in practice)
+        gs_status w = wait_event(staged[k], 0);
+        if (w != GS_OK) return w;
+    }
     if (h_bytes[k] < bytes) {
         if (h_stage[k]) GS_CUDA(cudaFreeHost(h_stage[k]));
         h_stage[k] = nullptr;

@@ -79,10 +79,11 @@ __device__ __forceinline__ bool fixed_key(float px, float py, uint32_t& key) {
     return false;
 }
 
-__device__ __forceinline__ uint32_t bbox_cell(float p, float c, float scale) {
-    float t = __fadd_rn(__fmul_rn(__fsub_rn(p, c), scale), (float)(1u << (kBBoxBits - 1)));
+// cell index along one axis, 2^bits cells (bits <= 15: exact in FP32)
+__device__ __forceinline__ uint32_t bbox_cell(float p, float c, float scale, int bits) {
+    float t = __fadd_rn(__fmul_rn(__fsub_rn(p, c), scale), (float)(1u << (bits - 1)));
     if (!(t >= 0.0f)) return 0u;
-    if (t >= (float)((1u << kBBoxBits) - 1)) return (1u << kBBoxBits) - 1;
+    if (t >= (float)((1u << bits) - 1)) return (1u << bits) - 1;
     return (uint32_t)t;
 }
 
@@ -148,9 +149,9 @@ __device__ __forceinline__ float4 bbox_block_minmax(Blk blk, const float2* __res
     return make_float4(mnx, mxx, mny, mxy);
 }
 
-// The box parameters from the extent: a square around it, 1/1024 margin, 2^kBBoxBits
-// cells per axis, in FP64.
-__device__ __forceinline__ BHParams bbox_params(float4 ext4) {
+// The box parameters from the extent: a square around it, 1/1024 margin, 2^bits cells
+// per axis, in FP64.
+__device__ __forceinline__ BHParams bbox_params(float4 ext4, int bits) {
     const double a = ext4.x, b = ext4.y, c = ext4.z, d = ext4.w;
     double cx = 0.5 * (a + b), cy = 0.5 * (c + d);
     double ext = b - a > d - c ? b - a : d - c;
@@ -158,12 +159,13 @@ __device__ __forceinline__ BHParams bbox_params(float4 ext4) {
     if (!isfinite(cx)) cx = 0.0;
     if (!isfinite(cy)) cy = 0.0;
     double half = ext * 0.5 * (1.0 + 1.0 / 1024.0);
-    double scale = (double)(1u << (kBBoxBits - 1)) / half;
+    double scale = (double)(1u << (bits - 1)) / half;
     BHParams p;
+    p.bits = bits;
     p.cx = (float)cx;
     p.cy = (float)cy;
     p.scale = (float)scale;
-    double side0 = (double)(1u << kBBoxBits) / (double)p.scale;
+    double side0 = (double)(1u << bits) / (double)p.scale;
     p.radius0 = (float)(side0 * side0 * 0.5);
     p.inv_scale = (float)(1.0 / (double)p.scale);
     return p;
@@ -207,7 +209,7 @@ __device__ __forceinline__ float4 bbox_reduce_partials(const float* __restrict__
 // and writes the box parameters.
 __device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ pos, uint32_t n,
                                           float* __restrict__ part, uint32_t* __restrict__ ticket,
-                                          BHParams* __restrict__ out) {
+                                          BHParams* __restrict__ out, int bits) {
     __shared__ bool last;
     const float4 m = bbox_block_minmax(blk, pos, n);
     if (threadIdx.x == 0) {
@@ -222,7 +224,7 @@ __device__ __forceinline__ void bbox_body(Blk blk, const float2* __restrict__ po
     if (!last) return;
     __threadfence();
     const float4 e = bbox_reduce_partials(part, blk.count);
-    if (threadIdx.x == 0) *out = bbox_params(e);
+    if (threadIdx.x == 0) *out = bbox_params(e, bits);
 }
 
 // ------------------------------------------------------------------------------------
@@ -253,7 +255,8 @@ __device__ __forceinline__ void keygen_body(Blk blk, int bbox_mode, const BHPara
         float2 q = pos_in[i];
         uint32_t key;
         if (bbox_mode) {
-            key = spread_bits(bbox_cell(q.x, p.cx, p.scale)) | (spread_bits(bbox_cell(q.y, p.cy, p.scale)) << 1);
+            key = spread_bits(bbox_cell(q.x, p.cx, p.scale, p.bits)) |
+                  (spread_bits(bbox_cell(q.y, p.cy, p.scale, p.bits)) << 1);
             ++valid;
         } else if (fixed_key(q.x, q.y, key)) {
             ++valid;
@@ -385,11 +388,12 @@ __device__ __forceinline__ void ext_add(uint32_t* __restrict__ ext, float mnx, f
 __global__ void __launch_bounds__(kKeyThreads)
 k_ext_keys(float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos_out, float* mass_out, uint32_t n,
            uint32_t* __restrict__ keys, uint32_t* __restrict__ hist, int passes, uint32_t* __restrict__ valid_count,
-           BHParams* __restrict__ params, const uint32_t* __restrict__ ext_in, uint32_t* __restrict__ ext_out) {
+           BHParams* __restrict__ params, const uint32_t* __restrict__ ext_in, uint32_t* __restrict__ ext_out,
+           int bits) {
     pdl_enter();
     __shared__ BHParams sp;
     if (threadIdx.x == 0) {
-        sp = bbox_params(ext_decode(ext_in));
+        sp = bbox_params(ext_decode(ext_in), bits);
         if (blockIdx.x == 0) {
             *params = sp;
             for (int j = 0; j < 4; ++j) ext_out[j] = 0xFFFFFFFFu;
@@ -1101,10 +1105,10 @@ constexpr int kGroupWarps = 2;
 constexpr int kGroupSize = 64;  // particles per walk
 // Records still to test.  Pops take the top 32 and push at most four internal children
 // each, one level deeper, so the stack holds at most one block of <= 128 entries per level
-// and blocks of strictly increasing level: <= 96 * D + 128 = 1280 for D = 12.  Overflow
+// and blocks of strictly increasing level: <= 96 * D + 128 = 1568 for D = 15.  Overflow
 // is still checked and reported.
-constexpr int kStackCap = 1280;
-static_assert(kStackCap >= 96 * (kBBoxBits > kFixedDepth ? kBBoxBits : kFixedDepth) + 128, "walk stack bound");
+constexpr int kStackCap = 1568;
+static_assert(kStackCap >= 96 * (kBBoxMaxBits > kFixedDepth ? kBBoxMaxBits : kFixedDepth) + 128, "walk stack bound");
 constexpr int kItemCap = 128;     // runs of particle leaves between evaluations
 constexpr int kNodeCap = 160;     // accepted nodes between evaluations
 
@@ -1519,6 +1523,8 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
                                          cap, stat, err, amag, alpha, floor2, ext);
 }
 
+__global__ void k_set_params(BHParams* __restrict__ out, BHParams v) { *out = v; }
+
 int grid_for(uint64_t n, int threads) {
     uint64_t b = (n + threads - 1) / threads;
     if (b > 152ull * 16) b = 152ull * 16;
@@ -1528,10 +1534,12 @@ int grid_for(uint64_t n, int threads) {
 
 }  // namespace
 
+// Bits per axis of the bounding-box keys (gs_params.key_bits, 0: the default 12).
+int bh_key_bits(const gs_params* p) { return p->key_bits ? p->key_bits : kBBoxBits; }
+
 // Records: the particle leaves plus at most level_cap(d) internal nodes per level d
 // (disjoint cells of >= 2 particles).
-uint64_t bh_capacity(int box_mode, uint64_t n_al) {
-    const int D = box_mode == GS_BOX_BOUNDING ? kBBoxBits : kFixedDepth;
+uint64_t bh_capacity(int D, uint64_t n_al) {
     uint64_t c = n_al + 64;
     for (int d = 0; d <= D; ++d) c += level_cap(d, (uint32_t)n_al);
     return c;
@@ -1544,6 +1552,7 @@ enum {
     kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrLevel = 16,
     kCtrBarrier = 32, kCtrCount = 40
 };
+static_assert(kHostCounters + kCtrCount <= kHostWords, "counter readback fits the pinned word block");
 
 // Lays the Barnes-Hut scratch out in the system's slab (sim_carve); while the system is
 // being sized (no slab yet) this only counts bytes.
@@ -1551,9 +1560,11 @@ void bh_carve(gs_sim* s) {
     BHWork& w = s->bh;
     const uint64_t n = s->n_al;
     const bool bbox = s->p.box_mode == GS_BOX_BOUNDING;
-    w.depth = bbox ? kBBoxBits : kFixedDepth;
-    w.passes = 3;  // 24-bit keys (bounding box) / 20-bit keys + removal bit (fixed box)
-    w.cap = bh_capacity(s->p.box_mode, n);
+    w.depth = bbox ? bh_key_bits(&s->p) : kFixedDepth;
+    // 8-bit digits: 2 * depth key bits in the bounding box (3 passes for 24-bit keys, 4 for
+    // 30-bit keys), 20-bit keys + removal bit in the fixed box (3 passes)
+    w.passes = bbox ? (2 * w.depth + 7) / 8 : 3;
+    w.cap = bh_capacity(w.depth, n);
     w.sort_tiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     w.scan_tiles = (uint32_t)((n + 1 + kScanTile - 1) / kScanTile);
     for (int b = 0; b < 2; ++b) {
@@ -1599,10 +1610,12 @@ cudaError_t bh_init(gs_sim* s) {
     if (e == cudaSuccess) e = cudaMemsetAsync(w.zero_base, 0, w.zero_bytes, s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(w.rec, 0, (w.cap + 32) * sizeof(float4), s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(w.skip, 0, (w.cap + 32) * sizeof(uint32_t), s->stream);
-    BHParams fixed{0.0f, 0.0f, (float)kGrid / (2.0f * kSimSize), kSimSize * kSimSize * 2.0f,
-                   2.0f * kSimSize / (float)kGrid};
-    if (e == cudaSuccess) e = cudaMemcpyAsync(w.params, &fixed, sizeof fixed, cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);  // `fixed` lives on this stack frame
+    const BHParams fixed{0.0f, 0.0f, (float)kGrid / (2.0f * kSimSize), kSimSize * kSimSize * 2.0f,
+                         2.0f * kSimSize / (float)kGrid, kFixedDepth};
+    if (e == cudaSuccess) {  // by value through a kernel argument: nothing on the host to wait for
+        k_set_params<<<1, 1, 0, s->stream>>>(w.params, fixed);
+        e = cudaGetLastError();
+    }
     // the cooperative moments launch: as many blocks as fit on the device at once
     int per_sm = 0, sms = 0;
     if (e == cudaSuccess)
@@ -1678,7 +1691,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     if (bbox) {  // the box from the extent carried with the input set
         GS_TRY_LAUNCH(launch(next_pdl(), k_ext_keys, keygen_blocks(n), kKeyThreads, st, s->pos[in], s->mass[in],
                              s->pos[out], s->mass[out], n, w.keys[0], w.hist, w.passes, ctr + kCtrValid, w.params,
-                             (const uint32_t*)(w.ext + 4 * in), w.ext + 4 * out));
+                             (const uint32_t*)(w.ext + 4 * in), w.ext + 4 * out, w.depth));
     } else {
         GS_TRY_LAUNCH(launch(next_pdl(), k_keygen, keygen_blocks(n), kKeyThreads, st, 0,
                              (const BHParams*)w.params, s->pos[in], s->mass[in], s->pos[out], s->mass[out], n,
@@ -1762,37 +1775,46 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
 }
 
 // Host readback of the most recent tree (not on the hot path).
+// Device-to-host copy on the system's stream, waited for with the system's bound.
+static gs_status read_back(gs_sim* s, void* dst, const void* src, size_t bytes) {
+    GS_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s->stream));
+    return sim_wait(s);
+}
+
+// Host readback of the most recent tree (not on the hot path).  A wait that times out
+// leaves its host buffer allocated: the copy into it may still be pending.
 gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
                         float* node_pos, float* node_mass, float* node_quad, uint64_t capacity,
                         uint64_t* tree_records) {
     BHWork& w = s->bh;
     const uint64_t n = s->n_al;
-    uint32_t ctr[kCtrCount];
-    GS_CUDA(cudaMemcpy(ctr, w.counters, sizeof ctr, cudaMemcpyDeviceToHost));
+    uint32_t* ctr = (uint32_t*)s->h_err + kHostCounters;  // pinned, owned by the system
+    gs_status st = read_back(s, ctr, w.counters, kCtrCount * sizeof(uint32_t));
+    if (st != GS_OK) return st;
     const uint64_t nv = ctr[kCtrValid];
     const uint64_t T = nv + ctr[kCtrInternal];
     if (tree_records) *tree_records = T;
     if (keys || sorted_src) {
-        uint32_t* hk = new uint32_t[n];
-        uint32_t* hi = new uint32_t[n];
-        cudaError_t e1 = cudaMemcpy(hk, w.keys[w.final_keys], n * 4, cudaMemcpyDeviceToHost);
-        cudaError_t e2 = cudaMemcpy(hi, w.idx[w.final_keys], n * 4, cudaMemcpyDeviceToHost);
-        if (e1 == cudaSuccess && e2 == cudaSuccess) {
+        uint32_t* hk = new uint32_t[2 * n];
+        uint32_t* hi = hk + n;
+        GS_CUDA(cudaMemcpyAsync(hk, w.keys[w.final_keys], n * 4, cudaMemcpyDeviceToHost, s->stream));
+        st = read_back(s, hi, w.idx[w.final_keys], n * 4);
+        if (st == GS_ERR_TIMEOUT) return st;
+        if (st == GS_OK) {
             for (uint64_t q = 0; q < n; ++q) {
                 if (keys && hi[q] < n) keys[hi[q]] = q < nv ? hk[q] : kKeyRemoved;
                 if (sorted_src) sorted_src[q] = q < nv ? hi[q] : (uint32_t)n;
             }
         }
         delete[] hk;
-        delete[] hi;
-        GS_CUDA(e1);
-        GS_CUDA(e2);
+        if (st != GS_OK) return st;
     }
     const uint64_t m = T < capacity ? T : capacity;
     if (m && (node_radius || node_pos || node_mass)) {
         float4* hr = new float4[m];
-        cudaError_t e1 = cudaMemcpy(hr, w.rec, m * sizeof(float4), cudaMemcpyDeviceToHost);
-        if (e1 == cudaSuccess) {
+        st = read_back(s, hr, w.rec, m * sizeof(float4));
+        if (st == GS_ERR_TIMEOUT) return st;
+        if (st == GS_OK) {
             for (uint64_t q = 0; q < m; ++q) {
                 if (node_pos) {
                     node_pos[2 * q] = hr[q].x;
@@ -1803,18 +1825,22 @@ gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_
             }
         }
         delete[] hr;
-        GS_CUDA(e1);
+        if (st != GS_OK) return st;
     }
-    if (m && node_skip) GS_CUDA(cudaMemcpy(node_skip, w.skip, m * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (m && node_skip) {
+        st = read_back(s, node_skip, w.skip, m * sizeof(uint32_t));
+        if (st != GS_OK) return st;
+    }
     if (m && node_quad) {
         if (!w.quad) {
             std::memset(node_quad, 0, 3 * m * sizeof(float));
         } else {
             float4* hq = new float4[m];
             uint32_t* hs = new uint32_t[m];
-            cudaError_t e1 = cudaMemcpy(hq, w.quad, m * sizeof(float4), cudaMemcpyDeviceToHost);
-            if (e1 == cudaSuccess) e1 = cudaMemcpy(hs, w.skip, m * sizeof(uint32_t), cudaMemcpyDeviceToHost);
-            if (e1 == cudaSuccess)
+            GS_CUDA(cudaMemcpyAsync(hq, w.quad, m * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+            st = read_back(s, hs, w.skip, m * sizeof(uint32_t));
+            if (st == GS_ERR_TIMEOUT) return st;
+            if (st == GS_OK)
                 for (uint64_t q = 0; q < m; ++q) {  // a particle leaf has no spread: zero moments
                     const bool leaf = hs[q] == 1u;
                     node_quad[3 * q] = leaf ? 0.0f : hq[q].x;
@@ -1823,7 +1849,7 @@ gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_
                 }
             delete[] hq;
             delete[] hs;
-            GS_CUDA(e1);
+            if (st != GS_OK) return st;
         }
     }
     return GS_OK;
@@ -1831,15 +1857,16 @@ gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_
 
 gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits,
                          uint64_t* nodes) {
-    uint32_t ctr[kCtrCount];
-    GS_CUDA(cudaMemcpy(ctr, s->bh.counters, sizeof ctr, cudaMemcpyDeviceToHost));
+    uint32_t* ctr = (uint32_t*)s->h_err + kHostCounters;
+    gs_status st = read_back(s, ctr, s->bh.counters, kCtrCount * sizeof(uint32_t));
+    if (st != GS_OK) return st;
     *nv = ctr[kCtrValid];
     *internal = ctr[kCtrInternal];
-    unsigned long long st[3];
-    memcpy(st, ctr + kCtrStat, sizeof st);
-    *inter = st[0];
-    *visits = st[1];
-    *nodes = st[2];
+    unsigned long long c[3];
+    memcpy(c, ctr + kCtrStat, sizeof c);
+    *inter = c[0];
+    *visits = c[1];
+    *nodes = c[2];
     return GS_OK;
 }
 
@@ -1901,7 +1928,7 @@ __global__ void __launch_bounds__(kBBoxThreads) kb_bbox(BatchArgs a) {
     pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
-    bbox_body(bb.blk, d.pos[bb.in], d.n_al, d.bbox_part, d.counters + kCtrBBox, d.params);
+    bbox_body(bb.blk, d.pos[bb.in], d.n_al, d.bbox_part, d.counters + kCtrBBox, d.params, d.depth);
 }
 
 __global__ void __launch_bounds__(kKeyThreads) kb_keygen(BatchArgs a) {

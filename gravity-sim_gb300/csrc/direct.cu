@@ -19,8 +19,6 @@
 // Roofline: 14 algorithmic FLOP per pair (2 sub, 2 FMA for r^2, rsqrt, 3 mul, 2 FMA),
 // 9 FP32 operations + 1 MUFU per pair, issued as packed f32x2 instructions for a thread's
 // two targets (4.5 issues + 1 MUFU per pair); FP32-bound.
-#include <mutex>
-
 #include "internal.cuh"
 
 namespace gsim {
@@ -320,19 +318,22 @@ k_energy_f64(const float2* __restrict__ pos, const float2* __restrict__ vel, con
 
 }  // namespace
 
-cudaError_t energy_f64(gs_sim* s, double* kinetic, double* potential) {
+gs_status energy_f64(gs_sim* s, double* kinetic, double* potential) {
     const uint32_t n = (uint32_t)s->n_al;
     const uint32_t blocks = (n + 255) / 256;
     double2* part = nullptr;
-    cudaError_t e = cudaMallocAsync(&part, blocks * sizeof(double2), s->stream);
-    if (e != cudaSuccess) return e;
+    GS_CUDA(cudaMallocAsync(&part, blocks * sizeof(double2), s->stream));
     k_energy_f64<<<blocks, 256, 0, s->stream>>>(s->pos[s->in], s->vel[s->in], s->mass[s->in], n, (double)s->eps2,
                                                  part);
     double2* host = new double2[blocks];
-    e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(host, part, blocks * sizeof(double2), cudaMemcpyDeviceToHost, s->stream);
     cudaFreeAsync(part, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    gs_status w = e == cudaSuccess ? sim_wait(s) : cuda_fail(e, "energy_f64");
+    if (w != GS_OK) {  // the readback may still be pending: keep its destination alive
+        if (w != GS_ERR_TIMEOUT) delete[] host;
+        return w;
+    }
     double ke = 0.0, pp = 0.0;
     for (uint32_t b = 0; b < blocks; ++b) {
         ke += host[b].x;
@@ -341,7 +342,7 @@ cudaError_t energy_f64(gs_sim* s, double* kinetic, double* potential) {
     delete[] host;
     *kinetic = ke;
     *potential = -0.5 * (double)s->G * pp;  // every pair was counted from both ends
-    return e;
+    return GS_OK;
 }
 
 static int pick_chunks(uint64_t n_al, int ipt) {
@@ -465,30 +466,18 @@ constexpr uint32_t kNoAllocMaxTiles = GS_NOALLOC_MAX_PARTICLES / (kDirectBlock *
 static __device__ __align__(256) float4 g_noalloc_partials[kNoAllocPartialBytes / sizeof(float4)];
 static __device__ __align__(256) uint32_t g_noalloc_tickets[kNoAllocMaxTiles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-float4* g_noalloc_partials_addr[kMaxDevices] = {};
-uint32_t* g_noalloc_tickets_addr[kMaxDevices] = {};
-
-// Device addresses of the two arrays on the current device, looked up once per device.
-// The host-side names are stand-ins, not device addresses, so they are never passed to
-// a kernel directly.
-gs_status noalloc_scratch(int dev, float4** partials, uint32_t** tickets) {
-    if (dev < 0 || dev >= kMaxDevices) {
-        set_error("gs_direct_step_noalloc: device ordinal above 63");
-        return GS_ERR_INVALID_ARGUMENT;
-    }
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_partials_addr[dev]) {
-        void* p = nullptr;
-        void* t = nullptr;
-        GS_CUDA(cudaGetSymbolAddress(&p, g_noalloc_partials));
-        GS_CUDA(cudaGetSymbolAddress(&t, g_noalloc_tickets));
-        g_noalloc_partials_addr[dev] = (float4*)p;
-        g_noalloc_tickets_addr[dev] = (uint32_t*)t;
-    }
-    *partials = g_noalloc_partials_addr[dev];
-    *tickets = g_noalloc_tickets_addr[dev];
+// Device addresses of the two arrays in the current context, looked up on every call:
+// the lookup allocates nothing and is cheap, and a cached address could outlive the
+// module it points into (cudaDeviceReset, or another context on the same ordinal).  The
+// host-side names are stand-ins, not device addresses, so they are never passed to a
+// kernel directly.
+gs_status noalloc_scratch(float4** partials, uint32_t** tickets) {
+    void* p = nullptr;
+    void* t = nullptr;
+    GS_CUDA(cudaGetSymbolAddress(&p, g_noalloc_partials));
+    GS_CUDA(cudaGetSymbolAddress(&t, g_noalloc_tickets));
+    *partials = (float4*)p;
+    *tickets = (uint32_t*)t;
     return GS_OK;
 }
 
@@ -514,11 +503,9 @@ extern "C" gs_status gs_direct_step_noalloc(const float* d_pos_in, const float* 
                   "of its built-in scratch; use gs_create / gs_run for larger systems");
         return GS_ERR_CAPACITY;
     }
-    int dev = 0;
-    GS_CUDA(cudaGetDevice(&dev));
     float4* partials = nullptr;
     uint32_t* tickets = nullptr;
-    gs_status st = noalloc_scratch(dev, &partials, &tickets);
+    gs_status st = noalloc_scratch(&partials, &tickets);
     if (st != GS_OK) return st;
 
     const uint32_t n_al = (uint32_t)n;

@@ -23,9 +23,15 @@ constexpr uint32_t kAlignment = 64;         // GetRequiredParticleAlignment()
 constexpr float kSimSize = 500.0f;          // BarnesHutSimulation.cpp:580
 constexpr uint32_t kGrid = 1024;            // BarnesHutSimulation.cpp:582
 constexpr int kFixedDepth = 10;             // finest level of the fixed box
-constexpr int kBBoxBits = 12;               // per-axis bits in bounding-box mode (24-bit keys)
+constexpr int kBBoxBits = 12;               // default per-axis bits in bounding-box mode (24-bit keys)
+constexpr int kBBoxMaxBits = 15;            // largest per-axis bits (30-bit keys, 4 radix passes)
 constexpr uint32_t kKeyRemovedSort = 1u << 20;  // sort key of removed particles (fixed box)
 constexpr uint32_t kKeyRemoved = 0xFFFFFFFFu;   // reported key of removed particles
+
+// pinned host words of a system (gs_sim::h_err): the device error word at 0, counter
+// readbacks from kHostCounters on
+constexpr int kHostWords = 64;
+constexpr int kHostCounters = 16;
 
 // stage indices of gs_stats.stage_ms
 enum Stage { kStageBBox = 0, kStageKeys, kStageSort, kStageScan, kStageRecords, kStageSums, kStageForce, kStageDirect };
@@ -97,10 +103,11 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
 struct BHParams {
     float cx, cy, scale, radius0;  // bounding box (fixed box: 0, 0, 1.024, 500000)
     float inv_scale;               // float(1 / scale), taken once in FP64
+    int bits;                      // cells per axis 2^bits (bounding box; 10 for the fixed box)
 };
 
 struct BHWork {
-    int depth = 0;        // finest level D (10 fixed box, 15 bounding box)
+    int depth = 0;        // finest level D (10 fixed box, key_bits in bounding-box mode)
     int passes = 0;       // radix passes of 8 bits
     uint64_t cap = 0;     // record capacity
     uint32_t* keys[2] = {nullptr, nullptr};
@@ -219,7 +226,8 @@ struct gs_sim {
     float floor2 = 0;       // squared theta floor of the relative criterion
     float2* acc = nullptr;  // GS_FLAG_RECORD_ACCEL
     int* d_err = nullptr;
-    int* h_err = nullptr;   // pinned host copy of d_err (check_device_error)
+    int* h_err = nullptr;   // pinned host words: [0] copy of d_err (check_device_error),
+                            // [kHostCounters ..) counter readbacks (gsim::kHostWords in all)
     gsim::BHWork bh;
     gsim::DirectWork dw;
     cudaEvent_t batch_done = nullptr;
@@ -240,6 +248,7 @@ struct gs_sim {
     size_t carved = 0;               // bytes laid out so far (sim_carve)
     cudaEvent_t follow = nullptr;    // a batch step this system's next work must follow
     bool own_work = false;           // work submitted on its own stream since the last batch run
+    uint64_t timeout_ns = 0;         // bound of every host wait on this system (0: 600 s)
 };
 
 namespace gsim {
@@ -253,6 +262,13 @@ gs_status cuda_fail(cudaError_t e, const char* what);
         cudaError_t _e = (call);                               \
         if (_e != cudaSuccess) return gsim::cuda_fail(_e, #call); \
     } while (0)
+
+// Bounded host waits (GS_ERR_TIMEOUT after timeout_ns; 0: 600 s): an event, a stream
+// (through a private event), or everything enqueued on a system's stream so far (its
+// timeout, gs_set_timeout).
+gs_status wait_event(cudaEvent_t ev, uint64_t timeout_ns);
+gs_status wait_stream(cudaStream_t st, uint64_t timeout_ns);
+gs_status sim_wait(gs_sim* s);
 
 // Device memory of a system: one slab from the device's default pool (stream-ordered on
 // the system's stream, kept cached), carved into 256-byte aligned buffers.  Carving with
@@ -268,9 +284,10 @@ void direct_carve(gs_sim* s);
 cudaError_t direct_init(gs_sim* s);
 cudaError_t direct_step(gs_sim* s, int in, int out, bool profile);
 cudaError_t accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* d_targets, double2* d_out);
-cudaError_t energy_f64(gs_sim* s, double* kinetic, double* potential);
+gs_status energy_f64(gs_sim* s, double* kinetic, double* potential);
 void free_snapshot_ring(const gs_sim* s);
-uint64_t bh_capacity(int box_mode, uint64_t n_al);
+uint64_t bh_capacity(int depth, uint64_t n_al);
+int bh_key_bits(const gs_params* p);
 
 // batched stages (one launch per stage over every system of a plan)
 void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]);

@@ -130,10 +130,9 @@ void free_snapshot_ring(const gs_sim* s) {
     }
     if (!r) return;
     cudaSetDevice(r->device);
-    cudaStreamSynchronize(r->reader);
-    if (r->pos) cudaFreeAsync(r->pos, r->reader);
+    if (r->pos) cudaFreeAsync(r->pos, r->reader);  // stream-ordered after every read
     if (r->fb) cudaFreeAsync(r->fb, r->reader);
-    cudaStreamSynchronize(r->reader);
+    (void)wait_stream(r->reader, s->timeout_ns);
     for (auto e : r->ready)
         if (e) cudaEventDestroy(e);
     cudaStreamDestroy(r->reader);
@@ -177,9 +176,8 @@ gs_status gs_render_points(gs_sim* s, uint32_t width, uint32_t height, const flo
     cudaError_t e = splat(s->pos[s->in], (uint32_t)s->n, camera, width, height, fb, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(image, fb, bytes, cudaMemcpyDeviceToHost, s->stream);
     cudaFreeAsync(fb, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     GS_CUDA(e);
-    return GS_OK;
+    return sim_wait(s);
 }
 
 gs_status gs_snapshot_take(gs_sim* s, uint32_t slots, uint64_t* ticket) {
@@ -250,8 +248,7 @@ gs_status gs_snapshot_positions(gs_sim* s, uint64_t ticket, float* pos_xy) {
     GS_CUDA(cudaStreamWaitEvent(r->reader, r->ready[k], 0));
     GS_CUDA(cudaMemcpyAsync(pos_xy, r->pos + (size_t)k * r->n, r->n * sizeof(float2), cudaMemcpyDeviceToHost,
                             r->reader));
-    GS_CUDA(cudaStreamSynchronize(r->reader));
-    return GS_OK;
+    return wait_stream(r->reader, s->timeout_ns);
 }
 
 gs_status gs_snapshot_render(gs_sim* s, uint64_t ticket, uint32_t width, uint32_t height, const float* camera,
@@ -269,8 +266,7 @@ gs_status gs_snapshot_render(gs_sim* s, uint64_t ticket, uint32_t width, uint32_
     GS_CUDA(cudaStreamWaitEvent(r->reader, r->ready[k], 0));
     GS_CUDA(splat(r->pos + (size_t)k * r->n, (uint32_t)r->n, camera, width, height, r->fb, r->reader));
     GS_CUDA(cudaMemcpyAsync(image, r->fb, (size_t)width * height, cudaMemcpyDeviceToHost, r->reader));
-    GS_CUDA(cudaStreamSynchronize(r->reader));
-    return GS_OK;
+    return wait_stream(r->reader, s->timeout_ns);
 }
 
 gs_status gs_write_ppm(const char* path, uint32_t width, uint32_t height, const uint8_t* image) {

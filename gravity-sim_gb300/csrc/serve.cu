@@ -245,7 +245,8 @@ gs_status step(gs_server* s) {
     if (s->members.empty()) return GS_OK;
     const uint32_t depth = s->cfg.steps_in_flight ? s->cfg.steps_in_flight : 2;
     while (s->inflight.size() >= depth) {
-        GS_CUDA(cudaEventSynchronize(s->inflight.front()));
+        gs_status w = wait_event(s->inflight.front(), 0);
+        if (w != GS_OK) return w;
         s->spare.push_back(s->inflight.front());
         s->inflight.pop_front();
     }
@@ -299,7 +300,7 @@ void destroy_server(gs_server* s) {
     s->cv.notify_all();
     for (auto& t : s->workers) t.join();
     cudaSetDevice(s->eng.device);
-    if (s->eng.root) cudaStreamSynchronize(s->eng.root);
+    if (s->eng.root) (void)wait_stream(s->eng.root, 0);
     for (auto& kv : s->all) {
         release(s, kv.second);
         delete kv.second;

@@ -20,6 +20,7 @@
 namespace gsim {
 
 static thread_local std::string g_last_error;
+constexpr uint64_t kDefaultTimeoutNs = 600ull * 1000000000ull;
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -93,27 +94,8 @@ cudaError_t keep_pool_memory(int device) {
     return e;
 }
 
-gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
-                        float* node_pos, float* node_mass, float* node_quad, uint64_t capacity,
-                        uint64_t* tree_records);
-gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits,
-                         uint64_t* nodes);
-
-}  // namespace gsim
-
-using namespace gsim;
-
-namespace {
-
-constexpr uint64_t kMaxParticles = 1ull << 28;
-constexpr uint64_t kMaxBarnesHutParticles = 1ull << 26;  // keeps record indices below 2^31
-constexpr uint64_t kDefaultTimeoutNs = 600ull * 1000000000ull;
-
-gs_status invalid(const char* msg) {
-    set_error(msg);
-    return GS_ERR_INVALID_ARGUMENT;
-}
-
+// Host waits on the GPU are bounded: they poll with a deadline and give up with
+// GS_ERR_TIMEOUT after it (timeout_ns 0: 600 s), so a hung device never hangs the caller.
 gs_status wait_event(cudaEvent_t ev, uint64_t timeout_ns) {
     if (!timeout_ns) timeout_ns = kDefaultTimeoutNs;
     auto t0 = std::chrono::steady_clock::now();
@@ -133,6 +115,43 @@ gs_status wait_event(cudaEvent_t ev, uint64_t timeout_ns) {
     }
 }
 
+gs_status wait_stream(cudaStream_t st, uint64_t timeout_ns) {
+    cudaEvent_t ev = nullptr;
+    GS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, st);
+    gs_status r = e == cudaSuccess ? wait_event(ev, timeout_ns) : cuda_fail(e, "cudaEventRecord");
+    cudaEventDestroy(ev);  // released once it completes, if the wait gave up
+    return r;
+}
+
+gs_status sim_wait(gs_sim* s) {
+    GS_CUDA(cudaEventRecord(s->batch_done, s->stream));
+    s->batch_pending = true;
+    gs_status w = wait_event(s->batch_done, s->timeout_ns);
+    if (w == GS_OK) s->batch_pending = false;
+    return w;
+}
+
+gs_status bh_debug_tree(gs_sim* s, uint32_t* keys, uint32_t* sorted_src, uint32_t* node_skip, float* node_radius,
+                        float* node_pos, float* node_mass, float* node_quad, uint64_t capacity,
+                        uint64_t* tree_records);
+gs_status bh_read_counts(gs_sim* s, uint64_t* nv, uint64_t* internal, uint64_t* inter, uint64_t* visits,
+                         uint64_t* nodes);
+
+}  // namespace gsim
+
+using namespace gsim;
+
+namespace {
+
+constexpr uint64_t kMaxParticles = 1ull << 28;
+constexpr uint64_t kMaxBarnesHutParticles = 1ull << 26;  // keeps record indices below 2^31
+
+gs_status invalid(const char* msg) {
+    set_error(msg);
+    return GS_ERR_INVALID_ARGUMENT;
+}
+
 // Status of a device error word.
 gs_status device_error(int err) {
     if (err) {
@@ -148,14 +167,15 @@ gs_status device_error(int err) {
 // into the system's pinned word, then the stream synchronisation).
 gs_status check_device_error(gs_sim* s) {
     GS_CUDA(cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    GS_CUDA(cudaStreamSynchronize(s->stream));
+    gs_status w = sim_wait(s);
+    if (w != GS_OK) return w;
     return device_error(*s->h_err);
 }
 
 void free_sim(gs_sim* s) {
     if (!s) return;
     cudaSetDevice(s->device);
-    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->stream) (void)wait_stream(s->stream, s->timeout_ns);
     free_snapshot_ring(s);
     for (int p = 0; p < 2; ++p)
         if (s->graph[p]) cudaGraphExecDestroy(s->graph[p]);
@@ -272,9 +292,9 @@ gs_status upload(gs_sim* s, const float* pos, const float* vel, const float* mas
     GS_CUDA(cudaGetLastError());
     ++s->kernel_launches;
     // the host arrays must have been read before this returns; a bounded wait (it also
-    // covers whatever was submitted before the upload)
-    GS_CUDA(cudaEventRecord(s->batch_done, s->stream));
-    return wait_event(s->batch_done, 0);
+    // covers whatever was submitted before the upload).  After a timeout the kernel may
+    // still read them: the caller keeps them until a gs_sync succeeds.
+    return sim_wait(s);
 }
 
 cudaError_t enqueue_step(gs_sim* s, int in, bool profile) {
@@ -287,7 +307,8 @@ gs_status account_profile(gs_sim* s) {
     s->profile_pending = false;
     for (int st = 0; st < GS_STAGE_COUNT; ++st) {
         if (!(s->stage_ran & (1u << st))) continue;
-        GS_CUDA(cudaEventSynchronize(s->ev[2 * st + 1]));
+        gs_status w = wait_event(s->ev[2 * st + 1], s->timeout_ns);
+        if (w != GS_OK) return w;
         float ms = 0.f;
         GS_CUDA(cudaEventElapsedTime(&ms, s->ev[2 * st], s->ev[2 * st + 1]));
         s->stats.stage_ms[st] += ms;
@@ -315,6 +336,7 @@ void gs_params_init(gs_params* p) {
     p->flags = 0;
     p->relative_accuracy = 0.006f;
     p->relative_theta_floor = 0.0f;
+    p->key_bits = kBBoxBits;
 }
 
 const char* gs_status_string(gs_status s) {
@@ -339,7 +361,9 @@ uint64_t gs_required_alignment(int32_t algorithm) {
     return kAlignment;
 }
 
-uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count) { return bh_capacity(box_mode, aligned_count); }
+uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count) {
+    return bh_capacity(box_mode == GS_BOX_BOUNDING ? kBBoxMaxBits : kFixedDepth, aligned_count);
+}
 
 uint64_t gs_footprint(const gs_params* p, uint64_t n) {
     if (!p || !n) return 0;
@@ -375,6 +399,8 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
     if ((params->flags & GS_FLAG_RELATIVE_MAC) &&
         !(params->relative_theta_floor >= 0.0f && params->relative_theta_floor < INFINITY))
         return invalid("gs_create: relative_theta_floor must be finite and >= 0");
+    if (params->key_bits < 0 || params->key_bits > kBBoxMaxBits)
+        return invalid("gs_create: key_bits must be 1..15 (0: 12)");
     if ((params->flags & GS_FLAG_PLAIN_SUM) && params->algorithm != GS_DIRECT_SUM)
         return invalid("gs_create: GS_FLAG_PLAIN_SUM applies to direct sum only");
     if ((params->flags & (GS_FLAG_QUADRUPOLE | GS_FLAG_SAFE_RADIUS | GS_FLAG_GROUP_WALK)) &&
@@ -423,7 +449,7 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
     GS_TRY(keep_pool_memory(s->device));
     GS_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     GS_TRY(cudaEventCreateWithFlags(&s->batch_done, cudaEventDisableTiming));
-    GS_TRY(cudaMallocHost((void**)&s->h_err, sizeof(int)));
+    GS_TRY(cudaMallocHost((void**)&s->h_err, kHostWords * sizeof(int)));
     for (auto& e : s->ev) GS_TRY(cudaEventCreate(&e));
     carve_all(s);  // sizing pass
     GS_TRY(cudaMallocAsync(&s->slab, s->carved, s->stream));
@@ -448,7 +474,7 @@ gs_status gs_run(gs_sim* s, uint32_t count) {
     follow_batch(s);
     s->own_work = true;
     if (s->batch_pending) {  // wait for the previous submit, like the reference's fence wait
-        gs_status w = wait_event(s->batch_done, 0);
+        gs_status w = wait_event(s->batch_done, s->timeout_ns);
         if (w != GS_OK) return w;
         s->batch_pending = false;
     }
@@ -504,7 +530,7 @@ gs_status gs_sync(gs_sim* s, uint64_t timeout_ns) {
     GS_CUDA(cudaSetDevice(s->device));
     follow_batch(s);
     if (s->batch_pending) {
-        gs_status w = wait_event(s->batch_done, timeout_ns);
+        gs_status w = wait_event(s->batch_done, timeout_ns ? timeout_ns : s->timeout_ns);
         if (w != GS_OK) return w;
         s->batch_pending = false;
     }
@@ -532,7 +558,7 @@ gs_status gs_get_particles(gs_sim* s, float* pos, float* vel, float* mass) {
         ++s->kernel_launches;
         GS_CUDA(cudaEventRecord(s->batch_done, s->stream));
         s->batch_pending = true;
-        gs_status w = wait_event(s->batch_done, 0);
+        gs_status w = wait_event(s->batch_done, s->timeout_ns);
         if (w != GS_OK) return w;
         s->batch_pending = false;
         if (s->profile_pending) {
@@ -542,7 +568,7 @@ gs_status gs_get_particles(gs_sim* s, float* pos, float* vel, float* mass) {
         return device_error(*s->h_err);
     }
     if (s->batch_pending) {
-        gs_status w = wait_event(s->batch_done, 0);
+        gs_status w = wait_event(s->batch_done, s->timeout_ns);
         if (w != GS_OK) return w;
         s->batch_pending = false;
     }
@@ -556,8 +582,7 @@ gs_status gs_get_particles(gs_sim* s, float* pos, float* vel, float* mass) {
     if (pos) GS_CUDA(cudaMemcpyAsync(pos, s->pos[in], s->n * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
     if (vel) GS_CUDA(cudaMemcpyAsync(vel, s->vel[in], s->n * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
     if (mass) GS_CUDA(cudaMemcpyAsync(mass, s->mass[in], s->n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
-    GS_CUDA(cudaStreamSynchronize(s->stream));
-    return GS_OK;
+    return sim_wait(s);
 }
 
 gs_status gs_set_particles(gs_sim* s, const float* pos, const float* vel, const float* mass) {
@@ -583,8 +608,8 @@ gs_status gs_get_accel(gs_sim* s, float* acc) {
     if (!s->acc) return invalid("gs_get_accel: create the simulation with GS_FLAG_RECORD_ACCEL");
     gs_status st = gs_sync(s, 0);
     if (st != GS_OK) return st;
-    GS_CUDA(cudaMemcpy(acc, s->acc, s->n * sizeof(float2), cudaMemcpyDeviceToHost));
-    return GS_OK;
+    GS_CUDA(cudaMemcpyAsync(acc, s->acc, s->n * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    return sim_wait(s);
 }
 
 gs_status gs_get_stats(gs_sim* s, gs_stats* out) {
@@ -614,6 +639,12 @@ gs_status gs_reset_stats(gs_sim* s) {
     return GS_OK;
 }
 
+gs_status gs_set_timeout(gs_sim* s, uint64_t timeout_ns) {
+    if (!s) return invalid("gs_set_timeout: sim is NULL");
+    s->timeout_ns = timeout_ns;
+    return GS_OK;
+}
+
 uint64_t gs_particle_count(const gs_sim* s) { return s ? s->n : 0; }
 uint64_t gs_aligned_particle_count(const gs_sim* s) { return s ? s->n_al : 0; }
 void* gs_stream(gs_sim* s) { return s ? (void*)s->stream : nullptr; }
@@ -639,9 +670,8 @@ gs_status gs_accel_f64(gs_sim* s, uint32_t n_targets, const uint32_t* targets, d
         e = cudaMemcpyAsync(acc, dout, n_targets * sizeof(double2), cudaMemcpyDeviceToHost, s->stream);
     if (dt) cudaFreeAsync(dt, s->stream);
     if (dout) cudaFreeAsync(dout, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     GS_CUDA(e);
-    return GS_OK;
+    return sim_wait(s);
 }
 
 gs_status gs_energy_f64(gs_sim* s, double* kinetic, double* potential) {
@@ -649,7 +679,24 @@ gs_status gs_energy_f64(gs_sim* s, double* kinetic, double* potential) {
     gs_status st = gs_sync(s, 0);
     if (st != GS_OK) return st;
     s->own_work = true;
-    GS_CUDA(energy_f64(s, kinetic, potential));
+    return energy_f64(s, kinetic, potential);
+}
+
+gs_status gs_debug_state(gs_sim* s, float* pos, float* vel, float* mass, float* amag) {
+    if (!s) return invalid("gs_debug_state: sim is NULL");
+    gs_status st = gs_sync(s, 0);
+    if (st != GS_OK) return st;
+    const int in = s->in;
+    const size_t n = s->n_al;
+    if (pos) GS_CUDA(cudaMemcpyAsync(pos, s->pos[in], n * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    if (vel) GS_CUDA(cudaMemcpyAsync(vel, s->vel[in], n * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    if (mass) GS_CUDA(cudaMemcpyAsync(mass, s->mass[in], n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    const float* d_amag = s->p.algorithm == GS_BARNES_HUT ? s->bh.amag : nullptr;
+    if (amag && d_amag) GS_CUDA(cudaMemcpyAsync(amag, d_amag, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    st = sim_wait(s);
+    if (st != GS_OK) return st;
+    if (amag && !d_amag)
+        for (size_t i = 0; i < n; ++i) amag[i] = std::nanf("");
     return GS_OK;
 }
 

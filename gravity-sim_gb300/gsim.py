@@ -32,6 +32,7 @@ EXPORTS = (
     "gs_server_submit", "gs_server_poll", "gs_server_request", "gs_server_result", "gs_server_get_stats",
     "gs_server_clock", "gs_server_run_trace", "gs_server_destroy", "gs_energy_f64", "gs_camera_start",
     "gs_render_points", "gs_snapshot_take", "gs_snapshot_positions", "gs_snapshot_render", "gs_write_ppm",
+    "gs_set_timeout", "gs_debug_state",
 )
 FLAG_PLAIN_SUM = 0x80
 FLAG_RELATIVE_MAC = 0x100
@@ -46,7 +47,7 @@ class Params(C.Structure):
                 ("simulation_speed", C.c_float), ("softening_len", C.c_float),
                 ("accuracy_parameter", C.c_float), ("algorithm", C.c_int32), ("box_mode", C.c_int32),
                 ("math_mode", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32),
-                ("relative_accuracy", C.c_float), ("relative_theta_floor", C.c_float)]
+                ("relative_accuracy", C.c_float), ("relative_theta_floor", C.c_float), ("key_bits", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -138,6 +139,10 @@ def lib():
     L.gs_stream.restype = C.c_void_p
     L.gs_destroy.argtypes = [sim]
     L.gs_destroy.restype = None
+    L.gs_set_timeout.argtypes = [sim, C.c_uint64]
+    L.gs_set_timeout.restype = st
+    L.gs_debug_state.argtypes = [sim, _FP, _FP, _FP, _FP]
+    L.gs_debug_state.restype = st
     L.gs_accel_f64.argtypes = [sim, C.c_uint32, _UP, _DP]
     L.gs_accel_f64.restype = st
     L.gs_debug_bh_tree.argtypes = [sim, _UP, _UP, _UP, _FP, _FP, _FP, _FP, C.c_uint64, C.POINTER(C.c_uint64)]
@@ -304,6 +309,10 @@ class Simulation:
     def sync(self, timeout_ns=0):
         _check(lib().gs_sync(self._h, timeout_ns))
 
+    def set_timeout(self, timeout_ns):
+        """Bound of every host wait of this system (0: 600 s)."""
+        _check(lib().gs_set_timeout(self._h, timeout_ns))
+
     def get_particles(self):
         pos = np.empty((self.n, 2), np.float32)
         vel = np.empty((self.n, 2), np.float32)
@@ -373,6 +382,17 @@ class Simulation:
         out = np.empty((len(t), 2), np.float64)
         _check(lib().gs_accel_f64(self._h, len(t), t.ctypes.data_as(_UP), out.ctypes.data_as(_DP)))
         return out
+
+    def padded_state(self):
+        """All N_al particles of the current state (padding included) and the |a| the next
+        relative-criterion step reads (NaN: unknown)."""
+        n_al = self.n_al
+        pos = np.empty((n_al, 2), np.float32)
+        vel = np.empty((n_al, 2), np.float32)
+        mass = np.empty(n_al, np.float32)
+        amag = np.empty(n_al, np.float32)
+        _check(lib().gs_debug_state(self._h, _fp(pos), _fp(vel), _fp(mass), _fp(amag)))
+        return pos, vel, mass, amag
 
     def bh_tree(self):
         n_al = self.n_al

@@ -55,7 +55,8 @@ typedef enum gs_algorithm { GS_DIRECT_SUM = 0, GS_BARNES_HUT = 1 } gs_algorithm;
 
 /* Barnes-Hut box: the reference's fixed +-500 box with a 1024x1024 finest grid and
  * removal of particles that leave it, or a per-step square bounding box with
- * 2^12 x 2^12 finest cells (24-bit keys) and no removal. */
+ * 2^k x 2^k finest cells (gs_params.key_bits = k: 12 by default, 24-bit Morton keys; 15
+ * gives 30-bit keys) and no removal. */
 typedef enum gs_box_mode { GS_BOX_FIXED_500 = 0, GS_BOX_BOUNDING = 1 } gs_box_mode;
 
 /* FAST: hardware rsqrt; direct sum in shared-memory tiles with Kahan-compensated
@@ -115,6 +116,9 @@ typedef struct gs_params {
     uint32_t flags;            /* GS_FLAG_* */
     float relative_accuracy;   /* alpha of GS_FLAG_RELATIVE_MAC, default 0.006 */
     float relative_theta_floor; /* theta floor of GS_FLAG_RELATIVE_MAC, default 0: accuracy_parameter */
+    int32_t key_bits;          /* GS_BOX_BOUNDING: Morton bits per axis, 1..15 (default 12: 24-bit keys
+                                  in 3 radix passes; 15: 30-bit keys in 4); 0 means 12.  The reference's
+                                  fixed box uses 10 (InitShader.comp:80-98) */
 } gs_params;
 
 typedef struct gs_sim gs_sim;
@@ -146,13 +150,25 @@ GS_API uint64_t gs_required_alignment(int32_t algorithm);
 GS_API gs_status gs_create(const gs_params* params, uint64_t particle_count, const float* pos_xy,
                     const float* vel_xy, const float* mass, gs_sim** out);
 /* Enqueue `count` steps.  Like RunSimulations it first waits for the previous gs_run
- * batch to finish (bounded: GS_ERR_TIMEOUT after 600 s), then submits and returns. */
+ * batch to finish (bounded: GS_ERR_TIMEOUT after the system's timeout), then submits and
+ * returns. */
 GS_API gs_status gs_run(gs_sim* sim, uint32_t count);
-/* Wait for all submitted steps; timeout_ns = 0 waits up to 600 s. */
+/* Wait for all submitted steps; timeout_ns = 0 uses the system's timeout. */
 GS_API gs_status gs_sync(gs_sim* sim, uint64_t timeout_ns);
-/* Copy the current state (first N particles) to host arrays; any may be NULL. */
+/* Bound of every host wait this system makes (gs_run, gs_sync with 0, the particle
+ * transfers, readbacks): GS_ERR_TIMEOUT after timeout_ns nanoseconds; 0 (the default)
+ * means 600 s.  No counterpart in the reference, whose fence waits do not time out. */
+GS_API gs_status gs_set_timeout(gs_sim* sim, uint64_t timeout_ns);
+/* Copy the current state (first N particles) to host arrays; any may be NULL.  Pinned
+ * (page-locked or registered) arrays are written in place by a kernel queued behind the
+ * submitted steps.  If the wait for it times out (GS_ERR_TIMEOUT), that kernel may still
+ * write them later: keep the arrays alive and untouched until gs_sync returns GS_OK. */
 GS_API gs_status gs_get_particles(gs_sim* sim, float* pos_xy, float* vel_xy, float* mass);
-/* Replace the whole state (first N particles; padding reset to zero particles). */
+/* Replace the whole state (first N particles; padding reset to zero particles).  Pinned
+ * arrays are read in place by a kernel queued behind the submitted steps; the call
+ * returns once they have been read, except after GS_ERR_TIMEOUT, when they stay in use
+ * until gs_sync returns GS_OK.  A device error raised by steps submitted before this call
+ * is returned by it (GS_ERR_DEVICE) after the upload has replaced the state. */
 GS_API gs_status gs_set_particles(gs_sim* sim, const float* pos_xy, const float* vel_xy,
                            const float* mass);
 /* Accelerations (without G) of the last step, in particle order; needs GS_FLAG_RECORD_ACCEL. */
@@ -183,9 +199,15 @@ GS_API gs_status gs_debug_bh_tree(gs_sim* sim, uint32_t* keys, uint32_t* sorted_
                            uint32_t* node_skip, float* node_radius, float* node_pos,
                            float* node_mass, float* node_quad, uint64_t capacity,
                            uint64_t* tree_records);
+/* The whole current state, padding included: N_al = gs_aligned_particle_count particles
+ * (zero-mass padding particles move under the field like the reference's), and the |a|
+ * per particle that the relative opening criterion of the next step reads (NaN where
+ * unknown or without GS_FLAG_RELATIVE_MAC).  Any pointer may be NULL.  Diagnostic: it lets
+ * a checker restart a CPU restatement from the device's exact state at any step. */
+GS_API gs_status gs_debug_state(gs_sim* sim, float* pos_xy, float* vel_xy, float* mass, float* amag);
 /* Records the tree of aligned_count particles can hold: the leaves plus, for every level
- * d of the box mode (0..10 fixed box, 0..12 bounding box), min(4^d, aligned_count/2 + 1)
- * internal nodes, plus 64. */
+ * d of the box mode (0..10 fixed box, 0..15 bounding box: any key_bits), min(4^d,
+ * aligned_count/2 + 1) internal nodes, plus 64. */
 GS_API uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count);
 
 /* One direct-sum step (FAST math) on caller-owned device buffers, allocating nothing.
@@ -201,8 +223,9 @@ GS_API uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count);
  *   - Runs on the calling thread's current device, on `stream` (a cudaStream_t, NULL for
  *     the legacy default stream), asynchronously.
  *   - Scratch lives in fixed device arrays inside this library (about 4 MiB per GPU that
- *     loads it, held until the process exits).  The first call on each device looks up
- *     their device addresses; make that first call before any stream capture.
+ *     loads it, held until the process exits).  Every call looks up their device
+ *     addresses in the current context (no allocation); the first call on a device also
+ *     loads the library's module there, so make it before any stream capture.
  *   - Every call shares those arrays: calls that overlap on the GPU (other streams,
  *     other threads) race and give wrong results.  Serialise them on one stream. */
 #define GS_NOALLOC_MAX_PARTICLES 65536

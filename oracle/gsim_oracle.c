@@ -36,7 +36,8 @@
 #define SIM_SIZE 500.0f  /* BarnesHutSimulation.cpp:580 simulationSize */
 #define GRID 1024u       /* BarnesHutSimulation.cpp:582 treeSize */
 #define GRID_LEVELS 11   /* depths 0..10 */
-#define BBOX_BITS 12     /* bounding-box mode: 12 bits per axis, 24-bit keys */
+#define BBOX_BITS 12     /* bounding-box mode default: 12 bits per axis, 24-bit keys */
+#define BBOX_MAX_BITS 15 /* bounding-box mode maximum: 15 bits per axis, 30-bit keys */
 
 /* ------------------------------------------------------------------------------ */
 /* tiny parallel-for: dynamic chunks over [0, n), deterministic results because   */
@@ -307,41 +308,44 @@ static inline int fixed_box_key(float px, float py, uint32_t* key) {
 
 typedef struct {
     float cx, cy, scale, radius0, inv_scale;
+    int bits; /* cells per axis: 2^bits */
 } bbox_params;
 
-/* Bounding-box mode: square box around min/max of all positions, 2^15 cells per axis. */
-static bbox_params bbox_from_minmax(double minx, double maxx, double miny, double maxy) {
+/* Bounding-box mode: square box around min/max of all positions (1/1024 margin),
+ * 2^bits cells per axis (bits 12: 24-bit keys, 15: 30-bit keys). */
+static bbox_params bbox_from_minmax(double minx, double maxx, double miny, double maxy, int bits) {
     bbox_params b;
+    b.bits = bits;
     double cx = 0.5 * (minx + maxx), cy = 0.5 * (miny + maxy);
     double ext = maxx - minx > maxy - miny ? maxx - minx : maxy - miny;
     if (!(ext > 0.0) || !isfinite(ext)) ext = 1.0;
     if (!isfinite(cx)) cx = 0.0;
     if (!isfinite(cy)) cy = 0.0;
     double half = ext * 0.5 * (1.0 + 1.0 / 1024.0);
-    double scale = (double)(1u << (BBOX_BITS - 1)) / half;
+    double scale = (double)(1u << (bits - 1)) / half;
     b.cx = (float)cx;
     b.cy = (float)cy;
     b.scale = (float)scale;
-    double side0 = (double)(1u << BBOX_BITS) / (double)b.scale;
+    double side0 = (double)(1u << bits) / (double)b.scale;
     b.radius0 = (float)(side0 * side0 * 0.5);
     b.inv_scale = (float)(1.0 / (double)b.scale);
     return b;
 }
 
-static inline uint32_t bbox_cell(float p, float c, float scale) {
-    float t = (p - c) * scale + (float)(1u << (BBOX_BITS - 1));
+static inline uint32_t bbox_cell(float p, float c, float scale, int bits) {
+    float t = (p - c) * scale + (float)(1u << (bits - 1));
     if (!(t >= 0.0f)) return 0;
-    if (t >= (float)((1u << BBOX_BITS) - 1)) return (1u << BBOX_BITS) - 1;
+    if (t >= (float)((1u << bits) - 1)) return (1u << bits) - 1;
     return (uint32_t)t;
 }
 
 static inline uint32_t bbox_key(float px, float py, const bbox_params* b) {
-    return spread_bits(bbox_cell(px, b->cx, b->scale)) |
-           (spread_bits(bbox_cell(py, b->cy, b->scale)) << 1);
+    return spread_bits(bbox_cell(px, b->cx, b->scale, b->bits)) |
+           (spread_bits(bbox_cell(py, b->cy, b->scale, b->bits)) << 1);
 }
 
 uint64_t orc_bh_node_capacity(int box_mode, uint32_t n_al) {
-    uint64_t levels = box_mode == ORC_BOX_BOUNDING ? BBOX_BITS + 1 : GRID_LEVELS;
+    uint64_t levels = box_mode == ORC_BOX_BOUNDING ? BBOX_MAX_BITS + 1 : GRID_LEVELS;
     return (uint64_t)n_al + levels * (uint64_t)(n_al / 2) + 64;
 }
 
@@ -908,7 +912,9 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
                           float* mass_in, float* pos_out, float* vel_out, float* mass_out,
                           float dt, float G, float eps2, float theta2, orc_bh_out* out,
                           int nthreads) {
-    const int D = box_mode == ORC_BOX_BOUNDING ? BBOX_BITS : GRID_LEVELS - 1;
+    int bits = out && out->key_bits ? (int)out->key_bits : BBOX_BITS;
+    if (bits < 1 || bits > BBOX_MAX_BITS) return -1;
+    const int D = box_mode == ORC_BOX_BOUNDING ? bits : GRID_LEVELS - 1;
     const int key_bits = 2 * D;
     const double t_build = now_seconds();
     uint32_t* key = (uint32_t*)malloc((size_t)n_al * sizeof(uint32_t));
@@ -916,7 +922,7 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
     uint32_t* sidx = (uint32_t*)malloc((size_t)n_al * sizeof(uint32_t));
     float radius0;
     bbox_params bp = {0.0f, 0.0f, (float)GRID / (2.0f * SIM_SIZE), SIM_SIZE * SIM_SIZE * 2.0f,
-                      2.0f * SIM_SIZE / (float)GRID};
+                      2.0f * SIM_SIZE / (float)GRID, 10};
 
     if (box_mode == ORC_BOX_BOUNDING) {
         double mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
@@ -927,7 +933,7 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
             if (y < mny) mny = y;
             if (y > mxy) mxy = y;
         }
-        bp = bbox_from_minmax(mnx, mxx, mny, mxy);
+        bp = bbox_from_minmax(mnx, mxx, mny, mxy, bits);
         for (uint32_t i = 0; i < n_al; ++i) key[i] = bbox_key(pos_in[2 * i], pos_in[2 * i + 1], &bp);
         radius0 = bp.radius0;
     } else {

@@ -76,6 +76,8 @@ typedef struct orc_bh_out {
     float rel_floor2;        /* squared theta floor of the relative criterion */
     const float* amag_in;    /* [n_al] |a| of the previous step per particle (NaN: unknown) */
     float* amag_out;         /* [n_al] |a| of this step (written when not NULL) */
+    /* input of the bounding-box mode */
+    uint32_t key_bits;       /* bits per axis, 1..15 (0: 12, 24-bit keys; 15: 30-bit keys) */
 } orc_bh_out;
 
 /* Direct sum, SimShader.comp order: for every i, sum j = 0 .. n-1 in order. */

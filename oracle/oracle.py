@@ -32,7 +32,8 @@ class BHOut(C.Structure):
                 ("box_center_x", C.c_float), ("box_center_y", C.c_float), ("box_scale", C.c_float),
                 ("box_radius0", C.c_float), ("build_seconds", C.c_double), ("walk_seconds", C.c_double),
                 ("max_stack", C.c_uint32), ("max_warp_interactions", C.c_uint64),
-                ("rel_alpha", C.c_float), ("rel_floor2", C.c_float), ("amag_in", _FP), ("amag_out", _FP)]
+                ("rel_alpha", C.c_float), ("rel_floor2", C.c_float), ("amag_in", _FP), ("amag_out", _FP),
+                ("key_bits", C.c_uint32)]
 
 
 _lib = None
@@ -142,15 +143,21 @@ def direct_accel_f64(pos, mass, softening=0.2, targets=None, threads=os.cpu_coun
 
 
 def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, G=1.0, softening=0.2, theta=1.0,
-            keep_tree=True, threads=os.cpu_count(), walk_stride=1, flags=0, rel_alpha=0.0, rel_floor=None):
-    """One Barnes-Hut step; returns a dict with keys, sorted_src and the preorder records."""
+            keep_tree=True, threads=os.cpu_count(), walk_stride=1, flags=0, rel_alpha=0.0, rel_floor=None,
+            key_bits=0, amag_in=None):
+    """One Barnes-Hut step; returns a dict with keys, sorted_src and the preorder records.
+    key_bits: bounding-box cells per axis as a power of two (0: 12).  amag_in: the previous
+    |a| per particle to use instead of the state's own (relative criterion)."""
     (pi, vi, mi), (po, vo, mo) = state.sets()
     n_al = state.n_al
     L = lib()
     cap = int(L.orc_bh_node_capacity(box_mode, n_al))
     out = BHOut()
     out.walk_stride = walk_stride
+    out.key_bits = key_bits
     amag_out = None
+    if amag_in is not None:
+        state.amag = np.ascontiguousarray(amag_in, np.float32).copy()
     if flags & RELATIVE_MAC:  # |a| of this step; particles the walk skips keep their value
         amag_out = state.amag.copy()
         out.rel_alpha = rel_alpha
@@ -180,8 +187,9 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
         L.orc_bh_grid_step(n_al, _fp(pi), _fp(vi), _fp(mi), _fp(po), _fp(vo), _fp(mo), dt_eff, G, eps2, th2,
                            C.byref(out), threads)
     else:
-        L.orc_bh_sorted_step_ex(box_mode, flags, n_al, _fp(pi), _fp(vi), _fp(mi), _fp(po), _fp(vo), _fp(mo),
-                                dt_eff, G, eps2, th2, C.byref(out), threads)
+        if L.orc_bh_sorted_step_ex(box_mode, flags, n_al, _fp(pi), _fp(vi), _fp(mi), _fp(po), _fp(vo), _fp(mo),
+                                   dt_eff, G, eps2, th2, C.byref(out), threads) != 0:
+            raise ValueError("orc_bh_sorted_step_ex rejected its arguments")
     state.flip()
     if amag_out is not None:
         state.amag = amag_out

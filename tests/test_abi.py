@@ -31,8 +31,8 @@ def test_exports_every_declared_symbol(gs):
 def test_alignment_and_capacity(gs):
     assert gs.required_alignment(gs.DIRECT_SUM) == 64
     assert gs.required_alignment(gs.BARNES_HUT) == 64
-    # leaves + at most min(4^d, n/2 + 1) internal nodes per level d (levels 0..10 / 0..12) + 64
-    for box, depth in ((gs.BOX_FIXED_500, 10), (gs.BOX_BOUNDING, 12)):
+    # leaves + at most min(4^d, n/2 + 1) internal nodes per level d (levels 0..10 / 0..15) + 64
+    for box, depth in ((gs.BOX_FIXED_500, 10), (gs.BOX_BOUNDING, 15)):
         for n in (64, 640, 1 << 20):
             levels = sum(min(4 ** d, n // 2 + 1) for d in range(depth + 1))
             assert gs.node_capacity(box, n) == n + levels + 64
@@ -109,3 +109,16 @@ def test_fails_loudly_without_gpu(gs):
     with pytest.raises(gs.GsimError) as e:
         gs.Simulation(p, v, m)
     assert e.value.status == 8  # GS_ERR_NO_DEVICE: no CPU fallback
+
+
+def test_create_rejects_bad_key_bits_before_any_device_call(gs):
+    """Parameter validation comes first: an out-of-range key width is refused with
+    GS_ERR_INVALID_ARGUMENT whether or not a GPU is present."""
+    pos = np.zeros((64, 2), np.float32)
+    mass = np.ones(64, np.float32)
+    for bits in (-1, 16):
+        p = gs.default_params(algorithm=gs.BARNES_HUT, box_mode=gs.BOX_BOUNDING, key_bits=bits)
+        h = ctypes.c_void_p()
+        st = gs.lib().gs_create(ctypes.byref(p), 64, gs._fp(pos), gs._fp(pos), gs._fp(mass), ctypes.byref(h))
+        assert st == 1 and not h.value
+        assert b"key_bits" in gs.lib().gs_last_error()

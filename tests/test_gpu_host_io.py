@@ -81,3 +81,41 @@ def test_pinned_readback_matches_pageable(gs, offset):
         _get_into(gs, sim, hp, None, None)
         assert np.array_equal(hp.view(np.uint32), p.view(np.uint32))
         assert np.all(np.isnan(hm))
+
+
+def test_timeout_leaves_pinned_arrays_in_use(gs):
+    """A transfer whose bounded wait runs out returns GS_ERR_TIMEOUT with its kernel still
+    queued behind the submitted steps; the pinned arrays stay in use until gs_sync
+    succeeds, and then hold what the call promised (include/gsim.h)."""
+    torch = pytest.importorskip("torch")
+    n = 131072  # direct sum: about 7 ms per step, so 20 steps outlast a 1 ms bound
+    pos, vel, mass = gs.generate(gs.GEN_UNIFORM_DISK, n, size=100.0, seed=21)
+    with gs.Simulation(pos, vel, mass, algorithm=gs.DIRECT_SUM) as sim, \
+            gs.Simulation(pos, vel, mass, algorithm=gs.DIRECT_SUM) as ref:
+        ref.run(20)
+        want = _words(ref)
+        hp = _pinned(torch, np.full((n, 2), np.nan, np.float32))
+        hv = _pinned(torch, np.full((n, 2), np.nan, np.float32))
+        hm = _pinned(torch, np.full(n, np.nan, np.float32))
+        sim.run(20)
+        sim.set_timeout(1000000)  # 1 ms
+        st = gs.lib().gs_get_particles(sim.handle, gs._fp(hp), gs._fp(hv), gs._fp(hm))
+        assert st == 4  # GS_ERR_TIMEOUT: the steps are still running
+        sim.set_timeout(0)
+        sim.sync()
+        got = np.concatenate([hp.ravel(), hv.ravel(), hm.ravel()]).view(np.uint32)
+        assert np.array_equal(got, want)  # the queued readback wrote them after the steps
+
+        # an upload behind running steps: after the timeout and a successful sync, the
+        # state is the uploaded one
+        p2, v2, m2 = gs.generate(gs.GEN_SPIRAL, n, size=100.0, seed=22)
+        sim.run(20)
+        up = [_pinned(torch, a) for a in (p2, v2, m2)]  # in use until the sync below
+        sim.set_timeout(1000000)
+        st = gs.lib().gs_set_particles(sim.handle, *[gs._fp(a) for a in up])
+        assert st == 4
+        sim.set_timeout(0)
+        sim.sync()
+        del up
+        p, v, m = sim.get_particles()
+        assert np.array_equal(p, p2) and np.array_equal(v, v2) and np.array_equal(m, m2)

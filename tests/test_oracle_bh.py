@@ -198,3 +198,27 @@ def test_relative_criterion_alpha_zero_is_direct_sum(gs, orc):
     orc.bh_step(a, box_mode=orc.BOX_BOUNDING, theta=0.0, flags=flags, rel_alpha=0.0)
     orc.direct_step(b)
     np.testing.assert_allclose(a.current()[1], b.current()[1], rtol=2e-4, atol=1e-4 * np.abs(b.current()[1]).max())
+
+
+@pytest.mark.parametrize("kind,n", [(17, 5000), (2, 3000), (16, 64)])
+def test_key_bits_refine(gs, orc, kind, n):
+    """Bounding-box keys of 15 bits per axis (30-bit Morton codes) refine the 12-bit cells
+    of the same box: the scale is 8x the 12-bit one exactly, so key15 >> 6 == key12 for
+    every particle, and the deeper tree keeps every structural invariant."""
+    pos, vel, mass = gs.generate(kind, n, size=100.0, seed=9)
+    r12 = orc.bh_step(orc.State(pos, vel, mass), box_mode=orc.BOX_BOUNDING, key_bits=12)
+    r15 = orc.bh_step(orc.State(pos, vel, mass), box_mode=orc.BOX_BOUNDING, key_bits=15)
+    assert r15["box"][:2] == r12["box"][:2]
+    assert np.array_equal(r15["keys"] >> 6, r12["keys"])
+    assert np.all(r15["keys"] < (1 << 30))
+    keys = r15["keys"][r15["sorted_src"][: r15["valid_count"]]]
+    assert np.all(np.diff(keys.astype(np.int64)) >= 0)
+    check_tree(r15, r15["box"][3], r15["valid_count"])
+    assert r15["tree_size"] >= r12["tree_size"]
+
+
+def test_key_bits_out_of_range(orc):
+    pos = np.zeros((64, 2), np.float32)
+    for bits in (16, 40):
+        with pytest.raises(ValueError):
+            orc.bh_step(orc.State(pos, pos, np.ones(64, np.float32)), box_mode=orc.BOX_BOUNDING, key_bits=bits)
