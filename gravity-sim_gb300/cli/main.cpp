@@ -55,7 +55,8 @@ const char* kHelp =
     "\t--benchmark: Reports the wall-clock runtime of all simulations.\n"
     "\t--accurate: Barnes-Hut accurate mode (quadrupoles, safe opening radius, group walk).\n"
     "\t--relative-accuracy: With --accurate, open nodes by the relative criterion with this alpha\n"
-    "\t\t(0.006 with floor 0.3 and accuracy parameter 0.35: about 1e-3 RMS force error).\n"
+    "\t\t(0.006 with floor 0.2: below 1e-3 RMS force error; the accuracy parameter then sets\n"
+    "\t\tthe walk that estimates |a| for a step without a previous one, 1 is enough).\n"
     "\t--relative-floor: The theta floor of that criterion, defaulted to the accuracy parameter.\n";
 
 struct Logger {

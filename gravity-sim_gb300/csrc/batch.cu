@@ -201,14 +201,20 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
     return GS_OK;
 }
 
-cudaError_t BatchEngine::enqueue(uint32_t par) {
+bool BatchEngine::needs_estimate() const {
+    for (const gs_sim* s : order)
+        if (s->p.algorithm == GS_BARNES_HUT && (s->p.flags & GS_FLAG_RELATIVE_MAC) && !s->amag_known) return true;
+    return false;
+}
+
+cudaError_t BatchEngine::enqueue(uint32_t par, bool estimate) {
     const bool both = plan.n_bh && plan.n_direct;
     cudaError_t e = cudaSuccess;
     if (both) {
         e = cudaEventRecord(fork, root);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
     }
-    if (e == cudaSuccess) e = bh_batch_step(plan, par, root);
+    if (e == cudaSuccess) e = bh_batch_step(plan, par, root, estimate);
     if (e == cudaSuccess) e = direct_batch_step(plan, par, both ? side : root);
     if (both) {
         if (e == cudaSuccess) e = cudaEventRecord(join, side);
@@ -222,6 +228,7 @@ void BatchEngine::advance() {
     for (gs_sim* s : order) {
         s->in ^= 1;  // NextComputeIndices
         ++s->steps_done;
+        s->amag_known = true;
     }
 }
 
@@ -233,7 +240,8 @@ bool BatchEngine::in_step() const {
 
 uint32_t BatchEngine::launches_per_step() const {
     uint32_t k = 0;
-    if (plan.n_bh)  // clear keys scan records nodes force, radix passes, box, moment levels
+    if (plan.n_bh)  // clear keys scan records nodes force, radix passes, box, moment levels (the
+                    // |a| estimate pass of a step after a member joined or was reset not included)
         k += 6u + (uint32_t)plan.passes + (plan.bbox ? 1u : 0u) + (uint32_t)(plan.depth - kLevelTop + 1);
     if (plan.n_direct) k += 1u;
     return k;
@@ -249,7 +257,7 @@ struct gs_batch {
     BatchEngine eng;
     std::vector<cudaEvent_t> member_ev;  // orders the batch after each member's own work
     cudaEvent_t done = nullptr;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};  // [parity], [2 + parity] with the estimate
     bool pending = false;
 };
 
@@ -341,24 +349,26 @@ gs_status gs_batch_run(gs_batch* b, uint32_t steps) {
     const bool graphs = !(b->flags & GS_BATCH_NO_GRAPH);
     for (uint32_t c = 0; c < steps; ++c) {
         const uint32_t par = (uint32_t)(b->eng.step & 1);
+        const bool est = b->eng.needs_estimate();
+        const uint32_t gi = par + (est ? 2u : 0u);
         if (graphs) {
-            if (!b->graph[par]) {
+            if (!b->graph[gi]) {
                 cudaGraph_t g = nullptr;
                 GS_CUDA(cudaStreamBeginCapture(b->eng.root, cudaStreamCaptureModeThreadLocal));
-                cudaError_t e = b->eng.enqueue(par);
+                cudaError_t e = b->eng.enqueue(par, est);
                 cudaError_t e2 = cudaStreamEndCapture(b->eng.root, &g);
                 if (e != cudaSuccess) {
                     if (g) cudaGraphDestroy(g);
                     return cuda_fail(e, "gs_batch_run capture");
                 }
                 GS_CUDA(e2);
-                e = cudaGraphInstantiate(&b->graph[par], g, 0);
+                e = cudaGraphInstantiate(&b->graph[gi], g, 0);
                 cudaGraphDestroy(g);
                 GS_CUDA(e);
             }
-            GS_CUDA(cudaGraphLaunch(b->graph[par], b->eng.root));
+            GS_CUDA(cudaGraphLaunch(b->graph[gi], b->eng.root));
         } else {
-            GS_CUDA(b->eng.enqueue(par));
+            GS_CUDA(b->eng.enqueue(par, est));
         }
         b->eng.advance();
     }

@@ -31,9 +31,12 @@ struct BatchEngine {
     void destroy();
     // Plans `members` (any order; may be empty) with their current parities.
     gs_status set_members(const std::vector<gs_sim*>& members);
-    // Enqueues one batched step for step parity `par` (no host bookkeeping).
-    cudaError_t enqueue(uint32_t par);
-    // Host bookkeeping of one enqueued step: member parities flip.
+    // Enqueues one batched step for step parity `par` (no host bookkeeping); `estimate`
+    // adds the |a| estimate pass for members without a previous |a|.
+    cudaError_t enqueue(uint32_t par, bool estimate);
+    // A member has no previous |a| for the relative criterion (it joined or was reset).
+    bool needs_estimate() const;
+    // Host bookkeeping of one enqueued step: member parities flip, |a| becomes known.
     void advance();
     // True while every member is at the parity the plan expects.
     bool in_step() const;

@@ -1276,7 +1276,11 @@ __device__ __forceinline__ void eval_leaves(GroupSmem& g, uint32_t n_items, cons
     }
 }
 
-template <bool EXACT, bool QUAD, bool COUNT>
+// ESTIMATE: the |a| estimate pass of the relative criterion.  A group whose particles all
+// have a previous |a| returns at once; any other group walks with the theta test and
+// writes only the |a| of its particles (no integration), which the following normal pass
+// then opens nodes by.
+template <bool EXACT, bool QUAD, bool COUNT, bool ESTIMATE>
 __device__ __forceinline__ void force_group_body(
     Blk blk, GroupSmem& g, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ skey,
     const uint32_t* __restrict__ counts, const float4* __restrict__ rec, const uint32_t* __restrict__ skip,
@@ -1291,6 +1295,7 @@ __device__ __forceinline__ void force_group_body(
     const uint32_t T = min(nv + counts[1], cap);
     const uint32_t g0 = group * kGroupSize;
     if (g0 >= nv || T == 0) return;
+    if (ESTIMATE && !amag) return;  // a batch member without the relative criterion
     // particles: slot g0 + lane (.x of every pair) and g0 + 32 + lane (.y)
     const uint32_t s0 = g0 + lane, s1 = s0 + 32;
     const uint32_t i0 = s0 < nv ? sidx[s0] : 0u, i1 = s1 < nv ? sidx[s1] : 0u;
@@ -1331,9 +1336,10 @@ __device__ __forceinline__ void force_group_body(
     if (amag) {
         const float a0 = v0 ? amag[i0] : INFINITY, a1 = v1 ? amag[i1] : INFINITY;
         const bool unknown = __any_sync(0xffffffffu, isnan(a0) || isnan(a1));
+        if (ESTIMATE && !unknown) return;  // warp-uniform: nothing to estimate
         float amin = fminf(a0, a1);
         for (int o = 16; o; o >>= 1) amin = fminf(amin, __shfl_xor_sync(0xffffffffu, amin, o));
-        relative = !unknown;
+        relative = !ESTIMATE && !unknown;
         const float tol = alpha * amin;
         tol2 = tol * tol;
     }
@@ -1479,6 +1485,7 @@ __device__ __forceinline__ void force_group_body(
         if (v0) amag[i0] = __fsqrt_rn(fmaf(ax.x, ax.x, ay.x * ay.x));
         if (v1) amag[i1] = __fsqrt_rn(fmaf(ax.y, ax.y, ay.y * ay.y));
     }
+    if (ESTIMATE) return;
     float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;  // of the new positions
     if (v0) {
         if (acc_rec) acc_rec[i0] = make_float2(ax.x, ay.x);
@@ -1507,7 +1514,7 @@ __device__ __forceinline__ void force_group_body(
     if (ext) ext_add(ext, mnx, mxx, mny, mxy);  // bounding-box mode: the next step's box
 }
 
-template <bool EXACT, bool QUAD, bool COUNT>
+template <bool EXACT, bool QUAD, bool COUNT, bool ESTIMATE>
 __global__ void __launch_bounds__(kGroupWarps * 32)
 k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ counts,
               const float4* __restrict__ rec, const uint32_t* __restrict__ skip, const float4* __restrict__ quad,
@@ -1518,9 +1525,23 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
               float floor2, uint32_t* __restrict__ ext) {
     pdl_enter();
     __shared__ GroupSmem smem[kGroupWarps];
-    force_group_body<EXACT, QUAD, COUNT>(grid_blk(), smem[threadIdx.x >> 5], sidx, skey, counts, rec, skip, quad,
-                                         kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2, theta2, k, hdt,
-                                         cap, stat, err, amag, alpha, floor2, ext);
+    force_group_body<EXACT, QUAD, COUNT, ESTIMATE>(grid_blk(), smem[threadIdx.x >> 5], sidx, skey, counts, rec, skip,
+                                                   quad, kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2,
+                                                   theta2, k, hdt, cap, stat, err, amag, alpha, floor2, ext);
+}
+
+// The group-walk kernel of a math mode / moments / counting / estimate combination (the
+// estimate pass exists only with quadrupoles, which the relative criterion needs).
+template <bool EST>
+auto force_group_kernel(bool exact, bool quad, bool count) {
+    if (EST) {
+        return exact ? (count ? k_force_group<true, true, true, EST> : k_force_group<true, true, false, EST>)
+                     : (count ? k_force_group<false, true, true, EST> : k_force_group<false, true, false, EST>);
+    }
+    return exact ? (quad ? (count ? k_force_group<true, true, true, EST> : k_force_group<true, true, false, EST>)
+                         : (count ? k_force_group<true, false, true, EST> : k_force_group<true, false, false, EST>))
+                 : (quad ? (count ? k_force_group<false, true, true, EST> : k_force_group<false, true, false, EST>)
+                         : (count ? k_force_group<false, false, true, EST> : k_force_group<false, false, false, EST>));
 }
 
 __global__ void k_set_params(BHParams* __restrict__ out, BHParams v) { *out = v; }
@@ -1670,7 +1691,7 @@ cudaError_t launch_coop(bool pdl, void (*kernel)(KArgs...), int grid, int block,
         if (_e != cudaSuccess) return _e;      \
     } while (0)
 
-cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
+cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
     BHWork& w = s->bh;
     cudaStream_t st = s->stream;
     const uint32_t n = (uint32_t)s->n_al;
@@ -1750,12 +1771,20 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile) {
     const bool fpdl = next_pdl();
     if (s->p.flags & GS_FLAG_GROUP_WALK) {
         const bool quad = w.quad != nullptr;
-        auto fn = exact ? (quad ? (count ? k_force_group<true, true, true> : k_force_group<true, true, false>)
-                                : (count ? k_force_group<true, false, true> : k_force_group<true, false, false>))
-                        : (quad ? (count ? k_force_group<false, true, true> : k_force_group<false, true, false>)
-                                : (count ? k_force_group<false, false, true> : k_force_group<false, false, false>));
         const int blocks = (int)((n / kGroupSize + kGroupWarps - 1) / kGroupWarps);
-        GS_TRY_LAUNCH(launch(fpdl, fn, blocks, kGroupWarps * 32, st, sidx, skey, (const uint32_t*)(ctr + kCtrValid),
+        bool npdl = fpdl;
+        if (estimate && w.amag && quad) {  // |a| of groups that have none, by the theta test
+            GS_TRY_LAUNCH(launch(fpdl, force_group_kernel<true>(exact, quad, count), blocks, kGroupWarps * 32, st,
+                                 sidx, skey, (const uint32_t*)(ctr + kCtrValid), (const float4*)w.rec,
+                                 (const uint32_t*)w.skip, (const float4*)w.quad, (const uint4*)w.kids,
+                                 (const float2*)s->pos[in], (const float2*)s->vel[in], s->pos[out], s->vel[out],
+                                 (float2*)nullptr, n, s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err,
+                                 w.amag, s->p.relative_accuracy, s->floor2, (uint32_t*)nullptr));
+            count_launch(s);
+            npdl = pdl;
+        }
+        auto fn = force_group_kernel<false>(exact, quad, count);
+        GS_TRY_LAUNCH(launch(npdl, fn, blocks, kGroupWarps * 32, st, sidx, skey, (const uint32_t*)(ctr + kCtrValid),
                              (const float4*)w.rec, (const uint32_t*)w.skip, (const float4*)w.quad,
                              (const uint4*)w.kids, (const float2*)s->pos[in], (const float2*)s->vel[in], s->pos[out],
                              s->vel[out], s->acc, n, s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err,
@@ -1998,7 +2027,7 @@ __global__ void __launch_bounds__(512) kb_top_sums(BatchArgs a) {
                         d.nodeinfo, d.msum, d.quad, d.safe, d.bbox, d.params);
 }
 
-template <bool EXACT, bool QUAD, bool COUNT>
+template <bool EXACT, bool QUAD, bool COUNT, bool ESTIMATE>
 __global__ void __launch_bounds__(kGroupWarps * 32) kb_force_group(BatchArgs a, uint32_t* __restrict__ work) {
     pdl_enter();
     __shared__ GroupSmem smem[kGroupWarps];
@@ -2013,7 +2042,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32) kb_force_group(BatchArgs a, 
         const BatchBlock bb = batch_block(a, b);
         const SysDesc& d = *bb.d;
         const int f = d.passes & 1;
-        force_group_body<EXACT, QUAD, COUNT>(bb.blk, smem[threadIdx.x >> 5], d.idx[f], d.keys[f],
+        force_group_body<EXACT, QUAD, COUNT, ESTIMATE>(bb.blk, smem[threadIdx.x >> 5], d.idx[f], d.keys[f],
                                              d.counters + kCtrValid, d.rec, d.skip, d.quad, d.kids, d.pos[bb.in],
                                              d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2,
                                              d.theta2, d.k, d.hdt, d.cap,
@@ -2099,22 +2128,28 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
     blocks[kTabForce] = (uint32_t)((n + per_block - 1) / per_block);
 }
 
+namespace {
+template <bool EST>
+auto batch_force_group_kernel(bool exact, bool quad, bool count) {
+    if (EST) {
+        return exact ? (count ? kb_force_group<true, true, true, EST> : kb_force_group<true, true, false, EST>)
+                     : (count ? kb_force_group<false, true, true, EST> : kb_force_group<false, true, false, EST>);
+    }
+    return exact ? (quad ? (count ? kb_force_group<true, true, true, EST> : kb_force_group<true, true, false, EST>)
+                         : (count ? kb_force_group<true, false, true, EST> : kb_force_group<true, false, false, EST>))
+                 : (quad ? (count ? kb_force_group<false, true, true, EST> : kb_force_group<false, true, false, EST>)
+                         : (count ? kb_force_group<false, false, true, EST> : kb_force_group<false, false, false, EST>));
+}
+}  // namespace
+
 int bh_batch_force_grid(const BatchPlan& p) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaError_t e;
     if (p.group) {
-        if (p.exact)
-            e = p.quad ? (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<true, true, true>, kGroupWarps * 32, 0)
-                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<true, true, false>, kGroupWarps * 32, 0))
-                       : (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<true, false, true>, kGroupWarps * 32, 0)
-                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<true, false, false>, kGroupWarps * 32, 0));
-        else
-            e = p.quad ? (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<false, true, true>, kGroupWarps * 32, 0)
-                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<false, true, false>, kGroupWarps * 32, 0))
-                       : (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<false, false, true>, kGroupWarps * 32, 0)
-                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force_group<false, false, false>, kGroupWarps * 32, 0));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_force_group_kernel<false>(p.exact, p.quad, p.count),
+                                                          kGroupWarps * 32, 0);
     } else {
         e = p.exact ? (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<true, true>, kForceWarps * 32, 0)
                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<true, false>, kForceWarps * 32, 0))
@@ -2126,7 +2161,7 @@ int bh_batch_force_grid(const BatchPlan& p) {
     return sms * per_sm;
 }
 
-cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st) {
+cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bool estimate) {
     if (!p.n_bh) return cudaSuccess;
     auto args = [&](int tab) { return BatchArgs{p.d_descs, p.d_tab[tab], p.n_bh, step}; };
     // the clear follows whatever the stream did before; every later stage overlaps its
@@ -2147,12 +2182,11 @@ cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st) {
                          args(kTabOne)));
     const int fg = p.force_grid < (int)p.total[kTabForce] ? p.force_grid : (int)p.total[kTabForce];
     if (p.group) {
-        auto fn = p.exact ? (p.quad ? (p.count ? kb_force_group<true, true, true> : kb_force_group<true, true, false>)
-                                    : (p.count ? kb_force_group<true, false, true> : kb_force_group<true, false, false>))
-                          : (p.quad ? (p.count ? kb_force_group<false, true, true> : kb_force_group<false, true, false>)
-                                    : (p.count ? kb_force_group<false, false, true>
-                                               : kb_force_group<false, false, false>));
-        GS_TRY_LAUNCH(launch(true, fn, fg, kGroupWarps * 32, st, args(kTabForce), p.d_work));
+        if (estimate && p.quad)  // |a| of the groups that have none (members that just joined or were reset)
+            GS_TRY_LAUNCH(launch(true, batch_force_group_kernel<true>(p.exact, p.quad, p.count), fg, kGroupWarps * 32,
+                                 st, args(kTabForce), p.d_work + 1));
+        GS_TRY_LAUNCH(launch(true, batch_force_group_kernel<false>(p.exact, p.quad, p.count), fg, kGroupWarps * 32, st,
+                             args(kTabForce), p.d_work));
     } else {
         auto fn = p.exact ? (p.count ? kb_force<true, true> : kb_force<true, false>)
                           : (p.count ? kb_force<false, true> : kb_force<false, false>);

@@ -203,7 +203,7 @@ struct BatchPlan {
     SysDesc* d_descs = nullptr;
     uint32_t* d_tab[kTabCount] = {};
     uint32_t total[kTabCount] = {};
-    uint32_t* d_work = nullptr;  // [0] next force block
+    uint32_t* d_work = nullptr;  // [0] next force block, [1] next estimate-pass block
     int passes = 0;
     int depth = 0;               // finest level of the Barnes-Hut members (all share the box mode)
     bool bbox = false, quad = false, group = false, exact = false, count = false, direct_exact = false;
@@ -234,15 +234,16 @@ struct gs_sim {
     bool batch_pending = false;
     cudaEvent_t ev[2 * GS_STAGE_COUNT] = {};
     gs_stats stats{};
-    // CUDA graphs: one per ping-pong parity
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    // CUDA graphs: one per ping-pong parity [in], and [2 + in] with the |a| estimate pass
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
     uint64_t steps_done = 0;
     bool capturing = false;          // stage events become external event-record graph nodes
     uint32_t stage_ran = 0;          // stages recorded in the current step (GS_FLAG_PROFILE)
     bool profile_pending = false;    // stage events of the last step not yet accumulated
-    uint32_t graph_stages[2] = {0, 0};  // stages recorded by each captured graph
+    uint32_t graph_stages[4] = {0, 0, 0, 0};  // stages recorded by each captured graph
     uint32_t launches_in_step = 0;   // kernels enqueued by the step being built
-    uint32_t launches_per_step[2] = {0, 0};  // per ping-pong parity (graph replay count)
+    uint32_t launches_per_step[4] = {0, 0, 0, 0};  // per graph (replay count)
+    bool amag_known = false;         // relative criterion: every particle has its previous |a|
     uint64_t kernel_launches = 0;    // kernels launched since creation
     void* slab = nullptr;            // every device buffer of the system
     size_t carved = 0;               // bytes laid out so far (sim_carve)
@@ -279,7 +280,7 @@ cudaError_t keep_pool_memory(int device);
 // layout, initial contents and step launchers (return cudaError_t of the launch)
 void bh_carve(gs_sim* s);
 cudaError_t bh_init(gs_sim* s);
-cudaError_t bh_step(gs_sim* s, int in, int out, bool profile);
+cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate);
 void direct_carve(gs_sim* s);
 cudaError_t direct_init(gs_sim* s);
 cudaError_t direct_step(gs_sim* s, int in, int out, bool profile);
@@ -293,7 +294,7 @@ int bh_key_bits(const gs_params* p);
 void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]);
 void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]);
 int bh_batch_force_grid(const BatchPlan& p);
-cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st);
+cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bool estimate);
 cudaError_t direct_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st);
 void bh_set_final_keys(gs_sim* s);
 

@@ -268,7 +268,7 @@ gs_status step(gs_server* s) {
         s->dirty = false;
         ++s->st.plan_changes;
     }
-    GS_CUDA(s->eng.enqueue((uint32_t)(s->eng.step & 1)));
+    GS_CUDA(s->eng.enqueue((uint32_t)(s->eng.step & 1), s->eng.needs_estimate()));
     s->eng.advance();
     ++s->st.batched_steps;
     cudaEvent_t done = take_event(s);

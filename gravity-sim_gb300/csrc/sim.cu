@@ -177,8 +177,8 @@ void free_sim(gs_sim* s) {
     cudaSetDevice(s->device);
     if (s->stream) (void)wait_stream(s->stream, s->timeout_ns);
     free_snapshot_ring(s);
-    for (int p = 0; p < 2; ++p)
-        if (s->graph[p]) cudaGraphExecDestroy(s->graph[p]);
+    for (auto& g : s->graph)
+        if (g) cudaGraphExecDestroy(g);
     if (s->slab) cudaFreeAsync(s->slab, s->stream);
     s->slab = nullptr;
     for (auto& e : s->ev)
@@ -286,6 +286,7 @@ gs_status upload(gs_sim* s, const float* pos, const float* vel, const float* mas
     }
     uint32_t* ext = s->bh.ext ? s->bh.ext + 4 * a : nullptr;
     if (ext) GS_CUDA(cudaMemsetAsync(ext, 0xFF, 4 * sizeof(uint32_t), s->stream));
+    s->amag_known = false;  // k_upload marks every |a| unknown
     k_upload<<<copy_blocks(s->n_al), 256, 0, s->stream>>>(sp, sv, sm, s->pos[a], s->vel[a], s->mass[0], s->pos[b],
                                                           s->vel[b], s->bh.amag, (uint32_t)n, (uint32_t)s->n_al, ext,
                                                           s->d_err, s->h_err);
@@ -297,10 +298,16 @@ gs_status upload(gs_sim* s, const float* pos, const float* vel, const float* mas
     return sim_wait(s);
 }
 
-cudaError_t enqueue_step(gs_sim* s, int in, bool profile) {
+cudaError_t enqueue_step(gs_sim* s, int in, bool profile, bool estimate) {
     const int out = in ^ 1;
-    if (s->p.algorithm == GS_BARNES_HUT) return bh_step(s, in, out, profile);
+    if (s->p.algorithm == GS_BARNES_HUT) return bh_step(s, in, out, profile, estimate);
     return direct_step(s, in, out, profile);
+}
+
+// The next step has to estimate |a| first: the relative criterion with no previous |a|
+// (after gs_create or gs_set_particles).
+bool needs_estimate(const gs_sim* s) {
+    return s->p.algorithm == GS_BARNES_HUT && (s->p.flags & GS_FLAG_RELATIVE_MAC) && !s->amag_known;
 }
 
 gs_status account_profile(gs_sim* s) {
@@ -488,13 +495,15 @@ gs_status gs_run(gs_sim* s, uint32_t count) {
             if (a != GS_OK) return a;
         }
         s->stage_ran = 0;
+        const bool est = needs_estimate(s);
+        const int gi = in + (est ? 2 : 0);
         if (graphs) {
-            if (!s->graph[in]) {
+            if (!s->graph[gi]) {
                 cudaGraph_t g = nullptr;
                 s->launches_in_step = 0;
                 s->capturing = true;
                 GS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-                cudaError_t e = enqueue_step(s, in, profile);
+                cudaError_t e = enqueue_step(s, in, profile, est);
                 cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
                 s->capturing = false;
                 if (e != cudaSuccess) {
@@ -502,20 +511,21 @@ gs_status gs_run(gs_sim* s, uint32_t count) {
                     return cuda_fail(e, "step capture");
                 }
                 GS_CUDA(e2);
-                e = cudaGraphInstantiate(&s->graph[in], g, 0);
+                e = cudaGraphInstantiate(&s->graph[gi], g, 0);
                 cudaGraphDestroy(g);
                 GS_CUDA(e);
-                s->launches_per_step[in] = s->launches_in_step;
-                s->graph_stages[in] = s->stage_ran;
+                s->launches_per_step[gi] = s->launches_in_step;
+                s->graph_stages[gi] = s->stage_ran;
             }
-            s->stage_ran = s->graph_stages[in];
-            GS_CUDA(cudaGraphLaunch(s->graph[in], s->stream));
-            s->kernel_launches += s->launches_per_step[in];
+            s->stage_ran = s->graph_stages[gi];
+            GS_CUDA(cudaGraphLaunch(s->graph[gi], s->stream));
+            s->kernel_launches += s->launches_per_step[gi];
         } else {
             s->launches_in_step = 0;
-            GS_CUDA(enqueue_step(s, in, profile));
+            GS_CUDA(enqueue_step(s, in, profile, est));
             s->kernel_launches += s->launches_in_step;
         }
+        s->amag_known = true;  // this step leaves every particle's |a|
         if (profile) s->profile_pending = true;  // read back before the next step records again
         s->in ^= 1;  // NextComputeIndices
         ++s->steps_done;

@@ -95,12 +95,14 @@ typedef enum gs_math_mode { GS_MATH_FAST = 0, GS_MATH_REFERENCE = 1 } gs_math_mo
  * i.e. m r^3 / d^5 (the size of the first term a quadrupole expansion leaves out) is at
  * most alpha times the smallest |a| the group's particles had in the previous step
  * (without G) -- or when R <= D theta_f^2: the floor theta_f bounds the walk of a group
- * whose smallest |a| is tiny, as near the centre of a disk.  alpha is
- * gs_params.relative_accuracy, theta_f gs_params.relative_theta_floor (0: theta).  A
- * step with no previous |a| for some particle of the group (the first step after
- * gs_create or gs_set_particles) uses the theta test (accuracy_parameter) alone for that
- * group.  alpha = 0.006 with floor 0.3 and theta 0.35 gives <= 1e-3 RMS force error on
- * the 500k spiral at every step. */
+ * whose smallest |a| is tiny (near the centre of a disk, or where neighbours cancel the
+ * field).  alpha is gs_params.relative_accuracy, theta_f gs_params.relative_theta_floor
+ * (0: theta).  A group with no previous |a| for some particle (every group in the first
+ * step after gs_create or gs_set_particles) first estimates its particles' |a| by a walk
+ * with the theta test (accuracy_parameter; the reference's theta = 1 is enough), then
+ * opens nodes by the relative criterion with those estimates.  alpha = 0.006 with floor
+ * 0.2 gives <= 8e-4 RMS force error at every step on the 500k spiral and on uniform disks
+ * at rest, measured on 4096-17000-particle samples against the FP64 direct sum. */
 #define GS_FLAG_RELATIVE_MAC 0x100u
 
 typedef struct gs_params {

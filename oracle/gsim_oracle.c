@@ -461,52 +461,18 @@ static void walk_warp(void* p, uint64_t item, int worker) {
 #define GROUP_SIZE 64
 #define GROUP_STACK_CAP 2048
 #define GMAX 64
-static void group_walk_warp(void* p, uint64_t item, int worker) {
-    const walk_ctx* c = (const walk_ctx*)p;
-    const uint64_t w = item * c->stride;
-    float px[GMAX], py[GMAX], ax[GMAX][2], ay[GMAX][2]; /* node, leaf */
-    int valid[GMAX];
-    const uint32_t G = c->group_size;
-    int nvalid = 0;
-    float gx0[4], gx1[4], gy0[4], gy1[4];
-    for (int b = 0; b < 4; ++b) {
-        gx0[b] = gy0[b] = INFINITY;
-        gx1[b] = gy1[b] = -INFINITY;
-    }
-    for (uint32_t l = 0; l < G; ++l) {
-        uint32_t s = (uint32_t)w * G + l;
-        uint32_t i = c->src[s];
-        valid[l] = i != c->n_al;
-        px[l] = valid[l] ? c->pos_in[2 * i] : 0.0f;
-        py[l] = valid[l] ? c->pos_in[2 * i + 1] : 0.0f;
-        ax[l][0] = ay[l][0] = ax[l][1] = ay[l][1] = 0.0f;
-        nvalid += valid[l];
-    }
-    if (!nvalid || !c->tree_size) return;
-    {
-        const uint32_t kf = c->skey[(uint32_t)w * G], kl = c->skey[(uint32_t)w * G + (uint32_t)nvalid - 1];
-        const int shift = kf == kl ? -1 : ((31 - __builtin_clz(kf ^ kl)) & ~1);
-        for (int l = 0; l < nvalid; ++l) { /* valid lanes are a prefix of the warp */
-            const int b = shift < 0 ? 0 : (int)((c->skey[(uint32_t)w * G + (uint32_t)l] >> shift) & 3u);
-            gx0[b] = fminf(gx0[b], px[l]);
-            gx1[b] = fmaxf(gx1[b], px[l]);
-            gy0[b] = fminf(gy0[b], py[l]);
-            gy1[b] = fmaxf(gy1[b], py[l]);
-        }
-    }
-    /* relative criterion: the group's smallest previous |a|; NaN if any is unknown */
-    float amin = INFINITY;
-    if (c->amag_in)
-        for (uint32_t l = 0; l < G; ++l) {
-            if (!valid[l]) continue;
-            const float a = c->amag_in[c->src[(uint32_t)w * G + l]];
-            if (isnan(a) || isnan(amin)) amin = NAN;
-            else if (a < amin) amin = a;
-        }
-    const int relative = c->amag_in && amin >= 0.0f;
-    const float tol = c->rel_alpha * amin, tol2 = tol * tol;
+/* One walk of a group: every valid lane's node and leaf accelerations (ax/ay[l][0] node,
+ * [1] leaf) for the opening test `relative` (tol2 = (alpha a_min)^2, with the floor) or
+ * theta (theta2).  Adds the interactions and visits, and raises *max_size. */
+static void group_walk_once(const walk_ctx* c, uint64_t w, uint32_t G, int nvalid, const int* valid,
+                            const float* px, const float* py, const float* gx0, const float* gx1,
+                            const float* gy0, const float* gy1, int relative, float tol2, float theta2,
+                            float (*ax)[2], float (*ay)[2], uint64_t* inter_out, uint64_t* visits_out,
+                            uint32_t* max_size_out) {
+    (void)w;
+    for (uint32_t l = 0; l < G; ++l) ax[l][0] = ay[l][0] = ax[l][1] = ay[l][1] = 0.0f;
     uint32_t stack[GROUP_STACK_CAP + 160];
-    uint32_t size = 1, max_size = 1;
+    uint32_t size = 1, max_size = *max_size_out;
     stack[0] = 0;
     uint64_t inter = 0, visits = 0;
     while (size) {
@@ -535,7 +501,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
                     const float rhs = tol2 * ((d4 * d4) * d2);
                     accept = (r <= d2 && lhs <= rhs) || r <= d2 * c->rel_floor2;
                 } else {
-                    accept = c->radius[n] <= d2 * c->theta2;
+                    accept = c->radius[n] <= d2 * theta2;
                 }
             }
             if (accept) { /* one item: the record itself (a leaf only when the root is one) */
@@ -587,12 +553,81 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
         if (size > max_size) max_size = size;
         if (size > GROUP_STACK_CAP) size = GROUP_STACK_CAP; /* reported through max_stack */
     }
+    *inter_out += inter;
+    *visits_out += visits;
+    *max_size_out = max_size;
+}
+
+/* |a| of an acceleration, the value the relative criterion compares against */
+static inline float accel_magnitude(float ax, float ay) { return sqrtf(fmaf(ax, ax, ay * ay)); }
+
+static void group_walk_warp(void* p, uint64_t item, int worker) {
+    const walk_ctx* c = (const walk_ctx*)p;
+    const uint64_t w = item * c->stride;
+    float px[GMAX], py[GMAX], ax[GMAX][2], ay[GMAX][2]; /* node, leaf */
+    int valid[GMAX];
+    const uint32_t G = c->group_size;
+    int nvalid = 0;
+    float gx0[4], gx1[4], gy0[4], gy1[4];
+    for (int b = 0; b < 4; ++b) {
+        gx0[b] = gy0[b] = INFINITY;
+        gx1[b] = gy1[b] = -INFINITY;
+    }
+    for (uint32_t l = 0; l < G; ++l) {
+        uint32_t s = (uint32_t)w * G + l;
+        uint32_t i = c->src[s];
+        valid[l] = i != c->n_al;
+        px[l] = valid[l] ? c->pos_in[2 * i] : 0.0f;
+        py[l] = valid[l] ? c->pos_in[2 * i + 1] : 0.0f;
+        nvalid += valid[l];
+    }
+    if (!nvalid || !c->tree_size) return;
+    {
+        const uint32_t kf = c->skey[(uint32_t)w * G], kl = c->skey[(uint32_t)w * G + (uint32_t)nvalid - 1];
+        const int shift = kf == kl ? -1 : ((31 - __builtin_clz(kf ^ kl)) & ~1);
+        for (int l = 0; l < nvalid; ++l) { /* valid lanes are a prefix of the warp */
+            const int b = shift < 0 ? 0 : (int)((c->skey[(uint32_t)w * G + (uint32_t)l] >> shift) & 3u);
+            gx0[b] = fminf(gx0[b], px[l]);
+            gx1[b] = fmaxf(gx1[b], px[l]);
+            gy0[b] = fminf(gy0[b], py[l]);
+            gy1[b] = fmaxf(gy1[b], py[l]);
+        }
+    }
+    uint64_t inter = 0, visits = 0;
+    uint32_t max_size = 1;
+    /* relative criterion: the group's smallest previous |a|; NaN if any is unknown */
+    float amin = INFINITY;
+    if (c->amag_in)
+        for (uint32_t l = 0; l < G; ++l) {
+            if (!valid[l]) continue;
+            const float a = c->amag_in[c->src[(uint32_t)w * G + l]];
+            if (isnan(a) || isnan(amin)) amin = NAN;
+            else if (a < amin) amin = a;
+        }
+    if (c->amag_in && isnan(amin)) {
+        /* no previous |a| for some particle (first step after a reset): estimate every
+         * particle's |a| of the group by a walk with the theta test, then open nodes by the
+         * relative criterion with those estimates */
+        group_walk_once(c, w, G, nvalid, valid, px, py, gx0, gx1, gy0, gy1, 0, 0.0f, c->theta2, ax, ay, &inter,
+                        &visits, &max_size);
+        amin = INFINITY;
+        for (uint32_t l = 0; l < G; ++l) {
+            if (!valid[l]) continue;
+            const float a = accel_magnitude(ax[l][0] + ax[l][1], ay[l][0] + ay[l][1]);
+            if (isnan(a) || isnan(amin)) amin = NAN;
+            else if (a < amin) amin = a;
+        }
+    }
+    const int relative = c->amag_in && amin >= 0.0f;
+    const float tol = c->rel_alpha * amin, tol2 = tol * tol;
+    group_walk_once(c, w, G, nvalid, valid, px, py, gx0, gx1, gy0, gy1, relative, tol2, c->theta2, ax, ay, &inter,
+                    &visits, &max_size);
     for (uint32_t l = 0; l < G; ++l) {
         if (!valid[l]) continue;
         uint32_t i = c->src[(uint32_t)w * G + l];
         float vx = c->vel_in[2 * i], vy = c->vel_in[2 * i + 1];
         const float axl = ax[l][0] + ax[l][1], ayl = ay[l][0] + ay[l][1];
-        if (c->amag_out) c->amag_out[i] = sqrtf(fmaf(axl, axl, ayl * ayl));
+        if (c->amag_out) c->amag_out[i] = accel_magnitude(axl, ayl);
         float nvx = fmaf(axl, c->k, vx), nvy = fmaf(ayl, c->k, vy);
         c->pos_out[2 * i] = fmaf(vx + nvx, c->hdt, px[l]);
         c->pos_out[2 * i + 1] = fmaf(vy + nvy, c->hdt, py[l]);

@@ -37,8 +37,10 @@ def test_argument_checks(gs):
 @pytest.mark.gpu
 @pytest.mark.parametrize("algo,extra", [("barnes-hut", ["--math=reference"]), ("direct-sum", []),
                                         ("barnes-hut", ["--box=bbox", "--accurate", "--accuracy-parameter=0.35"]),
-                                        ("barnes-hut", ["--box=bbox", "--accurate", "--accuracy-parameter=0.35",
-                                                        "--relative-accuracy=0.006", "--relative-floor=0.3"])])
+                                        ("barnes-hut", ["--box=bbox", "--accurate", "--accuracy-parameter=1",
+                                                        "--relative-accuracy=0.006", "--relative-floor=0.2"]),
+                                        ("barnes-hut", ["--box=bbox", "--key-bits=15", "--accurate",
+                                                        "--accuracy-parameter=0.5"])])
 def test_file_roundtrip_matches_binding(gs, tmp_path, algo, extra):
     pos, vel, mass = gs.generate(gs.GEN_GALAXY, 3000, size=100.0, seed=17)
     fin, fout = str(tmp_path / "in.txt"), str(tmp_path / "out.txt")
@@ -52,9 +54,12 @@ def test_file_roundtrip_matches_binding(gs, tmp_path, algo, extra):
     if "--math=reference" in extra:
         kw["math_mode"] = gs.MATH_REFERENCE
     if "--box=bbox" in extra:
-        kw.update(box_mode=gs.BOX_BOUNDING, flags=gs.FLAGS_ACCURATE, accuracy_parameter=0.35)
+        kw.update(box_mode=gs.BOX_BOUNDING, flags=gs.FLAGS_ACCURATE,
+                  accuracy_parameter=float([a for a in extra if a.startswith("--accuracy-parameter=")][0][21:]))
+    if "--key-bits=15" in extra:
+        kw["key_bits"] = 15
     if "--relative-accuracy=0.006" in extra:
-        kw.update(flags=gs.FLAGS_ACCURATE | gs.FLAG_RELATIVE_MAC, relative_accuracy=0.006, relative_theta_floor=0.3)
+        kw.update(flags=gs.FLAGS_ACCURATE | gs.FLAG_RELATIVE_MAC, relative_accuracy=0.006, relative_theta_floor=0.2)
     with gs.Simulation(p2, v2, m2, **kw) as sim:
         sim.run(7)
         p, v, m = sim.get_particles()

@@ -187,8 +187,10 @@ def test_tuner_smoke(gs):
 
 def test_relative_criterion_batch_bit_identical(gs):
     """Members with the relative opening criterion and different alphas and floors: each
-    keeps its own |a| buffer, alpha and floor in the batch and matches its twin alone, through a
-    first step (theta test) and later ones (relative test)."""
+    keeps its own |a| buffer, alpha and floor in the batch and matches its twin alone,
+    through a first step (|a| estimated by the theta walk, then the relative walk), later
+    ones (relative walk), and a step after one member alone was reset (only its groups
+    estimate)."""
     rel = dict(algorithm=1, box_mode=1, flags=0x170 | 0x8, accuracy_parameter=0.5)
     specs = [(17, 30000, 100.0, dict(rel, relative_accuracy=0.007, relative_theta_floor=0.3)),
              (16, 5000, 100.0, dict(rel, relative_accuracy=0.02)),
@@ -203,3 +205,41 @@ def test_relative_criterion_batch_bit_identical(gs):
         b.run(3)
         b.sync()
         _assert_same(alone, batched, specs)
+        pos, vel, mass = gs.generate(16, 5000, size=100.0, seed=99)
+        for s in (alone[1], batched[1]):
+            s.set_particles(pos, vel, mass)
+        _run_alone(alone, 2)
+        b.run(2)
+        b.sync()
+        _assert_same(alone, batched, specs)
+
+
+def test_batched_uniform_disk_at_rest_error_gate(gs):
+    """The batched line's parameters (accurate mode, relative criterion alpha 0.006 with
+    floor 0.2, theta 1 for the |a| estimate) on a uniform disk that starts at rest (the
+    case where neighbours cancel the field of many particles), N = 68,893, batched beside
+    a spiral and a direct-sum system: after 110 steps, each of three more steps has RMS
+    relative force error <= 1e-3 against the FP64 direct sum on 16384 particles."""
+    rel = dict(algorithm=1, box_mode=1, flags=0x170 | 0x1, accuracy_parameter=1.0, relative_accuracy=0.006,
+               relative_theta_floor=0.2)
+    specs = [(16, 68893, 100.0, rel), (17, 40000, 100.0, rel), (16, 2000, 100.0, DIRECT)]
+    sims = _make(gs, specs, 1004258)
+    disk = sims[0]
+    sub = np.random.default_rng(2).choice(68893, 16384, replace=False).astype(np.uint32)
+    rms = []
+    with gs.Batch(sims) as b:
+        b.run(110)
+        b.sync()
+        for _ in range(3):
+            start = disk.get_particles()
+            b.run(1)
+            b.sync()
+            acc = disk.get_accel()[sub].astype(np.float64)
+            with gs.Simulation(*start, algorithm=gs.DIRECT_SUM) as ref:
+                a64 = ref.accel_f64(sub)
+            e = np.linalg.norm(acc - a64, axis=1) / np.linalg.norm(a64, axis=1)
+            rms.append(float(np.sqrt(np.mean(e ** 2))))
+    for s in sims:
+        s.close()
+    print("uniform disk at rest, batched, RMS per step:", ", ".join(f"{r:.3e}" for r in rms))
+    assert max(rms) <= 1e-3

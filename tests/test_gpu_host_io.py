@@ -19,8 +19,8 @@ def _pinned(torch, a, offset=0):
 
 
 def _params(gs):
-    return gs.default_params(algorithm=gs.BARNES_HUT, box_mode=gs.BOX_BOUNDING, accuracy_parameter=0.35,
-                             relative_accuracy=0.006, relative_theta_floor=0.3,
+    return gs.default_params(algorithm=gs.BARNES_HUT, box_mode=gs.BOX_BOUNDING, accuracy_parameter=1.0,
+                             relative_accuracy=0.006, relative_theta_floor=0.2,
                              flags=gs.FLAGS_ACCURATE | gs.FLAG_RELATIVE_MAC | gs.FLAG_COUNT_INTERACTIONS)
 
 
