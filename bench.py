@@ -6,20 +6,22 @@ from the enclosed mass + 5% dispersion, masses U[1,10]), softening 0.2, dt = 1e-
 seeded synthetic input, gated at <= 1e-3 RMS relative force error against the FP64
 direct sum at every measured step: accurate mode (bounding box, quadrupoles, safe opening
 radius, group walk) with the relative opening criterion, alpha = 0.006 with a theta floor
-of 0.3 (the first step, which has no previous |a|, uses theta = 0.35).  Beside it: the same accurate mode with the geometric criterion alone at
-theta = 0.35 (the cheapest theta that holds the gate at every step), and the reference's
-own opening rule at theta = 1 (fixed +-500 box, monopoles, warp vote) with its error; the
+of 0.2; a step without a previous |a| (the first, and every end-to-end step, since an
+upload forgets |a|) first estimates |a| by a walk at theta = 1.  Beside it: the same
+accurate mode with the geometric criterion alone at theta = 0.3, and the reference's own
+opening rule at theta = 1 (fixed +-500 box, monopoles, warp vote) with its error; the
 latter does not meet the gate.  A step is one simulation step of the whole system.
 
   value  particle-steps/s, device time (CUDA events on the simulation's stream), state
          resident in HBM; L2 flushed (256 MiB write) before every timed step
   e2e    the same metric through the C ABI with host buffers: every step uploads the
          state from pinned host memory (gs_set_particles), runs one step (gs_run) and
-         reads the state back (gs_get_particles), host wall clock.  An upload forgets
-         the previous |a|, so these steps open nodes by theta = 0.35 alone
+         reads the state back (gs_get_particles), host wall clock
   roofline  the traversal kernel: algorithmic FLOP of the accepted interactions
          (14 per monopole, 33 per quadrupole) over its CUDA-event time, against the
          FP32 FMA rate
+  direct_config  direct sum, N = 4096 uniform disk at rest, 10 steps (its own roofline,
+           error and CPU baseline)
   batched  512 systems of uneven N stepped together, against each run alone
   served   a Poisson stream of simulation requests through the serving loop, against the
            plain path taking them one at a time (p50 / p99 latency)
@@ -28,7 +30,7 @@ latter does not meet the gate.  A step is one simulation step of the whole syste
 
 Multi-GPU: independent replicas (the path has no exchange step), one per rank.
 `--impl reference` times the CPU restatement of the reference's algorithm (oracle/,
-all host threads) on the same workload.
+all host threads) on the same workload; it loads nothing of the library.
 """
 import argparse
 import json
@@ -50,34 +52,38 @@ METRIC = "particle-steps/s (BH N=500k; batched/served vs plain) at <=1e-3 rel fo
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA at 2070 MHz
 ACCURATE = 0x70  # GS_FLAGS_ACCURATE
 RELATIVE = 0x100  # GS_FLAG_RELATIVE_MAC
-# DRAM bytes per launch of the traversal kernel, from one ncu capture of that workload
-# (dram__bytes_read.sum + dram__bytes_write.sum), by workload name
-FORCE_TRAFFIC_BYTES = {
-    "bh500k": 55.017472e6 + 1.798656e6,
+DIRECT_SUM, BARNES_HUT = 0, 1  # gs_algorithm
+BOX_FIXED, BOX_BOUNDING = 0, 1  # gs_box_mode
+GEN_UNIFORM_DISK, GEN_SPIRAL, GEN_EXP_DISK_COLLISION = 16, 17, 18  # gs_generate_type
+ERROR_SAMPLE = 16384  # particles whose FP64 force the gated error is measured on
+# DRAM bytes of one launch of the traversal kernel on a workload, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum), and that launch's algorithmic bytes
+FORCE_CAPTURE = {
+    "bh500k": {"traffic": 55.017472e6 + 1.798656e6, "algorithmic": 49.034480e6},
 }
 
 
 def workloads():
-    import gsim
-
-    spiral = dict(algo=gsim.BARNES_HUT, gen=gsim.GEN_SPIRAL, n=500000, size=100.0, seed=2002)
+    spiral = dict(algo=BARNES_HUT, gen=GEN_SPIRAL, n=500000, size=100.0, seed=2002)
     return {
-        "bh500k": dict(spiral, box=gsim.BOX_BOUNDING, theta=0.35, alpha=0.006, floor=0.3, flags=ACCURATE | RELATIVE,
+        "bh500k": dict(spiral, box=BOX_BOUNDING, theta=1.0, alpha=0.006, floor=0.2, flags=ACCURATE | RELATIVE,
                        oracle_flags=15,
                        desc="Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, safe "
                             "radius, 64-particle group walk), relative opening criterion alpha=0.006 with "
-                            "theta floor 0.3 (theta=0.35 without a previous |a|), softening 0.2, dt=1e-3"),
-        "bh500k-theta": dict(spiral, box=gsim.BOX_BOUNDING, theta=0.35, flags=ACCURATE, oracle_flags=7,
+                            "theta floor 0.2 (|a| estimated by a theta=1 walk where none is known), softening "
+                            "0.2, dt=1e-3"),
+        "bh500k-theta": dict(spiral, box=BOX_BOUNDING, theta=0.3, flags=ACCURATE, oracle_flags=7,
                              desc="Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, "
-                                  "safe radius, 64-particle group walk), geometric criterion theta=0.35, "
+                                  "safe radius, 64-particle group walk), geometric criterion theta=0.3, "
                                   "softening 0.2, dt=1e-3"),
-        "bh500k-reference-rule": dict(spiral, box=gsim.BOX_FIXED_500, theta=1.0, flags=0, oracle_flags=0,
+        "bh500k-reference-rule": dict(spiral, box=BOX_FIXED, theta=1.0, flags=0, oracle_flags=0,
                                       desc="Barnes-Hut N=500000 spiral galaxy, the reference's opening rule "
                                            "(fixed +-500 box, monopoles, warp vote) theta=1, softening 0.2, dt=1e-3"),
-        "direct4096": dict(algo=gsim.DIRECT_SUM, gen=gsim.GEN_UNIFORM_DISK, n=4096, size=100.0, seed=1001, box=0,
-                           theta=1.0, flags=0, oracle_flags=0,
-                           desc="direct sum N=4096 uniform disk r=100, softening 0.2, dt=1e-3"),
-        "direct50k": dict(algo=gsim.DIRECT_SUM, gen=gsim.GEN_EXP_DISK_COLLISION, n=50000, size=100.0, seed=1003,
+        "direct4096": dict(algo=DIRECT_SUM, gen=GEN_UNIFORM_DISK, n=4096, size=100.0, seed=1001, box=0,
+                           theta=1.0, flags=0, oracle_flags=0, steps=10,
+                           desc="direct sum N=4096 uniform disk r=100 at rest, masses U[1,10], softening 0.2, "
+                                "dt=1e-3, 10 steps"),
+        "direct50k": dict(algo=DIRECT_SUM, gen=GEN_EXP_DISK_COLLISION, n=50000, size=100.0, seed=1003,
                           box=0, theta=1.0, flags=0, oracle_flags=0,
                           desc="direct sum N=50000 two exponential disks at (+-50,0), v=(0,+-3)"),
     }
@@ -256,17 +262,19 @@ def make_params(gsim, wl, local, flags):
                                device=local, flags=wl["flags"] | flags)
 
 
-def step_errors(gsim, params, pos, vel, mass, sub, steps):
+def step_errors(gsim, params, pos, vel, mass, sub, steps, warm=0):
     """Relative force error against the FP64 direct sum on the particles `sub`, for each
-    of `steps` consecutive steps after one warm step (which leaves the previous |a| that
-    the relative criterion needs).  FP64 forces of each step's starting state come from a
-    direct-sum system holding that state (gs_accel_f64)."""
+    of `steps` consecutive steps after `warm` unmeasured ones, from a new system holding
+    the given state (so the first step is one without a previous |a|).  FP64 forces of
+    each step's starting state come from a direct-sum system holding that state
+    (gs_accel_f64)."""
     p = gsim.Params.from_buffer_copy(params)
     p.flags |= gsim.FLAG_RECORD_ACCEL
     d = gsim.default_params(algorithm=gsim.DIRECT_SUM, device=p.device)
     errs = []
     with gsim.Simulation(pos, vel, mass, params=p) as es:
-        es.run(1)
+        if warm:
+            es.run(warm)
         for _ in range(steps):
             start = es.get_particles()
             es.run(1)
@@ -275,6 +283,14 @@ def step_errors(gsim, params, pos, vel, mass, sub, steps):
                 a64 = fs.accel_f64(sub)
             errs.append(np.linalg.norm(acc - a64, axis=1) / np.maximum(np.linalg.norm(a64, axis=1), 1e-30))
     return errs
+
+
+def error_summary(errs):
+    """RMS of each step, the worst (the gated figure), and median / p99 / max over all."""
+    rms = [float(np.sqrt(np.mean(e ** 2))) for e in errs]
+    e = np.concatenate(errs)
+    return {"rms": max(rms), "rms_per_step": rms, "median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)),
+            "max": float(e.max())}
 
 
 def interaction_counts(gsim, wl, pos, vel, mass, local):
@@ -345,11 +361,9 @@ BATCH_DESC = ("512 independent systems, N log-uniform in [1024, 262144] (seed 10
 
 
 def batch_specs(count=512, seed=1004, lo=1024, hi=262144):
-    import gsim
-
     rng = np.random.default_rng(seed)
     n = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64)
-    kind = np.where(rng.random(count) < 0.5, gsim.GEN_UNIFORM_DISK, gsim.GEN_SPIRAL)
+    kind = np.where(rng.random(count) < 0.5, GEN_UNIFORM_DISK, GEN_SPIRAL)
     return [(int(k), int(x), seed * 1000 + j) for j, (k, x) in enumerate(zip(kind, n))]
 
 
@@ -428,18 +442,10 @@ def measure_batched(gsim, torch, args, local):
         dev_p += a.elapsed_time(z) / 1e3
     wall_p = time.perf_counter() - w0  # includes the warm-up steps
 
-    # force error of a sample of members (from the current state: a warm step, then the
-    # next step against FP64)
-    errs = []
-    rng = np.random.default_rng(1)
-    for j in sorted(rng.choice(len(sims), 8, replace=False)):
-        kind, n, seed = specs[j]
-        pos, vel, mass = sims[j].get_particles()
-        sub = rng.choice(n, min(1024, n), replace=False).astype(np.uint32)
-        e = step_errors(gsim, batch_params(gsim, local, n, xo, theta, alpha, floor), pos, vel, mass, sub, 1)[0]
-        errs.append({"n": n, "kind": "spiral" if kind == gsim.GEN_SPIRAL else "uniform disk",
-                     "algorithm": "barnes-hut" if n >= xo else "direct", "rms": float(np.sqrt(np.mean(e ** 2))),
-                     "max": float(e.max())})
+    # force error of a stratified sample of members, from each one's current state (after
+    # all the steps above): the first step has no previous |a| (it estimates it), the
+    # second opens nodes by the |a| the first left
+    errs = _member_errors(gsim, local, specs, sims, xo, theta, alpha, floor)
     for s in sims:
         s.close()
     value = total_n * steps / dev_b
@@ -451,8 +457,33 @@ def measure_batched(gsim, torch, args, local):
             "kernels_per_step": kps, "gpu_launches": kps * steps,
             "plain_one_at_a_time": {"value": plain, "device_s": dev_p, "wall_s_incl_warmup": wall_p},
             "speedup_vs_plain": value / plain, "wall_value": total_n * steps / wall_b,
-            "force_error_sample": errs, "setup_s": setup_s,
+            "force_error_sample": errs, "force_error_worst_rms": max(e["rms"] for e in errs), "setup_s": setup_s,
             "l2": "flushed (256 MiB write) before every timed batched step and before each plain system"}
+
+
+def _member_errors(gsim, local, specs, sims, xo, theta, alpha, floor, per_kind=12, sample=4096, steps=2):
+    """Force error of `per_kind` Barnes-Hut members of each generator type (evenly spread
+    over their sizes) and two direct-sum members, on `sample` particles each, at `steps`
+    steps from the member's current state."""
+    chosen = []
+    for kind in (GEN_UNIFORM_DISK, GEN_SPIRAL):
+        idx = sorted((j for j, (k, n, _) in enumerate(specs) if k == kind and n >= xo), key=lambda j: specs[j][1])
+        if idx:
+            chosen += [idx[int(q)] for q in np.unique(np.linspace(0, len(idx) - 1, per_kind).round())]
+    small = sorted((j for j, (_, n, _) in enumerate(specs) if n < xo), key=lambda j: specs[j][1])
+    chosen += [small[0], small[-1]] if small else []
+    rng = np.random.default_rng(1)
+    out = []
+    for j in sorted(set(chosen)):
+        kind, n, _ = specs[j]
+        pos, vel, mass = sims[j].get_particles()
+        sub = rng.choice(n, min(sample, n), replace=False).astype(np.uint32)
+        errs = step_errors(gsim, batch_params(gsim, local, n, xo, theta, alpha, floor), pos, vel, mass, sub, steps)
+        r = error_summary(errs)
+        out.append({"n": n, "kind": "spiral" if kind == GEN_SPIRAL else "uniform disk",
+                    "algorithm": "barnes-hut" if n >= xo else "direct", "rms": r["rms"],
+                    "rms_per_step": r["rms_per_step"], "max": r["max"], "subsample": int(len(sub))})
+    return out
 
 
 SERVE_DESC = ("Poisson stream (mean 200 requests/s, seed 1005) of simulation requests: N log-uniform in "
@@ -469,7 +500,7 @@ def serve_trace(count, seed=1005, rate=200.0, lo=2048, hi=1 << 20):
     arrivals = np.cumsum(gaps) - gaps[0]
     n = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64)
     steps = rng.integers(10, 1001, count)
-    gen = rng.choice([gsim.GEN_UNIFORM_DISK, gsim.GEN_SPIRAL, gsim.GEN_EXP_DISK_COLLISION], count)
+    gen = rng.choice([GEN_UNIFORM_DISK, GEN_SPIRAL, GEN_EXP_DISK_COLLISION], count)
     reqs = [gsim.make_request(int(n[j]), int(steps[j]), int(gen[j]), seed=seed * 100000 + j) for j in range(count)]
     return reqs, arrivals
 
@@ -516,11 +547,34 @@ def measure_served(gsim, torch, args, local, crossover, theta, alpha, floor):
         lat_p.append(time.perf_counter() - start - a)
     makespan_p = time.perf_counter() - start - float(arrivals[0])
     plain = {"value": work / makespan_p, "makespan_s": makespan_p, "latency": _latency_summary(lat_p)}
+    served["force_error_sample"] = _request_errors(gsim, reqs, d, b, crossover)
+    served["force_error_worst_rms"] = max(e["rms"] for e in served["force_error_sample"])
     return {"workload": SERVE_DESC % bh_mode_desc(theta, alpha, floor), "requests": len(reqs), "theta": theta,
             "alpha": alpha, "theta_floor": floor, "crossover_n": crossover,
             "particle_steps": work, "value": served["value"], "unit": "particle-steps/s", "served": served,
             "plain_sequential": plain, "speedup_vs_plain": served["value"] / plain["value"],
             "max_resident_particles": args.serve_max_particles, "policy": "fifo with conservative backfill"}
+
+
+def _request_errors(gsim, reqs, d, b, crossover, per_kind=2, sample=4096, steps=3):
+    """Force error of served requests: `per_kind` requests of each generator type (the
+    smallest and the largest Barnes-Hut ones of the trace), each stepped alone from its
+    generated state with the served parameters -- a served request ends bit-identical to
+    the same system run alone -- on `sample` particles at each of its first `steps` steps."""
+    names = {GEN_UNIFORM_DISK: "uniform disk", GEN_SPIRAL: "spiral", GEN_EXP_DISK_COLLISION: "two-disk collision"}
+    rng = np.random.default_rng(2)
+    out = []
+    for kind in names:
+        rs = sorted((r for r in reqs if r.generator == kind and r.particle_count >= crossover),
+                    key=lambda r: r.particle_count)
+        for r in ([rs[0], rs[-1]] if len(rs) > 1 else rs)[:per_kind]:
+            n = r.particle_count
+            pos, vel, mass = gsim.generate(r.generator, n, size=r.generate_size, seed=r.seed)
+            sub = rng.choice(n, min(sample, n), replace=False).astype(np.uint32)
+            res = error_summary(step_errors(gsim, b, pos, vel, mass, sub, steps))
+            out.append({"n": n, "kind": names[kind], "rms": res["rms"], "rms_per_step": res["rms_per_step"],
+                        "max": res["max"], "subsample": int(len(sub))})
+    return out
 
 
 PREC_DESC = ("direct sum N=50000, two exponential disks (scale length 20, truncated at r <= 50) centred at "
@@ -574,88 +628,149 @@ def precision_study(gsim, torch, args, local, steps=1000, every=100, sample=2048
             "variants": out}
 
 
-def force_error(gsim, wl, pos, vel, mass, local, steps=4):
+def force_error(gsim, wl, pos, vel, mass, local, steps=5):
     """Relative force error against the FP64 direct sum (GPU FP64 kernel) on a
-    4096-particle subsample, at each of `steps` steps after a warm step: the RMS of the
-    worst step (the gated figure), each step's RMS, and median / p99 / max over all."""
-    sub = np.random.default_rng(0).choice(wl["n"], min(4096, wl["n"]), replace=False).astype(np.uint32)
-    errs = step_errors(gsim, make_params(gsim, wl, local, 0), pos, vel, mass, sub, steps)
-    rms = [float(np.sqrt(np.mean(e ** 2))) for e in errs]
-    e = np.concatenate(errs)
-    return {"rms": max(rms), "rms_per_step": rms, "median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)),
-            "max": float(e.max()), "subsample": int(len(sub)), "steps": f"steps 2..{steps + 1} from the generated state"}
+    16384-particle subsample, at each of the first `steps` steps from the generated state
+    (the first has no previous |a|): the RMS of the worst step (the gated figure), each
+    step's RMS, and median / p99 / max over all."""
+    sub = np.random.default_rng(0).choice(wl["n"], min(ERROR_SAMPLE, wl["n"]), replace=False).astype(np.uint32)
+    r = error_summary(step_errors(gsim, make_params(gsim, wl, local, 0), pos, vel, mass, sub, steps))
+    r.update(subsample=int(len(sub)), steps=f"steps 1..{steps} from the generated state")
+    return r
 
 
-def roofline_of(gsim, wl, m):
-    if wl["algo"] == gsim.BARNES_HUT:
+def force_algorithmic_bytes(wl, m):
+    """Bytes the traversal kernel must move once per launch: tree records (16 B each), the
+    moments and child links of internal records (32 B each), the particle state read and
+    written (32 B per particle), the sorted key and order (8 B) and the previous and new
+    |a| (8 B) per particle."""
+    n_al = (wl["n"] + 63) // 64 * 64
+    amag = 8 if wl["flags"] & RELATIVE else 0
+    return 16 * m["tree_records"] + 32 * m["internal_nodes"] + (32 + 8 + amag) * n_al
+
+
+def roofline_of(gsim, wl, m, capture=None):
+    """FP32 roofline of the force kernel.  `capture`: DRAM bytes of one launch of the same
+    kernel on the same workload from an ncu capture, with the algorithmic bytes of that
+    launch; the line's traffic is that figure scaled to this run's algorithmic bytes."""
+    algorithmic = None
+    if wl["algo"] == BARNES_HUT:
         t = m["stage_ms"]["force"] / 1e3
         # 14 FLOP per monopole interaction (particle leaves; every record under the
         # reference rule), 33 per quadrupole interaction (accurate-mode nodes)
         quads = m["node_interactions"] if wl["flags"] & 0x10 else 0
         flops = 14.0 * (m["interactions"] - quads) + 33.0 * quads
         achieved = flops / t / 1e12
+        algorithmic = force_algorithmic_bytes(wl, m)
         extra = {"kernel": "k_force_group" if wl["flags"] & 0x40 else "k_force",
                  "interactions_per_step": m["interactions"], "quadrupole_interactions_per_step": quads,
                  "tests_per_step": m["tests"], "tree_records": m["tree_records"],
-                 "internal_nodes": m["internal_nodes"],
-                 "flop_model": "14 FLOP per monopole (leaf) interaction, 33 per quadrupole (node) interaction (FMA = 2)"}
+                 "internal_nodes": m["internal_nodes"], "algorithmic_bytes": algorithmic,
+                 "flop_model": "14 FLOP per monopole (leaf) interaction, 33 per quadrupole (node) interaction "
+                               "(FMA = 2); interactions of both walks of a step that estimates |a| are counted"}
     else:
         t = m["stage_ms"]["direct"] / 1e3
         n_al = (wl["n"] + 63) // 64 * 64
         achieved = 14.0 * n_al * n_al / t / 1e12
         extra = {"kernel": "k_direct_fast", "pairs_per_step": n_al * n_al, "flop_model": "14 FLOP per pair"}
-    traffic = FORCE_TRAFFIC_BYTES.get(wl.get("name"))
+    traffic = source = None
+    if capture and algorithmic:
+        traffic = capture["traffic"] * algorithmic / capture["algorithmic"]
+        source = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this workload "
+                  f"({capture['traffic'] / 1e6:.2f} MB at {capture['algorithmic'] / 1e6:.2f} MB algorithmic), "
+                  f"scaled by this run's algorithmic bytes; ncu cannot run inside the timed bench")
     r = {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-         "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": traffic,
-         "traffic_source": ("dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this "
-                            "workload (ncu --set full, profiles/k_force_group_bh500k_relative.md)") if traffic else None,
+         "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": traffic, "traffic_source": source,
          "peak_source": "nominal FP32 FMA rate at 2070 MHz (MEASURED_PEAKS.json has no FP32 figure)",
          "stage_ms_per_step": m["stage_ms"]}
     r.update(extra)
     return r
 
 
-def cpu_baseline(wl, pos, vel, mass, seconds_budget=30.0):
-    """The CPU restatement (oracle/) on all host threads, one step of the same workload;
-    the force walk is sampled (every k-th warp) when a full step would exceed the budget."""
+def _cpu_bh_step_seconds(oracle, wl, pos, vel, mass, threads, budget):
+    """Seconds of one Barnes-Hut step of the oracle on `threads` threads: the second step
+    of the system (a full first step leaves every particle's |a|), with the force walk
+    sampled (every k-th group, its time scaled by k) when a full step would exceed the
+    budget.  Returns (seconds, stride)."""
+    st = oracle.State(pos, vel, mass)
+    kw = dict(box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads, flags=wl["oracle_flags"],
+              rel_alpha=wl.get("alpha", 0.0), rel_floor=wl.get("floor"))
+    r = oracle.bh_step(st, **kw)  # the full first step (time estimate of the second)
+    stride = max(1, int(np.ceil((r["build_seconds"] + r["walk_seconds"]) / budget)))
+    r = oracle.bh_step(st, walk_stride=stride, **kw)
+    return r["build_seconds"] + stride * r["walk_seconds"], stride
+
+
+def cpu_baseline(wl, pos, vel, mass, seconds_budget=15.0):
+    """The CPU restatement (oracle/) of one step of the same workload, on all host threads
+    and on one core; a long Barnes-Hut force walk is sampled."""
     from oracle import oracle
 
     threads = os.cpu_count() or 1
-    if wl["algo"] == 1:
-        st = oracle.State(pos, vel, mass)
-        kw = dict(box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads, flags=wl["oracle_flags"],
-                  rel_alpha=wl.get("alpha", 0.0), rel_floor=wl.get("floor"))
-        r = oracle.bh_step(st, walk_stride=16, **kw)  # time estimate
-        est = r["build_seconds"] + 16 * r["walk_seconds"]
-        stride = max(1, int(np.ceil(est / seconds_budget)))
-        if wl["oracle_flags"] & oracle.RELATIVE_MAC:  # a full first step leaves every particle's |a|
+    out = {}
+    for cores in (threads, 1):
+        if wl["algo"] == BARNES_HUT:
+            t, stride = _cpu_bh_step_seconds(oracle, wl, pos, vel, mass, cores, seconds_budget)
+            sample = (f"1 step of the same {wl['n']}-particle system (the second, after a full first step): tree "
+                      f"build on 1 thread, force walk on {cores} thread(s)" +
+                      (f" over every {stride}-th group of 64, its time scaled by {stride}" if stride > 1 else ""))
+        else:
             st = oracle.State(pos, vel, mass)
-            oracle.bh_step(st, **kw)
-        r = oracle.bh_step(st, walk_stride=stride, **kw)
-        t = r["build_seconds"] + stride * r["walk_seconds"]
-        sample = (f"1 step of the same {wl['n']}-particle system (the second, after a full first step): full "
-                  f"tree build (1 thread), force walk of every {stride}-th group of 64 on {threads} threads, "
-                  f"walk time scaled by {stride}" if stride > 1 else
-                  f"1 full step of the same {wl['n']}-particle system (the second, after a full first step): "
-                  f"tree build on 1 thread, force walk on {threads} threads")
-    else:
-        st = oracle.State(pos, vel, mass)
-        t0 = time.perf_counter()
-        oracle.direct_step(st, threads=threads)
-        t = time.perf_counter() - t0
-        sample = f"1 step of the same {wl['n']}-particle system on {threads} threads"
-    return {"value": wl["n"] / t, "unit": "particle-steps/s", "cores": threads, "kind": "port", "sample": sample}
+            t0 = time.perf_counter()
+            oracle.direct_step(st, threads=cores)
+            t = time.perf_counter() - t0
+            sample = f"1 step of the same {wl['n']}-particle system on {cores} thread(s)"
+        out[cores] = {"value": wl["n"] / t, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                      "sample": sample}
+    r = dict(out[threads])
+    r["single_core"] = out[1]
+    return r
+
+
+def direct_config(gsim, torch, args, local):
+    """Direct sum, N = 4096 uniform disk at rest, 10 steps: device time per step (CUDA
+    events, L2 flushed before each step), FP32 roofline, force error of every step
+    against the FP64 direct sum on all particles, and the CPU baseline."""
+    wl = dict(workloads()["direct4096"], name="direct4096")
+    pos, vel, mass = gsim.generate(wl["gen"], wl["n"], size=wl["size"], seed=wl["seed"])
+    steps = wl["steps"]
+    p = make_params(gsim, wl, local, 0)
+    with gsim.Simulation(pos, vel, mass, params=p) as sim:
+        stream = torch.cuda.ExternalStream(sim.stream(), device=local)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+        times = []
+        for rep in range(args.warmup + 1):  # warm-up runs of the 10 steps, then the timed one
+            sim.set_particles(pos, vel, mass)
+            sim.sync()
+            starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+            ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+            with torch.cuda.stream(stream):
+                for k in range(steps):
+                    flush.zero_()
+                    starts[k].record(stream)
+                    sim.run(1)
+                    ends[k].record(stream)
+            sim.sync()
+            times = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+        dev_ms = float(sum(times))
+    err = error_summary(step_errors(gsim, p, pos, vel, mass, np.arange(wl["n"], dtype=np.uint32), steps))
+    m = {"stage_ms": {"direct": dev_ms / steps}}
+    return {"workload": wl["desc"], "value": wl["n"] * steps / (dev_ms / 1e3), "unit": "particle-steps/s",
+            "steps": steps, "ms_per_step": dev_ms / steps, "roofline": roofline_of(gsim, wl, m),
+            "force_error_vs_fp64": dict(err, subsample=wl["n"], steps="steps 1..10 from the generated state"),
+            "cpu_baseline": cpu_baseline(wl, pos, vel, mass),
+            "l2": "flushed (256 MiB write) before every timed step"}
 
 
 def run_reference(args, wl):
-    """--impl reference: the CPU restatement of the reference's algorithm, all host threads."""
-    import gsim
+    """--impl reference: the CPU restatement of the reference's algorithm, all host threads,
+    on inputs from the oracle's own generators (nothing of the library is loaded)."""
     from oracle import oracle
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if int(os.environ.get("RANK", "0")) != 0:
         return 0
-    pos, vel, mass = gsim.generate(wl["gen"], wl["n"], size=wl["size"], seed=wl["seed"])
+    pos, vel, mass = oracle.generate(wl["gen"], wl["n"], size=wl["size"], seed=wl["seed"])
     threads = os.cpu_count() or 1
     st = oracle.State(pos, vel, mass)
     budget = 150.0 / max(1, args.steps + args.warmup)  # whole run within a few minutes
@@ -663,7 +778,7 @@ def run_reference(args, wl):
     kw = dict(box_mode=wl["box"], theta=wl["theta"], keep_tree=False, threads=threads, flags=wl["oracle_flags"],
               rel_alpha=wl.get("alpha", 0.0), rel_floor=wl.get("floor"))
     for k in range(args.warmup + args.steps):
-        if wl["algo"] == 1:
+        if wl["algo"] == BARNES_HUT:
             if k == 0:  # a full step: time estimate, and every particle's |a| for the next
                 r = oracle.bh_step(st, **kw)
                 t = r["build_seconds"] + r["walk_seconds"]
@@ -680,12 +795,13 @@ def run_reference(args, wl):
     tot = float(np.sum(times))
     value = wl["n"] * len(times) / tot
     sample = (f"each step: full tree build + force walk of every {stride}-th group of 64, walk time scaled by "
-              f"{stride}" if wl["algo"] == 1 and stride > 1 else "each step: one full step of the system")
+              f"{stride}" if wl["algo"] == BARNES_HUT and stride > 1 else "each step: one full step of the system")
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "impl": "reference", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded generator)",
-           "config": {"workload": wl["desc"], "particles": wl["n"], "l2": "n/a (CPU)"},
+           "config": {"workload": wl["desc"], "particles_per_gpu": wl["n"], "parallelism": f"replicas x{world}"},
+           "l2": "n/a (CPU)",
            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                             "sample": sample},
            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -705,20 +821,20 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-system batched line")
     ap.add_argument("--batch-steps", type=int, default=50)
-    ap.add_argument("--batch-theta", type=float, default=0.35,
-                    help="theta of the batched and served Barnes-Hut systems (steps without a previous |a|)")
-    ap.add_argument("--batch-floor", type=float, default=0.3,
+    ap.add_argument("--batch-theta", type=float, default=1.0,
+                    help="theta of the batched and served Barnes-Hut systems (the |a| estimate of a step "
+                         "without a previous |a|)")
+    ap.add_argument("--batch-floor", type=float, default=0.2,
                     help="theta floor of the relative criterion of the batched and served systems")
     ap.add_argument("--batch-alpha", type=float, default=0.006,
                     help="relative criterion alpha of the batched and served Barnes-Hut systems (0: theta alone)")
     ap.add_argument("--no-served", action="store_true", help="skip the served (request stream) line")
     ap.add_argument("--no-precision", action="store_true", help="skip the direct-sum precision study")
+    ap.add_argument("--no-direct-config", action="store_true", help="skip the N=4096 direct-sum line")
     ap.add_argument("--serve-requests", type=int, default=100)
     ap.add_argument("--serve-max-particles", type=int, default=0, help="resident particle cap (0: budget only)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
-
-    import gsim
 
     wl = dict(workloads()[args.workload], name=args.workload)
     if args.impl == "reference":
@@ -727,6 +843,7 @@ def main():
     import build as pkg_build
 
     pkg_build.build()
+    import gsim
     import torch
 
     world, rank, local, dist = dist_setup()
@@ -784,6 +901,9 @@ def main():
     precision = None
     if rank == 0 and world == 1 and not args.no_precision:
         precision = precision_study(gsim, torch, args, local)
+    direct = None
+    if rank == 0 and world == 1 and not args.no_direct_config:
+        direct = direct_config(gsim, torch, args, local)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, pos, vel, mass)
@@ -792,13 +912,13 @@ def main():
         out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-               "config": {"workload": wl["desc"], "particles_per_gpu": wl["n"], "parallelism": f"replicas x{world}",
-                          "l2": "flushed (256 MiB write) before every timed step"},
-               "e2e": e2e, "gpu_launches": m["launches"] * world, "roofline": roofline_of(gsim, wl, m),
+               "config": {"workload": wl["desc"], "particles_per_gpu": wl["n"], "parallelism": f"replicas x{world}"},
+               "l2": "flushed (256 MiB write) before every timed step",
+               "e2e": e2e, "gpu_launches": m["launches"] * world,
+               "roofline": roofline_of(gsim, wl, m, FORCE_CAPTURE.get(args.workload)),
                "cpu_baseline": cpu, "force_error_vs_fp64": err, "clocks": m["clocks"],
-               "accurate_theta_only": theta_only, "reference_rule_theta1": secondary, "batched": batched,
-               "served": served,
-               "direct_precision_study": precision}
+               "accurate_theta_only": theta_only, "reference_rule_theta1": secondary, "direct_config": direct,
+               "batched": batched, "served": served, "direct_precision_study": precision}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

@@ -368,6 +368,8 @@ typedef struct {
     uint32_t stride;        /* walk warps stride*item */
     int group_walk;         /* ORC_BH_GROUP_WALK semantics */
     uint32_t* max_stack;    /* per worker */
+    uint32_t* group_visits; /* optional per-group outputs (orc_bh_out) */
+    uint64_t* group_inter;
     uint64_t* max_inter;    /* per worker: largest per-warp interaction count */
     uint32_t group_size;    /* particles per group walk (64) */
     float rel_alpha, rel_floor2; /* ORC_BH_RELATIVE_MAC: alpha, floor^2, previous and new |a| */
@@ -636,6 +638,8 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
     }
     c->interactions[worker] += inter;
     c->visits[worker] += visits;
+    if (c->group_visits) c->group_visits[w] = (uint32_t)visits;
+    if (c->group_inter) c->group_inter[w] = inter;
     if (max_size > c->max_stack[worker]) c->max_stack[worker] = max_size;
     if (inter > c->max_inter[worker]) c->max_inter[worker] = inter;
 }
@@ -1138,6 +1142,10 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
         wc.amag_in = out->amag_in;
         wc.amag_out = out->amag_out;
     }
+    if (out) {
+        wc.group_visits = out->group_visits;
+        wc.group_inter = out->group_interactions;
+    }
     run_walk(&wc, nthreads, out);
 
     if (out) {
@@ -1170,5 +1178,194 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
     free(msy);
     free(quad);
     free(src);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------ */
+/* seeded generators -- the library's gs_generate restated, so that the CPU       */
+/* baseline and the reference arm make their inputs without the library.  The     */
+/* presets follow ParticleSystem.cpp:15-149 (draw order per particle: angle,       */
+/* radius, mass) with an explicit seed: splitmix64, 24-bit float conversion.      */
+/* ------------------------------------------------------------------------------ */
+static const double ORC_PI = 3.14159265358979323846;
+
+typedef struct { uint64_t s; } orc_rng;
+static uint64_t rng_next(orc_rng* r) { /* splitmix64 */
+    uint64_t z = (r->s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static float rng_uniform(orc_rng* r) { return (float)(rng_next(r) >> 40) * (1.0f / 16777216.0f); }
+static double rng_uniform_open(orc_rng* r) {
+    return ((double)(rng_next(r) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+static double rng_normal(orc_rng* r) { /* Box-Muller */
+    double u1 = rng_uniform_open(r), u2 = rng_uniform_open(r);
+    return sqrt(-2.0 * log(u1)) * cos(2.0 * ORC_PI * u2);
+}
+
+static void og_random(orc_rng* r, size_t n, float size, float mn, float mx, float* p, float* v, float* m) {
+    for (size_t i = 0; i < n; ++i) {
+        float theta = (float)((double)(rng_uniform(r) * 2.0f) * ORC_PI);
+        float rad = sqrtf(1.0f - rng_uniform(r)) * size;
+        p[2 * i] = rad * cosf(theta);
+        p[2 * i + 1] = rad * sinf(theta);
+        v[2 * i] = v[2 * i + 1] = 0.0f;
+        m[i] = rng_uniform(r) * (mx - mn) + mn;
+    }
+}
+
+static void og_galaxy(orc_rng* r, size_t n, float size, float mn, float mx, float G, float* p, float* v, float* m) {
+    float avg = (mn + mx) * 0.5f;
+    float vel = sqrtf(G * (float)n * avg / (size * size * size));
+    for (size_t i = 0; i < n; ++i) {
+        float theta = (float)((double)(rng_uniform(r) * 2.0f) * ORC_PI);
+        float rad = (1.0f - rng_uniform(r)) * size;
+        float sn = sinf(theta), cs = cosf(theta);
+        p[2 * i] = rad * cs;
+        p[2 * i + 1] = rad * sn;
+        v[2 * i] = -sn * rad * vel;
+        v[2 * i + 1] = cs * rad * vel;
+        m[i] = rng_uniform(r) * (mx - mn) + mn;
+    }
+}
+
+static void og_collision(orc_rng* r, size_t n, float size, float mn, float mx, float G, float* p, float* v,
+                         float* m) {
+    float gs = size / 3.0f;
+    float avg = (mn + mx) * 0.25f;
+    float vel = sqrtf(G * (float)n * avg / (gs * gs * gs));
+    for (size_t i = 0; i < n; ++i) {
+        float side = i < (n >> 1) ? -1.0f : 1.0f;
+        float theta = (float)((double)(rng_uniform(r) * 2.0f) * ORC_PI);
+        float rad = (1.0f - rng_uniform(r)) * gs;
+        float sn = sinf(theta), cs = cosf(theta);
+        p[2 * i] = rad * cs + side * gs * 2.0f;
+        p[2 * i + 1] = rad * sn;
+        v[2 * i] = -sn * rad * vel - side * gs * 0.1f;
+        v[2 * i + 1] = cs * rad * vel;
+        m[i] = rng_uniform(r) * (mx - mn) + mn;
+    }
+}
+
+static void og_symmetric(orc_rng* r, size_t n, float size, float mn, float mx, float G, float* p, float* v,
+                         float* m) {
+    float gs = size / 3.0f;
+    float avg = (mn + mx) * 0.25f;
+    float vel = sqrtf(G * (float)n * avg / (gs * gs * gs));
+    for (size_t i = 0; i + 1 < n; i += 2) {
+        float theta = (float)((double)(rng_uniform(r) * 2.0f) * ORC_PI);
+        float rad = (1.0f - rng_uniform(r)) * gs;
+        float sn = sinf(theta), cs = cosf(theta);
+        p[2 * i] = rad * cs - gs * 2.0f;
+        p[2 * i + 1] = rad * sn;
+        v[2 * i] = -sn * rad * vel + gs * 0.1f;
+        v[2 * i + 1] = cs * rad * vel;
+        m[i] = rng_uniform(r) * (mx - mn) + mn;
+        p[2 * i + 2] = -p[2 * i];
+        p[2 * i + 3] = p[2 * i + 1];
+        v[2 * i + 2] = -sn * rad * vel - gs * 0.1f;
+        v[2 * i + 3] = -cs * rad * vel;
+        m[i + 1] = m[i];
+    }
+}
+
+static void og_uniform_disk(orc_rng* r, size_t n, float radius, float mn, float mx, float* p, float* v, float* m) {
+    for (size_t i = 0; i < n; ++i) {
+        double rad = radius * sqrt((double)rng_uniform(r));
+        double phi = 2.0 * ORC_PI * (double)rng_uniform(r);
+        p[2 * i] = (float)(rad * cos(phi));
+        p[2 * i + 1] = (float)(rad * sin(phi));
+        v[2 * i] = v[2 * i + 1] = 0.0f;
+        m[i] = mn + (mx - mn) * rng_uniform(r);
+    }
+}
+
+static const double* og_sort_key;
+static int og_by_radius(const void* a, const void* b) { /* radius, then index: a total order */
+    const size_t i = *(const size_t*)a, j = *(const size_t*)b;
+    if (og_sort_key[i] < og_sort_key[j]) return -1;
+    if (og_sort_key[i] > og_sort_key[j]) return 1;
+    return i < j ? -1 : (i > j ? 1 : 0);
+}
+
+/* exponential disk (scale h, truncated at rmax) around (cx, cy), optional two-arm
+ * logarithmic spiral, circular velocity from the enclosed sample mass plus Gaussian
+ * dispersion disp * v_c per component, plus a bulk velocity */
+static void og_exp_disk(orc_rng* r, size_t n, double h, double rmax, double pitch_deg, double amp, double disp,
+                        double cx, double cy, double bvx, double bvy, float mn, float mx, float G, float* p, float* v,
+                        float* m) {
+    double* rad = (double*)malloc(n * sizeof(double));
+    double* phi = (double*)malloc(n * sizeof(double));
+    size_t* order = (size_t*)malloc(n * sizeof(size_t));
+    const double cot = 1.0 / tan(pitch_deg * ORC_PI / 180.0);
+    for (size_t i = 0; i < n; ++i) {
+        double rr;
+        do {
+            rr = -h * log(rng_uniform_open(r) * rng_uniform_open(r)); /* Gamma(2, h) */
+        } while (rr > rmax);
+        double ph;
+        if (amp > 0.0) {
+            for (;;) {
+                ph = 2.0 * ORC_PI * rng_uniform_open(r);
+                double f = 1.0 + amp * cos(2.0 * (ph - log(rr) * cot));
+                if (rng_uniform_open(r) * (1.0 + amp) <= f) break;
+            }
+        } else {
+            ph = 2.0 * ORC_PI * rng_uniform_open(r);
+        }
+        rad[i] = rr;
+        phi[i] = ph;
+        m[i] = mn + (mx - mn) * rng_uniform(r);
+        order[i] = i;
+    }
+    og_sort_key = rad;
+    qsort(order, n, sizeof(size_t), og_by_radius);
+    double enclosed = 0.0;
+    for (size_t q = 0; q < n; ++q) {
+        size_t i = order[q];
+        double rr = rad[i];
+        double vc = rr > 0.0 ? sqrt((double)G * enclosed / rr) : 0.0;
+        enclosed += m[i];
+        double c = cos(phi[i]), s = sin(phi[i]);
+        p[2 * i] = (float)(cx + rr * c);
+        p[2 * i + 1] = (float)(cy + rr * s);
+        double vx = -s * vc + disp * vc * rng_normal(r) + bvx;
+        double vy = c * vc + disp * vc * rng_normal(r) + bvy;
+        v[2 * i] = (float)vx;
+        v[2 * i + 1] = (float)vy;
+    }
+    free(rad);
+    free(phi);
+    free(order);
+}
+
+int orc_generate(int type, uint64_t count, float size, float mn, float mx, float G, uint64_t seed, float* pos,
+                 float* vel, float* mass) {
+    if (!count || !pos || !vel || !mass) return -1;
+    orc_rng r = {seed};
+    switch (type) {
+        case 0: og_random(&r, count, size, mn, mx, pos, vel, mass); break;
+        case 1: og_galaxy(&r, count, size, mn, mx, G, pos, vel, mass); break;
+        case 2: og_collision(&r, count, size, mn, mx, G, pos, vel, mass); break;
+        case 3:
+            if (count & 1) return -1;
+            og_symmetric(&r, count, size, mn, mx, G, pos, vel, mass);
+            break;
+        case 16: og_uniform_disk(&r, count, size, mn, mx, pos, vel, mass); break;
+        case 17: /* scale 30, radius 100 confines, pitch 15 deg, amplitude 0.3, 5% dispersion */
+            og_exp_disk(&r, count, 30.0 * size / 100.0, size, 15.0, 0.3, 0.05, 0.0, 0.0, 0.0, 0.0, mn, mx, G, pos, vel,
+                        mass);
+            break;
+        case 18: { /* two disks, scale 20, truncated at r <= 50, at (+-50, 0), v = (0, +-3) */
+            size_t h = count / 2;
+            og_exp_disk(&r, h, 20.0, 50.0, 15.0, 0.0, 0.0, -50.0, 0.0, 0.0, -3.0, mn, mx, G, pos, vel, mass);
+            og_exp_disk(&r, count - h, 20.0, 50.0, 15.0, 0.0, 0.0, 50.0, 0.0, 0.0, 3.0, mn, mx, G, pos + 2 * h,
+                        vel + 2 * h, mass + h);
+            break;
+        }
+        default: return -1;
+    }
     return 0;
 }

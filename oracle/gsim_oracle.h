@@ -78,6 +78,10 @@ typedef struct orc_bh_out {
     float* amag_out;         /* [n_al] |a| of this step (written when not NULL) */
     /* input of the bounding-box mode */
     uint32_t key_bits;       /* bits per axis, 1..15 (0: 12, 24-bit keys; 15: 30-bit keys) */
+    /* optional outputs of the group walk: records tested and interactions of each group
+     * of 64 sorted slots (n_al / 64 entries, estimate walk included) */
+    uint32_t* group_visits;
+    uint64_t* group_interactions;
 } orc_bh_out;
 
 /* Direct sum, SimShader.comp order: for every i, sum j = 0 .. n-1 in order. */
@@ -126,6 +130,11 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
                           float* mass_in, float* pos_out, float* vel_out, float* mass_out,
                           float dt, float G, float eps2, float theta2, orc_bh_out* out,
                           int nthreads);
+
+/* The library's seeded generators (gs_generate types 0-3, 16-18), restated: the same
+ * particles for the same arguments.  Returns 0, or -1 for an unknown type or bad count. */
+int orc_generate(int type, uint64_t count, float size, float mn, float mx, float G, uint64_t seed, float* pos,
+                 float* vel, float* mass);
 
 /* Upper bound on preorder records for n_al particles in either mode. */
 uint64_t orc_bh_node_capacity(int box_mode, uint32_t n_al);

@@ -33,7 +33,7 @@ class BHOut(C.Structure):
                 ("box_radius0", C.c_float), ("build_seconds", C.c_double), ("walk_seconds", C.c_double),
                 ("max_stack", C.c_uint32), ("max_warp_interactions", C.c_uint64),
                 ("rel_alpha", C.c_float), ("rel_floor2", C.c_float), ("amag_in", _FP), ("amag_out", _FP),
-                ("key_bits", C.c_uint32)]
+                ("key_bits", C.c_uint32), ("group_visits", _UP), ("group_interactions", C.POINTER(C.c_uint64))]
 
 
 _lib = None
@@ -66,12 +66,25 @@ def lib():
         L.orc_energy_f64.restype = C.c_double
         L.orc_render_points.argtypes = [C.c_uint32, _FP, _FP, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint8)]
         L.orc_render_points.restype = None
+        L.orc_generate.argtypes = [C.c_int, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_uint64,
+                                   _FP, _FP, _FP]
+        L.orc_generate.restype = C.c_int
         _lib = L
     return _lib
 
 
 def _fp(a):
     return a.ctypes.data_as(_FP)
+
+
+def generate(kind, n, size=100.0, min_mass=1.0, max_mass=10.0, G=1.0, seed=1):
+    """The library's seeded generators restated on the CPU: pos (n, 2), vel (n, 2), mass (n,)."""
+    pos = np.empty((n, 2), np.float32)
+    vel = np.empty((n, 2), np.float32)
+    mass = np.empty(n, np.float32)
+    if lib().orc_generate(kind, n, size, min_mass, max_mass, G, seed, _fp(pos), _fp(vel), _fp(mass)) != 0:
+        raise ValueError("orc_generate: unknown generator type or bad count")
+    return pos, vel, mass
 
 
 def pad_state(pos, vel, mass, align=64):
@@ -144,7 +157,7 @@ def direct_accel_f64(pos, mass, softening=0.2, targets=None, threads=os.cpu_coun
 
 def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, G=1.0, softening=0.2, theta=1.0,
             keep_tree=True, threads=os.cpu_count(), walk_stride=1, flags=0, rel_alpha=0.0, rel_floor=None,
-            key_bits=0, amag_in=None):
+            key_bits=0, amag_in=None, group_stats=False):
     """One Barnes-Hut step; returns a dict with keys, sorted_src and the preorder records.
     key_bits: bounding-box cells per axis as a power of two (0: 12).  amag_in: the previous
     |a| per particle to use instead of the state's own (relative criterion)."""
@@ -155,6 +168,12 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
     out = BHOut()
     out.walk_stride = walk_stride
     out.key_bits = key_bits
+    gv = gi = None
+    if group_stats:  # records tested and interactions of each group of 64 (group walk)
+        gv = np.zeros(n_al // 64, np.uint32)
+        gi = np.zeros(n_al // 64, np.uint64)
+        out.group_visits = gv.ctypes.data_as(_UP)
+        out.group_interactions = gi.ctypes.data_as(C.POINTER(C.c_uint64))
     amag_out = None
     if amag_in is not None:
         state.amag = np.ascontiguousarray(amag_in, np.float32).copy()
@@ -202,6 +221,8 @@ def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, 
                build_seconds=out.build_seconds, walk_seconds=out.walk_seconds, max_stack=out.max_stack,
                max_warp_interactions=out.max_warp_interactions,
                box=(out.box_center_x, out.box_center_y, out.box_scale, out.box_radius0))
+    if group_stats:
+        res.update(group_visits=gv, group_interactions=gi)
     return res
 
 
