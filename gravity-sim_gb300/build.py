@@ -20,7 +20,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", "-I" + INCLUDE]
-CUDA_SOURCES = ["direct.cu", "bh.cu", "sim.cu", "batch.cu", "serve.cu", "render.cu"]
+CUDA_SOURCES = ["force_fast.cu", "force_exact.cu", "bh.cu", "direct.cu", "sim.cu", "batch.cu", "serve.cu",
+                "render.cu", "tune.cu"]
 CXX_SOURCES = ["host.cpp"]
 
 

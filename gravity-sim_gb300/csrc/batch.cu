@@ -55,6 +55,7 @@ gs_status check_batch_members(gs_sim* const* sims, size_t count, const char* who
 
 cudaError_t BatchEngine::init(int dev) {
     device = dev;
+    gs_shape_defaults(&shape);
     cudaError_t e = cudaSetDevice(dev);
     if (e == cudaSuccess) e = keep_pool_memory(dev);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&root, cudaStreamNonBlocking);
@@ -94,6 +95,12 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
     });
     const size_t n = order.size();
     BatchPlan p;
+    p.shape = shape;
+    // the counting kernels exist for the default shape only (2 group walks per block)
+    bool counting = false;
+    for (const gs_sim* s : order)
+        if (s->p.algorithm == GS_BARNES_HUT && (s->p.flags & GS_FLAG_COUNT_INTERACTIONS)) counting = true;
+    const uint32_t force_warps = counting ? 2u : shape.force_warps;
     std::vector<SysDesc> descs(n);
     std::vector<uint32_t> blocks(n * kTabCount, 0u);
     parity0.assign(n, 0);
@@ -116,11 +123,11 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
         d.hdt = 0.5f * s->dt_eff;
         parity0[i] = s->in;
         if (s->p.algorithm == GS_BARNES_HUT) {
-            bh_batch_desc(s, d, &blocks[i * kTabCount]);
+            bh_batch_desc(s, d, &blocks[i * kTabCount], shape, force_warps);
             bh_set_final_keys(s);
             ++p.n_bh;
         } else {
-            direct_batch_desc(s, d, &blocks[i * kTabCount]);
+            direct_batch_desc(s, d, &blocks[i * kTabCount], shape);
             ++p.n_direct;
         }
     }
@@ -190,11 +197,7 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
     p.count = bh0 && (bh0->p.flags & GS_FLAG_COUNT_INTERACTIONS);
     p.direct_exact = dir0 && dir0->p.math_mode == GS_MATH_REFERENCE;
     p.direct_plain = dir0 && (dir0->p.flags & GS_FLAG_PLAIN_SUM);
-    if (bh0) {
-        const int variant = (p.group ? 1 : 0) | (p.exact ? 2 : 0) | (p.quad ? 4 : 0) | (p.count ? 8 : 0);
-        if (!force_grid_cache[variant]) force_grid_cache[variant] = bh_batch_force_grid(p);
-        p.force_grid = force_grid_cache[variant];
-    }
+    if (bh0) p.force_grid = bh_batch_force_grid(p);  // resident blocks of the persistent force launch
     plan = p;
     cur = k;
     step = 0;
@@ -289,6 +292,20 @@ void free_batch(gs_batch* b) {
 
 }  // namespace
 
+namespace gsim {
+gs_status batch_key(gs_batch* b, gs_params* params, uint64_t* total) {
+    const gs_sim* first_bh = nullptr;
+    uint64_t sum = 0;
+    for (const gs_sim* s : b->sims) {
+        sum += s->n;
+        if (!first_bh && s->p.algorithm == GS_BARNES_HUT) first_bh = s;
+    }
+    *params = first_bh ? first_bh->p : b->sims[0]->p;
+    *total = sum;
+    return GS_OK;
+}
+}  // namespace gsim
+
 extern "C" {
 
 gs_status gs_batch_create(gs_sim* const* sims, uint32_t count, uint32_t flags, gs_batch** out) {
@@ -318,6 +335,12 @@ gs_status gs_batch_create(gs_sim* const* sims, uint32_t count, uint32_t flags, g
         free_batch(b);
         return st;
     }
+    {  // the batch's launch shape: the tuned entry of its total particles, else the defaults
+        gs_params kp;
+        uint64_t total = 0;
+        st = batch_key(b, &kp, &total);
+        if (st == GS_OK) batch_shape_for(&kp, total, &b->eng.shape);
+    }
     st = b->eng.set_members(b->sims);
     if (st != GS_OK) {
         free_batch(b);
@@ -325,6 +348,31 @@ gs_status gs_batch_create(gs_sim* const* sims, uint32_t count, uint32_t flags, g
     }
     *out = b;
     return GS_OK;
+}
+
+gs_status gs_batch_get_shape(gs_batch* b, gs_shape* out) {
+    if (!b || !out) return fail("gs_batch_get_shape: NULL argument");
+    *out = b->eng.shape;
+    return GS_OK;
+}
+
+gs_status gs_batch_set_shape(gs_batch* b, const gs_shape* sh) {
+    if (!b || !sh) return fail("gs_batch_set_shape: NULL argument");
+    std::string why;
+    if (!shape_valid(*sh, &why)) return fail("gs_batch_set_shape: " + why);
+    GS_CUDA(cudaSetDevice(b->eng.device));
+    if (b->pending) {  // the step graphs may still run: wait before dropping them
+        gs_status w = wait_event(b->done, 0);
+        if (w != GS_OK) return w;
+    }
+    drop_graphs(b);
+    b->eng.shape = *sh;
+    for (gs_sim* s : b->sims)  // a direct-sum member keeps its own j-split: it must fit its scratch
+        if (s->p.algorithm == GS_DIRECT_SUM && direct_chunks_needed(s, s->shape) > s->direct_max_chunks) {
+            set_error("gs_batch_set_shape: a member's j-split does not fit its scratch");
+            return GS_ERR_CAPACITY;
+        }
+    return b->eng.set_members(b->sims);
 }
 
 gs_status gs_batch_run(gs_batch* b, uint32_t steps) {

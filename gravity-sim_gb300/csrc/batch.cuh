@@ -25,7 +25,7 @@ struct BatchEngine {
     void* h_stage[2] = {nullptr, nullptr};
     size_t h_bytes[2] = {0, 0};
     cudaEvent_t staged[2] = {nullptr, nullptr};  // the copy out of staging k is done
-    int force_grid_cache[16] = {};               // persistent force grid by force-kernel variant
+    gs_shape shape{};                            // launch shapes of the batched kernels
 
     cudaError_t init(int dev);
     void destroy();

@@ -32,30 +32,10 @@
 #include <cstdio>
 #include <cstring>
 
-#include "internal.cuh"
+#include "bh_common.cuh"
 
 namespace gsim {
 namespace {
-
-// Every stage is written as a __device__ body that takes its block's index and the
-// number of blocks working on its system.  A plain launch passes blockIdx.x / gridDim.x;
-// a batched launch (one grid over many systems) passes the block's index within its
-// system.  No body's result depends on how many blocks it gets, so a system computes the
-// same bits alone and in a batch.
-struct Blk {
-    uint32_t id, count;
-};
-__device__ __forceinline__ Blk grid_blk() { return Blk{blockIdx.x, gridDim.x}; }
-
-// Programmatic dependent launch: every step kernel lets the next launch in its stream
-// start as soon as all of its blocks have begun, then waits until the kernel before it
-// has finished and its writes are visible.  Each kernel therefore still runs strictly
-// after its predecessor (and transitively after all earlier ones); only the launch
-// latency between them is hidden.  Without the launch attribute both are no-ops.
-__device__ __forceinline__ void pdl_enter() {
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-}
 
 // ------------------------------------------------------------------------------------
 // keys
@@ -316,17 +296,6 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_
     return r;
 }
 
-__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
-    return *((volatile const uint32_t*)p);
-}
-
-// Acquire load of a barrier counter.
-__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
 // Barrier over every block of a cooperative launch (all blocks are co-resident, so
 // every block reaches it).  Block leaders count arrivals on `bar` and wait for `target`;
 // the wait is bounded, and a block that gives up sets the error flag, which makes the
@@ -355,29 +324,6 @@ __device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, int* e
     }
     __syncthreads();
     return s_ok != 0;
-}
-
-// The extent {min x, max x, min y, max y} of a state set from its ordered words.
-__device__ __forceinline__ float4 ext_decode(const uint32_t* __restrict__ ext) {
-    return make_float4(__uint_as_float(ord_bits(__ldcg(ext + 0))), __uint_as_float(ord_bits(~__ldcg(ext + 1))),
-                       __uint_as_float(ord_bits(__ldcg(ext + 2))), __uint_as_float(ord_bits(~__ldcg(ext + 3))));
-}
-
-// Adds min/max of positions to a state set's extent words: a warp reduction (fminf/fmaxf
-// skip NaN), then one atomic per word from lane 0.  Every lane of the warp must call it.
-__device__ __forceinline__ void ext_add(uint32_t* __restrict__ ext, float mnx, float mxx, float mny, float mxy) {
-    for (int o = 16; o; o >>= 1) {
-        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
-        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
-        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
-        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMin(ext + 0, ord_word(__float_as_uint(mnx)));
-        atomicMin(ext + 1, ~ord_word(__float_as_uint(mxx)));
-        atomicMin(ext + 2, ord_word(__float_as_uint(mny)));
-        atomicMin(ext + 3, ~ord_word(__float_as_uint(mxy)));
-    }
 }
 
 // Keys in bounding-box mode.  The extent of the input positions was gathered while they
@@ -409,13 +355,14 @@ k_ext_keys(float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos
 // ------------------------------------------------------------------------------------
 // Tiles are taken from a per-system ticket, so a tile only waits on tiles that earlier
 // running blocks took: no deadlock, whichever grid the blocks belong to.
-template <bool IDENTITY>
+// KPT keys per thread: tiles of 256 * KPT keys; LB: look-back width.
+template <bool IDENTITY, int KPT, int LB>
 __device__ __forceinline__ void sort_pass_body(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
                                                int shift, const uint32_t* __restrict__ hist,
                                                uint32_t* __restrict__ status, uint32_t* __restrict__ ticket,
                                                int* __restrict__ err) {
-    constexpr int KPT = kSortKeysPerThread;
+    constexpr int kSortTile = kSortThreads * KPT;
     constexpr int W = kSortThreads / 32;
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_whist[W][256];
@@ -462,9 +409,10 @@ __device__ __forceinline__ void sort_pass_body(const uint32_t* __restrict__ kin,
         s_whist[w][t] = tot;
         tot += c;
     }
-    // decoupled look-back over earlier tiles for digit t, kLookback tiles per round trip:
-    // the aggregates are added nearest first up to the first inclusive prefix; a tile not
-    // yet published ends the window, and the next window starts there
+    // decoupled look-back over earlier tiles for digit t, LB tiles per round trip: the
+    // aggregates are added nearest first up to the first inclusive prefix; a tile not yet
+    // published ends the window, and the next window starts there.  Tile t resolves about
+    // t / LB round trips after tile 0, so the window width sets the pass's latency.
     uint32_t excl = 0;
     uint32_t* st = status + (size_t)tile * 256 + t;
     if (tile == 0) {
@@ -474,14 +422,14 @@ __device__ __forceinline__ void sort_pass_body(const uint32_t* __restrict__ kin,
         int64_t p = (int64_t)tile - 1;
         uint32_t spins = 0;
         while (p >= 0) {
-            uint32_t w[kLookback];
+            uint32_t w[LB];
 #pragma unroll
-            for (int k = 0; k < kLookback; ++k)
+            for (int k = 0; k < LB; ++k)
                 w[k] = p - k >= 0 ? ld_volatile(status + (size_t)(p - k) * 256 + t) : (2u << 30);
             bool stop = false, done = false;
             int used = 0;
 #pragma unroll
-            for (int k = 0; k < kLookback; ++k) {
+            for (int k = 0; k < LB; ++k) {
                 if (stop) continue;
                 const uint32_t f = w[k] >> 30;
                 if (f == 0u) {
@@ -493,7 +441,7 @@ __device__ __forceinline__ void sort_pass_body(const uint32_t* __restrict__ kin,
                 }
             }
             if (done) break;
-            if (used < kLookback && ++spins > kSpinLimit) {
+            if (used < LB && ++spins > kSpinLimit) {
                 atomicOr(err, kErrSortWait);
                 break;
             }
@@ -529,18 +477,41 @@ __device__ __forceinline__ void sort_pass_body(const uint32_t* __restrict__ kin,
     }
 }
 
-template <bool IDENTITY>
+template <bool IDENTITY, int KPT, int LB>
 __global__ void __launch_bounds__(kSortThreads)
 k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
             uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
             uint32_t* __restrict__ status, uint32_t* __restrict__ ticket, int* __restrict__ err) {
     pdl_enter();
-    sort_pass_body<IDENTITY>(kin, vin, kout, vout, n, shift, hist, status, ticket, err);
+    sort_pass_body<IDENTITY, KPT, LB>(kin, vin, kout, vout, n, shift, hist, status, ticket, err);
+}
+
+// radix pass kernel of a tile size and look-back width (first pass: values are the identity)
+using SortPassFn = void (*)(const uint32_t*, const uint32_t*, uint32_t*, uint32_t*, uint32_t, int, const uint32_t*,
+                            uint32_t*, uint32_t*, int*);
+template <int KPT>
+SortPassFn sort_pass_kernel_kpt(bool identity, uint32_t lb) {
+    switch (lb) {
+        case 8: return identity ? k_sort_pass<true, KPT, 8> : k_sort_pass<false, KPT, 8>;
+        case 16: return identity ? k_sort_pass<true, KPT, 16> : k_sort_pass<false, KPT, 16>;
+        default: return identity ? k_sort_pass<true, KPT, 32> : k_sort_pass<false, KPT, 32>;
+    }
+}
+SortPassFn sort_pass_kernel(bool identity, const gs_shape& sh) {
+    return sh.sort_keys_per_thread == 8 ? sort_pass_kernel_kpt<8>(identity, sh.sort_lookback)
+                                        : sort_pass_kernel_kpt<16>(identity, sh.sort_lookback);
+}
+// radix-sort tiles of n keys under a shape
+inline uint32_t sort_tiles_of(uint64_t n, const gs_shape& sh) {
+    const uint64_t tile = (uint64_t)kSortThreads * (sh.sort_keys_per_thread == 8 ? 8 : 16);
+    return (uint32_t)((n + tile - 1) / tile);
 }
 
 // ------------------------------------------------------------------------------------
 // internal nodes per slot + exclusive scan (decoupled look-back)
 // ------------------------------------------------------------------------------------
+// R: earlier tiles each lane of the look-back warp reads per round trip (32 R per warp).
+template <int R>
 __device__ __forceinline__ void meta_scan_body(const uint32_t* __restrict__ skey, uint32_t n_items,
                                                const uint32_t* __restrict__ valid_count, int D,
                                                uint32_t* __restrict__ E, uint32_t* __restrict__ status,
@@ -566,7 +537,7 @@ __device__ __forceinline__ void meta_scan_body(const uint32_t* __restrict__ skey
     }
     uint32_t total;
     uint32_t texcl = block_exclusive_scan_256(sum, s_warp, total);
-    if (t < 32) {  // warp 0: publish, then look back over 32 earlier tiles per round trip
+    if (t < 32) {  // warp 0: publish, then look back over 32 R earlier tiles per round trip
         uint32_t excl = 0;
         uint32_t* st = status + tile;
         if (tile == 0) {
@@ -576,25 +547,35 @@ __device__ __forceinline__ void meta_scan_body(const uint32_t* __restrict__ skey
             int64_t p = (int64_t)tile - 1;
             uint32_t spins = 0;
             while (p >= 0) {  // every value below is uniform over the warp
-                const int64_t q = p - t;  // lane t reads the t-th tile back
-                const uint32_t w = q >= 0 ? ld_volatile(status + q) : (2u << 30);
-                const uint32_t f = w >> 30;
-                const uint32_t stopm = __ballot_sync(0xffffffffu, f != 1u);  // unpublished or inclusive
-                const int k = stopm ? __ffs(stopm) - 1 : 32;
-                const uint32_t kf = __shfl_sync(0xffffffffu, f, k & 31);
-                const bool inclusive = k < 32 && kf == 2u;
-                // the aggregates nearer than lane k, and lane k's value if it is inclusive
-                excl += __reduce_add_sync(0xffffffffu, (t < k || (t == k && inclusive)) ? (w & 0x3fffffffu) : 0u);
-                if (inclusive) break;
-                if (k < 32) {  // tile p - k has not published yet: wait for it
-                    if (++spins > kSpinLimit) {
-                        if (t == 0) atomicOr(err, kErrScanWait);
-                        break;
-                    }
-                    p -= k;
-                } else {
-                    p -= 32;
+                uint32_t w[R];
+#pragma unroll
+                for (int r = 0; r < R; ++r) {  // lane t reads the (32 r + t)-th tile back
+                    const int64_t q = p - 32 * r - t;
+                    w[r] = q >= 0 ? ld_volatile(status + q) : (2u << 30);
                 }
+                bool done = false, wait = false;
+                int64_t used = 0;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {  // nearest 32 first
+                    if (done || wait) continue;
+                    const uint32_t f = w[r] >> 30;
+                    const uint32_t stopm = __ballot_sync(0xffffffffu, f != 1u);  // unpublished or inclusive
+                    const int k = stopm ? __ffs(stopm) - 1 : 32;
+                    const uint32_t kf = __shfl_sync(0xffffffffu, f, k & 31);
+                    const bool inclusive = k < 32 && kf == 2u;
+                    // the aggregates nearer than lane k, and lane k's value if it is inclusive
+                    excl += __reduce_add_sync(0xffffffffu,
+                                              (t < k || (t == k && inclusive)) ? (w[r] & 0x3fffffffu) : 0u);
+                    if (inclusive) done = true;
+                    else if (k < 32) wait = true;  // tile p - used - k has not published yet
+                    used += inclusive ? 0 : k;
+                }
+                if (done) break;
+                if (wait && ++spins > kSpinLimit) {
+                    if (t == 0) atomicOr(err, kErrScanWait);
+                    break;
+                }
+                p -= used;
             }
             if (t == 0) atomicExch(st, (2u << 30) | (excl + total));
         }
@@ -611,12 +592,16 @@ __device__ __forceinline__ void meta_scan_body(const uint32_t* __restrict__ skey
     }
 }
 
+template <int R>
 __global__ void __launch_bounds__(kScanThreads)
 k_meta_scan(const uint32_t* __restrict__ skey, uint32_t n_items, const uint32_t* __restrict__ valid_count,
             int D, uint32_t* __restrict__ E, uint32_t* __restrict__ status, uint32_t* __restrict__ ticket,
             uint32_t* __restrict__ internal_count, int* __restrict__ err) {
     pdl_enter();
-    meta_scan_body(skey, n_items, valid_count, D, E, status, ticket, internal_count, err);
+    meta_scan_body<R>(skey, n_items, valid_count, D, E, status, ticket, internal_count, err);
+}
+inline auto meta_scan_kernel(uint32_t lookback) {
+    return lookback >= 128 ? k_meta_scan<4> : lookback >= 64 ? k_meta_scan<2> : k_meta_scan<1>;
 }
 
 // ------------------------------------------------------------------------------------
@@ -638,13 +623,6 @@ __device__ __forceinline__ uint32_t cell_end(const uint32_t* k, uint32_t a, uint
     }
     return a;
 }
-
-// Child descriptors of an internal record: up to four children in Morton order, each a
-// record index with kKidLeaf set for a particle leaf, kKidNone when absent; a
-// finest-level cell stores {kKidFinest, first leaf, leaf count, -}.
-constexpr uint32_t kKidNone = 0xFFFFFFFFu;
-constexpr uint32_t kKidFinest = 0xFFFFFFFEu;
-constexpr uint32_t kKidLeaf = 0x80000000u;
 
 // record index of the particle leaf of sorted slot t
 __device__ __forceinline__ uint32_t leaf_of(const uint32_t* skey, const uint32_t* E, uint32_t t, uint32_t nv, int D) {
@@ -1007,551 +985,7 @@ k_coop_sums(const uint32_t* __restrict__ level_count, const uint32_t* __restrict
         top_sums_body<QUAD>(level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, quad, safe, bbox_mode, bpp);
 }
 
-// ------------------------------------------------------------------------------------
-// traversal + integrator (ForceShader.comp:78-152)
-// ------------------------------------------------------------------------------------
-constexpr int kForceWarps = 4;
-
-template <bool EXACT, bool COUNT>
-__device__ __forceinline__ void force_body(Blk blk, const uint32_t* __restrict__ sidx,
-                                           const uint32_t* __restrict__ counts, const float4* __restrict__ rec,
-                                           const uint32_t* __restrict__ skip, const float2* __restrict__ pos_in,
-                                           const float2* __restrict__ vel_in, float2* __restrict__ pos_out,
-                                           float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
-                                           float eps2, float theta2, float k, float hdt, uint32_t cap,
-                                           unsigned long long* __restrict__ stat, uint32_t* __restrict__ ext) {
-    __shared__ float4 wrec[kForceWarps][32];
-    __shared__ uint32_t wskip[kForceWarps][32];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t group = blk.id * kForceWarps + warp;
-    const uint32_t nv = counts[0];
-    const uint32_t T = min(nv + counts[1], cap);  // preorder records
-    if (group * 32 >= nv) return;       // no particle in this warp: nothing to write
-    const uint32_t s = group * 32 + lane;
-    const uint32_t i = s < nv ? sidx[s] : 0u;
-    const bool valid = s < nv && i < n_al;  // i < n_al unless the sort failed (error flag set)
-    const float2 p = valid ? pos_in[i] : make_float2(0.0f, 0.0f);
-    float ax = 0.0f, ay = 0.0f;
-    unsigned long long n_acc = 0, n_vis = 0;
-    uint32_t base = 0, ind = 0;
-    wrec[warp][lane] = rec[lane];
-    wskip[warp][lane] = skip[lane];
-    __syncwarp();
-    while (ind < T) {
-        if (ind - base >= 32u) {  // warp-uniform: reload the 32-record window
-            base = ind & ~31u;
-            __syncwarp();
-            wrec[warp][lane] = rec[base + lane];
-            wskip[warp][lane] = skip[base + lane];
-            __syncwarp();
-        }
-        const float4 q = wrec[warp][ind - base];
-        const float dx = q.x - p.x, dy = q.y - p.y;
-        const float d2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
-        const bool ok = !valid || q.w <= d2 * theta2;
-        if (COUNT) ++n_vis;
-        if (__all_sync(0xffffffffu, ok)) {
-            const float r = EXACT ? __fdiv_rn(1.0f, __fsqrt_rn(d2)) : rsqrtf(d2);
-            const float sc = ((q.z * r) * r) * r;
-            ax = fmaf(dx, sc, ax);
-            ay = fmaf(dy, sc, ay);
-            if (COUNT) n_acc += valid;
-            ind += max(wskip[warp][ind - base], 1u);  // >= 1: the walk always advances
-        } else {
-            ++ind;
-        }
-    }
-    if (COUNT) {
-        for (int o = 16; o; o >>= 1) n_acc += __shfl_xor_sync(0xffffffffu, n_acc, o);
-        if (lane == 0) {
-            atomicAdd(&stat[0], n_acc);
-            atomicAdd(&stat[1], n_vis);
-        }
-    }
-    float2 np = make_float2(0.0f, 0.0f);
-    if (valid) {
-        if (acc_rec) acc_rec[i] = make_float2(ax, ay);
-        const float2 v = vel_in[i];
-        const float nvx = fmaf(ax, k, v.x), nvy = fmaf(ay, k, v.y);  // ForceShader.comp:145-146
-        np = make_float2(fmaf(v.x + nvx, hdt, p.x), fmaf(v.y + nvy, hdt, p.y));
-        pos_out[i] = np;
-        vel_out[i] = make_float2(nvx, nvy);
-    }
-    if (ext)  // bounding-box mode: the next step's box
-        ext_add(ext, valid ? np.x : INFINITY, valid ? np.x : -INFINITY, valid ? np.y : INFINITY,
-                valid ? np.y : -INFINITY);
-}
-
-template <bool EXACT, bool COUNT>
-__global__ void __launch_bounds__(kForceWarps * 32)
-k_force(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ counts, const float4* __restrict__ rec,
-        const uint32_t* __restrict__ skip, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
-        float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec, uint32_t n_al,
-        float eps2, float theta2, float k, float hdt, uint32_t cap, unsigned long long* __restrict__ stat,
-        uint32_t* __restrict__ ext) {
-    pdl_enter();
-    force_body<EXACT, COUNT>(grid_blk(), sidx, counts, rec, skip, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al,
-                             eps2, theta2, k, hdt, cap, stat, ext);
-}
-
-// ------------------------------------------------------------------------------------
-// accurate-mode traversal (no counterpart in the reference): the 64 particles of 64
-// consecutive sorted slots share one walk, run by one warp (two particles per lane); 32
-// records are tested at once (one per lane) against the bounding boxes of the group;
-// accepted nodes and runs of particle leaves are collected and every lane then sums them
-// for its two particles with packed f32x2 instructions (quadrupole term for nodes).
-// ------------------------------------------------------------------------------------
-constexpr int kGroupWarps = 2;
-constexpr int kGroupSize = 64;  // particles per walk
-// Records still to test.  Pops take the top 32 and push at most four internal children
-// each, one level deeper, so the stack holds at most one block of <= 128 entries per level
-// and blocks of strictly increasing level: <= 96 * D + 128 = 1568 for D = 15.  Overflow
-// is still checked and reported.
-constexpr int kStackCap = 1568;
-static_assert(kStackCap >= 96 * (kBBoxMaxBits > kFixedDepth ? kBBoxMaxBits : kFixedDepth) + 128, "walk stack bound");
-constexpr int kItemCap = 128;     // runs of particle leaves between evaluations
-constexpr int kNodeCap = 160;     // accepted nodes between evaluations
-
-// 1/sqrt: correctly rounded (REFERENCE math) or the hardware approximation (FAST math;
-// d2 >= eps^2 > 0 is never subnormal, so the flush-to-zero form loses nothing)
-__device__ __forceinline__ float rsqrt_fast(float x) {
-    float r;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
-template <bool EXACT>
-__device__ __forceinline__ float inv_sqrt(float d2) {
-    return EXACT ? __fdiv_rn(1.0f, __fsqrt_rn(d2)) : rsqrt_fast(d2);
-}
-
-// Evaluation order.  Each particle sums the accepted nodes and the particle leaves of its
-// walk separately, each in walk order, into a node and a leaf accumulator; its
-// acceleration is node + leaf.  How the warp batches its evaluations therefore does not
-// change a bit of the result.
-struct GroupSmem {
-    uint32_t stack[kStackCap];
-    uint32_t node[kNodeCap];      // accepted node records
-    uint32_t it_start[kItemCap];  // runs of particle leaves: first record
-    uint32_t it_count[kItemCap];  // record count
-    uint32_t off[kItemCap];       // exclusive record offsets of the runs
-    float cx[32], cy[32], cm[32];     // one chunk of gathered records: centre of mass (or particle), mass
-    float qxx[32], qxy[32], qyy[32], mt[32];  // node terms 7.5 S and -1.5 tr(S) of node records
-};
-
-// One record (x, y, m) on the lane's two particles (P = their x, Q = their y):
-// d = (x, y) - p, d2 = dx^2 + dy^2 + eps^2, a += d * (((m r) r) r) with r = 1/sqrt(d2),
-// the CPU restatement's pair_scale sequence, two particles at once.
-template <bool EXACT>
-__device__ __forceinline__ void monopole_x2(float x, float y, float m, float2 P, float2 Q, float2 E2, float2& acx,
-                                            float2& acy) {
-    const float2 dx = sub2(make_float2(x, x), P), dy = sub2(make_float2(y, y), Q);
-    const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
-    const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
-    const float2 sc = mul2(mul2(mul2(make_float2(m, m), r), r), r);
-    acx = fma2(dx, sc, acx);
-    acy = fma2(dy, sc, acy);
-}
-
-// One node with second moments on the lane's two particles.  The monopole and
-// quadrupole terms of the softened potential,
-//   a = d (m r^3 - 1.5 tr(S) r^5 + 7.5 (d.S.d) r^7) - 3 r^5 S d,   r = 1/sqrt(d2),
-// are evaluated as r^3 (d (m + r^2 (mt + r^2 u)) - 0.4 r^2 S'' d) with the node terms
-// S'' = 7.5 S and mt = -1.5 tr(S) formed once per node (eval_nodes): 21 operations per
-// particle instead of 23, the CPU restatement's sequence (quad_accumulate).
-template <bool EXACT>
-__device__ __forceinline__ void quadrupole_x2(float x, float y, float m, float qxx, float qxy, float qyy, float mt,
-                                              float2 P, float2 Q, float2 E2, float2& acx, float2& acy) {
-    const float2 dx = sub2(make_float2(x, x), P), dy = sub2(make_float2(y, y), Q);
-    const float2 d2 = fma2(dx, dx, fma2(dy, dy, E2));
-    const float2 r = make_float2(inv_sqrt<EXACT>(d2.x), inv_sqrt<EXACT>(d2.y));
-    const float2 r2 = mul2(r, r);
-    const float2 r3 = mul2(r2, r);
-    const float2 Sxx = make_float2(qxx, qxx), Sxy = make_float2(qxy, qxy), Syy = make_float2(qyy, qyy);
-    const float2 srx = fma2(Sxx, dx, mul2(Sxy, dy));
-    const float2 sry = fma2(Sxy, dx, mul2(Syy, dy));
-    const float2 u = fma2(dx, srx, mul2(dy, sry));
-    const float2 t = fma2(fma2(u, r2, make_float2(mt, mt)), r2, make_float2(m, m));
-    const float2 k = mul2(make_float2(-0.4f, -0.4f), r2);
-    const float2 ix = fma2(srx, k, mul2(dx, t));
-    const float2 iy = fma2(sry, k, mul2(dy, t));
-    acx = fma2(r3, ix, acx);
-    acy = fma2(r3, iy, acy);
-}
-
-// Sum the count accepted nodes (quadrupole term with QUAD) for the lane's two particles,
-// 32 at a time: lane l loads node l of the next chunk while the current one is summed.
-template <bool EXACT, bool QUAD>
-__device__ __forceinline__ void eval_nodes(GroupSmem& g, uint32_t count, const float4* __restrict__ rec,
-                                           const float4* __restrict__ quad, float2 P, float2 Q, float2 E2,
-                                           float2& acx, float2& acy, int lane) {
-    if (!count) return;
-    float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qq = q;
-    if ((uint32_t)lane < count) {
-        const uint32_t r = g.node[lane];
-        q = __ldg(&rec[r]);
-        if (QUAD) qq = __ldg(&quad[r]);
-    }
-    for (uint32_t f0 = 0; f0 < count; f0 += 32) {
-        const uint32_t m = min(count - f0, 32u);
-        g.cx[lane] = q.x;
-        g.cy[lane] = q.y;
-        g.cm[lane] = q.z;
-        if (QUAD) {
-            g.qxx[lane] = 7.5f * qq.x;
-            g.qxy[lane] = 7.5f * qq.y;
-            g.qyy[lane] = 7.5f * qq.z;
-            g.mt[lane] = -1.5f * (qq.x + qq.z);
-        }
-        __syncwarp();
-        const uint32_t fn = f0 + 32 + lane;
-        if (fn < count) {
-            const uint32_t r = g.node[fn];
-            q = __ldg(&rec[r]);
-            if (QUAD) qq = __ldg(&quad[r]);
-        }
-#pragma unroll 4
-        for (uint32_t j = 0; j < m; ++j) {
-            if (QUAD)
-                quadrupole_x2<EXACT>(g.cx[j], g.cy[j], g.cm[j], g.qxx[j], g.qxy[j], g.qyy[j], g.mt[j], P, Q, E2, acx,
-                                     acy);
-            else
-                monopole_x2<EXACT>(g.cx[j], g.cy[j], g.cm[j], P, Q, E2, acx, acy);
-        }
-        __syncwarp();
-    }
-}
-
-// Record f of the leaf runs (last run with off <= f).
-__device__ __forceinline__ float4 gather_leaf(const GroupSmem& g, uint32_t n_items, uint32_t f,
-                                              const float4* __restrict__ rec) {
-    uint32_t lo = 0, hi = n_items - 1;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        if (g.off[mid] <= f) lo = mid;
-        else hi = mid - 1;
-    }
-    return __ldg(&rec[g.it_start[lo] + (f - g.off[lo])]);
-}
-
-// Sum the particle leaves of the n_items runs as monopoles, 32 records at a time.
-template <bool EXACT>
-__device__ __forceinline__ void eval_leaves(GroupSmem& g, uint32_t n_items, const float4* __restrict__ rec,
-                                            float2 P, float2 Q, float2 E2, float2& acx, float2& acy, int lane) {
-    if (!n_items) return;
-    // exclusive record offsets of all runs: lane l owns runs [4l, 4l + 4)
-    uint32_t c4[kItemCap / 32], sum = 0;
-#pragma unroll
-    for (int t = 0; t < kItemCap / 32; ++t) {
-        const uint32_t it = lane * (kItemCap / 32) + t;
-        c4[t] = it < n_items ? g.it_count[it] : 0u;
-        sum += c4[t];
-    }
-    uint32_t x = sum;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
-    uint32_t run = x - sum;
-#pragma unroll
-    for (int t = 0; t < kItemCap / 32; ++t) {
-        g.off[lane * (kItemCap / 32) + t] = run;
-        run += c4[t];
-    }
-    __syncwarp();
-    float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if ((uint32_t)lane < total) q = gather_leaf(g, n_items, lane, rec);
-    for (uint32_t f0 = 0; f0 < total; f0 += 32) {
-        const uint32_t m = min(total - f0, 32u);
-        g.cx[lane] = q.x;
-        g.cy[lane] = q.y;
-        g.cm[lane] = q.z;
-        __syncwarp();
-        const uint32_t fn = f0 + 32 + lane;
-        if (fn < total) q = gather_leaf(g, n_items, fn, rec);
-#pragma unroll 4
-        for (uint32_t j = 0; j < m; ++j) monopole_x2<EXACT>(g.cx[j], g.cy[j], g.cm[j], P, Q, E2, acx, acy);
-        __syncwarp();
-    }
-}
-
-// ESTIMATE: the |a| estimate pass of the relative criterion.  A group whose particles all
-// have a previous |a| returns at once; any other group walks with the theta test and
-// writes only the |a| of its particles (no integration), which the following normal pass
-// then opens nodes by.
-template <bool EXACT, bool QUAD, bool COUNT, bool ESTIMATE>
-__device__ __forceinline__ void force_group_body(
-    Blk blk, GroupSmem& g, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ skey,
-    const uint32_t* __restrict__ counts, const float4* __restrict__ rec, const uint32_t* __restrict__ skip,
-    const float4* __restrict__ quad, const uint4* __restrict__ kids, const float2* __restrict__ pos_in,
-    const float2* __restrict__ vel_in, float2* __restrict__ pos_out, float2* __restrict__ vel_out,
-    float2* __restrict__ acc_rec, uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
-    unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha,
-    float floor2, uint32_t* __restrict__ ext) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t group = blk.id * kGroupWarps + warp;
-    const uint32_t nv = counts[0];
-    const uint32_t T = min(nv + counts[1], cap);
-    const uint32_t g0 = group * kGroupSize;
-    if (g0 >= nv || T == 0) return;
-    if (ESTIMATE && !amag) return;  // a batch member without the relative criterion
-    // particles: slot g0 + lane (.x of every pair) and g0 + 32 + lane (.y)
-    const uint32_t s0 = g0 + lane, s1 = s0 + 32;
-    const uint32_t i0 = s0 < nv ? sidx[s0] : 0u, i1 = s1 < nv ? sidx[s1] : 0u;
-    const bool v0 = s0 < nv && i0 < n_al, v1 = s1 < nv && i1 < n_al;  // i < n_al unless the sort failed
-    const float2 p0 = v0 ? pos_in[i0] : make_float2(0.0f, 0.0f);
-    const float2 p1 = v1 ? pos_in[i1] : make_float2(0.0f, 0.0f);
-    // Sub-boxes: the particles are split by their cell at the coarsest level where the
-    // first and last keys of the group differ, so a group that crosses a coarse Morton
-    // boundary is not given one box spanning the empty space between its ends.
-    const uint32_t kf = skey[g0], kl = skey[min(g0 + kGroupSize - 1, nv - 1)];
-    const int shift = kf == kl ? -1 : ((31 - __clz(kf ^ kl)) & ~1);
-    const int box0 = !v0 ? -1 : (shift < 0 ? 0 : (int)((skey[s0] >> shift) & 3u));
-    const int box1 = !v1 ? -1 : (shift < 0 ? 0 : (int)((skey[s1] >> shift) & 3u));
-    float bx0[4], bx1[4], by0[4], by1[4];
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        const bool in0 = box0 == b, in1 = box1 == b;
-        float x0 = fminf(in0 ? p0.x : INFINITY, in1 ? p1.x : INFINITY);
-        float x1 = fmaxf(in0 ? p0.x : -INFINITY, in1 ? p1.x : -INFINITY);
-        float y0 = fminf(in0 ? p0.y : INFINITY, in1 ? p1.y : INFINITY);
-        float y1 = fmaxf(in0 ? p0.y : -INFINITY, in1 ? p1.y : -INFINITY);
-        for (int o = 16; o; o >>= 1) {
-            x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
-            x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
-            y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
-            y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
-        }
-        bx0[b] = x0;
-        bx1[b] = x1;
-        by0[b] = y0;
-        by1[b] = y1;
-    }
-    // Relative criterion: the smallest previous |a| of the group, NaN when any is unknown
-    // (then the group takes the theta test).  Each group reads and rewrites only its own
-    // particles' |a|, so one buffer serves as input and output.
-    bool relative = false;
-    float tol2 = 0.0f;
-    if (amag) {
-        const float a0 = v0 ? amag[i0] : INFINITY, a1 = v1 ? amag[i1] : INFINITY;
-        const bool unknown = __any_sync(0xffffffffu, isnan(a0) || isnan(a1));
-        if (ESTIMATE && !unknown) return;  // warp-uniform: nothing to estimate
-        float amin = fminf(a0, a1);
-        for (int o = 16; o; o >>= 1) amin = fminf(amin, __shfl_xor_sync(0xffffffffu, amin, o));
-        relative = !ESTIMATE && !unknown;
-        const float tol = alpha * amin;
-        tol2 = tol * tol;
-    }
-    const float2 P = make_float2(p0.x, p1.x), Q = make_float2(p0.y, p1.y), E2 = make_float2(eps2, eps2);
-    // node and leaf accumulators of the two particles (.x particle 0, .y particle 1)
-    float2 anx = make_float2(0.0f, 0.0f), any = anx, alx = anx, aly = anx;
-    unsigned long long n_int = 0, n_test = 0, n_node = 0;
-    uint32_t size = 0, n_nodes = 0, n_items = 0;
-    if (skip[0] == 1u) {  // a single particle: the root is its leaf
-        if (lane == 0) {
-            g.it_start[0] = 0u;
-            g.it_count[0] = 1u;
-        }
-        n_items = 1;
-    } else {
-        if (lane == 0) g.stack[0] = 0u;
-        size = 1;
-    }
-    __syncwarp();
-
-    while (size > 0) {
-        if (n_nodes > (uint32_t)(kNodeCap - 32)) {
-            eval_nodes<EXACT, QUAD>(g, n_nodes, rec, quad, P, Q, E2, anx, any, lane);
-            n_nodes = 0;
-        }
-        if (n_items > (uint32_t)(kItemCap - 64)) {
-            eval_leaves<EXACT>(g, n_items, rec, P, Q, E2, alx, aly, lane);
-            n_items = 0;
-        }
-        const uint32_t np = min(size, 32u);
-        const uint32_t base = size - np;
-        const bool act = lane < (int)np;
-        const uint32_t n = act ? g.stack[base + lane] : 0u;
-        __syncwarp();
-        size = base;
-        if (COUNT) n_test += np;
-        uint32_t a0 = 0, c0 = 0, a1 = 0, c1 = 0, nl = 0, nn = 0;
-        uint32_t pu0 = 0, pu1 = 0, pu2 = 0, pu3 = 0, npu = 0;
-        if (act) {  // every stacked record is an internal node
-            const float4 q = rec[n];
-            const uint4 kd = kids[n];
-            float d2 = INFINITY;  // nearest sub-box; an empty one gives +inf
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const float ex = fmaxf(fmaxf(bx0[b] - q.x, q.x - bx1[b]), 0.0f);
-                const float ey = fmaxf(fmaxf(by0[b] - q.y, q.y - by1[b]), 0.0f);
-                d2 = fminf(d2, fmaf(ex, ex, fmaf(ey, ey, eps2)));
-            }
-            bool accept;
-            if (relative) {  // m^2 R^3 <= tol^2 D^5 with R <= D (R: squared opening radius), or theta
-                const float lhs = (q.z * q.z) * ((q.w * q.w) * q.w);
-                const float d4 = d2 * d2;
-                accept = (q.w <= d2 && lhs <= tol2 * ((d4 * d4) * d2)) || q.w <= d2 * floor2;
-            } else {
-                accept = q.w <= d2 * theta2;
-            }
-            if (accept) {
-                nn = 1;
-            } else if (kd.x == kKidFinest) {
-                a0 = kd.y;
-                c0 = kd.z;
-                nl = 1;
-            } else {
-                const uint32_t kk[4] = {kd.x, kd.y, kd.z, kd.w};
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    const uint32_t c = kk[t];
-                    if (c == kKidNone) continue;
-                    if (c & kKidLeaf) {
-                        const uint32_t r = c & ~kKidLeaf;
-                        if (nl == 1 && a0 + c0 == r) ++c0;        // extend the open run
-                        else if (nl == 2 && a1 + c1 == r) ++c1;
-                        else if (nl == 0) { a0 = r; c0 = 1; nl = 1; }
-                        else { a1 = r; c1 = 1; nl = 2; }
-                    } else {
-                        if (npu == 0) pu0 = c;
-                        else if (npu == 1) pu1 = c;
-                        else if (npu == 2) pu2 = c;
-                        else pu3 = c;
-                        ++npu;
-                    }
-                }
-            }
-        }
-        // offsets in lane order, three counts in one scan: nodes <= 32, runs <= 64 and
-        // pushes <= 128 in warp total, so the 8/8/16-bit fields never carry
-        const uint32_t mine = nn | (nl << 8) | (npu << 16);
-        uint32_t x = mine;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        const uint32_t ex = x - mine, tot = __shfl_sync(0xffffffffu, x, 31);
-        const uint32_t noff = ex & 0xffu, loff = (ex >> 8) & 0xffu, poff = ex >> 16;
-        const uint32_t ntot = tot & 0xffu, ltot = (tot >> 8) & 0xffu;
-        uint32_t ptot = tot >> 16;
-        if (size + ptot > (uint32_t)kStackCap) {  // beyond the depth bound: report, do not overrun
-            if (lane == 0) atomicOr(err, kErrTree);
-            ptot = 0;
-            npu = 0;
-        }
-        if (nn) g.node[n_nodes + noff] = n;
-        if (nl > 0) {
-            g.it_start[n_items + loff] = a0;
-            g.it_count[n_items + loff] = c0;
-        }
-        if (nl > 1) {
-            g.it_start[n_items + loff + 1] = a1;
-            g.it_count[n_items + loff + 1] = c1;
-        }
-        if (COUNT) {
-            n_int += nn + (nl > 0 ? c0 : 0u) + (nl > 1 ? c1 : 0u);
-            n_node += nn;
-        }
-        uint32_t* dst = g.stack + size + poff;
-        if (npu > 0) dst[0] = pu0;
-        if (npu > 1) dst[1] = pu1;
-        if (npu > 2) dst[2] = pu2;
-        if (npu > 3) dst[3] = pu3;
-
-        n_nodes += ntot;
-        n_items += ltot;
-        size += ptot;
-        __syncwarp();
-    }
-    eval_nodes<EXACT, QUAD>(g, n_nodes, rec, quad, P, Q, E2, anx, any, lane);
-    eval_leaves<EXACT>(g, n_items, rec, P, Q, E2, alx, aly, lane);
-    if (COUNT) {
-        if (skip[0] == 1u && lane == 0) n_int += 1;
-        for (int o = 16; o; o >>= 1) {
-            n_int += __shfl_xor_sync(0xffffffffu, n_int, o);
-            n_node += __shfl_xor_sync(0xffffffffu, n_node, o);
-        }
-        const unsigned long long nval = __popc(__ballot_sync(0xffffffffu, v0)) + __popc(__ballot_sync(0xffffffffu, v1));
-        if (lane == 0) {
-            atomicAdd(&stat[0], n_int * nval);
-            atomicAdd(&stat[1], n_test);
-            atomicAdd(&stat[2], n_node * nval);
-        }
-    }
-    const float2 ax = add2(anx, alx), ay = add2(any, aly);  // node + leaf, per particle
-    if (amag) {
-        if (v0) amag[i0] = __fsqrt_rn(fmaf(ax.x, ax.x, ay.x * ay.x));
-        if (v1) amag[i1] = __fsqrt_rn(fmaf(ax.y, ax.y, ay.y * ay.y));
-    }
-    if (ESTIMATE) return;
-    float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;  // of the new positions
-    if (v0) {
-        if (acc_rec) acc_rec[i0] = make_float2(ax.x, ay.x);
-        const float2 v = vel_in[i0];
-        const float nvx = fmaf(ax.x, k, v.x), nvy = fmaf(ay.x, k, v.y);
-        const float2 np = make_float2(fmaf(v.x + nvx, hdt, p0.x), fmaf(v.y + nvy, hdt, p0.y));
-        pos_out[i0] = np;
-        vel_out[i0] = make_float2(nvx, nvy);
-        mnx = fminf(mnx, np.x);
-        mxx = fmaxf(mxx, np.x);
-        mny = fminf(mny, np.y);
-        mxy = fmaxf(mxy, np.y);
-    }
-    if (v1) {
-        if (acc_rec) acc_rec[i1] = make_float2(ax.y, ay.y);
-        const float2 v = vel_in[i1];
-        const float nvx = fmaf(ax.y, k, v.x), nvy = fmaf(ay.y, k, v.y);
-        const float2 np = make_float2(fmaf(v.x + nvx, hdt, p1.x), fmaf(v.y + nvy, hdt, p1.y));
-        pos_out[i1] = np;
-        vel_out[i1] = make_float2(nvx, nvy);
-        mnx = fminf(mnx, np.x);
-        mxx = fmaxf(mxx, np.x);
-        mny = fminf(mny, np.y);
-        mxy = fmaxf(mxy, np.y);
-    }
-    if (ext) ext_add(ext, mnx, mxx, mny, mxy);  // bounding-box mode: the next step's box
-}
-
-template <bool EXACT, bool QUAD, bool COUNT, bool ESTIMATE>
-__global__ void __launch_bounds__(kGroupWarps * 32)
-k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ counts,
-              const float4* __restrict__ rec, const uint32_t* __restrict__ skip, const float4* __restrict__ quad,
-              const uint4* __restrict__ kids, const float2* __restrict__ pos_in, const float2* __restrict__ vel_in,
-              float2* __restrict__ pos_out, float2* __restrict__ vel_out, float2* __restrict__ acc_rec,
-              uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
-              unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha,
-              float floor2, uint32_t* __restrict__ ext) {
-    pdl_enter();
-    __shared__ GroupSmem smem[kGroupWarps];
-    force_group_body<EXACT, QUAD, COUNT, ESTIMATE>(grid_blk(), smem[threadIdx.x >> 5], sidx, skey, counts, rec, skip,
-                                                   quad, kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2,
-                                                   theta2, k, hdt, cap, stat, err, amag, alpha, floor2, ext);
-}
-
-// The group-walk kernel of a math mode / moments / counting / estimate combination (the
-// estimate pass exists only with quadrupoles, which the relative criterion needs).
-template <bool EST>
-auto force_group_kernel(bool exact, bool quad, bool count) {
-    if (EST) {
-        return exact ? (count ? k_force_group<true, true, true, EST> : k_force_group<true, true, false, EST>)
-                     : (count ? k_force_group<false, true, true, EST> : k_force_group<false, true, false, EST>);
-    }
-    return exact ? (quad ? (count ? k_force_group<true, true, true, EST> : k_force_group<true, true, false, EST>)
-                         : (count ? k_force_group<true, false, true, EST> : k_force_group<true, false, false, EST>))
-                 : (quad ? (count ? k_force_group<false, true, true, EST> : k_force_group<false, true, false, EST>)
-                         : (count ? k_force_group<false, false, true, EST> : k_force_group<false, false, false, EST>));
-}
-
 __global__ void k_set_params(BHParams* __restrict__ out, BHParams v) { *out = v; }
-
-int grid_for(uint64_t n, int threads) {
-    uint64_t b = (n + threads - 1) / threads;
-    if (b > 152ull * 16) b = 152ull * 16;
-    if (b < 1) b = 1;
-    return (int)b;
-}
 
 }  // namespace
 
@@ -1566,15 +1000,6 @@ uint64_t bh_capacity(int D, uint64_t n_al) {
     return c;
 }
 
-// counters layout inside the zeroed block
-// [kCtrStat..+5]: accepted interactions, records tested, node interactions (u64 each);
-// [kCtrLevel..+15]: internal nodes per level
-enum {
-    kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrLevel = 16,
-    kCtrBarrier = 32, kCtrCount = 40
-};
-static_assert(kHostCounters + kCtrCount <= kHostWords, "counter readback fits the pinned word block");
-
 // Lays the Barnes-Hut scratch out in the system's slab (sim_carve); while the system is
 // being sized (no slab yet) this only counts bytes.
 void bh_carve(gs_sim* s) {
@@ -1586,7 +1011,7 @@ void bh_carve(gs_sim* s) {
     // 30-bit keys), 20-bit keys + removal bit in the fixed box (3 passes)
     w.passes = bbox ? (2 * w.depth + 7) / 8 : 3;
     w.cap = bh_capacity(w.depth, n);
-    w.sort_tiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
+    w.sort_tiles = (uint32_t)((n + kSortThreads * 8 - 1) / (kSortThreads * 8));  // status for the smallest tiles
     w.scan_tiles = (uint32_t)((n + 1 + kScanTile - 1) / kScanTile);
     for (int b = 0; b < 2; ++b) {
         sim_carve(s, (void**)&w.keys[b], n * sizeof(uint32_t));
@@ -1644,52 +1069,10 @@ cudaError_t bh_init(gs_sim* s) {
             &per_sm, w.quad ? k_coop_sums<true> : k_coop_sums<false>, kCoopSumsThreads, 0);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     if (e == cudaSuccess && per_sm < 1) e = cudaErrorCooperativeLaunchTooLarge;
-    w.sums_grid = per_sm * sms;
+    w.sums_per_sm = per_sm;
+    w.sms = sms;
     return e;
 }
-
-namespace {
-// Launch `kernel` on `st`.  With `pdl` the launch may begin while the previous kernel in
-// the stream is still running; the kernel waits for it on entry (pdl_enter).
-template <typename... KArgs, typename... Args>
-cudaError_t launch(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3((unsigned)block);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
-
-// The same as a cooperative launch: every block of the grid is resident at once.
-template <typename... KArgs, typename... Args>
-cudaError_t launch_coop(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3((unsigned)block);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[2];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[1].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = pdl ? 2 : 1;
-    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
-}  // namespace
-
-#define GS_TRY_LAUNCH(call)                    \
-    do {                                       \
-        cudaError_t _e = (call);               \
-        if (_e != cudaSuccess) return _e;      \
-    } while (0)
 
 cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
     BHWork& w = s->bh;
@@ -1724,7 +1107,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
     for (int ps = 0; ps < w.passes; ++ps) {
         const int a = ps & 1, b = a ^ 1;
         uint32_t* status = w.sort_status + (size_t)ps * w.sort_tiles * 256;
-        GS_TRY_LAUNCH(launch(next_pdl(), ps == 0 ? k_sort_pass<true> : k_sort_pass<false>, (int)w.sort_tiles,
+        GS_TRY_LAUNCH(launch(next_pdl(), sort_pass_kernel(ps == 0, s->shape), (int)sort_tiles_of(n, s->shape),
                              kSortThreads, st, (const uint32_t*)w.keys[a], (const uint32_t*)(ps == 0 ? nullptr : w.idx[a]),
                              w.keys[b], w.idx[b], n, 8 * ps, (const uint32_t*)(w.hist + 256 * ps), status,
                              ctr + kCtrSort + ps, s->d_err));
@@ -1735,7 +1118,8 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
     const uint32_t* skey = w.keys[w.final_keys];
     const uint32_t* sidx = w.idx[w.final_keys];
     stage_begin(s, kStageScan, profile);
-    GS_TRY_LAUNCH(launch(next_pdl(), k_meta_scan, (int)w.scan_tiles, kScanThreads, st, skey, n + 1,
+    GS_TRY_LAUNCH(launch(next_pdl(), meta_scan_kernel(s->shape.scan_lookback), (int)w.scan_tiles, kScanThreads, st,
+                         skey, n + 1,
                          (const uint32_t*)(ctr + kCtrValid), w.depth, w.E, w.scan_status, ctr + kCtrScan,
                          ctr + kCtrInternal, s->d_err));
     count_launch(s);
@@ -1755,7 +1139,9 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
         const int safe = (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0;
         const int bb = bbox ? 1 : 0;
         float4* quad = w.quad;
-        GS_TRY_LAUNCH(launch_coop(next_pdl(), quad ? k_coop_sums<true> : k_coop_sums<false>, w.sums_grid,
+        const int per_sm = (int)s->shape.moment_blocks_per_sm < w.sums_per_sm ? (int)s->shape.moment_blocks_per_sm
+                                                                                : w.sums_per_sm;
+        GS_TRY_LAUNCH(launch_coop(next_pdl(), quad ? k_coop_sums<true> : k_coop_sums<false>, w.sms * per_sm,
                                   kCoopSumsThreads, st, (const uint32_t*)(ctr + kCtrLevel), (const uint32_t*)w.levels,
                                   n, skey, w.depth, w.rec, (const uint4*)w.kids, (const uint2*)w.nodeinfo, w.msum,
                                   quad, safe, bb, (const BHParams*)w.params, ctr + kCtrBarrier, s->d_err));
@@ -1769,35 +1155,46 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
     const bool count = (s->p.flags & GS_FLAG_COUNT_INTERACTIONS) != 0;
     unsigned long long* stat = (unsigned long long*)(ctr + kCtrStat);
     const bool fpdl = next_pdl();
-    if (s->p.flags & GS_FLAG_GROUP_WALK) {
-        const bool quad = w.quad != nullptr;
-        const int blocks = (int)((n / kGroupSize + kGroupWarps - 1) / kGroupWarps);
-        bool npdl = fpdl;
-        if (estimate && w.amag && quad) {  // |a| of groups that have none, by the theta test
-            GS_TRY_LAUNCH(launch(fpdl, force_group_kernel<true>(exact, quad, count), blocks, kGroupWarps * 32, st,
-                                 sidx, skey, (const uint32_t*)(ctr + kCtrValid), (const float4*)w.rec,
-                                 (const uint32_t*)w.skip, (const float4*)w.quad, (const uint4*)w.kids,
-                                 (const float2*)s->pos[in], (const float2*)s->vel[in], s->pos[out], s->vel[out],
-                                 (float2*)nullptr, n, s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err,
-                                 w.amag, s->p.relative_accuracy, s->floor2, (uint32_t*)nullptr));
-            count_launch(s);
-            npdl = pdl;
-        }
-        auto fn = force_group_kernel<false>(exact, quad, count);
-        GS_TRY_LAUNCH(launch(npdl, fn, blocks, kGroupWarps * 32, st, sidx, skey, (const uint32_t*)(ctr + kCtrValid),
-                             (const float4*)w.rec, (const uint32_t*)w.skip, (const float4*)w.quad,
-                             (const uint4*)w.kids, (const float2*)s->pos[in], (const float2*)s->vel[in], s->pos[out],
-                             s->vel[out], s->acc, n, s->eps2, s->theta2, k, hdt, (uint32_t)w.cap, stat, s->d_err,
-                             w.amag, s->p.relative_accuracy, s->floor2, w.ext ? w.ext + 4 * out : nullptr));
-    } else {
-        auto fn = exact ? (count ? k_force<true, true> : k_force<true, false>)
-                        : (count ? k_force<false, true> : k_force<false, false>);
-        const int blocks = (int)((n / 32 + kForceWarps - 1) / kForceWarps);
-        GS_TRY_LAUNCH(launch(fpdl, fn, blocks, kForceWarps * 32, st, sidx, (const uint32_t*)(ctr + kCtrValid),
-                             (const float4*)w.rec, (const uint32_t*)w.skip, (const float2*)s->pos[in],
-                             (const float2*)s->vel[in], s->pos[out], s->vel[out], s->acc, n, s->eps2, s->theta2, k,
-                             hdt, (uint32_t)w.cap, stat, w.ext ? w.ext + 4 * out : nullptr));
+    ForceLaunch f;
+    f.st = st;
+    f.pdl = fpdl;
+    f.group = (s->p.flags & GS_FLAG_GROUP_WALK) != 0;
+    f.quad = w.quad != nullptr;
+    f.count = count;
+    f.shape = s->shape;
+    f.sidx = sidx;
+    f.skey = skey;
+    f.counts = ctr + kCtrValid;
+    f.rec = w.rec;
+    f.skip = w.skip;
+    f.quad_m = w.quad;
+    f.kids = w.kids;
+    f.pos_in = s->pos[in];
+    f.vel_in = s->vel[in];
+    f.pos_out = s->pos[out];
+    f.vel_out = s->vel[out];
+    f.n_al = n;
+    f.cap = (uint32_t)w.cap;
+    f.eps2 = s->eps2;
+    f.theta2 = s->theta2;
+    f.k = k;
+    f.hdt = hdt;
+    f.alpha = s->p.relative_accuracy;
+    f.floor2 = s->floor2;
+    f.stat = stat;
+    f.err = s->d_err;
+    f.amag = w.amag;
+    auto run = exact ? force_launch_exact : force_launch_fast;
+    if (f.group && estimate && w.amag && f.quad) {  // |a| of groups that have none, by the theta test
+        ForceLaunch e = f;
+        e.estimate = true;  // writes |a| only: no integration, no extent
+        GS_TRY_LAUNCH(run(e));
+        count_launch(s);
+        f.pdl = pdl;
     }
+    f.acc = s->acc;
+    f.ext = w.ext ? w.ext + 4 * out : nullptr;
+    GS_TRY_LAUNCH(run(f));
     count_launch(s);
     stage_end(s, kStageForce, profile);
     return cudaGetLastError();
@@ -1910,41 +1307,6 @@ void bh_set_final_keys(gs_sim* s) { s->bh.final_keys = s->bh.passes & 1; }
 // ------------------------------------------------------------------------------------
 namespace {
 
-// system s with first[s] <= b < first[s + 1] (systems with no blocks are skipped)
-__device__ __forceinline__ uint32_t batch_sys(const uint32_t* __restrict__ first, uint32_t nsys, uint32_t b) {
-    uint32_t lo = 0, hi = nsys;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&first[mid]) <= b) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-struct BatchArgs {
-    const SysDesc* descs;
-    const uint32_t* first;
-    uint32_t nsys;
-    uint32_t step;
-};
-
-struct BatchBlock {
-    const SysDesc* d;
-    Blk blk;
-    int in, out;
-};
-
-__device__ __forceinline__ BatchBlock batch_block(const BatchArgs& a, uint32_t b) {
-    const uint32_t s = batch_sys(a.first, a.nsys, b);
-    const uint32_t f0 = __ldg(&a.first[s]), f1 = __ldg(&a.first[s + 1]);
-    BatchBlock r;
-    r.d = a.descs + s;
-    r.blk = Blk{b - f0, f1 - f0};
-    r.in = (int)((r.d->parity + a.step) & 1u);
-    r.out = r.in ^ 1;
-    return r;
-}
-
 __global__ void __launch_bounds__(256) kb_clear(BatchArgs a, uint32_t* __restrict__ work) {
     const BatchBlock bb = batch_block(a, blockIdx.x);
     if (blockIdx.x == 0 && threadIdx.x < 4) work[threadIdx.x] = 0u;
@@ -1971,22 +1333,23 @@ __global__ void __launch_bounds__(kKeyThreads) kb_keygen(BatchArgs a) {
                 d.keys[0], d.hist, d.passes, d.counters + kCtrValid);
 }
 
-template <bool IDENTITY>
+template <bool IDENTITY, int KPT, int LB>
 __global__ void __launch_bounds__(kSortThreads) kb_sort_pass(BatchArgs a, int ps) {
     pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     const int x = ps & 1, y = x ^ 1;
-    sort_pass_body<IDENTITY>(d.keys[x], IDENTITY ? nullptr : d.idx[x], d.keys[y], d.idx[y], d.n_al, 8 * ps,
+    sort_pass_body<IDENTITY, KPT, LB>(d.keys[x], IDENTITY ? nullptr : d.idx[x], d.keys[y], d.idx[y], d.n_al, 8 * ps,
                              d.hist + 256 * ps, d.sort_status + (size_t)ps * d.sort_tiles * 256,
                              d.counters + kCtrSort + ps, d.err);
 }
 
+template <int R>
 __global__ void __launch_bounds__(kScanThreads) kb_meta_scan(BatchArgs a) {
     pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
-    meta_scan_body(d.keys[d.passes & 1], d.n_al + 1, d.counters + kCtrValid, d.depth, d.E, d.scan_status,
+    meta_scan_body<R>(d.keys[d.passes & 1], d.n_al + 1, d.counters + kCtrValid, d.depth, d.E, d.scan_status,
                    d.counters + kCtrScan, d.counters + kCtrInternal, d.err);
 }
 
@@ -2027,56 +1390,12 @@ __global__ void __launch_bounds__(512) kb_top_sums(BatchArgs a) {
                         d.nodeinfo, d.msum, d.quad, d.safe, d.bbox, d.params);
 }
 
-template <bool EXACT, bool QUAD, bool COUNT, bool ESTIMATE>
-__global__ void __launch_bounds__(kGroupWarps * 32) kb_force_group(BatchArgs a, uint32_t* __restrict__ work) {
-    pdl_enter();
-    __shared__ GroupSmem smem[kGroupWarps];
-    __shared__ uint32_t s_b;
-    const uint32_t total = __ldg(&a.first[a.nsys]);
-    for (;;) {
-        __syncthreads();  // every thread has read the previous s_b
-        if (threadIdx.x == 0) s_b = atomicAdd(work, 1u);
-        __syncthreads();
-        const uint32_t b = s_b;
-        if (b >= total) break;
-        const BatchBlock bb = batch_block(a, b);
-        const SysDesc& d = *bb.d;
-        const int f = d.passes & 1;
-        force_group_body<EXACT, QUAD, COUNT, ESTIMATE>(bb.blk, smem[threadIdx.x >> 5], d.idx[f], d.keys[f],
-                                             d.counters + kCtrValid, d.rec, d.skip, d.quad, d.kids, d.pos[bb.in],
-                                             d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2,
-                                             d.theta2, d.k, d.hdt, d.cap,
-                                             (unsigned long long*)(d.counters + kCtrStat), d.err, d.amag, d.alpha,
-                                             d.floor2, d.ext ? d.ext + 4 * bb.out : nullptr);
-    }
-}
-
-template <bool EXACT, bool COUNT>
-__global__ void __launch_bounds__(kForceWarps * 32) kb_force(BatchArgs a, uint32_t* __restrict__ work) {
-    pdl_enter();
-    __shared__ uint32_t s_b;
-    const uint32_t total = __ldg(&a.first[a.nsys]);
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) s_b = atomicAdd(work, 1u);
-        __syncthreads();
-        const uint32_t b = s_b;
-        if (b >= total) break;
-        const BatchBlock bb = batch_block(a, b);
-        const SysDesc& d = *bb.d;
-        const int f = d.passes & 1;
-        force_body<EXACT, COUNT>(bb.blk, d.idx[f], d.counters + kCtrValid, d.rec, d.skip, d.pos[bb.in],
-                                 d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2, d.theta2, d.k,
-                                 d.hdt, d.cap, (unsigned long long*)(d.counters + kCtrStat),
-                                 d.ext ? d.ext + 4 * bb.out : nullptr);
-    }
-}
-
 }  // namespace
 
 // Descriptor and per-stage block counts of one Barnes-Hut system; the counts are the
 // plain path's, except that the bounding box uses no more blocks than its particles fill.
-void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
+void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount], const gs_shape& shape,
+                   uint32_t force_warps) {
     const BHWork& w = s->bh;
     d.keys[0] = w.keys[0];
     d.keys[1] = w.keys[1];
@@ -2120,45 +1439,48 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
     }
     blocks[kTabGrid] = (uint32_t)grid_for(n, 256);
     blocks[kTabKeys] = (uint32_t)keygen_blocks(n);
-    blocks[kTabSort] = w.sort_tiles;
+    blocks[kTabSort] = sort_tiles_of(n, shape);
     blocks[kTabScan] = w.scan_tiles;
     blocks[kTabOne] = 1;
-    const uint64_t per_block = (s->p.flags & GS_FLAG_GROUP_WALK) ? (uint64_t)kGroupWarps * kGroupSize
+    const uint64_t per_block = (s->p.flags & GS_FLAG_GROUP_WALK) ? (uint64_t)force_warps * kGroupSize
                                                                    : (uint64_t)kForceWarps * 32;
     blocks[kTabForce] = (uint32_t)((n + per_block - 1) / per_block);
 }
 
 namespace {
-template <bool EST>
-auto batch_force_group_kernel(bool exact, bool quad, bool count) {
-    if (EST) {
-        return exact ? (count ? kb_force_group<true, true, true, EST> : kb_force_group<true, true, false, EST>)
-                     : (count ? kb_force_group<false, true, true, EST> : kb_force_group<false, true, false, EST>);
+template <int KPT>
+auto batch_sort_pass_kernel_kpt(bool identity, uint32_t lb) {
+    switch (lb) {
+        case 8: return identity ? kb_sort_pass<true, KPT, 8> : kb_sort_pass<false, KPT, 8>;
+        case 16: return identity ? kb_sort_pass<true, KPT, 16> : kb_sort_pass<false, KPT, 16>;
+        default: return identity ? kb_sort_pass<true, KPT, 32> : kb_sort_pass<false, KPT, 32>;
     }
-    return exact ? (quad ? (count ? kb_force_group<true, true, true, EST> : kb_force_group<true, true, false, EST>)
-                         : (count ? kb_force_group<true, false, true, EST> : kb_force_group<true, false, false, EST>))
-                 : (quad ? (count ? kb_force_group<false, true, true, EST> : kb_force_group<false, true, false, EST>)
-                         : (count ? kb_force_group<false, false, true, EST> : kb_force_group<false, false, false, EST>));
+}
+auto batch_sort_pass_kernel(bool identity, const gs_shape& sh) {
+    return sh.sort_keys_per_thread == 8 ? batch_sort_pass_kernel_kpt<8>(identity, sh.sort_lookback)
+                                        : batch_sort_pass_kernel_kpt<16>(identity, sh.sort_lookback);
 }
 }  // namespace
 
+static BatchForceLaunch batch_force(const BatchPlan& p, uint32_t step, cudaStream_t st) {
+    BatchForceLaunch b;
+    b.st = st;
+    b.descs = p.d_descs;
+    b.first = p.d_tab[kTabForce];
+    b.nsys = p.n_bh;
+    b.step = step;
+    b.group = p.group;
+    b.quad = p.quad;
+    b.count = p.count;
+    b.shape = p.shape;
+    return b;
+}
+
 int bh_batch_force_grid(const BatchPlan& p) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e;
-    if (p.group) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_force_group_kernel<false>(p.exact, p.quad, p.count),
-                                                          kGroupWarps * 32, 0);
-    } else {
-        e = p.exact ? (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<true, true>, kForceWarps * 32, 0)
-                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<true, false>, kForceWarps * 32, 0))
-                    : (p.count ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<false, true>, kForceWarps * 32, 0)
-                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_force<false, false>, kForceWarps * 32, 0));
-    }
-    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
-    if (sms < 1) sms = 152;
-    return sms * per_sm;
+    BatchForceLaunch b = batch_force(p, 0, nullptr);
+    int grid = 0;
+    const cudaError_t e = (p.exact ? batch_force_launch_exact : batch_force_launch_fast)(b, &grid);
+    return e == cudaSuccess && grid > 0 ? grid : 152;
 }
 
 cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bool estimate) {
@@ -2170,9 +1492,13 @@ cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bo
     if (p.bbox) GS_TRY_LAUNCH(launch(true, kb_bbox, (int)p.total[kTabBBox], kBBoxThreads, st, args(kTabBBox)));
     GS_TRY_LAUNCH(launch(true, kb_keygen, (int)p.total[kTabKeys], kKeyThreads, st, args(kTabKeys)));
     for (int ps = 0; ps < p.passes; ++ps)
-        GS_TRY_LAUNCH(launch(true, ps == 0 ? kb_sort_pass<true> : kb_sort_pass<false>, (int)p.total[kTabSort],
-                             kSortThreads, st, args(kTabSort), ps));
-    GS_TRY_LAUNCH(launch(true, kb_meta_scan, (int)p.total[kTabScan], kScanThreads, st, args(kTabScan)));
+        GS_TRY_LAUNCH(launch(true, batch_sort_pass_kernel(ps == 0, p.shape), (int)p.total[kTabSort], kSortThreads, st,
+                             args(kTabSort), ps));
+    {
+        const uint32_t lb = p.shape.scan_lookback;
+        GS_TRY_LAUNCH(launch(true, lb >= 128 ? kb_meta_scan<4> : lb >= 64 ? kb_meta_scan<2> : kb_meta_scan<1>,
+                             (int)p.total[kTabScan], kScanThreads, st, args(kTabScan)));
+    }
     GS_TRY_LAUNCH(launch(true, kb_records, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
     GS_TRY_LAUNCH(launch(true, kb_nodes, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
     for (int lv = p.depth; lv > kLevelTop; --lv)
@@ -2181,17 +1507,17 @@ cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bo
     GS_TRY_LAUNCH(launch(true, p.quad ? kb_top_sums<true> : kb_top_sums<false>, (int)p.total[kTabOne], 512, st,
                          args(kTabOne)));
     const int fg = p.force_grid < (int)p.total[kTabForce] ? p.force_grid : (int)p.total[kTabForce];
-    if (p.group) {
-        if (estimate && p.quad)  // |a| of the groups that have none (members that just joined or were reset)
-            GS_TRY_LAUNCH(launch(true, batch_force_group_kernel<true>(p.exact, p.quad, p.count), fg, kGroupWarps * 32,
-                                 st, args(kTabForce), p.d_work + 1));
-        GS_TRY_LAUNCH(launch(true, batch_force_group_kernel<false>(p.exact, p.quad, p.count), fg, kGroupWarps * 32, st,
-                             args(kTabForce), p.d_work));
-    } else {
-        auto fn = p.exact ? (p.count ? kb_force<true, true> : kb_force<true, false>)
-                          : (p.count ? kb_force<false, true> : kb_force<false, false>);
-        GS_TRY_LAUNCH(launch(true, fn, fg, kForceWarps * 32, st, args(kTabForce), p.d_work));
+    BatchForceLaunch b = batch_force(p, step, st);
+    b.grid = fg;
+    auto run = p.exact ? batch_force_launch_exact : batch_force_launch_fast;
+    if (estimate && p.group && p.quad) {  // |a| of the groups that have none (members that just joined or were reset)
+        BatchForceLaunch e = b;
+        e.estimate = true;
+        e.work = p.d_work + 1;
+        GS_TRY_LAUNCH(run(e, nullptr));
     }
+    b.work = p.d_work;
+    GS_TRY_LAUNCH(run(b, nullptr));
     return cudaGetLastError();
 }
 

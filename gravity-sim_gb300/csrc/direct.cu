@@ -26,7 +26,7 @@ namespace {
 
 constexpr int kDirectBlock = 128;
 constexpr int kDirectTileJ = 64;
-constexpr int kDirectIpt = 2;  // targets per thread, kDirectIpt / 2 packed f32x2 pairs
+constexpr int kDirectIpt = 2;  // default targets per thread (gs_shape.direct_targets: 2 or 4), in packed f32x2 pairs
 
 // Block (bx, by) of a system: i-tile bx, j-chunk by.  A plain launch passes blockIdx.x /
 // blockIdx.y, a batched launch the block's position inside its system's grid.  KAHAN
@@ -235,7 +235,7 @@ __device__ __forceinline__ uint32_t direct_batch_sys(const uint32_t* __restrict_
     return lo;
 }
 
-template <bool EXACT, bool KAHAN>
+template <bool EXACT, bool KAHAN, int IPT>
 __global__ void __launch_bounds__(EXACT ? 64 : kDirectBlock)
 kb_direct(const SysDesc* __restrict__ descs, const uint32_t* __restrict__ first, uint32_t nsys, uint32_t step) {
     const uint32_t s = direct_batch_sys(first, nsys, blockIdx.x);
@@ -246,7 +246,7 @@ kb_direct(const SysDesc* __restrict__ descs, const uint32_t* __restrict__ first,
         direct_ref_body(b, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out], d.acc, d.n_al, d.eps2, d.k,
                         d.hdt);
     else
-        direct_fast_body<kDirectIpt, KAHAN>(b % d.itiles, b / d.itiles, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out],
+        direct_fast_body<IPT, KAHAN>(b % d.itiles, b / d.itiles, d.pos[in], d.vel[in], d.mass[in], d.pos[out], d.vel[out],
                             d.acc, d.n_al, (int)d.chunks, d.jchunk, d.eps2, d.k, d.hdt, d.partials, d.tickets);
 }
 
@@ -345,9 +345,11 @@ gs_status energy_f64(gs_sim* s, double* kinetic, double* potential) {
     return GS_OK;
 }
 
-static int pick_chunks(uint64_t n_al, int ipt) {
+// j-chunks of a plain launch: enough blocks for blocks_per_sm on every SM, at least 256
+// sources per chunk, at most 64 chunks
+static int pick_chunks(uint64_t n_al, int ipt, uint32_t blocks_per_sm) {
     const uint64_t itiles = (n_al + kDirectBlock * ipt - 1) / (kDirectBlock * ipt);
-    const uint64_t want_blocks = 152ull * 12;
+    const uint64_t want_blocks = 152ull * blocks_per_sm;
     uint64_t c = (want_blocks + itiles - 1) / itiles;
     uint64_t max_c = n_al / 256;  // keep at least 256 sources per chunk
     if (c > max_c) c = max_c;
@@ -356,34 +358,46 @@ static int pick_chunks(uint64_t n_al, int ipt) {
     return (int)c;
 }
 
-// Lays the j-chunk partials and tickets out in the system's slab (sizing pass: counts).
+static int shape_ipt(const gs_shape& sh) { return sh.direct_targets == 4 ? 4 : 2; }
+
+// Lays the j-chunk partials and tickets out in the system's slab (sizing pass: counts):
+// for the chunks of the creation shape with either targets-per-thread value, tickets for
+// the most i-tiles (2 targets per thread).
 void direct_carve(gs_sim* s) {
     DirectWork& w = s->dw;
-    w.ipt = kDirectIpt;
+    w.ipt = shape_ipt(s->shape);
     w.block = kDirectBlock;
-    w.chunks = pick_chunks(s->n_al, w.ipt);
+    const int c2 = pick_chunks(s->n_al, 2, s->shape.direct_blocks_per_sm);
+    const int c4 = pick_chunks(s->n_al, 4, s->shape.direct_blocks_per_sm);
+    s->direct_max_chunks = (uint32_t)(c2 > c4 ? c2 : c4);
     w.partials = nullptr;
     w.tickets = nullptr;
-    if (w.chunks > 1) {
-        const uint64_t itiles = (s->n_al + kDirectBlock * w.ipt - 1) / (kDirectBlock * w.ipt);
-        sim_carve(s, (void**)&w.partials, sizeof(float4) * s->n_al * (size_t)w.chunks);
+    if (s->direct_max_chunks > 1) {
+        const uint64_t itiles = (s->n_al + kDirectBlock * 2 - 1) / (kDirectBlock * 2);
+        sim_carve(s, (void**)&w.partials, sizeof(float4) * s->n_al * (size_t)s->direct_max_chunks);
         sim_carve(s, (void**)&w.tickets, sizeof(uint32_t) * itiles);
     }
+}
+
+uint32_t direct_chunks_needed(const gs_sim* s, const gs_shape& sh) {
+    return (uint32_t)pick_chunks(s->n_al, shape_ipt(sh), sh.direct_blocks_per_sm);
 }
 
 cudaError_t direct_init(gs_sim* s) {
     const DirectWork& w = s->dw;
     if (!w.tickets) return cudaSuccess;
-    const uint64_t itiles = (s->n_al + kDirectBlock * w.ipt - 1) / (kDirectBlock * w.ipt);
+    const uint64_t itiles = (s->n_al + kDirectBlock * 2 - 1) / (kDirectBlock * 2);
     return cudaMemsetAsync(w.tickets, 0, sizeof(uint32_t) * itiles, s->stream);
 }
 
-// plain-path grid of k_direct_fast: i-tiles x j-chunks, each chunk a multiple of 64 sources
-static void direct_shape(const gs_sim* s, uint32_t& itiles, uint32_t& jchunk, uint32_t& chunks) {
+// Grid of k_direct_fast for `ipt` targets per thread: i-tiles x j-chunks, each chunk a
+// multiple of 64 sources.  The chunks come from the system's own shape, so a system sums
+// in the same order whichever targets per thread run it (alone or in a batch).
+static void direct_grid(const gs_sim* s, int ipt, uint32_t& itiles, uint32_t& jchunk, uint32_t& chunks) {
     const uint32_t n_al = (uint32_t)s->n_al;
-    const DirectWork& w = s->dw;
-    itiles = (n_al + kDirectBlock * w.ipt - 1) / (kDirectBlock * w.ipt);
-    jchunk = (n_al + w.chunks - 1) / w.chunks;
+    const uint32_t c = direct_chunks_needed(s, s->shape);
+    itiles = (n_al + kDirectBlock * ipt - 1) / (kDirectBlock * ipt);
+    jchunk = (n_al + c - 1) / c;
     jchunk = (jchunk + kDirectTileJ - 1) / kDirectTileJ * kDirectTileJ;
     chunks = (n_al + jchunk - 1) / jchunk;
 }
@@ -398,10 +412,13 @@ cudaError_t direct_step(gs_sim* s, int in, int out, bool profile) {
                                                        s->vel[out], s->acc, n_al, s->eps2, k, hdt);
     } else {
         DirectWork& w = s->dw;
+        const int ipt = shape_ipt(s->shape);
         uint32_t itiles, jchunk, chunks;
-        direct_shape(s, itiles, jchunk, chunks);
+        direct_grid(s, ipt, itiles, jchunk, chunks);
         dim3 grid(itiles, chunks);
-        auto fn = (s->p.flags & GS_FLAG_PLAIN_SUM) ? k_direct_fast<kDirectIpt, false> : k_direct_fast<kDirectIpt, true>;
+        const bool plain = (s->p.flags & GS_FLAG_PLAIN_SUM) != 0;
+        auto fn = ipt == 4 ? (plain ? k_direct_fast<4, false> : k_direct_fast<4, true>)
+                           : (plain ? k_direct_fast<2, false> : k_direct_fast<2, true>);
         fn<<<grid, kDirectBlock, 0, s->stream>>>(s->pos[in], s->vel[in], s->mass[in], s->pos[out], s->vel[out],
                                                   s->acc, n_al, (int)chunks, jchunk, s->eps2, k, hdt, w.partials,
                                                   w.tickets);
@@ -411,10 +428,10 @@ cudaError_t direct_step(gs_sim* s, int in, int out, bool profile) {
     return cudaGetLastError();
 }
 
-void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
+void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount], const gs_shape& batch_shape) {
     for (int t = 0; t < kTabCount; ++t) blocks[t] = 0;
     uint32_t itiles, jchunk, chunks;
-    direct_shape(s, itiles, jchunk, chunks);
+    direct_grid(s, shape_ipt(batch_shape), itiles, jchunk, chunks);
     d.itiles = itiles;
     d.jchunk = jchunk;
     d.chunks = chunks;
@@ -426,14 +443,13 @@ void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]) {
 cudaError_t direct_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st) {
     if (!p.n_direct) return cudaSuccess;
     const SysDesc* descs = p.d_descs + p.n_bh;
+    const bool four = shape_ipt(p.shape) == 4;
     if (p.direct_exact)
-        kb_direct<true, false><<<p.total[kTabDirect], 64, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct, step);
-    else if (p.direct_plain)
-        kb_direct<false, false><<<p.total[kTabDirect], kDirectBlock, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct,
-                                                                              step);
+        kb_direct<true, false, 2><<<p.total[kTabDirect], 64, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct, step);
     else
-        kb_direct<false, true><<<p.total[kTabDirect], kDirectBlock, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct,
-                                                                             step);
+        (p.direct_plain ? (four ? kb_direct<false, false, 4> : kb_direct<false, false, 2>)
+                        : (four ? kb_direct<false, true, 4> : kb_direct<false, true, 2>))
+            <<<p.total[kTabDirect], kDirectBlock, 0, st>>>(descs, p.d_tab[kTabDirect], p.n_direct, step);
     return cudaGetLastError();
 }
 
@@ -510,7 +526,7 @@ extern "C" gs_status gs_direct_step_noalloc(const float* d_pos_in, const float* 
 
     const uint32_t n_al = (uint32_t)n;
     const uint32_t itiles = (n_al + kDirectBlock * kDirectIpt - 1) / (kDirectBlock * kDirectIpt);
-    int chunks = pick_chunks(n_al, kDirectIpt);
+    int chunks = pick_chunks(n_al, kDirectIpt, 12);
     const int fit = (int)(kNoAllocPartialBytes / (sizeof(float4) * n_al));  // >= 4 for n <= 65536
     if (chunks > fit) chunks = fit;
     uint32_t jchunk = (n_al + chunks - 1) / chunks;

@@ -42,10 +42,8 @@ constexpr int kErrScanWait = 2;
 constexpr int kErrTree = 4;
 constexpr int kErrBarrierWait = 8;
 
-// radix sort shape: 256 threads x 16 keys per tile
+// radix sort: 256 threads x 8 or 16 keys per tile (gs_shape.sort_keys_per_thread)
 constexpr int kSortThreads = 256;
-constexpr int kSortKeysPerThread = 16;
-constexpr int kSortTile = kSortThreads * kSortKeysPerThread;
 // single-pass scan shape
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
@@ -55,8 +53,6 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kLevelTop = 4;
 // bounded spin for decoupled look-back: after this many polls the kernel flags an error
 constexpr uint32_t kSpinLimit = 1u << 24;
-// earlier tiles whose status a look-back reads per round trip
-constexpr int kLookback = 8;
 
 // Order-preserving code of a float: unsigned comparison of the words orders the values
 // (-inf < ... < -0 < +0 < ... < +inf), so atomicMin on words takes a minimum and atomicMin
@@ -126,7 +122,7 @@ struct BHWork {
     float* amag = nullptr;             // [n_al] |a| of the last step, NaN: unknown (GS_FLAG_RELATIVE_MAC)
     uint32_t* ext = nullptr;           // [2][4] extent of each state set's positions (bounding-box mode):
                                        // {min x, ~max x, min y, ~max y} as ordered words (ord_word)
-    int sums_grid = 0;                 // blocks of the cooperative moments launch (all co-resident)
+    int sums_per_sm = 0, sms = 0;      // co-resident blocks per SM of the cooperative moments launch, SMs
     uint4* kids = nullptr;             // [cap] child descriptors of internal records
     uint32_t* levels = nullptr;        // internal records by level (level_off / level_cap in bh.cu)
     uint2* nodeinfo = nullptr;         // [cap] {a key of the cell, level} of an internal record
@@ -140,10 +136,9 @@ struct BHWork {
 };
 
 struct DirectWork {
-    int ipt = 2;           // particles per thread
+    int ipt = 2;           // particles per thread of the creation shape
     int block = 128;       // threads per block
-    int chunks = 1;        // j-range split
-    float4* partials = nullptr;  // [chunks][N_al] {sx, sy, cx, cy}
+    float4* partials = nullptr;  // [direct_max_chunks][N_al] {sx, sy, cx, cy}
     uint32_t* tickets = nullptr; // [i-tiles]
 };
 
@@ -208,6 +203,7 @@ struct BatchPlan {
     int depth = 0;               // finest level of the Barnes-Hut members (all share the box mode)
     bool bbox = false, quad = false, group = false, exact = false, count = false, direct_exact = false;
     bool direct_plain = false;   // direct-sum members add their partials plainly (GS_FLAG_PLAIN_SUM)
+    gs_shape shape{};            // launch shapes of the batched kernels (the batch's, see gs_batch_create)
     int force_grid = 0;          // persistent force grid (resident blocks)
 };
 
@@ -244,6 +240,8 @@ struct gs_sim {
     uint32_t launches_in_step = 0;   // kernels enqueued by the step being built
     uint32_t launches_per_step[4] = {0, 0, 0, 0};  // per graph (replay count)
     bool amag_known = false;         // relative criterion: every particle has its previous |a|
+    gs_shape shape{};                // launch shapes (gs_set_shape; graphs are captured with them)
+    uint32_t direct_max_chunks = 1;  // j-chunks the direct-sum scratch was laid out for
     uint64_t kernel_launches = 0;    // kernels launched since creation
     void* slab = nullptr;            // every device buffer of the system
     size_t carved = 0;               // bytes laid out so far (sim_carve)
@@ -263,6 +261,14 @@ gs_status cuda_fail(cudaError_t e, const char* what);
         cudaError_t _e = (call);                               \
         if (_e != cudaSuccess) return gsim::cuda_fail(_e, #call); \
     } while (0)
+
+// Launch shapes: checks a shape's values (message on failure); the shape a new system of
+// these parameters gets (the tuned table of tune.cu, else the defaults).
+bool shape_valid(const gs_shape& sh, std::string* why);
+void shape_for(const gs_params* p, uint64_t n, gs_shape* out);
+void batch_shape_for(const gs_params* p, uint64_t total, gs_shape* out);
+// The parameters and total particles a batch's tuned-table entry is keyed by.
+gs_status batch_key(gs_batch* b, gs_params* params, uint64_t* total);
 
 // Bounded host waits (GS_ERR_TIMEOUT after timeout_ns; 0: 600 s): an event, a stream
 // (through a private event), or everything enqueued on a system's stream so far (its
@@ -290,9 +296,59 @@ void free_snapshot_ring(const gs_sim* s);
 uint64_t bh_capacity(int depth, uint64_t n_al);
 int bh_key_bits(const gs_params* p);
 
+// One launch of a system's traversal kernel (force_fast.cu / force_exact.cu).  The group
+// walk takes its warps per block and list caps from `shape`; the interaction-counting
+// variants exist for the default shape only (2 warps, long lists) and use it.
+struct ForceLaunch {
+    cudaStream_t st = nullptr;
+    bool pdl = false;
+    bool group = false, quad = false, count = false, estimate = false;
+    gs_shape shape{};
+    const uint32_t* sidx = nullptr;
+    const uint32_t* skey = nullptr;
+    const uint32_t* counts = nullptr;
+    const float4* rec = nullptr;
+    const uint32_t* skip = nullptr;
+    const float4* quad_m = nullptr;
+    const uint4* kids = nullptr;
+    const float2* pos_in = nullptr;
+    const float2* vel_in = nullptr;
+    float2* pos_out = nullptr;
+    float2* vel_out = nullptr;
+    float2* acc = nullptr;
+    uint32_t n_al = 0, cap = 0;
+    float eps2 = 0, theta2 = 0, k = 0, hdt = 0, alpha = 0, floor2 = 0;
+    unsigned long long* stat = nullptr;
+    int* err = nullptr;
+    float* amag = nullptr;
+    uint32_t* ext = nullptr;
+};
+cudaError_t force_launch_fast(const ForceLaunch& f);
+cudaError_t force_launch_exact(const ForceLaunch& f);
+
+// One launch of the batched (persistent) traversal kernel over the Barnes-Hut systems of
+// a plan; `grid` 0 asks only for the resident-block count (returned in *grid_out).
+struct BatchForceLaunch {
+    cudaStream_t st = nullptr;
+    const SysDesc* descs = nullptr;
+    const uint32_t* first = nullptr;
+    uint32_t nsys = 0, step = 0;
+    uint32_t* work = nullptr;
+    int grid = 0;
+    bool group = false, quad = false, count = false, estimate = false;
+    gs_shape shape{};
+};
+cudaError_t batch_force_launch_fast(const BatchForceLaunch& b, int* grid_out);
+cudaError_t batch_force_launch_exact(const BatchForceLaunch& b, int* grid_out);
+// Group-walk (warps, short lists) combinations that exist as kernels.
+bool force_shape_supported(uint32_t warps, uint32_t short_lists);
+
 // batched stages (one launch per stage over every system of a plan)
-void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]);
-void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount]);
+// force_warps: group walks per block of the batch's traversal launch (its block table)
+void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount], const gs_shape& shape, uint32_t force_warps);
+void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount], const gs_shape& batch_shape);
+// j-chunks the direct sum of `s` splits into under a shape (its scratch holds direct_max_chunks)
+uint32_t direct_chunks_needed(const gs_sim* s, const gs_shape& sh);
 int bh_batch_force_grid(const BatchPlan& p);
 cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bool estimate);
 cudaError_t direct_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st);

@@ -457,6 +457,7 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
     GS_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     GS_TRY(cudaEventCreateWithFlags(&s->batch_done, cudaEventDisableTiming));
     GS_TRY(cudaMallocHost((void**)&s->h_err, kHostWords * sizeof(int)));
+    shape_for(params, n, &s->shape);
     for (auto& e : s->ev) GS_TRY(cudaEventCreate(&e));
     carve_all(s);  // sizing pass
     GS_TRY(cudaMallocAsync(&s->slab, s->carved, s->stream));
@@ -646,6 +647,47 @@ gs_status gs_get_stats(gs_sim* s, gs_stats* out) {
 gs_status gs_reset_stats(gs_sim* s) {
     if (!s) return invalid("gs_reset_stats: sim is NULL");
     std::memset(&s->stats, 0, sizeof s->stats);
+    return GS_OK;
+}
+
+void gs_shape_defaults(gs_shape* out) {
+    if (!out) return;
+    out->sort_keys_per_thread = 16;
+    out->sort_lookback = 32;
+    out->scan_lookback = 32;
+    out->force_warps = 2;
+    out->force_short_lists = 0;
+    out->direct_targets = 2;
+    out->direct_blocks_per_sm = 12;
+    out->moment_blocks_per_sm = 2;
+}
+
+gs_status gs_get_shape(gs_sim* s, gs_shape* out) {
+    if (!s || !out) return invalid("gs_get_shape: NULL argument");
+    *out = s->shape;
+    return GS_OK;
+}
+
+gs_status gs_set_shape(gs_sim* s, const gs_shape* sh) {
+    if (!s || !sh) return invalid("gs_set_shape: NULL argument");
+    std::string why;
+    if (!shape_valid(*sh, &why)) return invalid(("gs_set_shape: " + why).c_str());
+    if (s->p.algorithm == GS_DIRECT_SUM && direct_chunks_needed(s, *sh) > s->direct_max_chunks) {
+        set_error("gs_set_shape: direct_blocks_per_sm needs more j-chunk scratch than the system was created with");
+        return GS_ERR_CAPACITY;
+    }
+    GS_CUDA(cudaSetDevice(s->device));
+    if (s->batch_pending) {  // captured graphs may be running: wait before dropping them
+        gs_status w = wait_event(s->batch_done, s->timeout_ns);
+        if (w != GS_OK) return w;
+        s->batch_pending = false;
+    }
+    for (auto& g : s->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    s->shape = *sh;
     return GS_OK;
 }
 

@@ -32,8 +32,12 @@ EXPORTS = (
     "gs_server_submit", "gs_server_poll", "gs_server_request", "gs_server_result", "gs_server_get_stats",
     "gs_server_clock", "gs_server_run_trace", "gs_server_destroy", "gs_energy_f64", "gs_camera_start",
     "gs_render_points", "gs_snapshot_take", "gs_snapshot_positions", "gs_snapshot_render", "gs_write_ppm",
-    "gs_set_timeout", "gs_debug_state",
+    "gs_set_timeout", "gs_debug_state", "gs_get_shape", "gs_set_shape", "gs_shape_defaults", "gs_tune_shape",
+    "gs_tune_batch_shape", "gs_load_shape_cache", "gs_clear_shape_table", "gs_batch_get_shape",
+    "gs_batch_set_shape",
 )
+SHAPE_FIELDS = ("sort_keys_per_thread", "sort_lookback", "scan_lookback", "force_warps", "force_short_lists",
+                "direct_targets", "direct_blocks_per_sm", "moment_blocks_per_sm")
 FLAG_PLAIN_SUM = 0x80
 FLAG_RELATIVE_MAC = 0x100
 SERVE_FIFO, SERVE_SHORTEST_FIRST = 0, 1
@@ -48,6 +52,17 @@ class Params(C.Structure):
                 ("accuracy_parameter", C.c_float), ("algorithm", C.c_int32), ("box_mode", C.c_int32),
                 ("math_mode", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32),
                 ("relative_accuracy", C.c_float), ("relative_theta_floor", C.c_float), ("key_bits", C.c_int32)]
+
+
+class Shape(C.Structure):
+    _fields_ = [(k, C.c_uint32) for k in SHAPE_FIELDS]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k in SHAPE_FIELDS}
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("best", Shape), ("best_ms", C.c_double), ("default_ms", C.c_double), ("candidates", C.c_uint32)]
 
 
 class Stats(C.Structure):
@@ -143,6 +158,25 @@ def lib():
     L.gs_set_timeout.restype = st
     L.gs_debug_state.argtypes = [sim, _FP, _FP, _FP, _FP]
     L.gs_debug_state.restype = st
+    L.gs_get_shape.argtypes = [sim, C.POINTER(Shape)]
+    L.gs_get_shape.restype = st
+    L.gs_set_shape.argtypes = [sim, C.POINTER(Shape)]
+    L.gs_set_shape.restype = st
+    L.gs_shape_defaults.argtypes = [C.POINTER(Shape)]
+    L.gs_shape_defaults.restype = None
+    L.gs_tune_shape.argtypes = [C.POINTER(Params), C.c_uint64, C.c_int32, C.c_uint64, C.c_uint32, C.c_char_p,
+                                C.POINTER(TuneResult)]
+    L.gs_tune_shape.restype = st
+    L.gs_tune_batch_shape.argtypes = [C.c_void_p, C.c_uint32, C.c_char_p, C.POINTER(TuneResult)]
+    L.gs_tune_batch_shape.restype = st
+    L.gs_load_shape_cache.argtypes = [C.c_char_p, C.POINTER(C.c_uint32)]
+    L.gs_load_shape_cache.restype = st
+    L.gs_clear_shape_table.argtypes = []
+    L.gs_clear_shape_table.restype = None
+    L.gs_batch_get_shape.argtypes = [C.c_void_p, C.POINTER(Shape)]
+    L.gs_batch_get_shape.restype = st
+    L.gs_batch_set_shape.argtypes = [C.c_void_p, C.POINTER(Shape)]
+    L.gs_batch_set_shape.restype = st
     L.gs_accel_f64.argtypes = [sim, C.c_uint32, _UP, _DP]
     L.gs_accel_f64.restype = st
     L.gs_debug_bh_tree.argtypes = [sim, _UP, _UP, _UP, _FP, _FP, _FP, _FP, C.c_uint64, C.POINTER(C.c_uint64)]
@@ -309,6 +343,17 @@ class Simulation:
     def sync(self, timeout_ns=0):
         _check(lib().gs_sync(self._h, timeout_ns))
 
+    def shape(self):
+        sh = Shape()
+        _check(lib().gs_get_shape(self._h, C.byref(sh)))
+        return sh
+
+    def set_shape(self, shape=None, **kw):
+        sh = Shape.from_buffer_copy(shape) if shape is not None else self.shape()
+        for k, v in kw.items():
+            setattr(sh, k, v)
+        _check(lib().gs_set_shape(self._h, C.byref(sh)))
+
     def set_timeout(self, timeout_ns):
         """Bound of every host wait of this system (0: 600 s)."""
         _check(lib().gs_set_timeout(self._h, timeout_ns))
@@ -446,6 +491,22 @@ class Batch:
     def sync(self, timeout_ns=0):
         _check(lib().gs_batch_sync(self._h, timeout_ns))
 
+    def shape(self):
+        sh = Shape()
+        _check(lib().gs_batch_get_shape(self._h, C.byref(sh)))
+        return sh
+
+    def set_shape(self, shape=None, **kw):
+        sh = Shape.from_buffer_copy(shape) if shape is not None else self.shape()
+        for k, v in kw.items():
+            setattr(sh, k, v)
+        _check(lib().gs_batch_set_shape(self._h, C.byref(sh)))
+
+    def tune(self, steps=5, cache_path=None):
+        r = TuneResult()
+        _check(lib().gs_tune_batch_shape(self._h, steps, cache_path.encode() if cache_path else None, C.byref(r)))
+        return r
+
     @property
     def kernels_per_step(self):
         return int(lib().gs_batch_kernels_per_step(self._h))
@@ -463,6 +524,31 @@ def tune_crossover(direct_params, bh_params, min_n=1024, max_n=262144, particles
     k = t.sizes
     return dict(crossover=int(t.crossover), n=[int(x) for x in t.n[:k]], direct_ms=list(t.direct_ms[:k]),
                 bh_ms=list(t.bh_ms[:k]))
+
+
+def shape_defaults():
+    sh = Shape()
+    lib().gs_shape_defaults(C.byref(sh))
+    return sh
+
+
+def tune_shape(params, n, generator=GEN_UNIFORM_DISK, seed=1, steps=10, cache_path=None):
+    """Launch-shape autotuner (gs_tune_shape): the fastest shape for this workload, entered in
+    the process's tuned table (and the cache file, if given)."""
+    r = TuneResult()
+    _check(lib().gs_tune_shape(C.byref(params), n, generator, seed, steps,
+                               cache_path.encode() if cache_path else None, C.byref(r)))
+    return r
+
+
+def load_shape_cache(path):
+    count = C.c_uint32(0)
+    _check(lib().gs_load_shape_cache(path.encode() if path else None, C.byref(count)))
+    return count.value
+
+
+def clear_shape_table():
+    lib().gs_clear_shape_table()
 
 
 def footprint(params, n):

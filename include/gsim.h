@@ -125,6 +125,23 @@ typedef struct gs_params {
 
 typedef struct gs_sim gs_sim;
 
+/* Launch shapes of a system's kernels.  The reference fixes its workgroup sizes
+ * (src/Simulation/BarnesHut/BarnesHutSimulation.cpp:9-10,
+ * src/Simulation/Direct/DirectSimulation.cpp:9); here each system gets a shape from the
+ * tuned table (gs_tune_shape) or the defaults, and gs_set_shape can change it between
+ * steps.  No field changes a result bit, except direct_blocks_per_sm in FAST math, which
+ * sets how the direct sum splits its j-range over blocks (and so its summation grouping). */
+typedef struct gs_shape {
+    uint32_t sort_keys_per_thread; /* radix-sort tile = 256 threads x this: 8 or 16 (default) */
+    uint32_t sort_lookback;        /* earlier tiles a radix pass reads per look-back round trip: 8, 16, 32 */
+    uint32_t scan_lookback;        /* the same for the node scan: 32, 64, 128 */
+    uint32_t force_warps;          /* group walks per block of the accurate traversal: 1, 2 (default), 4 */
+    uint32_t force_short_lists;    /* 0: evaluate after 160 nodes / 96 leaf runs; 1: after 96 / 64 */
+    uint32_t direct_targets;       /* direct-sum particles per thread (FAST math): 2 (default) or 4 */
+    uint32_t direct_blocks_per_sm; /* direct-sum j-split target, blocks per SM: 1..32 (default 12) */
+    uint32_t moment_blocks_per_sm; /* blocks per SM of the cooperative moments launch: 1 or 2 (default) */
+} gs_shape;
+
 /* Statistics: stage times accumulate over steps since gs_reset_stats (GS_FLAG_PROFILE);
  * tree counts are those of the most recent step. */
 #define GS_STAGE_COUNT 8
@@ -157,6 +174,12 @@ GS_API gs_status gs_create(const gs_params* params, uint64_t particle_count, con
 GS_API gs_status gs_run(gs_sim* sim, uint32_t count);
 /* Wait for all submitted steps; timeout_ns = 0 uses the system's timeout. */
 GS_API gs_status gs_sync(gs_sim* sim, uint64_t timeout_ns);
+/* The system's launch shapes; changing them drops its captured step graphs.  A
+ * direct_blocks_per_sm that needs more j-chunk scratch than gs_create laid out is refused
+ * (GS_ERR_CAPACITY). */
+GS_API gs_status gs_get_shape(gs_sim* sim, gs_shape* out);
+GS_API gs_status gs_set_shape(gs_sim* sim, const gs_shape* shape);
+GS_API void gs_shape_defaults(gs_shape* out);
 /* Bound of every host wait this system makes (gs_run, gs_sync with 0, the particle
  * transfers, readbacks): GS_ERR_TIMEOUT after timeout_ns nanoseconds; 0 (the default)
  * means 600 s.  No counterpart in the reference, whose fence waits do not time out. */
@@ -280,6 +303,39 @@ typedef struct gs_tuning {
 GS_API gs_status gs_tune_crossover(const gs_params* direct_params, const gs_params* bh_params,
                                    uint64_t min_n, uint64_t max_n, uint64_t particles_per_probe,
                                    uint64_t seed, gs_tuning* out);
+
+/* ---- launch-shape autotuner (no counterpart in the reference) ----
+ *
+ * gs_tune_shape times candidate gs_shape values on a system of n particles made by
+ * gs_generate(generator, seed) with these parameters, and keeps the fastest: coordinate
+ * descent over the knobs that apply (Barnes-Hut: sort tile, sort and scan look-back
+ * widths, group-walk warps per block and list caps, moments grid; direct sum: targets per
+ * thread and the j-split), each candidate timed with CUDA events as the median of `steps`
+ * warm steps with the L2 flushed before each.  The winner goes into the process's tuned
+ * table under (device name and SM count, algorithm, box mode, key bits, math mode, the
+ * accurate / relative / plain-sum flags, floor(log2 N)); gs_create gives a new system the
+ * entry of its key, else the defaults (gs_shape_defaults).  With `cache_path` (or, when it
+ * is NULL, the environment variable GSIM_SHAPE_CACHE) the table is also written there as
+ * JSON, and gs_load_shape_cache reads such a file back (later processes, other callers).
+ * gs_tune_batch_shape does the same for the batched kernels of an existing batch, keyed by
+ * the batch's total particles; gs_batch_create consults those entries. */
+typedef struct gs_tune_result {
+    gs_shape best;
+    double best_ms;          /* per step with the best shape */
+    double default_ms;       /* per step with gs_shape_defaults */
+    uint32_t candidates;     /* shapes timed */
+} gs_tune_result;
+GS_API gs_status gs_tune_shape(const gs_params* params, uint64_t n, int32_t generator, uint64_t seed,
+                               uint32_t steps, const char* cache_path, gs_tune_result* out);
+GS_API gs_status gs_tune_batch_shape(gs_batch* batch, uint32_t steps, const char* cache_path, gs_tune_result* out);
+/* Reads a cache file written by the tuner into the tuned table (path NULL:
+ * GSIM_SHAPE_CACHE; no such file: GS_ERR_IO).  *entries (may be NULL) gets the count. */
+GS_API gs_status gs_load_shape_cache(const char* path, uint32_t* entries);
+/* Empties the tuned table (new systems get the defaults again). */
+GS_API void gs_clear_shape_table(void);
+/* Launch shape of a batch's kernels, and changing it (re-plans; drops the step graphs). */
+GS_API gs_status gs_batch_get_shape(gs_batch* batch, gs_shape* out);
+GS_API gs_status gs_batch_set_shape(gs_batch* batch, const gs_shape* shape);
 
 /* Device bytes gs_create allocates for a system with these parameters (the admission
  * measure of gs_server).  The default memory pool may round each allocation up. */
