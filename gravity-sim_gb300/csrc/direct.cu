@@ -4,8 +4,9 @@
 // src/Simulation/Direct/DirectSimulation.cpp:306-319).
 //
 // FAST mode (k_direct_fast): each block owns an i-tile of 128*IPT particles and one
-// j-chunk; j is staged 64 at a time in shared memory as float4 {x, y, m, 0} and
-// broadcast to all threads; every thread keeps IPT targets in registers.  Each 64-wide
+// j-chunk; j is staged 64 at a time in shared memory as float4 {x, y, m, 0} (loaded as
+// float4 pairs of positions and float2 pairs of masses: j-tiles start at multiples of 64)
+// and broadcast to all threads; every thread keeps IPT targets in registers.  Each 64-wide
 // tile is summed plainly in FP32, and the tile partials are added with Kahan
 // compensation.  When the j-range is split over several blocks (small N, to fill 152
 // SMs), every block stores its compensated partial and the last block to finish an
@@ -67,9 +68,11 @@ __device__ __forceinline__ void direct_fast_body(uint32_t bx, uint32_t by, const
 
     for (uint32_t jt = j0; jt < j1; jt += kDirectTileJ) {
         __syncthreads();
-        if (t < kDirectTileJ) {
-            float2 q = pos[jt + t];
-            sj[t] = make_float4(q.x, q.y, mass[jt + t], 0.f);
+        if (t < kDirectTileJ / 2) {  // one float4 of two positions and one float2 of their masses per thread
+            const float4 q = reinterpret_cast<const float4*>(pos)[(jt >> 1) + t];
+            const float2 m = reinterpret_cast<const float2*>(mass)[(jt >> 1) + t];
+            sj[2 * t] = make_float4(q.x, q.y, m.x, 0.f);
+            sj[2 * t + 1] = make_float4(q.z, q.w, m.y, 0.f);
         }
         __syncthreads();
         // Pairs of the thread's targets share packed f32x2 instructions (each lane rounds
@@ -512,6 +515,12 @@ extern "C" gs_status gs_direct_step_noalloc(const float* d_pos_in, const float* 
     if (n == 0 || n % kAlignment != 0) {
         set_error("gs_direct_step_noalloc: the particle count must be a positive multiple of 64 "
                   "(pad with zero-mass particles, as ParticleSystem does)");
+        return GS_ERR_INVALID_ARGUMENT;
+    }
+    if (((uintptr_t)d_pos_in & 15u) || ((uintptr_t)d_mass & 7u) || ((uintptr_t)d_vel_in & 7u) ||
+        ((uintptr_t)d_pos_out & 7u) || ((uintptr_t)d_vel_out & 7u)) {
+        set_error("gs_direct_step_noalloc: pos_in must be 16-byte aligned and the other arrays 8-byte aligned "
+                  "(the kernel reads positions as float4 pairs)");
         return GS_ERR_INVALID_ARGUMENT;
     }
     if (n > GS_NOALLOC_MAX_PARTICLES) {

@@ -244,7 +244,8 @@ GS_API uint64_t gs_bh_node_capacity(int32_t box_mode, uint64_t aligned_count);
  *     interleaved for pos and vel); n must be a multiple of 64 (pad with zero-mass
  *     particles at the origin, as ParticleSystem does) and at most
  *     GS_NOALLOC_MAX_PARTICLES, else GS_ERR_INVALID_ARGUMENT / GS_ERR_CAPACITY.
- *     Outputs must not alias inputs.
+ *     Outputs must not alias inputs.  d_pos_in must be 16-byte aligned, the other arrays
+ *     8-byte aligned (cudaMalloc gives 256), else GS_ERR_INVALID_ARGUMENT.
  *   - Runs on the calling thread's current device, on `stream` (a cudaStream_t, NULL for
  *     the legacy default stream), asynchronously.
  *   - Scratch lives in fixed device arrays inside this library (about 4 MiB per GPU that

@@ -80,3 +80,7 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gs):
     st = step(buf.data_ptr(), buf.data_ptr(), m.data_ptr(), out_p.data_ptr(), out_v.data_ptr(), 100, 1.0, 1e-3, 0.2,
               None)
     assert st == 1  # not a multiple of 64
+    # positions are read as 16-byte float4 pairs: a misaligned array is refused before any launch
+    st = step(buf.data_ptr() + 8, buf.data_ptr(), m.data_ptr(), out_p.data_ptr(), out_v.data_ptr(), 64, 1.0, 1e-3,
+              0.2, None)
+    assert st == 1 and "aligned" in gs.lib().gs_last_error().decode()
