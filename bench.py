@@ -76,6 +76,10 @@ def workloads():
                              desc="Barnes-Hut N=500000 spiral galaxy, accurate mode (bounding box, quadrupole, "
                                   "safe radius, 64-particle group walk), geometric criterion theta=0.3, "
                                   "softening 0.2, dt=1e-3"),
+        "bh500k-30bit": dict(spiral, box=BOX_BOUNDING, theta=1.0, alpha=0.006, floor=0.2, flags=ACCURATE | RELATIVE,
+                             oracle_flags=15, key_bits=15,
+                             desc="the headline workload with 15 bits per axis: 30-bit bounding-box Morton keys "
+                                  "(4 radix passes, 16 tree levels)"),
         "bh500k-reference-rule": dict(spiral, box=BOX_FIXED, theta=1.0, flags=0, oracle_flags=0,
                                       desc="Barnes-Hut N=500000 spiral galaxy, the reference's opening rule "
                                            "(fixed +-500 box, monopoles, warp vote) theta=1, softening 0.2, dt=1e-3"),
@@ -259,7 +263,15 @@ def job_value(dist, particles, steps, dev_ms):
 def make_params(gsim, wl, local, flags):
     return gsim.default_params(algorithm=wl["algo"], box_mode=wl["box"], accuracy_parameter=wl["theta"],
                                relative_accuracy=wl.get("alpha", 0.0), relative_theta_floor=wl.get("floor", 0.0),
-                               device=local, flags=wl["flags"] | flags)
+                               key_bits=wl.get("key_bits", 0), device=local, flags=wl["flags"] | flags)
+
+
+def autotune(gsim, wl, local, steps=10):
+    """The launch-shape autotuner (gs_tune_shape) on the workload's own system; systems of
+    this key created afterwards get the shape it picks."""
+    r = gsim.tune_shape(make_params(gsim, wl, local, 0), wl["n"], generator=wl["gen"], seed=wl["seed"], steps=steps)
+    return {"shape": r.best.as_dict(), "ms_per_step": r.best_ms, "default_shape_ms_per_step": r.default_ms,
+            "candidates_timed": int(r.candidates)}
 
 
 def step_errors(gsim, params, pos, vel, mass, sub, steps, warm=0):
@@ -408,6 +420,9 @@ def measure_batched(gsim, torch, args, local):
     stream = torch.cuda.ExternalStream(batch.stream, device=local)
     batch.run(args.warmup)
     batch.sync()
+    tb = batch.tune(steps=3) if not args.no_tune else None  # the batched kernels' launch shape
+    tuned = {"shape": tb.best.as_dict(), "ms_per_step": tb.best_ms, "default_shape_ms_per_step": tb.default_ms,
+             "candidates_timed": int(tb.candidates)} if tb else None
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     torch.cuda.synchronize()
@@ -454,7 +469,7 @@ def measure_batched(gsim, torch, args, local):
             "theta_floor": floor, "value": value, "unit": "particle-steps/s", "steps": steps,
             "ms_per_step": dev_b * 1e3 / steps, "systems": len(specs), "particles": int(total_n),
             "barnes_hut_systems": n_bh, "direct_systems": len(specs) - n_bh, "crossover_n": xo, "tuning": tune,
-            "kernels_per_step": kps, "gpu_launches": kps * steps,
+            "kernels_per_step": kps, "gpu_launches": kps * steps, "autotuned": tuned,
             "plain_one_at_a_time": {"value": plain, "device_s": dev_p, "wall_s_incl_warmup": wall_p},
             "speedup_vs_plain": value / plain, "wall_value": total_n * steps / wall_b,
             "force_error_sample": errs, "force_error_worst_rms": max(e["rms"] for e in errs), "setup_s": setup_s,
@@ -533,20 +548,50 @@ def measure_served(gsim, torch, args, local, crossover, theta, alpha, floor):
               "peak_memory_gb": st["peak_memory_in_use"] / 1e9,
               "peak_resident_particles": st["peak_resident_particles"], "failed": st["failed"]}
 
-    # plain sequential path: one request at a time in arrival order, real-time arrivals
+    served["gpu_busy_s"] = st["gpu_busy_seconds"]
+    served["gpu_busy_fraction"] = st["gpu_busy_seconds"] / makespan
+
+    # plain sequential path: one request at a time in arrival order, real-time arrivals;
+    # where its time goes, per phase (host wall clock; the steps also in device time)
     lat_p = []
+    bd = dict(wait_for_arrival_s=0.0, generate_s=0.0, create_and_upload_s=0.0, steps_wall_s=0.0,
+              steps_device_s=0.0, readback_s=0.0, destroy_s=0.0)
     start = time.perf_counter()
     for r, a in zip(reqs, arrivals):
         now = time.perf_counter() - start
         if now < a:
             time.sleep(a - now)
+            bd["wait_for_arrival_s"] += a - now
+        t0 = time.perf_counter()
         pos, vel, mass = gsim.generate(r.generator, r.particle_count, size=r.generate_size, seed=r.seed)
-        with gsim.Simulation(pos, vel, mass, params=d if r.particle_count < crossover else b) as sim:
+        t1 = time.perf_counter()
+        sim = gsim.Simulation(pos, vel, mass, params=d if r.particle_count < crossover else b)
+        t2 = time.perf_counter()
+        stream = torch.cuda.ExternalStream(sim.stream(), device=local)
+        ea, ez = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            ea.record(stream)
             sim.run(r.steps)
-            sim.get_particles()
+            ez.record(stream)
+        sim.sync()
+        t3 = time.perf_counter()
+        sim.get_particles()
+        t4 = time.perf_counter()
+        sim.close()
+        t5 = time.perf_counter()
+        bd["generate_s"] += t1 - t0
+        bd["create_and_upload_s"] += t2 - t1
+        bd["steps_wall_s"] += t3 - t2
+        bd["steps_device_s"] += ea.elapsed_time(ez) / 1e3
+        bd["readback_s"] += t4 - t3
+        bd["destroy_s"] += t5 - t4
         lat_p.append(time.perf_counter() - start - a)
     makespan_p = time.perf_counter() - start - float(arrivals[0])
-    plain = {"value": work / makespan_p, "makespan_s": makespan_p, "latency": _latency_summary(lat_p)}
+    plain = {"value": work / makespan_p, "makespan_s": makespan_p, "latency": _latency_summary(lat_p),
+             "breakdown": bd, "gpu_busy_fraction": bd["steps_device_s"] / makespan_p}
+    # the served path is GPU-bound when its device time fills its makespan; then no
+    # scheduling can beat plain makespan / served device time on this trace
+    served["speedup_ceiling_at_its_gpu_time"] = makespan_p / max(st["gpu_busy_seconds"], 1e-9)
     served["force_error_sample"] = _request_errors(gsim, reqs, d, b, crossover)
     served["force_error_worst_rms"] = max(e["rms"] for e in served["force_error_sample"])
     return {"workload": SERVE_DESC % bh_mode_desc(theta, alpha, floor), "requests": len(reqs), "theta": theta,
@@ -734,6 +779,7 @@ def direct_config(gsim, torch, args, local):
     wl = dict(workloads()["direct4096"], name="direct4096")
     pos, vel, mass = gsim.generate(wl["gen"], wl["n"], size=wl["size"], seed=wl["seed"])
     steps = wl["steps"]
+    tuned = autotune(gsim, wl, local) if not args.no_tune else None
     p = make_params(gsim, wl, local, 0)
     with gsim.Simulation(pos, vel, mass, params=p) as sim:
         stream = torch.cuda.ExternalStream(sim.stream(), device=local)
@@ -758,7 +804,7 @@ def direct_config(gsim, torch, args, local):
     return {"workload": wl["desc"], "value": wl["n"] * steps / (dev_ms / 1e3), "unit": "particle-steps/s",
             "steps": steps, "ms_per_step": dev_ms / steps, "roofline": roofline_of(gsim, wl, m),
             "force_error_vs_fp64": dict(err, subsample=wl["n"], steps="steps 1..10 from the generated state"),
-            "cpu_baseline": cpu_baseline(wl, pos, vel, mass),
+            "cpu_baseline": cpu_baseline(wl, pos, vel, mass), "autotuned": tuned,
             "l2": "flushed (256 MiB write) before every timed step"}
 
 
@@ -831,6 +877,7 @@ def main():
     ap.add_argument("--no-served", action="store_true", help="skip the served (request stream) line")
     ap.add_argument("--no-precision", action="store_true", help="skip the direct-sum precision study")
     ap.add_argument("--no-direct-config", action="store_true", help="skip the N=4096 direct-sum line")
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner (default shapes)")
     ap.add_argument("--serve-requests", type=int, default=100)
     ap.add_argument("--serve-max-particles", type=int, default=0, help="resident particle cap (0: budget only)")
     args = ap.parse_args()
@@ -849,6 +896,7 @@ def main():
     world, rank, local, dist = dist_setup()
     torch.cuda.set_device(local)
     pos, vel, mass = gsim.generate(wl["gen"], wl["n"], size=wl["size"], seed=wl["seed"] + rank)
+    tuned = autotune(gsim, wl, local) if not args.no_tune else None
     m = measure(gsim, torch, wl, pos, vel, mass, args, local, dist, sample_clocks=True)
     sim = m.pop("sim")
     max_ms = reduce_op(dist, m["dev_ms"], "max")
@@ -880,10 +928,10 @@ def main():
     sim.close()
 
     err = force_error(gsim, wl, pos, vel, mass, local) if rank == 0 else None
-    secondary = theta_only = None
+    secondary = theta_only = keys30 = None
     if rank == 0 and world == 1 and args.workload == "bh500k" and not args.no_secondary:
         lines = []
-        for name in ("bh500k-theta", "bh500k-reference-rule"):
+        for name in ("bh500k-theta", "bh500k-30bit", "bh500k-reference-rule"):
             wl2 = dict(workloads()[name], name=name)
             m2 = measure(gsim, torch, wl2, pos, vel, mass, args, local, None, sample_clocks=False)
             m2.pop("sim").close()
@@ -891,7 +939,7 @@ def main():
                           "ms_per_step": m2["dev_ms"] / args.steps, "stage_ms_per_step": m2["stage_ms"],
                           "interactions_per_step": m2.get("interactions"),
                           "force_error_vs_fp64": force_error(gsim, wl2, pos, vel, mass, local)})
-        theta_only, secondary = lines
+        theta_only, keys30, secondary = lines
     batched = served = None
     if rank == 0 and world == 1 and not args.no_batched:
         batched = measure_batched(gsim, torch, args, local)
@@ -917,7 +965,8 @@ def main():
                "e2e": e2e, "gpu_launches": m["launches"] * world,
                "roofline": roofline_of(gsim, wl, m, FORCE_CAPTURE.get(args.workload)),
                "cpu_baseline": cpu, "force_error_vs_fp64": err, "clocks": m["clocks"],
-               "accurate_theta_only": theta_only, "reference_rule_theta1": secondary, "direct_config": direct,
+               "autotuned": tuned, "accurate_theta_only": theta_only, "keys_30bit": keys30,
+               "reference_rule_theta1": secondary, "direct_config": direct,
                "batched": batched, "served": served, "direct_precision_study": precision}
         print(json.dumps(out))
     if dist is not None:

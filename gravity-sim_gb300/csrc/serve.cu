@@ -62,6 +62,9 @@ struct gs_server {
     bool dirty = false;
     std::deque<cudaEvent_t> inflight;  // one event per enqueued step, oldest first
     std::vector<cudaEvent_t> spare;
+    // device time of the batched steps: a timing-event pair around each, summed once done
+    std::deque<std::pair<cudaEvent_t, cudaEvent_t>> timed;
+    std::vector<cudaEvent_t> spare_timing;
     gs_server_stats st{};
     // input generators
     std::mutex mu;
@@ -110,6 +113,33 @@ cudaEvent_t take_event(gs_server* s) {
     cudaEvent_t e = nullptr;
     cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     return e;
+}
+
+cudaEvent_t take_timing_event(gs_server* s) {
+    if (!s->spare_timing.empty()) {
+        cudaEvent_t e = s->spare_timing.back();
+        s->spare_timing.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Adds the device time of finished batched steps to the statistics (no waiting).
+void account_gpu_time(gs_server* s) {
+    while (!s->timed.empty()) {
+        auto [a, b] = s->timed.front();
+        if (cudaEventQuery(b) != cudaSuccess) {
+            (void)cudaGetLastError();
+            break;
+        }
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) s->st.gpu_busy_seconds += 1e-3 * ms;
+        s->spare_timing.push_back(a);
+        s->spare_timing.push_back(b);
+        s->timed.pop_front();
+    }
 }
 
 void fail_request(gs_server* s, Request* r, const std::string& why) {
@@ -268,7 +298,11 @@ gs_status step(gs_server* s) {
         s->dirty = false;
         ++s->st.plan_changes;
     }
+    cudaEvent_t t_begin = take_timing_event(s), t_end = take_timing_event(s);
+    GS_CUDA(cudaEventRecord(t_begin, s->eng.root));
     GS_CUDA(s->eng.enqueue((uint32_t)(s->eng.step & 1), s->eng.needs_estimate()));
+    GS_CUDA(cudaEventRecord(t_end, s->eng.root));
+    s->timed.emplace_back(t_begin, t_end);
     s->eng.advance();
     ++s->st.batched_steps;
     cudaEvent_t done = take_event(s);
@@ -307,6 +341,11 @@ void destroy_server(gs_server* s) {
     }
     for (auto e : s->inflight) cudaEventDestroy(e);
     for (auto e : s->spare) cudaEventDestroy(e);
+    for (auto& ab : s->timed) {
+        cudaEventDestroy(ab.first);
+        cudaEventDestroy(ab.second);
+    }
+    for (auto e : s->spare_timing) cudaEventDestroy(e);
     s->eng.destroy();
     delete s;
 }
@@ -395,6 +434,7 @@ gs_status gs_server_poll(gs_server* s, uint32_t* finished) {
     if (!s) return bad("gs_server_poll: server is NULL");
     if (finished) *finished = 0;
     GS_CUDA(cudaSetDevice(s->eng.device));
+    account_gpu_time(s);
     gs_status g = retire(s, finished);
     if (g == GS_OK) g = admit(s);
     if (g == GS_OK) g = step(s);
@@ -438,6 +478,8 @@ gs_status gs_server_result(gs_server* s, uint64_t id, float* pos, float* vel, fl
 
 gs_status gs_server_get_stats(gs_server* s, gs_server_stats* out) {
     if (!s || !out) return bad("gs_server_get_stats: NULL argument");
+    GS_CUDA(cudaSetDevice(s->eng.device));
+    account_gpu_time(s);
     *out = s->st;
     return GS_OK;
 }

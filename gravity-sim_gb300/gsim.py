@@ -98,7 +98,8 @@ class RequestStatus(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "finished", "failed", "queued", "resident", "memory_in_use",
                                           "peak_memory_in_use", "resident_particles", "peak_resident_particles",
-                                          "batched_steps", "plan_changes", "particle_steps")]
+                                          "batched_steps", "plan_changes", "particle_steps")] + \
+               [("gpu_busy_seconds", C.c_double)]
 
 
 class GsimError(RuntimeError):

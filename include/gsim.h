@@ -400,6 +400,7 @@ typedef struct gs_server_stats {
     uint64_t batched_steps;       /* gs_server_poll steps enqueued */
     uint64_t plan_changes;        /* member-set changes */
     uint64_t particle_steps;      /* sum of N x steps of finished requests */
+    double gpu_busy_seconds;      /* device time of the finished batched steps (CUDA events) */
 } gs_server_stats;
 
 GS_API gs_status gs_server_create(const gs_server_config* config, gs_server** out);
