@@ -243,9 +243,11 @@ bool BatchEngine::in_step() const {
 
 uint32_t BatchEngine::launches_per_step() const {
     uint32_t k = 0;
-    if (plan.n_bh)  // clear keys scan records nodes force, radix passes, box, moment levels (the
-                    // |a| estimate pass of a step after a member joined or was reset not included)
-        k += 6u + (uint32_t)plan.passes + (plan.bbox ? 1u : 0u) + (uint32_t)(plan.depth - kLevelTop + 1);
+    if (plan.n_bh)  // clear keys scan records nodes force, radix passes, box, then the moment
+                    // prefix (quadrupole mode) or the moment levels (the |a| estimate pass of a
+                    // step after a member joined or was reset not included)
+        k += 6u + (uint32_t)plan.passes + (plan.bbox ? 1u : 0u) +
+             (plan.quad ? 3u : (uint32_t)(plan.depth - kLevelTop + 1));
     if (plan.n_direct) k += 1u;
     return k;
 }

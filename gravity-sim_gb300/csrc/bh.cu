@@ -20,10 +20,17 @@
 //   k_records     preorder records: node (d, s) at s + E(s) + d - dmin(s), particle leaf
 //                 at s + E(s) + e(s); skip = end + E(end) - index (the reference's count.y),
 //                 radius = radius0 / 4^d (TreeMoveShader.comp:70-71)
+//   monopole mode (the reference's rule):
 //   k_coop_sums   mass and mass-moment sums level by level, finest first (one cooperative
 //                 launch, a grid barrier between deep levels, one block for the top
 //                 levels; a batch launches kb_level_sums per level), children in the order
 //                 of TreeInitShader.comp:78-80; centre of mass as TreeMoveShader.comp:66-67
+//   quadrupole mode (accurate mode, moments.cuh): exact integer sums instead --
+//   k_mom_tiles   the sums of every tile of 1024 sorted slots
+//   k_mom_scan    their exclusive prefix at every slot
+//   k_mom_nodes   each internal node's centre, mass, opening radius and second moments
+//                 from the prefix at its first slot and one past its last (k_nodes keeps
+//                 the end)
 //   k_force       ForceShader.comp:78-152 semantics: one warp walks the preorder records
 //                 for 32 consecutive sorted slots; a record is accepted only if every
 //                 lane satisfies radius <= d2 * theta^2; 32-record window staged in shared
@@ -33,6 +40,7 @@
 #include <cstring>
 
 #include "bh_common.cuh"
+#include "moments.cuh"
 
 namespace gsim {
 namespace {
@@ -220,17 +228,20 @@ inline int keygen_blocks(uint64_t n) {
     return (int)(b < 1 ? 1 : b > (uint64_t)kKeyBlocks ? kKeyBlocks : b);
 }
 
+// mmax (quadrupole mode, else null): the largest mass after the removal, as float bits
+// (masses >= 0 order like their bits), for the grid of the exact moment sums.
 __device__ __forceinline__ void keygen_body(Blk blk, int bbox_mode, const BHParams* __restrict__ bp,
                                             float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos_out,
                                             float* mass_out,  // mass sets may alias
                                             uint32_t n, uint32_t* __restrict__ keys, uint32_t* __restrict__ hist,
-                                            int passes, uint32_t* __restrict__ valid_count) {
+                                            int passes, uint32_t* __restrict__ valid_count,
+                                            uint32_t* __restrict__ mmax = nullptr) {
     __shared__ uint32_t sh[4][256];
     for (int i = threadIdx.x; i < 4 * 256; i += kKeyThreads) (&sh[0][0])[i] = 0u;
     __syncthreads();
     BHParams p;
     if (bbox_mode) p = *bp;
-    uint32_t valid = 0;
+    uint32_t valid = 0, mbits = 0;
     for (uint32_t i = blk.id * kKeyThreads + threadIdx.x; i < n; i += blk.count * kKeyThreads) {
         float2 q = pos_in[i];
         uint32_t key;
@@ -238,8 +249,16 @@ __device__ __forceinline__ void keygen_body(Blk blk, int bbox_mode, const BHPara
             key = spread_bits(bbox_cell(q.x, p.cx, p.scale, p.bits)) |
                   (spread_bits(bbox_cell(q.y, p.cy, p.scale, p.bits)) << 1);
             ++valid;
+            if (mmax) {
+                const float m = mass_in[i];
+                if (m > 0.0f) mbits = max(mbits, __float_as_uint(m));
+            }
         } else if (fixed_key(q.x, q.y, key)) {
             ++valid;
+            if (mmax) {
+                const float m = mass_in[i];
+                if (m > 0.0f) mbits = max(mbits, __float_as_uint(m));
+            }
         } else {  // InitShader.comp:110-117
             key = kKeyRemovedSort;
             const float2 gone = make_float2(-kSimSize * 2.0f, -kSimSize * 2.0f);
@@ -253,6 +272,10 @@ __device__ __forceinline__ void keygen_body(Blk blk, int bbox_mode, const BHPara
     }
     for (int o = 16; o; o >>= 1) valid += __shfl_xor_sync(0xffffffffu, valid, o);
     if ((threadIdx.x & 31) == 0 && valid) atomicAdd(valid_count, valid);
+    if (mmax) {
+        mbits = __reduce_max_sync(0xffffffffu, mbits);
+        if ((threadIdx.x & 31) == 0 && mbits) atomicMax(mmax, mbits);
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < passes * 256; i += kKeyThreads) {
         uint32_t c = (&sh[0][0])[i];
@@ -263,9 +286,10 @@ __device__ __forceinline__ void keygen_body(Blk blk, int bbox_mode, const BHPara
 __global__ void __launch_bounds__(kKeyThreads)
 k_keygen(int bbox_mode, const BHParams* __restrict__ bp, float2* __restrict__ pos_in, float* mass_in,
          float2* __restrict__ pos_out, float* mass_out, uint32_t n, uint32_t* __restrict__ keys,
-         uint32_t* __restrict__ hist, int passes, uint32_t* __restrict__ valid_count) {
+         uint32_t* __restrict__ hist, int passes, uint32_t* __restrict__ valid_count, uint32_t* __restrict__ mmax) {
     pdl_enter();
-    keygen_body(grid_blk(), bbox_mode, bp, pos_in, mass_in, pos_out, mass_out, n, keys, hist, passes, valid_count);
+    keygen_body(grid_blk(), bbox_mode, bp, pos_in, mass_in, pos_out, mass_out, n, keys, hist, passes, valid_count,
+                mmax);
 }
 
 // ------------------------------------------------------------------------------------
@@ -335,7 +359,7 @@ __global__ void __launch_bounds__(kKeyThreads)
 k_ext_keys(float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos_out, float* mass_out, uint32_t n,
            uint32_t* __restrict__ keys, uint32_t* __restrict__ hist, int passes, uint32_t* __restrict__ valid_count,
            BHParams* __restrict__ params, const uint32_t* __restrict__ ext_in, uint32_t* __restrict__ ext_out,
-           int bits) {
+           int bits, uint32_t* __restrict__ mmax) {
     pdl_enter();
     __shared__ BHParams sp;
     if (threadIdx.x == 0) {
@@ -346,7 +370,7 @@ k_ext_keys(float2* __restrict__ pos_in, float* mass_in, float2* __restrict__ pos
         }
     }
     __syncthreads();
-    keygen_body(grid_blk(), 1, &sp, pos_in, mass_in, pos_out, mass_out, n, keys, hist, passes, valid_count);
+    keygen_body(grid_blk(), 1, &sp, pos_in, mass_in, pos_out, mass_out, n, keys, hist, passes, valid_count, mmax);
 }
 
 
@@ -592,6 +616,122 @@ __device__ __forceinline__ void meta_scan_body(const uint32_t* __restrict__ skey
     }
 }
 
+// Quadrupole mode: the exact moment sums of the sorted slots (moments.cuh).
+struct MomIn {
+    const BHParams* bp;          // box of the step
+    const uint32_t* mmax;        // float bits of the largest mass
+    int bbox;                    // box mode
+    int4* qv;                    // [N_al] integer mass and position per slot (k_records)
+    i128* prefix;                // six columns [stride] of exclusive prefixes (null: monopole mode)
+    size_t stride;               // N_al + 1
+    MomSums* agg;                // [tiles] each tile's sums
+    uint32_t* nend;              // [cap] one past the last slot of internal node j (k_nodes)
+};
+
+constexpr int kMomThreads = 256, kMomItems = 4;  // k_mom_scan: threads and slots per thread
+constexpr int kMomTile = kMomThreads * kMomItems;
+
+// one column of a slot's sums from its integer mass and position
+__device__ __forceinline__ i128 mom_column(int4 q, int ch) {
+    switch (ch) {
+        case 0: return (i128)q.x;
+        case 1: return (i128)((long long)q.x * q.y);
+        case 2: return (i128)((long long)q.x * q.z);
+        case 3: return mul_i64_i32((long long)q.x * q.y, q.y);
+        case 4: return mul_i64_i32((long long)q.x * q.y, q.z);
+        default: return mul_i64_i32((long long)q.x * q.z, q.z);
+    }
+}
+__device__ __forceinline__ i128 mom_get(const MomSums& a, int ch) {
+    return ch == 0 ? a.m : ch == 1 ? a.x : ch == 2 ? a.y : ch == 3 ? a.xx : ch == 4 ? a.xy : a.yy;
+}
+
+// Exact sums of every slot of one tile, in every thread of the block (s_w: scratch).
+__device__ __forceinline__ MomSums mom_block_total(MomSums a, MomSums* s_w) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    mom_warp_sum(a);
+    __syncthreads();  // s_w may still be read by an earlier use
+    if (lane == 0) s_w[warp] = a;
+    __syncthreads();
+    MomSums tsum;
+    mom_clear(tsum);
+    for (int w = 0; w < kMomThreads / 32; ++w) mom_add(tsum, s_w[w]);
+    return tsum;
+}
+
+// k_mom_tiles: the exact sums of each tile of kMomTile slots.
+__device__ __forceinline__ void mom_tiles_body(uint32_t tile, uint32_t nv, const MomIn& mi) {
+    __shared__ MomSums s_w[kMomThreads / 32];
+    const uint64_t first = (uint64_t)tile * kMomTile;
+    MomSums c;
+    mom_clear(c);
+#pragma unroll
+    for (int j = 0; j < kMomItems; ++j) {
+        const uint64_t sl = first + (uint64_t)j * kMomThreads + threadIdx.x;  // coalesced
+        if (sl < nv) mom_add_q(c, mi.qv[sl]);
+    }
+    const MomSums tsum = mom_block_total(c, s_w);
+    if (threadIdx.x == 0) mi.agg[tile] = tsum;
+}
+
+// k_mom_scan: the exclusive prefix of the exact sums at the slots of one tile: the sums
+// of the tiles before it (every block adds them up itself: integer sums, any order),
+// then, with the tile staged in shared memory, each thread's kMomItems consecutive slots
+// and a block scan.  The prefix is written one column at a time through shared memory,
+// so that the stores are contiguous.
+// 16-byte elements padded by one every eight: a thread's kMomItems consecutive elements
+// and a warp's consecutive elements both fall in distinct banks
+__device__ __forceinline__ int mom_pad(int i) { return i + (i >> 3); }
+
+__device__ __forceinline__ void mom_scan_body(uint32_t tile, uint32_t n_items, uint32_t nv, const MomIn& mi) {
+    __shared__ int4 s_q[kMomTile + kMomTile / 8];
+    __shared__ ulonglong2 s_out[kMomTile + kMomTile / 8];
+    __shared__ MomSums s_w[kMomThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint64_t first = (uint64_t)tile * kMomTile;
+    MomSums a;
+    mom_clear(a);
+    for (uint32_t j = t; j < tile; j += kMomThreads) mom_add(a, mom_ldcg(mi.agg + j));
+    const MomSums base = mom_block_total(a, s_w);
+    for (int k = t; k < kMomTile; k += kMomThreads) {
+        const uint64_t sl = first + k;
+        s_q[mom_pad(k)] = sl < nv ? mi.qv[sl] : make_int4(0, 0, 0, 0);
+    }
+    __syncthreads();
+    MomSums c;
+    mom_clear(c);
+#pragma unroll
+    for (int j = 0; j < kMomItems; ++j) mom_add_q(c, s_q[mom_pad(t * kMomItems + j)]);
+    MomSums incl = c;
+    mom_warp_scan(incl, lane);
+    if (lane == 31) s_w[warp] = incl;  // the last read of s_w was before the staging sync
+    __syncthreads();
+    MomSums b = base;  // this thread's first slot
+    for (int w = 0; w < warp; ++w) mom_add(b, s_w[w]);
+    b.m += incl.m - c.m;
+    b.x += incl.x - c.x;
+    b.y += incl.y - c.y;
+    b.xx += incl.xx - c.xx;
+    b.xy += incl.xy - c.xy;
+    b.yy += incl.yy - c.yy;
+    ulonglong2* out = reinterpret_cast<ulonglong2*>(mi.prefix);
+    for (int ch = 0; ch < 6; ++ch) {
+        i128 run = mom_get(b, ch);
+#pragma unroll
+        for (int j = 0; j < kMomItems; ++j) {
+            s_out[mom_pad(t * kMomItems + j)] = make_ulonglong2((unsigned long long)run,
+                                                                (unsigned long long)((u128)run >> 64));
+            run += mom_column(s_q[mom_pad(t * kMomItems + j)], ch);
+        }
+        __syncthreads();
+        for (int k = t; k < kMomTile; k += kMomThreads) {
+            const uint64_t sl = first + k;
+            if (sl < n_items) out[ch * mi.stride + sl] = s_out[mom_pad(k)];
+        }
+        __syncthreads();
+    }
+}
+
 template <int R>
 __global__ void __launch_bounds__(kScanThreads)
 k_meta_scan(const uint32_t* __restrict__ skey, uint32_t n_items, const uint32_t* __restrict__ valid_count,
@@ -600,6 +740,19 @@ k_meta_scan(const uint32_t* __restrict__ skey, uint32_t n_items, const uint32_t*
     pdl_enter();
     meta_scan_body<R>(skey, n_items, valid_count, D, E, status, ticket, internal_count, err);
 }
+// Quadrupole mode: the exact moment sums of every tile, then their exclusive prefix at
+// every slot.
+__global__ void __launch_bounds__(kMomThreads)
+k_mom_tiles(const uint32_t* __restrict__ valid_count, MomIn mi) {
+    pdl_enter();
+    mom_tiles_body(blockIdx.x, *valid_count, mi);
+}
+__global__ void __launch_bounds__(kMomThreads, 3)
+k_mom_scan(uint32_t n_items, const uint32_t* __restrict__ valid_count, MomIn mi) {
+    pdl_enter();
+    mom_scan_body(blockIdx.x, n_items, *valid_count, mi);
+}
+
 inline auto meta_scan_kernel(uint32_t lookback) {
     return lookback >= 128 ? k_meta_scan<4> : lookback >= 64 ? k_meta_scan<2> : k_meta_scan<1>;
 }
@@ -639,8 +792,10 @@ __device__ __forceinline__ void records_body(Blk blk, const uint32_t* __restrict
                                              const float2* __restrict__ pos, const float* __restrict__ mass,
                                              float4* __restrict__ rec, uint32_t* __restrict__ skip,
                                              uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al,
-                                             int* __restrict__ err) {
+                                             int* __restrict__ err, const MomIn& mi) {
     const uint32_t nv = *valid_count;
+    MomScale sc;
+    if (mi.prefix) sc = mom_scale(mi.bbox, *mi.bp, *mi.mmax);
     for (uint32_t s = blk.id * 256 + threadIdx.x; s < nv; s += blk.count * 256) {
         const int dmin = slot_dmin(skey, s, D), dmax = slot_dmax(skey, s, nv, D);
         const uint32_t Es = E[s];
@@ -656,8 +811,10 @@ __device__ __forceinline__ void records_body(Blk blk, const uint32_t* __restrict
             continue;
         }
         const float2 p = pos[i];
-        rec[leaf] = make_float4(p.x, p.y, mass[i], 0.0f);
+        const float m = mass[i];
+        rec[leaf] = make_float4(p.x, p.y, m, 0.0f);
         skip[leaf] = 1u;
+        if (mi.prefix) mi.qv[s] = mom_quantize(p, m, sc);
         for (int k = 0; k < e; ++k) node_slot[Es + k] = s;
     }
 }
@@ -666,9 +823,44 @@ __global__ void __launch_bounds__(256)
 k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ E,
           const uint32_t* __restrict__ valid_count, int D, const float2* __restrict__ pos,
           const float* __restrict__ mass, float4* __restrict__ rec, uint32_t* __restrict__ skip,
-          uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al, int* __restrict__ err) {
+          uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al, int* __restrict__ err, MomIn mi) {
     pdl_enter();
-    records_body(grid_blk(), skey, sidx, E, valid_count, D, pos, mass, rec, skip, node_slot, cap, n_al, err);
+    records_body(grid_blk(), skey, sidx, E, valid_count, D, pos, mass, rec, skip, node_slot, cap, n_al, err, mi);
+}
+
+__device__ __forceinline__ uint32_t compact_bits(uint32_t v) {  // inverse of spread_bits
+    v &= 0x55555555u;
+    v = (v | (v >> 1)) & 0x33333333u;
+    v = (v | (v >> 2)) & 0x0f0f0f0fu;
+    v = (v | (v >> 4)) & 0x00ff00ffu;
+    v = (v | (v >> 8)) & 0x0000ffffu;
+    return v;
+}
+
+// Squared distance from the centre of mass to the farthest corner of the level-d cell
+// holding `key` (the accurate mode's opening radius), in FP32 with the same operation
+// sequence as the CPU restatement:
+//   fixed box:    side = 1000 / 2^d, x0 = -500 + ix * side          (both exact)
+//   bounding box: side = 2^(D-d) * inv, x0 = cx + (ix * 2^(D-d) - 2^(D-1)) * inv
+//   m = max(|c - x0|, |x0 + side - c|) per axis, bmax^2 = fma(mx, mx, my * my)
+__device__ __forceinline__ float cell_bmax2(int bbox_mode, const BHParams& bp, int D, int d, uint32_t key, float cx,
+                                            float cy) {
+    const uint32_t pre = key >> (2 * (D - d));
+    const float ix = (float)compact_bits(pre), iy = (float)compact_bits(pre >> 1);
+    float x0, y0, side;
+    if (bbox_mode) {
+        const float w = (float)(1u << (D - d));
+        side = __fmul_rn(w, bp.inv_scale);
+        x0 = __fadd_rn(bp.cx, __fmul_rn(__fsub_rn(__fmul_rn(ix, w), (float)(1u << (D - 1))), bp.inv_scale));
+        y0 = __fadd_rn(bp.cy, __fmul_rn(__fsub_rn(__fmul_rn(iy, w), (float)(1u << (D - 1))), bp.inv_scale));
+    } else {
+        side = __fdiv_rn(2.0f * kSimSize, (float)(1u << d));
+        x0 = __fadd_rn(-kSimSize, __fmul_rn(ix, side));
+        y0 = __fadd_rn(-kSimSize, __fmul_rn(iy, side));
+    }
+    const float mx = fmaxf(fabsf(__fsub_rn(cx, x0)), fabsf(__fsub_rn(__fadd_rn(x0, side), cx)));
+    const float my = fmaxf(fabsf(__fsub_rn(cy, y0)), fabsf(__fsub_rn(__fadd_rn(y0, side), cy)));
+    return __fmaf_rn(mx, mx, __fmul_rn(my, my));
 }
 
 // Internal nodes by level: the nodes of level d are listed in levels[level_off(d) ..),
@@ -686,13 +878,16 @@ __host__ __device__ __forceinline__ uint32_t level_off(int d, uint32_t n_al) {
 // One thread per internal node (d, s): skip (the reference's count.y), the level radius
 // of TreeMoveShader.comp:70-71, the child descriptors, and the node's entry in the list
 // of its level (slots reserved per block: a shared histogram, one atomic per level).
+// Quadrupole mode (mi.prefix set): the record itself is left to k_mom_nodes, which reads
+// the node's end slot from mi.nend.
 __device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E,
                                            const uint32_t* __restrict__ counts, int D,
                                            const BHParams* __restrict__ bp, const uint32_t* __restrict__ node_slot,
                                            float4* __restrict__ rec, uint32_t* __restrict__ skip,
                                            uint4* __restrict__ kids, uint2* __restrict__ nodeinfo,
                                            uint32_t* __restrict__ level_count, uint32_t* __restrict__ levels,
-                                           uint32_t n_al, uint64_t cap, int* __restrict__ err) {
+                                           uint32_t n_al, uint64_t cap, int* __restrict__ err, const MomIn& mi,
+                                           float4* __restrict__ quad, int safe) {
     __shared__ uint32_t s_cnt[16], s_base[16];
     const uint32_t nv = counts[0], M = counts[1];
     const float radius0 = bp->radius0;
@@ -749,7 +944,8 @@ __device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__
                     }
                     kids[at] = make_uint4(kid[0], kid[1], kid[2], kid[3]);
                 }
-                rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
+                if (mi.prefix) mi.nend[j] = end;
+                else rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
                 skip[at] = end + E[end] - at;
                 nodeinfo[at] = make_uint2(ks, (uint32_t)d);  // a key of the cell, its level
                 rank = atomicAdd(&s_cnt[d], 1u);
@@ -767,63 +963,60 @@ __device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__
     }
 }
 
+// Quadrupole mode: one thread per internal node: its centre, mass, opening radius and
+// second moments from the exact prefix sums at its first slot and one past its last.
+__device__ __forceinline__ void mom_nodes_body(Blk blk, const uint32_t* __restrict__ counts, int D,
+                                               const BHParams* __restrict__ bp,
+                                               const uint32_t* __restrict__ node_slot,
+                                               const uint2* __restrict__ nodeinfo, float4* __restrict__ rec,
+                                               float4* __restrict__ quad, int safe, uint64_t cap, const MomIn& mi) {
+    const uint32_t nv = counts[0], M = counts[1];
+    const BHParams bpv = *bp;
+    const MomScale sc = mom_scale(mi.bbox, bpv, *mi.mmax);
+    for (uint32_t j = blk.id * 256 + threadIdx.x; j < M; j += blk.count * 256) {
+        const uint32_t s = node_slot[j];
+        const uint64_t at = (uint64_t)s + j;
+        if (s >= nv || at >= cap) continue;  // only after a failed sort or scan (k_nodes set the error flag)
+        const uint32_t end = mi.nend[j];
+        if (end > nv) continue;
+        const uint2 info = nodeinfo[at];
+        const int d = (int)info.y;
+        float cx, cy, m;
+        float4 q;
+        mom_node(mom_load(mi.prefix, mi.stride, end), mom_load(mi.prefix, mi.stride, s), sc, cx, cy, m, q);
+        const float r0 = __fdiv_rn(bpv.radius0, (float)(1u << (2 * d)));
+        rec[at] = make_float4(cx, cy, m, safe ? cell_bmax2(mi.bbox, bpv, D, d, info.x, cx, cy) : r0);
+        quad[at] = q;
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_mom_nodes(const uint32_t* __restrict__ counts, int D, const BHParams* __restrict__ bp,
+            const uint32_t* __restrict__ node_slot, const uint2* __restrict__ nodeinfo, float4* __restrict__ rec,
+            float4* __restrict__ quad, int safe, uint64_t cap, MomIn mi) {
+    pdl_enter();
+    mom_nodes_body(grid_blk(), counts, D, bp, node_slot, nodeinfo, rec, quad, safe, cap, mi);
+}
+
 __global__ void __launch_bounds__(256)
 k_nodes(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ E, const uint32_t* __restrict__ counts,
         int D, const BHParams* __restrict__ bp, const uint32_t* __restrict__ node_slot, float4* __restrict__ rec,
         uint32_t* __restrict__ skip, uint4* __restrict__ kids, uint2* __restrict__ nodeinfo,
         uint32_t* __restrict__ level_count, uint32_t* __restrict__ levels, uint32_t n_al, uint64_t cap,
-        int* __restrict__ err) {
+        int* __restrict__ err, MomIn mi, float4* __restrict__ quad, int safe) {
     pdl_enter();
     nodes_body(grid_blk(), skey, E, counts, D, bp, node_slot, rec, skip, kids, nodeinfo, level_count, levels, n_al,
-               cap, err);
+               cap, err, mi, quad, safe);
 }
 
-__device__ __forceinline__ uint32_t compact_bits(uint32_t v) {  // inverse of spread_bits
-    v &= 0x55555555u;
-    v = (v | (v >> 1)) & 0x33333333u;
-    v = (v | (v >> 2)) & 0x0f0f0f0fu;
-    v = (v | (v >> 4)) & 0x00ff00ffu;
-    v = (v | (v >> 8)) & 0x0000ffffu;
-    return v;
-}
-
-// Squared distance from the centre of mass to the farthest corner of the level-d cell
-// holding `key` (the accurate mode's opening radius), in FP32 with the same operation
-// sequence as the CPU restatement:
-//   fixed box:    side = 1000 / 2^d, x0 = -500 + ix * side          (both exact)
-//   bounding box: side = 2^(D-d) * inv, x0 = cx + (ix * 2^(D-d) - 2^(D-1)) * inv
-//   m = max(|c - x0|, |x0 + side - c|) per axis, bmax^2 = fma(mx, mx, my * my)
-__device__ __forceinline__ float cell_bmax2(int bbox_mode, const BHParams& bp, int D, int d, uint32_t key, float cx,
-                                            float cy) {
-    const uint32_t pre = key >> (2 * (D - d));
-    const float ix = (float)compact_bits(pre), iy = (float)compact_bits(pre >> 1);
-    float x0, y0, side;
-    if (bbox_mode) {
-        const float w = (float)(1u << (D - d));
-        side = __fmul_rn(w, bp.inv_scale);
-        x0 = __fadd_rn(bp.cx, __fmul_rn(__fsub_rn(__fmul_rn(ix, w), (float)(1u << (D - 1))), bp.inv_scale));
-        y0 = __fadd_rn(bp.cy, __fmul_rn(__fsub_rn(__fmul_rn(iy, w), (float)(1u << (D - 1))), bp.inv_scale));
-    } else {
-        side = __fdiv_rn(2.0f * kSimSize, (float)(1u << d));
-        x0 = __fadd_rn(-kSimSize, __fmul_rn(ix, side));
-        y0 = __fadd_rn(-kSimSize, __fmul_rn(iy, side));
-    }
-    const float mx = fmaxf(fabsf(__fsub_rn(cx, x0)), fabsf(__fsub_rn(__fadd_rn(x0, side), cx)));
-    const float my = fmaxf(fabsf(__fsub_rn(cy, y0)), fabsf(__fsub_rn(__fadd_rn(y0, side), cy)));
-    return __fmaf_rn(mx, mx, __fmul_rn(my, my));
-}
-
-// One child's contribution: mass, centre of mass and (internal children) moments.
-// Loads go through L2 (ld.cg): internal children were written by other threads of the
-// same launch.
+// One child's contribution: mass, centre of mass and mass moments.  Loads go through L2
+// (ld.cg): internal children were written by other threads of the same launch.
 struct KidData {
     float m, x, y;   // mass and centre of mass (particle position for a leaf)
     float mx, my;    // mass moments (x*m, y*m for a leaf)
-    float4 q;        // second central moments (zero for a leaf)
 };
 
-template <bool QUAD>
-__device__ __forceinline__ KidData kid_data(uint32_t c, const float4* rec, const float2* msum, const float4* quad) {
+__device__ __forceinline__ KidData kid_data(uint32_t c, const float4* rec, const float2* msum) {
     KidData k;
     if (c & kKidLeaf) {
         const float4 r = __ldcg(&rec[c & ~kKidLeaf]);
@@ -832,7 +1025,6 @@ __device__ __forceinline__ KidData kid_data(uint32_t c, const float4* rec, const
         k.y = r.y;
         k.mx = __fmul_rn(r.x, r.z);
         k.my = __fmul_rn(r.y, r.z);
-        k.q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     } else {
         const float4 r = __ldcg(&rec[c]);
         const float2 m2 = __ldcg(&msum[c]);
@@ -841,23 +1033,20 @@ __device__ __forceinline__ KidData kid_data(uint32_t c, const float4* rec, const
         k.y = r.y;
         k.mx = m2.x;
         k.my = m2.y;
-        k.q = QUAD ? __ldcg(&quad[c]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     return k;
 }
 
-// Mass, mass moments (children in Morton order, TreeInitShader.comp:78-80), centre of
-// mass (TreeMoveShader.comp:66-67), second central moments (QUAD) and the safe opening
-// radius (SAFE) of node `at`.
-template <bool QUAD>
+// Monopole mode: mass, mass moments (children in Morton order, TreeInitShader.comp:78-80),
+// centre of mass (TreeMoveShader.comp:66-67) and the opening radius (the safe radius
+// with GS_FLAG_SAFE_RADIUS) of node `at`.
 __device__ void compute_node(uint32_t at, int D, int safe, int bbox_mode, const BHParams& bp,
                              const uint32_t* __restrict__ skey, float4* rec, const uint4* __restrict__ kids,
-                             const uint2* __restrict__ nodeinfo, float2* msum, float4* quad) {
+                             const uint2* __restrict__ nodeinfo, float2* msum) {
     const uint4 kd = kids[at];
     const uint2 info = nodeinfo[at];                    // {a key of the cell, level}
     const float r0 = safe ? 0.0f : __ldcg(&rec[at]).w;  // the level radius k_nodes wrote
-    float sx = 0.0f, sy = 0.0f, sm = 0.0f, cx, cy;
-    float qxx = 0.0f, qxy = 0.0f, qyy = 0.0f;
+    float sx = 0.0f, sy = 0.0f, sm = 0.0f;
     if (kd.x == kKidFinest) {  // particle leaves at kd.y .. kd.y + kd.z - 1
         for (uint32_t t = 0; t < kd.z; ++t) {
             const float4 r = __ldcg(&rec[kd.y + t]);
@@ -865,29 +1054,13 @@ __device__ void compute_node(uint32_t at, int D, int safe, int bbox_mode, const 
             sy = __fadd_rn(sy, __fmul_rn(r.y, r.z));
             sm = __fadd_rn(sm, r.z);
         }
-        cx = sx;
-        cy = sy;
-        if (sm != 0.0f) {
-            cx = __fdiv_rn(sx, sm);
-            cy = __fdiv_rn(sy, sm);
-        }
-        if (QUAD) {
-            for (uint32_t t = 0; t < kd.z; ++t) {
-                const float4 r = __ldcg(&rec[kd.y + t]);
-                const float ddx = __fsub_rn(r.x, cx), ddy = __fsub_rn(r.y, cy);
-                const float tx = __fmul_rn(r.z, ddx);
-                qxx = __fmaf_rn(tx, ddx, qxx);
-                qxy = __fmaf_rn(tx, ddy, qxy);
-                qyy = __fmaf_rn(__fmul_rn(r.z, ddy), ddy, qyy);
-            }
-        }
     } else {
         // children fill the descriptor from the front; kKidNone marks the unused tail
         const uint32_t kk[4] = {kd.x, kd.y, kd.z, kd.w};
         KidData c[4];
 #pragma unroll
         for (int t = 0; t < 4; ++t)
-            if (kk[t] != kKidNone) c[t] = kid_data<QUAD>(kk[t], rec, msum, quad);
+            if (kk[t] != kKidNone) c[t] = kid_data(kk[t], rec, msum);
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
             if (kk[t] == kKidNone) continue;
@@ -895,31 +1068,13 @@ __device__ void compute_node(uint32_t at, int D, int safe, int bbox_mode, const 
             sy = __fadd_rn(sy, c[t].my);
             sm = __fadd_rn(sm, c[t].m);
         }
-        cx = sx;
-        cy = sy;
-        if (sm != 0.0f) {
-            cx = __fdiv_rn(sx, sm);
-            cy = __fdiv_rn(sy, sm);
-        }
-        if (QUAD) {  // parallel-axis sum over the children in order
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                if (kk[t] == kKidNone) continue;
-                if (!(kk[t] & kKidLeaf)) {  // internal child: its own moments
-                    qxx = __fadd_rn(qxx, c[t].q.x);
-                    qxy = __fadd_rn(qxy, c[t].q.y);
-                    qyy = __fadd_rn(qyy, c[t].q.z);
-                }
-                const float ddx = __fsub_rn(c[t].x, cx), ddy = __fsub_rn(c[t].y, cy);
-                const float tx = __fmul_rn(c[t].m, ddx);
-                qxx = __fmaf_rn(tx, ddx, qxx);
-                qxy = __fmaf_rn(tx, ddy, qxy);
-                qyy = __fmaf_rn(__fmul_rn(c[t].m, ddy), ddy, qyy);
-            }
-        }
+    }
+    float cx = sx, cy = sy;
+    if (sm != 0.0f) {
+        cx = __fdiv_rn(sx, sm);
+        cy = __fdiv_rn(sy, sm);
     }
     msum[at] = make_float2(sx, sy);
-    if (QUAD) quad[at] = make_float4(qxx, qxy, qyy, 0.0f);
     const float r = safe ? cell_bmax2(bbox_mode, bp, D, (int)info.y, info.x, cx, cy) : r0;
     rec[at] = make_float4(cx, cy, sm, r);
 }
@@ -927,48 +1082,46 @@ __device__ void compute_node(uint32_t at, int D, int safe, int bbox_mode, const 
 // Moments level by level, finest first: every node of level d is computed by one thread
 // once the launch for level d + 1 has finished, so no node waits on another.  Every node
 // sums its children in the fixed Morton order.
-template <bool QUAD>
 __device__ __forceinline__ void level_sums_body(Blk blk, int d, const uint32_t* __restrict__ level_count,
                                                 const uint32_t* __restrict__ levels, uint32_t n_al,
                                                 const uint32_t* __restrict__ skey, int D, float4* rec,
                                                 const uint4* __restrict__ kids, const uint2* __restrict__ nodeinfo,
-                                                float2* msum, float4* quad, int safe, int bbox_mode,
+                                                float2* msum, int safe, int bbox_mode,
                                                 const BHParams* __restrict__ bpp) {
     const uint32_t cnt = min(level_count[d], level_cap(d, n_al));
     const uint32_t* list = levels + level_off(d, n_al);
     const BHParams bp = *bpp;
     for (uint32_t t = blk.id * 256 + threadIdx.x; t < cnt; t += blk.count * 256)
-        compute_node<QUAD>(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum, quad);
+        compute_node(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum);
 }
 
 // Levels kLevelTop .. 0 in one block, a barrier between levels.
-template <bool QUAD>
 __device__ __forceinline__ void top_sums_body(const uint32_t* __restrict__ level_count,
                                               const uint32_t* __restrict__ levels, uint32_t n_al,
                                               const uint32_t* __restrict__ skey, int D, float4* rec,
                                               const uint4* __restrict__ kids, const uint2* __restrict__ nodeinfo,
-                                              float2* msum, float4* quad, int safe, int bbox_mode,
+                                              float2* msum, int safe, int bbox_mode,
                                               const BHParams* __restrict__ bpp) {
     const BHParams bp = *bpp;
     for (int d = min(kLevelTop, D); d >= 0; --d) {
         const uint32_t cnt = min(level_count[d], level_cap(d, n_al));
         const uint32_t* list = levels + level_off(d, n_al);
         for (uint32_t t = threadIdx.x; t < cnt; t += blockDim.x)
-            compute_node<QUAD>(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum, quad);
+            compute_node(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum);
         __syncthreads();  // level d is complete (and visible to the block) before level d - 1
     }
 }
 
-// Moments of every level in one cooperative launch: levels D .. kLevelTop + 1 spread over
-// the whole grid, a grid barrier after each, then levels kLevelTop .. 0 in block 0 with
-// block barriers.  Each level's nodes are computed exactly as by the per-level launches.
+// Monopole moments of every level in one cooperative launch: levels D .. kLevelTop + 1
+// spread over the whole grid, a grid barrier after each, then levels kLevelTop .. 0 in
+// block 0 with block barriers.  Each level's nodes are computed exactly as by the
+// per-level launches.
 constexpr int kCoopSumsThreads = 256;
 
-template <bool QUAD>
 __global__ void __launch_bounds__(kCoopSumsThreads, 2)
 k_coop_sums(const uint32_t* __restrict__ level_count, const uint32_t* __restrict__ levels, uint32_t n_al,
             const uint32_t* __restrict__ skey, int D, float4* rec, const uint4* __restrict__ kids,
-            const uint2* __restrict__ nodeinfo, float2* msum, float4* quad, int safe, int bbox_mode,
+            const uint2* __restrict__ nodeinfo, float2* msum, int safe, int bbox_mode,
             const BHParams* __restrict__ bpp, uint32_t* __restrict__ bar, int* __restrict__ err) {
     pdl_enter();
     const BHParams bp = *bpp;
@@ -977,12 +1130,11 @@ k_coop_sums(const uint32_t* __restrict__ level_count, const uint32_t* __restrict
         const uint32_t cnt = min(level_count[d], level_cap(d, n_al));
         const uint32_t* list = levels + level_off(d, n_al);
         for (uint32_t t = blockIdx.x * kCoopSumsThreads + threadIdx.x; t < cnt; t += gridDim.x * kCoopSumsThreads)
-            compute_node<QUAD>(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum, quad);
+            compute_node(list[t], D, safe, bbox_mode, bp, skey, rec, kids, nodeinfo, msum);
         target += gridDim.x;
         if (!grid_sync(bar, target, err)) return;
     }
-    if (blockIdx.x == 0)
-        top_sums_body<QUAD>(level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, quad, safe, bbox_mode, bpp);
+    if (blockIdx.x == 0) top_sums_body(level_count, levels, n_al, skey, D, rec, kids, nodeinfo, msum, safe, bbox_mode, bpp);
 }
 
 __global__ void k_set_params(BHParams* __restrict__ out, BHParams v) { *out = v; }
@@ -1026,7 +1178,19 @@ void bh_carve(gs_sim* s) {
     sim_carve(s, (void**)&w.nodeinfo, w.cap * sizeof(uint2));
     sim_carve(s, (void**)&w.node_slot, w.cap * sizeof(uint32_t));
     w.quad = nullptr;
-    if (s->p.flags & GS_FLAG_QUADRUPOLE) sim_carve(s, (void**)&w.quad, w.cap * sizeof(float4));
+    w.mom_q = nullptr;
+    w.mom_prefix = nullptr;
+    w.mom_agg = nullptr;
+    w.mom_nend = nullptr;
+    w.mom_blocks = 0;
+    if (s->p.flags & GS_FLAG_QUADRUPOLE) {
+        w.mom_blocks = (uint32_t)((n + 1 + kMomTile - 1) / kMomTile);
+        sim_carve(s, (void**)&w.quad, w.cap * sizeof(float4));
+        sim_carve(s, (void**)&w.mom_q, n * sizeof(int4));
+        sim_carve(s, (void**)&w.mom_prefix, 6 * (n + 1) * sizeof(__int128));
+        sim_carve(s, (void**)&w.mom_agg, (size_t)w.mom_blocks * sizeof(MomSums));
+        sim_carve(s, (void**)&w.mom_nend, w.cap * sizeof(uint32_t));
+    }
     w.amag = nullptr;
     if (s->p.flags & GS_FLAG_RELATIVE_MAC) sim_carve(s, (void**)&w.amag, n * sizeof(float));
     w.ext = nullptr;
@@ -1066,7 +1230,7 @@ cudaError_t bh_init(gs_sim* s) {
     int per_sm = 0, sms = 0;
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, w.quad ? k_coop_sums<true> : k_coop_sums<false>, kCoopSumsThreads, 0);
+            &per_sm, k_coop_sums, kCoopSumsThreads, 0);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     if (e == cudaSuccess && per_sm < 1) e = cudaErrorCooperativeLaunchTooLarge;
     w.sums_per_sm = per_sm;
@@ -1095,11 +1259,12 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
     if (bbox) {  // the box from the extent carried with the input set
         GS_TRY_LAUNCH(launch(next_pdl(), k_ext_keys, keygen_blocks(n), kKeyThreads, st, s->pos[in], s->mass[in],
                              s->pos[out], s->mass[out], n, w.keys[0], w.hist, w.passes, ctr + kCtrValid, w.params,
-                             (const uint32_t*)(w.ext + 4 * in), w.ext + 4 * out, w.depth));
+                             (const uint32_t*)(w.ext + 4 * in), w.ext + 4 * out, w.depth,
+                             w.quad ? ctr + kCtrMaxMass : nullptr));
     } else {
         GS_TRY_LAUNCH(launch(next_pdl(), k_keygen, keygen_blocks(n), kKeyThreads, st, 0,
                              (const BHParams*)w.params, s->pos[in], s->mass[in], s->pos[out], s->mass[out], n,
-                             w.keys[0], w.hist, w.passes, ctr + kCtrValid));
+                             w.keys[0], w.hist, w.passes, ctr + kCtrValid, w.quad ? ctr + kCtrMaxMass : nullptr));
     }
     count_launch(s);
     stage_end(s, kStageKeys, profile);
@@ -1124,29 +1289,53 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
                          ctr + kCtrInternal, s->d_err));
     count_launch(s);
     stage_end(s, kStageScan, profile);
+    MomIn mi{};
+    if (w.quad) {  // exact moment sums: integer values in k_records, prefix in k_mom_scan, moments in k_nodes
+        mi.bp = w.params;
+        mi.mmax = ctr + kCtrMaxMass;
+        mi.bbox = bbox ? 1 : 0;
+        mi.qv = w.mom_q;
+        mi.prefix = w.mom_prefix;
+        mi.stride = n + 1;
+        mi.agg = w.mom_agg;
+        mi.nend = w.mom_nend;
+    }
     stage_begin(s, kStageRecords, profile);
     GS_TRY_LAUNCH(launch(next_pdl(), k_records, grid_for(n, 256), 256, st, skey, sidx, (const uint32_t*)w.E,
                          (const uint32_t*)(ctr + kCtrValid), w.depth, (const float2*)s->pos[in],
-                         (const float*)s->mass[in], w.rec, w.skip, w.node_slot, w.cap, n, s->d_err));
+                         (const float*)s->mass[in], w.rec, w.skip, w.node_slot, w.cap, n, s->d_err, mi));
+    if (w.quad) {
+        GS_TRY_LAUNCH(launch(next_pdl(), k_mom_tiles, (int)w.mom_blocks, kMomThreads, st,
+                             (const uint32_t*)(ctr + kCtrValid), mi));
+        GS_TRY_LAUNCH(launch(next_pdl(), k_mom_scan, (int)w.mom_blocks, kMomThreads, st, n + 1,
+                             (const uint32_t*)(ctr + kCtrValid), mi));
+        count_launch(s, 2);
+    }
     GS_TRY_LAUNCH(launch(next_pdl(), k_nodes, grid_for(n, 256), 256, st, skey, (const uint32_t*)w.E,
                          (const uint32_t*)(ctr + kCtrValid), w.depth, (const BHParams*)w.params,
                          (const uint32_t*)w.node_slot, w.rec, w.skip, w.kids, w.nodeinfo, ctr + kCtrLevel, w.levels,
-                         n, w.cap, s->d_err));
+                         n, w.cap, s->d_err, mi, w.quad, (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0));
     count_launch(s, 2);
+    if (w.quad) {
+        GS_TRY_LAUNCH(launch(next_pdl(), k_mom_nodes, grid_for(n, 256), 256, st, (const uint32_t*)(ctr + kCtrValid),
+                             w.depth, (const BHParams*)w.params, (const uint32_t*)w.node_slot,
+                             (const uint2*)w.nodeinfo, w.rec, w.quad, (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0,
+                             (uint64_t)w.cap, mi));
+        count_launch(s);
+    }
     stage_end(s, kStageRecords, profile);
     stage_begin(s, kStageSums, profile);
-    {
+    if (!w.quad) {  // monopole moments, level by level (the quadrupole mode has them from k_nodes)
         const int safe = (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0;
         const int bb = bbox ? 1 : 0;
-        float4* quad = w.quad;
         const int per_sm = (int)s->shape.moment_blocks_per_sm < w.sums_per_sm ? (int)s->shape.moment_blocks_per_sm
                                                                                 : w.sums_per_sm;
-        GS_TRY_LAUNCH(launch_coop(next_pdl(), quad ? k_coop_sums<true> : k_coop_sums<false>, w.sms * per_sm,
-                                  kCoopSumsThreads, st, (const uint32_t*)(ctr + kCtrLevel), (const uint32_t*)w.levels,
-                                  n, skey, w.depth, w.rec, (const uint4*)w.kids, (const uint2*)w.nodeinfo, w.msum,
-                                  quad, safe, bb, (const BHParams*)w.params, ctr + kCtrBarrier, s->d_err));
+        GS_TRY_LAUNCH(launch_coop(next_pdl(), k_coop_sums, w.sms * per_sm, kCoopSumsThreads, st,
+                                  (const uint32_t*)(ctr + kCtrLevel), (const uint32_t*)w.levels, n, skey, w.depth,
+                                  w.rec, (const uint4*)w.kids, (const uint2*)w.nodeinfo, w.msum, safe, bb,
+                                  (const BHParams*)w.params, ctr + kCtrBarrier, s->d_err));
+        count_launch(s);
     }
-    count_launch(s);
     stage_end(s, kStageSums, profile);
     stage_begin(s, kStageForce, profile);
     const float k = s->G * s->dt_eff;  // ForceShader.comp:145 (GRAVITATIONAL_CONST * SIMULATION_TIME)
@@ -1330,7 +1519,23 @@ __global__ void __launch_bounds__(kKeyThreads) kb_keygen(BatchArgs a) {
     // box from the positions themselves)
     if (d.ext && bb.blk.id == 0 && threadIdx.x < 4) d.ext[4 * bb.out + threadIdx.x] = 0xFFFFFFFFu;
     keygen_body(bb.blk, d.bbox, d.params, d.pos[bb.in], d.mass[bb.in], d.pos[bb.out], d.mass[bb.out], d.n_al,
-                d.keys[0], d.hist, d.passes, d.counters + kCtrValid);
+                d.keys[0], d.hist, d.passes, d.counters + kCtrValid, d.quad ? d.counters + kCtrMaxMass : nullptr);
+}
+
+// the exact moment sums of a quadrupole-mode member (all fields null otherwise)
+__device__ __forceinline__ MomIn batch_mom_in(const SysDesc& d) {
+    MomIn mi{};
+    if (d.quad) {
+        mi.bp = d.params;
+        mi.mmax = d.counters + kCtrMaxMass;
+        mi.bbox = d.bbox;
+        mi.qv = d.mom_q;
+        mi.prefix = d.mom_prefix;
+        mi.stride = (size_t)d.n_al + 1;
+        mi.agg = d.mom_agg;
+        mi.nend = d.mom_nend;
+    }
+    return mi;
 }
 
 template <bool IDENTITY, int KPT, int LB>
@@ -1353,13 +1558,28 @@ __global__ void __launch_bounds__(kScanThreads) kb_meta_scan(BatchArgs a) {
                    d.counters + kCtrScan, d.counters + kCtrInternal, d.err);
 }
 
+__global__ void __launch_bounds__(kMomThreads) kb_mom_tiles(BatchArgs a) {
+    pdl_enter();
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    const MomIn mi = batch_mom_in(d);
+    if (mi.prefix) mom_tiles_body(bb.blk.id, d.counters[kCtrValid], mi);
+}
+__global__ void __launch_bounds__(kMomThreads, 2) kb_mom_scan(BatchArgs a) {
+    pdl_enter();
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    const MomIn mi = batch_mom_in(d);
+    if (mi.prefix) mom_scan_body(bb.blk.id, d.n_al + 1, d.counters[kCtrValid], mi);
+}
+
 __global__ void __launch_bounds__(256) kb_records(BatchArgs a) {
     pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     const int f = d.passes & 1;
     records_body(bb.blk, d.keys[f], d.idx[f], d.E, d.counters + kCtrValid, d.depth, d.pos[bb.in], d.mass[bb.in],
-                 d.rec, d.skip, d.node_slot, d.cap, d.n_al, d.err);
+                 d.rec, d.skip, d.node_slot, d.cap, d.n_al, d.err, batch_mom_in(d));
 }
 
 __global__ void __launch_bounds__(256) kb_nodes(BatchArgs a) {
@@ -1367,27 +1587,36 @@ __global__ void __launch_bounds__(256) kb_nodes(BatchArgs a) {
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     nodes_body(bb.blk, d.keys[d.passes & 1], d.E, d.counters + kCtrValid, d.depth, d.params, d.node_slot, d.rec,
-               d.skip, d.kids, d.nodeinfo, d.counters + kCtrLevel, d.levels, d.n_al, d.cap, d.err);
+               d.skip, d.kids, d.nodeinfo, d.counters + kCtrLevel, d.levels, d.n_al, d.cap, d.err,
+               batch_mom_in(d), d.quad, d.safe);
+}
+
+__global__ void __launch_bounds__(256) kb_mom_nodes(BatchArgs a) {
+    pdl_enter();
+    const BatchBlock bb = batch_block(a, blockIdx.x);
+    const SysDesc& d = *bb.d;
+    const MomIn mi = batch_mom_in(d);
+    if (mi.prefix)
+        mom_nodes_body(bb.blk, d.counters + kCtrValid, d.depth, d.params, d.node_slot, d.nodeinfo, d.rec, d.quad,
+                       d.safe, d.cap, mi);
 }
 
 // level lv of every system (systems shallower than lv have nothing to do)
-template <bool QUAD>
 __global__ void __launch_bounds__(256) kb_level_sums(BatchArgs a, int lv) {
     pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     if (lv > d.depth) return;
-    level_sums_body<QUAD>(bb.blk, lv, d.counters + kCtrLevel, d.levels, d.n_al, d.keys[d.passes & 1], d.depth, d.rec,
-                          d.kids, d.nodeinfo, d.msum, d.quad, d.safe, d.bbox, d.params);
+    level_sums_body(bb.blk, lv, d.counters + kCtrLevel, d.levels, d.n_al, d.keys[d.passes & 1], d.depth, d.rec,
+                    d.kids, d.nodeinfo, d.msum, d.safe, d.bbox, d.params);
 }
 
-template <bool QUAD>
 __global__ void __launch_bounds__(512) kb_top_sums(BatchArgs a) {
     pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
-    top_sums_body<QUAD>(d.counters + kCtrLevel, d.levels, d.n_al, d.keys[d.passes & 1], d.depth, d.rec, d.kids,
-                        d.nodeinfo, d.msum, d.quad, d.safe, d.bbox, d.params);
+    top_sums_body(d.counters + kCtrLevel, d.levels, d.n_al, d.keys[d.passes & 1], d.depth, d.rec, d.kids, d.nodeinfo,
+                  d.msum, d.safe, d.bbox, d.params);
 }
 
 }  // namespace
@@ -1411,6 +1640,10 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount], const gs_s
 
     d.msum = w.msum;
     d.quad = w.quad;
+    d.mom_q = w.mom_q;
+    d.mom_prefix = w.mom_prefix;
+    d.mom_agg = w.mom_agg;
+    d.mom_nend = w.mom_nend;
     d.amag = w.amag;
     d.ext = w.ext;
     d.alpha = s->p.relative_accuracy;
@@ -1441,6 +1674,7 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount], const gs_s
     blocks[kTabKeys] = (uint32_t)keygen_blocks(n);
     blocks[kTabSort] = sort_tiles_of(n, shape);
     blocks[kTabScan] = w.scan_tiles;
+    blocks[kTabMom] = w.mom_blocks;
     blocks[kTabOne] = 1;
     const uint64_t per_block = (s->p.flags & GS_FLAG_GROUP_WALK) ? (uint64_t)force_warps * kGroupSize
                                                                    : (uint64_t)kForceWarps * 32;
@@ -1500,12 +1734,17 @@ cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bo
                              (int)p.total[kTabScan], kScanThreads, st, args(kTabScan)));
     }
     GS_TRY_LAUNCH(launch(true, kb_records, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
+    if (p.quad) {
+        GS_TRY_LAUNCH(launch(true, kb_mom_tiles, (int)p.total[kTabMom], kMomThreads, st, args(kTabMom)));
+        GS_TRY_LAUNCH(launch(true, kb_mom_scan, (int)p.total[kTabMom], kMomThreads, st, args(kTabMom)));
+    }
     GS_TRY_LAUNCH(launch(true, kb_nodes, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
-    for (int lv = p.depth; lv > kLevelTop; --lv)
-        GS_TRY_LAUNCH(launch(true, p.quad ? kb_level_sums<true> : kb_level_sums<false>, (int)p.total[kTabGrid], 256,
-                             st, args(kTabGrid), lv));
-    GS_TRY_LAUNCH(launch(true, p.quad ? kb_top_sums<true> : kb_top_sums<false>, (int)p.total[kTabOne], 512, st,
-                         args(kTabOne)));
+    if (p.quad) GS_TRY_LAUNCH(launch(true, kb_mom_nodes, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
+    if (!p.quad) {  // monopole moments level by level; the quadrupole mode has them from kb_nodes
+        for (int lv = p.depth; lv > kLevelTop; --lv)
+            GS_TRY_LAUNCH(launch(true, kb_level_sums, (int)p.total[kTabGrid], 256, st, args(kTabGrid), lv));
+        GS_TRY_LAUNCH(launch(true, kb_top_sums, (int)p.total[kTabOne], 512, st, args(kTabOne)));
+    }
     const int fg = p.force_grid < (int)p.total[kTabForce] ? p.force_grid : (int)p.total[kTabForce];
     BatchForceLaunch b = batch_force(p, step, st);
     b.grid = fg;

@@ -8,10 +8,11 @@ namespace gsim {
 
 // counters layout inside the zeroed block
 // [kCtrStat..+5]: accepted interactions, records tested, node interactions (u64 each);
-// [kCtrLevel..+15]: internal nodes per level
+// [kCtrLevel..+15]: internal nodes per level; [kCtrMaxMass]: float bits of the largest
+// mass (quadrupole mode)
 enum {
     kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrLevel = 16,
-    kCtrBarrier = 32, kCtrCount = 40
+    kCtrBarrier = 32, kCtrMaxMass = 33, kCtrCount = 40
 };
 static_assert(kHostCounters + kCtrCount <= kHostWords, "counter readback fits the pinned word block");
 

@@ -102,6 +102,8 @@ struct BHParams {
     int bits;                      // cells per axis 2^bits (bounding box; 10 for the fixed box)
 };
 
+struct MomSums;  // moments.cuh
+
 struct BHWork {
     int depth = 0;        // finest level D (10 fixed box, key_bits in bounding-box mode)
     int passes = 0;       // radix passes of 8 bits
@@ -124,6 +126,12 @@ struct BHWork {
                                        // {min x, ~max x, min y, ~max y} as ordered words (ord_word)
     int sums_per_sm = 0, sms = 0;      // co-resident blocks per SM of the cooperative moments launch, SMs
     uint4* kids = nullptr;             // [cap] child descriptors of internal records
+    // quadrupole mode: exact moment sums (moments.cuh)
+    int4* mom_q = nullptr;             // [N_al] integer mass and position per sorted slot
+    __int128* mom_prefix = nullptr;    // [6][N_al + 1] exclusive prefix of the six sums per slot
+    MomSums* mom_agg = nullptr;        // [mom_blocks] sums of each tile of the moment scan
+    uint32_t* mom_nend = nullptr;      // [cap] one past the last slot of each internal node
+    uint32_t mom_blocks = 0;           // tiles of the moment scan
     uint32_t* levels = nullptr;        // internal records by level (level_off / level_cap in bh.cu)
     uint2* nodeinfo = nullptr;         // [cap] {a key of the cell, level} of an internal record
     uint32_t* node_slot = nullptr;     // [cap] start slot of internal node j (ordinal)
@@ -169,6 +177,10 @@ struct SysDesc {
     uint32_t* ext;    // extents of the two state sets (bounding-box mode), or null
     float alpha, floor2;
     uint4* kids;
+    int4* mom_q;
+    __int128* mom_prefix;
+    MomSums* mom_agg;
+    uint32_t* mom_nend;
     uint32_t* levels;
     uint2* nodeinfo;
     uint32_t* node_slot;
@@ -188,7 +200,7 @@ struct SysDesc {
 // Per-stage block tables of a batch: table t holds the exclusive prefix of the blocks each
 // system gets in stage t; a block finds its system by binary search.
 enum BatchTable {
-    kTabClear = 0, kTabBBox, kTabKeys, kTabGrid, kTabSort, kTabScan, kTabOne, kTabForce, kTabDirect, kTabCount
+    kTabClear = 0, kTabBBox, kTabKeys, kTabGrid, kTabSort, kTabScan, kTabOne, kTabForce, kTabDirect, kTabMom, kTabCount
 };
 
 // What the batched launchers need: descriptors (Barnes-Hut systems first, largest first),

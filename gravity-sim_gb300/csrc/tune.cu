@@ -227,7 +227,9 @@ struct Knob {
     std::vector<uint32_t> values;
 };
 
-std::vector<Knob> knobs_for(int algorithm, bool group_walk) {
+// quadrupole mode: the moments come from exact sums (no cooperative moments launch), so
+// the moments grid is not a knob
+std::vector<Knob> knobs_for(int algorithm, bool group_walk, bool quadrupole) {
     std::vector<Knob> k;
     if (algorithm == GS_DIRECT_SUM) {
         k.push_back({5, {2, 4}});
@@ -238,7 +240,7 @@ std::vector<Knob> knobs_for(int algorithm, bool group_walk) {
     k.push_back({1, {8, 16, 32}});
     k.push_back({2, {32, 64, 128}});
     if (group_walk) k.push_back({-1, {10, 20, 21, 40}});  // warps * 10 + short lists
-    k.push_back({7, {1, 2}});
+    if (!quadrupole) k.push_back({7, {1, 2}});
     if (algorithm == kAlgoBatch) k.push_back({5, {2, 4}});  // the batch's direct-sum members
     return k;
 }
@@ -370,7 +372,8 @@ gs_status gs_tune_shape(const gs_params* params, uint64_t n, int32_t generator, 
         if (st != GS_OK) return st;
     }
     std::memset(out, 0, sizeof *out);
-    st = descend(knobs_for(p.algorithm, (p.flags & GS_FLAG_GROUP_WALK) != 0), measure, out);
+    st = descend(knobs_for(p.algorithm, (p.flags & GS_FLAG_GROUP_WALK) != 0, (p.flags & GS_FLAG_QUADRUPOLE) != 0),
+                 measure, out);
     if (sim) gs_destroy(sim);
     if (st != GS_OK) return st;
     Entry e;
@@ -409,7 +412,9 @@ gs_status gs_tune_batch_shape(gs_batch* b, uint32_t steps, const char* cache_pat
         return time_steps(bs, fl, steps, [&]() { return gs_batch_run(b, 1); }, ms);
     };
     std::memset(out, 0, sizeof *out);
-    st = descend(knobs_for(kAlgoBatch, (key_params.flags & GS_FLAG_GROUP_WALK) != 0), measure, out);
+    st = descend(knobs_for(kAlgoBatch, (key_params.flags & GS_FLAG_GROUP_WALK) != 0,
+                           (key_params.flags & GS_FLAG_QUADRUPOLE) != 0),
+                 measure, out);
     if (st != GS_OK) {
         gs_batch_set_shape(b, &keep);
         return st;

@@ -139,7 +139,8 @@ typedef struct gs_shape {
     uint32_t force_short_lists;    /* 0: evaluate after 160 nodes / 96 leaf runs; 1: after 96 / 64 */
     uint32_t direct_targets;       /* direct-sum particles per thread (FAST math): 2 (default) or 4 */
     uint32_t direct_blocks_per_sm; /* direct-sum j-split target, blocks per SM: 1..32 (default 12) */
-    uint32_t moment_blocks_per_sm; /* blocks per SM of the cooperative moments launch: 1 or 2 (default) */
+    uint32_t moment_blocks_per_sm; /* blocks per SM of the cooperative moments launch of the monopole
+                                      mode: 1 or 2 (default); the quadrupole mode has no such launch */
 } gs_shape;
 
 /* Statistics: stage times accumulate over steps since gs_reset_stats (GS_FLAG_PROFILE);

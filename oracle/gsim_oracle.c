@@ -939,6 +939,128 @@ static float cell_bmax2(int box_mode, const bbox_params* bp, int D, int d, uint3
     return fmaf(mx, mx, my * my);
 }
 
+/* ------------------------------------------------------------------------------ */
+/* accurate-mode moments (ORC_BH_QUADRUPOLE): exact integer sums                   */
+/* ------------------------------------------------------------------------------ */
+/* Every particle is put on an integer grid: masses as m_q = rint(m 2^(31-em)) with
+ * max mass = f 2^em (f in [0.5, 1)), positions as x_q = rint(x 2^(30-e)) - rint(bx 2^(30-e))
+ * with the box centre bx and half-size h = f 2^e, clamped to +-2^30.  A node's sums M = sum m_q,
+ * X = sum m_q x_q, Y, XX = sum m_q x_q^2, XY, YY are exact 128-bit integers (no order
+ * of summation changes them), taken as differences of prefix sums over the sorted
+ * slots.  They are rounded to FP32 once:
+ *   centre  cx = bx + (f(X) / f(M)) 2^(e-30),  mass  m = f(M) 2^(em-31)
+ *   second central moments about an integer origin x0 = rint(f(X) / f(M)) near the
+ *   centre (exact: Dx = X - x0 M, Sxx = XX - x0 (X + Dx), Sxy = XY - x0 Y - y0 Dx),
+ *   Qxx = f(Sxx) - f(Dx) (f(Dx) / f(M)), Qxy = f(Sxy) - f(Dx) (f(Dy) / f(M)),
+ *   Qyy = f(Syy) - f(Dy) (f(Dy) / f(M)), scaled by 2^(2(e-30)) then 2^(em-31);
+ * f() rounds a 128-bit integer to the nearest float (ties to even).  A node of zero mass
+ * gets centre (0, 0) and zero moments.  Positions: 2^-30 of the half-size; masses:
+ * 2^-31 of the largest. */
+typedef __int128 i128;
+typedef unsigned __int128 u128;
+typedef struct {
+    i128 m, x, y, xx, xy, yy;
+} mom_sums;
+typedef struct {
+    float bx, by, iqs, ims, qs, ms;
+} mom_scale;
+
+static float i128_to_float(i128 v) {
+    const int neg = v < 0;
+    const u128 u = neg ? (u128)0 - (u128)v : (u128)v;
+    const uint64_t hi = (uint64_t)(u >> 64);
+    float f;
+    if (!hi) {
+        f = (float)(uint64_t)u;
+    } else { /* the top 64 bits with a sticky bit round like the whole value */
+        const int sh = 64 - __builtin_clzll(hi);
+        const uint64_t t = (uint64_t)(u >> sh) | (uint64_t)((u & (((u128)1 << sh) - 1)) != 0);
+        f = (float)t * ldexpf(1.0f, sh);
+    }
+    return neg ? -f : f;
+}
+
+static int exponent_of(float v, int lo, int hi) { /* v = f 2^e, f in [0.5, 1); 0 for v <= 0 */
+    int e = 0;
+    if (v > 0.0f) frexpf(v, &e);
+    return e < lo ? lo : e > hi ? hi : e;
+}
+
+static mom_scale moment_scale(float bx, float by, float half, float mmax) {
+    mom_scale s;
+    const int e = exponent_of(half, -96, 127), em = exponent_of(mmax, -94, 127);
+    s.bx = bx;
+    s.by = by;
+    s.qs = ldexpf(1.0f, 30 - e);
+    s.iqs = ldexpf(1.0f, e - 30);
+    s.ms = ldexpf(1.0f, 31 - em);
+    s.ims = ldexpf(1.0f, em - 31);
+    return s;
+}
+
+/* p 2^(30-e), b 2^(30-e) and m 2^(31-em) are exact scalings by powers of two, each
+ * rounded to the nearest integer (not p - b, which rounds to the spacing of the larger
+ * operand) */
+static inline int64_t quantize_pos(float p, float b, float qs) {
+    const float pq = rintf(p * qs), bq = rintf(b * qs);
+    if (!(fabsf(pq) < 9.0e18f) || !(fabsf(bq) < 9.0e18f)) return 0; /* beyond 64 bits, or NaN */
+    int64_t q = (int64_t)pq - (int64_t)bq;
+    if (q < -1073741824ll) q = -1073741824ll;
+    if (q > 1073741824ll) q = 1073741824ll;
+    return q;
+}
+
+static inline int64_t quantize_mass(float m, float ms) {
+    return m > 0.0f ? (int64_t)rintf(m * ms) : 0;
+}
+
+static inline void mom_add_particle(mom_sums* a, float px, float py, float m, const mom_scale* sc) {
+    const int64_t mq = quantize_mass(m, sc->ms);
+    const int64_t xq = quantize_pos(px, sc->bx, sc->qs), yq = quantize_pos(py, sc->by, sc->qs);
+    const int64_t mx = mq * xq, my = mq * yq;
+    a->m += mq;
+    a->x += mx;
+    a->y += my;
+    a->xx += (i128)mx * xq;
+    a->xy += (i128)mx * yq;
+    a->yy += (i128)my * yq;
+}
+
+static void mom_node(const mom_sums* hi, const mom_sums* lo, const mom_scale* sc, float* cx, float* cy, float* m,
+                     float* q3) {
+    mom_sums a;
+    a.m = hi->m - lo->m;
+    a.x = hi->x - lo->x;
+    a.y = hi->y - lo->y;
+    a.xx = hi->xx - lo->xx;
+    a.xy = hi->xy - lo->xy;
+    a.yy = hi->yy - lo->yy;
+    if (a.m == 0) {
+        *cx = *cy = *m = 0.0f;
+        q3[0] = q3[1] = q3[2] = 0.0f;
+        return;
+    }
+    const float mf = i128_to_float(a.m);
+    const float cxq = i128_to_float(a.x) / mf, cyq = i128_to_float(a.y) / mf;
+    *cx = sc->bx + cxq * sc->iqs;
+    *cy = sc->by + cyq * sc->iqs;
+    *m = mf * sc->ims;
+    const int64_t x0 = (int64_t)rintf(cxq), y0 = (int64_t)rintf(cyq);
+    const i128 dx = a.x - (i128)x0 * a.m, dy = a.y - (i128)y0 * a.m;
+    const i128 sxx = a.xx - (i128)x0 * (a.x + dx);
+    const i128 sxy = a.xy - (i128)x0 * a.y - (i128)y0 * dx;
+    const i128 syy = a.yy - (i128)y0 * (a.y + dy);
+    const float dxf = i128_to_float(dx), dyf = i128_to_float(dy);
+    const float ux = dxf / mf, uy = dyf / mf;
+    const float qxx = i128_to_float(sxx) - dxf * ux;
+    const float qxy = i128_to_float(sxy) - dxf * uy;
+    const float qyy = i128_to_float(syy) - dyf * uy;
+    const float s2 = sc->iqs * sc->iqs;
+    q3[0] = (qxx * s2) * sc->ims;
+    q3[1] = (qxy * s2) * sc->ims;
+    q3[2] = (qyy * s2) * sc->ims;
+}
+
 int orc_bh_sorted_step(int box_mode, uint32_t n_al, float* pos_in, float* vel_in,
                        float* mass_in, float* pos_out, float* vel_out, float* mass_out,
                        float dt, float G, float eps2, float theta2, orc_bh_out* out,
@@ -1042,71 +1164,69 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
         nmass[leaf] = mass_in[i];
     }
 
-    /* mass and mass-moment sums, finest level first */
-    for (int d = D; d >= 0; --d) {
+    if (quad) { /* accurate mode: exact integer sums over each node's particles */
+        float mmax = 0.0f;
+        for (uint32_t i = 0; i < n_al; ++i)
+            if (mass_in[i] > mmax) mmax = mass_in[i];
+        const float half = box_mode == ORC_BOX_BOUNDING ? ldexpf(bp.inv_scale, bp.bits - 1) : SIM_SIZE;
+        const float bx = box_mode == ORC_BOX_BOUNDING ? bp.cx : 0.0f;
+        const float by = box_mode == ORC_BOX_BOUNDING ? bp.cy : 0.0f;
+        const mom_scale sc = moment_scale(bx, by, half, mmax);
+        mom_sums* P = (mom_sums*)calloc((size_t)nv + 1, sizeof(mom_sums));
+        for (uint32_t t = 0; t < nv; ++t) { /* exclusive prefix over the sorted slots */
+            P[t + 1] = P[t];
+            const uint32_t i = sidx[t];
+            mom_add_particle(&P[t + 1], pos_in[2 * i], pos_in[2 * i + 1], mass_in[i], &sc);
+        }
         for (uint32_t s = 0; s < nv; ++s) {
-            if (d < dmin[s] || d > dmax[s]) continue;
-            uint64_t at = s + E[s] + (uint64_t)(d - dmin[s]);
-            uint32_t end = nend[at];
-            float sx = 0.0f, sy = 0.0f, sm = 0.0f;
-            uint32_t t = s;
-            while (t < end) {
-                if (d < D && dmin[t] <= d + 1 && d + 1 <= dmax[t]) {
-                    uint64_t ch = t + E[t] + (uint64_t)(d + 1 - dmin[t]);
-                    sx = sx + msx[ch];
-                    sy = sy + msy[ch];
-                    sm = sm + nmass[ch];
-                    t = nend[ch];
-                } else {
-                    uint32_t i = sidx[t];
-                    float m = mass_in[i];
-                    sx = sx + pos_in[2 * i] * m;
-                    sy = sy + pos_in[2 * i + 1] * m;
-                    sm = sm + m;
-                    t += 1;
-                }
+            for (int d = dmin[s]; d <= dmax[s]; ++d) {
+                uint64_t at = s + E[s] + (uint64_t)(d - dmin[s]);
+                float cx, cy, m;
+                mom_node(&P[nend[at]], &P[s], &sc, &cx, &cy, &m, &quad[3 * at]);
+                npos[2 * at] = cx;
+                npos[2 * at + 1] = cy;
+                nmass[at] = m;
+                if (flags & ORC_BH_SAFE_RADIUS) radius[at] = cell_bmax2(box_mode, &bp, D, d, skey[s], cx, cy);
             }
-            msx[at] = sx;
-            msy[at] = sy;
-            nmass[at] = sm;
-            if (sm != 0.0f) {
-                sx = sx / sm;
-                sy = sy / sm;
-            }
-            npos[2 * at] = sx;
-            npos[2 * at + 1] = sy;
-            if (quad) { /* second central moments about the centre of mass, children in order */
-                float qxx = 0.0f, qxy = 0.0f, qyy = 0.0f;
-                t = s;
+        }
+        free(P);
+    } else {
+        /* mass and mass-moment sums, finest level first, children in Morton order
+         * (TreeInitShader.comp:78-80), centre of mass TreeMoveShader.comp:66-67 */
+        for (int d = D; d >= 0; --d) {
+            for (uint32_t s = 0; s < nv; ++s) {
+                if (d < dmin[s] || d > dmax[s]) continue;
+                uint64_t at = s + E[s] + (uint64_t)(d - dmin[s]);
+                uint32_t end = nend[at];
+                float sx = 0.0f, sy = 0.0f, sm = 0.0f;
+                uint32_t t = s;
                 while (t < end) {
-                    float mc, xc, yc;
                     if (d < D && dmin[t] <= d + 1 && d + 1 <= dmax[t]) {
                         uint64_t ch = t + E[t] + (uint64_t)(d + 1 - dmin[t]);
-                        mc = nmass[ch];
-                        xc = npos[2 * ch];
-                        yc = npos[2 * ch + 1];
-                        qxx = qxx + quad[3 * ch];
-                        qxy = qxy + quad[3 * ch + 1];
-                        qyy = qyy + quad[3 * ch + 2];
+                        sx = sx + msx[ch];
+                        sy = sy + msy[ch];
+                        sm = sm + nmass[ch];
                         t = nend[ch];
                     } else {
                         uint32_t i = sidx[t];
-                        mc = mass_in[i];
-                        xc = pos_in[2 * i];
-                        yc = pos_in[2 * i + 1];
+                        float m = mass_in[i];
+                        sx = sx + pos_in[2 * i] * m;
+                        sy = sy + pos_in[2 * i + 1] * m;
+                        sm = sm + m;
                         t += 1;
                     }
-                    float ddx = xc - sx, ddy = yc - sy;
-                    float tx = mc * ddx;
-                    qxx = fmaf(tx, ddx, qxx);
-                    qxy = fmaf(tx, ddy, qxy);
-                    qyy = fmaf(mc * ddy, ddy, qyy);
                 }
-                quad[3 * at] = qxx;
-                quad[3 * at + 1] = qxy;
-                quad[3 * at + 2] = qyy;
+                msx[at] = sx;
+                msy[at] = sy;
+                nmass[at] = sm;
+                if (sm != 0.0f) {
+                    sx = sx / sm;
+                    sy = sy / sm;
+                }
+                npos[2 * at] = sx;
+                npos[2 * at + 1] = sy;
+                if (flags & ORC_BH_SAFE_RADIUS) radius[at] = cell_bmax2(box_mode, &bp, D, d, skey[s], sx, sy);
             }
-            if (flags & ORC_BH_SAFE_RADIUS) radius[at] = cell_bmax2(box_mode, &bp, D, d, skey[s], sx, sy);
         }
     }
 

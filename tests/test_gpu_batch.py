@@ -69,8 +69,8 @@ def test_mixed_batch_bit_identical(gs, flags):
         s.reset_stats()
     _run_alone(alone, 3)
     with gs.Batch(batched, flags=flags) as b:
-        # clear bbox keys 3x sort scan records nodes, moments (levels 12..5 + one top launch), force; direct
-        assert b.kernels_per_step == 1 + 1 + 1 + 3 + 1 + 1 + 1 + 9 + 1 + 1
+        # clear bbox keys 3x sort scan records, moment tiles and prefix, nodes, node moments, force; direct
+        assert b.kernels_per_step == 1 + 1 + 1 + 3 + 1 + 1 + 2 + 1 + 1 + 1 + 1
         b.run(3)
         b.sync()
         _assert_same(alone, batched, MIXED)

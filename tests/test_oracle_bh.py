@@ -90,12 +90,16 @@ def test_bounding_box_force_accuracy(gs, orc):
 
 
 def test_accurate_mode_moments_and_radius(gs, orc):
-    """Second central moments and safe opening radius of every node, against numpy."""
+    """Mass, centre of mass, second central moments and safe opening radius of every node
+    against numpy in FP64: the accurate mode takes them from exact integer sums (positions
+    on a grid of 2^-30 of the box half-size, masses of 2^-31 of the largest) rounded once,
+    so they agree to about FP32 rounding."""
     pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 3000, seed=13)
     st = orc.State(pos, vel, mass)
     r = orc.bh_step(st, box_mode=orc.BOX_BOUNDING, theta=0.35, flags=orc.ACCURATE)
     skip, npos, nmass, quad, rad = r["skip"], r["pos"], r["mass"], r["quad"], r["radius"]
     P, _, M = orc.pad_state(pos, vel, mass)
+    half = float(np.abs(P[:3000]).max()) * 2
     leaf_src = {}
     # leaves in preorder map to sorted slots in order
     leaves = np.nonzero(skip == 1)[0]
@@ -103,20 +107,41 @@ def test_accurate_mode_moments_and_radius(gs, orc):
     for li, i in zip(leaves, src):
         leaf_src[li] = i
     checked = 0
-    for n in np.nonzero(skip > 1)[0][:300]:
+    for n in np.nonzero(skip > 1)[0]:
         members = [leaf_src[q] for q in range(n + 1, n + skip[n]) if skip[q] == 1]
         m = M[members].astype(np.float64)
         x = P[members].astype(np.float64)
+        if m.sum() == 0:  # padding particles only: centre (0, 0), no moments
+            assert nmass[n] == 0 and np.all(npos[n] == 0) and np.all(quad[n] == 0)
+            continue
         c = (m[:, None] * x).sum(0) / m.sum()
+        assert abs(nmass[n] - m.sum()) <= 1e-6 * m.sum()
+        assert np.all(np.abs(npos[n] - c) <= 1e-6 * half)
         d = x - c
         sxx, sxy, syy = (m * d[:, 0] ** 2).sum(), (m * d[:, 0] * d[:, 1]).sum(), (m * d[:, 1] ** 2).sum()
-        scale = max(1e-3, sxx + syy)
-        assert abs(quad[n, 0] - sxx) < 1e-3 * scale and abs(quad[n, 1] - sxy) < 1e-3 * scale
-        assert abs(quad[n, 2] - syy) < 1e-3 * scale
+        scale = sxx + syy + m.sum() * (1e-6 * half) ** 2
+        assert abs(quad[n, 0] - sxx) < 1e-5 * scale and abs(quad[n, 1] - sxy) < 1e-5 * scale
+        assert abs(quad[n, 2] - syy) < 1e-5 * scale
         # every member lies within the opening radius of the centre of mass
         assert np.max(((x - npos[n].astype(np.float64)) ** 2).sum(1)) <= rad[n] * (1 + 1e-5) + 1e-9
         checked += 1
-    assert checked > 100
+    assert checked > 1000
+
+
+@pytest.mark.parametrize("box_mode", [0, 1])
+def test_accurate_mode_moments_independent_of_input_order(gs, orc, box_mode):
+    """Exact sums: reversing the particles' input order changes no bit of any node's
+    centre, mass or second moments (the reference's FP32 child sums would)."""
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, 4000, size=300.0, seed=17)
+    rev = slice(None, None, -1)
+    out = []
+    for p, v, m in ((pos, vel, mass), (pos[rev].copy(), vel[rev].copy(), mass[rev].copy())):
+        st = orc.State(p, v, m)
+        r = orc.bh_step(st, box_mode=box_mode, theta=0.35, flags=orc.ACCURATE)
+        internal = r["skip"] > 1
+        out.append((r["pos"][internal], r["mass"][internal], r["quad"][internal]))
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_accurate_mode_theta_zero_is_direct_sum(gs, orc):
