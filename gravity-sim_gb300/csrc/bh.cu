@@ -891,9 +891,12 @@ __device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__
     __shared__ uint32_t s_cnt[16], s_base[16];
     const uint32_t nv = counts[0], M = counts[1];
     const float radius0 = bp->radius0;
+    const bool lists = mi.prefix == nullptr;  // the level lists serve only the level-by-level moments
     for (uint32_t j0 = blk.id * 256; j0 < M; j0 += blk.count * 256) {  // uniform over the block
-        if (threadIdx.x < 16) s_cnt[threadIdx.x] = 0u;
-        __syncthreads();
+        if (lists) {
+            if (threadIdx.x < 16) s_cnt[threadIdx.x] = 0u;
+            __syncthreads();
+        }
         const uint32_t j = j0 + threadIdx.x;
         int d = -1;
         uint32_t at = 0, rank = 0;
@@ -948,9 +951,10 @@ __device__ __forceinline__ void nodes_body(Blk blk, const uint32_t* __restrict__
                 else rec[at] = make_float4(0.0f, 0.0f, 0.0f, __fdiv_rn(radius0, (float)(1u << (2 * d))));
                 skip[at] = end + E[end] - at;
                 nodeinfo[at] = make_uint2(ks, (uint32_t)d);  // a key of the cell, its level
-                rank = atomicAdd(&s_cnt[d], 1u);
+                if (lists) rank = atomicAdd(&s_cnt[d], 1u);
             }
         }
+        if (!lists) continue;
         __syncthreads();
         if (threadIdx.x < 16 && s_cnt[threadIdx.x]) s_base[threadIdx.x] = atomicAdd(&level_count[threadIdx.x], s_cnt[threadIdx.x]);
         __syncthreads();
@@ -1174,7 +1178,9 @@ void bh_carve(gs_sim* s) {
     sim_carve(s, (void**)&w.skip, (w.cap + 32) * sizeof(uint32_t));
     sim_carve(s, (void**)&w.msum, w.cap * sizeof(float2));
     sim_carve(s, (void**)&w.kids, w.cap * sizeof(uint4));
-    sim_carve(s, (void**)&w.levels, (size_t)level_off(w.depth + 1, (uint32_t)n) * sizeof(uint32_t));
+    w.levels = nullptr;  // internal records by level: only the level-by-level moments read them
+    if (!(s->p.flags & GS_FLAG_QUADRUPOLE))
+        sim_carve(s, (void**)&w.levels, (size_t)level_off(w.depth + 1, (uint32_t)n) * sizeof(uint32_t));
     sim_carve(s, (void**)&w.nodeinfo, w.cap * sizeof(uint2));
     sim_carve(s, (void**)&w.node_slot, w.cap * sizeof(uint32_t));
     w.quad = nullptr;
