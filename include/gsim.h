@@ -71,15 +71,20 @@ typedef enum gs_math_mode { GS_MATH_FAST = 0, GS_MATH_REFERENCE = 1 } gs_math_mo
 #define GS_FLAG_COUNT_INTERACTIONS 0x8u /* count accepted Barnes-Hut interactions */
 /* Accurate Barnes-Hut mode (no counterpart in the reference, whose opening rule
  * s^2/2 <= d^2 theta^2 with monopoles is tens of percent off at theta = 1).  The tree
- * (keys, order, topology, centres of mass) is unchanged; these flags add:
- *   QUADRUPOLE   second central moments per node, quadrupole term for accepted nodes
+ * (keys, order, topology) is unchanged; these flags add:
+ *   QUADRUPOLE   second central moments per node, quadrupole term for accepted nodes;
+ *                every node's mass, centre of mass and second moments come from exact
+ *                integer sums over its particles (masses on a grid of 2^-31 of the
+ *                largest, positions of 2^-30 of the box half-size; masses <= 0 count
+ *                as 0), rounded to FP32 once, so they do not depend on the order in
+ *                which particles are added (the reference's FP32 child sums do)
  *   SAFE_RADIUS  opening radius = squared distance from the centre of mass to the
  *                farthest cell corner (equals s^2/2 for a centred mass)
  *   GROUP_WALK   each warp's 64 particles (two per lane) share one walk that tests
  *                records against up to four sub-boxes of the group, 32 records at a
  *                time, and sums interaction items densely
- * GS_FLAGS_ACCURATE sets all three (theta = 0.35 gives <= 1e-3 RMS force error on the
- * 500k spiral). */
+ * GS_FLAGS_ACCURATE sets all three (theta = 0.3 gives <= 1e-3 RMS force error on the
+ * 500k spiral at most steps; GS_FLAG_RELATIVE_MAC below does so at every step). */
 #define GS_FLAG_QUADRUPOLE 0x10u
 #define GS_FLAG_SAFE_RADIUS 0x20u
 #define GS_FLAG_GROUP_WALK 0x40u
