@@ -62,6 +62,9 @@ cudaError_t BatchEngine::init(int dev) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&moments.side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&moments.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&moments.join, cudaEventDisableTiming);
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&staged[k], cudaEventDisableTiming);
     return e;
 }
@@ -70,6 +73,7 @@ void BatchEngine::destroy() {
     cudaSetDevice(device);
     if (root) (void)wait_stream(root, 0);
     if (side) (void)wait_stream(side, 0);
+    if (moments.side) (void)wait_stream(moments.side, 0);
     for (int k = 0; k < 2; ++k) {
         if (d_block[k]) cudaFreeAsync(d_block[k], root);
         if (h_stage[k]) cudaFreeHost(h_stage[k]);
@@ -82,6 +86,10 @@ void BatchEngine::destroy() {
     if (join) cudaEventDestroy(join);
     if (root) cudaStreamDestroy(root);
     if (side) cudaStreamDestroy(side);
+    if (moments.fork) cudaEventDestroy(moments.fork);
+    if (moments.join) cudaEventDestroy(moments.join);
+    if (moments.side) cudaStreamDestroy(moments.side);
+    moments = StepFork{};
     fork = join = nullptr;
     root = side = nullptr;
 }
@@ -217,7 +225,7 @@ cudaError_t BatchEngine::enqueue(uint32_t par, bool estimate) {
         e = cudaEventRecord(fork, root);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
     }
-    if (e == cudaSuccess) e = bh_batch_step(plan, par, root, estimate);
+    if (e == cudaSuccess) e = bh_batch_step(plan, par, root, estimate, moments);
     if (e == cudaSuccess) e = direct_batch_step(plan, par, both ? side : root);
     if (both) {
         if (e == cudaSuccess) e = cudaEventRecord(join, side);

@@ -15,6 +15,7 @@ struct BatchEngine {
     cudaStream_t root = nullptr;  // Barnes-Hut stages; the step's order point
     cudaStream_t side = nullptr;  // the direct-sum launch, beside the Barnes-Hut stages
     cudaEvent_t fork = nullptr, join = nullptr;
+    StepFork moments;            // the quadrupole moment prefix, beside the node layout
     std::vector<gs_sim*> order;  // plan order: Barnes-Hut largest first, then direct sum
     std::vector<int> parity0;    // each member's compute-input set when the plan was built
     uint64_t step = 0;           // steps enqueued since then

@@ -1310,10 +1310,20 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
     GS_TRY_LAUNCH(launch(next_pdl(), k_records, grid_for(n, 256), 256, st, skey, sidx, (const uint32_t*)w.E,
                          (const uint32_t*)(ctr + kCtrValid), w.depth, (const float2*)s->pos[in],
                          (const float*)s->mass[in], w.rec, w.skip, w.node_slot, w.cap, n, s->d_err, mi));
+    // Quadrupole mode without stage events: the moment prefix (k_mom_tiles, k_mom_scan)
+    // and the node layout (k_nodes) read only what k_records and the scan wrote and write
+    // disjoint buffers, so the prefix runs on the second stream beside k_nodes and
+    // k_mom_nodes waits for both.
+    const bool fork = w.quad && pdl;
+    cudaStream_t mst = fork ? s->side : st;
+    if (fork) {
+        GS_TRY_LAUNCH(cudaEventRecord(s->fork_ev, st));
+        GS_TRY_LAUNCH(cudaStreamWaitEvent(mst, s->fork_ev, 0));
+    }
     if (w.quad) {
-        GS_TRY_LAUNCH(launch(next_pdl(), k_mom_tiles, (int)w.mom_blocks, kMomThreads, st,
+        GS_TRY_LAUNCH(launch(fork ? false : next_pdl(), k_mom_tiles, (int)w.mom_blocks, kMomThreads, mst,
                              (const uint32_t*)(ctr + kCtrValid), mi));
-        GS_TRY_LAUNCH(launch(next_pdl(), k_mom_scan, (int)w.mom_blocks, kMomThreads, st, n + 1,
+        GS_TRY_LAUNCH(launch(fork ? true : next_pdl(), k_mom_scan, (int)w.mom_blocks, kMomThreads, mst, n + 1,
                              (const uint32_t*)(ctr + kCtrValid), mi));
         count_launch(s, 2);
     }
@@ -1322,6 +1332,11 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
                          (const uint32_t*)w.node_slot, w.rec, w.skip, w.kids, w.nodeinfo, ctr + kCtrLevel, w.levels,
                          n, w.cap, s->d_err, mi, w.quad, (s->p.flags & GS_FLAG_SAFE_RADIUS) ? 1 : 0));
     count_launch(s, 2);
+    if (fork) {  // the join: k_mom_nodes follows both streams with a plain launch
+        GS_TRY_LAUNCH(cudaEventRecord(s->join_ev, mst));
+        GS_TRY_LAUNCH(cudaStreamWaitEvent(st, s->join_ev, 0));
+        first = true;
+    }
     if (w.quad) {
         GS_TRY_LAUNCH(launch(next_pdl(), k_mom_nodes, grid_for(n, 256), 256, st, (const uint32_t*)(ctr + kCtrValid),
                              w.depth, (const BHParams*)w.params, (const uint32_t*)w.node_slot,
@@ -1723,7 +1738,7 @@ int bh_batch_force_grid(const BatchPlan& p) {
     return e == cudaSuccess && grid > 0 ? grid : 152;
 }
 
-cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bool estimate) {
+cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bool estimate, const StepFork& f) {
     if (!p.n_bh) return cudaSuccess;
     auto args = [&](int tab) { return BatchArgs{p.d_descs, p.d_tab[tab], p.n_bh, step}; };
     // the clear follows whatever the stream did before; every later stage overlaps its
@@ -1740,12 +1755,23 @@ cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bo
                              (int)p.total[kTabScan], kScanThreads, st, args(kTabScan)));
     }
     GS_TRY_LAUNCH(launch(true, kb_records, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
+    // the moment prefix beside the node layout, as in bh_step
+    const bool fork = p.quad && f.side;
+    cudaStream_t mst = fork ? f.side : st;
+    if (fork) {
+        GS_TRY_LAUNCH(cudaEventRecord(f.fork, st));
+        GS_TRY_LAUNCH(cudaStreamWaitEvent(mst, f.fork, 0));
+    }
     if (p.quad) {
-        GS_TRY_LAUNCH(launch(true, kb_mom_tiles, (int)p.total[kTabMom], kMomThreads, st, args(kTabMom)));
-        GS_TRY_LAUNCH(launch(true, kb_mom_scan, (int)p.total[kTabMom], kMomThreads, st, args(kTabMom)));
+        GS_TRY_LAUNCH(launch(!fork, kb_mom_tiles, (int)p.total[kTabMom], kMomThreads, mst, args(kTabMom)));
+        GS_TRY_LAUNCH(launch(true, kb_mom_scan, (int)p.total[kTabMom], kMomThreads, mst, args(kTabMom)));
     }
     GS_TRY_LAUNCH(launch(true, kb_nodes, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
-    if (p.quad) GS_TRY_LAUNCH(launch(true, kb_mom_nodes, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
+    if (fork) {
+        GS_TRY_LAUNCH(cudaEventRecord(f.join, mst));
+        GS_TRY_LAUNCH(cudaStreamWaitEvent(st, f.join, 0));
+    }
+    if (p.quad) GS_TRY_LAUNCH(launch(!fork, kb_mom_nodes, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
     if (!p.quad) {  // monopole moments level by level; the quadrupole mode has them from kb_nodes
         for (int lv = p.depth; lv > kLevelTop; --lv)
             GS_TRY_LAUNCH(launch(true, kb_level_sums, (int)p.total[kTabGrid], 256, st, args(kTabGrid), lv));

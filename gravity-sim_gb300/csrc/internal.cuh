@@ -226,6 +226,8 @@ struct gs_sim {
     uint64_t n = 0, n_al = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;     // second stream of a step's fork (quadrupole moment prefix)
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     float2* pos[2] = {nullptr, nullptr};
     float2* vel[2] = {nullptr, nullptr};
     float* mass[2] = {nullptr, nullptr};
@@ -362,7 +364,13 @@ void direct_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount], const 
 // j-chunks the direct sum of `s` splits into under a shape (its scratch holds direct_max_chunks)
 uint32_t direct_chunks_needed(const gs_sim* s, const gs_shape& sh);
 int bh_batch_force_grid(const BatchPlan& p);
-cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bool estimate);
+// A second stream and two events: the moment prefix of the quadrupole mode runs there,
+// beside the node layout (no fork when `side` is null).
+struct StepFork {
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bool estimate, const StepFork& f);
 cudaError_t direct_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st);
 void bh_set_final_keys(gs_sim* s);
 

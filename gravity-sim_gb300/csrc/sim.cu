@@ -176,6 +176,7 @@ void free_sim(gs_sim* s) {
     if (!s) return;
     cudaSetDevice(s->device);
     if (s->stream) (void)wait_stream(s->stream, s->timeout_ns);
+    if (s->side) (void)wait_stream(s->side, s->timeout_ns);
     free_snapshot_ring(s);
     for (auto& g : s->graph)
         if (g) cudaGraphExecDestroy(g);
@@ -184,6 +185,9 @@ void free_sim(gs_sim* s) {
     for (auto& e : s->ev)
         if (e) cudaEventDestroy(e);
     if (s->batch_done) cudaEventDestroy(s->batch_done);
+    if (s->fork_ev) cudaEventDestroy(s->fork_ev);
+    if (s->join_ev) cudaEventDestroy(s->join_ev);
+    if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->h_err) cudaFreeHost(s->h_err);
     delete s;
@@ -456,6 +460,9 @@ gs_status gs_create(const gs_params* params, uint64_t n, const float* pos, const
     GS_TRY(keep_pool_memory(s->device));
     GS_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     GS_TRY(cudaEventCreateWithFlags(&s->batch_done, cudaEventDisableTiming));
+    GS_TRY(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    GS_TRY(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
+    GS_TRY(cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming));
     GS_TRY(cudaMallocHost((void**)&s->h_err, kHostWords * sizeof(int)));
     shape_for(params, n, &s->shape);
     for (auto& e : s->ev) GS_TRY(cudaEventCreate(&e));
