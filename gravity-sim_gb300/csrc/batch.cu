@@ -81,6 +81,9 @@ void BatchEngine::destroy() {
         d_block[k] = h_stage[k] = nullptr;
         staged[k] = nullptr;
     }
+    if (d_heavy) cudaFreeAsync(d_heavy, root);
+    d_heavy = nullptr;
+    heavy_cap = 0;
     if (root) (void)wait_stream(root, 0);
     if (fork) cudaEventDestroy(fork);
     if (join) cudaEventDestroy(join);
@@ -205,6 +208,21 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
     p.count = bh0 && (bh0->p.flags & GS_FLAG_COUNT_INTERACTIONS);
     p.direct_exact = dir0 && dir0->p.math_mode == GS_MATH_REFERENCE;
     p.direct_plain = dir0 && (dir0->p.flags & GS_FLAG_PLAIN_SUM);
+    // the costly-group list of the relative criterion: one entry per group of 64 slots of
+    // every member that has the criterion (stream-ordered growth, like the plan blocks)
+    size_t groups = 0;
+    for (size_t i = 0; i < p.n_bh; ++i)
+        if (order[i]->bh.heavy_flag) groups += order[i]->n_al / 64 + 1;
+    if (groups && p.quad && p.group) {
+        if (heavy_cap < groups) {
+            if (d_heavy) GS_CUDA(cudaFreeAsync(d_heavy, root));
+            d_heavy = nullptr;
+            heavy_cap = 0;
+            GS_CUDA(cudaMallocAsync((void**)&d_heavy, groups * sizeof(uint2), root));
+            heavy_cap = groups;
+        }
+        p.d_heavy = d_heavy;
+    }
     if (bh0) p.force_grid = bh_batch_force_grid(p);  // resident blocks of the persistent force launch
     plan = p;
     cur = k;

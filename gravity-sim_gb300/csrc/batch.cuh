@@ -26,6 +26,8 @@ struct BatchEngine {
     void* h_stage[2] = {nullptr, nullptr};
     size_t h_bytes[2] = {0, 0};
     cudaEvent_t staged[2] = {nullptr, nullptr};  // the copy out of staging k is done
+    uint2* d_heavy = nullptr;                    // costly groups of a step, all members
+    size_t heavy_cap = 0;                        // entries d_heavy holds
     gs_shape shape{};                            // launch shapes of the batched kernels
 
     cudaError_t init(int dev);

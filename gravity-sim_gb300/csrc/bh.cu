@@ -819,13 +819,27 @@ __device__ __forceinline__ void records_body(Blk blk, const uint32_t* __restrict
     }
 }
 
+// The costly groups of the step (relative criterion, quadrupole mode): a flag per group
+// and the list the traversal's warp pairs take (heavy_list_body).  Written by the records
+// kernel, which every later stage of the step follows by a full dependency (the moment
+// prefix starts after it completes).
+struct HeavyOut {
+    const float* amag;  // null: no costly groups
+    uint8_t* flag;
+    uint2* list;
+    uint32_t* count;
+    uint32_t tag;
+};
+
 __global__ void __launch_bounds__(256)
 k_records(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ E,
           const uint32_t* __restrict__ valid_count, int D, const float2* __restrict__ pos,
           const float* __restrict__ mass, float4* __restrict__ rec, uint32_t* __restrict__ skip,
-          uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al, int* __restrict__ err, MomIn mi) {
+          uint32_t* __restrict__ node_slot, uint64_t cap, uint32_t n_al, int* __restrict__ err, MomIn mi,
+          HeavyOut ho) {
     pdl_enter();
     records_body(grid_blk(), skey, sidx, E, valid_count, D, pos, mass, rec, skip, node_slot, cap, n_al, err, mi);
+    if (ho.amag) heavy_list_body(grid_blk(), sidx, valid_count, ho.amag, n_al, ho.flag, ho.list, ho.count, ho.tag);
 }
 
 __device__ __forceinline__ uint32_t compact_bits(uint32_t v) {  // inverse of spread_bits
@@ -1198,7 +1212,13 @@ void bh_carve(gs_sim* s) {
         sim_carve(s, (void**)&w.mom_nend, w.cap * sizeof(uint32_t));
     }
     w.amag = nullptr;
-    if (s->p.flags & GS_FLAG_RELATIVE_MAC) sim_carve(s, (void**)&w.amag, n * sizeof(float));
+    w.heavy_flag = nullptr;
+    w.heavy_list = nullptr;
+    if (s->p.flags & GS_FLAG_RELATIVE_MAC) {
+        sim_carve(s, (void**)&w.amag, n * sizeof(float));
+        sim_carve(s, (void**)&w.heavy_flag, (n / kGroupSize + 1) * sizeof(uint8_t));
+        sim_carve(s, (void**)&w.heavy_list, (n / kGroupSize + 1) * sizeof(uint2));
+    }
     w.ext = nullptr;
     if (bbox) sim_carve(s, (void**)&w.ext, 8 * sizeof(uint32_t));
     sim_carve(s, (void**)&w.bbox_part, kBBoxBlocks * 4 * sizeof(float));
@@ -1306,10 +1326,14 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
         mi.agg = w.mom_agg;
         mi.nend = w.mom_nend;
     }
+    // costly groups of the relative criterion's main pass, walked by warp pairs
+    const bool heavy = w.heavy_flag && w.quad && (s->p.flags & GS_FLAG_GROUP_WALK);
+    HeavyOut ho{};
+    if (heavy) ho = HeavyOut{w.amag, w.heavy_flag, w.heavy_list, ctr + kCtrHeavy, 0u};
     stage_begin(s, kStageRecords, profile);
     GS_TRY_LAUNCH(launch(next_pdl(), k_records, grid_for(n, 256), 256, st, skey, sidx, (const uint32_t*)w.E,
                          (const uint32_t*)(ctr + kCtrValid), w.depth, (const float2*)s->pos[in],
-                         (const float*)s->mass[in], w.rec, w.skip, w.node_slot, w.cap, n, s->d_err, mi));
+                         (const float*)s->mass[in], w.rec, w.skip, w.node_slot, w.cap, n, s->d_err, mi, ho));
     // Quadrupole mode without stage events: the moment prefix (k_mom_tiles, k_mom_scan)
     // and the node layout (k_nodes) read only what k_records and the scan wrote and write
     // disjoint buffers, so the prefix runs on the second stream beside k_nodes and
@@ -1394,6 +1418,11 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
     f.stat = stat;
     f.err = s->d_err;
     f.amag = w.amag;
+    if (heavy) {
+        f.heavy = w.heavy_flag;
+        f.heavy_list = w.heavy_list;
+        f.heavy_count = ctr + kCtrHeavy;
+    }
     auto run = exact ? force_launch_exact : force_launch_fast;
     if (f.group && estimate && w.amag && f.quad) {  // |a| of groups that have none, by the theta test
         ForceLaunch e = f;
@@ -1594,13 +1623,17 @@ __global__ void __launch_bounds__(kMomThreads, 2) kb_mom_scan(BatchArgs a) {
     if (mi.prefix) mom_scan_body(bb.blk.id, d.n_al + 1, d.counters[kCtrValid], mi);
 }
 
-__global__ void __launch_bounds__(256) kb_records(BatchArgs a) {
+__global__ void __launch_bounds__(256) kb_records(BatchArgs a, uint2* __restrict__ heavy_list,
+                                                  uint32_t* __restrict__ heavy_count) {
     pdl_enter();
     const BatchBlock bb = batch_block(a, blockIdx.x);
     const SysDesc& d = *bb.d;
     const int f = d.passes & 1;
     records_body(bb.blk, d.keys[f], d.idx[f], d.E, d.counters + kCtrValid, d.depth, d.pos[bb.in], d.mass[bb.in],
                  d.rec, d.skip, d.node_slot, d.cap, d.n_al, d.err, batch_mom_in(d));
+    if (heavy_list && d.amag)  // the costly groups of every member with the relative criterion
+        heavy_list_body(bb.blk, d.idx[f], d.counters + kCtrValid, d.amag, d.n_al, d.heavy, heavy_list, heavy_count,
+                        (uint32_t)(bb.d - a.descs));
 }
 
 __global__ void __launch_bounds__(256) kb_nodes(BatchArgs a) {
@@ -1666,6 +1699,7 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount], const gs_s
     d.mom_agg = w.mom_agg;
     d.mom_nend = w.mom_nend;
     d.amag = w.amag;
+    d.heavy = w.heavy_flag;
     d.ext = w.ext;
     d.alpha = s->p.relative_accuracy;
     d.floor2 = s->floor2;
@@ -1728,6 +1762,10 @@ static BatchForceLaunch batch_force(const BatchPlan& p, uint32_t step, cudaStrea
     b.quad = p.quad;
     b.count = p.count;
     b.shape = p.shape;
+    if (p.d_heavy) {
+        b.heavy_list = p.d_heavy;
+        b.heavy_work = p.d_work + 2;
+    }
     return b;
 }
 
@@ -1754,7 +1792,8 @@ cudaError_t bh_batch_step(const BatchPlan& p, uint32_t step, cudaStream_t st, bo
         GS_TRY_LAUNCH(launch(true, lb >= 128 ? kb_meta_scan<4> : lb >= 64 ? kb_meta_scan<2> : kb_meta_scan<1>,
                              (int)p.total[kTabScan], kScanThreads, st, args(kTabScan)));
     }
-    GS_TRY_LAUNCH(launch(true, kb_records, (int)p.total[kTabGrid], 256, st, args(kTabGrid)));
+    GS_TRY_LAUNCH(launch(true, kb_records, (int)p.total[kTabGrid], 256, st, args(kTabGrid), p.d_heavy,
+                         p.d_heavy ? p.d_work + 2 : nullptr));
     // the moment prefix beside the node layout, as in bh_step
     const bool fork = p.quad && f.side;
     cudaStream_t mst = fork ? f.side : st;

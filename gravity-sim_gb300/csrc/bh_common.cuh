@@ -9,10 +9,10 @@ namespace gsim {
 // counters layout inside the zeroed block
 // [kCtrStat..+5]: accepted interactions, records tested, node interactions (u64 each);
 // [kCtrLevel..+15]: internal nodes per level; [kCtrMaxMass]: float bits of the largest
-// mass (quadrupole mode)
+// mass (quadrupole mode); [kCtrHeavy]: entries of the costly-group list
 enum {
     kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrLevel = 16,
-    kCtrBarrier = 32, kCtrMaxMass = 33, kCtrCount = 40
+    kCtrBarrier = 32, kCtrMaxMass = 33, kCtrHeavy = 34, kCtrCount = 40
 };
 static_assert(kHostCounters + kCtrCount <= kHostWords, "counter readback fits the pinned word block");
 
@@ -91,6 +91,40 @@ __device__ __forceinline__ uint32_t batch_sys(const uint32_t* __restrict__ first
         else hi = mid;
     }
     return lo;
+}
+
+// Costly groups of the relative criterion's main pass (their walks run on warp pairs,
+// force_kernels.cuh): every previous |a| of the group known and the smallest below
+// kHeavyRatio times the largest.
+constexpr float kHeavyRatio = 0.1f;
+
+// One warp per group: the group's flag for the main traversal and, for a costly group, an
+// entry {tag, group} of the list the warp pairs take (relative criterion, main pass).
+__device__ __forceinline__ void heavy_list_body(Blk blk, const uint32_t* __restrict__ sidx,
+                                                const uint32_t* __restrict__ counts, const float* __restrict__ amag,
+                                                uint32_t n_al, uint8_t* __restrict__ flag, uint2* __restrict__ list,
+                                                uint32_t* __restrict__ list_count, uint32_t tag) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t nv = counts[0];
+    const uint32_t G = (nv + kGroupSize - 1) / kGroupSize;
+    const uint32_t wpb = blockDim.x >> 5;
+    for (uint32_t grp = blk.id * wpb + warp; grp < G; grp += blk.count * wpb) {
+        const uint32_t s0 = grp * kGroupSize + lane, s1 = s0 + 32;
+        const uint32_t i0 = s0 < nv ? sidx[s0] : 0u, i1 = s1 < nv ? sidx[s1] : 0u;
+        const bool v0 = s0 < nv && i0 < n_al, v1 = s1 < nv && i1 < n_al;
+        const float a0 = v0 ? amag[i0] : INFINITY, a1 = v1 ? amag[i1] : INFINITY;
+        const bool unknown = __any_sync(0xffffffffu, isnan(a0) || isnan(a1));
+        float amin = fminf(a0, a1), amax = fmaxf(v0 ? a0 : 0.0f, v1 ? a1 : 0.0f);
+        for (int o = 16; o; o >>= 1) {
+            amin = fminf(amin, __shfl_xor_sync(0xffffffffu, amin, o));
+            amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+        }
+        const bool heavy = !unknown && amin < kHeavyRatio * amax;
+        if (lane == 0) {
+            flag[grp] = heavy ? 1u : 0u;
+            if (heavy) list[atomicAdd(list_count, 1u)] = make_uint2(tag, grp);
+        }
+    }
 }
 
 struct BatchArgs {

@@ -122,6 +122,8 @@ struct BHWork {
     float2* msum = nullptr;            // [cap]
     float4* quad = nullptr;            // [cap] {sxx, sxy, syy, -} (GS_FLAG_QUADRUPOLE)
     float* amag = nullptr;             // [n_al] |a| of the last step, NaN: unknown (GS_FLAG_RELATIVE_MAC)
+    uint8_t* heavy_flag = nullptr;     // [n_al / 64] costly group (walked by a warp pair), relative criterion
+    uint2* heavy_list = nullptr;       // [n_al / 64] {0, group} of the costly groups of the step
     uint32_t* ext = nullptr;           // [2][4] extent of each state set's positions (bounding-box mode):
                                        // {min x, ~max x, min y, ~max y} as ordered words (ord_word)
     int sums_per_sm = 0, sms = 0;      // co-resident blocks per SM of the cooperative moments launch, SMs
@@ -174,6 +176,7 @@ struct SysDesc {
     float2* msum;
     float4* quad;
     float* amag;      // relative criterion: |a| per particle, or null for the theta test
+    uint8_t* heavy;   // relative criterion: costly-group flag per group of 64 slots
     uint32_t* ext;    // extents of the two state sets (bounding-box mode), or null
     float alpha, floor2;
     uint4* kids;
@@ -210,7 +213,9 @@ struct BatchPlan {
     SysDesc* d_descs = nullptr;
     uint32_t* d_tab[kTabCount] = {};
     uint32_t total[kTabCount] = {};
-    uint32_t* d_work = nullptr;  // [0] next force block, [1] next estimate-pass block
+    uint32_t* d_work = nullptr;  // [0] next force block, [1] next estimate-pass block,
+                                 // [2] entries of d_heavy, [3] next entry for a warp pair
+    uint2* d_heavy = nullptr;    // {member, group} of the costly groups of a step (relative criterion)
     int passes = 0;
     int depth = 0;               // finest level of the Barnes-Hut members (all share the box mode)
     bool bbox = false, quad = false, group = false, exact = false, count = false, direct_exact = false;
@@ -336,6 +341,11 @@ struct ForceLaunch {
     int* err = nullptr;
     float* amag = nullptr;
     uint32_t* ext = nullptr;
+    // costly groups walked by warp pairs (relative criterion, main pass): flag per group,
+    // the step's list and its length
+    const uint8_t* heavy = nullptr;
+    const uint2* heavy_list = nullptr;
+    const uint32_t* heavy_count = nullptr;
 };
 cudaError_t force_launch_fast(const ForceLaunch& f);
 cudaError_t force_launch_exact(const ForceLaunch& f);
@@ -351,6 +361,8 @@ struct BatchForceLaunch {
     int grid = 0;
     bool group = false, quad = false, count = false, estimate = false;
     gs_shape shape{};
+    const uint2* heavy_list = nullptr;  // the batch's costly groups, or null
+    uint32_t* heavy_work = nullptr;     // [0] entries, [1] next entry
 };
 cudaError_t batch_force_launch_fast(const BatchForceLaunch& b, int* grid_out);
 cudaError_t batch_force_launch_exact(const BatchForceLaunch& b, int* grid_out);

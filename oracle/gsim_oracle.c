@@ -458,10 +458,17 @@ static void walk_warp(void* p, uint64_t item, int worker) {
  *   - every particle of the group sums the accepted nodes (quadrupole term) and the
  *     particle leaves (monopoles) separately, each in walk order, into a node and a leaf
  *     accumulator; its acceleration is node + leaf; then it is integrated.
- * The CUDA kernel (bh.cu, force_group_body) batches its evaluations differently; with
- * this accumulation rule the batching changes no bit. */
+ *   - a costly group (relative criterion, every previous |a| known, smallest below
+ *     HEAVY_RATIO times the largest) is walked by two warps at once: pops take the top
+ *     min(64, size) records, and item i of the node list (record i of the leaf runs) goes
+ *     to part (i / 32) mod 2; each part sums its items in walk order from zero, and the
+ *     node (leaf) accumulator is part 0 + part 1.  The set of tested and accepted records
+ *     is the same as with 32-record pops; only the order of the sums differs.
+ * The CUDA kernel (force_kernels.cuh, force_group_body / force_pair_body) batches its
+ * evaluations differently; with this accumulation rule the batching changes no bit. */
+#define HEAVY_RATIO 0.1f
 #define GROUP_SIZE 64
-#define GROUP_STACK_CAP 2048
+#define GROUP_STACK_CAP 4096
 #define GMAX 64
 /* One walk of a group: every valid lane's node and leaf accelerations (ax/ay[l][0] node,
  * [1] leaf) for the opening test `relative` (tol2 = (alpha a_min)^2, with the floor) or
@@ -469,18 +476,23 @@ static void walk_warp(void* p, uint64_t item, int worker) {
 static void group_walk_once(const walk_ctx* c, uint64_t w, uint32_t G, int nvalid, const int* valid,
                             const float* px, const float* py, const float* gx0, const float* gx1,
                             const float* gy0, const float* gy1, int relative, float tol2, float theta2,
-                            float (*ax)[2], float (*ay)[2], uint64_t* inter_out, uint64_t* visits_out,
+                            int pair, float (*ax)[2], float (*ay)[2], uint64_t* inter_out, uint64_t* visits_out,
                             uint32_t* max_size_out) {
     (void)w;
-    for (uint32_t l = 0; l < G; ++l) ax[l][0] = ay[l][0] = ax[l][1] = ay[l][1] = 0.0f;
-    uint32_t stack[GROUP_STACK_CAP + 160];
+    /* accumulators per particle, part and kind (node 0, leaf 1) */
+    static _Thread_local float acx[GMAX][2][2], acy[GMAX][2][2];
+    for (uint32_t l = 0; l < G; ++l)
+        for (int q = 0; q < 2; ++q) acx[l][q][0] = acy[l][q][0] = acx[l][q][1] = acy[l][q][1] = 0.0f;
+    const uint32_t width = pair ? 2 * WARP : WARP;
+    uint64_t n_node_items = 0, n_leaf_items = 0; /* item indices in walk order */
+    static _Thread_local uint32_t stack[GROUP_STACK_CAP + 4 * 2 * WARP];
     uint32_t size = 1, max_size = *max_size_out;
     stack[0] = 0;
     uint64_t inter = 0, visits = 0;
     while (size) {
-        uint32_t np = size < WARP ? size : WARP;
+        uint32_t np = size < width ? size : width;
         uint32_t base = size - np;
-        uint32_t popped[WARP];
+        uint32_t popped[2 * WARP];
         for (uint32_t j = 0; j < np; ++j) popped[j] = stack[base + j];
         size = base;
         for (uint32_t j = 0; j < np; ++j) {
@@ -509,6 +521,7 @@ static void group_walk_once(const walk_ctx* c, uint64_t w, uint32_t G, int nvali
             if (accept) { /* one item: the record itself (a leaf only when the root is one) */
                 const float nx = c->npos[2 * n], ny = c->npos[2 * n + 1], nm = c->nmass[n];
                 const int a = sk > 1 ? 0 : 1;
+                const int q = pair ? (int)((n_node_items++ >> 5) & 1u) : 0;
                 const quad_terms qt = c->quad ? quad_node(c->quad[3 * n], c->quad[3 * n + 1], c->quad[3 * n + 2])
                                               : quad_node(0.0f, 0.0f, 0.0f);
                 for (uint32_t l = 0; l < G; ++l) {
@@ -516,11 +529,11 @@ static void group_walk_once(const walk_ctx* c, uint64_t w, uint32_t G, int nvali
                     float dx = nx - px[l], dy = ny - py[l];
                     float d2 = pair_d2(dx, dy, c->eps2);
                     if (c->quad && sk > 1) {
-                        quad_accumulate(dx, dy, d2, nm, qt, &ax[l][a], &ay[l][a]);
+                        quad_accumulate(dx, dy, d2, nm, qt, &acx[l][q][a], &acy[l][q][a]);
                     } else {
                         float sc = pair_scale(nm, d2);
-                        ax[l][a] = fmaf(dx, sc, ax[l][a]);
-                        ay[l][a] = fmaf(dy, sc, ay[l][a]);
+                        acx[l][q][a] = fmaf(dx, sc, acx[l][q][a]);
+                        acy[l][q][a] = fmaf(dy, sc, acy[l][q][a]);
                     }
                 }
                 inter += (uint64_t)nvalid;
@@ -535,18 +548,19 @@ static void group_walk_once(const walk_ctx* c, uint64_t w, uint32_t G, int nvali
                     for (uint32_t q = ch; q < r; ++q) {
                         const float nx = c->npos[2 * q], ny = c->npos[2 * q + 1], nm = c->nmass[q];
                         const int a = 1;
+                        const int pq = pair ? (int)((n_leaf_items++ >> 5) & 1u) : 0;
                         for (uint32_t l = 0; l < G; ++l) {
                             if (!valid[l]) continue;
                             float dx = nx - px[l], dy = ny - py[l];
                             float sc = pair_scale(nm, pair_d2(dx, dy, c->eps2));
-                            ax[l][a] = fmaf(dx, sc, ax[l][a]);
-                            ay[l][a] = fmaf(dy, sc, ay[l][a]);
+                            acx[l][pq][a] = fmaf(dx, sc, acx[l][pq][a]);
+                            acy[l][pq][a] = fmaf(dy, sc, acy[l][pq][a]);
                         }
                     }
                     inter += (uint64_t)nvalid * (r - ch);
                     ch = r;
                 } else {
-                    if (size < GROUP_STACK_CAP + 160) stack[size] = ch;
+                    if (size < GROUP_STACK_CAP + 4 * 2 * WARP) stack[size] = ch;
                     ++size;
                     ch += c->skip[ch];
                 }
@@ -555,6 +569,11 @@ static void group_walk_once(const walk_ctx* c, uint64_t w, uint32_t G, int nvali
         if (size > max_size) max_size = size;
         if (size > GROUP_STACK_CAP) size = GROUP_STACK_CAP; /* reported through max_stack */
     }
+    for (uint32_t l = 0; l < G; ++l)
+        for (int a = 0; a < 2; ++a) {
+            ax[l][a] = pair ? acx[l][0][a] + acx[l][1][a] : acx[l][0][a];
+            ay[l][a] = pair ? acy[l][0][a] + acy[l][1][a] : acy[l][0][a];
+        }
     *inter_out += inter;
     *visits_out += visits;
     *max_size_out = max_size;
@@ -606,11 +625,12 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
             if (isnan(a) || isnan(amin)) amin = NAN;
             else if (a < amin) amin = a;
         }
+    const int amag_known = c->amag_in && !isnan(amin);
     if (c->amag_in && isnan(amin)) {
         /* no previous |a| for some particle (first step after a reset): estimate every
          * particle's |a| of the group by a walk with the theta test, then open nodes by the
          * relative criterion with those estimates */
-        group_walk_once(c, w, G, nvalid, valid, px, py, gx0, gx1, gy0, gy1, 0, 0.0f, c->theta2, ax, ay, &inter,
+        group_walk_once(c, w, G, nvalid, valid, px, py, gx0, gx1, gy0, gy1, 0, 0.0f, c->theta2, 0, ax, ay, &inter,
                         &visits, &max_size);
         amin = INFINITY;
         for (uint32_t l = 0; l < G; ++l) {
@@ -622,8 +642,17 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
     }
     const int relative = c->amag_in && amin >= 0.0f;
     const float tol = c->rel_alpha * amin, tol2 = tol * tol;
-    group_walk_once(c, w, G, nvalid, valid, px, py, gx0, gx1, gy0, gy1, relative, tol2, c->theta2, ax, ay, &inter,
-                    &visits, &max_size);
+    /* a costly group: every previous |a| known and the smallest below HEAVY_RATIO times
+     * the largest; walked by a warp pair (64-record pops, two-part sums) */
+    int pair = 0;
+    if (relative && amag_known) {
+        float amax = 0.0f;
+        for (uint32_t l = 0; l < G; ++l)
+            if (valid[l]) amax = fmaxf(amax, c->amag_in[c->src[(uint32_t)w * G + l]]);
+        pair = amin < HEAVY_RATIO * amax;
+    }
+    group_walk_once(c, w, G, nvalid, valid, px, py, gx0, gx1, gy0, gy1, relative, tol2, c->theta2, pair, ax, ay,
+                    &inter, &visits, &max_size);
     for (uint32_t l = 0; l < G; ++l) {
         if (!valid[l]) continue;
         uint32_t i = c->src[(uint32_t)w * G + l];
