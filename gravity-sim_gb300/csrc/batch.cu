@@ -212,7 +212,7 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
     // every member that has the criterion (stream-ordered growth, like the plan blocks)
     size_t groups = 0;
     for (size_t i = 0; i < p.n_bh; ++i)
-        if (order[i]->bh.heavy_flag) groups += order[i]->n_al / 64 + 1;
+        if (order[i]->bh.heavy_flag && order[i]->n_al >= kHeavyMinParticles) groups += order[i]->n_al / 64 + 1;
     if (groups && p.quad && p.group) {
         if (heavy_cap < groups) {
             if (d_heavy) GS_CUDA(cudaFreeAsync(d_heavy, root));

@@ -1327,7 +1327,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
         mi.nend = w.mom_nend;
     }
     // costly groups of the relative criterion's main pass, walked by warp pairs
-    const bool heavy = w.heavy_flag && w.quad && (s->p.flags & GS_FLAG_GROUP_WALK);
+    const bool heavy = w.heavy_flag && w.quad && (s->p.flags & GS_FLAG_GROUP_WALK) && n >= kHeavyMinParticles;
     HeavyOut ho{};
     if (heavy) ho = HeavyOut{w.amag, w.heavy_flag, w.heavy_list, ctr + kCtrHeavy, 0u};
     stage_begin(s, kStageRecords, profile);
@@ -1421,7 +1421,7 @@ cudaError_t bh_step(gs_sim* s, int in, int out, bool profile, bool estimate) {
     if (heavy) {
         f.heavy = w.heavy_flag;
         f.heavy_list = w.heavy_list;
-        f.heavy_count = ctr + kCtrHeavy;
+        f.heavy_work = ctr + kCtrHeavy;
     }
     auto run = exact ? force_launch_exact : force_launch_fast;
     if (f.group && estimate && w.amag && f.quad) {  // |a| of groups that have none, by the theta test
@@ -1631,7 +1631,7 @@ __global__ void __launch_bounds__(256) kb_records(BatchArgs a, uint2* __restrict
     const int f = d.passes & 1;
     records_body(bb.blk, d.keys[f], d.idx[f], d.E, d.counters + kCtrValid, d.depth, d.pos[bb.in], d.mass[bb.in],
                  d.rec, d.skip, d.node_slot, d.cap, d.n_al, d.err, batch_mom_in(d));
-    if (heavy_list && d.amag)  // the costly groups of every member with the relative criterion
+    if (heavy_list && d.heavy)  // the costly groups of every large member with the relative criterion
         heavy_list_body(bb.blk, d.idx[f], d.counters + kCtrValid, d.amag, d.n_al, d.heavy, heavy_list, heavy_count,
                         (uint32_t)(bb.d - a.descs));
 }
@@ -1699,7 +1699,7 @@ void bh_batch_desc(gs_sim* s, SysDesc& d, uint32_t blocks[kTabCount], const gs_s
     d.mom_agg = w.mom_agg;
     d.mom_nend = w.mom_nend;
     d.amag = w.amag;
-    d.heavy = w.heavy_flag;
+    d.heavy = s->n_al >= kHeavyMinParticles ? w.heavy_flag : nullptr;  // costly groups paired
     d.ext = w.ext;
     d.alpha = s->p.relative_accuracy;
     d.floor2 = s->floor2;

@@ -9,7 +9,7 @@ namespace gsim {
 // counters layout inside the zeroed block
 // [kCtrStat..+5]: accepted interactions, records tested, node interactions (u64 each);
 // [kCtrLevel..+15]: internal nodes per level; [kCtrMaxMass]: float bits of the largest
-// mass (quadrupole mode); [kCtrHeavy]: entries of the costly-group list
+// mass (quadrupole mode); [kCtrHeavy]: entries of the costly-group list, [+1] the next one
 enum {
     kCtrSort = 0, kCtrScan = 4, kCtrBBox = 5, kCtrValid = 6, kCtrInternal = 7, kCtrStat = 8, kCtrLevel = 16,
     kCtrBarrier = 32, kCtrMaxMass = 33, kCtrHeavy = 34, kCtrCount = 40

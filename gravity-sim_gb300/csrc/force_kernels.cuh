@@ -855,21 +855,36 @@ template <bool SHORT>
 using GroupSmemOf = GroupSmem<SHORT ? 96 : 160, SHORT ? 64 : 128>;
 
 // Shared memory of a traversal block: a walk per warp, and with HEAVY (the main pass of
-// the relative criterion) the same bytes as a walk per warp pair.
+// the relative criterion) the bytes of warps 2p and 2p + 1 also hold the walk of warp pair
+// p, so that a pair done with costly groups starts its own warps' walks at once.
 template <bool SHORT, int WARPS, bool HEAVY>
 struct ForceSmem {
     GroupSmemOf<SHORT> warp[WARPS];
+    __device__ __forceinline__ GroupSmemOf<SHORT>& walk(int w) { return warp[w]; }
+};
+template <bool SHORT>
+union PairSlot {
+    GroupSmemOf<SHORT> warp[2];
+    PairSmem pair;
 };
 template <bool SHORT, int WARPS>
 struct ForceSmem<SHORT, WARPS, true> {
-    union {
-        GroupSmemOf<SHORT> warp[WARPS];
-        PairSmem pair[WARPS / 2];
-    };
+    PairSlot<SHORT> slot[WARPS / 2];
+    __device__ __forceinline__ GroupSmemOf<SHORT>& walk(int w) { return slot[w >> 1].warp[w & 1]; }
 };
 
-// With HEAVY the first heavy_blocks blocks walk the listed costly groups, a warp pair per
-// group (heavy_list[u].y), before the other blocks' single-warp walks of the rest.
+// The next listed costly group for warp pair `pair` (hwork[0] entries, hwork[1] the next
+// to take), or a value >= hwork[0] when none is left.  Both warps of the pair call it.
+__device__ __forceinline__ uint32_t pair_ticket(uint32_t* __restrict__ hwork, uint32_t cnt, uint32_t* s_u, int pair) {
+    if ((threadIdx.x & 63u) == 0) s_u[pair] = __ldcg(&hwork[1]) < cnt ? atomicAdd(&hwork[1], 1u) : cnt;
+    pair_sync(pair);
+    const uint32_t u = s_u[pair];
+    pair_sync(pair);  // read by both warps before the pair's next ticket
+    return u;
+}
+
+// With HEAVY every warp pair first walks listed costly groups (heavy_list[u].y, taken in
+// order from hwork) and then each warp its own group: the costly walks start first.
 template <bool EXACT, bool QUAD, bool COUNT, bool ESTIMATE, int WARPS, bool SHORT, bool HEAVY>
 __global__ void __launch_bounds__(WARPS * 32)
 k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ counts,
@@ -879,32 +894,28 @@ k_force_group(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ sk
               uint32_t n_al, float eps2, float theta2, float k, float hdt, uint32_t cap,
               unsigned long long* __restrict__ stat, int* __restrict__ err, float* __restrict__ amag, float alpha,
               float floor2, uint32_t* __restrict__ ext, const uint8_t* __restrict__ heavy,
-              const uint2* __restrict__ heavy_list, const uint32_t* __restrict__ heavy_count, uint32_t heavy_blocks) {
+              const uint2* __restrict__ heavy_list, uint32_t* __restrict__ hwork) {
     pdl_enter();
     __shared__ ForceSmem<SHORT, WARPS, HEAVY> sm;
-    Blk blk = grid_blk();
     if constexpr (HEAVY) {
         static_assert(QUAD && !ESTIMATE && WARPS % 2 == 0, "warp pairs walk costly groups of the relative main pass");
-        if (blockIdx.x < heavy_blocks) {
-            const int pair = (int)(threadIdx.x >> 6), wp = (int)((threadIdx.x >> 5) & 1u);
-            const uint32_t stride = heavy_blocks * (WARPS / 2), cnt = *heavy_count;
-            for (uint32_t u = blockIdx.x * (WARPS / 2) + pair; u < cnt; u += stride)
-                force_pair_body<EXACT, COUNT>(heavy_list[u].y, pair, wp, sm.pair[pair], sidx, skey, counts, rec, skip,
-                                              quad, kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2, k,
-                                              hdt, cap, stat, err, amag, alpha, floor2, ext);
-            return;
-        }
-        blk = Blk{blockIdx.x - heavy_blocks, gridDim.x - heavy_blocks};
+        __shared__ uint32_t s_u[WARPS / 2];
+        const int pair = (int)(threadIdx.x >> 6), wp = (int)((threadIdx.x >> 5) & 1u);
+        const uint32_t cnt = hwork[0];
+        for (uint32_t u; (u = pair_ticket(hwork, cnt, s_u, pair)) < cnt;)
+            force_pair_body<EXACT, COUNT>(heavy_list[u].y, pair, wp, sm.slot[pair].pair, sidx, skey, counts, rec, skip,
+                                          quad, kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2, k, hdt,
+                                          cap, stat, err, amag, alpha, floor2, ext);
     }
-    force_group_body<EXACT, QUAD, COUNT, ESTIMATE, WARPS>(blk, sm.warp[threadIdx.x >> 5], sidx, skey, counts, rec, skip,
-                                                   quad, kids, pos_in, vel_in, pos_out, vel_out, acc_rec, n_al, eps2,
-                                                   theta2, k, hdt, cap, stat, err, amag, alpha, floor2, ext,
-                                                   HEAVY ? heavy : nullptr);
+    force_group_body<EXACT, QUAD, COUNT, ESTIMATE, WARPS>(grid_blk(), sm.walk((int)(threadIdx.x >> 5)), sidx, skey,
+                                                   counts, rec, skip, quad, kids, pos_in, vel_in, pos_out, vel_out,
+                                                   acc_rec, n_al, eps2, theta2, k, hdt, cap, stat, err, amag, alpha,
+                                                   floor2, ext, HEAVY ? heavy : nullptr);
 }
 
 // Batched: a persistent grid; with HEAVY each warp pair first takes costly groups
-// {member, group} from the batch's list (hwork[0] entries, hwork[1] the next), then every
-// block takes block units of the members from `work`.
+// {member, group} from the batch's list, then every block takes block units of the
+// members from `work`.
 template <bool EXACT, bool QUAD, bool COUNT, bool ESTIMATE, int WARPS, bool SHORT, bool HEAVY>
 __global__ void __launch_bounds__(WARPS * 32)
 kb_force_group(BatchArgs a, uint32_t* __restrict__ work, const uint2* __restrict__ heavy_list,
@@ -917,21 +928,16 @@ kb_force_group(BatchArgs a, uint32_t* __restrict__ work, const uint2* __restrict
         __shared__ uint32_t s_u[WARPS / 2];
         const int pair = (int)(threadIdx.x >> 6), wp = (int)((threadIdx.x >> 5) & 1u);
         const uint32_t cnt = hwork[0];
-        for (;;) {
-            if ((threadIdx.x & 63u) == 0) s_u[pair] = atomicAdd(&hwork[1], 1u);
-            pair_sync(pair);
-            const uint32_t u = s_u[pair];
-            pair_sync(pair);
-            if (u >= cnt) break;
+        for (uint32_t u; (u = pair_ticket(hwork, cnt, s_u, pair)) < cnt;) {
             const uint2 e = heavy_list[u];
             const SysDesc& d = a.descs[e.x];
             const int in = (int)((d.parity + a.step) & 1u), out = in ^ 1;
             const int f = d.passes & 1;
-            force_pair_body<EXACT, COUNT>(e.y, pair, wp, sm.pair[pair], d.idx[f], d.keys[f], d.counters + kCtrValid,
-                                          d.rec, d.skip, d.quad, d.kids, d.pos[in], d.vel[in], d.pos[out],
-                                          d.vel[out], d.acc, d.n_al, d.eps2, d.k, d.hdt, d.cap,
-                                          (unsigned long long*)(d.counters + kCtrStat), d.err, d.amag, d.alpha,
-                                          d.floor2, d.ext ? d.ext + 4 * out : nullptr);
+            force_pair_body<EXACT, COUNT>(e.y, pair, wp, sm.slot[pair].pair, d.idx[f], d.keys[f],
+                                          d.counters + kCtrValid, d.rec, d.skip, d.quad, d.kids, d.pos[in],
+                                          d.vel[in], d.pos[out], d.vel[out], d.acc, d.n_al, d.eps2, d.k, d.hdt,
+                                          d.cap, (unsigned long long*)(d.counters + kCtrStat), d.err, d.amag,
+                                          d.alpha, d.floor2, d.ext ? d.ext + 4 * out : nullptr);
         }
     }
     const uint32_t total = __ldg(&a.first[a.nsys]);
@@ -944,10 +950,10 @@ kb_force_group(BatchArgs a, uint32_t* __restrict__ work, const uint2* __restrict
         const BatchBlock bb = batch_block(a, b);
         const SysDesc& d = *bb.d;
         const int f = d.passes & 1;
-        force_group_body<EXACT, QUAD, COUNT, ESTIMATE, WARPS>(bb.blk, sm.warp[threadIdx.x >> 5], d.idx[f], d.keys[f],
-                                             d.counters + kCtrValid, d.rec, d.skip, d.quad, d.kids, d.pos[bb.in],
-                                             d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al, d.eps2,
-                                             d.theta2, d.k, d.hdt, d.cap,
+        force_group_body<EXACT, QUAD, COUNT, ESTIMATE, WARPS>(bb.blk, sm.walk((int)(threadIdx.x >> 5)), d.idx[f],
+                                             d.keys[f], d.counters + kCtrValid, d.rec, d.skip, d.quad, d.kids,
+                                             d.pos[bb.in], d.vel[bb.in], d.pos[bb.out], d.vel[bb.out], d.acc, d.n_al,
+                                             d.eps2, d.theta2, d.k, d.hdt, d.cap,
                                              (unsigned long long*)(d.counters + kCtrStat), d.err, d.amag, d.alpha,
                                              d.floor2, d.ext ? d.ext + 4 * bb.out : nullptr,
                                              HEAVY ? d.heavy : nullptr);
@@ -984,7 +990,7 @@ namespace {
 using GroupFn = void (*)(const uint32_t*, const uint32_t*, const uint32_t*, const float4*, const uint32_t*,
                          const float4*, const uint4*, const float2*, const float2*, float2*, float2*, float2*,
                          uint32_t, float, float, float, float, uint32_t, unsigned long long*, int*, float*, float,
-                         float, uint32_t*, const uint8_t*, const uint2*, const uint32_t*, uint32_t);
+                         float, uint32_t*, const uint8_t*, const uint2*, uint32_t*);
 using BatchGroupFn = void (*)(BatchArgs, uint32_t*, const uint2*, uint32_t*);
 
 // The group-walk kernel of one shape (counting variants: the default shape only); heavy:
@@ -1065,20 +1071,11 @@ cudaError_t force_launch_impl(const ForceLaunch& f) {
     int warps = 2;
     const bool heavy = f.heavy && f.quad && !f.estimate;
     GroupFn fn = pick_group<EXACT>(f.count, f.shape, f.quad, f.estimate, heavy, &warps);
-    // costly groups first: two warp pairs per SM, each taking every (pairs)-th listed group
-    uint32_t heavy_blocks = 0;
-    if (heavy) {
-        int dev = 0, sms = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return e;
-        heavy_blocks = (uint32_t)(2 * (sms > 0 ? sms : 152) / (warps / 2));
-    }
-    const int blocks = (int)((f.n_al / kGroupSize + warps - 1) / warps + heavy_blocks);
+    const int blocks = (int)((f.n_al / kGroupSize + warps - 1) / warps);
     return launch(f.pdl, fn, blocks, warps * 32, f.st, f.sidx, f.skey, f.counts, f.rec, f.skip, f.quad_m, f.kids,
                   f.pos_in, f.vel_in, f.pos_out, f.vel_out, f.acc, f.n_al, f.eps2, f.theta2, f.k, f.hdt, f.cap,
                   f.stat, f.err, f.amag, f.alpha, f.floor2, f.ext, heavy ? f.heavy : nullptr,
-                  heavy ? f.heavy_list : nullptr, heavy ? f.heavy_count : nullptr, heavy_blocks);
+                  heavy ? f.heavy_list : nullptr, heavy ? f.heavy_work : nullptr);
 }
 
 template <bool EXACT>

@@ -26,6 +26,9 @@ constexpr int kFixedDepth = 10;             // finest level of the fixed box
 constexpr int kBBoxBits = 12;               // default per-axis bits in bounding-box mode (24-bit keys)
 constexpr int kBBoxMaxBits = 15;            // largest per-axis bits (30-bit keys, 4 radix passes)
 constexpr uint32_t kKeyRemovedSort = 1u << 20;  // sort key of removed particles (fixed box)
+// Relative criterion: costly groups are walked by warp pairs in systems of at least this
+// many (padded) particles; smaller systems walk every group on one warp.
+constexpr uint32_t kHeavyMinParticles = 1u << 17;
 constexpr uint32_t kKeyRemoved = 0xFFFFFFFFu;   // reported key of removed particles
 
 // pinned host words of a system (gs_sim::h_err): the device error word at 0, counter
@@ -342,10 +345,10 @@ struct ForceLaunch {
     float* amag = nullptr;
     uint32_t* ext = nullptr;
     // costly groups walked by warp pairs (relative criterion, main pass): flag per group,
-    // the step's list and its length
+    // the step's list, and [0] its length, [1] the next entry to take
     const uint8_t* heavy = nullptr;
     const uint2* heavy_list = nullptr;
-    const uint32_t* heavy_count = nullptr;
+    uint32_t* heavy_work = nullptr;
 };
 cudaError_t force_launch_fast(const ForceLaunch& f);
 cudaError_t force_launch_exact(const ForceLaunch& f);

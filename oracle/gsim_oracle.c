@@ -458,7 +458,8 @@ static void walk_warp(void* p, uint64_t item, int worker) {
  *   - every particle of the group sums the accepted nodes (quadrupole term) and the
  *     particle leaves (monopoles) separately, each in walk order, into a node and a leaf
  *     accumulator; its acceleration is node + leaf; then it is integrated.
- *   - a costly group (relative criterion, every previous |a| known, smallest below
+ *   - a costly group (relative criterion, a system of at least HEAVY_MIN_PARTICLES
+ *     padded particles, every previous |a| of the group known, the smallest below
  *     HEAVY_RATIO times the largest) is walked by two warps at once: pops take the top
  *     min(64, size) records, and item i of the node list (record i of the leaf runs) goes
  *     to part (i / 32) mod 2; each part sums its items in walk order from zero, and the
@@ -467,6 +468,7 @@ static void walk_warp(void* p, uint64_t item, int worker) {
  * The CUDA kernel (force_kernels.cuh, force_group_body / force_pair_body) batches its
  * evaluations differently; with this accumulation rule the batching changes no bit. */
 #define HEAVY_RATIO 0.1f
+#define HEAVY_MIN_PARTICLES (1u << 17) /* systems with fewer (padded) particles walk every group alone */
 #define GROUP_SIZE 64
 #define GROUP_STACK_CAP 4096
 #define GMAX 64
@@ -645,7 +647,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
     /* a costly group: every previous |a| known and the smallest below HEAVY_RATIO times
      * the largest; walked by a warp pair (64-record pops, two-part sums) */
     int pair = 0;
-    if (relative && amag_known) {
+    if (relative && amag_known && c->n_al >= HEAVY_MIN_PARTICLES) {
         float amax = 0.0f;
         for (uint32_t l = 0; l < G; ++l)
             if (valid[l]) amax = fmaxf(amax, c->amag_in[c->src[(uint32_t)w * G + l]]);

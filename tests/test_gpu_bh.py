@@ -227,6 +227,36 @@ def test_relative_criterion_bit_exact(gs, orc, box, kind, n, size, alpha, floor)
                 np.testing.assert_array_equal(g, c)
 
 
+@pytest.mark.parametrize("kind,n,size", [(17, 140000, 100.0), (16, 131072, 100.0)])
+def test_costly_groups_pair_walk_bit_exact(gs, orc, kind, n, size):
+    """Systems of at least 2^17 particles walk their costly groups (every previous |a|
+    known, the smallest below a tenth of the largest) on warp pairs: 64-record pops, item i
+    of the node and leaf lists summed by warp (i / 32) mod 2.  REFERENCE math over three
+    steps (the first estimates |a|, so pairs start at the second): state, interaction and
+    visit counts bit-identical to the oracle, which restates the pair order; the steps do
+    pair some groups."""
+    pos, vel, mass = gs.generate(kind, n, size=size, seed=61)
+    st = orc.State(pos, vel, mass)
+    flags = orc.ACCURATE | orc.RELATIVE_MAC
+    paired = 0
+    with _sim(gs, pos, vel, mass, box_mode=1, math_mode=gs.MATH_REFERENCE, accuracy_parameter=1.0,
+              relative_accuracy=0.006, relative_theta_floor=0.2, flags=REL | gs.FLAG_COUNT_INTERACTIONS) as sim:
+        for step in range(3):
+            _, _, _, A = sim.padded_state()
+            sim.reset_stats()
+            sim.run(1)
+            o = orc.bh_step(st, box_mode=1, theta=1.0, flags=flags, rel_alpha=0.006, rel_floor=0.2)
+            s = sim.stats()
+            assert (s.interactions, s.warp_visits) == (o["interactions"], o["warp_visits"]), step
+            for g, c in zip(sim.get_particles(), st.current()):
+                np.testing.assert_array_equal(g, c)
+            if step:
+                nv = o["valid_count"]
+                a = A[o["sorted_src"][: nv // 64 * 64]].reshape(-1, 64)
+                paired += int(np.sum(a.min(1) < np.float32(0.1) * a.max(1)))
+    assert paired > 0
+
+
 def test_relative_criterion_500k_error_gate(gs):
     """N=500,000 spiral, bounding box, alpha=0.006 with floor 0.2: the second step (the
     first with a previous |a|) has RMS relative force error <= 1e-3 against the FP64
