@@ -27,8 +27,9 @@ constexpr int kBBoxBits = 12;               // default per-axis bits in bounding
 constexpr int kBBoxMaxBits = 15;            // largest per-axis bits (30-bit keys, 4 radix passes)
 constexpr uint32_t kKeyRemovedSort = 1u << 20;  // sort key of removed particles (fixed box)
 // Relative criterion: costly groups are walked by warp pairs in systems of at least this
-// many (padded) particles; smaller systems walk every group on one warp.
-constexpr uint32_t kHeavyMinParticles = 1u << 17;
+// many (padded) particles -- more groups than the traversal keeps resident at once, where
+// the longest walks trail the launch; smaller systems walk every group on one warp.
+constexpr uint32_t kHeavyMinParticles = 1u << 18;
 constexpr uint32_t kKeyRemoved = 0xFFFFFFFFu;   // reported key of removed particles
 
 // pinned host words of a system (gs_sim::h_err): the device error word at 0, counter

@@ -468,7 +468,7 @@ static void walk_warp(void* p, uint64_t item, int worker) {
  * The CUDA kernel (force_kernels.cuh, force_group_body / force_pair_body) batches its
  * evaluations differently; with this accumulation rule the batching changes no bit. */
 #define HEAVY_RATIO 0.1f
-#define HEAVY_MIN_PARTICLES (1u << 17) /* systems with fewer (padded) particles walk every group alone */
+#define HEAVY_MIN_PARTICLES (1u << 18) /* systems with fewer (padded) particles walk every group alone */
 #define GROUP_SIZE 64
 #define GROUP_STACK_CAP 4096
 #define GMAX 64

@@ -246,12 +246,12 @@ def test_batched_uniform_disk_at_rest_error_gate(gs):
 
 
 def test_costly_groups_batch_bit_identical(gs):
-    """Members of at least 2^17 particles walk their costly groups on warp pairs, taken
+    """Members of at least 2^18 particles walk their costly groups on warp pairs, taken
     from one list over the whole batch before any other walk; each member still matches its
     twin stepped alone (smaller members walk every group on one warp, as alone)."""
     rel = dict(algorithm=1, box_mode=1, flags=0x170 | 0x8, accuracy_parameter=1.0, relative_accuracy=0.006,
                relative_theta_floor=0.2)
-    specs = [(17, 150000, 100.0, rel), (16, 140000, 100.0, dict(rel, relative_accuracy=0.01)),
+    specs = [(17, 270000, 100.0, rel), (16, 262144, 100.0, dict(rel, relative_accuracy=0.01)),
              (17, 20000, 100.0, rel), (16, 2000, 100.0, DIRECT)]
     alone = _make(gs, specs, 1700)
     batched = _make(gs, specs, 1700)

@@ -227,9 +227,9 @@ def test_relative_criterion_bit_exact(gs, orc, box, kind, n, size, alpha, floor)
                 np.testing.assert_array_equal(g, c)
 
 
-@pytest.mark.parametrize("kind,n,size", [(17, 140000, 100.0), (16, 131072, 100.0)])
+@pytest.mark.parametrize("kind,n,size", [(17, 270000, 100.0), (16, 262144, 100.0)])
 def test_costly_groups_pair_walk_bit_exact(gs, orc, kind, n, size):
-    """Systems of at least 2^17 particles walk their costly groups (every previous |a|
+    """Systems of at least 2^18 particles walk their costly groups (every previous |a|
     known, the smallest below a tenth of the largest) on warp pairs: 64-record pops, item i
     of the node and leaf lists summed by warp (i / 32) mod 2.  REFERENCE math over three
     steps (the first estimates |a|, so pairs start at the second): state, interaction and
