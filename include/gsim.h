@@ -107,7 +107,12 @@ typedef enum gs_math_mode { GS_MATH_FAST = 0, GS_MATH_REFERENCE = 1 } gs_math_mo
  * with the theta test (accuracy_parameter; the reference's theta = 1 is enough), then
  * opens nodes by the relative criterion with those estimates.  alpha = 0.006 with floor
  * 0.2 gives <= 8e-4 RMS force error at every step on the 500k spiral and on uniform disks
- * at rest, measured on 4096-17000-particle samples against the FP64 direct sum. */
+ * at rest, measured on 4096-17000-particle samples against the FP64 direct sum.
+ * In a system of at least 2^18 (padded) particles, a group whose previous |a| are all
+ * known and whose smallest is below a tenth of its largest is walked by two warps:
+ * 64-record pops, and item i of its node (leaf) list summed by warp (i / 32) mod 2 from
+ * zero, the two partial sums added -- the same interactions, in another summation order
+ * (alone and in a batch alike). */
 #define GS_FLAG_RELATIVE_MAC 0x100u
 
 typedef struct gs_params {
@@ -140,7 +145,8 @@ typedef struct gs_shape {
     uint32_t sort_keys_per_thread; /* radix-sort tile = 256 threads x this: 8 or 16 (default) */
     uint32_t sort_lookback;        /* earlier tiles a radix pass reads per look-back round trip: 8, 16, 32 */
     uint32_t scan_lookback;        /* the same for the node scan: 32, 64, 128 */
-    uint32_t force_warps;          /* group walks per block of the accurate traversal: 1, 2 (default), 4 */
+    uint32_t force_warps;          /* group walks per block of the accurate traversal: 1, 2 (default), 4;
+                                      1 runs as 2 where costly groups are walked by warp pairs */
     uint32_t force_short_lists;    /* 0: evaluate after 160 nodes / 96 leaf runs; 1: after 96 / 64 */
     uint32_t direct_targets;       /* direct-sum particles per thread (FAST math): 2 (default) or 4 */
     uint32_t direct_blocks_per_sm; /* direct-sum j-split target, blocks per SM: 1..32 (default 12) */
