@@ -10,7 +10,8 @@ pytestmark = pytest.mark.gpu
 
 def _pinned(torch, a, offset=0):
     """A float32 copy of `a` in pinned host memory, starting `offset` floats into the
-    allocation (offset 1 gives an address that is 4- but not 8-byte aligned)."""
+    allocation (offset 1 gives an address that is 4- but not 8-byte aligned, offset 2 one
+    that is 8- but not 16-byte aligned)."""
     flat = np.ascontiguousarray(a, np.float32).ravel()
     buf = torch.empty(flat.size + offset, dtype=torch.float32).pin_memory().numpy()
     out = buf[offset:offset + flat.size]
@@ -33,7 +34,7 @@ def _get_into(gs, sim, pos, vel, mass):
     gs._check(gs.lib().gs_get_particles(sim.handle, gs._fp(pos), gs._fp(vel), gs._fp(mass)))
 
 
-@pytest.mark.parametrize("offset", [0, 1])
+@pytest.mark.parametrize("offset", [0, 1, 2])
 def test_pinned_upload_matches_pageable(gs, offset):
     torch = pytest.importorskip("torch")
     n = 5000  # not a multiple of 64: the padding slots are written too
@@ -60,7 +61,7 @@ def test_pinned_upload_matches_pageable(gs, offset):
     b.close()
 
 
-@pytest.mark.parametrize("offset", [0, 1])
+@pytest.mark.parametrize("offset", [0, 1, 2])
 def test_pinned_readback_matches_pageable(gs, offset):
     torch = pytest.importorskip("torch")
     n = 3001
