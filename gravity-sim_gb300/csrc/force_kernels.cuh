@@ -556,8 +556,9 @@ __device__ __forceinline__ void force_group_body(
 // Costly groups: a warp pair per walk.  With the relative criterion a group whose smallest
 // previous |a| is far below its largest (every |a| known and a_min < kHeavyRatio a_max)
 // opens many more records than the others: on the 500k spiral such groups sum 2.4x the
-// mean interactions and their single-warp walks trailed the traversal launch.  Their
-// walks run first, each on two warps of one block: pops take the top min(64, size)
+// mean interactions and their single-warp walks trailed the traversal launch.  In systems
+// of at least kHeavyMinParticles particles (more groups than the launch keeps resident)
+// their walks run first, each on two warps of one block: pops take the top min(64, size)
 // records (warp w tests entries [32w, 32w + 32) of the popped range), the block's pair
 // scans the counts of both warps, and item i of the node list (record i of the flattened
 // leaf runs) is summed by warp (i / 32) mod 2, each warp from zero in walk order; the node
