@@ -715,6 +715,7 @@ __device__ __forceinline__ void mom_scan_body(uint32_t tile, uint32_t n_items, u
     b.xy += incl.xy - c.xy;
     b.yy += incl.yy - c.yy;
     ulonglong2* out = reinterpret_cast<ulonglong2*>(mi.prefix);
+#pragma unroll
     for (int ch = 0; ch < 6; ++ch) {
         i128 run = mom_get(b, ch);
 #pragma unroll
@@ -747,7 +748,7 @@ k_mom_tiles(const uint32_t* __restrict__ valid_count, MomIn mi) {
     pdl_enter();
     mom_tiles_body(blockIdx.x, *valid_count, mi);
 }
-__global__ void __launch_bounds__(kMomThreads, 3)
+__global__ void __launch_bounds__(kMomThreads, 2)
 k_mom_scan(uint32_t n_items, const uint32_t* __restrict__ valid_count, MomIn mi) {
     pdl_enter();
     mom_scan_body(blockIdx.x, n_items, *valid_count, mi);
