@@ -257,6 +257,29 @@ def test_costly_groups_pair_walk_bit_exact(gs, orc, kind, n, size):
     assert paired > 0
 
 
+@pytest.mark.parametrize("box", [0, 1])
+def test_costly_groups_pair_walk_every_force_shape(gs, orc, box):
+    """The warp-pair walk in every traversal shape (one warp per block runs as two, four
+    warps hold two pairs with their own barriers, short lists): REFERENCE math, two steps
+    of a 270,000-particle spiral in either box, bit-identical to the oracle."""
+    n = 270000
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, n, size=100.0, seed=63)
+    st = orc.State(pos, vel, mass)
+    want = []
+    for _ in range(2):
+        orc.bh_step(st, box_mode=box, theta=1.0, flags=orc.ACCURATE | orc.RELATIVE_MAC, rel_alpha=0.006,
+                    rel_floor=0.2, keep_tree=False)
+        want.append([a.copy() for a in st.current()])
+    for warps, short in ((1, 0), (2, 0), (2, 1), (4, 0)):
+        with _sim(gs, pos, vel, mass, box_mode=box, math_mode=gs.MATH_REFERENCE, accuracy_parameter=1.0,
+                  relative_accuracy=0.006, relative_theta_floor=0.2, flags=REL) as sim:
+            sim.set_shape(force_warps=warps, force_short_lists=short)
+            for k in range(2):
+                sim.run(1)
+                for g, c in zip(sim.get_particles(), want[k]):
+                    np.testing.assert_array_equal(g, c, err_msg=f"shape {warps}/{short} step {k}")
+
+
 def test_relative_criterion_500k_error_gate(gs):
     """N=500,000 spiral, bounding box, alpha=0.006 with floor 0.2: the second step (the
     first with a previous |a|) has RMS relative force error <= 1e-3 against the FP64
