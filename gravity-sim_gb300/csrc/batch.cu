@@ -107,11 +107,16 @@ gs_status BatchEngine::set_members(const std::vector<gs_sim*>& members) {
     const size_t n = order.size();
     BatchPlan p;
     p.shape = shape;
-    // the counting kernels exist for the default shape only (2 group walks per block)
-    bool counting = false;
-    for (const gs_sim* s : order)
-        if (s->p.algorithm == GS_BARNES_HUT && (s->p.flags & GS_FLAG_COUNT_INTERACTIONS)) counting = true;
-    const uint32_t force_warps = counting ? 2u : shape.force_warps;
+    // the counting kernels exist for the default shape only (2 group walks per block), and
+    // warp pairs for costly groups need an even number of warps per block (one runs as two)
+    bool counting = false, pairs = false;
+    for (const gs_sim* s : order) {
+        if (s->p.algorithm != GS_BARNES_HUT) continue;
+        if (s->p.flags & GS_FLAG_COUNT_INTERACTIONS) counting = true;
+        if (s->bh.heavy_flag && s->bh.quad && (s->p.flags & GS_FLAG_GROUP_WALK) && s->n_al >= kHeavyMinParticles)
+            pairs = true;
+    }
+    const uint32_t force_warps = counting ? 2u : (pairs && shape.force_warps == 1) ? 2u : shape.force_warps;
     std::vector<SysDesc> descs(n);
     std::vector<uint32_t> blocks(n * kTabCount, 0u);
     parity0.assign(n, 0);

@@ -262,3 +262,8 @@ def test_costly_groups_batch_bit_identical(gs):
         b.run(3)
         b.sync()
         _assert_same(alone, batched, specs)
+        b.set_shape(force_warps=1)  # runs as two warps per block: pairs need both
+        b.run(2)
+        b.sync()
+        _run_alone(alone, 2)
+        _assert_same(alone, batched, specs)
