@@ -469,6 +469,10 @@ static void walk_warp(void* p, uint64_t item, int worker) {
  * evaluations differently; with this accumulation rule the batching changes no bit. */
 #define HEAVY_RATIO 0.1f
 #define HEAVY_MIN_PARTICLES (1u << 18) /* systems with fewer (padded) particles walk every group alone */
+/* 0: every group walks alone whatever its size (a check that pairing changes only the
+ * order of the sums; not a mode of the library) */
+static int g_heavy_pairs = 1;
+void orc_set_heavy_pairs(int on) { g_heavy_pairs = on; }
 #define GROUP_SIZE 64
 #define GROUP_STACK_CAP 4096
 #define GMAX 64
@@ -647,7 +651,7 @@ static void group_walk_warp(void* p, uint64_t item, int worker) {
     /* a costly group: every previous |a| known and the smallest below HEAVY_RATIO times
      * the largest; walked by a warp pair (64-record pops, two-part sums) */
     int pair = 0;
-    if (relative && amag_known && c->n_al >= HEAVY_MIN_PARTICLES) {
+    if (g_heavy_pairs && relative && amag_known && c->n_al >= HEAVY_MIN_PARTICLES) {
         float amax = 0.0f;
         for (uint32_t l = 0; l < G; ++l)
             if (valid[l]) amax = fmaxf(amax, c->amag_in[c->src[(uint32_t)w * G + l]]);

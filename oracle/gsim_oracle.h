@@ -136,6 +136,10 @@ int orc_bh_sorted_step_ex(int box_mode, int flags, uint32_t n_al, float* pos_in,
 int orc_generate(int type, uint64_t count, float size, float mn, float mx, float G, uint64_t seed, float* pos,
                  float* vel, float* mass);
 
+/* 0: costly groups walk alone as well (a test switch: pairing changes only the order of
+ * the sums); 1 (default): they walk as warp pairs, as the library does. */
+void orc_set_heavy_pairs(int on);
+
 /* Upper bound on preorder records for n_al particles in either mode. */
 uint64_t orc_bh_node_capacity(int box_mode, uint32_t n_al);
 

@@ -60,6 +60,8 @@ def lib():
         L.orc_bh_sorted_step_ex.argtypes = [C.c_int, C.c_int, C.c_uint32, _FP, _FP, _FP, _FP, _FP, _FP, C.c_float,
                                             C.c_float, C.c_float, C.c_float, C.POINTER(BHOut), C.c_int]
         L.orc_bh_sorted_step_ex.restype = C.c_int
+        L.orc_set_heavy_pairs.argtypes = [C.c_int]
+        L.orc_set_heavy_pairs.restype = None
         L.orc_bh_node_capacity.argtypes = [C.c_int, C.c_uint32]
         L.orc_bh_node_capacity.restype = C.c_uint64
         L.orc_energy_f64.argtypes = [C.c_uint32, _FP, _FP, _FP, C.c_double, C.c_double]
@@ -153,6 +155,12 @@ def direct_accel_f64(pos, mass, softening=0.2, targets=None, threads=os.cpu_coun
     lib().orc_direct_accel_f64(len(mass), _fp(pos), _fp(mass), eps2, len(t), t.ctypes.data_as(_UP),
                                out.ctypes.data_as(_DP), threads)
     return out
+
+
+def set_heavy_pairs(on):
+    """Whether costly groups of large systems walk as warp pairs (the default, as the
+    library does) or alone: a test switch, pairing changes only the order of the sums."""
+    lib().orc_set_heavy_pairs(1 if on else 0)
 
 
 def bh_step(state, method="sorted", box_mode=BOX_FIXED_500, dt=1e-3, speed=1.0, G=1.0, softening=0.2, theta=1.0,

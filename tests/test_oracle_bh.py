@@ -266,3 +266,32 @@ def test_key_bits_out_of_range(orc):
     for bits in (16, 40):
         with pytest.raises(ValueError):
             orc.bh_step(orc.State(pos, pos, np.ones(64, np.float32)), box_mode=orc.BOX_BOUNDING, key_bits=bits)
+
+
+def test_pair_walk_changes_only_the_order_of_sums(gs, orc):
+    """In a system of 2^18 particles the costly groups (every previous |a| known, the
+    smallest below a tenth of the largest) walk as warp pairs: 64-record pops and two-part
+    sums.  Against the same steps with every group walked alone: the same interactions and
+    visits at each step, and the same state up to the rounding of the reordered sums."""
+    n = 1 << 18
+    pos, vel, mass = gs.generate(gs.GEN_SPIRAL, n, size=100.0, seed=67)
+    kw = dict(box_mode=orc.BOX_BOUNDING, theta=1.0, flags=orc.ACCURATE | orc.RELATIVE_MAC, rel_alpha=0.006,
+              rel_floor=0.2, keep_tree=False)
+    runs = []
+    try:
+        for pairs in (True, False):
+            orc.set_heavy_pairs(pairs)
+            st = orc.State(pos, vel, mass)
+            stats = []
+            for _ in range(2):  # the first step estimates |a|: pairs start at the second
+                r = orc.bh_step(st, **kw)
+                stats.append((r["interactions"], r["warp_visits"]))
+            runs.append((stats, [a.copy() for a in st.current()]))
+    finally:
+        orc.set_heavy_pairs(True)
+    (sp, (pp, vp, mp)), (sa, (pa, va, ma)) = runs
+    assert sp == sa
+    assert np.array_equal(mp, ma)
+    assert not np.array_equal(vp, va)  # some groups were paired
+    np.testing.assert_allclose(vp, va, rtol=0, atol=1e-5 * np.abs(va).max())
+    np.testing.assert_allclose(pp, pa, rtol=0, atol=1e-6 * np.abs(pa).max())
